@@ -1,0 +1,793 @@
+// Host side of the asdpocs_gb300 C ABI: launcher drop-ins, mex-level entry
+// points, TV entry points and the device-resident ASD-POCS plans.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+#include <new>
+#include <vector>
+
+#include "kernels.h"
+
+namespace asd {
+
+// ------------------------------------------------------------------ errors
+static thread_local int g_status = 0;
+static thread_local char g_msg[512] = "";
+
+int set_error(int status, const char *fmt, ...) {
+  g_status = status;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_msg, sizeof g_msg, fmt, ap);
+  va_end(ap);
+  return status;
+}
+void clear_error() {
+  g_status = 0;
+  g_msg[0] = 0;
+}
+int cuda_status(cudaError_t e, const char *what) {
+  const int st = (e == cudaErrorMemoryAllocation) ? ASDPOCS_ERR_NOMEM
+                 : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+                     ? ASDPOCS_ERR_NODEV
+                     : ASDPOCS_ERR_CUDA;
+  return set_error(st, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// ------------------------------------------------ gateway geometry helpers
+// Ax_main_test.cpp:138-161 / Atx_main_test.cpp:149-172: every para field is
+// read as float; cos/sin of the float angle; lengths divided by the voxel
+// size in float; detector coordinates (i - n/2 + 0.5)*det evaluated in
+// double and rounded to float; dz = 1.
+struct GatewayGeo {
+  float cos_phi, sin_phi, SO, OD, scale, det;
+  std::vector<float> y_det, z_det;
+};
+
+static void gateway_geometry(double phi, double SO, double OD, double vxl,
+                             double detsize, int na, int nb, GatewayGeo &g) {
+  const float phif = (float)phi;
+  g.scale = (float)vxl;
+  g.cos_phi = cosf(phif);
+  g.sin_phi = sinf(phif);
+  g.SO = (float)SO / g.scale;
+  g.OD = (float)OD / g.scale;
+  g.det = (float)detsize / g.scale;
+  g.y_det.resize(na);
+  g.z_det.resize(nb);
+  for (int i = 0; i < na; i++)
+    g.y_det[i] = (float)(((double)(float)i - (double)(float)na / 2.0 + 0.5) *
+                         (double)g.det);
+  for (int i = 0; i < nb; i++)
+    g.z_det[i] = (float)(((double)(float)i - (double)(float)nb / 2.0 + 0.5) *
+                         (double)g.det);
+}
+
+// angle of view ii as the driver passes it: para.phi = -phi_vec(ii)/180*pi
+// (ASD_POCS_cuda.m:111,116), then read as float by the gateway.
+static float2 view_trig(double phi_deg) {
+  const double theta = phi_deg / 180.0 * 3.14159265358979323846;
+  const float phif = (float)(-1 * theta);
+  return make_float2(cosf(phif), sinf(phif));
+}
+
+// ------------------------------------- workspace of the host-pointer calls
+// Grow-only device buffers reused by the synchronous drop-ins, so a call
+// does not pay cudaMalloc/cudaFree (the reference allocates five buffers per
+// call, Ax_cone_gpu.cu:787-804).  One workspace per device, serialised.
+struct Workspace {
+  std::mutex mu;
+  void *buf = nullptr;
+  size_t cap = 0;
+  cudaStream_t st = nullptr;
+};
+static Workspace g_ws[64];
+
+static int ws_acquire(Workspace *&w, size_t bytes) {
+  int dev = 0;
+  ASD_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(ASDPOCS_ERR_NODEV, "device id");
+  w = &g_ws[dev];
+  if (!w->st) ASD_CUDA(cudaStreamCreateWithFlags(&w->st, cudaStreamNonBlocking));
+  if (bytes > w->cap) {
+    if (w->buf) cudaFree(w->buf);
+    w->buf = nullptr;
+    w->cap = 0;
+    ASD_CUDA(cudaMalloc(&w->buf, bytes));
+    w->cap = bytes;
+  }
+  return 0;
+}
+
+static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+static int check_dims(int nx, int ny, int nz, int na, int nb) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || na <= 0 || nb <= 0)
+    return set_error(ASDPOCS_ERR_ARG,
+                     "dimensions must be positive (nx=%d ny=%d nz=%d na=%d nb=%d)",
+                     nx, ny, nz, na, nb);
+  if ((long long)nx * ny * nz > (1LL << 34) || (long long)na * nb > (1LL << 31))
+    return set_error(ASDPOCS_ERR_ARG, "dimensions too large");
+  return 0;
+}
+
+}  // namespace asd
+
+using namespace asd;
+
+// ======================================================================
+extern "C" {
+
+const char *asdpocs_last_error(void) { return g_msg; }
+int asdpocs_last_status(void) { return g_status; }
+const char *asdpocs_version(void) { return "asdpocs_gb300 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------ projectors
+int asdpocs_ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
+                      float sin_phi, const float *y_det_d,
+                      const float *z_det_d, float SO, float OD, float scale,
+                      float dz, int nx, int ny, int nz, int na, int nb,
+                      void *stream) {
+  clear_error();
+  if (int e = check_dims(nx, ny, nz, na, nb)) return e;
+  if (!x_d || !y_d || !sr_d || !y_det_d || !z_det_d)
+    return set_error(ASDPOCS_ERR_ARG, "null pointer");
+  ViewGeo g{cos_phi, sin_phi, SO, OD, scale, 0.f, 0.f, dz, y_det_d, z_det_d};
+  Dims d{nx, ny, nz, na, nb};
+  ASD_CUDA(launch_ax(x_d, y_d, sr_d, g, d, (cudaStream_t)stream));
+  return 0;
+}
+
+int asdpocs_atx_device(float *x_d, const float *y_d, float *sc_d,
+                       float cos_phi, float sin_phi, const float *y_det_d,
+                       const float *z_det_d, float SO, float OD, float scale,
+                       float dy_det, float dz_det, float dz, int nx, int ny,
+                       int nz, int na, int nb, void *stream) {
+  clear_error();
+  if (int e = check_dims(nx, ny, nz, na, nb)) return e;
+  if (!x_d || !y_d || !sc_d || !y_det_d || !z_det_d)
+    return set_error(ASDPOCS_ERR_ARG, "null pointer");
+  ViewGeo g{cos_phi, sin_phi, SO, OD, scale, dy_det, dz_det, dz, y_det_d,
+            z_det_d};
+  Dims d{nx, ny, nz, na, nb};
+  ASD_CUDA(launch_atx(x_d, y_d, sc_d, g, d, (cudaStream_t)stream));
+  return 0;
+}
+
+static int ax_host(const float *X, float *y, float *sr, float cos_phi,
+                   float sin_phi, const float *y_det, const float *z_det,
+                   float SO, float OD, float scale, float dz, int nx, int ny,
+                   int nz, int na, int nb) {
+  clear_error();
+  if (int e = check_dims(nx, ny, nz, na, nb)) return e;
+  if (!X || !y || !sr || !y_det || !z_det)
+    return set_error(ASDPOCS_ERR_ARG, "null pointer");
+  const size_t N = (size_t)nx * ny * nz, M = (size_t)na * nb;
+  const size_t oX = 0, oY = align256(N * 4), oS = oY + align256(M * 4),
+               oA = oS + align256(M * 4), oB = oA + align256((size_t)na * 4),
+               tot = oB + align256((size_t)nb * 4);
+  Workspace *w;
+  if (int e = ws_acquire(w, tot)) return e;
+  std::lock_guard<std::mutex> lk(w->mu);
+  char *b = (char *)w->buf;
+  ASD_CUDA(cudaMemcpyAsync(b + oX, X, N * 4, cudaMemcpyHostToDevice, w->st));
+  ASD_CUDA(cudaMemcpyAsync(b + oA, y_det, (size_t)na * 4, cudaMemcpyHostToDevice, w->st));
+  ASD_CUDA(cudaMemcpyAsync(b + oB, z_det, (size_t)nb * 4, cudaMemcpyHostToDevice, w->st));
+  ViewGeo g{cos_phi, sin_phi, SO, OD, scale, 0.f, 0.f, dz, (const float *)(b + oA),
+            (const float *)(b + oB)};
+  Dims d{nx, ny, nz, na, nb};
+  ASD_CUDA(launch_ax((const float *)(b + oX), (float *)(b + oY), (float *)(b + oS), g, d, w->st));
+  ASD_CUDA(cudaMemcpyAsync(y, b + oY, M * 4, cudaMemcpyDeviceToHost, w->st));
+  ASD_CUDA(cudaMemcpyAsync(sr, b + oS, M * 4, cudaMemcpyDeviceToHost, w->st));
+  ASD_CUDA(cudaStreamSynchronize(w->st));
+  return 0;
+}
+
+static int atx_host(float *X, const float *yv, float *sc, float cos_phi,
+                    float sin_phi, const float *y_det, const float *z_det,
+                    float SO, float OD, float scale, float dy_det, float dz_det,
+                    float dz, int nx, int ny, int nz, int na, int nb) {
+  clear_error();
+  if (int e = check_dims(nx, ny, nz, na, nb)) return e;
+  if (!X || !yv || !sc || !y_det || !z_det)
+    return set_error(ASDPOCS_ERR_ARG, "null pointer");
+  const size_t N = (size_t)nx * ny * nz, M = (size_t)na * nb;
+  const size_t oX = 0, oS = align256(N * 4), oY = oS + align256(N * 4),
+               oA = oY + align256(M * 4), oB = oA + align256((size_t)na * 4),
+               tot = oB + align256((size_t)nb * 4);
+  Workspace *w;
+  if (int e = ws_acquire(w, tot)) return e;
+  std::lock_guard<std::mutex> lk(w->mu);
+  char *b = (char *)w->buf;
+  ASD_CUDA(cudaMemcpyAsync(b + oY, yv, M * 4, cudaMemcpyHostToDevice, w->st));
+  ASD_CUDA(cudaMemcpyAsync(b + oA, y_det, (size_t)na * 4, cudaMemcpyHostToDevice, w->st));
+  ASD_CUDA(cudaMemcpyAsync(b + oB, z_det, (size_t)nb * 4, cudaMemcpyHostToDevice, w->st));
+  ViewGeo g{cos_phi, sin_phi, SO, OD, scale, dy_det, dz_det, dz,
+            (const float *)(b + oA), (const float *)(b + oB)};
+  Dims d{nx, ny, nz, na, nb};
+  ASD_CUDA(launch_atx((float *)(b + oX), (const float *)(b + oY), (float *)(b + oS), g, d, w->st));
+  ASD_CUDA(cudaMemcpyAsync(X, b + oX, N * 4, cudaMemcpyDeviceToHost, w->st));
+  ASD_CUDA(cudaMemcpyAsync(sc, b + oS, N * 4, cudaMemcpyDeviceToHost, w->st));
+  ASD_CUDA(cudaStreamSynchronize(w->st));
+  return 0;
+}
+
+void Ax_cone_mf_gpu_new(float *X, float *y, float *sr, float cos_phi,
+                        float sin_phi, float *y_det, float *z_det, float SO,
+                        float OD, float scale, float dz, int nx, int ny, int nz,
+                        int na, int nb) {
+  ax_host(X, y, sr, cos_phi, sin_phi, y_det, z_det, SO, OD, scale, dz, nx, ny,
+          nz, na, nb);
+}
+
+void Atx_cone_mf_gpu_new(float *X, float *y, float *sc, float cos_phi,
+                         float sin_phi, float *y_det, float *z_det, float SO,
+                         float OD, float scale, float dy_det, float dz_det,
+                         float dz, int nx, int ny, int nz, int na, int nb) {
+  atx_host(X, y, sc, cos_phi, sin_phi, y_det, z_det, SO, OD, scale, dy_det,
+           dz_det, dz, nx, ny, nz, na, nb);
+}
+
+// ------------------------------------------------------ mex-level calls
+static int check_para(const asdpocs_para *p) {
+  if (!p) return set_error(ASDPOCS_ERR_ARG, "Error usage! (para is NULL)");
+  return check_dims(p->nx, p->ny, p->nz, p->na, p->nb);
+}
+
+int Ax_cone_gpu(const float *X, long long numel_X, const asdpocs_para *para,
+                float *y, float *sr) {
+  clear_error();
+  if (int e = check_para(para)) return e;
+  if (numel_X != (long long)para->nx * para->ny * para->nz)
+    return set_error(ASDPOCS_ERR_ARG, "Error size of input argument X!");
+  GatewayGeo g;
+  gateway_geometry(para->phi, para->SO, para->OD, para->vxlsize, para->detsize,
+                   para->na, para->nb, g);
+  return ax_host(X, y, sr, g.cos_phi, g.sin_phi, g.y_det.data(), g.z_det.data(),
+                 g.SO, g.OD, g.scale, 1.0f, para->nx, para->ny, para->nz,
+                 para->na, para->nb);
+}
+
+int Atx_cone_gpu(const float *Y, long long numel_Y, const asdpocs_para *para,
+                 float *x, float *sc) {
+  clear_error();
+  if (int e = check_para(para)) return e;
+  if (numel_Y != (long long)para->na * para->nb)
+    return set_error(ASDPOCS_ERR_ARG, "Error size of input argument Y!");
+  GatewayGeo g;
+  gateway_geometry(para->phi, para->SO, para->OD, para->vxlsize, para->detsize,
+                   para->na, para->nb, g);
+  return atx_host(x, Y, sc, g.cos_phi, g.sin_phi, g.y_det.data(),
+                  g.z_det.data(), g.SO, g.OD, g.scale, g.det, g.det, 1.0f,
+                  para->nx, para->ny, para->nz, para->na, para->nb);
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------------- TV
+template <class T>
+static int tv_host(const T *img, T *out, int nx, int ny, int nz, double alpha,
+                   int n, int pos, const T *old) {
+  clear_error();
+  if (!img || !out) return set_error(ASDPOCS_ERR_ARG, "null pointer");
+  if (nx <= 0 || ny <= 0 || nz <= 0)
+    return set_error(ASDPOCS_ERR_ARG, "bad image dimensions");
+  const size_t N = (size_t)nx * ny * nz;
+  const size_t tiles = (size_t)((nx + 31) / 32) * ((ny + 7) / 8) * nz;
+  const size_t oI = 0, oO = align256(N * sizeof(T)), oA = oO + align256(N * sizeof(T)),
+               oB = oA + align256(N * sizeof(T)), oS = oB + align256(N * sizeof(T)),
+               oP = oS + 256, oC = oP + align256(tiles * sizeof(double) * 3),
+               tot = oC + 256;
+  Workspace *w;
+  if (int e = ws_acquire(w, tot)) return e;
+  std::lock_guard<std::mutex> lk(w->mu);
+  char *b = (char *)w->buf;
+  ASD_CUDA(cudaMemsetAsync(b + oC, 0, 256, w->st));
+  ASD_CUDA(cudaMemcpyAsync(b + oI, img, N * sizeof(T), cudaMemcpyHostToDevice, w->st));
+  if (old)
+    ASD_CUDA(cudaMemcpyAsync(b + oO, old, N * sizeof(T), cudaMemcpyHostToDevice, w->st));
+  cudaError_t e;
+  if (sizeof(T) == 8)
+    e = tv_minimize_f64((double *)(b + oI), old ? (const double *)(b + oO) : nullptr,
+                        (double *)(b + oA), (double *)(b + oB), (double *)(b + oS),
+                        (double *)(b + oP), (unsigned *)(b + oC), nx, ny, nz, alpha,
+                        n, pos, w->st);
+  else
+    e = tv_minimize_f32((float *)(b + oI), old ? (const float *)(b + oO) : nullptr,
+                        (float *)(b + oA), (float *)(b + oB), (double *)(b + oS),
+                        (double *)(b + oP), (unsigned *)(b + oC), nx, ny, nz, alpha,
+                        n, pos, w->st);
+  ASD_CUDA(e);
+  ASD_CUDA(cudaMemcpyAsync(out, b + oI, N * sizeof(T), cudaMemcpyDeviceToHost, w->st));
+  ASD_CUDA(cudaStreamSynchronize(w->st));
+  return 0;
+}
+
+extern "C" {
+
+int imgTVGradMin(const double *img, double *img_out, int rowN, int colN,
+                 double alpha, int nTVIter, int pos, const double *img_old) {
+  return tv_host<double>(img, img_out, rowN, colN, 1, alpha, nTVIter, pos,
+                         img_old);
+}
+
+int imgTVGradMin3D(const double *img, double *img_out, int Nx, int Ny, int Nz,
+                   double alpha, int nTVIter, int pos, const double *img_old) {
+  if (Nz < 1) return set_error(ASDPOCS_ERR_ARG, "bad image dimensions");
+  if (Nz < 2) {
+    // MATLAB drops a trailing singleton dimension, so the reference never
+    // sees Nz == 1 in a valid call (it would read past the dimension array,
+    // imgTVGradMin3D.cpp:44-46).  Such calls are rejected.
+    return set_error(ASDPOCS_ERR_ARG,
+                     "imgTVGradMin3D expects a 3-D image (Nz >= 2)");
+  }
+  return tv_host<double>(img, img_out, Nx, Ny, Nz, alpha, nTVIter, pos,
+                         img_old);
+}
+
+int asdpocs_tv_device(float *img_d, const float *img_old_d, int nx, int ny,
+                      int nz, double alpha, int nTVIter, int pos,
+                      void *stream) {
+  clear_error();
+  if (!img_d) return set_error(ASDPOCS_ERR_ARG, "null pointer");
+  if (nx <= 0 || ny <= 0 || nz <= 0)
+    return set_error(ASDPOCS_ERR_ARG, "bad image dimensions");
+  const size_t N = (size_t)nx * ny * nz;
+  const size_t tiles = (size_t)((nx + 31) / 32) * ((ny + 7) / 8) * nz;
+  const size_t oA = 0, oB = align256(N * 4), oS = oB + align256(N * 4),
+               oP = oS + 256, oC = oP + align256(tiles * sizeof(double) * 3),
+               tot = oC + 256;
+  Workspace *w;
+  if (int e = ws_acquire(w, tot)) return e;
+  std::lock_guard<std::mutex> lk(w->mu);
+  char *b = (char *)w->buf;
+  cudaStream_t st = (cudaStream_t)stream;
+  ASD_CUDA(cudaMemsetAsync(b + oC, 0, 256, st));
+  ASD_CUDA(tv_minimize_f32(img_d, img_old_d, (float *)(b + oA), (float *)(b + oB),
+                           (double *)(b + oS), (double *)(b + oP),
+                           (unsigned *)(b + oC), nx, ny, nz, alpha, nTVIter, pos,
+                           st));
+  // the workspace is reused by the next call: finish before releasing it
+  ASD_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}
+
+void asdpocs_options_default(asdpocs_options *o) {
+  if (!o) return;
+  o->maxnumIter = 5;
+  o->numOfgradients = 20;
+  o->alpha = 0.02;
+  o->alpha_red = 0.95;
+  o->beta = 1.0;
+  o->beta_red = 0.995;
+  o->r_max = 0.95;
+  o->epsilon = 2.220446049250313e-16;
+  o->stopRelChg = 2.220446049250313e-16;
+}
+
+}  // extern "C"
+
+// ======================================================================
+// Plans: batched, device-resident ASD-POCS
+// ======================================================================
+struct asdpocs_plan_s {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  bool own_stream = false;
+  int batch = 0;
+  Dims d{};
+  int nv = 0, max_iter = 0, max_ng = 0;
+  std::vector<asdpocs_geometry> geom;
+  std::vector<asdpocs_options> opt;
+  std::vector<Inst> h_inst;
+  std::vector<int> has_ref;
+  Inst *d_inst = nullptr;
+  void *arena = nullptr;
+  size_t bytes = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace asd {
+
+static int plan_enqueue_iteration(asdpocs_plan p) {
+  for (int v = 0; v < p->nv; v++) {
+    ASD_CUDA(launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st));
+    ASD_CUDA(launch_sart_atx(p->d_inst, p->batch, p->d, v, p->st));
+  }
+  ASD_CUDA(launch_after_sweep(p->d_inst, p->batch, p->d, p->st));
+  for (int s = 0; s < p->max_ng; s++)
+    ASD_CUDA(launch_tv_step(p->d_inst, p->batch, p->d, s, p->max_ng, p->st));
+  ASD_CUDA(launch_finish_iter(p->d_inst, p->batch, p->d, p->max_ng, p->st));
+  return 0;
+}
+
+}  // namespace asd
+
+extern "C" {
+
+int asdpocs_plan_create(asdpocs_plan *out, int batch,
+                        const asdpocs_geometry *geom,
+                        const double *phi_vec_deg, const asdpocs_options *opt,
+                        unsigned long long hbm_budget_bytes, void *stream) {
+  clear_error();
+  if (!out || !geom || !phi_vec_deg || batch <= 0)
+    return set_error(ASDPOCS_ERR_ARG, "bad plan arguments");
+  *out = nullptr;
+  const asdpocs_geometry &g0 = geom[0];
+  if (int e = check_dims(g0.nx, g0.ny, g0.nz, g0.na, g0.nb)) return e;
+  if (g0.nv <= 0) return set_error(ASDPOCS_ERR_ARG, "nv must be positive");
+  for (int i = 1; i < batch; i++) {
+    const asdpocs_geometry &gi = geom[i];
+    if (gi.nx != g0.nx || gi.ny != g0.ny || gi.nz != g0.nz || gi.na != g0.na ||
+        gi.nb != g0.nb || gi.nv != g0.nv)
+      return set_error(ASDPOCS_ERR_ARG,
+                       "instances of one plan must share nx,ny,nz,na,nb,nv");
+  }
+  asdpocs_plan p = new (std::nothrow) asdpocs_plan_s;
+  if (!p) return set_error(ASDPOCS_ERR_NOMEM, "host allocation");
+  p->batch = batch;
+  p->d = Dims{g0.nx, g0.ny, g0.nz, g0.na, g0.nb};
+  p->nv = g0.nv;
+  p->geom.assign(geom, geom + batch);
+  p->opt.resize(batch);
+  for (int i = 0; i < batch; i++) {
+    if (opt)
+      p->opt[i] = opt[i];
+    else
+      asdpocs_options_default(&p->opt[i]);
+    if (p->opt[i].maxnumIter < 0 || p->opt[i].numOfgradients < 0) {
+      delete p;
+      return set_error(ASDPOCS_ERR_ARG, "negative iteration counts");
+    }
+    if (p->opt[i].maxnumIter > p->max_iter) p->max_iter = p->opt[i].maxnumIter;
+    if (p->opt[i].numOfgradients > p->max_ng)
+      p->max_ng = p->opt[i].numOfgradients;
+  }
+  p->has_ref.assign(batch, 0);
+  cudaGetDevice(&p->device);
+  if (stream) {
+    p->st = (cudaStream_t)stream;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&p->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete p;
+      return cuda_status(e, "cudaStreamCreate");
+    }
+    p->own_stream = true;
+  }
+  // ---- arena layout (per instance) ----
+  const size_t N = (size_t)g0.nx * g0.ny * g0.nz;
+  const size_t M = (size_t)g0.na * g0.nb;
+  const size_t nblk = (size_t)reduce_blocks_for(p->d);
+  const size_t per_img = align256(N * 4);
+  size_t off = 0;
+  struct Off {
+    size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, ydet, zdet, trig, rmse,
+        part, cnt, scal;
+  };
+  std::vector<Off> offs(batch);
+  for (int i = 0; i < batch; i++) {
+    Off &o = offs[i];
+    o.P = off; off += align256(M * p->nv * 4);
+    o.m = off; off += per_img;
+    o.m_pre = off; off += per_img;
+    o.m_res = off; off += per_img;
+    o.m_k1 = off; off += per_img;
+    o.I0 = off; off += per_img;
+    o.tvb = off; off += per_img;
+    o.tvc = off; off += per_img;
+    o.cor = off; off += align256(M * 4);
+    o.ydet = off; off += align256((size_t)g0.na * 4);
+    o.zdet = off; off += align256((size_t)g0.nb * 4);
+    o.trig = off; off += align256((size_t)p->nv * 8);
+    o.rmse = off; off += align256((size_t)(p->max_iter + 1) * 8);
+    o.part = off; off += align256(nblk * kMaxReduceK * 8);
+    o.cnt = off; off += 256;
+    o.scal = off; off += align256(sizeof(Scalars));
+  }
+  const size_t inst_off = off;
+  off += align256(sizeof(Inst) * batch);
+  p->bytes = off;
+  if (hbm_budget_bytes && off > hbm_budget_bytes) {
+    if (p->own_stream) cudaStreamDestroy(p->st);
+    delete p;
+    return set_error(ASDPOCS_ERR_NOMEM,
+                     "plan needs %zu bytes, over the HBM budget of %llu", off,
+                     hbm_budget_bytes);
+  }
+  cudaError_t e = cudaMalloc(&p->arena, off);
+  if (e != cudaSuccess) {
+    if (p->own_stream) cudaStreamDestroy(p->st);
+    delete p;
+    return cuda_status(e, "cudaMalloc(plan)");
+  }
+  char *b = (char *)p->arena;
+  e = cudaMemsetAsync(b, 0, off, p->st);
+  p->h_inst.resize(batch);
+  std::vector<float2> trig(p->nv);
+  for (int i = 0; i < batch && e == cudaSuccess; i++) {
+    const Off &o = offs[i];
+    Inst &I = p->h_inst[i];
+    GatewayGeo gg;
+    gateway_geometry(0.0, geom[i].SO, geom[i].OD, geom[i].vxlsize,
+                     geom[i].detsize, g0.na, g0.nb, gg);
+    I.g = ViewGeo{0.f, 0.f, gg.SO, gg.OD, gg.scale, gg.det, gg.det, 1.0f,
+                  (const float *)(b + o.ydet), (const float *)(b + o.zdet)};
+    for (int v = 0; v < p->nv; v++)
+      trig[v] = view_trig(phi_vec_deg[(size_t)i * p->nv + v]);
+    I.trig = (const float2 *)(b + o.trig);
+    I.P = (const float *)(b + o.P);
+    I.m = (float *)(b + o.m);
+    I.m_pre = (float *)(b + o.m_pre);
+    I.m_res = (float *)(b + o.m_res);
+    I.m_k1 = (float *)(b + o.m_k1);
+    I.I0 = (float *)(b + o.I0);
+    I.tv_b = (float *)(b + o.tvb);
+    I.tv_c = (float *)(b + o.tvc);
+    I.cor = (float *)(b + o.cor);
+    I.rmse = (double *)(b + o.rmse);
+    I.partials = (double *)(b + o.part);
+    I.counter = (unsigned *)(b + o.cnt);
+    I.s = (Scalars *)(b + o.scal);
+    e = cudaMemcpyAsync(b + o.ydet, gg.y_det.data(), (size_t)g0.na * 4,
+                        cudaMemcpyHostToDevice, p->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b + o.zdet, gg.z_det.data(), (size_t)g0.nb * 4,
+                          cudaMemcpyHostToDevice, p->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(b + o.trig, trig.data(), (size_t)p->nv * 8,
+                          cudaMemcpyHostToDevice, p->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);  // trig reused
+  }
+  p->d_inst = (Inst *)(b + inst_off);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(),
+                                            sizeof(Inst) * batch,
+                                            cudaMemcpyHostToDevice, p->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  if (e != cudaSuccess) {
+    asdpocs_plan_destroy(p);
+    return cuda_status(e, "plan setup");
+  }
+  *out = p;
+  return asdpocs_plan_reset(p);
+}
+
+int asdpocs_plan_destroy(asdpocs_plan p) {
+  if (!p) return 0;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  if (p->st) cudaStreamSynchronize(p->st);
+  if (p->arena) cudaFree(p->arena);
+  if (p->own_stream && p->st) cudaStreamDestroy(p->st);
+  delete p;
+  return 0;
+}
+
+unsigned long long asdpocs_plan_bytes(asdpocs_plan p) {
+  return p ? (unsigned long long)p->bytes : 0ULL;
+}
+
+static int plan_check(asdpocs_plan p, int inst) {
+  if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
+  if (inst < 0 || inst >= p->batch)
+    return set_error(ASDPOCS_ERR_ARG, "instance %d out of range", inst);
+  return 0;
+}
+
+static int plan_put(asdpocs_plan p, void *dst, const void *src, size_t bytes,
+                    int where) {
+  if (!src) {
+    ASD_CUDA(cudaMemsetAsync(dst, 0, bytes, p->st));
+  } else {
+    ASD_CUDA(cudaMemcpyAsync(dst, src, bytes,
+                             where ? cudaMemcpyDeviceToDevice
+                                   : cudaMemcpyHostToDevice,
+                             p->st));
+    if (!where) ASD_CUDA(cudaStreamSynchronize(p->st));
+  }
+  return 0;
+}
+
+int asdpocs_plan_set_sinogram(asdpocs_plan p, int inst, const float *P,
+                              int where) {
+  clear_error();
+  if (int e = plan_check(p, inst)) return e;
+  if (!P) return set_error(ASDPOCS_ERR_ARG, "null sinogram");
+  const size_t bytes = (size_t)p->d.na * p->d.nb * p->nv * 4;
+  return plan_put(p, (void *)p->h_inst[inst].P, P, bytes, where);
+}
+
+int asdpocs_plan_set_initial(asdpocs_plan p, int inst, const float *m0,
+                             int where) {
+  clear_error();
+  if (int e = plan_check(p, inst)) return e;
+  const size_t bytes = (size_t)p->d.nx * p->d.ny * p->d.nz * 4;
+  return plan_put(p, p->h_inst[inst].m_k1, m0, bytes, where);
+}
+
+int asdpocs_plan_set_reference(asdpocs_plan p, int inst, const float *I0,
+                               int where) {
+  clear_error();
+  if (int e = plan_check(p, inst)) return e;
+  const size_t bytes = (size_t)p->d.nx * p->d.ny * p->d.nz * 4;
+  p->has_ref[inst] = I0 != nullptr;
+  return plan_put(p, p->h_inst[inst].I0, I0, bytes, where);
+}
+
+int asdpocs_plan_reset(asdpocs_plan p) {
+  clear_error();
+  if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
+  const size_t bytes = (size_t)p->d.nx * p->d.ny * p->d.nz * 4;
+  std::vector<Scalars> hs(p->batch);
+  for (int i = 0; i < p->batch; i++) {
+    const asdpocs_options &o = p->opt[i];
+    Scalars &s = hs[i];
+    memset(&s, 0, sizeof s);
+    s.alpha = o.alpha;
+    s.beta = o.beta;
+    s.alpha_red = o.alpha_red;
+    s.beta_red = o.beta_red;
+    s.r_max = o.r_max;
+    s.epsilon = o.epsilon;
+    s.stopRelChg = o.stopRelChg;
+    s.k = 1;
+    s.maxIter = o.maxnumIter;
+    s.ng = o.numOfgradients;
+    s.done = o.maxnumIter <= 0;
+    s.has_ref = p->has_ref[i];
+    const Inst &I = p->h_inst[i];
+    ASD_CUDA(cudaMemcpyAsync(I.m, I.m_k1, bytes, cudaMemcpyDeviceToDevice, p->st));
+    ASD_CUDA(cudaMemcpyAsync(I.m_pre, I.m_k1, bytes, cudaMemcpyDeviceToDevice, p->st));
+    ASD_CUDA(cudaMemcpyAsync(I.m_res, I.m_k1, bytes, cudaMemcpyDeviceToDevice, p->st));
+    ASD_CUDA(cudaMemsetAsync(I.counter, 0, 256, p->st));
+    ASD_CUDA(cudaMemcpyAsync(I.s, &s, sizeof s, cudaMemcpyHostToDevice, p->st));
+  }
+  ASD_CUDA(cudaStreamSynchronize(p->st));
+  return 0;
+}
+
+int asdpocs_plan_run(asdpocs_plan p, int use_graph) {
+  clear_error();
+  if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
+  if (p->max_iter <= 0) return 0;
+  if (use_graph) {
+    if (!p->exec) {
+      ASD_CUDA(cudaStreamBeginCapture(p->st, cudaStreamCaptureModeThreadLocal));
+      const int rc = plan_enqueue_iteration(p);
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(p->st, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      ASD_CUDA(e);
+      p->graph = g;
+      ASD_CUDA(cudaGraphInstantiate(&p->exec, p->graph, 0));
+    }
+    for (int k = 0; k < p->max_iter; k++)
+      ASD_CUDA(cudaGraphLaunch(p->exec, p->st));
+  } else {
+    for (int k = 0; k < p->max_iter; k++)
+      if (int rc = plan_enqueue_iteration(p)) return rc;
+  }
+  return 0;
+}
+
+int asdpocs_plan_sync(asdpocs_plan p) {
+  clear_error();
+  if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
+  ASD_CUDA(cudaStreamSynchronize(p->st));
+  return 0;
+}
+
+int asdpocs_plan_get_image(asdpocs_plan p, int inst, float *m, int where) {
+  clear_error();
+  if (int e = plan_check(p, inst)) return e;
+  if (!m) return set_error(ASDPOCS_ERR_ARG, "null output");
+  const size_t bytes = (size_t)p->d.nx * p->d.ny * p->d.nz * 4;
+  ASD_CUDA(cudaMemcpyAsync(m, p->h_inst[inst].m_res, bytes,
+                           where ? cudaMemcpyDeviceToDevice
+                                 : cudaMemcpyDeviceToHost,
+                           p->st));
+  if (!where) ASD_CUDA(cudaStreamSynchronize(p->st));
+  return 0;
+}
+
+int asdpocs_plan_get_stats(asdpocs_plan p, int inst, asdpocs_stats *st,
+                           double *rmse) {
+  clear_error();
+  if (int e = plan_check(p, inst)) return e;
+  Scalars s;
+  ASD_CUDA(cudaMemcpyAsync(&s, p->h_inst[inst].s, sizeof s,
+                           cudaMemcpyDeviceToHost, p->st));
+  if (rmse && p->opt[inst].maxnumIter > 0)
+    ASD_CUDA(cudaMemcpyAsync(rmse, p->h_inst[inst].rmse,
+                             (size_t)p->opt[inst].maxnumIter * 8,
+                             cudaMemcpyDeviceToHost, p->st));
+  ASD_CUDA(cudaStreamSynchronize(p->st));
+  if (st) {
+    st->IterationNum = s.iterations;
+    st->dataTolerance = s.dd2;
+    st->alpha = s.alpha;
+    st->beta = s.beta;
+    st->dp = s.dp;
+    st->dg = s.dg;
+  }
+  return 0;
+}
+
+float *asdpocs_plan_sinogram_ptr(asdpocs_plan p, int inst) {
+  if (plan_check(p, inst)) return nullptr;
+  return (float *)p->h_inst[inst].P;
+}
+
+float *asdpocs_plan_image_ptr(asdpocs_plan p, int inst) {
+  if (plan_check(p, inst)) return nullptr;
+  return p->h_inst[inst].m_res;
+}
+
+// --------------------------------------------------- one-call drivers
+int ASD_POCS_cuda(const double *P, const double *phi_vec_deg,
+                  const asdpocs_geometry *geom, const asdpocs_options *opt,
+                  const double *m0, const double *I0, double *m_res,
+                  double *rmse, asdpocs_stats *out) {
+  clear_error();
+  if (!P || !phi_vec_deg || !geom || !m_res)
+    return set_error(ASDPOCS_ERR_ARG, "null argument");
+  asdpocs_plan p = nullptr;
+  if (int e = asdpocs_plan_create(&p, 1, geom, phi_vec_deg, opt, 0, nullptr))
+    return e;
+  const size_t N = (size_t)geom->nx * geom->ny * geom->nz;
+  const size_t PM = (size_t)geom->na * geom->nb * geom->nv;
+  std::vector<float> buf(PM > N ? PM : N);
+  int rc = 0;
+  for (size_t i = 0; i < PM; i++) buf[i] = (float)P[i];
+  rc = asdpocs_plan_set_sinogram(p, 0, buf.data(), 0);
+  if (!rc && m0) {
+    for (size_t i = 0; i < N; i++) buf[i] = (float)m0[i];
+    rc = asdpocs_plan_set_initial(p, 0, buf.data(), 0);
+  }
+  if (!rc && I0) {
+    for (size_t i = 0; i < N; i++) buf[i] = (float)I0[i];
+    rc = asdpocs_plan_set_reference(p, 0, buf.data(), 0);
+  }
+  if (!rc) rc = asdpocs_plan_reset(p);
+  if (!rc) rc = asdpocs_plan_run(p, 1);
+  if (!rc) rc = asdpocs_plan_get_image(p, 0, buf.data(), 0);
+  if (!rc) {
+    for (size_t i = 0; i < N; i++) m_res[i] = buf[i];
+    rc = asdpocs_plan_get_stats(p, 0, out, I0 ? rmse : nullptr);
+  }
+  const int saved = g_status;
+  char msg[512];
+  memcpy(msg, g_msg, sizeof msg);
+  asdpocs_plan_destroy(p);
+  if (rc) {
+    g_status = saved;
+    memcpy(g_msg, msg, sizeof msg);
+  }
+  return rc;
+}
+
+int SART_cuda_inline(const double *P, const double *phi_vec_deg,
+                     const asdpocs_geometry *geom, double lambda,
+                     const double *m0, double *m_out, double *dataTolerance) {
+  clear_error();
+  asdpocs_options o;
+  asdpocs_options_default(&o);
+  // one sweep, relaxation lambda, no TV (SART_cuda_inline.m:56-87)
+  o.maxnumIter = 1;
+  o.numOfgradients = 0;
+  o.beta = lambda;
+  asdpocs_stats st;
+  const int rc = ASD_POCS_cuda(P, phi_vec_deg, geom, &o, m0, nullptr, m_out,
+                               nullptr, &st);
+  if (rc == 0 && dataTolerance) *dataTolerance = st.dataTolerance;
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,47 @@
+// Launch wrappers of the device kernels (internal interface between the
+// kernel translation units and the host library).
+#pragma once
+#include "common.cuh"
+
+namespace asd {
+
+// ---- projectors (kernels_proj.cu) ----
+// Ax of one view: y, sr (na*nb) from x.
+cudaError_t launch_ax(const float *x, float *y, float *sr, const ViewGeo &g,
+                      const Dims &d, cudaStream_t st);
+// Atx of one view: x, sc (nx*ny*nz) from y.
+cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
+                       const Dims &d, cudaStream_t st);
+
+// Fused SART steps of view `view` for `batch` instances (ASD_POCS_cuda.m:
+// 116-131).  sart_ax: Ax of m, residual against P, dd2 accumulation, row
+// normalisation -> cor.  sart_atx: Atx of cor, column normalisation, update
+// m += beta*bp/sumC, positivity.
+cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
+                           int view, cudaStream_t st);
+cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
+                            int view, cudaStream_t st);
+
+// ---- TV and scalars (kernels_tv.cu) ----
+// FP64 / FP32 TV minimisation on device buffers (reference semantics).
+cudaError_t tv_minimize_f64(double *img, const double *img_old, double *work_a,
+                            double *work_b, double *scal, double *partials,
+                            unsigned *counter, int nx, int ny, int nz,
+                            double alpha, int n_iter, int pos, cudaStream_t st);
+cudaError_t tv_minimize_f32(float *img, const float *img_old, float *work_a,
+                            float *work_b, double *scal, double *partials,
+                            unsigned *counter, int nx, int ny, int nz,
+                            double alpha, int n_iter, int pos, cudaStream_t st);
+
+// Per-iteration ASD-POCS steps for a batch (ASD_POCS_cuda.m:137-170).
+cudaError_t launch_iter_begin(const Inst *insts, int batch, cudaStream_t st);
+cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
+                               cudaStream_t st);
+cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
+                           int step, int ng, cudaStream_t st);
+cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
+                               int ng, cudaStream_t st);
+
+int reduce_blocks_for(const Dims &d);
+
+}  // namespace asd

@@ -1,0 +1,334 @@
+// Device math of the ray-driven projector (Ax) and the voxel-driven
+// backprojector (Atx).
+//
+// Parity contract: every float operation below is an IEEE single-precision
+// operation in the same order as the reference expressions
+// (src/AxAtx/Ax_cone_gpu.cu), and the translation units that include this
+// file are compiled with -fmad=false, so nothing is contracted into a fused
+// multiply-add.  Division and square root are the IEEE-rounded ones
+// (-prec-div/-prec-sqrt default).  Per-ray/per-view quantities are hoisted
+// out of the inner loops only where the hoisted value is bit-identical to
+// the one the reference recomputes.
+#pragma once
+#include "common.cuh"
+
+namespace asd {
+
+// ---------------------------------------------------------------------------
+// Ax: partial sums of one ray over the columns iu = first, first+step, ...
+// (Ax_cone_gpu.cu:339-776).
+//
+// The ray is marched along its driving axis u (x when |dx|>|dy|, :372, else
+// y, :573).  In each column it spans [v1,v2] across the in-plane transverse
+// axis v and [w1,w2] in z (sorted by slope sign, :377-394).  The column
+// length l (:402) is split at the v-crossing (fraction rv from v1) and at the
+// z-crossing (fraction rz from w1); pieces are the overlaps of [0,rv],[rv,1]
+// with [0,rz],[rz,1], added in position order.  The reference enumerates
+// these overlaps as 16 explicit cases (:398-570); rows / slices that fall
+// outside the volume lose their pieces under the same range tests
+// (cy2==0 keeps only the upper row, cy2==ny only the lower one, ...).
+// Indices the reference would read out of bounds (|slope|>1 in z, which it
+// does not support) are skipped instead.
+// ---------------------------------------------------------------------------
+struct RayMarch {
+  float us, vs, slope1, slope2, len2, dz2sq, dz;
+  int nu, nv, nz, nu2, nv2, nz2;
+  int su, sv;  // memory strides of u and v
+  long long sz;
+};
+
+__device__ __forceinline__ RayMarch ray_setup(const ViewGeo &G, const Dims &D,
+                                              float ydet, float zdet) {
+  RayMarch R;
+  const float x1 = G.cos_phi * (-G.SO);
+  const float y1 = G.sin_phi * (-G.SO);
+  const float z1 = 0.0f;
+  const float x2 = G.cos_phi * G.OD - G.sin_phi * ydet;
+  const float y2 = G.sin_phi * G.OD + G.cos_phi * ydet;
+  const float z2 = zdet;
+  const bool xdrive = fabsf(x1 - x2) > fabsf(y1 - y2);
+  const float du = xdrive ? (x2 - x1) : (y2 - y1);
+  const float dv = xdrive ? (y2 - y1) : (x2 - x1);
+  R.us = xdrive ? x1 : y1;
+  R.vs = xdrive ? y1 : x1;
+  R.slope1 = dv / du;
+  R.slope2 = (z2 - z1) / du;
+  R.len2 = (x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2);
+  R.dz2sq = (z1 - z2) * (z1 - z2);
+  R.dz = G.dz;
+  R.nu = xdrive ? D.nx : D.ny;
+  R.nv = xdrive ? D.ny : D.nx;
+  R.nz = D.nz;
+  R.nu2 = R.nu / 2;
+  R.nv2 = R.nv / 2;
+  R.nz2 = D.nz / 2;
+  R.su = xdrive ? 1 : D.nx;
+  R.sv = xdrive ? D.nx : 1;
+  R.sz = (long long)D.nx * D.ny;
+  return R;
+}
+
+// Adds the contributions of columns first, first+step, ... to (ys, ss).
+template <class Loader>
+__device__ __forceinline__ void ray_columns(const RayMarch &R, int first,
+                                            int step, Loader ld, float &ys,
+                                            float &ss) {
+  for (int iu = first; iu < R.nu; iu += step) {
+    const float uu1 = (float)(iu - R.nu2);
+    const float uu2 = uu1 + 1;
+    float v1, v2, w1, w2;
+    if (R.slope1 >= 0) {
+      v1 = R.vs + R.slope1 * (uu1 - R.us) + R.nv2;
+      v2 = R.vs + R.slope1 * (uu2 - R.us) + R.nv2;
+    } else {
+      v1 = R.vs + R.slope1 * (uu2 - R.us) + R.nv2;
+      v2 = R.vs + R.slope1 * (uu1 - R.us) + R.nv2;
+    }
+    const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
+    if (R.slope2 >= 0) {
+      w1 = (0.0f + R.slope2 * (uu1 - R.us)) / R.dz + R.nz2;
+      w2 = (0.0f + R.slope2 * (uu2 - R.us)) / R.dz + R.nz2;
+    } else {
+      w1 = (0.0f + R.slope2 * (uu2 - R.us)) / R.dz + R.nz2;
+      w2 = (0.0f + R.slope2 * (uu1 - R.us)) / R.dz + R.nz2;
+    }
+    const int cz1 = (int)floorf(w1), cz2 = (int)floorf(w2);
+    const bool vsplit = cv1 != cv2, zsplit = cz1 != cz2;
+    bool vlo, vhi, zlo, zhi;
+    if (!vsplit) {
+      vlo = cv1 >= 0 && cv1 <= R.nv - 1;
+      vhi = false;
+    } else if (cv2 > 0 && cv2 < R.nv) {
+      vlo = vhi = true;
+    } else {
+      vlo = cv2 == R.nv;
+      vhi = cv2 == 0;
+    }
+    if (!zsplit) {
+      zlo = cz1 >= 0 && cz1 <= R.nz - 1;
+      zhi = false;
+    } else if (cz2 > 0 && cz2 < R.nz) {
+      zlo = zhi = true;
+    } else {
+      zlo = cz2 == R.nz;
+      zhi = cz2 == 0;
+    }
+    vlo = vlo && cv1 >= 0 && cv1 < R.nv;
+    vhi = vhi && cv2 >= 0 && cv2 < R.nv;
+    zlo = zlo && cz1 >= 0 && cz1 < R.nz;
+    zhi = zhi && cz2 >= 0 && cz2 < R.nz;
+    if (!(vlo || vhi) || !(zlo || zhi)) continue;
+
+    const float d = v2 - v1;
+    const float l = sqrtf((d * d + 1) * (R.len2 + R.dz2sq) / R.len2);
+    const long long base = (long long)iu * R.su;
+    const long long ilo = base + (long long)cv1 * R.sv;
+    const long long ihi = base + (long long)cv2 * R.sv;
+    const long long zl = (long long)cz1 * R.sz, zh = (long long)cz2 * R.sz;
+#define ASD_PIECE(w, idx)   \
+  do {                      \
+    const float w_ = (w);   \
+    ys += w_ * ld(idx);     \
+    ss += w_;               \
+  } while (0)
+    if (!vsplit && !zsplit) {
+      ASD_PIECE(l, ilo + zl);
+    } else if (!vsplit) {
+      const float rz = (cz2 - w1) / (w2 - w1);
+      if (zlo) ASD_PIECE(rz * l, ilo + zl);
+      if (zhi) ASD_PIECE((1 - rz) * l, ilo + zh);
+    } else if (!zsplit) {
+      const float rv = (cv2 - v1) / d;
+      if (vlo) ASD_PIECE(rv * l, ilo + zl);
+      if (vhi) ASD_PIECE((1 - rv) * l, ihi + zl);
+    } else {
+      const float rv = (cv2 - v1) / d;
+      const float rz = (cz2 - w1) / (w2 - w1);
+      if (rv > rz) {
+        if (vlo && zlo) ASD_PIECE(rz * l, ilo + zl);
+        if (vlo && zhi) ASD_PIECE((rv - rz) * l, ilo + zh);
+        if (vhi && zhi) ASD_PIECE((1 - rv) * l, ihi + zh);
+      } else {
+        if (vlo && zlo) ASD_PIECE(rv * l, ilo + zl);
+        if (vhi && zlo) ASD_PIECE((rz - rv) * l, ihi + zl);
+        if (vhi && zhi) ASD_PIECE((1 - rz) * l, ihi + zh);
+      }
+    }
+#undef ASD_PIECE
+  }
+}
+
+// Warp-wide sum; the xor butterfly leaves bit-identical totals in every lane
+// (IEEE addition is commutative).
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Atx: chord length of a line through one voxel (find_l / find_l_3d,
+// Ax_cone_gpu.cu:16-209).  The line starts at the source; (rx,ry,rz) is the
+// source minus the voxel centre.  Faces normal to the dominant in-plane axis
+// are tested first (x,y,z when |a|>|b|, else y,x,z), each pair lower face
+// then upper face; the first two boundary points found define the chord.
+// Comparisons with NaN/inf (c == 0 in 2D) are false, as in the reference.
+// ---------------------------------------------------------------------------
+struct Hits {
+  int n;
+  float p0x, p0y, p0z, p1x, p1y, p1z;
+};
+
+__device__ __forceinline__ void add_hit(Hits &h, float a, float b, float c) {
+  if (h.n == 0) {
+    h.p0x = a;
+    h.p0y = b;
+    h.p0z = c;
+    h.n = 1;
+  } else if (h.n == 1) {
+    h.p1x = a;
+    h.p1y = b;
+    h.p1z = c;
+    h.n = 2;
+  }
+}
+
+// find_l: line (p1,q1)->(p2,q2) and a (dp x dq) box centred at (pc,qc).
+__device__ __forceinline__ float chord2(float p1, float q1, float p2, float q2,
+                                        float dp, float dq, float pc,
+                                        float qc) {
+  const float a = p2 - p1, b = q2 - q1;
+  const float hp = dp / 2.0f, hq = dq / 2.0f;
+  if (a == 0) return fabsf(p1 - pc) <= hp ? dq : 0.0f;
+  if (b == 0) return fabsf(q1 - qc) <= hq ? dp : 0.0f;
+  const float rp = p1 - pc, rq = q1 - qc;
+  Hits h;
+  h.n = 0;
+  const bool pfirst = fabsf(a) > fabsf(b);
+#pragma unroll
+  for (int pass = 0; pass < 2; pass++) {
+    if (h.n >= 2) break;
+    if ((pass == 0) == pfirst) {
+      const float s = b / a;
+      const float t = s * (-rp) + rq, u = s * hp;
+      if (fabsf(t - u) <= hq) add_hit(h, -hp, t - u, 0.f);
+      if (fabsf(t + u) <= hq) add_hit(h, hp, t + u, 0.f);
+    } else {
+      const float s = a / b;
+      const float t = s * (-rq) + rp, u = s * hq;
+      if (fabsf(t - u) <= hp) add_hit(h, t - u, -hq, 0.f);
+      if (fabsf(t + u) <= hp) add_hit(h, t + u, hq, 0.f);
+    }
+  }
+  if (h.n < 2) return 0.0f;
+  const float e0 = h.p1x - h.p0x, e1 = h.p1y - h.p0y;
+  return sqrtf(e0 * e0 + e1 * e1);
+}
+
+// find_l_3d with unit x/y voxel size and z size dz.
+__device__ __forceinline__ float chord3(float x1, float y1, float z1, float x2,
+                                        float y2, float z2, float dz, float xc,
+                                        float yc, float zc) {
+  const float a = x2 - x1, b = y2 - y1, c = z2 - z1;
+  const float hx = 1.0f / 2.0f, hy = 1.0f / 2.0f, hz = dz / 2.0f;
+  if (a == 0) return chord2(y1, z1, y2, z2, 1.0f, dz, yc, zc);
+  if (b == 0) return chord2(x1, z1, x2, z2, 1.0f, dz, xc, zc);
+  const float rx = x1 - xc, ry = y1 - yc, rz = z1 - zc;
+  const bool xfirst = fabsf(a) > fabsf(b);
+  Hits h;
+  h.n = 0;
+#pragma unroll
+  for (int pass = 0; pass < 3; pass++) {
+    if (h.n >= 2) break;
+    const int axis = pass == 2 ? 2 : (((pass == 0) == xfirst) ? 0 : 1);
+    if (axis == 0) {
+      float s = b / a;
+      const float t0 = s * (-rx) + ry, u0 = s * hx;
+      s = c / a;
+      const float t1 = s * (-rx) + rz, u1 = s * hx;
+      if (fabsf(t0 - u0) <= hy && fabsf(t1 - u1) <= hz)
+        add_hit(h, -hx, t0 - u0, t1 - u1);
+      if (fabsf(t0 + u0) <= hy && fabsf(t1 + u1) <= hz)
+        add_hit(h, hx, t0 + u0, t1 + u1);
+    } else if (axis == 1) {
+      float s = a / b;
+      const float t0 = s * (-ry) + rx, u0 = s * hy;
+      s = c / b;
+      const float t1 = s * (-ry) + rz, u1 = s * hy;
+      if (fabsf(t0 - u0) <= hx && fabsf(t1 - u1) <= hz)
+        add_hit(h, t0 - u0, -hy, t1 - u1);
+      if (fabsf(t0 + u0) <= hx && fabsf(t1 + u1) <= hz)
+        add_hit(h, t0 + u0, hy, t1 + u1);
+    } else {
+      float s = a / c;
+      const float t0 = s * (-rz) + rx, u0 = s * hz;
+      s = b / c;
+      const float t1 = s * (-rz) + ry, u1 = s * hz;
+      if (fabsf(t0 - u0) <= hx && fabsf(t1 - u1) <= hy)
+        add_hit(h, t0 - u0, t1 - u1, -hz);
+      if (fabsf(t0 + u0) <= hx && fabsf(t1 + u1) <= hy)
+        add_hit(h, t0 + u0, t1 + u1, hz);
+    }
+  }
+  if (h.n < 2) return 0.0f;
+  const float e0 = h.p1x - h.p0x, e1 = h.p1y - h.p0y, e2 = h.p1z - h.p0z;
+  return sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
+}
+
+// Per-voxel footprint of Atx (Ax_cone_gpu.cu:230-253).
+struct VoxelWin {
+  float xc, yc, zc;
+  int a0, a1, b0, b1;
+};
+
+__device__ __forceinline__ VoxelWin voxel_window(const ViewGeo &G,
+                                                 const Dims &D, int ix, int iy,
+                                                 int iz) {
+  VoxelWin w;
+  const float SD = G.SO + G.OD;
+  const int na2 = D.na / 2, nb2 = D.nb / 2;
+  const int nx2 = D.nx / 2, ny2 = D.ny / 2, nz2 = D.nz / 2;
+  const float d = sqrtf((1 + G.dz * G.dz) / 2);
+  // (float)(i + 0.5 - n2) is evaluated in double by the reference; for
+  // |i - n2| < 2^22 the float form below is the same exactly-representable
+  // value and avoids FP64 arithmetic (slow on this GPU).
+  w.zc = ((float)(iz - nz2) + 0.5f) * G.dz;
+  w.yc = (float)(iy - ny2) + 0.5f;
+  w.xc = (float)(ix - nx2) + 0.5f;
+  const float xr = G.cos_phi * w.xc + G.sin_phi * w.yc;
+  const float yr = -G.sin_phi * w.xc + G.cos_phi * w.yc;
+  float t = SD / ((xr + G.SO) * G.dy_det);
+  const int amax = (int)floorf((yr + 1) * t + na2);
+  const int amin = (int)floorf((yr - 1) * t + na2);
+  t = SD / ((xr + G.SO) * G.dz_det);
+  const int bmax = (int)floorf((w.zc + d) * t + nb2);
+  const int bmin = (int)floorf((w.zc - d) * t + nb2);
+  w.a0 = amin > 0 ? amin : 0;
+  w.a1 = amax < D.na - 1 ? amax : D.na - 1;
+  w.b0 = bmin > 0 ? bmin : 0;
+  w.b1 = bmax < D.nb - 1 ? bmax : D.nb - 1;
+  return w;
+}
+
+// Sums l*y and l over the voxel's footprint (reference loop order: ib outer,
+// ia inner; Ax_cone_gpu.cu:255-269).
+template <class YLoad>
+__device__ __forceinline__ void voxel_backproject(const ViewGeo &G,
+                                                  const Dims &D,
+                                                  const VoxelWin &w, YLoad yl,
+                                                  float &acc, float &accl) {
+  const float xs = G.cos_phi * (-G.SO), ys = G.sin_phi * (-G.SO), zs = 0.0f;
+  for (int ib = w.b0; ib <= w.b1; ib++) {
+    const float zd = G.z_det[ib];
+    for (int ia = w.a0; ia <= w.a1; ia++) {
+      const float yd_ = G.y_det[ia];
+      const float xd = G.cos_phi * G.OD - G.sin_phi * yd_;
+      const float ydd = G.sin_phi * G.OD + G.cos_phi * yd_;
+      const float l = chord3(xs, ys, zs, xd, ydd, zd, G.dz, w.xc, w.yc, w.zc);
+      acc += l * yl((long long)ib * D.na + ia);
+      accl += l;
+    }
+  }
+}
+
+}  // namespace asd

@@ -1,0 +1,218 @@
+/*
+ * asdpocs_gb300 -- C ABI of the GB300 (sm_103a) ASD-POCS hot path.
+ *
+ * Drop-in boundary for the reference's projector / TV / ASD-POCS path
+ * (imagereconstruction/ASD_POCS_mex_cuda_demo).  Every entry point is plain C:
+ * pointers, sizes and scalars only.
+ *
+ * Layouts (identical to the reference):
+ *   volume   x-fastest, idx = iz*ny*nx + iy*nx + ix   (Ax_cone_gpu.cu:237),
+ *            i.e. a MATLAB column-major [nx,ny,nz] array;
+ *   view     na*nb values, ia fastest, id = ib*na + ia   (Ax_cone_gpu.cu:360);
+ *   sinogram (na*nb) x nv column-major: view ii is contiguous
+ *            (ASD_POCS_cuda.m:121, P(:,ii)).
+ * Geometry at the launcher level is in voxel units (SO, OD, detector
+ * coordinates divided by the voxel size; Ax_main_test.cpp:141-161).
+ *
+ * Error behaviour: functions returning int return ASDPOCS_OK (0) or an
+ * asdpocs_status code; asdpocs_last_error() gives the message of the last
+ * failure on the calling thread.  The two launcher drop-ins keep the
+ * reference's void signatures; failures there are reported through
+ * asdpocs_last_status()/asdpocs_last_error().
+ */
+#ifndef ASDPOCS_GB300_H
+#define ASDPOCS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  ASDPOCS_OK = 0,
+  ASDPOCS_ERR_ARG = 1,     /* bad argument / size mismatch (mexErrMsgTxt)  */
+  ASDPOCS_ERR_CUDA = 2,    /* CUDA runtime error                           */
+  ASDPOCS_ERR_NOMEM = 3,   /* device allocation failed / over HBM budget   */
+  ASDPOCS_ERR_STATE = 4,   /* call not valid in the object's current state */
+  ASDPOCS_ERR_TIMEOUT = 5, /* a bounded device-side wait gave up           */
+  ASDPOCS_ERR_NODEV = 6    /* no CUDA device                               */
+} asdpocs_status;
+
+/* Message / status of the last failed call on this thread ("" / 0 if none). */
+const char *asdpocs_last_error(void);
+int asdpocs_last_status(void);
+/* Library version string. */
+const char *asdpocs_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Launcher drop-ins: identical signatures to the reference            */
+/* ------------------------------------------------------------------ */
+
+/* Replaces Ax_cone_mf_gpu_new (src/AxAtx/Ax_cone_gpu.cu:778-805).
+ * Host pointers; synchronous.  X: nx*ny*nz volume (input); y, sr: na*nb
+ * projection and ray sums (outputs); y_det[na], z_det[nb] detector
+ * coordinates; SO, OD in voxel units; scale = voxel size. */
+void Ax_cone_mf_gpu_new(float *X, float *y, float *sr, float cos_phi,
+                        float sin_phi, float *y_det, float *z_det, float SO,
+                        float OD, float scale, float dz, int nx, int ny, int nz,
+                        int na, int nb);
+
+/* Replaces Atx_cone_mf_gpu_new (src/AxAtx/Ax_cone_gpu.cu:299-331).
+ * Host pointers; synchronous.  Note the reference's naming: X (nx*ny*nz)
+ * and sc are OUTPUTS, y (na*nb) is the input view. */
+void Atx_cone_mf_gpu_new(float *X, float *y, float *sc, float cos_phi,
+                         float sin_phi, float *y_det, float *z_det, float SO,
+                         float OD, float scale, float dy_det, float dz_det,
+                         float dz, int nx, int ny, int nz, int na, int nb);
+
+/* ------------------------------------------------------------------ */
+/* Device-pointer variants (no copies; enqueued on `stream`)           */
+/* ------------------------------------------------------------------ */
+
+/* Same computation as Ax_cone_mf_gpu_new on device buffers.  stream is a
+ * cudaStream_t (NULL = legacy default stream).  Asynchronous. */
+int asdpocs_ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
+                      float sin_phi, const float *y_det_d,
+                      const float *z_det_d, float SO, float OD, float scale,
+                      float dz, int nx, int ny, int nz, int na, int nb,
+                      void *stream);
+
+/* Same computation as Atx_cone_mf_gpu_new on device buffers (x_d, sc_d
+ * outputs, y_d input).  Asynchronous. */
+int asdpocs_atx_device(float *x_d, const float *y_d, float *sc_d,
+                       float cos_phi, float sin_phi, const float *y_det_d,
+                       const float *z_det_d, float SO, float OD, float scale,
+                       float dy_det, float dz_det, float dz, int nx, int ny,
+                       int nz, int na, int nb, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* mex-level entry points (the para struct as a C struct)              */
+/* ------------------------------------------------------------------ */
+
+/* The fields the gateways read (Ax_main_test.cpp:48-126); lengths in mm,
+ * phi in radians (scalar). */
+typedef struct {
+  double SO, OD, vxlsize, detsize, phi;
+  int nx, ny, nz, na, nb;
+} asdpocs_para;
+
+/* [y,sr] = Ax_cone_gpu(single X, para)   (Ax_main_test.cpp:19-164).
+ * numel_X is checked against nx*ny*nz ("Error size of input argument X!").
+ * Host pointers; y, sr have na*nb elements. */
+int Ax_cone_gpu(const float *X, long long numel_X, const asdpocs_para *para,
+                float *y, float *sr);
+
+/* [x,sc] = Atx_cone_gpu(single Y, para)  (Atx_main_test.cpp:20-176).
+ * numel_Y is checked against na*nb.  x, sc have nx*ny*nz elements. */
+int Atx_cone_gpu(const float *Y, long long numel_Y, const asdpocs_para *para,
+                 float *x, float *sc);
+
+/* I2 = imgTVGradMin(I, alpha, nTVIter, pos[, I0])   (imgTVGradMin.cpp:16-140)
+ * I: rowN x colN double, column-major; img_old may be NULL (zeros).
+ * Computed on the GPU in FP64. */
+int imgTVGradMin(const double *img, double *img_out, int rowN, int colN,
+                 double alpha, int nTVIter, int pos, const double *img_old);
+
+/* I2 = imgTVGradMin3D(I, alpha, nTVIter, pos[, I0]) (imgTVGradMin3D.cpp:18-189)
+ * I: Nx x Ny x Nz double, column-major.  FP64 on the GPU. */
+int imgTVGradMin3D(const double *img, double *img_out, int Nx, int Ny, int Nz,
+                   double alpha, int nTVIter, int pos, const double *img_old);
+
+/* FP32 device variants of the TV minimisation (in place on img_d). */
+int asdpocs_tv_device(float *img_d, const float *img_old_d, int nx, int ny,
+                      int nz, double alpha, int nTVIter, int pos, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* ASD-POCS reconstruction jobs (device resident)                      */
+/* ------------------------------------------------------------------ */
+
+/* Option set of ASD_POCS_cuda.m:20-96 (defaults via asdpocs_options_default). */
+typedef struct {
+  int maxnumIter;       /* 5      */
+  int numOfgradients;   /* ng, 20 */
+  double alpha;         /* 0.02   */
+  double alpha_red;     /* 0.95   */
+  double beta;          /* 1      */
+  double beta_red;      /* 0.995  */
+  double r_max;         /* 0.95   */
+  double epsilon;       /* eps    */
+  double stopRelChg;    /* eps    */
+} asdpocs_options;
+void asdpocs_options_default(asdpocs_options *opt);
+
+/* Per-reconstruction outputs (the `out` struct of ASD_POCS_cuda.m:173-180). */
+typedef struct {
+  int IterationNum;
+  double dataTolerance; /* dd2 of the last SART sweep */
+  double alpha, beta;
+  double dp, dg;        /* last ||m-m_pre||, ||m_TV - m_SART|| */
+} asdpocs_stats;
+
+/* Geometry of one reconstruction instance (the para struct minus phi). */
+typedef struct {
+  int nx, ny, nz, na, nb, nv;
+  double SO, OD, vxlsize, detsize; /* mm */
+} asdpocs_geometry;
+
+typedef struct asdpocs_plan_s *asdpocs_plan;
+
+/* Create a plan for `batch` reconstructions that share nx,ny,nz,na,nb,nv.
+ * geom[i], phi_vec_deg[i*nv..] and opt[i] are per instance (geom/opt may
+ * point to one element when batch==1).  All device memory is allocated here;
+ * hbm_budget_bytes (0 = no limit) rejects plans that would exceed it. */
+int asdpocs_plan_create(asdpocs_plan *plan, int batch,
+                        const asdpocs_geometry *geom,
+                        const double *phi_vec_deg,
+                        const asdpocs_options *opt,
+                        unsigned long long hbm_budget_bytes, void *stream);
+int asdpocs_plan_destroy(asdpocs_plan plan);
+/* Device bytes held by the plan. */
+unsigned long long asdpocs_plan_bytes(asdpocs_plan plan);
+
+/* Load instance data.  `where`: 0 = host pointer (copied on the plan's
+ * stream), 1 = device pointer.  P: (na*nb) x nv float sinogram; m0 / I0:
+ * nx*ny*nz (NULL = zeros / no RMSE). */
+int asdpocs_plan_set_sinogram(asdpocs_plan plan, int inst, const float *P,
+                              int where);
+int asdpocs_plan_set_initial(asdpocs_plan plan, int inst, const float *m0,
+                             int where);
+int asdpocs_plan_set_reference(asdpocs_plan plan, int inst, const float *I0,
+                               int where);
+/* Reset iteration state (alpha, beta, k) of every instance to the options. */
+int asdpocs_plan_reset(asdpocs_plan plan);
+
+/* Run the ASD-POCS iterations of every instance (asynchronous on the plan's
+ * stream).  use_graph != 0 captures one iteration into a CUDA graph once
+ * and replays it. */
+int asdpocs_plan_run(asdpocs_plan plan, int use_graph);
+/* Wait for the plan's stream. */
+int asdpocs_plan_sync(asdpocs_plan plan);
+
+/* Results: m_res (post-SART image of the last iteration, nx*ny*nz floats),
+ * per-iteration RMSE (maxnumIter doubles, if a reference image was set) and
+ * the stats.  `where` as above; host copies synchronise the stream. */
+int asdpocs_plan_get_image(asdpocs_plan plan, int inst, float *m, int where);
+int asdpocs_plan_get_stats(asdpocs_plan plan, int inst, asdpocs_stats *st,
+                           double *rmse);
+/* Device pointer of an instance's sinogram / result image (for zero-copy
+ * pipelines). */
+float *asdpocs_plan_sinogram_ptr(asdpocs_plan plan, int inst);
+float *asdpocs_plan_image_ptr(asdpocs_plan plan, int inst);
+
+/* One-call equivalent of [m_res,out] = ASD_POCS_cuda(P, para): host buffers,
+ * FP64 in/out as in MATLAB (P: (na*nb) x nv, column-major; phi_vec in
+ * degrees; m0 / I0 may be NULL; rmse may be NULL). */
+int ASD_POCS_cuda(const double *P, const double *phi_vec_deg,
+                  const asdpocs_geometry *geom, const asdpocs_options *opt,
+                  const double *m0, const double *I0, double *m_res,
+                  double *rmse, asdpocs_stats *out);
+
+/* m = SART_cuda_inline(P, para): one SART sweep with relaxation lambda
+ * (SART_cuda_inline.m:17-108). */
+int SART_cuda_inline(const double *P, const double *phi_vec_deg,
+                     const asdpocs_geometry *geom, double lambda,
+                     const double *m0, double *m_out, double *dataTolerance);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,120 @@
+"""GPU parity of Ax / Atx (through the C ABI) against the golden vectors of
+the reference's own code and against the oracle.  Tolerance: relative L2
+error <= 1e-5 in FP32 (the spec bar); Atx additionally bit-exact
+(same operation order per voxel as the reference)."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import asd_pocs_mex_cuda_demo_gb300 as pkg
+from conftest import GOLDEN, rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+PROJ = sorted(glob.glob(os.path.join(GOLDEN, "proj_*.npz")))
+
+
+@pytest.mark.parametrize("path", PROJ, ids=[os.path.basename(p) for p in PROJ])
+def test_mex_level_vs_reference_vectors(gpu, path):
+    d = np.load(path)
+    nx, ny, nz, na, nb = (int(v) for v in d["dims"])
+    SO, OD, vx, det = d["geo"]
+    for k, a in enumerate(d["angles"]):
+        para = dict(SO=SO, OD=OD, vxlsize=vx, nx=nx, ny=ny, nz=nz, phi=-a / 180 * np.pi,
+                    detsize=det, na=na, nb=nb)
+        y, sr = pkg.Ax_cone_gpu(d["x"], para)
+        assert rel_l2(y, d["y"][k]) <= TOL, (a, rel_l2(y, d["y"][k]))
+        assert rel_l2(sr, d["sr"][k]) <= TOL
+        b, sc = pkg.Atx_cone_gpu(d["yview"], para)
+        assert np.array_equal(b, d["bp"][k]), (a, rel_l2(b, d["bp"][k]))
+        assert np.array_equal(sc, d["sc"][k])
+
+
+CASES = [
+    # nx, ny, nz, na, nb, SO, OD, det
+    (256, 256, 1, 512, 1, 541.0, 408.0, 1.0),
+    (512, 512, 1, 888, 1, 541.0, 408.0, 1.0),
+    (1, 1, 1, 3, 1, 541.0, 408.0, 1.0),
+    (3, 17, 1, 1, 1, 541.0, 408.0, 1.0),
+    (40, 40, 1, 80, 2, 405.941, 500.31, 0.6),
+    (48, 40, 24, 96, 48, 1000.0, 500.0, 0.8 * 5),
+    (17, 9, 5, 33, 7, 300.0, 200.0, 1.3),
+]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[str(c[:5]) for c in CASES])
+def test_launchers_vs_oracle(gpu, oracle_mod, case):
+    nx, ny, nz, na, nb, SO, OD, det = case
+    rng = np.random.default_rng(sum(case[:5]))
+    vx = SO / (SO + OD) * det * na / nx
+    x = rng.random(nx * ny * nz).astype(np.float32)
+    yv = rng.standard_normal(na * nb).astype(np.float32)
+    for a in [0.0, 90.0, 180.0, 270.0, 45.0] + rng.uniform(0, 360, 5).tolist():
+        g = oracle_mod.gateway_geometry(-a / 180 * np.pi, SO, OD, vx, det, na, nb)
+        yo, so = oracle_mod.ax(x, g, nx, ny, nz)
+        bo, co = oracle_mod.atx(yv, g, nx, ny, nz)
+        y = np.zeros(na * nb, np.float32)
+        sr = np.zeros(na * nb, np.float32)
+        pkg.Ax_cone_mf_gpu_new(x, y, sr, g["cos_phi"], g["sin_phi"], g["y_det"], g["z_det"],
+                               g["SO"], g["OD"], g["scale"], 1.0, nx, ny, nz, na, nb)
+        b = np.zeros(nx * ny * nz, np.float32)
+        sc = np.zeros(nx * ny * nz, np.float32)
+        pkg.Atx_cone_mf_gpu_new(b, yv, sc, g["cos_phi"], g["sin_phi"], g["y_det"],
+                                g["z_det"], g["SO"], g["OD"], g["scale"], g["det"],
+                                g["det"], 1.0, nx, ny, nz, na, nb)
+        assert rel_l2(y, yo) <= TOL, (a, rel_l2(y, yo))
+        assert rel_l2(sr, so) <= TOL
+        assert np.array_equal(b, bo), (a, rel_l2(b, bo))
+        assert np.array_equal(sc, co)
+
+
+def test_device_pointer_variants(gpu, oracle_mod):
+    import torch
+
+    from asd_pocs_mex_cuda_demo_gb300._lib import check, load
+
+    nx = ny = 96
+    nz, na, nb = 1, 192, 1
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = SO / (SO + OD) * det * na / nx
+    g = oracle_mod.gateway_geometry(-0.7, SO, OD, vx, det, na, nb)
+    x = torch.rand(nx * ny * nz, device=gpu)
+    ydet = torch.tensor(g["y_det"], device=gpu)
+    zdet = torch.tensor(g["z_det"], device=gpu)
+    y = torch.empty(na * nb, device=gpu)
+    sr = torch.empty(na * nb, device=gpu)
+    s = torch.cuda.current_stream().cuda_stream
+    L = load()
+    check(L.asdpocs_ax_device(x.data_ptr(), y.data_ptr(), sr.data_ptr(), g["cos_phi"],
+                              g["sin_phi"], ydet.data_ptr(), zdet.data_ptr(), g["SO"],
+                              g["OD"], g["scale"], 1.0, nx, ny, nz, na, nb, s))
+    b = torch.empty_like(x)
+    sc = torch.empty_like(x)
+    check(L.asdpocs_atx_device(b.data_ptr(), y.data_ptr(), sc.data_ptr(), g["cos_phi"],
+                               g["sin_phi"], ydet.data_ptr(), zdet.data_ptr(), g["SO"],
+                               g["OD"], g["scale"], g["det"], g["det"], 1.0, nx, ny, nz,
+                               na, nb, s))
+    torch.cuda.synchronize()
+    yo, so = oracle_mod.ax(x.cpu().numpy(), g, nx, ny, nz)
+    assert rel_l2(y.cpu().numpy(), yo) <= TOL
+    bo, co = oracle_mod.atx(y.cpu().numpy(), g, nx, ny, nz)
+    assert np.array_equal(b.cpu().numpy(), bo) and np.array_equal(sc.cpu().numpy(), co)
+
+
+def test_adjointness_gpu(gpu):
+    n, na = 128, 256
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = SO / (SO + OD) * det * na / n
+    rng = np.random.default_rng(11)
+    x = rng.random(n * n).astype(np.float32)
+    yv = rng.random(na).astype(np.float32)
+    for a in (13.0, 77.0, 200.0):
+        para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, phi=-a / 180 * np.pi,
+                    detsize=det, na=na, nb=1)
+        Ax, _ = pkg.Ax_cone_gpu(x, para)
+        Aty, _ = pkg.Atx_cone_gpu(yv, para)
+        lhs = float(np.dot(Ax.astype(np.float64), yv))
+        rhs = float(np.dot(x.astype(np.float64), Aty))
+        assert abs(lhs - rhs) / abs(lhs) < 2e-5
