@@ -91,6 +91,7 @@ SIGNATURES = [
     ("asdpocs_plan_get_stats", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Stats), _D]),
     ("asdpocs_plan_sinogram_ptr", C.c_void_p, [C.c_void_p, C.c_int]),
     ("asdpocs_plan_image_ptr", C.c_void_p, [C.c_void_p, C.c_int]),
+    ("asdpocs_plan_time_phase", C.c_int, [C.c_void_p, C.c_int, C.c_int, _D]),
     ("ASD_POCS_cuda", C.c_int, [_D, _D, C.POINTER(Geometry), C.POINTER(Options), _D, _D,
                                 _D, _D, C.POINTER(Stats)]),
     ("SART_cuda_inline", C.c_int, [_D, _D, C.POINTER(Geometry), C.c_double, _D, _D, _D]),

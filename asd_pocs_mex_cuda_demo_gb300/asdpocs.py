@@ -225,6 +225,14 @@ class Plan:
                     alpha=st.alpha, beta=st.beta, dp=st.dp, dg=st.dg,
                     RMSE=rmse[:st.IterationNum].copy())
 
+    def time_phase(self, phase: int, reps: int = 20) -> float:
+        """Average device milliseconds per launch of one phase kernel
+        (0 SART forward, 1 SART backward, 2 TV step, 3 sweep scalars) for the
+        whole batch; leaves the state modified (call reset())."""
+        ms = C.c_double()
+        check(load().asdpocs_plan_time_phase(self._h, int(phase), int(reps), C.byref(ms)))
+        return ms.value
+
     def sinogram_ptr(self, inst: int) -> int:
         return int(load().asdpocs_plan_sinogram_ptr(self._h, inst))
 

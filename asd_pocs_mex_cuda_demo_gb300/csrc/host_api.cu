@@ -730,6 +730,38 @@ float *asdpocs_plan_image_ptr(asdpocs_plan p, int inst) {
   return p->h_inst[inst].m_res;
 }
 
+int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
+                            double *avg_ms) {
+  clear_error();
+  if (!p || !avg_ms || reps <= 0 || phase < 0 || phase > 3)
+    return set_error(ASDPOCS_ERR_ARG, "bad profiling arguments");
+  cudaEvent_t e0, e1;
+  ASD_CUDA(cudaEventCreate(&e0));
+  ASD_CUDA(cudaEventCreate(&e1));
+  const int ng = p->max_ng > 0 ? p->max_ng : 1;
+  auto launch = [&](int i) -> cudaError_t {
+    switch (phase) {
+      case 0: return launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
+      case 1: return launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv, p->st);
+      case 2: return launch_tv_step(p->d_inst, p->batch, p->d, 1 + i % (ng > 1 ? ng - 1 : 1),
+                                    ng, p->st);
+      default: return launch_after_sweep(p->d_inst, p->batch, p->d, p->st);
+    }
+  };
+  cudaError_t e = launch(0);  // warm-up
+  if (e == cudaSuccess) e = cudaEventRecord(e0, p->st);
+  for (int i = 0; i < reps && e == cudaSuccess; i++) e = launch(i);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, p->st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ASD_CUDA(e);
+  *avg_ms = (double)ms / reps;
+  return 0;
+}
+
 // --------------------------------------------------- one-call drivers
 int ASD_POCS_cuda(const double *P, const double *phi_vec_deg,
                   const asdpocs_geometry *geom, const asdpocs_options *opt,

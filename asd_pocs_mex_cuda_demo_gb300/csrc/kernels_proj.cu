@@ -1,6 +1,11 @@
 // Projector kernels for sm_103a: Ax (ray-driven, one warp per ray) and Atx
 // (voxel-driven, one thread per voxel), standalone and fused with the SART
 // per-view update.  Compiled with -fmad=false (see projector.cuh).
+//
+// Atx stages the view's ray slopes in shared memory: each block first finds
+// the detector window its 32x8 voxel tile projects to, computes the slopes
+// of those rays once (two divisions per detector column, four per 3D ray),
+// then every (voxel, bin) pair reads them instead of dividing again.
 #include "kernels.h"
 #include "projector.cuh"
 #include "reduce.cuh"
@@ -9,12 +14,14 @@ namespace asd {
 
 namespace {
 
-constexpr int kAxWarps = 4;            // rays per Ax block
+constexpr int kAxWarps = 4;             // rays per Ax block
 constexpr int kAxThreads = kAxWarps * 32;
-constexpr int kTileX = 32, kTileY = 8; // Atx voxel tile (x fastest)
+constexpr int kTileX = 32, kTileY = 8;  // Atx voxel tile (x fastest)
 constexpr int kAtxThreads = kTileX * kTileY;
+constexpr int kTabA = 512;              // detector columns staged per block
+constexpr int kTabC = 2048;             // 3D rays staged per block
 
-__device__ __forceinline__ void tile_voxel(const Dims &D, int &ix, int &iy,
+__device__ __forceinline__ bool tile_voxel(const Dims &D, int &ix, int &iy,
                                            int &iz) {
   const int tx = (D.nx + kTileX - 1) / kTileX;
   const int ty = (D.ny + kTileY - 1) / kTileY;
@@ -25,41 +32,128 @@ __device__ __forceinline__ void tile_voxel(const Dims &D, int &ix, int &iy,
   iz = b / ty;
   ix = bx * kTileX + (threadIdx.x % kTileX);
   iy = by * kTileY + (threadIdx.x / kTileX);
+  return ix < D.nx && iy < D.ny;
 }
 
 int atx_blocks(const Dims &d) {
   return ((d.nx + kTileX - 1) / kTileX) * ((d.ny + kTileY - 1) / kTileY) * d.nz;
 }
 
-// ------------------------------------------------------------- standalone
+// ------------------------------------------------------------------- Ax
+// Partial sums of one ray in the lanes of a warp, reduced to every lane.
+template <class Loader>
+__device__ __forceinline__ void ax_warp(const ViewGeo &G, const Dims &D,
+                                        long long r, int lane, Loader ld,
+                                        float &ys, float &ss) {
+  const int ia = (int)(r % D.na), ib = (int)(r / D.na);
+  const float zd = G.z_det[ib];
+  const RayMarch R = ray_setup(G, D, G.y_det[ia], zd);
+  ys = 0.f;
+  ss = 0.f;
+  if (D.nz == 1 && zd == 0.0f)
+    ray_columns_planar(R, lane, 32, ld, ys, ss);
+  else
+    ray_columns(R, lane, 32, ld, ys, ss);
+  ys = warp_sum(ys);
+  ss = warp_sum(ss);
+}
+
 __global__ void __launch_bounds__(kAxThreads)
     k_ax(const float *__restrict__ x, float *__restrict__ y,
          float *__restrict__ sr, ViewGeo G, Dims D) {
   const int lane = threadIdx.x & 31;
   const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
   if (r >= (long long)D.na * D.nb) return;  // whole warp exits together
-  const int ia = (int)(r % D.na), ib = (int)(r / D.na);
-  const RayMarch R = ray_setup(G, D, G.y_det[ia], G.z_det[ib]);
-  float ys = 0.f, ss = 0.f;
-  ray_columns(R, lane, 32, [&](long long i) { return __ldg(x + i); }, ys, ss);
-  ys = warp_sum(ys);
-  ss = warp_sum(ss);
+  float ys, ss;
+  ax_warp(G, D, r, lane, [&](long long i) { return __ldg(x + i); }, ys, ss);
   if (lane == 0) {
     y[r] = ys * G.scale;
     sr[r] = ss * G.scale;
   }
 }
 
-__global__ void __launch_bounds__(kAtxThreads)
+// ------------------------------------------------------------------- Atx
+struct AtxShared {
+  float4 tabA[kTabA];
+  float4 tabC[kTabC];
+  int amin, amax, bmin, bmax;
+};
+
+// Footprint sum of one voxel using the block's staged ray tables, or the
+// direct per-pair computation when the block's window does not fit.
+// Must be called by every thread of the block (it synchronises).
+template <class YLoad>
+__device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
+                                              bool valid, int ix, int iy,
+                                              int iz, AtxShared &sh, YLoad yl,
+                                              float &acc, float &accl) {
+  const bool planar = D.nz == 1 && D.nb == 1 && G.z_det[0] == 0.0f;
+  VoxelWin w;
+  if (threadIdx.x == 0) {
+    sh.amin = 0x7fffffff;
+    sh.amax = -1;
+    sh.bmin = 0x7fffffff;
+    sh.bmax = -1;
+  }
+  __syncthreads();
+  if (valid) {
+    w = voxel_window(G, D, ix, iy, iz);
+    if (w.a0 <= w.a1 && w.b0 <= w.b1) {
+      atomicMin(&sh.amin, w.a0);
+      atomicMax(&sh.amax, w.a1);
+      atomicMin(&sh.bmin, w.b0);
+      atomicMax(&sh.bmax, w.b1);
+    }
+  }
+  __syncthreads();
+  const int amin = sh.amin, bmin = sh.bmin;
+  const int nA = sh.amax - amin + 1, nB = sh.bmax - bmin + 1;
+  acc = 0.f;
+  accl = 0.f;
+  if (nA <= 0) return;  // no voxel of the block sees the detector
+  const bool staged = nA <= kTabA && (planar || (long long)nA * nB <= kTabC);
+  if (staged) {
+    for (int k = threadIdx.x; k < nA; k += kAtxThreads)
+      sh.tabA[k] = ray_tab_a(G, G.y_det[amin + k]);
+    __syncthreads();
+    if (!planar) {
+      for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads)
+        sh.tabC[k] = ray_tab_c(sh.tabA[k % nA], G.z_det[bmin + k / nA]);
+      __syncthreads();
+    }
+  }
+  if (!valid) return;
+  if (!staged) {
+    voxel_backproject(G, D, w, yl, acc, accl);
+    return;
+  }
+  const float rx = G.cos_phi * (-G.SO) - w.xc;
+  const float ry = G.sin_phi * (-G.SO) - w.yc;
+  const float rz = 0.0f - w.zc;
+  for (int ib = w.b0; ib <= w.b1; ib++) {
+    const float c = G.z_det[ib] - 0.0f;
+    const long long row = (long long)ib * D.na;
+    const int trow = (ib - bmin) * nA - amin;
+    for (int ia = w.a0; ia <= w.a1; ia++) {
+      const float4 A = sh.tabA[ia - amin];
+      const float l = planar ? chord_planar(A, rx, ry, G.dz)
+                             : chord3_tab(A, sh.tabC[trow + ia], c, rx, ry, rz, G.dz);
+      acc += l * yl(row + ia);
+      accl += l;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kAtxThreads, 3)
     k_atx(float *__restrict__ x, const float *__restrict__ yv,
           float *__restrict__ sc, ViewGeo G, Dims D) {
+  __shared__ AtxShared sh;
   int ix, iy, iz;
-  tile_voxel(D, ix, iy, iz);
-  if (ix >= D.nx || iy >= D.ny) return;
-  const VoxelWin w = voxel_window(G, D, ix, iy, iz);
-  float acc = 0.f, accl = 0.f;
-  voxel_backproject(G, D, w, [&](long long i) { return __ldg(yv + i); }, acc,
-                    accl);
+  const bool valid = tile_voxel(D, ix, iy, iz);
+  float acc, accl;
+  atx_block_sum(G, D, valid, ix, iy, iz, sh,
+                [&](long long i) { return __ldg(yv + i); }, acc, accl);
+  if (!valid) return;
   const long long idx = ((long long)iz * D.ny + iy) * D.nx + ix;
   x[idx] = acc * G.scale;
   sc[idx] = accl * G.scale;
@@ -86,13 +180,9 @@ __global__ void __launch_bounds__(kAxThreads)
   const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
   double part[1] = {0.0};
   if (r < nr) {
-    const int ia = (int)(r % D.na), ib = (int)(r / D.na);
-    const RayMarch R = ray_setup(G, D, G.y_det[ia], G.z_det[ib]);
-    float ys = 0.f, ss = 0.f;
+    float ys, ss;
     const float *m = I.m;
-    ray_columns(R, lane, 32, [&](long long i) { return m[i]; }, ys, ss);
-    ys = warp_sum(ys);
-    ss = warp_sum(ss);
+    ax_warp(G, D, r, lane, [&](long long i) { return m[i]; }, ys, ss);
     if (lane == 0) {
       const float yv = ys * G.scale, srv = ss * G.scale;
       const float c0 = I.P[(long long)view * nr + r] - yv;
@@ -108,18 +198,19 @@ __global__ void __launch_bounds__(kAxThreads)
 
 // ASD_POCS_cuda.m:125-131: [bProj,sumC]=Atx(cor); sumC(sumC==0)=1;
 // m = m + beta*(bProj./sumC); m(m<0)=0.
-__global__ void __launch_bounds__(kAtxThreads)
+__global__ void __launch_bounds__(kAtxThreads, 3)
     k_sart_atx(const Inst *__restrict__ insts, Dims D, int view) {
+  __shared__ AtxShared sh;
   const Inst &I = insts[blockIdx.y];
   if (((volatile int *)&I.s->done)[0]) return;
   const ViewGeo G = view_of(I, view);
   int ix, iy, iz;
-  tile_voxel(D, ix, iy, iz);
-  if (ix >= D.nx || iy >= D.ny) return;
-  const VoxelWin w = voxel_window(G, D, ix, iy, iz);
-  float acc = 0.f, accl = 0.f;
+  const bool valid = tile_voxel(D, ix, iy, iz);
+  float acc, accl;
   const float *cor = I.cor;
-  voxel_backproject(G, D, w, [&](long long i) { return cor[i]; }, acc, accl);
+  atx_block_sum(G, D, valid, ix, iy, iz, sh,
+                [&](long long i) { return cor[i]; }, acc, accl);
+  if (!valid) return;
   const float bp = acc * G.scale, scv = accl * G.scale;
   const float beta = (float)I.s->beta;
   const long long idx = ((long long)iz * D.ny + iy) * D.nx + ix;

@@ -10,7 +10,13 @@
 // out of the inner loops only where the hoisted value is bit-identical to
 // the one the reference recomputes.
 #pragma once
+#include <math.h>
+
 #include "common.cuh"
+
+// Host+device: the same code also runs on the CPU in the host-side test of
+// the device math (tests/device_math).
+#define ASD_HD __host__ __device__ __forceinline__
 
 namespace asd {
 
@@ -37,7 +43,7 @@ struct RayMarch {
   long long sz;
 };
 
-__device__ __forceinline__ RayMarch ray_setup(const ViewGeo &G, const Dims &D,
+ASD_HD RayMarch ray_setup(const ViewGeo &G, const Dims &D,
                                               float ydet, float zdet) {
   RayMarch R;
   const float x1 = G.cos_phi * (-G.SO);
@@ -70,7 +76,7 @@ __device__ __forceinline__ RayMarch ray_setup(const ViewGeo &G, const Dims &D,
 
 // Adds the contributions of columns first, first+step, ... to (ys, ss).
 template <class Loader>
-__device__ __forceinline__ void ray_columns(const RayMarch &R, int first,
+ASD_HD void ray_columns(const RayMarch &R, int first,
                                             int step, Loader ld, float &ys,
                                             float &ss) {
   for (int iu = first; iu < R.nu; iu += step) {
@@ -158,6 +164,61 @@ __device__ __forceinline__ void ray_columns(const RayMarch &R, int first,
   }
 }
 
+// Planar case of ray_columns (nz == 1 and the ray in the plane z = 0, i.e.
+// z_det == 0): slope2 is +-0, so every column has w1 = w2 = 0, slice 0 and
+// len2 + dz2sq == len2; the z tests are dropped.  Bit-identical to the
+// generic march for these rays.
+template <class Loader>
+ASD_HD void ray_columns_planar(const RayMarch &R, int first,
+                                                   int step, Loader ld,
+                                                   float &ys, float &ss) {
+  for (int iu = first; iu < R.nu; iu += step) {
+    const float uu1 = (float)(iu - R.nu2);
+    const float uu2 = uu1 + 1;
+    float v1, v2;
+    if (R.slope1 >= 0) {
+      v1 = R.vs + R.slope1 * (uu1 - R.us) + R.nv2;
+      v2 = R.vs + R.slope1 * (uu2 - R.us) + R.nv2;
+    } else {
+      v1 = R.vs + R.slope1 * (uu2 - R.us) + R.nv2;
+      v2 = R.vs + R.slope1 * (uu1 - R.us) + R.nv2;
+    }
+    const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
+    const long long base = (long long)iu * R.su;
+    const float d = v2 - v1;
+    if (cv1 == cv2) {
+      if (cv1 < 0 || cv1 > R.nv - 1) continue;
+      const float l = sqrtf((d * d + 1) * R.len2 / R.len2);
+      const float w = l;
+      ys += w * ld(base + (long long)cv1 * R.sv);
+      ss += w;
+    } else {
+      bool vlo, vhi;
+      if (cv2 > 0 && cv2 < R.nv) {
+        vlo = vhi = true;
+      } else {
+        vlo = cv2 == R.nv;
+        vhi = cv2 == 0;
+      }
+      vlo = vlo && cv1 >= 0 && cv1 < R.nv;
+      vhi = vhi && cv2 >= 0 && cv2 < R.nv;
+      if (!(vlo || vhi)) continue;
+      const float l = sqrtf((d * d + 1) * R.len2 / R.len2);
+      const float rv = (cv2 - v1) / d;
+      if (vlo) {
+        const float w = rv * l;
+        ys += w * ld(base + (long long)cv1 * R.sv);
+        ss += w;
+      }
+      if (vhi) {
+        const float w = (1 - rv) * l;
+        ys += w * ld(base + (long long)cv2 * R.sv);
+        ss += w;
+      }
+    }
+  }
+}
+
 // Warp-wide sum; the xor butterfly leaves bit-identical totals in every lane
 // (IEEE addition is commutative).
 __device__ __forceinline__ float warp_sum(float v) {
@@ -179,7 +240,7 @@ struct Hits {
   float p0x, p0y, p0z, p1x, p1y, p1z;
 };
 
-__device__ __forceinline__ void add_hit(Hits &h, float a, float b, float c) {
+ASD_HD void add_hit(Hits &h, float a, float b, float c) {
   if (h.n == 0) {
     h.p0x = a;
     h.p0y = b;
@@ -194,7 +255,7 @@ __device__ __forceinline__ void add_hit(Hits &h, float a, float b, float c) {
 }
 
 // find_l: line (p1,q1)->(p2,q2) and a (dp x dq) box centred at (pc,qc).
-__device__ __forceinline__ float chord2(float p1, float q1, float p2, float q2,
+ASD_HD float chord2(float p1, float q1, float p2, float q2,
                                         float dp, float dq, float pc,
                                         float qc) {
   const float a = p2 - p1, b = q2 - q1;
@@ -226,7 +287,7 @@ __device__ __forceinline__ float chord2(float p1, float q1, float p2, float q2,
 }
 
 // find_l_3d with unit x/y voxel size and z size dz.
-__device__ __forceinline__ float chord3(float x1, float y1, float z1, float x2,
+ASD_HD float chord3(float x1, float y1, float z1, float x2,
                                         float y2, float z2, float dz, float xc,
                                         float yc, float zc) {
   const float a = x2 - x1, b = y2 - y1, c = z2 - z1;
@@ -281,7 +342,7 @@ struct VoxelWin {
   int a0, a1, b0, b1;
 };
 
-__device__ __forceinline__ VoxelWin voxel_window(const ViewGeo &G,
+ASD_HD VoxelWin voxel_window(const ViewGeo &G,
                                                  const Dims &D, int ix, int iy,
                                                  int iz) {
   VoxelWin w;
@@ -300,7 +361,9 @@ __device__ __forceinline__ VoxelWin voxel_window(const ViewGeo &G,
   float t = SD / ((xr + G.SO) * G.dy_det);
   const int amax = (int)floorf((yr + 1) * t + na2);
   const int amin = (int)floorf((yr - 1) * t + na2);
-  t = SD / ((xr + G.SO) * G.dz_det);
+  // same expression with dz_det (== dy_det in every gateway call, where the
+  // division need not be repeated)
+  if (G.dz_det != G.dy_det) t = SD / ((xr + G.SO) * G.dz_det);
   const int bmax = (int)floorf((w.zc + d) * t + nb2);
   const int bmin = (int)floorf((w.zc - d) * t + nb2);
   w.a0 = amin > 0 ? amin : 0;
@@ -313,7 +376,7 @@ __device__ __forceinline__ VoxelWin voxel_window(const ViewGeo &G,
 // Sums l*y and l over the voxel's footprint (reference loop order: ib outer,
 // ia inner; Ax_cone_gpu.cu:255-269).
 template <class YLoad>
-__device__ __forceinline__ void voxel_backproject(const ViewGeo &G,
+ASD_HD void voxel_backproject(const ViewGeo &G,
                                                   const Dims &D,
                                                   const VoxelWin &w, YLoad yl,
                                                   float &acc, float &accl) {
@@ -329,6 +392,129 @@ __device__ __forceinline__ void voxel_backproject(const ViewGeo &G,
       accl += l;
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Per-view ray tables for Atx.  The slopes find_l_3d divides out for every
+// (voxel, bin) pair depend on the ray only; they are computed once per ray
+// with the same float operations and reused:
+//   RayA (per detector column ia):  a = x2-x1, b = y2-y1, b/a, a/b
+//   RayC (per ray (ia, ib), 3D):    c/a, c/b, a/c, b/c  with c = z2 - z1
+// ---------------------------------------------------------------------------
+ASD_HD float4 ray_tab_a(const ViewGeo &G, float ydet) {
+  const float x1 = G.cos_phi * (-G.SO), y1 = G.sin_phi * (-G.SO);
+  const float x2 = G.cos_phi * G.OD - G.sin_phi * ydet;
+  const float y2 = G.sin_phi * G.OD + G.cos_phi * ydet;
+  const float a = x2 - x1, b = y2 - y1;
+  return make_float4(a, b, b / a, a / b);
+}
+
+ASD_HD float4 ray_tab_c(const float4 A, float zdet) {
+  const float c = zdet - 0.0f;
+  return make_float4(c / A.x, c / A.y, A.x / c, A.y / c);
+}
+
+// find_l on line direction (a, b) with precomputed b/a, a/b, relative start
+// (rp, rq) = start - box centre, half sizes (hp, hq), full sizes (dp, dq).
+ASD_HD float chord2_rel(float a, float b, float sba,
+                                            float sab, float rp, float rq,
+                                            float hp, float hq, float dp,
+                                            float dq) {
+  if (a == 0) return fabsf(rp) <= hp ? dq : 0.0f;
+  if (b == 0) return fabsf(rq) <= hq ? dp : 0.0f;
+  Hits h;
+  h.n = 0;
+  const bool pfirst = fabsf(a) > fabsf(b);
+#pragma unroll
+  for (int pass = 0; pass < 2; pass++) {
+    if (h.n >= 2) break;
+    if ((pass == 0) == pfirst) {
+      const float t = sba * (-rp) + rq, u = sba * hp;
+      if (fabsf(t - u) <= hq) add_hit(h, -hp, t - u, 0.f);
+      if (fabsf(t + u) <= hq) add_hit(h, hp, t + u, 0.f);
+    } else {
+      const float t = sab * (-rq) + rp, u = sab * hq;
+      if (fabsf(t - u) <= hp) add_hit(h, t - u, -hq, 0.f);
+      if (fabsf(t + u) <= hp) add_hit(h, t + u, hq, 0.f);
+    }
+  }
+  if (h.n < 2) return 0.0f;
+  const float e0 = h.p1x - h.p0x, e1 = h.p1y - h.p0y;
+  return sqrtf(e0 * e0 + e1 * e1);
+}
+
+// find_l_3d from the tables; (rx, ry, rz) = source - voxel centre.
+ASD_HD float chord3_tab(const float4 A, const float4 Cs,
+                                           float c, float rx, float ry,
+                                           float rz, float dz) {
+  const float a = A.x, b = A.y;
+  const float hx = 0.5f, hy = 0.5f, hz = dz / 2.0f;
+  if (a == 0) return chord2_rel(b, c, Cs.y, Cs.w, ry, rz, 0.5f, hz, 1.0f, dz);
+  if (b == 0) return chord2_rel(a, c, Cs.x, Cs.z, rx, rz, 0.5f, hz, 1.0f, dz);
+  const bool xfirst = fabsf(a) > fabsf(b);
+  Hits h;
+  h.n = 0;
+#pragma unroll
+  for (int pass = 0; pass < 3; pass++) {
+    if (h.n >= 2) break;
+    const int axis = pass == 2 ? 2 : (((pass == 0) == xfirst) ? 0 : 1);
+    if (axis == 0) {
+      const float t0 = A.z * (-rx) + ry, u0 = A.z * hx;
+      const float t1 = Cs.x * (-rx) + rz, u1 = Cs.x * hx;
+      if (fabsf(t0 - u0) <= hy && fabsf(t1 - u1) <= hz)
+        add_hit(h, -hx, t0 - u0, t1 - u1);
+      if (fabsf(t0 + u0) <= hy && fabsf(t1 + u1) <= hz)
+        add_hit(h, hx, t0 + u0, t1 + u1);
+    } else if (axis == 1) {
+      const float t0 = A.w * (-ry) + rx, u0 = A.w * hy;
+      const float t1 = Cs.y * (-ry) + rz, u1 = Cs.y * hy;
+      if (fabsf(t0 - u0) <= hx && fabsf(t1 - u1) <= hz)
+        add_hit(h, t0 - u0, -hy, t1 - u1);
+      if (fabsf(t0 + u0) <= hx && fabsf(t1 + u1) <= hz)
+        add_hit(h, t0 + u0, hy, t1 + u1);
+    } else {
+      const float t0 = Cs.z * (-rz) + rx, u0 = Cs.z * hz;
+      const float t1 = Cs.w * (-rz) + ry, u1 = Cs.w * hz;
+      if (fabsf(t0 - u0) <= hx && fabsf(t1 - u1) <= hy)
+        add_hit(h, t0 - u0, t1 - u1, -hz);
+      if (fabsf(t0 + u0) <= hx && fabsf(t1 + u1) <= hy)
+        add_hit(h, t0 + u0, t1 + u1, hz);
+    }
+  }
+  if (h.n < 2) return 0.0f;
+  const float e0 = h.p1x - h.p0x, e1 = h.p1y - h.p0y, e2 = h.p1z - h.p0z;
+  return sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
+}
+
+// find_l_3d for a planar geometry (nz == 1, nb == 1, z_det == 0): c == 0, the
+// z tests of the x/y faces always pass (|rz| == dz/2), the z faces never
+// match (their slopes are infinite) and every hit has z == rz, so the chord
+// is the in-plane one.  Lines with a == 0 or b == 0 fall back to the (y,z) or
+// (x,z) chord, which is the full voxel width (1) in this geometry.
+ASD_HD float chord_planar(const float4 A, float rx,
+                                             float ry, float dz) {
+  const float a = A.x, b = A.y;
+  if (a == 0) return b == 0 ? (fabsf(ry) <= 0.5f ? dz : 0.0f) : 1.0f;
+  if (b == 0) return 1.0f;
+  Hits h;
+  h.n = 0;
+  const bool xfirst = fabsf(a) > fabsf(b);
+#pragma unroll
+  for (int pass = 0; pass < 2; pass++) {
+    if (h.n >= 2) break;
+    if ((pass == 0) == xfirst) {
+      const float t = A.z * (-rx) + ry, u = A.z * 0.5f;
+      if (fabsf(t - u) <= 0.5f) add_hit(h, -0.5f, t - u, 0.f);
+      if (fabsf(t + u) <= 0.5f) add_hit(h, 0.5f, t + u, 0.f);
+    } else {
+      const float t = A.w * (-ry) + rx, u = A.w * 0.5f;
+      if (fabsf(t - u) <= 0.5f) add_hit(h, t - u, -0.5f, 0.f);
+      if (fabsf(t + u) <= 0.5f) add_hit(h, t + u, 0.5f, 0.f);
+    }
+  }
+  if (h.n < 2) return 0.0f;
+  const float e0 = h.p1x - h.p0x, e1 = h.p1y - h.p0y;
+  return sqrtf(e0 * e0 + e1 * e1);
 }
 
 }  // namespace asd

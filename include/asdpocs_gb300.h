@@ -198,6 +198,15 @@ int asdpocs_plan_get_stats(asdpocs_plan plan, int inst, asdpocs_stats *st,
 float *asdpocs_plan_sinogram_ptr(asdpocs_plan plan, int inst);
 float *asdpocs_plan_image_ptr(asdpocs_plan plan, int inst);
 
+/* Profiling hook: average device time (ms, CUDA events on the plan's
+ * stream) of `reps` back-to-back launches of one phase kernel for the whole
+ * batch.  phase: 0 = SART forward step (Ax + residual), 1 = SART backward
+ * step (Atx + update), 2 = one TV step (norm pass + update pass),
+ * 3 = end-of-sweep scalars.  The launches modify the plan's state: call
+ * asdpocs_plan_reset() before the next run. */
+int asdpocs_plan_time_phase(asdpocs_plan plan, int phase, int reps,
+                            double *avg_ms);
+
 /* One-call equivalent of [m_res,out] = ASD_POCS_cuda(P, para): host buffers,
  * FP64 in/out as in MATLAB (P: (na*nb) x nv, column-major; phi_vec in
  * degrees; m0 / I0 may be NULL; rmse may be NULL). */

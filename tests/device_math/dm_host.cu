@@ -1,0 +1,99 @@
+// Host build of the projector device math (csrc/projector.cuh) -- TEST
+// INFRASTRUCTURE.  The same __host__ __device__ functions the kernels call
+// run here on the CPU, so the CPU test suite can check the kernels' float
+// logic bit for bit against the oracle without a GPU:
+//   dm_ax   -- Ax with the columns of a ray split over `lanes` partial sums
+//              combined by the same xor butterfly as the warp reduction;
+//   dm_atx  -- Atx through the staged ray tables (ray_tab_a / ray_tab_c and
+//              chord_planar / chord3_tab), as k_atx runs it.
+// Compiled with -ffp-contract=off so the host compiler fuses nothing.
+#include <string.h>
+
+#include <vector>
+
+#include "../../asd_pocs_mex_cuda_demo_gb300/csrc/projector.cuh"
+
+using namespace asd;
+
+static ViewGeo geo(float c, float s, const float *yd, const float *zd, float SO,
+                   float OD, float scale, float ddy, float ddz, float dz) {
+  ViewGeo g{c, s, SO, OD, scale, ddy, ddz, dz, yd, zd};
+  return g;
+}
+
+extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,
+                      const float *yd, const float *zd, float SO, float OD,
+                      float scale, float dz, int nx, int ny, int nz, int na,
+                      int nb, int lanes) {
+  const ViewGeo G = geo(c, s, yd, zd, SO, OD, scale, 0.f, 0.f, dz);
+  const Dims D{nx, ny, nz, na, nb};
+  std::vector<float> py(lanes), ps(lanes);
+  for (long long r = 0; r < (long long)na * nb; r++) {
+    const int ia = (int)(r % na), ib = (int)(r / na);
+    const RayMarch R = ray_setup(G, D, yd[ia], zd[ib]);
+    const bool planar = nz == 1 && zd[ib] == 0.0f;
+    for (int l = 0; l < lanes; l++) {
+      float a = 0.f, b = 0.f;
+      auto ld = [&](long long i) { return x[i]; };
+      if (planar)
+        ray_columns_planar(R, l, lanes, ld, a, b);
+      else
+        ray_columns(R, l, lanes, ld, a, b);
+      py[l] = a;
+      ps[l] = b;
+    }
+    // xor butterfly (warp_sum): every lane ends with the same total
+    for (int o = lanes / 2; o > 0; o >>= 1) {
+      std::vector<float> ny_(py), ns_(ps);
+      for (int l = 0; l < lanes; l++) {
+        ny_[l] = py[l] + py[l ^ o];
+        ns_[l] = ps[l] + ps[l ^ o];
+      }
+      py.swap(ny_);
+      ps.swap(ns_);
+    }
+    y[r] = py[0] * G.scale;
+    sr[r] = ps[0] * G.scale;
+  }
+}
+
+extern "C" void dm_atx(float *x, const float *yv, float *sc, float c, float s,
+                       const float *yd, const float *zd, float SO, float OD,
+                       float scale, float ddy, float ddz, float dz, int nx,
+                       int ny, int nz, int na, int nb, int staged) {
+  const ViewGeo G = geo(c, s, yd, zd, SO, OD, scale, ddy, ddz, dz);
+  const Dims D{nx, ny, nz, na, nb};
+  const bool planar = nz == 1 && nb == 1 && zd[0] == 0.0f;
+  std::vector<float4> tA(na), tC(planar ? 0 : (size_t)na * nb);
+  for (int ia = 0; ia < na; ia++) tA[ia] = ray_tab_a(G, yd[ia]);
+  if (!planar)
+    for (long long k = 0; k < (long long)na * nb; k++)
+      tC[k] = ray_tab_c(tA[k % na], zd[k / na]);
+  for (int iz = 0; iz < nz; iz++)
+    for (int iy = 0; iy < ny; iy++)
+      for (int ix = 0; ix < nx; ix++) {
+        const VoxelWin w = voxel_window(G, D, ix, iy, iz);
+        float acc = 0.f, accl = 0.f;
+        if (!staged) {
+          voxel_backproject(G, D, w, [&](long long i) { return yv[i]; }, acc,
+                            accl);
+        } else {
+          const float rx = G.cos_phi * (-G.SO) - w.xc;
+          const float ry = G.sin_phi * (-G.SO) - w.yc;
+          const float rz = 0.0f - w.zc;
+          for (int ib = w.b0; ib <= w.b1; ib++) {
+            const float cc = zd[ib] - 0.0f;
+            for (int ia = w.a0; ia <= w.a1; ia++) {
+              const long long k = (long long)ib * na + ia;
+              const float l = planar ? chord_planar(tA[ia], rx, ry, dz)
+                                     : chord3_tab(tA[ia], tC[k], cc, rx, ry, rz, dz);
+              acc += l * yv[k];
+              accl += l;
+            }
+          }
+        }
+        const long long idx = ((long long)iz * ny + iy) * nx + ix;
+        x[idx] = acc * scale;
+        sc[idx] = accl * scale;
+      }
+}

@@ -79,6 +79,12 @@ def asdpocs_fixture():
     para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, na=na, nb=1, detsize=det,
                 phi_vec=phi, maxnumIter=6, alpha=0.2, alpha_red=0.95, I0=x)
     m, out = oracle.asdpocs(P, para, impl="reference")
+    # The reference's TV step (alpha*||m - m0||, ASD_POCS_cuda.m:151-158) is so
+    # large at alpha=0.2 that the iteration is chaotic: a 1e-7 relative change
+    # of P moves m by ~3e-2.  A second run at alpha=0.002 is well conditioned
+    # and pins the reconstruction tightly.
+    paras = dict(para, alpha=0.002)
+    ms, outs = oracle.asdpocs(P, paras, impl="reference")
     # 3D cone-beam, 16^3, 20 views, Poisson noise
     n3, na3, nb3, nv3 = 16, 32, 16, 20
     SO3, OD3, det3 = 1000.0, 500.0, 0.8 * 16
@@ -100,6 +106,9 @@ def asdpocs_fixture():
         P2=P, phi2=phi, geo2=np.array([n, na, SO, OD, vx, det]), x2=x, m2=m,
         out2=np.array([out["IterationNum"], out["dataTolerance"], out["alpha"], out["beta"]]),
         rmse2=out["RMSE"],
+        m2s=ms, rmse2s=outs["RMSE"],
+        out2s=np.array([outs["IterationNum"], outs["dataTolerance"], outs["alpha"],
+                        outs["beta"]]),
         P3=P3, phi3=phi3, geo3=np.array([n3, na3, nb3, SO3, OD3, vx3, det3]), x3=x3, m3=m3,
         out3=np.array([out3["IterationNum"], out3["dataTolerance"], out3["alpha"],
                        out3["beta"]]),
