@@ -47,6 +47,8 @@ struct Scalars {
   double dp;        // ||m - m_pre|| of the last sweep
   double d_tv;      // ||m - m_k1|| at TV entry (imgTVGradMin.cpp:57-60)
   double tv_coef;   // alpha*d/||v|| of the current TV step
+  float tv_coef_f;  // FP32 copies read by the per-voxel kernels
+  float beta_f;
   double dg;        // ||m_TV - m_SART||
   int k;            // 1-based iteration about to run / running
   int done;         // stop criterion met or maxnumIter reached

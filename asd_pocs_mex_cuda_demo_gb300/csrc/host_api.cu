@@ -629,6 +629,7 @@ int asdpocs_plan_reset(asdpocs_plan p) {
     memset(&s, 0, sizeof s);
     s.alpha = o.alpha;
     s.beta = o.beta;
+    s.beta_f = (float)o.beta;
     s.alpha_red = o.alpha_red;
     s.beta_red = o.beta_red;
     s.r_max = o.r_max;

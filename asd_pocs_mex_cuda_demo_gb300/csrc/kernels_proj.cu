@@ -19,7 +19,7 @@ constexpr int kAxThreads = kAxWarps * 32;
 constexpr int kTileX = 32, kTileY = 8;  // Atx voxel tile (x fastest)
 constexpr int kAtxThreads = kTileX * kTileY;
 constexpr int kTabA = 512;              // detector columns staged per block
-constexpr int kTabC = 2048;             // 3D rays staged per block
+constexpr int kTabC = 1536;             // 3D rays staged per block
 
 __device__ __forceinline__ bool tile_voxel(const Dims &D, int &ix, int &iy,
                                            int &iz) {
@@ -51,9 +51,9 @@ __device__ __forceinline__ void ax_warp(const ViewGeo &G, const Dims &D,
   ys = 0.f;
   ss = 0.f;
   if (D.nz == 1 && zd == 0.0f)
-    ray_columns_planar(R, lane, 32, ld, ys, ss);
+    ray_columns_planar<false>(R, lane, 32, ld, ys, ss);
   else
-    ray_columns(R, lane, 32, ld, ys, ss);
+    ray_columns<false>(R, lane, 32, ld, ys, ss);
   ys = warp_sum(ys);
   ss = warp_sum(ss);
 }
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(kAxThreads)
   const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
   if (r >= (long long)D.na * D.nb) return;  // whole warp exits together
   float ys, ss;
-  ax_warp(G, D, r, lane, [&](long long i) { return __ldg(x + i); }, ys, ss);
+  ax_warp(G, D, r, lane, [&](unsigned i) { return __ldg(x + i); }, ys, ss);
   if (lane == 0) {
     y[r] = ys * G.scale;
     sr[r] = ss * G.scale;
@@ -73,22 +73,41 @@ __global__ void __launch_bounds__(kAxThreads)
 }
 
 // ------------------------------------------------------------------- Atx
+// Shared staging of one block: the slopes of every ray its voxels see and the
+// view's values on those rays.
+template <bool kPlanar>
 struct AtxShared {
-  float4 tabA[kTabA];
-  float4 tabC[kTabC];
+  static constexpr int kA = kTabA;
+  static constexpr int kC = kPlanar ? kTabA : kTabC;
+  float4 tabA[kA];
+  float4 tabC[kPlanar ? 1 : kC];
+  float ys[kC];
   int amin, amax, bmin, bmax;
 };
 
-// Footprint sum of one voxel using the block's staged ray tables, or the
-// direct per-pair computation when the block's window does not fit.
-// Must be called by every thread of the block (it synchronises).
-template <class YLoad>
+// Footprint sum of one voxel (Ax_cone_gpu.cu:247-269) for every thread of
+// the block: each block finds the detector window of its voxel tile, stages
+// the window's ray slopes and view values in shared memory, and every lane of
+// a warp then walks the same number of (bin) steps -- the warp's longest
+// footprint -- with the face tests evaluated branch-free, so lanes seeing
+// different rays do not serialise.  Pairs are accumulated in the reference's
+// order (ib outer, ia inner).  A block whose window does not fit the staging
+// arrays (extreme geometry) falls back to the direct per-pair computation.
+// Must be called by every thread of the block.
+template <bool kPlanar, class YLoad>
 __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
                                               bool valid, int ix, int iy,
-                                              int iz, AtxShared &sh, YLoad yl,
-                                              float &acc, float &accl) {
-  const bool planar = D.nz == 1 && D.nb == 1 && G.z_det[0] == 0.0f;
+                                              int iz, AtxShared<kPlanar> &sh,
+                                              YLoad yl, float &acc,
+                                              float &accl) {
+  using Sh = AtxShared<kPlanar>;
+  // planar kernels verify the geometry they were chosen for (z_det == 0)
+  const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
   VoxelWin w;
+  w.a0 = 0;
+  w.a1 = -1;
+  w.b0 = 0;
+  w.b1 = -1;
   if (threadIdx.x == 0) {
     sh.amin = 0x7fffffff;
     sh.amax = -1;
@@ -111,50 +130,66 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   acc = 0.f;
   accl = 0.f;
   if (nA <= 0) return;  // no voxel of the block sees the detector
-  const bool staged = nA <= kTabA && (planar || (long long)nA * nB <= kTabC);
+  const bool staged = planar_ok && nA <= Sh::kA && (long long)nA * nB <= Sh::kC;
   if (staged) {
     for (int k = threadIdx.x; k < nA; k += kAtxThreads)
       sh.tabA[k] = ray_tab_a(G, G.y_det[amin + k]);
+    for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads)
+      sh.ys[k] = yl((long long)(bmin + k / nA) * D.na + amin + k % nA);
     __syncthreads();
-    if (!planar) {
+    if (!kPlanar) {
       for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads)
         sh.tabC[k] = ray_tab_c(sh.tabA[k % nA], G.z_det[bmin + k / nA]);
       __syncthreads();
     }
   }
-  if (!valid) return;
   if (!staged) {
-    voxel_backproject(G, D, w, yl, acc, accl);
+    if (valid) voxel_backproject(G, D, w, yl, acc, accl);
     return;
   }
   const float rx = G.cos_phi * (-G.SO) - w.xc;
   const float ry = G.sin_phi * (-G.SO) - w.yc;
   const float rz = 0.0f - w.zc;
-  for (int ib = w.b0; ib <= w.b1; ib++) {
-    const float c = G.z_det[ib] - 0.0f;
-    const long long row = (long long)ib * D.na;
-    const int trow = (ib - bmin) * nA - amin;
-    for (int ia = w.a0; ia <= w.a1; ia++) {
-      const float4 A = sh.tabA[ia - amin];
-      const float l = planar ? chord_planar(A, rx, ry, G.dz)
-                             : chord3_tab(A, sh.tabC[trow + ia], c, rx, ry, rz, G.dz);
-      acc += l * yl(row + ia);
-      accl += l;
+  const bool has = valid && w.a0 <= w.a1 && w.b0 <= w.b1;
+  const int cntA = has ? w.a1 - w.a0 + 1 : 0;
+  const int cntB = has ? w.b1 - w.b0 + 1 : 0;
+  const int kA = __reduce_max_sync(0xffffffffu, cntA);
+  const int kB = __reduce_max_sync(0xffffffffu, cntB);
+  const int a_off = w.a0 - amin;
+  for (int kb = 0; kb < kB; kb++) {
+    const bool onb = kb < cntB;
+    const int ib = w.b0 + kb;
+    const float c = kPlanar ? 0.0f : G.z_det[onb ? ib : bmin] - 0.0f;
+    const int row = (onb ? ib - bmin : 0) * nA + a_off;
+    for (int ka = 0; ka < kA; ka++) {
+      const bool on = onb && ka < cntA;
+      const int j = on ? row + ka : 0;
+      const float4 A = sh.tabA[on ? a_off + ka : 0];
+      float l;
+      if (kPlanar)
+        l = chord_planar_bf(A, rx, ry, G.dz);
+      else
+        l = chord3_bf(A, sh.tabC[j], c, rx, ry, rz, G.dz);
+      if (on) {
+        acc += l * sh.ys[j];
+        accl += l;
+      }
     }
   }
 }
 
-__global__ void __launch_bounds__(kAtxThreads, 3)
+template <bool kPlanar>
+__global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 3)
     k_atx(float *__restrict__ x, const float *__restrict__ yv,
           float *__restrict__ sc, ViewGeo G, Dims D) {
-  __shared__ AtxShared sh;
+  __shared__ AtxShared<kPlanar> sh;
   int ix, iy, iz;
   const bool valid = tile_voxel(D, ix, iy, iz);
   float acc, accl;
-  atx_block_sum(G, D, valid, ix, iy, iz, sh,
-                [&](long long i) { return __ldg(yv + i); }, acc, accl);
+  atx_block_sum<kPlanar>(G, D, valid, ix, iy, iz, sh,
+                         [&](long long i) { return __ldg(yv + i); }, acc, accl);
   if (!valid) return;
-  const long long idx = ((long long)iz * D.ny + iy) * D.nx + ix;
+  const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
   x[idx] = acc * G.scale;
   sc[idx] = accl * G.scale;
 }
@@ -178,16 +213,16 @@ __global__ void __launch_bounds__(kAxThreads)
   const int lane = threadIdx.x & 31;
   const long long nr = (long long)D.na * D.nb;
   const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
-  double part[1] = {0.0};
+  float part[1] = {0.f};
   if (r < nr) {
     float ys, ss;
     const float *m = I.m;
-    ax_warp(G, D, r, lane, [&](long long i) { return m[i]; }, ys, ss);
+    ax_warp(G, D, r, lane, [&](unsigned i) { return m[i]; }, ys, ss);
     if (lane == 0) {
       const float yv = ys * G.scale, srv = ss * G.scale;
       const float c0 = I.P[(long long)view * nr + r] - yv;
       I.cor[r] = c0 / (srv == 0.f ? 1.f : srv);
-      part[0] = (double)c0 * (double)c0;
+      part[0] = c0 * c0;
     }
   }
   double tot[1];
@@ -198,9 +233,10 @@ __global__ void __launch_bounds__(kAxThreads)
 
 // ASD_POCS_cuda.m:125-131: [bProj,sumC]=Atx(cor); sumC(sumC==0)=1;
 // m = m + beta*(bProj./sumC); m(m<0)=0.
-__global__ void __launch_bounds__(kAtxThreads, 3)
+template <bool kPlanar>
+__global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 3)
     k_sart_atx(const Inst *__restrict__ insts, Dims D, int view) {
-  __shared__ AtxShared sh;
+  __shared__ AtxShared<kPlanar> sh;
   const Inst &I = insts[blockIdx.y];
   if (((volatile int *)&I.s->done)[0]) return;
   const ViewGeo G = view_of(I, view);
@@ -208,12 +244,12 @@ __global__ void __launch_bounds__(kAtxThreads, 3)
   const bool valid = tile_voxel(D, ix, iy, iz);
   float acc, accl;
   const float *cor = I.cor;
-  atx_block_sum(G, D, valid, ix, iy, iz, sh,
-                [&](long long i) { return cor[i]; }, acc, accl);
+  atx_block_sum<kPlanar>(G, D, valid, ix, iy, iz, sh,
+                         [&](long long i) { return cor[i]; }, acc, accl);
   if (!valid) return;
   const float bp = acc * G.scale, scv = accl * G.scale;
-  const float beta = (float)I.s->beta;
-  const long long idx = ((long long)iz * D.ny + iy) * D.nx + ix;
+  const float beta = I.s->beta_f;
+  const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
   const float mn = I.m[idx] + beta * (bp / (scv == 0.f ? 1.f : scv));
   I.m[idx] = mn < 0.f ? 0.f : mn;
 }
@@ -233,7 +269,10 @@ cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
                        const Dims &d, cudaStream_t st) {
   const int blocks = atx_blocks(d);
   if (blocks == 0) return cudaSuccess;
-  k_atx<<<blocks, kAtxThreads, 0, st>>>(x, y, sc, g, d);
+  if (d.nz == 1 && d.nb == 1)
+    k_atx<true><<<blocks, kAtxThreads, 0, st>>>(x, y, sc, g, d);
+  else
+    k_atx<false><<<blocks, kAtxThreads, 0, st>>>(x, y, sc, g, d);
   return cudaGetLastError();
 }
 
@@ -247,8 +286,11 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
                             int view, cudaStream_t st) {
-  k_sart_atx<<<dim3(atx_blocks(d), batch), kAtxThreads, 0, st>>>(insts, d,
-                                                                 view);
+  const dim3 grid(atx_blocks(d), batch);
+  if (d.nz == 1 && d.nb == 1)
+    k_sart_atx<true><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+  else
+    k_sart_atx<false><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
   return cudaGetLastError();
 }
 

@@ -114,37 +114,56 @@ __device__ __forceinline__ T tv_grad(const Img<T> &u, int x, int y, int z) {
 
 // --------------------------------------------------- standalone TV kernels
 // scal[0] = d, scal[1] = ||v||^2 of the current step.
+// Grid sum of one value per thread: FP32 within warps for the FP32 path,
+// FP64 throughout for the FP64 entry points.
+__device__ __forceinline__ bool sum_all(float v, double *partials,
+                                        unsigned *counter, double &tot) {
+  const float vv[1] = {v};
+  double t[1];
+  const bool last = grid_sum<kThreads, 1>(vv, partials, counter, gridDim.x, t);
+  tot = t[0];
+  return last;
+}
+__device__ __forceinline__ bool sum_all(double v, double *partials,
+                                        unsigned *counter, double &tot) {
+  return grid_sum_d<kThreads>(v, partials, counter, gridDim.x, tot);
+}
+
 template <class T>
 __global__ void __launch_bounds__(kThreads)
     k_tv_dist(const T *__restrict__ img, const T *__restrict__ old, int nx,
               int ny, int nz, double *scal, double *partials,
               unsigned *counter) {
   int ix, iy, iz;
-  double v[1] = {0.0};
+  T v = T(0);
   if (tile_voxel(nx, ny, ix, iy, iz)) {
     const long long i = ((long long)iz * ny + iy) * nx + ix;
-    const double d = (double)img[i] - (old ? (double)old[i] : 0.0);
-    v[0] = d * d;
+    const T d = img[i] - (old ? old[i] : T(0));
+    v = d * d;
   }
-  double tot[1];
-  if (grid_sum<kThreads, 1>(v, partials, counter, gridDim.x, tot))
-    if (threadIdx.x == 0) scal[0] = sqrt(tot[0]);
+  double tot;
+  if (sum_all(v, partials, counter, tot))
+    if (threadIdx.x == 0) scal[0] = sqrt(tot);
 }
 
 template <class T>
 __global__ void __launch_bounds__(kThreads)
-    k_tv_norm(const T *__restrict__ src, int nx, int ny, int nz, double *scal,
-              double *partials, unsigned *counter) {
+    k_tv_norm(const T *__restrict__ src, int nx, int ny, int nz, double alpha,
+              double *scal, double *partials, unsigned *counter) {
   int ix, iy, iz;
-  double v[1] = {0.0};
+  T v = T(0);
   const Img<T> u{src, nx, ny, nz};
   if (tile_voxel(nx, ny, ix, iy, iz)) {
     const T g = tv_grad(u, ix, iy, iz);
-    v[0] = (double)g * (double)g;
+    v = g * g;
   }
-  double tot[1];
-  if (grid_sum<kThreads, 1>(v, partials, counter, gridDim.x, tot))
-    if (threadIdx.x == 0) scal[1] = sqrt(tot[0]);
+  double tot;
+  if (sum_all(v, partials, counter, tot))
+    if (threadIdx.x == 0) {
+      scal[1] = sqrt(tot);
+      scal[2] = alpha * scal[0] / scal[1];
+      *(float *)(scal + 3) = (float)scal[2];  // for the FP32 update pass
+    }
 }
 
 // img -= alpha*d*v/norm   (imgTVGradMin.cpp:104-107)
@@ -161,7 +180,7 @@ __global__ void __launch_bounds__(kThreads)
   if (sizeof(T) == 8) {
     r = (T)((double)src[i] - alpha * scal[0] * (double)g / scal[1]);
   } else {
-    const float coef = (float)(alpha * scal[0] / scal[1]);
+    const float coef = *(const float *)(scal + 3);
     r = src[i] - coef * g;
   }
   if (clamp && r < T(0)) r = T(0);
@@ -194,8 +213,8 @@ cudaError_t tv_minimize(T *img, const T *old, T *wa, T *wb, double *scal,
   for (int it = 0; it < n_iter; it++) {
     T *dst = (it == n_iter - 1) ? img : bufs[it & 1];
     if (dst == src) dst = bufs[(it + 1) & 1];
-    k_tv_norm<T><<<blocks, kThreads, 0, st>>>(src, nx, ny, nz, scal, partials,
-                                              counter);
+    k_tv_norm<T><<<blocks, kThreads, 0, st>>>(src, nx, ny, nz, alpha, scal,
+                                              partials, counter);
     const int clamp_now = (it == n_iter - 1) && pos == 1;
     k_tv_update<T><<<blocks, kThreads, 0, st>>>(src, dst, nx, ny, nz, alpha,
                                                 scal, clamp_now);
@@ -220,17 +239,17 @@ __global__ void __launch_bounds__(kThreads)
   const Inst &I = insts[blockIdx.y];
   if (inst_done(I)) return;
   int ix, iy, iz;
-  double v[3] = {0.0, 0.0, 0.0};
+  float v[3] = {0.f, 0.f, 0.f};
   if (tile_voxel(D.nx, D.ny, ix, iy, iz)) {
     const long long i = ((long long)iz * D.ny + iy) * D.nx + ix;
     const float m = I.m[i];
     I.m_res[i] = m;
-    const double a = (double)m - (double)I.m_pre[i];
-    const double b = (double)m - (double)I.m_k1[i];
+    const float a = m - I.m_pre[i];
+    const float b = m - I.m_k1[i];
     v[0] = a * a;
     v[1] = b * b;
     if (I.I0) {
-      const double c = (double)m - (double)I.I0[i];
+      const float c = m - I.I0[i];
       v[2] = c * c;
     }
   }
@@ -266,15 +285,18 @@ __global__ void __launch_bounds__(kThreads)
   const Inst &I = insts[blockIdx.y];
   if (inst_done(I) || step >= I.s->ng) return;
   int ix, iy, iz;
-  double v[1] = {0.0};
+  float v[1] = {0.f};
   const Img<float> u{tv_src(I, step), D.nx, D.ny, D.nz};
   if (tile_voxel(D.nx, D.ny, ix, iy, iz)) {
     const float g = tv_grad(u, ix, iy, iz);
-    v[0] = (double)g * (double)g;
+    v[0] = g * g;
   }
   double tot[1];
   if (grid_sum<kThreads, 1>(v, I.partials, I.counter, gridDim.x, tot))
-    if (threadIdx.x == 0) I.s->tv_coef = I.s->alpha * I.s->d_tv / sqrt(tot[0]);
+    if (threadIdx.x == 0) {
+      I.s->tv_coef = I.s->alpha * I.s->d_tv / sqrt(tot[0]);
+      I.s->tv_coef_f = (float)I.s->tv_coef;
+    }
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -287,7 +309,7 @@ __global__ void __launch_bounds__(kThreads)
   const Img<float> u{src, D.nx, D.ny, D.nz};
   const float g = tv_grad(u, ix, iy, iz);
   const long long i = ((long long)iz * D.ny + iy) * D.nx + ix;
-  const float coef = (float)I.s->tv_coef;
+  const float coef = I.s->tv_coef_f;
   tv_dst(I, step)[i] = src[i] - coef * g;
 }
 
@@ -299,7 +321,7 @@ __global__ void __launch_bounds__(kThreads)
   if (inst_done(I)) return;
   const int ng = I.s->ng;
   int ix, iy, iz;
-  double v[1] = {0.0};
+  float v[1] = {0.f};
   if (tile_voxel(D.nx, D.ny, ix, iy, iz)) {
     const long long i = ((long long)iz * D.ny + iy) * D.nx + ix;
     const float f0 = I.m[i];
@@ -308,7 +330,7 @@ __global__ void __launch_bounds__(kThreads)
       mn = tv_dst(I, ng - 1)[i];
       if (mn < 0.f) mn = 0.f;
     }
-    const double dlt = (double)mn - (double)f0;
+    const float dlt = mn - f0;
     v[0] = dlt * dlt;
     I.m[i] = mn;
     I.m_pre[i] = mn;
@@ -321,6 +343,7 @@ __global__ void __launch_bounds__(kThreads)
       if (s->dg > s->r_max * s->dp && sqrt(s->dd2) > s->epsilon)
         s->alpha = s->alpha * s->alpha_red;
       s->beta = s->beta * s->beta_red;
+      s->beta_f = (float)s->beta;
       if (s->k >= s->maxIter) {
         s->done = 1;
       } else {

@@ -20,6 +20,16 @@
 
 namespace asd {
 
+// a/b through the hardware reciprocal (within 2 ulp) in device code; the
+// IEEE quotient in the host build of this header.
+ASD_HD float fast_div(float a, float b) {
+#ifdef __CUDA_ARCH__
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // Ax: partial sums of one ray over the columns iu = first, first+step, ...
 // (Ax_cone_gpu.cu:339-776).
@@ -38,9 +48,9 @@ namespace asd {
 // ---------------------------------------------------------------------------
 struct RayMarch {
   float us, vs, slope1, slope2, len2, dz2sq, dz;
+  float lfac;  // (len2+dz2sq)/len2: column length factor (fast weights)
   int nu, nv, nz, nu2, nv2, nz2;
-  int su, sv;  // memory strides of u and v
-  long long sz;
+  unsigned su, sv, sz;  // memory strides of u, v and z (volumes < 2^31 voxels)
 };
 
 ASD_HD RayMarch ray_setup(const ViewGeo &G, const Dims &D,
@@ -68,14 +78,22 @@ ASD_HD RayMarch ray_setup(const ViewGeo &G, const Dims &D,
   R.nu2 = R.nu / 2;
   R.nv2 = R.nv / 2;
   R.nz2 = D.nz / 2;
-  R.su = xdrive ? 1 : D.nx;
-  R.sv = xdrive ? D.nx : 1;
-  R.sz = (long long)D.nx * D.ny;
+  R.su = xdrive ? 1u : (unsigned)D.nx;
+  R.sv = xdrive ? (unsigned)D.nx : 1u;
+  R.sz = (unsigned)D.nx * (unsigned)D.ny;
+  R.lfac = (R.len2 + R.dz2sq) / R.len2;
   return R;
 }
 
 // Adds the contributions of columns first, first+step, ... to (ys, ss).
-template <class Loader>
+// kExact = true evaluates every weight with the reference's expressions
+// (bit-identical per column).  kExact = false (the kernels) keeps every
+// branch decision identical -- cell indices and split tests use the same
+// float expressions -- but forms the weights without IEEE divisions: the
+// column length as sqrt((d*d+1)*lfac) (lfac = (len2+dz2sq)/len2 per ray) and
+// the split fractions with the hardware reciprocal, each within 2 ulp of the
+// reference's value.
+template <bool kExact = true, class Loader>
 ASD_HD void ray_columns(const RayMarch &R, int first,
                                             int step, Loader ld, float &ys,
                                             float &ss) {
@@ -91,12 +109,12 @@ ASD_HD void ray_columns(const RayMarch &R, int first,
       v2 = R.vs + R.slope1 * (uu1 - R.us) + R.nv2;
     }
     const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
-    if (R.slope2 >= 0) {
-      w1 = (0.0f + R.slope2 * (uu1 - R.us)) / R.dz + R.nz2;
-      w2 = (0.0f + R.slope2 * (uu2 - R.us)) / R.dz + R.nz2;
-    } else {
-      w1 = (0.0f + R.slope2 * (uu2 - R.us)) / R.dz + R.nz2;
-      w2 = (0.0f + R.slope2 * (uu1 - R.us)) / R.dz + R.nz2;
+    {
+      const float q1 = 0.0f + R.slope2 * ((R.slope2 >= 0 ? uu1 : uu2) - R.us);
+      const float q2 = 0.0f + R.slope2 * ((R.slope2 >= 0 ? uu2 : uu1) - R.us);
+      // q/dz: with dz == 1 (every gateway call) the division is the identity
+      w1 = (kExact || R.dz != 1.0f ? q1 / R.dz : q1) + R.nz2;
+      w2 = (kExact || R.dz != 1.0f ? q2 / R.dz : q2) + R.nz2;
     }
     const int cz1 = (int)floorf(w1), cz2 = (int)floorf(w2);
     const bool vsplit = cv1 != cv2, zsplit = cz1 != cz2;
@@ -126,11 +144,12 @@ ASD_HD void ray_columns(const RayMarch &R, int first,
     if (!(vlo || vhi) || !(zlo || zhi)) continue;
 
     const float d = v2 - v1;
-    const float l = sqrtf((d * d + 1) * (R.len2 + R.dz2sq) / R.len2);
-    const long long base = (long long)iu * R.su;
-    const long long ilo = base + (long long)cv1 * R.sv;
-    const long long ihi = base + (long long)cv2 * R.sv;
-    const long long zl = (long long)cz1 * R.sz, zh = (long long)cz2 * R.sz;
+    const float l = kExact ? sqrtf((d * d + 1) * (R.len2 + R.dz2sq) / R.len2)
+                           : sqrtf((d * d + 1) * R.lfac);
+    const unsigned base = (unsigned)iu * R.su;
+    const unsigned ilo = base + (unsigned)cv1 * R.sv;
+    const unsigned ihi = base + (unsigned)cv2 * R.sv;
+    const unsigned zl = (unsigned)cz1 * R.sz, zh = (unsigned)cz2 * R.sz;
 #define ASD_PIECE(w, idx)   \
   do {                      \
     const float w_ = (w);   \
@@ -140,16 +159,16 @@ ASD_HD void ray_columns(const RayMarch &R, int first,
     if (!vsplit && !zsplit) {
       ASD_PIECE(l, ilo + zl);
     } else if (!vsplit) {
-      const float rz = (cz2 - w1) / (w2 - w1);
+      const float rz = kExact ? (cz2 - w1) / (w2 - w1) : fast_div(cz2 - w1, w2 - w1);
       if (zlo) ASD_PIECE(rz * l, ilo + zl);
       if (zhi) ASD_PIECE((1 - rz) * l, ilo + zh);
     } else if (!zsplit) {
-      const float rv = (cv2 - v1) / d;
+      const float rv = kExact ? (cv2 - v1) / d : fast_div(cv2 - v1, d);
       if (vlo) ASD_PIECE(rv * l, ilo + zl);
       if (vhi) ASD_PIECE((1 - rv) * l, ihi + zl);
     } else {
-      const float rv = (cv2 - v1) / d;
-      const float rz = (cz2 - w1) / (w2 - w1);
+      const float rv = kExact ? (cv2 - v1) / d : fast_div(cv2 - v1, d);
+      const float rz = kExact ? (cz2 - w1) / (w2 - w1) : fast_div(cz2 - w1, w2 - w1);
       if (rv > rz) {
         if (vlo && zlo) ASD_PIECE(rz * l, ilo + zl);
         if (vlo && zhi) ASD_PIECE((rv - rz) * l, ilo + zh);
@@ -168,7 +187,7 @@ ASD_HD void ray_columns(const RayMarch &R, int first,
 // z_det == 0): slope2 is +-0, so every column has w1 = w2 = 0, slice 0 and
 // len2 + dz2sq == len2; the z tests are dropped.  Bit-identical to the
 // generic march for these rays.
-template <class Loader>
+template <bool kExact = true, class Loader>
 ASD_HD void ray_columns_planar(const RayMarch &R, int first,
                                                    int step, Loader ld,
                                                    float &ys, float &ss) {
@@ -184,13 +203,14 @@ ASD_HD void ray_columns_planar(const RayMarch &R, int first,
       v2 = R.vs + R.slope1 * (uu1 - R.us) + R.nv2;
     }
     const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
-    const long long base = (long long)iu * R.su;
+    const unsigned base = (unsigned)iu * R.su;
     const float d = v2 - v1;
     if (cv1 == cv2) {
       if (cv1 < 0 || cv1 > R.nv - 1) continue;
-      const float l = sqrtf((d * d + 1) * R.len2 / R.len2);
+      const float l = kExact ? sqrtf((d * d + 1) * R.len2 / R.len2)
+                             : sqrtf(d * d + 1);
       const float w = l;
-      ys += w * ld(base + (long long)cv1 * R.sv);
+      ys += w * ld(base + (unsigned)cv1 * R.sv);
       ss += w;
     } else {
       bool vlo, vhi;
@@ -203,16 +223,17 @@ ASD_HD void ray_columns_planar(const RayMarch &R, int first,
       vlo = vlo && cv1 >= 0 && cv1 < R.nv;
       vhi = vhi && cv2 >= 0 && cv2 < R.nv;
       if (!(vlo || vhi)) continue;
-      const float l = sqrtf((d * d + 1) * R.len2 / R.len2);
-      const float rv = (cv2 - v1) / d;
+      const float l = kExact ? sqrtf((d * d + 1) * R.len2 / R.len2)
+                             : sqrtf(d * d + 1);
+      const float rv = kExact ? (cv2 - v1) / d : fast_div(cv2 - v1, d);
       if (vlo) {
         const float w = rv * l;
-        ys += w * ld(base + (long long)cv1 * R.sv);
+        ys += w * ld(base + (unsigned)cv1 * R.sv);
         ss += w;
       }
       if (vhi) {
         const float w = (1 - rv) * l;
-        ys += w * ld(base + (long long)cv2 * R.sv);
+        ys += w * ld(base + (unsigned)cv2 * R.sv);
         ss += w;
       }
     }
@@ -515,6 +536,104 @@ ASD_HD float chord_planar(const float4 A, float rx,
   if (h.n < 2) return 0.0f;
   const float e0 = h.p1x - h.p0x, e1 = h.p1y - h.p0y;
   return sqrtf(e0 * e0 + e1 * e1);
+}
+
+// ---------------------------------------------------------------------------
+// Branch-free forms for the kernels.  The reference tests the faces in a
+// fixed order and keeps the first two points that pass; evaluating every
+// candidate (the tests have no side effects) and selecting the first two
+// valid ones in that order gives the same chord, without the divergent
+// early exits that serialise a warp whose lanes see different rays.
+// ---------------------------------------------------------------------------
+struct Pick2 {
+  int n;
+  float p0x, p0y, p0z, p1x, p1y, p1z;
+  ASD_HD void take(bool f, float x, float y, float z) {
+    if (f) {
+      if (n == 0) {
+        p0x = x;
+        p0y = y;
+        p0z = z;
+      } else if (n == 1) {
+        p1x = x;
+        p1y = y;
+        p1z = z;
+      }
+      n++;
+    }
+  }
+};
+
+// chord_planar without divergent control flow (same result).
+ASD_HD float chord_planar_bf(const float4 A, float rx, float ry, float dz) {
+  const float a = A.x, b = A.y;
+  const float tX = A.z * (-rx) + ry, uX = A.z * 0.5f;
+  const float tY = A.w * (-ry) + rx, uY = A.w * 0.5f;
+  const float xm = tX - uX, xp = tX + uX, ym = tY - uY, yp = tY + uY;
+  const bool fxm = fabsf(xm) <= 0.5f, fxp = fabsf(xp) <= 0.5f;
+  const bool fym = fabsf(ym) <= 0.5f, fyp = fabsf(yp) <= 0.5f;
+  const bool xfirst = fabsf(a) > fabsf(b);
+  Pick2 p;
+  p.n = 0;
+  p.p0x = p.p0y = p.p1x = p.p1y = p.p0z = p.p1z = 0.f;
+  // first axis pair, then the other
+  p.take(xfirst ? fxm : fym, xfirst ? -0.5f : ym, xfirst ? xm : -0.5f, 0.f);
+  p.take(xfirst ? fxp : fyp, xfirst ? 0.5f : yp, xfirst ? xp : 0.5f, 0.f);
+  p.take(xfirst ? fym : fxm, xfirst ? ym : -0.5f, xfirst ? -0.5f : xm, 0.f);
+  p.take(xfirst ? fyp : fxp, xfirst ? yp : 0.5f, xfirst ? 0.5f : xp, 0.f);
+  const float e0 = p.p1x - p.p0x, e1 = p.p1y - p.p0y;
+  const float l = p.n >= 2 ? sqrtf(e0 * e0 + e1 * e1) : 0.0f;
+  if (a == 0) return b == 0 ? (fabsf(ry) <= 0.5f ? dz : 0.0f) : 1.0f;
+  if (b == 0) return 1.0f;
+  return l;
+}
+
+// chord3_tab without divergent control flow in the common case (the a == 0
+// or b == 0 fallbacks keep their branch; they need an axis-aligned ray).
+ASD_HD float chord3_bf(const float4 A, const float4 Cs, float c, float rx,
+                       float ry, float rz, float dz) {
+  const float a = A.x, b = A.y;
+  const float hz = dz / 2.0f;
+  if (a == 0) return chord2_rel(b, c, Cs.y, Cs.w, ry, rz, 0.5f, hz, 1.0f, dz);
+  if (b == 0) return chord2_rel(a, c, Cs.x, Cs.z, rx, rz, 0.5f, hz, 1.0f, dz);
+  // x faces
+  const float xt0 = A.z * (-rx) + ry, xu0 = A.z * 0.5f;
+  const float xt1 = Cs.x * (-rx) + rz, xu1 = Cs.x * 0.5f;
+  const float xmy = xt0 - xu0, xmz = xt1 - xu1, xpy = xt0 + xu0, xpz = xt1 + xu1;
+  const bool fxm = fabsf(xmy) <= 0.5f && fabsf(xmz) <= hz;
+  const bool fxp = fabsf(xpy) <= 0.5f && fabsf(xpz) <= hz;
+  // y faces
+  const float yt0 = A.w * (-ry) + rx, yu0 = A.w * 0.5f;
+  const float yt1 = Cs.y * (-ry) + rz, yu1 = Cs.y * 0.5f;
+  const float ymx = yt0 - yu0, ymz = yt1 - yu1, ypx = yt0 + yu0, ypz = yt1 + yu1;
+  const bool fym = fabsf(ymx) <= 0.5f && fabsf(ymz) <= hz;
+  const bool fyp = fabsf(ypx) <= 0.5f && fabsf(ypz) <= hz;
+  // z faces
+  const float zt0 = Cs.z * (-rz) + rx, zu0 = Cs.z * hz;
+  const float zt1 = Cs.w * (-rz) + ry, zu1 = Cs.w * hz;
+  const float zmx = zt0 - zu0, zmy = zt1 - zu1, zpx = zt0 + zu0, zpy = zt1 + zu1;
+  const bool fzm = fabsf(zmx) <= 0.5f && fabsf(zmy) <= 0.5f;
+  const bool fzp = fabsf(zpx) <= 0.5f && fabsf(zpy) <= 0.5f;
+  const bool xfirst = fabsf(a) > fabsf(b);
+  Pick2 p;
+  p.n = 0;
+  p.p0x = p.p0y = p.p0z = p.p1x = p.p1y = p.p1z = 0.f;
+  if (xfirst) {
+    p.take(fxm, -0.5f, xmy, xmz);
+    p.take(fxp, 0.5f, xpy, xpz);
+    p.take(fym, ymx, -0.5f, ymz);
+    p.take(fyp, ypx, 0.5f, ypz);
+  } else {
+    p.take(fym, ymx, -0.5f, ymz);
+    p.take(fyp, ypx, 0.5f, ypz);
+    p.take(fxm, -0.5f, xmy, xmz);
+    p.take(fxp, 0.5f, xpy, xpz);
+  }
+  p.take(fzm, zmx, zmy, -hz);
+  p.take(fzp, zpx, zpy, hz);
+  if (p.n < 2) return 0.0f;
+  const float e0 = p.p1x - p.p0x, e1 = p.p1y - p.p0y, e2 = p.p1z - p.p0z;
+  return sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
 }
 
 }  // namespace asd

@@ -1,28 +1,31 @@
-// Deterministic grid reductions in FP64 (internal).
+// Deterministic grid reductions (internal).
 //
-// Each block reduces its values in a fixed tree order and stores the block
-// partial; the last block to finish (atomic ticket) sums the partials in
-// block order.  The result is bit-identical from run to run and independent
-// of block scheduling, so a reconstruction gives the same scalars alone and
-// inside a batch.  The ticket is reset by the last block, which makes the
+// GB300 executes FP64 at a small fraction of its FP32 rate, so per-element
+// work stays in FP32: each warp sums its 32 values with an FP32 xor
+// butterfly (relative error <= 5 roundings, ~3e-7), and only the per-warp
+// totals are accumulated in FP64 -- across the warps of a block, then across
+// blocks.  The block partials are summed by the last block to finish (atomic
+// ticket) in block order, so the result is bit-identical from run to run and
+// independent of scheduling; a reconstruction gives the same scalars alone
+// and inside a batch.  The ticket is reset by the last block, which keeps the
 // kernels replayable inside a CUDA graph.
 #pragma once
 #include "common.cuh"
 
 namespace asd {
 
+// Block totals in FP64 (valid in warp 0 after the call); sh holds
+// K * (NT/32) doubles.  Every thread of the block must call it.
 template <int NT, int K>
-__device__ __forceinline__ void block_sum(double (&v)[K], double *sh) {
-  // sh: K * (NT/32) doubles of shared memory
+__device__ __forceinline__ void block_sum_f(const float (&v)[K], double (&out)[K],
+                                            double *sh) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; k++) {
+    float s = v[k];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int k = 0; k < K; k++) sh[k * (NT / 32) + warp] = v[k];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sh[k * (NT / 32) + warp] = (double)s;
   }
   __syncthreads();
   if (warp == 0) {
@@ -30,8 +33,8 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *sh) {
     for (int k = 0; k < K; k++) {
       double t = lane < NT / 32 ? sh[k * (NT / 32) + lane] : 0.0;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      v[k] = t;
+      for (int o = NT / 64; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      out[k] = t;
     }
   }
   __syncthreads();
@@ -39,18 +42,20 @@ __device__ __forceinline__ void block_sum(double (&v)[K], double *sh) {
 
 // Grid-wide deterministic sum of K values per thread over the blocks
 // blockIdx.x = 0..nblocks-1 (blockIdx.y selects an independent reduction
-// through `partials`/`counter`).  `partials` holds nblocks*K doubles.  Returns true in every thread of the last
-// block, where `tot` then holds the totals; other blocks return false.
+// through `partials`/`counter`).  `partials` holds nblocks*K doubles.
+// Returns true in every thread of the last block, where `tot` then holds the
+// totals; other blocks return false.
 template <int NT, int K>
-__device__ __forceinline__ bool grid_sum(double (&v)[K], double *partials,
+__device__ __forceinline__ bool grid_sum(const float (&v)[K], double *partials,
                                          unsigned *counter, int nblocks,
                                          double (&tot)[K]) {
   __shared__ double sh[K * (NT / 32)];
   __shared__ bool last;
-  block_sum<NT, K>(v, sh);
+  double bs[K];
+  block_sum_f<NT, K>(v, bs, sh);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < K; k++) partials[(long long)blockIdx.x * K + k] = v[k];
+    for (int k = 0; k < K; k++) partials[(long long)blockIdx.x * K + k] = bs[k];
     __threadfence();
     const unsigned t = atomicAdd(counter, 1u);
     last = (t == (unsigned)nblocks - 1);
@@ -58,23 +63,77 @@ __device__ __forceinline__ bool grid_sum(double (&v)[K], double *partials,
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  double acc[K];
+  // FP64 over the block partials (nblocks per reduction; few per thread)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; k++) {
-    acc[k] = 0.0;
+    double a = 0.0;
     for (int b = threadIdx.x; b < nblocks; b += NT)
-      acc[k] += ((volatile double *)partials)[(long long)b * K + k];
+      a += ((volatile double *)partials)[(long long)b * K + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) sh[k * (NT / 32) + warp] = a;
   }
-  block_sum<NT, K>(acc, sh);  // totals land in warp 0
+  __syncthreads();
   __shared__ double bc[K];
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < K; k++) bc[k] = acc[k];
+    for (int k = 0; k < K; k++) {
+      double a = 0.0;
+      for (int w = 0; w < NT / 32; w++) a += sh[k * (NT / 32) + w];
+      bc[k] = a;
+    }
     *counter = 0u;
   }
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < K; k++) tot[k] = bc[k];
+  return true;
+}
+
+}  // namespace asd
+
+namespace asd {
+
+// FP64 variant for the FP64 entry points (the mex-level TV): every level of
+// the reduction in FP64, same deterministic last-block scheme.
+template <int NT>
+__device__ __forceinline__ bool grid_sum_d(double v, double *partials,
+                                           unsigned *counter, int nblocks,
+                                           double &tot) {
+  __shared__ double sh[NT / 32];
+  __shared__ bool last;
+  __shared__ double bc;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < NT / 32; w++) s += sh[w];
+    partials[blockIdx.x] = s;
+    __threadfence();
+    last = atomicAdd(counter, 1u) == (unsigned)nblocks - 1;
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double a = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += NT) a += ((volatile double *)partials)[b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  __syncthreads();
+  if (lane == 0) sh[warp] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < NT / 32; w++) s += sh[w];
+    bc = s;
+    *counter = 0u;
+  }
+  __syncthreads();
+  tot = bc;
   return true;
 }
 

@@ -3,9 +3,12 @@
 // run here on the CPU, so the CPU test suite can check the kernels' float
 // logic bit for bit against the oracle without a GPU:
 //   dm_ax   -- Ax with the columns of a ray split over `lanes` partial sums
-//              combined by the same xor butterfly as the warp reduction;
-//   dm_atx  -- Atx through the staged ray tables (ray_tab_a / ray_tab_c and
-//              chord_planar / chord3_tab), as k_atx runs it.
+//              combined by the same xor butterfly as the warp reduction,
+//              with the reference's weight expressions (exact=1) or the
+//              kernels' division-free ones (exact=0);
+//   dm_atx  -- Atx through the staged ray tables and the branch-free chords
+//              (ray_tab_a / ray_tab_c, chord_planar_bf / chord3_bf) as the
+//              kernels run it (staged=1), or the direct per-pair form.
 // Compiled with -ffp-contract=off so the host compiler fuses nothing.
 #include <string.h>
 
@@ -24,7 +27,7 @@ static ViewGeo geo(float c, float s, const float *yd, const float *zd, float SO,
 extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,
                       const float *yd, const float *zd, float SO, float OD,
                       float scale, float dz, int nx, int ny, int nz, int na,
-                      int nb, int lanes) {
+                      int nb, int lanes, int exact) {
   const ViewGeo G = geo(c, s, yd, zd, SO, OD, scale, 0.f, 0.f, dz);
   const Dims D{nx, ny, nz, na, nb};
   std::vector<float> py(lanes), ps(lanes);
@@ -35,10 +38,14 @@ extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,
     for (int l = 0; l < lanes; l++) {
       float a = 0.f, b = 0.f;
       auto ld = [&](long long i) { return x[i]; };
-      if (planar)
-        ray_columns_planar(R, l, lanes, ld, a, b);
+      if (planar && exact)
+        ray_columns_planar<true>(R, l, lanes, ld, a, b);
+      else if (planar)
+        ray_columns_planar<false>(R, l, lanes, ld, a, b);
+      else if (exact)
+        ray_columns<true>(R, l, lanes, ld, a, b);
       else
-        ray_columns(R, l, lanes, ld, a, b);
+        ray_columns<false>(R, l, lanes, ld, a, b);
       py[l] = a;
       ps[l] = b;
     }
@@ -85,8 +92,8 @@ extern "C" void dm_atx(float *x, const float *yv, float *sc, float c, float s,
             const float cc = zd[ib] - 0.0f;
             for (int ia = w.a0; ia <= w.a1; ia++) {
               const long long k = (long long)ib * na + ia;
-              const float l = planar ? chord_planar(tA[ia], rx, ry, dz)
-                                     : chord3_tab(tA[ia], tC[k], cc, rx, ry, rz, dz);
+              const float l = planar ? chord_planar_bf(tA[ia], rx, ry, dz)
+                                     : chord3_bf(tA[ia], tC[k], cc, rx, ry, rz, dz);
               acc += l * yv[k];
               accl += l;
             }
