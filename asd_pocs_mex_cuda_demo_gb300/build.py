@@ -22,8 +22,10 @@ LIB = os.path.join(LIBDIR, "libasdpocs_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE,
-          "--expt-relaxed-constexpr"]
+# host code (gateway geometry, per-view constants) must round every float
+# operation as written on both x86 and Arm hosts: no contraction into FMA
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
+          "-I", INCLUDE, "--expt-relaxed-constexpr"]
 # per-unit extra flags
 UNITS = {
     "kernels_proj.cu": ["-fmad=false"],

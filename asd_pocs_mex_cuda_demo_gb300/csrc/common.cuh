@@ -33,7 +33,18 @@ struct ViewGeo {
   float dy_det, dz_det, dz;
   const float *y_det;  // device, na
   const float *z_det;  // device, nb
+  // per-view constants of the backprojector footprint, with_constants()
+  float SD;    // SO + OD
+  float dwin;  // sqrtf((1 + dz*dz)/2), the footprint half-height
 };
+
+// Fills the derived constants with the reference's float expressions
+// (Ax_cone_gpu.cu:230,233).
+__host__ __device__ inline ViewGeo with_constants(ViewGeo g) {
+  g.SD = g.SO + g.OD;
+  g.dwin = sqrtf((1 + g.dz * g.dz) / 2);
+  return g;
+}
 
 // ---------------------------------------------------------------------------
 // Per-instance state of a batched ASD-POCS plan (device resident)

@@ -135,7 +135,8 @@ int asdpocs_ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
   if (int e = check_dims(nx, ny, nz, na, nb)) return e;
   if (!x_d || !y_d || !sr_d || !y_det_d || !z_det_d)
     return set_error(ASDPOCS_ERR_ARG, "null pointer");
-  ViewGeo g{cos_phi, sin_phi, SO, OD, scale, 0.f, 0.f, dz, y_det_d, z_det_d};
+  const ViewGeo g = with_constants(
+      ViewGeo{cos_phi, sin_phi, SO, OD, scale, 0.f, 0.f, dz, y_det_d, z_det_d});
   Dims d{nx, ny, nz, na, nb};
   ASD_CUDA(launch_ax(x_d, y_d, sr_d, g, d, (cudaStream_t)stream));
   return 0;
@@ -150,8 +151,8 @@ int asdpocs_atx_device(float *x_d, const float *y_d, float *sc_d,
   if (int e = check_dims(nx, ny, nz, na, nb)) return e;
   if (!x_d || !y_d || !sc_d || !y_det_d || !z_det_d)
     return set_error(ASDPOCS_ERR_ARG, "null pointer");
-  ViewGeo g{cos_phi, sin_phi, SO, OD, scale, dy_det, dz_det, dz, y_det_d,
-            z_det_d};
+  const ViewGeo g = with_constants(ViewGeo{cos_phi, sin_phi, SO, OD, scale,
+                                           dy_det, dz_det, dz, y_det_d, z_det_d});
   Dims d{nx, ny, nz, na, nb};
   ASD_CUDA(launch_atx(x_d, y_d, sc_d, g, d, (cudaStream_t)stream));
   return 0;
@@ -176,8 +177,9 @@ static int ax_host(const float *X, float *y, float *sr, float cos_phi,
   ASD_CUDA(cudaMemcpyAsync(b + oX, X, N * 4, cudaMemcpyHostToDevice, w->st));
   ASD_CUDA(cudaMemcpyAsync(b + oA, y_det, (size_t)na * 4, cudaMemcpyHostToDevice, w->st));
   ASD_CUDA(cudaMemcpyAsync(b + oB, z_det, (size_t)nb * 4, cudaMemcpyHostToDevice, w->st));
-  ViewGeo g{cos_phi, sin_phi, SO, OD, scale, 0.f, 0.f, dz, (const float *)(b + oA),
-            (const float *)(b + oB)};
+  const ViewGeo g = with_constants(ViewGeo{cos_phi, sin_phi, SO, OD, scale, 0.f,
+                                           0.f, dz, (const float *)(b + oA),
+                                           (const float *)(b + oB)});
   Dims d{nx, ny, nz, na, nb};
   ASD_CUDA(launch_ax((const float *)(b + oX), (float *)(b + oY), (float *)(b + oS), g, d, w->st));
   ASD_CUDA(cudaMemcpyAsync(y, b + oY, M * 4, cudaMemcpyDeviceToHost, w->st));
@@ -205,8 +207,9 @@ static int atx_host(float *X, const float *yv, float *sc, float cos_phi,
   ASD_CUDA(cudaMemcpyAsync(b + oY, yv, M * 4, cudaMemcpyHostToDevice, w->st));
   ASD_CUDA(cudaMemcpyAsync(b + oA, y_det, (size_t)na * 4, cudaMemcpyHostToDevice, w->st));
   ASD_CUDA(cudaMemcpyAsync(b + oB, z_det, (size_t)nb * 4, cudaMemcpyHostToDevice, w->st));
-  ViewGeo g{cos_phi, sin_phi, SO, OD, scale, dy_det, dz_det, dz,
-            (const float *)(b + oA), (const float *)(b + oB)};
+  const ViewGeo g = with_constants(ViewGeo{cos_phi, sin_phi, SO, OD, scale,
+                                           dy_det, dz_det, dz, (const float *)(b + oA),
+                                           (const float *)(b + oB)});
   Dims d{nx, ny, nz, na, nb};
   ASD_CUDA(launch_atx((float *)(b + oX), (const float *)(b + oY), (float *)(b + oS), g, d, w->st));
   ASD_CUDA(cudaMemcpyAsync(X, b + oX, N * 4, cudaMemcpyDeviceToHost, w->st));
@@ -515,8 +518,9 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     GatewayGeo gg;
     gateway_geometry(0.0, geom[i].SO, geom[i].OD, geom[i].vxlsize,
                      geom[i].detsize, g0.na, g0.nb, gg);
-    I.g = ViewGeo{0.f, 0.f, gg.SO, gg.OD, gg.scale, gg.det, gg.det, 1.0f,
-                  (const float *)(b + o.ydet), (const float *)(b + o.zdet)};
+    I.g = with_constants(ViewGeo{0.f, 0.f, gg.SO, gg.OD, gg.scale, gg.det, gg.det,
+                                 1.0f, (const float *)(b + o.ydet),
+                                 (const float *)(b + o.zdet)});
     for (int v = 0; v < p->nv; v++)
       trig[v] = view_trig(phi_vec_deg[(size_t)i * p->nv + v]);
     I.trig = (const float2 *)(b + o.trig);

@@ -85,14 +85,50 @@ struct AtxShared {
   int amin, amax, bmin, bmax;
 };
 
+// Detector bins whose rays can reach a pixel (planar geometry): the bins with
+// centres inside the shadow of the pixel's four corners, widened by 0.05 bin.
+// Rays of the other bins miss the pixel by more than 0.03 pixel widths at
+// the pixel, far beyond the ~1e-4 rounding of the reference's face tests, so
+// their chords are exactly 0 there too.  Returns false (no narrowing) when a
+// corner is not in front of the source.
+__device__ __forceinline__ bool shadow_bins(const ViewGeo &G, const Dims &D,
+                                            float xc, float yc, int &lo,
+                                            int &hi) {
+  const float xr = G.cos_phi * xc + G.sin_phi * yc;
+  const float yr = -G.sin_phi * xc + G.cos_phi * yc;
+  const float hc = 0.5f * G.cos_phi, hs = 0.5f * G.sin_phi;
+  const float inv_det = __frcp_rn(G.dy_det);
+  const float off = D.na * 0.5f - 0.5f;
+  float fmin = 3.0e38f, fmax = -3.0e38f;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float ex = (k & 1) ? 1.f : -1.f, ey = (k & 2) ? 1.f : -1.f;
+    const float px = xr + ex * hc + ey * hs;  // rotated corner
+    const float py = yr - ex * hs + ey * hc;
+    const float den = px + G.SO;
+    ok = ok && den > 1e-3f;
+    const float f = __fdividef(py * G.SD, den) * inv_det + off;
+    fmin = fminf(fmin, f);
+    fmax = fmaxf(fmax, f);
+  }
+  lo = (int)ceilf(fmin - 0.05f);
+  hi = (int)floorf(fmax + 0.05f);
+  return ok;
+}
+
 // Footprint sum of one voxel (Ax_cone_gpu.cu:247-269) for every thread of
 // the block: each block finds the detector window of its voxel tile, stages
 // the window's ray slopes and view values in shared memory, and every lane of
 // a warp then walks the same number of (bin) steps -- the warp's longest
 // footprint -- with the face tests evaluated branch-free, so lanes seeing
-// different rays do not serialise.  Pairs are accumulated in the reference's
-// order (ib outer, ia inner).  A block whose window does not fit the staging
-// arrays (extreme geometry) falls back to the direct per-pair computation.
+// different rays do not serialise.  In the planar geometry each lane walks
+// only the bins of its pixel's shadow (inside the reference's window); the
+// bins it skips have chords of exactly 0, which add nothing unless a view
+// value is not finite, so a block whose window holds NaN/inf walks the whole
+// window.  Pairs are accumulated in the reference's order (ib outer, ia
+// inner).  A block whose window does not fit the staging arrays (extreme
+// geometry) falls back to the direct per-pair computation.
 // Must be called by every thread of the block.
 template <bool kPlanar, class YLoad>
 __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
@@ -115,13 +151,23 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
     sh.bmax = -1;
   }
   __syncthreads();
+  bool has = false;
   if (valid) {
     w = voxel_window(G, D, ix, iy, iz);
-    if (w.a0 <= w.a1 && w.b0 <= w.b1) {
-      atomicMin(&sh.amin, w.a0);
-      atomicMax(&sh.amax, w.a1);
-      atomicMin(&sh.bmin, w.b0);
-      atomicMax(&sh.bmax, w.b1);
+    has = w.a0 <= w.a1 && w.b0 <= w.b1;
+  }
+  {
+    // block window: warp-reduced, then one shared atomic per warp
+    const int big = 0x7fffffff;
+    const int a0 = __reduce_min_sync(0xffffffffu, has ? w.a0 : big);
+    const int a1 = __reduce_max_sync(0xffffffffu, has ? w.a1 : -1);
+    const int b0 = __reduce_min_sync(0xffffffffu, has ? w.b0 : big);
+    const int b1 = __reduce_max_sync(0xffffffffu, has ? w.b1 : -1);
+    if ((threadIdx.x & 31) == 0 && a1 >= 0) {
+      atomicMin(&sh.amin, a0);
+      atomicMax(&sh.amax, a1);
+      atomicMin(&sh.bmin, b0);
+      atomicMax(&sh.bmax, b1);
     }
   }
   __syncthreads();
@@ -131,12 +177,16 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   accl = 0.f;
   if (nA <= 0) return;  // no voxel of the block sees the detector
   const bool staged = planar_ok && nA <= Sh::kA && (long long)nA * nB <= Sh::kC;
+  bool finite = true;
   if (staged) {
     for (int k = threadIdx.x; k < nA; k += kAtxThreads)
       sh.tabA[k] = ray_tab_a(G, G.y_det[amin + k]);
-    for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads)
-      sh.ys[k] = yl((long long)(bmin + k / nA) * D.na + amin + k % nA);
-    __syncthreads();
+    for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads) {
+      const float v = yl((long long)(bmin + k / nA) * D.na + amin + k % nA);
+      finite = finite && isfinite(v);
+      sh.ys[k] = v;
+    }
+    finite = __syncthreads_and(finite);
     if (!kPlanar) {
       for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads)
         sh.tabC[k] = ray_tab_c(sh.tabA[k % nA], G.z_det[bmin + k / nA]);
@@ -150,12 +200,19 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   const float rx = G.cos_phi * (-G.SO) - w.xc;
   const float ry = G.sin_phi * (-G.SO) - w.yc;
   const float rz = 0.0f - w.zc;
-  const bool has = valid && w.a0 <= w.a1 && w.b0 <= w.b1;
-  const int cntA = has ? w.a1 - w.a0 + 1 : 0;
+  int lo = w.a0, hi = w.a1;
+  if (kPlanar && finite && has) {
+    int slo, shi;
+    if (shadow_bins(G, D, w.xc, w.yc, slo, shi)) {
+      lo = max(lo, slo);
+      hi = min(hi, shi);
+    }
+  }
+  const int cntA = has && lo <= hi ? hi - lo + 1 : 0;
   const int cntB = has ? w.b1 - w.b0 + 1 : 0;
   const int kA = __reduce_max_sync(0xffffffffu, cntA);
   const int kB = __reduce_max_sync(0xffffffffu, cntB);
-  const int a_off = w.a0 - amin;
+  const int a_off = lo - amin;
   for (int kb = 0; kb < kB; kb++) {
     const bool onb = kb < cntB;
     const int ib = w.b0 + kb;
@@ -250,7 +307,7 @@ __global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 3)
   const float bp = acc * G.scale, scv = accl * G.scale;
   const float beta = I.s->beta_f;
   const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
-  const float mn = I.m[idx] + beta * (bp / (scv == 0.f ? 1.f : scv));
+  const float mn = I.m[idx] + beta * __fdividef(bp, scv == 0.f ? 1.f : scv);
   I.m[idx] = mn < 0.f ? 0.f : mn;
 }
 

@@ -34,16 +34,16 @@ __device__ __forceinline__ bool tile_voxel(int nx, int ny, int &ix, int &iy,
   return ix < nx && iy < ny;
 }
 
-template <class T>
-__device__ __forceinline__ T tv_sqrt(T v);
-template <>
-__device__ __forceinline__ double tv_sqrt<double>(double v) {
-  return sqrt(v);
+// num / sqrt(den): exact operations in FP64 (the mex-level entry points);
+// the hardware reciprocal square root in FP32 (the device-resident path,
+// within a few ulp of the FP64 stencil's value).
+__device__ __forceinline__ double tv_q(double num, double den) {
+  return num / sqrt(den);
 }
-template <>
-__device__ __forceinline__ float tv_sqrt<float>(float v) {
-  return sqrtf(v);
+__device__ __forceinline__ float tv_q(float num, float den) {
+  return num * rsqrtf(den);
 }
+
 template <class T>
 __device__ __forceinline__ T tv_eps();
 template <>
@@ -79,10 +79,9 @@ __device__ __forceinline__ T tv_grad2(const Img<T> &u, int x, int y) {
   const T xm = u(x - 1, y, 0), ym = u(x, y - 1, 0);
   const T xp = u(x + 1, y, 0), yp = u(x, y + 1, 0);
   const T xpym = u(x + 1, y - 1, 0), xmyp = u(x - 1, y + 1, 0);
-  const T g1 = ((c0 - xm) + (c0 - ym)) /
-               tv_sqrt<T>(eps + sqr(c0 - xm) + sqr(c0 - ym));
-  const T g2 = -(xp - c0) / tv_sqrt<T>(eps + sqr(xp - c0) + sqr(xp - xpym));
-  const T g3 = -(yp - c0) / tv_sqrt<T>(eps + sqr(yp - c0) + sqr(yp - xmyp));
+  const T g1 = tv_q((c0 - xm) + (c0 - ym), eps + sqr(c0 - xm) + sqr(c0 - ym));
+  const T g2 = tv_q(-(xp - c0), eps + sqr(xp - c0) + sqr(xp - xpym));
+  const T g3 = tv_q(-(yp - c0), eps + sqr(yp - c0) + sqr(yp - xmyp));
   return g1 + g2 + g3;
 }
 
@@ -96,14 +95,14 @@ __device__ __forceinline__ T tv_grad3(const Img<T> &u, int x, int y, int z) {
   const T xm_zp = u(x - 1, y, z + 1), ym_zp = u(x, y - 1, z + 1);
   const T xm_yp = u(x - 1, y + 1, z), yp_zm = u(x, y + 1, z - 1);
   const T xp_ym = u(x + 1, y - 1, z), xp_zm = u(x + 1, y, z - 1);
-  const T g1 = (T(6) * c0 - T(2) * (xm + ym + zm)) /
-               tv_sqrt<T>(eps + sqr(c0 - xm) + sqr(c0 - ym) + sqr(c0 - zm));
-  const T g2 = (T(2) * c0 - T(2) * zp) /
-               tv_sqrt<T>(eps + sqr(zp - xm_zp) + sqr(zp - ym_zp) + sqr(zp - c0));
-  const T g3 = (T(2) * c0 - T(2) * yp) /
-               tv_sqrt<T>(eps + sqr(yp - xm_yp) + sqr(yp - c0) + sqr(yp - yp_zm));
-  const T g4 = (T(2) * c0 - T(2) * xp) /
-               tv_sqrt<T>(eps + sqr(xp - c0) + sqr(xp - xp_ym) + sqr(xp - xp_zm));
+  const T g1 = tv_q(T(6) * c0 - T(2) * (xm + ym + zm),
+                    eps + sqr(c0 - xm) + sqr(c0 - ym) + sqr(c0 - zm));
+  const T g2 = tv_q(T(2) * c0 - T(2) * zp,
+                    eps + sqr(zp - xm_zp) + sqr(zp - ym_zp) + sqr(zp - c0));
+  const T g3 = tv_q(T(2) * c0 - T(2) * yp,
+                    eps + sqr(yp - xm_yp) + sqr(yp - c0) + sqr(yp - yp_zm));
+  const T g4 = tv_q(T(2) * c0 - T(2) * xp,
+                    eps + sqr(xp - c0) + sqr(xp - xp_ym) + sqr(xp - xp_zm));
   return g1 + g2 + g3 + g4;
 }
 

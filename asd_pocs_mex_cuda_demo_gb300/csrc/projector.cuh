@@ -367,10 +367,10 @@ ASD_HD VoxelWin voxel_window(const ViewGeo &G,
                                                  const Dims &D, int ix, int iy,
                                                  int iz) {
   VoxelWin w;
-  const float SD = G.SO + G.OD;
+  const float SD = G.SD;   // SO + OD
   const int na2 = D.na / 2, nb2 = D.nb / 2;
   const int nx2 = D.nx / 2, ny2 = D.ny / 2, nz2 = D.nz / 2;
-  const float d = sqrtf((1 + G.dz * G.dz) / 2);
+  const float d = G.dwin;  // sqrtf((1 + dz*dz)/2)
   // (float)(i + 0.5 - n2) is evaluated in double by the reference; for
   // |i - n2| < 2^22 the float form below is the same exactly-representable
   // value and avoids FP64 arithmetic (slow on this GPU).

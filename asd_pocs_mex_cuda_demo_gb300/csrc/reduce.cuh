@@ -1,37 +1,37 @@
 // Deterministic grid reductions (internal).
 //
-// GB300 executes FP64 at a small fraction of its FP32 rate, so per-element
-// work stays in FP32: each warp sums its 32 values with an FP32 xor
-// butterfly (relative error <= 5 roundings, ~3e-7), and only the per-warp
-// totals are accumulated in FP64 -- across the warps of a block, then across
-// blocks.  The block partials are summed by the last block to finish (atomic
-// ticket) in block order, so the result is bit-identical from run to run and
-// independent of scheduling; a reconstruction gives the same scalars alone
-// and inside a batch.  The ticket is reset by the last block, which keeps the
-// kernels replayable inside a CUDA graph.
+// GB300 executes FP64 at a small fraction of its FP32 rate, so everything
+// inside a block stays in FP32: each warp sums its 32 values with an FP32
+// xor butterfly and warp 0 sums the per-warp totals (a 256-value pairwise
+// tree: relative error <= 8 roundings, ~5e-7).  Only the block partials are
+// accumulated in FP64, by the last block to finish (atomic ticket), in block
+// order -- so the result is bit-identical from run to run and independent of
+// scheduling; a reconstruction gives the same scalars alone and inside a
+// batch.  The ticket is reset by the last block, which keeps the kernels
+// replayable inside a CUDA graph.
 #pragma once
 #include "common.cuh"
 
 namespace asd {
 
-// Block totals in FP64 (valid in warp 0 after the call); sh holds
-// K * (NT/32) doubles.  Every thread of the block must call it.
+// Block totals (valid in warp 0 after the call), FP32 tree; sh holds
+// K * (NT/32) floats.  Every thread of the block must call it.
 template <int NT, int K>
-__device__ __forceinline__ void block_sum_f(const float (&v)[K], double (&out)[K],
-                                            double *sh) {
+__device__ __forceinline__ void block_sum_f(const float (&v)[K], float (&out)[K],
+                                            float *sh) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < K; k++) {
     float s = v[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) sh[k * (NT / 32) + warp] = (double)s;
+    if (lane == 0) sh[k * (NT / 32) + warp] = s;
   }
   __syncthreads();
   if (warp == 0) {
 #pragma unroll
     for (int k = 0; k < K; k++) {
-      double t = lane < NT / 32 ? sh[k * (NT / 32) + lane] : 0.0;
+      float t = lane < NT / 32 ? sh[k * (NT / 32) + lane] : 0.f;
 #pragma unroll
       for (int o = NT / 64; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
       out[k] = t;
@@ -49,13 +49,14 @@ template <int NT, int K>
 __device__ __forceinline__ bool grid_sum(const float (&v)[K], double *partials,
                                          unsigned *counter, int nblocks,
                                          double (&tot)[K]) {
+  __shared__ float shf[K * (NT / 32)];
   __shared__ double sh[K * (NT / 32)];
   __shared__ bool last;
-  double bs[K];
-  block_sum_f<NT, K>(v, bs, sh);
+  float bs[K];
+  block_sum_f<NT, K>(v, bs, shf);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < K; k++) partials[(long long)blockIdx.x * K + k] = bs[k];
+    for (int k = 0; k < K; k++) partials[(long long)blockIdx.x * K + k] = (double)bs[k];
     __threadfence();
     const unsigned t = atomicAdd(counter, 1u);
     last = (t == (unsigned)nblocks - 1);

@@ -20,8 +20,7 @@ using namespace asd;
 
 static ViewGeo geo(float c, float s, const float *yd, const float *zd, float SO,
                    float OD, float scale, float ddy, float ddz, float dz) {
-  ViewGeo g{c, s, SO, OD, scale, ddy, ddz, dz, yd, zd};
-  return g;
+  return with_constants(ViewGeo{c, s, SO, OD, scale, ddy, ddz, dz, yd, zd});
 }
 
 extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,

@@ -118,3 +118,23 @@ def test_adjointness_gpu(gpu):
         lhs = float(np.dot(Ax.astype(np.float64), yv))
         rhs = float(np.dot(x.astype(np.float64), Aty))
         assert abs(lhs - rhs) / abs(lhs) < 2e-5
+
+
+def test_atx_non_finite_view_values_propagate_like_reference(gpu, oracle_mod):
+    # a NaN / inf view value reaches every voxel whose footprint window holds
+    # its bin, through the zero chords too (0*NaN), as in the reference loop
+    n, na = 64, 128
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = SO / (SO + OD) * det * na / n
+    yv = np.random.default_rng(5).random(na).astype(np.float32)
+    yv[40] = np.nan
+    yv[90] = np.inf
+    for a in (0.0, 33.0, 90.0):
+        g = oracle_mod.gateway_geometry(-a / 180 * np.pi, SO, OD, vx, det, na, 1)
+        bo, co = oracle_mod.atx(yv, g, n, n, 1)
+        para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, phi=-a / 180 * np.pi,
+                    detsize=det, na=na, nb=1)
+        b, sc = pkg.Atx_cone_gpu(yv, para)
+        assert np.isnan(bo).any()
+        assert np.array_equal(b, bo, equal_nan=True), a
+        assert np.array_equal(sc, co)
