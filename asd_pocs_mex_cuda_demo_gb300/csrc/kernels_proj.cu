@@ -125,8 +125,9 @@ __device__ __forceinline__ bool shadow_bins(const ViewGeo &G, const Dims &D,
 // different rays do not serialise.  In the planar geometry each lane walks
 // only the bins of its pixel's shadow (inside the reference's window); the
 // bins it skips have chords of exactly 0, which add nothing unless a view
-// value is not finite, so a block whose window holds NaN/inf walks the whole
-// window.  Pairs are accumulated in the reference's order (ib outer, ia
+// value is not finite, so a block whose window holds NaN/inf -- or an
+// axis-parallel ray, whose reference chord is not geometric -- walks the
+// whole window.  Pairs are accumulated in the reference's order (ib outer, ia
 // inner).  A block whose window does not fit the staging arrays (extreme
 // geometry) falls back to the direct per-pair computation.
 // Must be called by every thread of the block.
@@ -177,16 +178,22 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   accl = 0.f;
   if (nA <= 0) return;  // no voxel of the block sees the detector
   const bool staged = planar_ok && nA <= Sh::kA && (long long)nA * nB <= Sh::kC;
-  bool finite = true;
+  // narrowing to the pixel shadow needs finite view values and rays with
+  // both in-plane components (an axis-parallel ray's reference chord ignores
+  // one coordinate and is 1 for every voxel of the window)
+  bool narrow = true;
   if (staged) {
-    for (int k = threadIdx.x; k < nA; k += kAtxThreads)
-      sh.tabA[k] = ray_tab_a(G, G.y_det[amin + k]);
+    for (int k = threadIdx.x; k < nA; k += kAtxThreads) {
+      const float4 A = ray_tab_a(G, G.y_det[amin + k]);
+      narrow = narrow && A.x != 0.0f && A.y != 0.0f;
+      sh.tabA[k] = A;
+    }
     for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads) {
       const float v = yl((long long)(bmin + k / nA) * D.na + amin + k % nA);
-      finite = finite && isfinite(v);
+      narrow = narrow && isfinite(v);
       sh.ys[k] = v;
     }
-    finite = __syncthreads_and(finite);
+    narrow = __syncthreads_and(narrow);
     if (!kPlanar) {
       for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads)
         sh.tabC[k] = ray_tab_c(sh.tabA[k % nA], G.z_det[bmin + k / nA]);
@@ -201,7 +208,7 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   const float ry = G.sin_phi * (-G.SO) - w.yc;
   const float rz = 0.0f - w.zc;
   int lo = w.a0, hi = w.a1;
-  if (kPlanar && finite && has) {
+  if (kPlanar && narrow && has) {
     int slo, shi;
     if (shadow_bins(G, D, w.xc, w.yc, slo, shi)) {
       lo = max(lo, slo);

@@ -138,3 +138,20 @@ def test_atx_non_finite_view_values_propagate_like_reference(gpu, oracle_mod):
         assert np.isnan(bo).any()
         assert np.array_equal(b, bo, equal_nan=True), a
         assert np.array_equal(sc, co)
+
+
+@pytest.mark.parametrize("angle", [0.0, 90.0, 180.0, 270.0])
+def test_axis_parallel_central_ray(gpu, oracle_mod, angle):
+    # with an odd detector the central bin's ray is axis-parallel at these
+    # angles; the reference's chord then ignores one coordinate (length 1 for
+    # every voxel of the footprint window)
+    nx, ny, na = 33, 17, 41
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = SO / (SO + OD) * det * na / nx
+    yv = np.random.default_rng(9).random(na).astype(np.float32)
+    g = oracle_mod.gateway_geometry(-angle / 180 * np.pi, SO, OD, vx, det, na, 1)
+    bo, co = oracle_mod.atx(yv, g, nx, ny, 1)
+    para = dict(SO=SO, OD=OD, vxlsize=vx, nx=nx, ny=ny, nz=1, phi=-angle / 180 * np.pi,
+                detsize=det, na=na, nb=1)
+    b, sc = pkg.Atx_cone_gpu(yv, para)
+    assert np.array_equal(b, bo) and np.array_equal(sc, co)
