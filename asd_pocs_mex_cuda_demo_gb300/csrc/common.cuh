@@ -87,6 +87,37 @@ struct Inst {
 };
 
 constexpr int kMaxPartials = 1 << 22;  // blocks per reduction (sanity bound)
+
+// Voxel tiles of the voxel-driven kernels: 32 (x) by 8 (y) voxels of one z
+// slice per 256-thread block.  Grids are (x tiles, y tiles * nz, instances).
+constexpr int kTileX = 32, kTileY = 8;
+constexpr int kTileThreads = kTileX * kTileY;
+
+__host__ __device__ inline dim3 tile_grid(int nx, int ny, int nz, int batch) {
+  return dim3((nx + kTileX - 1) / kTileX, ((ny + kTileY - 1) / kTileY) * nz,
+              batch);
+}
+
+// Voxel of this thread; true if inside the volume.
+__device__ __forceinline__ bool tile_voxel(int nx, int ny, int nz, int &ix,
+                                           int &iy, int &iz) {
+  int by = blockIdx.y;
+  iz = 0;
+  if (nz > 1) {
+    const int ty = (ny + kTileY - 1) / kTileY;
+    iz = by / ty;
+    by -= iz * ty;
+  }
+  ix = blockIdx.x * kTileX + (threadIdx.x % kTileX);
+  iy = by * kTileY + (threadIdx.x / kTileX);
+  return ix < nx && iy < ny;
+}
+
+// Index of this block among the blocks of its instance, and their number.
+__device__ __forceinline__ int inst_block() {
+  return blockIdx.x + gridDim.x * blockIdx.y;
+}
+__device__ __forceinline__ int inst_blocks() { return gridDim.x * gridDim.y; }
 constexpr int kMaxReduceK = 3;          // values reduced together
 
 }  // namespace asd

@@ -16,27 +16,18 @@ namespace {
 
 constexpr int kAxWarps = 4;             // rays per Ax block
 constexpr int kAxThreads = kAxWarps * 32;
-constexpr int kTileX = 32, kTileY = 8;  // Atx voxel tile (x fastest)
-constexpr int kAtxThreads = kTileX * kTileY;
+constexpr int kAtxThreads = kTileThreads;
 constexpr int kTabA = 512;              // detector columns staged per block
 constexpr int kTabC = 1536;             // 3D rays staged per block
 
 __device__ __forceinline__ bool tile_voxel(const Dims &D, int &ix, int &iy,
                                            int &iz) {
-  const int tx = (D.nx + kTileX - 1) / kTileX;
-  const int ty = (D.ny + kTileY - 1) / kTileY;
-  int b = blockIdx.x;
-  const int bx = b % tx;
-  b /= tx;
-  const int by = b % ty;
-  iz = b / ty;
-  ix = bx * kTileX + (threadIdx.x % kTileX);
-  iy = by * kTileY + (threadIdx.x / kTileX);
-  return ix < D.nx && iy < D.ny;
+  return asd::tile_voxel(D.nx, D.ny, D.nz, ix, iy, iz);
 }
 
 int atx_blocks(const Dims &d) {
-  return ((d.nx + kTileX - 1) / kTileX) * ((d.ny + kTileY - 1) / kTileY) * d.nz;
+  const dim3 g = tile_grid(d.nx, d.ny, d.nz, 1);
+  return (int)(g.x * g.y);
 }
 
 // ------------------------------------------------------------------- Ax
@@ -271,7 +262,7 @@ __device__ __forceinline__ ViewGeo view_of(const Inst &I, int view) {
 // cor0=P(:,ii)-proj; dd2+=||cor0||^2; cor=cor0./sumR.
 __global__ void __launch_bounds__(kAxThreads)
     k_sart_ax(const Inst *__restrict__ insts, Dims D, int view) {
-  const Inst &I = insts[blockIdx.y];
+  const Inst &I = insts[blockIdx.z];
   if (((volatile int *)&I.s->done)[0]) return;
   const ViewGeo G = view_of(I, view);
   const int lane = threadIdx.x & 31;
@@ -290,7 +281,8 @@ __global__ void __launch_bounds__(kAxThreads)
     }
   }
   double tot[1];
-  if (grid_sum<kAxThreads, 1>(part, I.partials, I.counter, gridDim.x, tot)) {
+  if (grid_sum<kAxThreads, 1>(part, I.partials, I.counter, inst_block(),
+                              inst_blocks(), tot)) {
     if (threadIdx.x == 0) I.s->dd2_acc += tot[0];
   }
 }
@@ -301,7 +293,7 @@ template <bool kPlanar>
 __global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 3)
     k_sart_atx(const Inst *__restrict__ insts, Dims D, int view) {
   __shared__ AtxShared<kPlanar> sh;
-  const Inst &I = insts[blockIdx.y];
+  const Inst &I = insts[blockIdx.z];
   if (((volatile int *)&I.s->done)[0]) return;
   const ViewGeo G = view_of(I, view);
   int ix, iy, iz;
@@ -331,12 +323,11 @@ cudaError_t launch_ax(const float *x, float *y, float *sr, const ViewGeo &g,
 
 cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
                        const Dims &d, cudaStream_t st) {
-  const int blocks = atx_blocks(d);
-  if (blocks == 0) return cudaSuccess;
+  const dim3 grid = tile_grid(d.nx, d.ny, d.nz, 1);
   if (d.nz == 1 && d.nb == 1)
-    k_atx<true><<<blocks, kAtxThreads, 0, st>>>(x, y, sc, g, d);
+    k_atx<true><<<grid, kAtxThreads, 0, st>>>(x, y, sc, g, d);
   else
-    k_atx<false><<<blocks, kAtxThreads, 0, st>>>(x, y, sc, g, d);
+    k_atx<false><<<grid, kAtxThreads, 0, st>>>(x, y, sc, g, d);
   return cudaGetLastError();
 }
 
@@ -344,13 +335,13 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
                            int view, cudaStream_t st) {
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
-  k_sart_ax<<<dim3(blocks, batch), kAxThreads, 0, st>>>(insts, d, view);
+  k_sart_ax<<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, d, view);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
                             int view, cudaStream_t st) {
-  const dim3 grid(atx_blocks(d), batch);
+  const dim3 grid = tile_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz == 1 && d.nb == 1)
     k_sart_atx<true><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
   else

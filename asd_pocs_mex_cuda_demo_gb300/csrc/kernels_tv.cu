@@ -1,11 +1,17 @@
 // TV steepest-descent kernels (imgTVGradMin.cpp / imgTVGradMin3D.cpp) and
 // the per-iteration ASD-POCS scalar steps (ASD_POCS_cuda.m:137-170), sm_103a.
 //
-// The TV global norm forces a grid-wide dependency in every step, so a step
-// is two passes over the image: the first recomputes the stencil only for
-// ||v||^2 (deterministic grid sum), the second recomputes it and writes
-// m - (alpha*d/||v||)*v into the other buffer of a ping-pong pair.  Nothing
-// but the image is stored: 12 bytes per voxel per step in FP32.
+// Device-resident path (FP32 image, FP64 scalars): one kernel per TV step.
+// A block stages its 32x8 voxel tile of the current image with a halo of two
+// voxels in shared memory (zero outside the image, as the reference's padded
+// copy), computes the updated image m' = m - (alpha*d/||v||) v on the tile
+// plus a one-voxel halo, writes the tile of m', and evaluates the stencil of
+// m' on the tile for the next step's ||v'||^2 (deterministic grid sum).  A
+// step therefore reads the image once and writes it once (8 bytes per voxel)
+// and the ||v|| that every step needs before it can update comes out of the
+// previous kernel.  The end-of-sweep kernel provides ||v|| of the first
+// step; the last step also applies the positivity constraint and the
+// alpha/beta step control.
 #include "kernels.h"
 #include "reduce.cuh"
 
@@ -13,26 +19,7 @@ namespace asd {
 
 namespace {
 
-constexpr int kTileX = 32, kTileY = 8;
-constexpr int kThreads = kTileX * kTileY;
-
-__host__ __device__ inline int tiles(int nx, int ny, int nz) {
-  return ((nx + kTileX - 1) / kTileX) * ((ny + kTileY - 1) / kTileY) * nz;
-}
-
-__device__ __forceinline__ bool tile_voxel(int nx, int ny, int &ix, int &iy,
-                                           int &iz) {
-  const int tx = (nx + kTileX - 1) / kTileX;
-  const int ty = (ny + kTileY - 1) / kTileY;
-  int b = blockIdx.x;
-  const int bx = b % tx;
-  b /= tx;
-  const int by = b % ty;
-  iz = b / ty;
-  ix = bx * kTileX + (threadIdx.x % kTileX);
-  iy = by * kTileY + (threadIdx.x / kTileX);
-  return ix < nx && iy < ny;
-}
+constexpr int kThreads = kTileThreads;
 
 // num / sqrt(den): exact operations in FP64 (the mex-level entry points);
 // the hardware reciprocal square root in FP32 (the device-resident path,
@@ -55,30 +42,20 @@ __device__ __forceinline__ float tv_eps<float>() {
   return 1e-8f;
 }
 
-// Zero-padded read of the image (the reference's (n+2)-wide bordered copy).
-template <class T>
-struct Img {
-  const T *p;
-  int nx, ny, nz;
-  __device__ __forceinline__ T operator()(int x, int y, int z) const {
-    if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return T(0);
-    return p[((long long)z * ny + y) * nx + x];
-  }
-};
-
 template <class T>
 __device__ __forceinline__ T sqr(T v) {
   return v * v;
 }
 
-// imgTVGradMin.cpp:84-97 (x = row index r, fastest; y = column index c).
-template <class T>
-__device__ __forceinline__ T tv_grad2(const Img<T> &u, int x, int y) {
+// imgTVGradMin.cpp:84-97; u(dx, dy, dz) reads the image at an offset from
+// the voxel (zero outside the image).  x = row index r (fastest).
+template <class T, class U>
+__device__ __forceinline__ T tv_grad2(const U &u) {
   const T eps = tv_eps<T>();
-  const T c0 = u(x, y, 0);
-  const T xm = u(x - 1, y, 0), ym = u(x, y - 1, 0);
-  const T xp = u(x + 1, y, 0), yp = u(x, y + 1, 0);
-  const T xpym = u(x + 1, y - 1, 0), xmyp = u(x - 1, y + 1, 0);
+  const T c0 = u(0, 0, 0);
+  const T xm = u(-1, 0, 0), ym = u(0, -1, 0);
+  const T xp = u(1, 0, 0), yp = u(0, 1, 0);
+  const T xpym = u(1, -1, 0), xmyp = u(-1, 1, 0);
   const T g1 = tv_q((c0 - xm) + (c0 - ym), eps + sqr(c0 - xm) + sqr(c0 - ym));
   const T g2 = tv_q(-(xp - c0), eps + sqr(xp - c0) + sqr(xp - xpym));
   const T g3 = tv_q(-(yp - c0), eps + sqr(yp - c0) + sqr(yp - xmyp));
@@ -86,15 +63,15 @@ __device__ __forceinline__ T tv_grad2(const Img<T> &u, int x, int y) {
 }
 
 // imgTVGradMin3D.cpp:114-140 (image index x + y*Nx + z*Nx*Ny).
-template <class T>
-__device__ __forceinline__ T tv_grad3(const Img<T> &u, int x, int y, int z) {
+template <class T, class U>
+__device__ __forceinline__ T tv_grad3(const U &u) {
   const T eps = tv_eps<T>();
-  const T c0 = u(x, y, z);
-  const T xm = u(x - 1, y, z), ym = u(x, y - 1, z), zm = u(x, y, z - 1);
-  const T xp = u(x + 1, y, z), yp = u(x, y + 1, z), zp = u(x, y, z + 1);
-  const T xm_zp = u(x - 1, y, z + 1), ym_zp = u(x, y - 1, z + 1);
-  const T xm_yp = u(x - 1, y + 1, z), yp_zm = u(x, y + 1, z - 1);
-  const T xp_ym = u(x + 1, y - 1, z), xp_zm = u(x + 1, y, z - 1);
+  const T c0 = u(0, 0, 0);
+  const T xm = u(-1, 0, 0), ym = u(0, -1, 0), zm = u(0, 0, -1);
+  const T xp = u(1, 0, 0), yp = u(0, 1, 0), zp = u(0, 0, 1);
+  const T xm_zp = u(-1, 0, 1), ym_zp = u(0, -1, 1);
+  const T xm_yp = u(-1, 1, 0), yp_zm = u(0, 1, -1);
+  const T xp_ym = u(1, -1, 0), xp_zm = u(1, 0, -1);
   const T g1 = tv_q(T(6) * c0 - T(2) * (xm + ym + zm),
                     eps + sqr(c0 - xm) + sqr(c0 - ym) + sqr(c0 - zm));
   const T g2 = tv_q(T(2) * c0 - T(2) * zp,
@@ -106,26 +83,37 @@ __device__ __forceinline__ T tv_grad3(const Img<T> &u, int x, int y, int z) {
   return g1 + g2 + g3 + g4;
 }
 
-template <class T>
-__device__ __forceinline__ T tv_grad(const Img<T> &u, int x, int y, int z) {
-  return u.nz >= 2 ? tv_grad3(u, x, y, z) : tv_grad2(u, x, y);
+template <class T, class U>
+__device__ __forceinline__ T tv_grad(const U &u, bool is3d) {
+  return is3d ? tv_grad3<T>(u) : tv_grad2<T>(u);
 }
 
+// Global-memory accessor with zero padding (standalone entry points).
+template <class T>
+struct GlobalAt {
+  const T *p;
+  int nx, ny, nz, x, y, z;
+  __device__ __forceinline__ T operator()(int dx, int dy, int dz) const {
+    const int xx = x + dx, yy = y + dy, zz = z + dz;
+    if (xx < 0 || yy < 0 || zz < 0 || xx >= nx || yy >= ny || zz >= nz) return T(0);
+    return p[((long long)zz * ny + yy) * nx + xx];
+  }
+};
+
 // --------------------------------------------------- standalone TV kernels
-// scal[0] = d, scal[1] = ||v||^2 of the current step.
-// Grid sum of one value per thread: FP32 within warps for the FP32 path,
-// FP64 throughout for the FP64 entry points.
+// scal[0] = d, scal[1] = ||v||, scal[2] = alpha*d/||v|| (+ FP32 copy at 3).
 __device__ __forceinline__ bool sum_all(float v, double *partials,
                                         unsigned *counter, double &tot) {
   const float vv[1] = {v};
   double t[1];
-  const bool last = grid_sum<kThreads, 1>(vv, partials, counter, gridDim.x, t);
+  const bool last = grid_sum<kThreads, 1>(vv, partials, counter, inst_block(),
+                                          inst_blocks(), t);
   tot = t[0];
   return last;
 }
 __device__ __forceinline__ bool sum_all(double v, double *partials,
                                         unsigned *counter, double &tot) {
-  return grid_sum_d<kThreads>(v, partials, counter, gridDim.x, tot);
+  return grid_sum_d<kThreads>(v, partials, counter, inst_blocks(), tot);
 }
 
 template <class T>
@@ -135,7 +123,7 @@ __global__ void __launch_bounds__(kThreads)
               unsigned *counter) {
   int ix, iy, iz;
   T v = T(0);
-  if (tile_voxel(nx, ny, ix, iy, iz)) {
+  if (tile_voxel(nx, ny, nz, ix, iy, iz)) {
     const long long i = ((long long)iz * ny + iy) * nx + ix;
     const T d = img[i] - (old ? old[i] : T(0));
     v = d * d;
@@ -151,9 +139,8 @@ __global__ void __launch_bounds__(kThreads)
               double *scal, double *partials, unsigned *counter) {
   int ix, iy, iz;
   T v = T(0);
-  const Img<T> u{src, nx, ny, nz};
-  if (tile_voxel(nx, ny, ix, iy, iz)) {
-    const T g = tv_grad(u, ix, iy, iz);
+  if (tile_voxel(nx, ny, nz, ix, iy, iz)) {
+    const T g = tv_grad<T>(GlobalAt<T>{src, nx, ny, nz, ix, iy, iz}, nz >= 2);
     v = g * g;
   }
   double tot;
@@ -171,9 +158,8 @@ __global__ void __launch_bounds__(kThreads)
     k_tv_update(const T *__restrict__ src, T *__restrict__ dst, int nx, int ny,
                 int nz, double alpha, const double *scal, int clamp) {
   int ix, iy, iz;
-  if (!tile_voxel(nx, ny, ix, iy, iz)) return;
-  const Img<T> u{src, nx, ny, nz};
-  const T g = tv_grad(u, ix, iy, iz);
+  if (!tile_voxel(nx, ny, nz, ix, iy, iz)) return;
+  const T g = tv_grad<T>(GlobalAt<T>{src, nx, ny, nz, ix, iy, iz}, nz >= 2);
   const long long i = ((long long)iz * ny + iy) * nx + ix;
   T r;
   if (sizeof(T) == 8) {
@@ -202,21 +188,20 @@ cudaError_t tv_minimize(T *img, const T *old, T *wa, T *wb, double *scal,
                         double *partials, unsigned *counter, int nx, int ny,
                         int nz, double alpha, int n_iter, int pos,
                         cudaStream_t st) {
-  const int blocks = tiles(nx, ny, nz);
-  if (blocks == 0) return cudaSuccess;
-  if (blocks > kMaxPartials) return cudaErrorInvalidValue;
-  k_tv_dist<T><<<blocks, kThreads, 0, st>>>(img, old, nx, ny, nz, scal,
-                                            partials, counter);
+  const dim3 grid = tile_grid(nx, ny, nz, 1);
+  if ((long long)grid.x * grid.y > kMaxPartials) return cudaErrorInvalidValue;
+  k_tv_dist<T><<<grid, kThreads, 0, st>>>(img, old, nx, ny, nz, scal, partials,
+                                          counter);
   const T *src = img;
   T *bufs[2] = {wa, wb};
   for (int it = 0; it < n_iter; it++) {
     T *dst = (it == n_iter - 1) ? img : bufs[it & 1];
     if (dst == src) dst = bufs[(it + 1) & 1];
-    k_tv_norm<T><<<blocks, kThreads, 0, st>>>(src, nx, ny, nz, alpha, scal,
-                                              partials, counter);
+    k_tv_norm<T><<<grid, kThreads, 0, st>>>(src, nx, ny, nz, alpha, scal,
+                                            partials, counter);
     const int clamp_now = (it == n_iter - 1) && pos == 1;
-    k_tv_update<T><<<blocks, kThreads, 0, st>>>(src, dst, nx, ny, nz, alpha,
-                                                scal, clamp_now);
+    k_tv_update<T><<<grid, kThreads, 0, st>>>(src, dst, nx, ny, nz, alpha,
+                                              scal, clamp_now);
     src = dst;
   }
   if (n_iter > 0 && src != img) {
@@ -226,21 +211,99 @@ cudaError_t tv_minimize(T *img, const T *old, T *wa, T *wb, double *scal,
   return cudaGetLastError();
 }
 
-// ------------------------------------------- batched ASD-POCS scalar steps
+// ------------------------------------------- batched ASD-POCS: tiled steps
+// Shared tile of an image with a halo of H voxels (zero outside the image).
+template <int H, bool k3D>
+struct Tile {
+  static constexpr int W = kTileX + 2 * H, Hh = kTileY + 2 * H;
+  static constexpr int D = k3D ? 1 + 2 * H : 1;
+  float v[D][Hh][W];
+};
+
+template <int H, bool k3D>
+struct TileAt {  // accessor centred on tile position (tx, ty, tz)
+  const Tile<H, k3D> &t;
+  int tx, ty, tz;
+  __device__ __forceinline__ float operator()(int dx, int dy, int dz) const {
+    return t.v[tz + dz][ty + dy][tx + dx];
+  }
+};
+
+// Loads the tile (origin x0, y0 of the block, slice z) with its halo.
+template <int H, bool k3D>
+__device__ __forceinline__ void load_tile(Tile<H, k3D> &t, const float *src,
+                                          const Dims &D, int x0, int y0,
+                                          int z) {
+  constexpr int W = Tile<H, k3D>::W, Hh = Tile<H, k3D>::Hh, Dd = Tile<H, k3D>::D;
+  for (int k = threadIdx.x; k < W * Hh * Dd; k += kThreads) {
+    const int tx = k % W, ty = (k / W) % Hh, tz = k / (W * Hh);
+    const int x = x0 - H + tx, y = y0 - H + ty, zz = k3D ? z - H + tz : z;
+    float v = 0.f;
+    if (x >= 0 && y >= 0 && zz >= 0 && x < D.nx && y < D.ny && zz < D.nz)
+      v = src[((unsigned)zz * D.ny + y) * D.nx + x];
+    t.v[tz][ty][tx] = v;
+  }
+}
+
 __device__ __forceinline__ bool inst_done(const Inst &I) {
   return ((volatile int *)&I.s->done)[0] != 0;
 }
 
+__device__ __forceinline__ const float *tv_src(const Inst &I, int step) {
+  return step == 0 ? I.m : ((step & 1) ? I.tv_b : I.tv_c);
+}
+__device__ __forceinline__ float *tv_dst(const Inst &I, int step) {
+  return (step & 1) ? I.tv_c : I.tv_b;
+}
+
+__device__ __forceinline__ void tile_origin(const Dims &D, int &x0, int &y0,
+                                            int &z) {
+  int by = blockIdx.y;
+  z = 0;
+  if (D.nz > 1) {
+    const int ty = (D.ny + kTileY - 1) / kTileY;
+    z = by / ty;
+    by -= z * ty;
+  }
+  x0 = blockIdx.x * kTileX;
+  y0 = by * kTileY;
+}
+
+// End-of-iteration scalars (ASD_POCS_cuda.m:166-170) by the last block.
+__device__ __forceinline__ void finish_scalars(Scalars *s, double dg2) {
+  s->dg = sqrt(dg2);
+  if (s->dg > s->r_max * s->dp && sqrt(s->dd2) > s->epsilon)
+    s->alpha = s->alpha * s->alpha_red;
+  s->beta = s->beta * s->beta_red;
+  s->beta_f = (float)s->beta;
+  if (s->k >= s->maxIter) {
+    s->done = 1;
+  } else {
+    s->k = s->k + 1;
+  }
+}
+
 // After the SART sweep (ASD_POCS_cuda.m:137-149): dd, m_res, RMSE, dp and the
-// stop test; also d = ||m - m_k1|| for the TV step (imgTVGradMin.cpp:57-60).
+// stop test; d = ||m - m_k1|| (imgTVGradMin.cpp:57-60) and ||v|| of the first
+// TV step, giving its step size alpha*d/||v||.
+template <bool k3D>
 __global__ void __launch_bounds__(kThreads)
     k_after_sweep(const Inst *__restrict__ insts, Dims D) {
-  const Inst &I = insts[blockIdx.y];
+  __shared__ Tile<1, k3D> t;
+  const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
-  int ix, iy, iz;
-  float v[3] = {0.f, 0.f, 0.f};
-  if (tile_voxel(D.nx, D.ny, ix, iy, iz)) {
-    const long long i = ((long long)iz * D.ny + iy) * D.nx + ix;
+  const bool tv = I.s->ng > 0;
+  int x0, y0, z;
+  tile_origin(D, x0, y0, z);
+  if (tv) {
+    load_tile(t, I.m, D, x0, y0, z);
+    __syncthreads();
+  }
+  const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
+  const int ix = x0 + tx, iy = y0 + ty;
+  float v[4] = {0.f, 0.f, 0.f, 0.f};
+  if (ix < D.nx && iy < D.ny) {
+    const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
     const float m = I.m[i];
     I.m_res[i] = m;
     const float a = m - I.m_pre[i];
@@ -251,9 +314,15 @@ __global__ void __launch_bounds__(kThreads)
       const float c = m - I.I0[i];
       v[2] = c * c;
     }
+    if (tv) {
+      const float g =
+          tv_grad<float>(TileAt<1, k3D>{t, tx + 1, ty + 1, k3D ? 1 : 0}, k3D);
+      v[3] = g * g;
+    }
   }
-  double tot[3];
-  if (grid_sum<kThreads, 3>(v, I.partials, I.counter, gridDim.x, tot)) {
+  double tot[4];
+  if (grid_sum<kThreads, 4>(v, I.partials, I.counter, inst_block(),
+                            inst_blocks(), tot)) {
     if (threadIdx.x == 0) {
       Scalars *s = I.s;
       const double N = (double)D.nx * D.ny * D.nz;
@@ -266,63 +335,99 @@ __global__ void __launch_bounds__(kThreads)
         s->done = 1;
       } else {
         s->d_tv = sqrt(tot[1]);
+        s->tv_coef = s->alpha * s->d_tv / sqrt(tot[3]);
+        s->tv_coef_f = (float)s->tv_coef;
       }
     }
   }
 }
 
-__device__ __forceinline__ const float *tv_src(const Inst &I, int step) {
-  return step == 0 ? I.m : ((step & 1) ? I.tv_b : I.tv_c);
-}
-__device__ __forceinline__ float *tv_dst(const Inst &I, int step) {
-  return (step & 1) ? I.tv_c : I.tv_b;
-}
-
-// ||v||^2 of TV step `step`; last block sets tv_coef = alpha*d/||v||.
+// TV step `step` (imgTVGradMin.cpp:62-108): m' = m - tv_coef*v(m) into the
+// other buffer, and ||v(m')|| for the next step.  The last step (when there
+// are at least two, so that it reads a work buffer) also does the work of
+// k_finish_iter: positivity, dg, alpha/beta, and writes m' back to the
+// image and to m_pre.
+template <bool k3D>
 __global__ void __launch_bounds__(kThreads)
-    k_tv_norm_batch(const Inst *__restrict__ insts, Dims D, int step) {
-  const Inst &I = insts[blockIdx.y];
-  if (inst_done(I) || step >= I.s->ng) return;
-  int ix, iy, iz;
-  float v[1] = {0.f};
-  const Img<float> u{tv_src(I, step), D.nx, D.ny, D.nz};
-  if (tile_voxel(D.nx, D.ny, ix, iy, iz)) {
-    const float g = tv_grad(u, ix, iy, iz);
-    v[0] = g * g;
-  }
-  double tot[1];
-  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, gridDim.x, tot))
-    if (threadIdx.x == 0) {
-      I.s->tv_coef = I.s->alpha * I.s->d_tv / sqrt(tot[0]);
-      I.s->tv_coef_f = (float)I.s->tv_coef;
-    }
-}
-
-__global__ void __launch_bounds__(kThreads)
-    k_tv_update_batch(const Inst *__restrict__ insts, Dims D, int step) {
-  const Inst &I = insts[blockIdx.y];
-  if (inst_done(I) || step >= I.s->ng) return;
-  int ix, iy, iz;
-  if (!tile_voxel(D.nx, D.ny, ix, iy, iz)) return;
-  const float *src = tv_src(I, step);
-  const Img<float> u{src, D.nx, D.ny, D.nz};
-  const float g = tv_grad(u, ix, iy, iz);
-  const long long i = ((long long)iz * D.ny + iy) * D.nx + ix;
-  const float coef = I.s->tv_coef_f;
-  tv_dst(I, step)[i] = src[i] - coef * g;
-}
-
-// End of an iteration (ASD_POCS_cuda.m:155-170 after TV): positivity
-// (imgTVGradMin.cpp:110-116), dg, alpha/beta updates, next k.
-__global__ void __launch_bounds__(kThreads)
-    k_finish_iter(const Inst *__restrict__ insts, Dims D) {
-  const Inst &I = insts[blockIdx.y];
+    k_tv_step(const Inst *__restrict__ insts, Dims D, int step) {
+  __shared__ Tile<2, k3D> t2;
+  __shared__ Tile<1, k3D> t1;
+  const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
+  if (step >= ng) return;
+  const bool last = step == ng - 1;
+  const bool fused_finish = last && ng >= 2;
+  const float coef = I.s->tv_coef_f;
+  const float *src = tv_src(I, step);
+  int x0, y0, z;
+  tile_origin(D, x0, y0, z);
+  load_tile(t2, src, D, x0, y0, z);
+  __syncthreads();
+  // m' on the tile and a one-voxel halo (zero outside the image)
+  {
+    constexpr int W = Tile<1, k3D>::W, Hh = Tile<1, k3D>::Hh, Dd = Tile<1, k3D>::D;
+    for (int k = threadIdx.x; k < W * Hh * Dd; k += kThreads) {
+      const int tx = k % W, ty = (k / W) % Hh, tz = k / (W * Hh);
+      const int x = x0 - 1 + tx, y = y0 - 1 + ty, zz = k3D ? z - 1 + tz : z;
+      float v = 0.f;
+      if (x >= 0 && y >= 0 && zz >= 0 && x < D.nx && y < D.ny && zz < D.nz) {
+        const TileAt<2, k3D> u{t2, tx + 1, ty + 1, k3D ? tz + 1 : 0};
+        v = u(0, 0, 0) - coef * tv_grad<float>(u, k3D);
+      }
+      t1.v[tz][ty][tx] = v;
+    }
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
+  const int ix = x0 + tx, iy = y0 + ty;
+  float v[1] = {0.f};
+  if (ix < D.nx && iy < D.ny) {
+    const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
+    const TileAt<1, k3D> u{t1, tx + 1, ty + 1, k3D ? 1 : 0};
+    const float mn = u(0, 0, 0);
+    if (fused_finish) {
+      const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
+      const float f0 = I.m[i];
+      const float dlt = mc - f0;
+      v[0] = dlt * dlt;
+      I.m[i] = mc;
+      I.m_pre[i] = mc;
+    } else {
+      tv_dst(I, step)[i] = mn;
+      if (!last) {
+        const float g = tv_grad<float>(u, k3D);
+        v[0] = g * g;
+      }
+    }
+  }
+  double tot[1];
+  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, inst_block(),
+                            inst_blocks(), tot)) {
+    if (threadIdx.x == 0) {
+      Scalars *s = I.s;
+      if (fused_finish) {
+        finish_scalars(s, tot[0]);
+      } else if (!last) {
+        s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
+        s->tv_coef_f = (float)s->tv_coef;
+      }
+    }
+  }
+}
+
+// End of an iteration for instances whose last TV step did not finish it
+// (ng == 0 or ng == 1): positivity (after a TV step), dg, alpha/beta, k.
+__global__ void __launch_bounds__(kThreads)
+    k_finish_iter(const Inst *__restrict__ insts, Dims D) {
+  const Inst &I = insts[blockIdx.z];
+  if (inst_done(I)) return;
+  const int ng = I.s->ng;
+  if (ng >= 2) return;  // finished by the last TV step
   int ix, iy, iz;
   float v[1] = {0.f};
-  if (tile_voxel(D.nx, D.ny, ix, iy, iz)) {
-    const long long i = ((long long)iz * D.ny + iy) * D.nx + ix;
+  if (tile_voxel(D.nx, D.ny, D.nz, ix, iy, iz)) {
+    const unsigned i = ((unsigned)iz * D.ny + iy) * D.nx + ix;
     const float f0 = I.m[i];
     float mn = f0;
     if (ng > 0) {
@@ -335,20 +440,9 @@ __global__ void __launch_bounds__(kThreads)
     I.m_pre[i] = mn;
   }
   double tot[1];
-  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, gridDim.x, tot)) {
-    if (threadIdx.x == 0) {
-      Scalars *s = I.s;
-      s->dg = sqrt(tot[0]);
-      if (s->dg > s->r_max * s->dp && sqrt(s->dd2) > s->epsilon)
-        s->alpha = s->alpha * s->alpha_red;
-      s->beta = s->beta * s->beta_red;
-      s->beta_f = (float)s->beta;
-      if (s->k >= s->maxIter) {
-        s->done = 1;
-      } else {
-        s->k = s->k + 1;
-      }
-    }
+  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, inst_block(),
+                            inst_blocks(), tot)) {
+    if (threadIdx.x == 0) finish_scalars(I.s, tot[0]);
   }
 }
 
@@ -377,25 +471,30 @@ cudaError_t launch_iter_begin(const Inst *, int, cudaStream_t) {
 
 cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
                                cudaStream_t st) {
-  k_after_sweep<<<dim3(tiles(d.nx, d.ny, d.nz), batch), kThreads, 0, st>>>(
-      insts, d);
+  const dim3 grid = tile_grid(d.nx, d.ny, d.nz, batch);
+  if (d.nz > 1)
+    k_after_sweep<true><<<grid, kThreads, 0, st>>>(insts, d);
+  else
+    k_after_sweep<false><<<grid, kThreads, 0, st>>>(insts, d);
   return cudaGetLastError();
 }
 
 cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
                            int step, int ng, cudaStream_t st) {
   (void)ng;
-  const dim3 grid(tiles(d.nx, d.ny, d.nz), batch);
-  k_tv_norm_batch<<<grid, kThreads, 0, st>>>(insts, d, step);
-  k_tv_update_batch<<<grid, kThreads, 0, st>>>(insts, d, step);
+  const dim3 grid = tile_grid(d.nx, d.ny, d.nz, batch);
+  if (d.nz > 1)
+    k_tv_step<true><<<grid, kThreads, 0, st>>>(insts, d, step);
+  else
+    k_tv_step<false><<<grid, kThreads, 0, st>>>(insts, d, step);
   return cudaGetLastError();
 }
 
 cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
                                int ng, cudaStream_t st) {
   (void)ng;
-  k_finish_iter<<<dim3(tiles(d.nx, d.ny, d.nz), batch), kThreads, 0, st>>>(
-      insts, d);
+  k_finish_iter<<<tile_grid(d.nx, d.ny, d.nz, batch), kThreads, 0, st>>>(insts,
+                                                                         d);
   return cudaGetLastError();
 }
 

@@ -564,25 +564,45 @@ struct Pick2 {
   }
 };
 
-// chord_planar without divergent control flow (same result).
+// chord_planar without divergent control flow (same result).  The faces are
+// relabelled so the dominant in-plane axis comes first ("primary", tested
+// first by the reference) and the other second; the chord is then
+//   both primary faces hit -> primary-  to primary+,
+//   one primary face hit   -> that point to the first secondary face hit,
+//   none                   -> secondary- to secondary+,
+// which is the reference's "first two hits" rule for a convex pixel.  Every
+// point coordinate is the same float expression as in the reference, and the
+// squared length is a sum of the same two terms (in swapped order when y is
+// primary, which does not change an IEEE sum).
 ASD_HD float chord_planar_bf(const float4 A, float rx, float ry, float dz) {
   const float a = A.x, b = A.y;
-  const float tX = A.z * (-rx) + ry, uX = A.z * 0.5f;
-  const float tY = A.w * (-ry) + rx, uY = A.w * 0.5f;
-  const float xm = tX - uX, xp = tX + uX, ym = tY - uY, yp = tY + uY;
-  const bool fxm = fabsf(xm) <= 0.5f, fxp = fabsf(xp) <= 0.5f;
-  const bool fym = fabsf(ym) <= 0.5f, fyp = fabsf(yp) <= 0.5f;
   const bool xfirst = fabsf(a) > fabsf(b);
-  Pick2 p;
-  p.n = 0;
-  p.p0x = p.p0y = p.p1x = p.p1y = p.p0z = p.p1z = 0.f;
-  // first axis pair, then the other
-  p.take(xfirst ? fxm : fym, xfirst ? -0.5f : ym, xfirst ? xm : -0.5f, 0.f);
-  p.take(xfirst ? fxp : fyp, xfirst ? 0.5f : yp, xfirst ? xp : 0.5f, 0.f);
-  p.take(xfirst ? fym : fxm, xfirst ? ym : -0.5f, xfirst ? -0.5f : xm, 0.f);
-  p.take(xfirst ? fyp : fxp, xfirst ? yp : 0.5f, xfirst ? 0.5f : xp, 0.f);
-  const float e0 = p.p1x - p.p0x, e1 = p.p1y - p.p0y;
-  const float l = p.n >= 2 ? sqrtf(e0 * e0 + e1 * e1) : 0.0f;
+  const float s1 = xfirst ? A.z : A.w, s2 = xfirst ? A.w : A.z;
+  const float r1 = xfirst ? rx : ry, r2 = xfirst ? ry : rx;
+  const float t1 = s1 * (-r1) + r2, u1 = s1 * 0.5f;
+  const float t2 = s2 * (-r2) + r1, u2 = s2 * 0.5f;
+  const float pm = t1 - u1, pp = t1 + u1;  // primary faces, at -0.5 / +0.5
+  const float sm = t2 - u2, sp = t2 + u2;  // secondary faces
+  const bool fpm = fabsf(pm) <= 0.5f, fpp = fabsf(pp) <= 0.5f;
+  const bool fsm = fabsf(sm) <= 0.5f, fsp = fabsf(sp) <= 0.5f;
+  float e1, e2;
+  bool ok;
+  if (fpm && fpp) {
+    e1 = 1.0f;  // 0.5 - (-0.5)
+    e2 = pp - pm;
+    ok = true;
+  } else if (fpm || fpp) {
+    const float p0a = fpm ? -0.5f : 0.5f, p0b = fpm ? pm : pp;
+    const float q1a = fsm ? sm : sp, q1b = fsm ? -0.5f : 0.5f;
+    e1 = q1a - p0a;
+    e2 = q1b - p0b;
+    ok = fsm || fsp;
+  } else {
+    e1 = sp - sm;
+    e2 = 1.0f;
+    ok = fsm && fsp;
+  }
+  const float l = ok ? sqrtf(e1 * e1 + e2 * e2) : 0.0f;
   if (a == 0) return b == 0 ? (fabsf(ry) <= 0.5f ? dz : 0.0f) : 1.0f;
   if (b == 0) return 1.0f;
   return l;

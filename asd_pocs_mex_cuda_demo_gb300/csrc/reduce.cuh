@@ -41,14 +41,14 @@ __device__ __forceinline__ void block_sum_f(const float (&v)[K], float (&out)[K]
 }
 
 // Grid-wide deterministic sum of K values per thread over the blocks
-// blockIdx.x = 0..nblocks-1 (blockIdx.y selects an independent reduction
-// through `partials`/`counter`).  `partials` holds nblocks*K doubles.
-// Returns true in every thread of the last block, where `tot` then holds the
-// totals; other blocks return false.
+// bid = 0..nblocks-1 of one reduction (other grid dimensions select
+// independent reductions through `partials`/`counter`).  `partials` holds
+// nblocks*K doubles.  Returns true in every thread of the last block, where
+// `tot` then holds the totals; other blocks return false.
 template <int NT, int K>
 __device__ __forceinline__ bool grid_sum(const float (&v)[K], double *partials,
-                                         unsigned *counter, int nblocks,
-                                         double (&tot)[K]) {
+                                         unsigned *counter, int bid,
+                                         int nblocks, double (&tot)[K]) {
   __shared__ float shf[K * (NT / 32)];
   __shared__ double sh[K * (NT / 32)];
   __shared__ bool last;
@@ -56,7 +56,7 @@ __device__ __forceinline__ bool grid_sum(const float (&v)[K], double *partials,
   block_sum_f<NT, K>(v, bs, shf);
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int k = 0; k < K; k++) partials[(long long)blockIdx.x * K + k] = (double)bs[k];
+    for (int k = 0; k < K; k++) partials[(long long)bid * K + k] = (double)bs[k];
     __threadfence();
     const unsigned t = atomicAdd(counter, 1u);
     last = (t == (unsigned)nblocks - 1);
