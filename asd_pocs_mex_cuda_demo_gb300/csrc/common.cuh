@@ -81,7 +81,7 @@ struct Inst {
   float *tv_b, *tv_c;        // TV ping-pong buffers
   float *cor;                // correction of the current view, na*nb
   double *rmse;              // [maxIter]
-  double *partials;          // reduction partials [blocks * 3]
+  double *partials;          // reduction partials [blocks * kMaxReduceK]
   unsigned *counter;         // reduction ticket
   Scalars *s;
 };
@@ -118,6 +118,6 @@ __device__ __forceinline__ int inst_block() {
   return blockIdx.x + gridDim.x * blockIdx.y;
 }
 __device__ __forceinline__ int inst_blocks() { return gridDim.x * gridDim.y; }
-constexpr int kMaxReduceK = 3;          // values reduced together
+constexpr int kMaxReduceK = 4;          // values reduced together (partials sizing)
 
 }  // namespace asd

@@ -49,6 +49,7 @@ template <int NT, int K>
 __device__ __forceinline__ bool grid_sum(const float (&v)[K], double *partials,
                                          unsigned *counter, int bid,
                                          int nblocks, double (&tot)[K]) {
+  static_assert(K <= kMaxReduceK, "partials are sized for kMaxReduceK values");
   __shared__ float shf[K * (NT / 32)];
   __shared__ double sh[K * (NT / 32)];
   __shared__ bool last;
@@ -113,7 +114,7 @@ __device__ __forceinline__ bool grid_sum_d(double v, double *partials,
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < NT / 32; w++) s += sh[w];
-    partials[blockIdx.x] = s;
+    partials[inst_block()] = s;
     __threadfence();
     last = atomicAdd(counter, 1u) == (unsigned)nblocks - 1;
   }
