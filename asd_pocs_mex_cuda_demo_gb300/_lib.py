@@ -75,6 +75,9 @@ SIGNATURES = [
                                  C.c_int, _D]),
     ("asdpocs_tv_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
                                     C.c_double, C.c_int, C.c_int, C.c_void_p]),
+    ("asdpocs_tv_device_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                            C.c_int, C.c_double, C.c_int, C.c_int,
+                                            C.c_void_p]),
     ("asdpocs_options_default", None, [C.POINTER(Options)]),
     ("asdpocs_plan_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int,
                                       C.POINTER(Geometry), _D, C.POINTER(Options),

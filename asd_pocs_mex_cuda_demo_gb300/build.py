@@ -31,6 +31,7 @@ UNITS = {
     "kernels_proj.cu": ["-fmad=false"],
     "kernels_tv.cu": [],
     "host_api.cu": [],
+    "noalloc.cu": [],
 }
 
 

@@ -121,6 +121,20 @@ int imgTVGradMin3D(const double *img, double *img_out, int Nx, int Ny, int Nz,
 int asdpocs_tv_device(float *img_d, const float *img_old_d, int nx, int ny,
                       int nz, double alpha, int nTVIter, int pos, void *stream);
 
+/* Allocation-free form of asdpocs_tv_device (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc -- an external
+ * allocator that owns device memory, a fixed memory budget, or a real-time
+ * loop that must not stall on an allocation: the work images and reduction
+ * scratch live in a fixed array of about 8.5 MB that every GPU loading the
+ * library holds until exit.  Images are limited to nx*ny*nz <= 1,048,576
+ * voxels (larger ones are rejected with ASDPOCS_ERR_ARG).  Asynchronous on
+ * `stream`; the first call on a device looks up the array's address and
+ * should come before any stream capture.  All calls share the array, so
+ * calls that overlap on the GPU race. */
+int asdpocs_tv_device_noalloc(float *img_d, const float *img_old_d, int nx,
+                              int ny, int nz, double alpha, int nTVIter,
+                              int pos, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* ASD-POCS reconstruction jobs (device resident)                      */
 /* ------------------------------------------------------------------ */
