@@ -8,7 +8,7 @@ bytes per launch are then (FP32):
 
 * fused Ax  (SART forward step) : 4*nnz + 8*na*nb   (m per nonzero; P in, cor out)
 * fused Atx (SART backward step): 4*nnz + 8*N       (cor per nonzero; m in, m out)
-* one TV step (two passes)      : 12*N              (read, re-read, write)
+* one TV step (one fused pass)  : 8*N               (read m, write m')
 """
 from __future__ import annotations
 
@@ -76,4 +76,4 @@ def ax_bytes(nnz, M):
 
 
 def tv_step_bytes(N):
-    return 12 * N
+    return 8 * N
