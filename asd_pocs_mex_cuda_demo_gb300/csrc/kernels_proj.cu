@@ -42,7 +42,7 @@ __device__ __forceinline__ void ax_warp(const ViewGeo &G, const Dims &D,
   ys = 0.f;
   ss = 0.f;
   if (D.nz == 1 && zd == 0.0f)
-    ray_columns_planar<false>(R, lane, 32, ld, ys, ss);
+    ray_columns_planar_fast(R, lane, 32, ld, ys, ss);
   else
     ray_columns<false>(R, lane, 32, ld, ys, ss);
   ys = warp_sum(ys);
@@ -173,12 +173,18 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   // both in-plane components (an axis-parallel ray's reference chord ignores
   // one coordinate and is 1 for every voxel of the window)
   bool narrow = true;
+  bool allx = true, ally = true;  // every ray of the window x- / y-dominant
   if (staged) {
     for (int k = threadIdx.x; k < nA; k += kAtxThreads) {
       const float4 A = ray_tab_a(G, G.y_det[amin + k]);
       narrow = narrow && A.x != 0.0f && A.y != 0.0f;
+      const bool xf = fabsf(A.x) > fabsf(A.y);
+      allx = allx && xf;
+      ally = ally && !xf;
       sh.tabA[k] = A;
     }
+    allx = __syncthreads_and(allx);
+    ally = __syncthreads_and(ally);
     for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads) {
       const float v = yl((long long)(bmin + k / nA) * D.na + amin + k % nA);
       narrow = narrow && isfinite(v);
@@ -211,6 +217,23 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   const int kA = __reduce_max_sync(0xffffffffu, cntA);
   const int kB = __reduce_max_sync(0xffffffffu, cntB);
   const int a_off = lo - amin;
+  if (kPlanar && narrow && (allx || ally)) {
+    // common case: no axis-parallel ray and one dominant axis for the whole
+    // window; the chord needs no per-ray selection
+    const int j0 = has ? a_off : 0;
+    for (int ka = 0; ka < kA; ka++) {
+      const bool on = ka < cntA;
+      const int j = on ? j0 + ka : 0;
+      const float4 A = sh.tabA[j];
+      const float l = allx ? chord_planar_axis<true>(A, rx, ry)
+                           : chord_planar_axis<false>(A, rx, ry);
+      if (on) {
+        acc += l * sh.ys[j];
+        accl += l;
+      }
+    }
+    return;
+  }
   for (int kb = 0; kb < kB; kb++) {
     const bool onb = kb < cntB;
     const int ib = w.b0 + kb;

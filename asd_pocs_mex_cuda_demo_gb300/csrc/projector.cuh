@@ -240,6 +240,63 @@ ASD_HD void ray_columns_planar(const RayMarch &R, int first,
   }
 }
 
+// The kernels' form of ray_columns_planar<false>: the same cells, weights
+// and accumulation order, computed without control flow.  Each column yields
+// at most two pieces (lower and upper row) with their validity; a group of
+// U columns is evaluated first, then its (predicated) loads are issued
+// together, then the pieces are accumulated in order -- so a lane keeps 2U
+// loads in flight instead of waiting on each column in turn.
+template <int U = 4, class Loader>
+ASD_HD void ray_columns_planar_fast(const RayMarch &R, int first, int step,
+                                    Loader ld, float &ys, float &ss) {
+  const bool pos = R.slope1 >= 0;
+  for (int iu0 = first; iu0 < R.nu; iu0 += U * step) {
+    float w_lo[U], w_hi[U], x_lo[U], x_hi[U];
+    unsigned i_lo[U], i_hi[U];
+    bool f_lo[U], f_hi[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      const int iu = iu0 + k * step;
+      const float uu1 = (float)(iu - R.nu2);
+      const float uu2 = uu1 + 1;
+      const float ua = pos ? uu1 : uu2, ub = pos ? uu2 : uu1;
+      const float v1 = R.vs + R.slope1 * (ua - R.us) + R.nv2;
+      const float v2 = R.vs + R.slope1 * (ub - R.us) + R.nv2;
+      const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
+      const bool split = cv1 != cv2;
+      const bool mid = cv2 > 0 && cv2 < R.nv;
+      const bool in = iu < R.nu;
+      f_lo[k] = in && cv1 >= 0 && cv1 < R.nv &&
+                (split ? (mid || cv2 == R.nv) : true);
+      f_hi[k] = in && split && cv2 >= 0 && cv2 < R.nv && (mid || cv2 == 0);
+      const float d = v2 - v1;
+      const float l = sqrtf(d * d + 1);
+      const float rv = fast_div(cv2 - v1, d);
+      w_lo[k] = split ? rv * l : l;
+      w_hi[k] = (1 - rv) * l;
+      const unsigned base = (unsigned)iu * R.su;
+      i_lo[k] = base + (unsigned)cv1 * R.sv;
+      i_hi[k] = base + (unsigned)cv2 * R.sv;
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      x_lo[k] = f_lo[k] ? ld(i_lo[k]) : 0.f;
+      x_hi[k] = f_hi[k] ? ld(i_hi[k]) : 0.f;
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      if (f_lo[k]) {
+        ys += w_lo[k] * x_lo[k];
+        ss += w_lo[k];
+      }
+      if (f_hi[k]) {
+        ys += w_hi[k] * x_hi[k];
+        ss += w_hi[k];
+      }
+    }
+  }
+}
+
 // Warp-wide sum; the xor butterfly leaves bit-identical totals in every lane
 // (IEEE addition is commutative).
 __device__ __forceinline__ float warp_sum(float v) {
@@ -606,6 +663,38 @@ ASD_HD float chord_planar_bf(const float4 A, float rx, float ry, float dz) {
   if (a == 0) return b == 0 ? (fabsf(ry) <= 0.5f ? dz : 0.0f) : 1.0f;
   if (b == 0) return 1.0f;
   return l;
+}
+
+// chord_planar_bf for a ray known to have a != 0, b != 0 and the given
+// dominant axis (XF: |a| > |b|): the same expressions without the selects.
+template <bool XF>
+ASD_HD float chord_planar_axis(const float4 A, float rx, float ry) {
+  const float s1 = XF ? A.z : A.w, s2 = XF ? A.w : A.z;
+  const float r1 = XF ? rx : ry, r2 = XF ? ry : rx;
+  const float t1 = s1 * (-r1) + r2, u1 = s1 * 0.5f;
+  const float t2 = s2 * (-r2) + r1, u2 = s2 * 0.5f;
+  const float pm = t1 - u1, pp = t1 + u1;
+  const float sm = t2 - u2, sp = t2 + u2;
+  const bool fpm = fabsf(pm) <= 0.5f, fpp = fabsf(pp) <= 0.5f;
+  const bool fsm = fabsf(sm) <= 0.5f, fsp = fabsf(sp) <= 0.5f;
+  float e1, e2;
+  bool ok;
+  if (fpm && fpp) {
+    e1 = 1.0f;
+    e2 = pp - pm;
+    ok = true;
+  } else if (fpm || fpp) {
+    const float p0a = fpm ? -0.5f : 0.5f, p0b = fpm ? pm : pp;
+    const float q1a = fsm ? sm : sp, q1b = fsm ? -0.5f : 0.5f;
+    e1 = q1a - p0a;
+    e2 = q1b - p0b;
+    ok = fsm || fsp;
+  } else {
+    e1 = sp - sm;
+    e2 = 1.0f;
+    ok = fsm && fsp;
+  }
+  return ok ? sqrtf(e1 * e1 + e2 * e2) : 0.0f;
 }
 
 // chord3_tab without divergent control flow in the common case (the a == 0

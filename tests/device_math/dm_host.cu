@@ -40,7 +40,7 @@ extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,
       if (planar && exact)
         ray_columns_planar<true>(R, l, lanes, ld, a, b);
       else if (planar)
-        ray_columns_planar<false>(R, l, lanes, ld, a, b);
+        ray_columns_planar_fast(R, l, lanes, ld, a, b);
       else if (exact)
         ray_columns<true>(R, l, lanes, ld, a, b);
       else
@@ -91,8 +91,15 @@ extern "C" void dm_atx(float *x, const float *yv, float *sc, float c, float s,
             const float cc = zd[ib] - 0.0f;
             for (int ia = w.a0; ia <= w.a1; ia++) {
               const long long k = (long long)ib * na + ia;
-              const float l = planar ? chord_planar_bf(tA[ia], rx, ry, dz)
-                                     : chord3_bf(tA[ia], tC[k], cc, rx, ry, rz, dz);
+              float l;
+              if (planar && tA[ia].x != 0.0f && tA[ia].y != 0.0f)
+                l = fabsf(tA[ia].x) > fabsf(tA[ia].y)
+                        ? chord_planar_axis<true>(tA[ia], rx, ry)
+                        : chord_planar_axis<false>(tA[ia], rx, ry);
+              else if (planar)
+                l = chord_planar_bf(tA[ia], rx, ry, dz);
+              else
+                l = chord3_bf(tA[ia], tC[k], cc, rx, ry, rz, dz);
               acc += l * yv[k];
               accl += l;
             }
