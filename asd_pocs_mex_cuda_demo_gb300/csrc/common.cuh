@@ -113,6 +113,36 @@ __device__ __forceinline__ bool tile_voxel(int nx, int ny, int nz, int &ix,
   return ix < nx && iy < ny;
 }
 
+// Batched voxel kernels give each block a group of kTilesPerBlock tile rows
+// (same x tile, consecutive y tiles of one z slice) so that the block's
+// fixed cost -- instance and view set-up, dependent loads -- is paid once per
+// group.  Grids are (x tiles, y groups * nz, instances).
+constexpr int kTilesPerBlock = 4;
+
+__host__ __device__ inline dim3 group_grid(int nx, int ny, int nz, int batch) {
+  const int ty = (ny + kTileY - 1) / kTileY;
+  const int gy = (ty + kTilesPerBlock - 1) / kTilesPerBlock;
+  return dim3((nx + kTileX - 1) / kTileX, gy * nz, batch);
+}
+
+// Origin of tile t (0 <= t < kTilesPerBlock) of this block's group; false
+// when the group has fewer tiles (block-uniform).
+__device__ __forceinline__ bool group_tile(int ny, int nz, int t, int &x0,
+                                           int &y0, int &z) {
+  const int ty = (ny + kTileY - 1) / kTileY;
+  int g = blockIdx.y;
+  z = 0;
+  if (nz > 1) {
+    const int gy = (ty + kTilesPerBlock - 1) / kTilesPerBlock;
+    z = g / gy;
+    g -= z * gy;
+  }
+  const int tyi = g * kTilesPerBlock + t;
+  x0 = blockIdx.x * kTileX;
+  y0 = tyi * kTileY;
+  return tyi < ty;
+}
+
 // Index of this block among the blocks of its instance, and their number.
 __device__ __forceinline__ int inst_block() {
   return blockIdx.x + gridDim.x * blockIdx.y;

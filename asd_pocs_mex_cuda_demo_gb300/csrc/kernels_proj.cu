@@ -186,7 +186,8 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
     allx = __syncthreads_and(allx);
     ally = __syncthreads_and(ally);
     for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads) {
-      const float v = yl((long long)(bmin + k / nA) * D.na + amin + k % nA);
+      const int r = kPlanar ? 0 : k / nA, c = kPlanar ? k : k - r * nA;
+      const float v = yl((long long)(bmin + r) * D.na + amin + c);
       narrow = narrow && isfinite(v);
       sh.ys[k] = v;
     }
@@ -319,18 +320,25 @@ __global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 3)
   const Inst &I = insts[blockIdx.z];
   if (((volatile int *)&I.s->done)[0]) return;
   const ViewGeo G = view_of(I, view);
-  int ix, iy, iz;
-  const bool valid = tile_voxel(D, ix, iy, iz);
-  float acc, accl;
-  const float *cor = I.cor;
-  atx_block_sum<kPlanar>(G, D, valid, ix, iy, iz, sh,
-                         [&](long long i) { return cor[i]; }, acc, accl);
-  if (!valid) return;
-  const float bp = acc * G.scale, scv = accl * G.scale;
   const float beta = I.s->beta_f;
-  const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
-  const float mn = I.m[idx] + beta * __fdividef(bp, scv == 0.f ? 1.f : scv);
-  I.m[idx] = mn < 0.f ? 0.f : mn;
+  float *m = I.m;
+  const float *cor = I.cor;
+  for (int t = 0; t < kTilesPerBlock; t++) {
+    int x0, y0, iz;
+    if (!group_tile(D.ny, D.nz, t, x0, y0, iz)) break;
+    const int ix = x0 + threadIdx.x % kTileX, iy = y0 + threadIdx.x / kTileX;
+    const bool valid = ix < D.nx && iy < D.ny;
+    float acc, accl;
+    atx_block_sum<kPlanar>(G, D, valid, ix, iy, iz, sh,
+                           [&](long long i) { return cor[i]; }, acc, accl);
+    if (valid) {
+      const float bp = acc * G.scale, scv = accl * G.scale;
+      const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+      const float mn = m[idx] + beta * __fdividef(bp, scv == 0.f ? 1.f : scv);
+      m[idx] = mn < 0.f ? 0.f : mn;
+    }
+    __syncthreads();  // the staging arrays are reused by the next tile
+  }
 }
 
 }  // namespace
@@ -364,7 +372,7 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
                             int view, cudaStream_t st) {
-  const dim3 grid = tile_grid(d.nx, d.ny, d.nz, batch);
+  const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz == 1 && d.nb == 1)
     k_sart_atx<true><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
   else

@@ -256,19 +256,6 @@ __device__ __forceinline__ float *tv_dst(const Inst &I, int step) {
   return (step & 1) ? I.tv_c : I.tv_b;
 }
 
-__device__ __forceinline__ void tile_origin(const Dims &D, int &x0, int &y0,
-                                            int &z) {
-  int by = blockIdx.y;
-  z = 0;
-  if (D.nz > 1) {
-    const int ty = (D.ny + kTileY - 1) / kTileY;
-    z = by / ty;
-    by -= z * ty;
-  }
-  x0 = blockIdx.x * kTileX;
-  y0 = by * kTileY;
-}
-
 // End-of-iteration scalars (ASD_POCS_cuda.m:166-170) by the last block.
 __device__ __forceinline__ void finish_scalars(Scalars *s, double dg2) {
   s->dg = sqrt(dg2);
@@ -293,32 +280,35 @@ __global__ void __launch_bounds__(kThreads)
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const bool tv = I.s->ng > 0;
-  int x0, y0, z;
-  tile_origin(D, x0, y0, z);
-  if (tv) {
-    load_tile(t, I.m, D, x0, y0, z);
-    __syncthreads();
-  }
   const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
-  const int ix = x0 + tx, iy = y0 + ty;
   float v[4] = {0.f, 0.f, 0.f, 0.f};
-  if (ix < D.nx && iy < D.ny) {
-    const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
-    const float m = I.m[i];
-    I.m_res[i] = m;
-    const float a = m - I.m_pre[i];
-    const float b = m - I.m_k1[i];
-    v[0] = a * a;
-    v[1] = b * b;
-    if (I.I0) {
-      const float c = m - I.I0[i];
-      v[2] = c * c;
-    }
+  for (int g = 0; g < kTilesPerBlock; g++) {
+    int x0, y0, z;
+    if (!group_tile(D.ny, D.nz, g, x0, y0, z)) break;
     if (tv) {
-      const float g =
-          tv_grad<float>(TileAt<1, k3D>{t, tx + 1, ty + 1, k3D ? 1 : 0}, k3D);
-      v[3] = g * g;
+      load_tile(t, I.m, D, x0, y0, z);
+      __syncthreads();
     }
+    const int ix = x0 + tx, iy = y0 + ty;
+    if (ix < D.nx && iy < D.ny) {
+      const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
+      const float m = I.m[i];
+      I.m_res[i] = m;
+      const float a = m - I.m_pre[i];
+      const float b = m - I.m_k1[i];
+      v[0] += a * a;
+      v[1] += b * b;
+      if (I.I0) {
+        const float c = m - I.I0[i];
+        v[2] += c * c;
+      }
+      if (tv) {
+        const float gr =
+            tv_grad<float>(TileAt<1, k3D>{t, tx + 1, ty + 1, k3D ? 1 : 0}, k3D);
+        v[3] += gr * gr;
+      }
+    }
+    __syncthreads();  // the tile is reused by the next group member
   }
   double tot[4];
   if (grid_sum<kThreads, 4>(v, I.partials, I.counter, inst_block(),
@@ -360,46 +350,50 @@ __global__ void __launch_bounds__(kThreads)
   const bool fused_finish = last && ng >= 2;
   const float coef = I.s->tv_coef_f;
   const float *src = tv_src(I, step);
-  int x0, y0, z;
-  tile_origin(D, x0, y0, z);
-  load_tile(t2, src, D, x0, y0, z);
-  __syncthreads();
-  // m' on the tile and a one-voxel halo (zero outside the image)
-  {
-    constexpr int W = Tile<1, k3D>::W, Hh = Tile<1, k3D>::Hh, Dd = Tile<1, k3D>::D;
-    for (int k = threadIdx.x; k < W * Hh * Dd; k += kThreads) {
-      const int tx = k % W, ty = (k / W) % Hh, tz = k / (W * Hh);
-      const int x = x0 - 1 + tx, y = y0 - 1 + ty, zz = k3D ? z - 1 + tz : z;
-      float v = 0.f;
-      if (x >= 0 && y >= 0 && zz >= 0 && x < D.nx && y < D.ny && zz < D.nz) {
-        const TileAt<2, k3D> u{t2, tx + 1, ty + 1, k3D ? tz + 1 : 0};
-        v = u(0, 0, 0) - coef * tv_grad<float>(u, k3D);
-      }
-      t1.v[tz][ty][tx] = v;
-    }
-  }
-  __syncthreads();
+  float *dst = tv_dst(I, step);
   const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
-  const int ix = x0 + tx, iy = y0 + ty;
   float v[1] = {0.f};
-  if (ix < D.nx && iy < D.ny) {
-    const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
-    const TileAt<1, k3D> u{t1, tx + 1, ty + 1, k3D ? 1 : 0};
-    const float mn = u(0, 0, 0);
-    if (fused_finish) {
-      const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
-      const float f0 = I.m[i];
-      const float dlt = mc - f0;
-      v[0] = dlt * dlt;
-      I.m[i] = mc;
-      I.m_pre[i] = mc;
-    } else {
-      tv_dst(I, step)[i] = mn;
-      if (!last) {
-        const float g = tv_grad<float>(u, k3D);
-        v[0] = g * g;
+  for (int g = 0; g < kTilesPerBlock; g++) {
+    int x0, y0, z;
+    if (!group_tile(D.ny, D.nz, g, x0, y0, z)) break;
+    load_tile(t2, src, D, x0, y0, z);
+    __syncthreads();
+    // m' on the tile and a one-voxel halo (zero outside the image)
+    {
+      constexpr int W = Tile<1, k3D>::W, Hh = Tile<1, k3D>::Hh, Dd = Tile<1, k3D>::D;
+      for (int k = threadIdx.x; k < W * Hh * Dd; k += kThreads) {
+        const int hx = k % W, hy = (k / W) % Hh, hz = k / (W * Hh);
+        const int x = x0 - 1 + hx, y = y0 - 1 + hy, zz = k3D ? z - 1 + hz : z;
+        float val = 0.f;
+        if (x >= 0 && y >= 0 && zz >= 0 && x < D.nx && y < D.ny && zz < D.nz) {
+          const TileAt<2, k3D> u{t2, hx + 1, hy + 1, k3D ? hz + 1 : 0};
+          val = u(0, 0, 0) - coef * tv_grad<float>(u, k3D);
+        }
+        t1.v[hz][hy][hx] = val;
       }
     }
+    __syncthreads();
+    const int ix = x0 + tx, iy = y0 + ty;
+    if (ix < D.nx && iy < D.ny) {
+      const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
+      const TileAt<1, k3D> u{t1, tx + 1, ty + 1, k3D ? 1 : 0};
+      const float mn = u(0, 0, 0);
+      if (fused_finish) {
+        const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
+        const float f0 = I.m[i];
+        const float dlt = mc - f0;
+        v[0] += dlt * dlt;
+        I.m[i] = mc;
+        I.m_pre[i] = mc;
+      } else {
+        dst[i] = mn;
+        if (!last) {
+          const float gr = tv_grad<float>(u, k3D);
+          v[0] += gr * gr;
+        }
+      }
+    }
+    __syncthreads();  // both tiles are reused by the next group member
   }
   double tot[1];
   if (grid_sum<kThreads, 1>(v, I.partials, I.counter, inst_block(),
@@ -471,7 +465,7 @@ cudaError_t launch_iter_begin(const Inst *, int, cudaStream_t) {
 
 cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
                                cudaStream_t st) {
-  const dim3 grid = tile_grid(d.nx, d.ny, d.nz, batch);
+  const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1)
     k_after_sweep<true><<<grid, kThreads, 0, st>>>(insts, d);
   else
@@ -482,7 +476,7 @@ cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
 cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
                            int step, int ng, cudaStream_t st) {
   (void)ng;
-  const dim3 grid = tile_grid(d.nx, d.ny, d.nz, batch);
+  const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1)
     k_tv_step<true><<<grid, kThreads, 0, st>>>(insts, d, step);
   else
