@@ -66,7 +66,7 @@ struct Scalars {
   int iterations;   // out.IterationNum
   int maxIter, ng;
   int has_ref;      // I0 present
-  int pad;
+  int narrow;       // current view: no axis-parallel ray, finite residuals
 };
 
 struct Inst {
@@ -80,6 +80,8 @@ struct Inst {
   float *I0;                 // reference image or nullptr
   float *tv_b, *tv_c;        // TV ping-pong buffers
   float *cor;                // correction of the current view, na*nb
+  float4 *tabA;              // ray slopes of the current view, na (ray_tab_a)
+  float4 *tabC;              // 3D ray slopes of the current view, na*nb
   double *rmse;              // [maxIter]
   double *partials;          // reduction partials [blocks * kMaxReduceK]
   unsigned *counter;         // reduction ticket

@@ -470,7 +470,7 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   size_t off = 0;
   struct Off {
     size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, ydet, zdet, trig, rmse,
-        part, cnt, scal;
+        part, cnt, scal, tabA, tabC;
   };
   std::vector<Off> offs(batch);
   for (int i = 0; i < batch; i++) {
@@ -484,6 +484,8 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     o.tvb = off; off += per_img;
     o.tvc = off; off += per_img;
     o.cor = off; off += align256(M * 4);
+    o.tabA = off; off += align256((size_t)g0.na * 16);
+    o.tabC = off; off += align256((g0.nz > 1 || g0.nb > 1) ? M * 16 : 16);
     o.ydet = off; off += align256((size_t)g0.na * 4);
     o.zdet = off; off += align256((size_t)g0.nb * 4);
     o.trig = off; off += align256((size_t)p->nv * 8);
@@ -533,6 +535,8 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     I.tv_b = (float *)(b + o.tvb);
     I.tv_c = (float *)(b + o.tvc);
     I.cor = (float *)(b + o.cor);
+    I.tabA = (float4 *)(b + o.tabA);
+    I.tabC = (float4 *)(b + o.tabC);
     I.rmse = (double *)(b + o.rmse);
     I.partials = (double *)(b + o.part);
     I.counter = (unsigned *)(b + o.cnt);

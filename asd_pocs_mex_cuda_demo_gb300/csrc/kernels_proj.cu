@@ -284,6 +284,10 @@ __device__ __forceinline__ ViewGeo view_of(const Inst &I, int view) {
 
 // ASD_POCS_cuda.m:117-123: [proj,sumR]=Ax(m); sumR(sumR==0)=1;
 // cor0=P(:,ii)-proj; dd2+=||cor0||^2; cor=cor0./sumR.
+// Also writes the view's ray slope tables for the backward step that follows
+// (ray_tab_a per detector column, ray_tab_c per 3D ray) and sets
+// Scalars::narrow when the view has no axis-parallel ray and only finite
+// residuals, which lets that step walk each pixel's shadow only.
 __global__ void __launch_bounds__(kAxThreads)
     k_sart_ax(const Inst *__restrict__ insts, Dims D, int view) {
   const Inst &I = insts[blockIdx.z];
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(kAxThreads)
   const int lane = threadIdx.x & 31;
   const long long nr = (long long)D.na * D.nb;
   const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
-  float part[1] = {0.f};
+  float part[3] = {0.f, 0.f, 0.f};  // dd2, axis-parallel rays, non-finite cor
   if (r < nr) {
     float ys, ss;
     const float *m = I.m;
@@ -300,44 +304,108 @@ __global__ void __launch_bounds__(kAxThreads)
     if (lane == 0) {
       const float yv = ys * G.scale, srv = ss * G.scale;
       const float c0 = I.P[(long long)view * nr + r] - yv;
-      I.cor[r] = c0 / (srv == 0.f ? 1.f : srv);
+      const float cr = c0 / (srv == 0.f ? 1.f : srv);
+      I.cor[r] = cr;
       part[0] = c0 * c0;
+      part[2] = isfinite(cr) ? 0.f : 1.f;
+      const int ia = (int)(r % D.na), ib = (int)(r / D.na);
+      const float4 A = ray_tab_a(G, G.y_det[ia]);
+      if (ib == 0) {
+        I.tabA[ia] = A;
+        part[1] = (A.x == 0.0f || A.y == 0.0f) ? 1.f : 0.f;
+      }
+      if (D.nz > 1 || D.nb > 1) I.tabC[r] = ray_tab_c(A, G.z_det[ib]);
     }
   }
-  double tot[1];
-  if (grid_sum<kAxThreads, 1>(part, I.partials, I.counter, inst_block(),
+  double tot[3];
+  if (grid_sum<kAxThreads, 3>(part, I.partials, I.counter, inst_block(),
                               inst_blocks(), tot)) {
-    if (threadIdx.x == 0) I.s->dd2_acc += tot[0];
+    if (threadIdx.x == 0) {
+      I.s->dd2_acc += tot[0];
+      I.s->narrow = tot[1] == 0.0 && tot[2] == 0.0;
+    }
   }
 }
 
 // ASD_POCS_cuda.m:125-131: [bProj,sumC]=Atx(cor); sumC(sumC==0)=1;
 // m = m + beta*(bProj./sumC); m(m<0)=0.
+// Reads the view's ray tables and residuals (written by k_sart_ax) through
+// the L1 cache, so no block-wide staging or barrier is needed; each lane
+// walks its footprint (or, in the planar geometry when the view allows it,
+// its pixel's shadow) in warp-uniform steps, pairs accumulated in the
+// reference's order.
 template <bool kPlanar>
-__global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 3)
+__global__ void __launch_bounds__(kAtxThreads, 4)
     k_sart_atx(const Inst *__restrict__ insts, Dims D, int view) {
-  __shared__ AtxShared<kPlanar> sh;
   const Inst &I = insts[blockIdx.z];
   if (((volatile int *)&I.s->done)[0]) return;
   const ViewGeo G = view_of(I, view);
   const float beta = I.s->beta_f;
+  const bool narrow = kPlanar && I.s->narrow && G.z_det[0] == 0.0f;
+  const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
   float *m = I.m;
-  const float *cor = I.cor;
+  const float *__restrict__ cor = I.cor;
+  const float4 *__restrict__ tabA = I.tabA;
+  const float4 *__restrict__ tabC = I.tabC;
+  const float rx0 = G.cos_phi * (-G.SO), ry0 = G.sin_phi * (-G.SO);
   for (int t = 0; t < kTilesPerBlock; t++) {
     int x0, y0, iz;
     if (!group_tile(D.ny, D.nz, t, x0, y0, iz)) break;
     const int ix = x0 + threadIdx.x % kTileX, iy = y0 + threadIdx.x / kTileX;
     const bool valid = ix < D.nx && iy < D.ny;
-    float acc, accl;
-    atx_block_sum<kPlanar>(G, D, valid, ix, iy, iz, sh,
-                           [&](long long i) { return cor[i]; }, acc, accl);
+    float acc = 0.f, accl = 0.f;
+    VoxelWin w;
+    bool has = false;
+    if (valid) {
+      w = voxel_window(G, D, ix, iy, iz);
+      has = w.a0 <= w.a1 && w.b0 <= w.b1;
+    }
+    if (!planar_ok) {
+      // planar kernel on a geometry with z_det != 0: direct per-pair form
+      if (valid) voxel_backproject(G, D, w, [&](long long i) { return cor[i]; }, acc, accl);
+    } else {
+      int lo = has ? w.a0 : 0, hi = has ? w.a1 : -1;
+      if (narrow && has) {
+        int slo, shi;
+        if (shadow_bins(G, D, w.xc, w.yc, slo, shi)) {
+          lo = max(lo, slo);
+          hi = min(hi, shi);
+        }
+      }
+      const int cntA = has && lo <= hi ? hi - lo + 1 : 0;
+      const int cntB = has ? w.b1 - w.b0 + 1 : 0;
+      const int kA = __reduce_max_sync(0xffffffffu, cntA);
+      const int kB = kPlanar ? (kA > 0 ? 1 : 0) : __reduce_max_sync(0xffffffffu, cntB);
+      const float rx = rx0 - (has ? w.xc : 0.f), ry = ry0 - (has ? w.yc : 0.f);
+      const float rz = 0.0f - (has ? w.zc : 0.f);
+      for (int kb = 0; kb < kB; kb++) {
+        const bool onb = kb < cntB;
+        const int ib = w.b0 + kb;
+        const float c = kPlanar ? 0.0f : (onb ? __ldg(G.z_det + ib) : 1.0f) - 0.0f;
+        const int row = onb ? ib * D.na : 0;
+        for (int ka = 0; ka < kA; ka++) {
+          const bool on = onb && ka < cntA;
+          const int ia = on ? lo + ka : 0;
+          const float4 A = __ldg(tabA + ia);
+          const float yv = on ? __ldg(cor + row + ia) : 0.f;
+          float l;
+          if (kPlanar)
+            l = chord_planar_bf(A, rx, ry, G.dz);
+          else
+            l = chord3_bf(A, __ldg(tabC + row + ia), c, rx, ry, rz, G.dz);
+          if (on) {
+            acc += l * yv;
+            accl += l;
+          }
+        }
+      }
+    }
     if (valid) {
       const float bp = acc * G.scale, scv = accl * G.scale;
       const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
       const float mn = m[idx] + beta * __fdividef(bp, scv == 0.f ? 1.f : scv);
       m[idx] = mn < 0.f ? 0.f : mn;
     }
-    __syncthreads();  // the staging arrays are reused by the next tile
   }
 }
 
