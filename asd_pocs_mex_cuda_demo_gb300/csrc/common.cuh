@@ -66,7 +66,7 @@ struct Scalars {
   int iterations;   // out.IterationNum
   int maxIter, ng;
   int has_ref;      // I0 present
-  int narrow;       // current view: no axis-parallel ray, finite residuals
+  int cor_finite;   // current view: every residual finite (set by Ax)
 };
 
 struct Inst {
@@ -80,7 +80,8 @@ struct Inst {
   float *I0;                 // reference image or nullptr
   float *tv_b, *tv_c;        // TV ping-pong buffers
   float *cor;                // correction of the current view, na*nb
-  float4 *tabA;              // ray slopes of the current view, na (ray_tab_a)
+  float4 *tabA;              // ray slopes of every view, nv*na (ray_tab_a)
+  int *vflags;               // per view: kViewAxisParallel | kViewNotX | kViewNotY
   float4 *tabC;              // 3D ray slopes of the current view, na*nb
   double *rmse;              // [maxIter]
   double *partials;          // reduction partials [blocks * kMaxReduceK]
@@ -89,6 +90,10 @@ struct Inst {
 };
 
 constexpr int kMaxPartials = 1 << 22;  // blocks per reduction (sanity bound)
+
+// View flags (Inst::vflags): some ray of the view has no x (or no y)
+// extent; some ray is not x-dominant; some ray is not y-dominant.
+constexpr int kViewAxisParallel = 1, kViewNotX = 2, kViewNotY = 4;
 
 // Voxel tiles of the voxel-driven kernels: 32 (x) by 8 (y) voxels of one z
 // slice per 256-thread block.  Grids are (x tiles, y tiles * nz, instances).

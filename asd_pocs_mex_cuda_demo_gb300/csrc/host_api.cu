@@ -387,6 +387,7 @@ struct asdpocs_plan_s {
   std::vector<asdpocs_options> opt;
   std::vector<Inst> h_inst;
   std::vector<int> has_ref;
+  std::vector<int> view_axis;  // per view: 1 / 2 / 0 (see launch_sart_atx)
   Inst *d_inst = nullptr;
   void *arena = nullptr;
   size_t bytes = 0;
@@ -399,7 +400,7 @@ namespace asd {
 static int plan_enqueue_iteration(asdpocs_plan p) {
   for (int v = 0; v < p->nv; v++) {
     ASD_CUDA(launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st));
-    ASD_CUDA(launch_sart_atx(p->d_inst, p->batch, p->d, v, p->st));
+    ASD_CUDA(launch_sart_atx(p->d_inst, p->batch, p->d, v, p->view_axis[v], p->st));
   }
   ASD_CUDA(launch_after_sweep(p->d_inst, p->batch, p->d, p->st));
   for (int s = 0; s < p->max_ng; s++)
@@ -470,7 +471,7 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   size_t off = 0;
   struct Off {
     size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, ydet, zdet, trig, rmse,
-        part, cnt, scal, tabA, tabC;
+        part, cnt, scal, tabA, tabC, vflags;
   };
   std::vector<Off> offs(batch);
   for (int i = 0; i < batch; i++) {
@@ -484,7 +485,8 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     o.tvb = off; off += per_img;
     o.tvc = off; off += per_img;
     o.cor = off; off += align256(M * 4);
-    o.tabA = off; off += align256((size_t)g0.na * 16);
+    o.tabA = off; off += align256((size_t)g0.na * p->nv * 16);
+    o.vflags = off; off += align256((size_t)p->nv * 4);
     o.tabC = off; off += align256((g0.nz > 1 || g0.nb > 1) ? M * 16 : 16);
     o.ydet = off; off += align256((size_t)g0.na * 4);
     o.zdet = off; off += align256((size_t)g0.nb * 4);
@@ -536,6 +538,7 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     I.tv_c = (float *)(b + o.tvc);
     I.cor = (float *)(b + o.cor);
     I.tabA = (float4 *)(b + o.tabA);
+    I.vflags = (int *)(b + o.vflags);
     I.tabC = (float4 *)(b + o.tabC);
     I.rmse = (double *)(b + o.rmse);
     I.partials = (double *)(b + o.part);
@@ -555,6 +558,24 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(),
                                             sizeof(Inst) * batch,
                                             cudaMemcpyHostToDevice, p->st);
+  if (e == cudaSuccess) e = launch_view_tables(p->d_inst, batch, p->d, p->nv, p->st);
+  // per-view chord specialisation, valid when every instance agrees
+  std::vector<int> vf((size_t)p->nv);
+  p->view_axis.assign(p->nv, 0);
+  std::vector<int> acc((size_t)p->nv, 0);
+  for (int i = 0; i < batch && e == cudaSuccess; i++) {
+    e = cudaMemcpyAsync(vf.data(), p->h_inst[i].vflags, (size_t)p->nv * 4,
+                        cudaMemcpyDeviceToHost, p->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+    for (int v = 0; v < p->nv; v++) acc[v] |= vf[v];
+  }
+  for (int v = 0; v < p->nv; v++) {
+    if (acc[v] & kViewAxisParallel) continue;
+    if (!(acc[v] & kViewNotX))
+      p->view_axis[v] = 1;
+    else if (!(acc[v] & kViewNotY))
+      p->view_axis[v] = 2;
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
   if (e != cudaSuccess) {
     asdpocs_plan_destroy(p);
@@ -751,7 +772,8 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {
       case 0: return launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
-      case 1: return launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv, p->st);
+      case 1: return launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv,
+                                     p->view_axis[i % p->nv], p->st);
       case 2: return launch_tv_step(p->d_inst, p->batch, p->d, 1 + i % (ng > 1 ? ng - 1 : 1),
                                     ng, p->st);
       default: return launch_after_sweep(p->d_inst, p->batch, p->d, p->st);

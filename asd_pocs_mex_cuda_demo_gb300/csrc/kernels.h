@@ -19,8 +19,10 @@ cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
 // m += beta*bp/sumC, positivity.
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
                            int view, cudaStream_t st);
+// axis: 1 (2) when every instance's rays of this view are x- (y-) dominant
+// and none is axis-parallel (view flags), else 0.
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, cudaStream_t st);
+                            int view, int axis, cudaStream_t st);
 
 // ---- TV and scalars (kernels_tv.cu) ----
 // FP64 / FP32 TV minimisation on device buffers (reference semantics).
@@ -43,5 +45,10 @@ cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
                                int ng, cudaStream_t st);
 
 int reduce_blocks_for(const Dims &d);
+
+// Ray slope tables and flags of every view (Inst::tabA, Inst::vflags, which
+// must be zeroed first), computed once per plan.
+cudaError_t launch_view_tables(const Inst *insts, int batch, const Dims &d,
+                               int nv, cudaStream_t st);
 
 }  // namespace asd

@@ -282,12 +282,32 @@ __device__ __forceinline__ ViewGeo view_of(const Inst &I, int view) {
   return g;
 }
 
+// Ray slope tables of every view (Inst::tabA) and the view flags, once per
+// plan: grid (ceil(na/128), nv, instances).
+__global__ void __launch_bounds__(128)
+    k_view_tables(const Inst *__restrict__ insts, Dims D) {
+  const Inst &I = insts[blockIdx.z];
+  const int view = blockIdx.y;
+  const int ia = blockIdx.x * 128 + threadIdx.x;
+  const ViewGeo G = view_of(I, view);
+  int f = 0;
+  if (ia < D.na) {
+    const float4 A = ray_tab_a(G, G.y_det[ia]);
+    I.tabA[(long long)view * D.na + ia] = A;
+    const bool xf = fabsf(A.x) > fabsf(A.y);
+    f = (A.x == 0.0f || A.y == 0.0f ? kViewAxisParallel : 0) |
+        (xf ? 0 : kViewNotX) | (xf ? kViewNotY : 0);
+  }
+  f = __reduce_or_sync(0xffffffffu, f);
+  if ((threadIdx.x & 31) == 0 && f) atomicOr(I.vflags + view, f);
+}
+
 // ASD_POCS_cuda.m:117-123: [proj,sumR]=Ax(m); sumR(sumR==0)=1;
 // cor0=P(:,ii)-proj; dd2+=||cor0||^2; cor=cor0./sumR.
-// Also writes the view's ray slope tables for the backward step that follows
-// (ray_tab_a per detector column, ray_tab_c per 3D ray) and sets
-// Scalars::narrow when the view has no axis-parallel ray and only finite
-// residuals, which lets that step walk each pixel's shadow only.
+// Also records whether every residual is finite (Scalars::cor_finite), and
+// for 3D geometry writes the view's per-ray slopes ray_tab_c for the
+// backward step that follows.
+template <bool k3D>
 __global__ void __launch_bounds__(kAxThreads)
     k_sart_ax(const Inst *__restrict__ insts, Dims D, int view) {
   const Inst &I = insts[blockIdx.z];
@@ -296,7 +316,7 @@ __global__ void __launch_bounds__(kAxThreads)
   const int lane = threadIdx.x & 31;
   const long long nr = (long long)D.na * D.nb;
   const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
-  float part[3] = {0.f, 0.f, 0.f};  // dd2, axis-parallel rays, non-finite cor
+  float part[2] = {0.f, 0.f};  // dd2, non-finite residuals
   if (r < nr) {
     float ys, ss;
     const float *m = I.m;
@@ -307,45 +327,43 @@ __global__ void __launch_bounds__(kAxThreads)
       const float cr = c0 / (srv == 0.f ? 1.f : srv);
       I.cor[r] = cr;
       part[0] = c0 * c0;
-      part[2] = isfinite(cr) ? 0.f : 1.f;
-      const int ia = (int)(r % D.na), ib = (int)(r / D.na);
-      const float4 A = ray_tab_a(G, G.y_det[ia]);
-      if (ib == 0) {
-        I.tabA[ia] = A;
-        part[1] = (A.x == 0.0f || A.y == 0.0f) ? 1.f : 0.f;
+      part[1] = isfinite(cr) ? 0.f : 1.f;
+      if (k3D) {
+        const int ia = (int)(r % D.na), ib = (int)(r / D.na);
+        I.tabC[r] = ray_tab_c(I.tabA[(long long)view * D.na + ia], G.z_det[ib]);
       }
-      if (D.nz > 1 || D.nb > 1) I.tabC[r] = ray_tab_c(A, G.z_det[ib]);
     }
   }
-  double tot[3];
-  if (grid_sum<kAxThreads, 3>(part, I.partials, I.counter, inst_block(),
+  double tot[2];
+  if (grid_sum<kAxThreads, 2>(part, I.partials, I.counter, inst_block(),
                               inst_blocks(), tot)) {
     if (threadIdx.x == 0) {
       I.s->dd2_acc += tot[0];
-      I.s->narrow = tot[1] == 0.0 && tot[2] == 0.0;
+      I.s->cor_finite = tot[1] == 0.0;
     }
   }
 }
 
-// ASD_POCS_cuda.m:125-131: [bProj,sumC]=Atx(cor); sumC(sumC==0)=1;
-// m = m + beta*(bProj./sumC); m(m<0)=0.
-// Reads the view's ray tables and residuals (written by k_sart_ax) through
-// the L1 cache, so no block-wide staging or barrier is needed; each lane
-// walks its footprint (or, in the planar geometry when the view allows it,
-// its pixel's shadow) in warp-uniform steps, pairs accumulated in the
-// reference's order.
-template <bool kPlanar>
-__global__ void __launch_bounds__(kAtxThreads, 4)
-    k_sart_atx(const Inst *__restrict__ insts, Dims D, int view) {
-  const Inst &I = insts[blockIdx.z];
-  if (((volatile int *)&I.s->done)[0]) return;
-  const ViewGeo G = view_of(I, view);
+// Planar chord for a window whose rays share dominant axis AX (1: x, 2: y;
+// no axis-parallel ray), or any ray (AX == 0).
+template <int AX>
+__device__ __forceinline__ float chord_sel(const float4 A, float rx, float ry,
+                                           float dz) {
+  if (AX == 1) return chord_planar_axis<true>(A, rx, ry);
+  if (AX == 2) return chord_planar_axis<false>(A, rx, ry);
+  return chord_planar_bf(A, rx, ry, dz);
+}
+
+// Backward step over this block's tile group (see k_sart_atx).
+template <bool kPlanar, int AX>
+__device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
+                                               const Dims &D,
+                                               const float4 *__restrict__ tabA,
+                                               bool narrow) {
   const float beta = I.s->beta_f;
-  const bool narrow = kPlanar && I.s->narrow && G.z_det[0] == 0.0f;
   const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
   float *m = I.m;
   const float *__restrict__ cor = I.cor;
-  const float4 *__restrict__ tabA = I.tabA;
   const float4 *__restrict__ tabC = I.tabC;
   const float rx0 = G.cos_phi * (-G.SO), ry0 = G.sin_phi * (-G.SO);
   for (int t = 0; t < kTilesPerBlock; t++) {
@@ -362,7 +380,8 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
     }
     if (!planar_ok) {
       // planar kernel on a geometry with z_det != 0: direct per-pair form
-      if (valid) voxel_backproject(G, D, w, [&](long long i) { return cor[i]; }, acc, accl);
+      if (valid)
+        voxel_backproject(G, D, w, [&](long long i) { return cor[i]; }, acc, accl);
     } else {
       int lo = has ? w.a0 : 0, hi = has ? w.a1 : -1;
       if (narrow && has) {
@@ -375,7 +394,8 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
       const int cntA = has && lo <= hi ? hi - lo + 1 : 0;
       const int cntB = has ? w.b1 - w.b0 + 1 : 0;
       const int kA = __reduce_max_sync(0xffffffffu, cntA);
-      const int kB = kPlanar ? (kA > 0 ? 1 : 0) : __reduce_max_sync(0xffffffffu, cntB);
+      const int kB =
+          kPlanar ? (kA > 0 ? 1 : 0) : __reduce_max_sync(0xffffffffu, cntB);
       const float rx = rx0 - (has ? w.xc : 0.f), ry = ry0 - (has ? w.yc : 0.f);
       const float rz = 0.0f - (has ? w.zc : 0.f);
       for (int kb = 0; kb < kB; kb++) {
@@ -390,7 +410,7 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
           const float yv = on ? __ldg(cor + row + ia) : 0.f;
           float l;
           if (kPlanar)
-            l = chord_planar_bf(A, rx, ry, G.dz);
+            l = chord_sel<AX>(A, rx, ry, G.dz);
           else
             l = chord3_bf(A, __ldg(tabC + row + ia), c, rx, ry, rz, G.dz);
           if (on) {
@@ -407,6 +427,28 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
       m[idx] = mn < 0.f ? 0.f : mn;
     }
   }
+}
+
+// ASD_POCS_cuda.m:125-131: [bProj,sumC]=Atx(cor); sumC(sumC==0)=1;
+// m = m + beta*(bProj./sumC); m(m<0)=0.
+// Reads the view's ray tables and residuals through the L1 cache, so no
+// block-wide staging or barrier is needed; each lane walks its footprint
+// (or, in the planar geometry when the view allows it, its pixel's shadow)
+// in warp-uniform steps, pairs accumulated in the reference's order.  AX != 0
+// (chosen by the host from the view flags, when every instance's rays of this
+// view share one dominant axis and none is axis-parallel) selects the
+// axis-specialised chord.
+template <bool kPlanar, int AX>
+__global__ void __launch_bounds__(kAtxThreads, 4)
+    k_sart_atx(const Inst *__restrict__ insts, Dims D, int view) {
+  const Inst &I = insts[blockIdx.z];
+  if (((volatile int *)&I.s->done)[0]) return;
+  const ViewGeo G = view_of(I, view);
+  const float4 *tabA = I.tabA + (long long)view * D.na;
+  const int vf = I.vflags[view];
+  const bool narrow = kPlanar && !(vf & kViewAxisParallel) && I.s->cor_finite &&
+                      G.z_det[0] == 0.0f;
+  sart_atx_tiles<kPlanar, AX>(I, G, D, tabA, narrow);
 }
 
 }  // namespace
@@ -434,17 +476,30 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
                            int view, cudaStream_t st) {
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
-  k_sart_ax<<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, d, view);
+  if (d.nz > 1 || d.nb > 1)
+    k_sart_ax<true><<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, d, view);
+  else
+    k_sart_ax<false><<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, d, view);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, cudaStream_t st) {
+                            int view, int axis, cudaStream_t st) {
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
-  if (d.nz == 1 && d.nb == 1)
-    k_sart_atx<true><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+  if (d.nz > 1 || d.nb > 1)
+    k_sart_atx<false, 0><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+  else if (axis == 1)
+    k_sart_atx<true, 1><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+  else if (axis == 2)
+    k_sart_atx<true, 2><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
   else
-    k_sart_atx<false><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+    k_sart_atx<true, 0><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_view_tables(const Inst *insts, int batch, const Dims &d,
+                               int nv, cudaStream_t st) {
+  k_view_tables<<<dim3((d.na + 127) / 128, nv, batch), 128, 0, st>>>(insts, d);
   return cudaGetLastError();
 }
 
