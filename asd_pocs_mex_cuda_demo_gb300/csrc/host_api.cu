@@ -3,6 +3,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <mutex>
@@ -388,6 +389,7 @@ struct asdpocs_plan_s {
   std::vector<Inst> h_inst;
   std::vector<int> has_ref;
   std::vector<int> view_axis;  // per view: 1 / 2 / 0 (see launch_sart_atx)
+  bool shared = false;         // all instances share geometry and angles
   Inst *d_inst = nullptr;
   void *arena = nullptr;
   size_t bytes = 0;
@@ -400,7 +402,11 @@ namespace asd {
 static int plan_enqueue_iteration(asdpocs_plan p) {
   for (int v = 0; v < p->nv; v++) {
     ASD_CUDA(launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st));
-    ASD_CUDA(launch_sart_atx(p->d_inst, p->batch, p->d, v, p->view_axis[v], p->st));
+    if (p->shared)
+      ASD_CUDA(launch_sart_atx_shared(p->d_inst, p->batch, p->d, v,
+                                      p->view_axis[v], p->st));
+    else
+      ASD_CUDA(launch_sart_atx(p->d_inst, p->batch, p->d, v, p->view_axis[v], p->st));
   }
   ASD_CUDA(launch_after_sweep(p->d_inst, p->batch, p->d, p->st));
   for (int s = 0; s < p->max_ng; s++)
@@ -452,6 +458,17 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
       p->max_ng = p->opt[i].numOfgradients;
   }
   p->has_ref.assign(batch, 0);
+  // instances with identical geometry and view angles share the projector
+  // coefficients of every view
+  p->shared = batch > 1;
+  for (int i = 1; i < batch && p->shared; i++) {
+    const asdpocs_geometry &gi = geom[i];
+    p->shared = gi.SO == g0.SO && gi.OD == g0.OD && gi.vxlsize == g0.vxlsize &&
+                gi.detsize == g0.detsize &&
+                memcmp(phi_vec_deg, phi_vec_deg + (size_t)i * g0.nv,
+                       sizeof(double) * (size_t)g0.nv) == 0;
+  }
+  if (getenv("ASDPOCS_NO_SHARED_GEOMETRY")) p->shared = false;
   cudaGetDevice(&p->device);
   if (stream) {
     p->st = (cudaStream_t)stream;
@@ -772,8 +789,11 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {
       case 0: return launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
-      case 1: return launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv,
-                                     p->view_axis[i % p->nv], p->st);
+      case 1:
+        return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, i % p->nv,
+                                                  p->view_axis[i % p->nv], p->st)
+                         : launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv,
+                                           p->view_axis[i % p->nv], p->st);
       case 2: return launch_tv_step(p->d_inst, p->batch, p->d, 1 + i % (ng > 1 ? ng - 1 : 1),
                                     ng, p->st);
       default: return launch_after_sweep(p->d_inst, p->batch, p->d, p->st);

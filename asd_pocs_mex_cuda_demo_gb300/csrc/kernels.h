@@ -46,6 +46,12 @@ cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
 
 int reduce_blocks_for(const Dims &d);
 
+// Backward step for a batch whose instances share geometry and view angles:
+// chords computed once per voxel and applied to groups of instances.
+cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
+                                   const Dims &d, int view, int axis,
+                                   cudaStream_t st);
+
 // Ray slope tables and flags of every view (Inst::tabA, Inst::vflags, which
 // must be zeroed first), computed once per plan.
 cudaError_t launch_view_tables(const Inst *insts, int batch, const Dims &d,

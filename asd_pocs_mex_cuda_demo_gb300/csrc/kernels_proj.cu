@@ -451,6 +451,153 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
   sart_atx_tiles<kPlanar, AX>(I, G, D, tabA, narrow);
 }
 
+// ---------------------------------------------------------------------------
+// Shared-geometry backward step: when every instance of a plan has the same
+// geometry and view angles, the chords of a (voxel, bin) pair are the same
+// for all of them.  A block then handles one voxel tile for a group of
+// kShareGroup instances: each lane computes the chords of its voxel's pairs
+// once (kPairChunk at a time) and applies them to every instance of the
+// group -- the backprojection becomes a sparse-matrix by dense-matrix
+// product over the group.  Each instance accumulates its pairs in the
+// reference's order, so the result is bit-identical to k_sart_atx.
+// ---------------------------------------------------------------------------
+constexpr int kShareGroup = 16;
+constexpr int kPairChunk = 4;
+
+template <bool kPlanar, int AX>
+__global__ void __launch_bounds__(kAtxThreads, 2)
+    k_sart_atx_shared(const Inst *__restrict__ insts, int batch, Dims D,
+                      int view) {
+  __shared__ const float *s_cor[kShareGroup];
+  __shared__ float *s_m[kShareGroup];
+  __shared__ float s_beta[kShareGroup];
+  __shared__ unsigned s_active;
+  __shared__ int s_finite;
+  const int g0 = blockIdx.z * kShareGroup;
+  const int gn = min(kShareGroup, batch - g0);
+  if (threadIdx.x == 0) {
+    s_active = 0u;
+    s_finite = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x < gn) {
+    const Inst &Ib = insts[g0 + threadIdx.x];
+    const bool live = ((volatile int *)&Ib.s->done)[0] == 0;
+    s_cor[threadIdx.x] = Ib.cor;
+    s_m[threadIdx.x] = Ib.m;
+    s_beta[threadIdx.x] = Ib.s->beta_f;
+    if (live) {
+      atomicOr(&s_active, 1u << threadIdx.x);
+      if (!Ib.s->cor_finite) atomicAnd(&s_finite, 0);
+    }
+  }
+  __syncthreads();
+  const unsigned active = s_active;
+  if (!active) return;
+  const Inst &I0 = insts[g0];
+  const ViewGeo G = view_of(I0, view);
+  const float4 *__restrict__ tabA = I0.tabA + (long long)view * D.na;
+  const float4 *__restrict__ tabC = I0.tabC;
+  const int vf = I0.vflags[view];
+  const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
+  const bool narrow = kPlanar && planar_ok && !(vf & kViewAxisParallel) && s_finite;
+  int ix, iy, iz;
+  const bool valid = tile_voxel(D, ix, iy, iz);
+  VoxelWin w;
+  bool has = false;
+  if (valid) {
+    w = voxel_window(G, D, ix, iy, iz);
+    has = w.a0 <= w.a1 && w.b0 <= w.b1;
+  }
+  float acc[kShareGroup];
+#pragma unroll
+  for (int b = 0; b < kShareGroup; b++) acc[b] = 0.f;
+  float accl = 0.f;
+  if (!planar_ok) {
+    // planar kernel on a geometry with z_det != 0: direct per-pair form
+    if (valid) {
+      const float xs = G.cos_phi * (-G.SO), ys0 = G.sin_phi * (-G.SO);
+      for (int ib = w.b0; ib <= w.b1; ib++)
+        for (int ia = w.a0; ia <= w.a1; ia++) {
+          const float yd_ = G.y_det[ia];
+          const float l = chord3(xs, ys0, 0.0f, G.cos_phi * G.OD - G.sin_phi * yd_,
+                                 G.sin_phi * G.OD + G.cos_phi * yd_, G.z_det[ib],
+                                 G.dz, w.xc, w.yc, w.zc);
+          accl += l;
+#pragma unroll
+          for (int b = 0; b < kShareGroup; b++)
+            if (b < gn) acc[b] += l * s_cor[b][(long long)ib * D.na + ia];
+        }
+    }
+  } else {
+    int lo = has ? w.a0 : 0, hi = has ? w.a1 : -1;
+    if (narrow && has) {
+      int slo, shi;
+      if (shadow_bins(G, D, w.xc, w.yc, slo, shi)) {
+        lo = max(lo, slo);
+        hi = min(hi, shi);
+      }
+    }
+    const int cntA = has && lo <= hi ? hi - lo + 1 : 0;
+    const int cntB = has ? w.b1 - w.b0 + 1 : 0;
+    const int kA = __reduce_max_sync(0xffffffffu, cntA);
+    const int kB =
+        kPlanar ? (kA > 0 ? 1 : 0) : __reduce_max_sync(0xffffffffu, cntB);
+    const float rx = G.cos_phi * (-G.SO) - (has ? w.xc : 0.f);
+    const float ry = G.sin_phi * (-G.SO) - (has ? w.yc : 0.f);
+    const float rz = 0.0f - (has ? w.zc : 0.f);
+    for (int kb = 0; kb < kB; kb++) {
+      const bool onb = kb < cntB;
+      const int ib = w.b0 + kb;
+      const float c = kPlanar ? 0.0f : (onb ? __ldg(G.z_det + ib) : 1.0f) - 0.0f;
+      const int row = onb ? ib * D.na : 0;
+      for (int c0 = 0; c0 < kA; c0 += kPairChunk) {
+        float l[kPairChunk];
+        int idx[kPairChunk];
+        bool on[kPairChunk];
+#pragma unroll
+        for (int j = 0; j < kPairChunk; j++) {
+          const int ka = c0 + j;
+          on[j] = onb && ka < cntA;
+          const int ia = on[j] ? lo + ka : 0;
+          idx[j] = row + ia;
+          l[j] = 0.f;
+          if (ka < kA) {  // warp-uniform
+            const float4 A = __ldg(tabA + ia);
+            l[j] = kPlanar ? chord_sel<AX>(A, rx, ry, G.dz)
+                           : chord3_bf(A, __ldg(tabC + row + ia), c, rx, ry, rz,
+                                       G.dz);
+          }
+          if (on[j]) accl += l[j];
+        }
+#pragma unroll
+        for (int b = 0; b < kShareGroup; b++) {
+          if (b < gn && ((active >> b) & 1u)) {
+            const float *__restrict__ cb = s_cor[b];
+            float a = acc[b];
+#pragma unroll
+            for (int j = 0; j < kPairChunk; j++)
+              if (on[j]) a += l[j] * __ldg(cb + idx[j]);
+            acc[b] = a;
+          }
+        }
+      }
+    }
+  }
+  if (!valid) return;
+  const float scv = accl * G.scale;
+  const unsigned vi = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+#pragma unroll
+  for (int b = 0; b < kShareGroup; b++) {
+    if (b < gn && ((active >> b) & 1u)) {
+      float *mb = s_m[b];
+      const float bp = acc[b] * G.scale;
+      const float mn = mb[vi] + s_beta[b] * __fdividef(bp, scv == 0.f ? 1.f : scv);
+      mb[vi] = mn < 0.f ? 0.f : mn;
+    }
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_ax(const float *x, float *y, float *sr, const ViewGeo &g,
@@ -494,6 +641,22 @@ cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
     k_sart_atx<true, 2><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
   else
     k_sart_atx<true, 0><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
+                                   const Dims &d, int view, int axis,
+                                   cudaStream_t st) {
+  dim3 grid = tile_grid(d.nx, d.ny, d.nz, 1);
+  grid.z = (batch + kShareGroup - 1) / kShareGroup;
+  if (d.nz > 1 || d.nb > 1)
+    k_sart_atx_shared<false, 0><<<grid, kAtxThreads, 0, st>>>(insts, batch, d, view);
+  else if (axis == 1)
+    k_sart_atx_shared<true, 1><<<grid, kAtxThreads, 0, st>>>(insts, batch, d, view);
+  else if (axis == 2)
+    k_sart_atx_shared<true, 2><<<grid, kAtxThreads, 0, st>>>(insts, batch, d, view);
+  else
+    k_sart_atx_shared<true, 0><<<grid, kAtxThreads, 0, st>>>(insts, batch, d, view);
   return cudaGetLastError();
 }
 

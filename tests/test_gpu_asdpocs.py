@@ -148,3 +148,37 @@ def test_hbm_budget_admission(gpu):
     with pytest.raises(pkg.AsdpocsError) as e:
         pkg.Plan(para, para["phi_vec"], hbm_budget_bytes=1024)
     assert e.value.status == 3
+
+
+def test_shared_geometry_batch_equals_alone_bitwise(gpu, monkeypatch):
+    # instances with the same geometry and angles take the shared-coefficient
+    # backward step; each result must equal its single-instance run exactly
+    n, na, nv = 64, 128, 30
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = phantoms.fov_voxel_size(SO, OD, det, na, n)
+    phi = phantoms.views(nv)
+    para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, na=na, nb=1, detsize=det,
+                phi_vec=phi, maxnumIter=3, alpha=0.002)
+    Ps = []
+    for s in range(5):
+        x = phantoms.random_ellipses(n, 40 + s).astype(np.float32)
+        P = np.stack([pkg.Ax_cone_gpu(x, dict(para, phi=-a / 180 * np.pi))[0] for a in phi],
+                     axis=1)
+        Ps.append(phantoms.poisson_noise(P, 1e5, 40 + s))
+    alone = []
+    for P in Ps:
+        with pkg.Plan(para, phi) as pl:
+            pl.set_sinogram(0, P.ravel(order="F"))
+            pl.reset()
+            pl.run()
+            alone.append(pl.image(0))
+    for force_per_instance in (False, True):
+        if force_per_instance:
+            monkeypatch.setenv("ASDPOCS_NO_SHARED_GEOMETRY", "1")
+        with pkg.Plan([para] * 5, [phi] * 5) as pl:
+            for k, P in enumerate(Ps):
+                pl.set_sinogram(k, P.ravel(order="F"))
+            pl.reset()
+            pl.run()
+            for k in range(5):
+                assert np.array_equal(pl.image(k), alone[k]), (force_per_instance, k)
