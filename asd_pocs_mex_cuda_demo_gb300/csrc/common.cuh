@@ -79,7 +79,9 @@ struct Inst {
   float *m_k1;               // TV distance reference (m0)
   float *I0;                 // reference image or nullptr
   float *tv_b, *tv_c;        // TV ping-pong buffers
-  float *cor;                // correction of the current view, na*nb
+  float *cor;                // correction of the current view: element r at
+  int cor_stride;            //   cor[r * cor_stride] (1, or kShareSlots when
+                             //   a shared-geometry group interleaves them)
   float4 *tabA;              // ray slopes of every view, nv*na (ray_tab_a)
   int *vflags;               // per view: kViewAxisParallel | kViewNotX | kViewNotY
   float4 *tabC;              // 3D ray slopes of the current view, na*nb
@@ -90,6 +92,10 @@ struct Inst {
 };
 
 constexpr int kMaxPartials = 1 << 22;  // blocks per reduction (sanity bound)
+
+// Instances per group of the shared-geometry kernels; their residuals are
+// stored interleaved, cor[r * kShareSlots + slot].
+constexpr int kShareSlots = 16;
 
 // View flags (Inst::vflags): some ray of the view has no x (or no y)
 // extent; some ray is not x-dominant; some ray is not y-dominant.

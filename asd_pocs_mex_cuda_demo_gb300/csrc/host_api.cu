@@ -501,7 +501,11 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     o.I0 = off; off += per_img;
     o.tvb = off; off += per_img;
     o.tvc = off; off += per_img;
-    o.cor = off; off += align256(M * 4);
+    // shared-geometry groups interleave their residuals in the buffer of
+    // the group's first instance (kShareSlots values per ray)
+    o.cor = off;
+    off += align256((p->shared && i % kShareSlots == 0) ? M * 4 * kShareSlots
+                                                        : M * 4);
     o.tabA = off; off += align256((size_t)g0.na * p->nv * 16);
     o.vflags = off; off += align256((size_t)p->nv * 4);
     o.tabC = off; off += align256((g0.nz > 1 || g0.nb > 1) ? M * 16 : 16);
@@ -553,7 +557,13 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     I.I0 = (float *)(b + o.I0);
     I.tv_b = (float *)(b + o.tvb);
     I.tv_c = (float *)(b + o.tvc);
-    I.cor = (float *)(b + o.cor);
+    if (p->shared) {
+      I.cor = (float *)(b + offs[i - i % kShareSlots].cor) + i % kShareSlots;
+      I.cor_stride = kShareSlots;
+    } else {
+      I.cor = (float *)(b + o.cor);
+      I.cor_stride = 1;
+    }
     I.tabA = (float4 *)(b + o.tabA);
     I.vflags = (int *)(b + o.vflags);
     I.tabC = (float4 *)(b + o.tabC);

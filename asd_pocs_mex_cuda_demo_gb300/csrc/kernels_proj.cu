@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(kAxThreads)
       const float yv = ys * G.scale, srv = ss * G.scale;
       const float c0 = I.P[(long long)view * nr + r] - yv;
       const float cr = c0 / (srv == 0.f ? 1.f : srv);
-      I.cor[r] = cr;
+      I.cor[r * I.cor_stride] = cr;
       part[0] = c0 * c0;
       part[1] = isfinite(cr) ? 0.f : 1.f;
       if (k3D) {
@@ -461,14 +461,13 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 // product over the group.  Each instance accumulates its pairs in the
 // reference's order, so the result is bit-identical to k_sart_atx.
 // ---------------------------------------------------------------------------
-constexpr int kShareGroup = 16;
+constexpr int kShareGroup = kShareSlots;
 constexpr int kPairChunk = 4;
 
 template <bool kPlanar, int AX>
 __global__ void __launch_bounds__(kAtxThreads, 2)
     k_sart_atx_shared(const Inst *__restrict__ insts, int batch, Dims D,
                       int view) {
-  __shared__ const float *s_cor[kShareGroup];
   __shared__ float *s_m[kShareGroup];
   __shared__ float s_beta[kShareGroup];
   __shared__ unsigned s_active;
@@ -483,7 +482,6 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
   if (threadIdx.x < gn) {
     const Inst &Ib = insts[g0 + threadIdx.x];
     const bool live = ((volatile int *)&Ib.s->done)[0] == 0;
-    s_cor[threadIdx.x] = Ib.cor;
     s_m[threadIdx.x] = Ib.m;
     s_beta[threadIdx.x] = Ib.s->beta_f;
     if (live) {
@@ -496,6 +494,8 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
   if (!active) return;
   const Inst &I0 = insts[g0];
   const ViewGeo G = view_of(I0, view);
+  // the group's residuals, interleaved: ray r of slot b at corg[r*16 + b]
+  const float4 *__restrict__ corg = (const float4 *)I0.cor;
   const float4 *__restrict__ tabA = I0.tabA + (long long)view * D.na;
   const float4 *__restrict__ tabC = I0.tabC;
   const int vf = I0.vflags[view];
@@ -524,9 +524,15 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
                                  G.sin_phi * G.OD + G.cos_phi * yd_, G.z_det[ib],
                                  G.dz, w.xc, w.yc, w.zc);
           accl += l;
+          const long long r = (long long)ib * D.na + ia;
 #pragma unroll
-          for (int b = 0; b < kShareGroup; b++)
-            if (b < gn) acc[b] += l * s_cor[b][(long long)ib * D.na + ia];
+          for (int q = 0; q < kShareGroup / 4; q++) {
+            const float4 c4 = __ldg(corg + r * (kShareGroup / 4) + q);
+            acc[4 * q] += l * c4.x;
+            acc[4 * q + 1] += l * c4.y;
+            acc[4 * q + 2] += l * c4.z;
+            acc[4 * q + 3] += l * c4.w;
+          }
         }
     }
   } else {
@@ -571,14 +577,16 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
           if (on[j]) accl += l[j];
         }
 #pragma unroll
-        for (int b = 0; b < kShareGroup; b++) {
-          if (b < gn && ((active >> b) & 1u)) {
-            const float *__restrict__ cb = s_cor[b];
-            float a = acc[b];
+        for (int j = 0; j < kPairChunk; j++) {
+          if (on[j]) {
 #pragma unroll
-            for (int j = 0; j < kPairChunk; j++)
-              if (on[j]) a += l[j] * __ldg(cb + idx[j]);
-            acc[b] = a;
+            for (int q = 0; q < kShareGroup / 4; q++) {
+              const float4 c4 = __ldg(corg + (long long)idx[j] * (kShareGroup / 4) + q);
+              acc[4 * q] += l[j] * c4.x;
+              acc[4 * q + 1] += l[j] * c4.y;
+              acc[4 * q + 2] += l[j] * c4.z;
+              acc[4 * q + 3] += l[j] * c4.w;
+            }
           }
         }
       }
