@@ -401,10 +401,7 @@ namespace asd {
 
 static int plan_enqueue_iteration(asdpocs_plan p) {
   for (int v = 0; v < p->nv; v++) {
-    if (p->shared)
-      ASD_CUDA(launch_sart_ax_shared(p->d_inst, p->batch, p->d, v, p->st));
-    else
-      ASD_CUDA(launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st));
+    ASD_CUDA(launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st));
     if (p->shared)
       ASD_CUDA(launch_sart_atx_shared(p->d_inst, p->batch, p->d, v,
                                       p->view_axis[v], p->st));
@@ -801,9 +798,7 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   const int ng = p->max_ng > 0 ? p->max_ng : 1;
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {
-      case 0:
-        return p->shared ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, i % p->nv, p->st)
-                         : launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
+      case 0: return launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
       case 1:
         return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, i % p->nv,
                                                   p->view_axis[i % p->nv], p->st)

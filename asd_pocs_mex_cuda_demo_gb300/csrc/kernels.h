@@ -46,11 +46,6 @@ cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
 
 int reduce_blocks_for(const Dims &d);
 
-// Forward step for a batch whose instances share geometry and view angles
-// (planar geometry; other geometries take launch_sart_ax).
-cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
-                                  int view, cudaStream_t st);
-
 // Backward step for a batch whose instances share geometry and view angles:
 // chords computed once per voxel and applied to groups of instances.
 cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,

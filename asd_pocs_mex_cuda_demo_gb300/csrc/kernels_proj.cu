@@ -42,7 +42,7 @@ __device__ __forceinline__ void ax_warp(const ViewGeo &G, const Dims &D,
   ys = 0.f;
   ss = 0.f;
   if (D.nz == 1 && zd == 0.0f)
-    ray_columns_planar_fast<2>(R, lane, 32, ld, ys, ss);
+    ray_columns_planar_fast(R, lane, 32, ld, ys, ss);
   else
     ray_columns<false>(R, lane, 32, ld, ys, ss);
   ys = warp_sum(ys);
@@ -452,107 +452,6 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 }
 
 // ---------------------------------------------------------------------------
-// Shared-geometry forward step (planar geometry): one warp per ray computes
-// the ray's column pieces once and applies them to the images of a group of
-// kShareSlots instances (see ray_columns_planar_group); lane 0 then forms
-// each instance's residual and writes it interleaved.  The per-instance
-// ||P - Ax||^2 and non-finite counts are reduced deterministically: block
-// partials per instance, summed in block order by the group's last block.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kAxThreads)
-    k_sart_ax_shared(const Inst *__restrict__ insts, int batch, Dims D,
-                     int view) {
-  constexpr int NG = kShareSlots;
-  __shared__ const float *s_m[NG];
-  __shared__ const float *s_P[NG];
-  __shared__ unsigned s_active;
-  __shared__ float s_part[kAxWarps][NG][2];
-  __shared__ bool s_last;
-  const int g0 = blockIdx.z * NG;
-  const int gn = min(NG, batch - g0);
-  if (threadIdx.x == 0) s_active = 0u;
-  __syncthreads();
-  const long long nr = (long long)D.na * D.nb;
-  if (threadIdx.x < gn) {
-    const Inst &Ib = insts[g0 + threadIdx.x];
-    s_m[threadIdx.x] = Ib.m;
-    s_P[threadIdx.x] = Ib.P + (long long)view * nr;
-    if (((volatile int *)&Ib.s->done)[0] == 0)
-      atomicOr(&s_active, 1u << threadIdx.x);
-  }
-  __syncthreads();
-  const unsigned active = s_active;
-  if (!active) return;
-  const Inst &I0 = insts[g0];
-  const ViewGeo G = view_of(I0, view);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long r = (long long)blockIdx.x * kAxWarps + warp;
-  float ys[NG];
-#pragma unroll
-  for (int g = 0; g < NG; g++) ys[g] = 0.f;
-  float ss = 0.f;
-  if (r < nr) {
-    const int ia = (int)(r % D.na);
-    const RayMarch R = ray_setup(G, D, G.y_det[ia], 0.0f);
-    ray_columns_planar_group<NG, 2>(
-        R, lane, 32, [&](int g, unsigned i) { return s_m[g][i]; }, active, ys, ss);
-    ss = warp_sum(ss);
-#pragma unroll
-    for (int g = 0; g < NG; g++) ys[g] = warp_sum(ys[g]);
-  }
-  if (lane == 0) {
-#pragma unroll
-    for (int g = 0; g < NG; g++) {
-      float c2 = 0.f, bad = 0.f;
-      if (r < nr && g < gn && ((active >> g) & 1u)) {
-        const float yv = ys[g] * G.scale, srv = ss * G.scale;
-        const float c0 = s_P[g][r] - yv;
-        const float cr = c0 / (srv == 0.f ? 1.f : srv);
-        I0.cor[r * kShareSlots + g] = cr;
-        c2 = c0 * c0;
-        bad = isfinite(cr) ? 0.f : 1.f;
-      }
-      s_part[warp][g][0] = c2;
-      s_part[warp][g][1] = bad;
-    }
-  }
-  __syncthreads();
-  const int bid = blockIdx.x, nblocks = gridDim.x;
-  if (threadIdx.x < gn) {
-    const int g = threadIdx.x;
-    float c2 = 0.f, bad = 0.f;
-#pragma unroll
-    for (int w = 0; w < kAxWarps; w++) {
-      c2 += s_part[w][g][0];
-      bad += s_part[w][g][1];
-    }
-    double *part = insts[g0 + g].partials;
-    part[2 * bid] = (double)c2;
-    part[2 * bid + 1] = (double)bad;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(I0.counter, 1u) == (unsigned)nblocks - 1;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  if (threadIdx.x < gn && ((active >> threadIdx.x) & 1u)) {
-    const Inst &Ib = insts[g0 + threadIdx.x];
-    const volatile double *part = Ib.partials;
-    double c2 = 0.0, bad = 0.0;
-    for (int b = 0; b < nblocks; b++) {
-      c2 += part[2 * b];
-      bad += part[2 * b + 1];
-    }
-    Ib.s->dd2_acc += c2;
-    Ib.s->cor_finite = bad == 0.0;
-  }
-  if (threadIdx.x == 0) *I0.counter = 0u;
-}
-
-// ---------------------------------------------------------------------------
 // Shared-geometry backward step: when every instance of a plan has the same
 // geometry and view angles, the chords of a (voxel, bin) pair are the same
 // for all of them.  A block then handles one voxel tile for a group of
@@ -750,16 +649,6 @@ cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
     k_sart_atx<true, 2><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
   else
     k_sart_atx<true, 0><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
-                                  int view, cudaStream_t st) {
-  if (d.nz > 1 || d.nb > 1) return launch_sart_ax(insts, batch, d, view, st);
-  const long long nr = (long long)d.na * d.nb;
-  const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
-  k_sart_ax_shared<<<dim3(blocks, 1, (batch + kShareSlots - 1) / kShareSlots),
-                     kAxThreads, 0, st>>>(insts, batch, d, view);
   return cudaGetLastError();
 }
 

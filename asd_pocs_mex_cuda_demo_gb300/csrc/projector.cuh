@@ -297,68 +297,6 @@ ASD_HD void ray_columns_planar_fast(const RayMarch &R, int first, int step,
   }
 }
 
-// ray_columns_planar_fast applied to G images at once (the images share the
-// ray's cells and weights): column pieces are computed once, then every
-// image's values are loaded and accumulated in the same order as the
-// single-image form, so each ys[g] is bit-identical to a separate call.
-template <int G, int U = 2, class Loader>
-ASD_HD void ray_columns_planar_group(const RayMarch &R, int first, int step,
-                                     Loader ld, unsigned active, float (&ys)[G],
-                                     float &ss) {
-  const bool pos = R.slope1 >= 0;
-  for (int iu0 = first; iu0 < R.nu; iu0 += U * step) {
-    float w_lo[U], w_hi[U];
-    unsigned i_lo[U], i_hi[U];
-    bool f_lo[U], f_hi[U];
-#pragma unroll
-    for (int k = 0; k < U; k++) {
-      const int iu = iu0 + k * step;
-      const float uu1 = (float)(iu - R.nu2);
-      const float uu2 = uu1 + 1;
-      const float ua = pos ? uu1 : uu2, ub = pos ? uu2 : uu1;
-      const float v1 = R.vs + R.slope1 * (ua - R.us) + R.nv2;
-      const float v2 = R.vs + R.slope1 * (ub - R.us) + R.nv2;
-      const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
-      const bool split = cv1 != cv2;
-      const bool mid = cv2 > 0 && cv2 < R.nv;
-      const bool in = iu < R.nu;
-      f_lo[k] = in && cv1 >= 0 && cv1 < R.nv &&
-                (split ? (mid || cv2 == R.nv) : true);
-      f_hi[k] = in && split && cv2 >= 0 && cv2 < R.nv && (mid || cv2 == 0);
-      const float d = v2 - v1;
-      const float l = sqrtf(d * d + 1);
-      const float rv = fast_div(cv2 - v1, d);
-      w_lo[k] = split ? rv * l : l;
-      w_hi[k] = (1 - rv) * l;
-      const unsigned base = (unsigned)iu * R.su;
-      i_lo[k] = base + (unsigned)cv1 * R.sv;
-      i_hi[k] = base + (unsigned)cv2 * R.sv;
-    }
-#pragma unroll
-    for (int k = 0; k < U; k++) {
-      if (f_lo[k]) ss += w_lo[k];
-      if (f_hi[k]) ss += w_hi[k];
-    }
-#pragma unroll
-    for (int g = 0; g < G; g++) {
-      if (!((active >> g) & 1u)) continue;
-      float xl[U], xh[U];
-#pragma unroll
-      for (int k = 0; k < U; k++) {
-        xl[k] = f_lo[k] ? ld(g, i_lo[k]) : 0.f;
-        xh[k] = f_hi[k] ? ld(g, i_hi[k]) : 0.f;
-      }
-      float a = ys[g];
-#pragma unroll
-      for (int k = 0; k < U; k++) {
-        if (f_lo[k]) a += w_lo[k] * xl[k];
-        if (f_hi[k]) a += w_hi[k] * xh[k];
-      }
-      ys[g] = a;
-    }
-  }
-}
-
 // Warp-wide sum; the xor butterfly leaves bit-identical totals in every lane
 // (IEEE addition is commutative).
 __device__ __forceinline__ float warp_sum(float v) {

@@ -40,7 +40,7 @@ extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,
       if (planar && exact)
         ray_columns_planar<true>(R, l, lanes, ld, a, b);
       else if (planar)
-        ray_columns_planar_fast<2>(R, l, lanes, ld, a, b);
+        ray_columns_planar_fast(R, l, lanes, ld, a, b);
       else if (exact)
         ray_columns<true>(R, l, lanes, ld, a, b);
       else
@@ -109,32 +109,4 @@ extern "C" void dm_atx(float *x, const float *yv, float *sc, float c, float s,
         x[idx] = acc * scale;
         sc[idx] = accl * scale;
       }
-}
-
-// ray_columns_planar_group over 3 images against three single-image runs:
-// returns the number of rays whose sums differ in any bit (expected 0).
-extern "C" int dm_group_mismatches(const float *x0, const float *x1,
-                                   const float *x2, float c, float s,
-                                   const float *yd, float SO, float OD,
-                                   int nx, int ny, int na) {
-  const float zd = 0.0f;
-  const ViewGeo G = geo(c, s, yd, &zd, SO, OD, 1.0f, 0.f, 0.f, 1.0f);
-  const Dims D{nx, ny, 1, na, 1};
-  const float *xs[3] = {x0, x1, x2};
-  int bad = 0;
-  for (int ia = 0; ia < na; ia++) {
-    const RayMarch R = ray_setup(G, D, yd[ia], 0.0f);
-    for (int lane = 0; lane < 32; lane++) {
-      float ys[3] = {0.f, 0.f, 0.f}, ss = 0.f;
-      ray_columns_planar_group<3, 2>(
-          R, lane, 32, [&](int g, unsigned i) { return xs[g][i]; }, 7u, ys, ss);
-      for (int g = 0; g < 3; g++) {
-        float y1 = 0.f, s1 = 0.f;
-        ray_columns_planar_fast<2>(R, lane, 32, [&](unsigned i) { return xs[g][i]; },
-                                   y1, s1);
-        if (y1 != ys[g] || s1 != ss) bad++;
-      }
-    }
-  }
-  return bad;
 }

@@ -82,18 +82,3 @@ def test_device_math_matches_oracle(dm, oracle_mod, case):
                       g["SO"], g["OD"], g["scale"], g["det"], g["det"], 1.0, nx, ny, nz,
                       na, nb, staged)
             assert np.array_equal(b, bo) and np.array_equal(sc, co), (a, staged)
-
-
-def test_group_march_matches_single_image_march(dm, oracle_mod):
-    F = C.POINTER(C.c_float)
-    dm.dm_group_mismatches.argtypes = [F, F, F, C.c_float, C.c_float, F, C.c_float,
-                                       C.c_float, C.c_int, C.c_int, C.c_int]
-    n, na = 48, 96
-    rng = np.random.default_rng(3)
-    xs = [rng.random(n * n).astype(np.float32) for _ in range(3)]
-    for a in (0.0, 37.0, 45.0, 133.0):
-        g = oracle_mod.gateway_geometry(-a / 180 * np.pi, 541.0, 408.0, 1.1, 1.0, na, 1)
-        yd = g["y_det"].copy()
-        assert dm.dm_group_mismatches(_p(xs[0]), _p(xs[1]), _p(xs[2]), g["cos_phi"],
-                                      g["sin_phi"], _p(yd), g["SO"], g["OD"], n, n,
-                                      na) == 0, a
