@@ -38,6 +38,10 @@ mxArray *mxCreateNumericMatrix(mwSize m, mwSize n, mxClassID cls,
                                mxComplexity c);
 mxArray *mxCreateNumericArray(mwSize ndim, const mwSize *dims, mxClassID cls,
                               mxComplexity c);
+mxArray *mxCreateStructMatrix(mwSize m, mwSize n, int nfields,
+                              const char **names);
+void mxSetField(mxArray *s, mwIndex i, const char *name, mxArray *v);
+mxArray *mxCreateDoubleScalar(double v);
 int mexPrintf(const char *fmt, ...);
 int mexEvalString(const char *cmd);
 void mexErrMsgTxt(const char *msg);

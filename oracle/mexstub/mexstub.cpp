@@ -75,6 +75,30 @@ mxArray *mxCreateNumericMatrix(mwSize m, mwSize n, mxClassID cls,
 mxArray *mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity c) {
   return mxCreateNumericMatrix(m, n, mxDOUBLE_CLASS, c);
 }
+mxArray *mxCreateStructMatrix(mwSize, mwSize, int nfields, const char **names) {
+  mxArray *a = new mxArray_tag;
+  a->cls = mxSTRUCT_CLASS;
+  a->dims = {1, 1};
+  for (int i = 0; i < nfields; i++) {
+    a->names.push_back(names[i]);
+    a->fields.push_back(nullptr);
+  }
+  return a;
+}
+void mxSetField(mxArray *s, mwIndex, const char *name, mxArray *v) {
+  for (size_t i = 0; i < s->names.size(); i++)
+    if (s->names[i] == name) {
+      s->fields[i] = v;
+      return;
+    }
+  s->names.push_back(name);
+  s->fields.push_back(v);
+}
+mxArray *mxCreateDoubleScalar(double v) {
+  mxArray *a = mxCreateDoubleMatrix(1, 1, mxREAL);
+  *(double *)a->data.data() = v;
+  return a;
+}
 int mexPrintf(const char *fmt, ...) {
   (void)fmt;
   return 0;
@@ -112,11 +136,36 @@ void stub_free(mxArray *a) {
 }
 }
 
-/* renamed mexFunctions of the reference sources (see build_ref.sh) */
-void ref_mex_ax(int, mxArray *[], int, const mxArray *[]);
-void ref_mex_atx(int, mxArray *[], int, const mxArray *[]);
-void ref_mex_tv2d(int, mxArray *[], int, const mxArray *[]);
-void ref_mex_tv3d(int, mxArray *[], int, const mxArray *[]);
+/* renamed mexFunctions of the reference sources (see build_ref.sh); weak so
+ * that the stub also links into libraries without them (the tests of this
+ * repository's own gateways) */
+__attribute__((weak)) void ref_mex_ax(int, mxArray *[], int, const mxArray *[]);
+__attribute__((weak)) void ref_mex_atx(int, mxArray *[], int, const mxArray *[]);
+__attribute__((weak)) void ref_mex_tv2d(int, mxArray *[], int, const mxArray *[]);
+__attribute__((weak)) void ref_mex_tv3d(int, mxArray *[], int, const mxArray *[]);
+
+typedef void (*mex_fn)(int, mxArray *[], int, const mxArray *[]);
+
+/* Calls any mexFunction; returns 0, or 1 with the mexErrMsgTxt text. */
+extern "C" int stub_call_fn(void *fn, int nlhs, mxArray **plhs, int nrhs,
+                            const mxArray **prhs, char *err, int errlen) {
+  for (int i = 0; i < nlhs; i++) plhs[i] = nullptr;
+  try {
+    if (!fn) throw std::runtime_error("mexFunction not linked");
+    ((mex_fn)fn)(nlhs, plhs, nrhs, prhs);
+  } catch (const std::exception &e) {
+    if (err && errlen > 0) {
+      std::strncpy(err, e.what(), (size_t)errlen - 1);
+      err[errlen - 1] = 0;
+    }
+    return 1;
+  }
+  return 0;
+}
+
+extern "C" mxArray *stub_get_field(mxArray *s, const char *name) {
+  return mxGetField(s, 0, name);
+}
 
 /* which: 0 Ax_cone_gpu, 1 Atx_cone_gpu, 2 imgTVGradMin, 3 imgTVGradMin3D.
  * Returns 0, or 1 with the mexErrMsgTxt text in err. */
@@ -124,13 +173,13 @@ extern "C" int stub_call(int which, int nlhs, mxArray **plhs, int nrhs,
                          const mxArray **prhs, char *err, int errlen) {
   for (int i = 0; i < nlhs; i++) plhs[i] = nullptr;
   try {
-    switch (which) {
-      case 0: ref_mex_ax(nlhs, plhs, nrhs, prhs); break;
-      case 1: ref_mex_atx(nlhs, plhs, nrhs, prhs); break;
-      case 2: ref_mex_tv2d(nlhs, plhs, nrhs, prhs); break;
-      case 3: ref_mex_tv3d(nlhs, plhs, nrhs, prhs); break;
-      default: throw std::runtime_error("bad mex id");
-    }
+    mex_fn f = which == 0   ? ref_mex_ax
+               : which == 1 ? ref_mex_atx
+               : which == 2 ? ref_mex_tv2d
+               : which == 3 ? ref_mex_tv3d
+                            : nullptr;
+    if (!f) throw std::runtime_error("mexFunction not linked");
+    f(nlhs, plhs, nrhs, prhs);
   } catch (const std::exception &e) {
     if (err && errlen > 0) {
       std::strncpy(err, e.what(), (size_t)errlen - 1);

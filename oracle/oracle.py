@@ -72,7 +72,15 @@ def lib():
 
 
 def ref_available() -> bool:
-    return os.path.exists(REF_SO)
+    """The reference host build exists here and loads (it is built only where
+    the reference checkout is, and not for another machine's architecture)."""
+    if not os.path.exists(REF_SO):
+        return False
+    try:
+        C.CDLL(REF_SO)
+    except OSError:
+        return False
+    return True
 
 
 def ref():
