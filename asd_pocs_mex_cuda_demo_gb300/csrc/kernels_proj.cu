@@ -76,49 +76,18 @@ struct AtxShared {
   int amin, amax, bmin, bmax;
 };
 
-// Detector bins whose rays can reach a pixel (planar geometry): the bins with
-// centres inside the shadow of the pixel's four corners, widened by 0.05 bin.
-// Rays of the other bins miss the pixel by more than 0.03 pixel widths at
-// the pixel, far beyond the ~1e-4 rounding of the reference's face tests, so
-// their chords are exactly 0 there too.  Returns false (no narrowing) when a
-// corner is not in front of the source.
-__device__ __forceinline__ bool shadow_bins(const ViewGeo &G, const Dims &D,
-                                            float xc, float yc, int &lo,
-                                            int &hi) {
-  const float xr = G.cos_phi * xc + G.sin_phi * yc;
-  const float yr = -G.sin_phi * xc + G.cos_phi * yc;
-  const float hc = 0.5f * G.cos_phi, hs = 0.5f * G.sin_phi;
-  const float inv_det = __frcp_rn(G.dy_det);
-  const float off = D.na * 0.5f - 0.5f;
-  float fmin = 3.0e38f, fmax = -3.0e38f;
-  bool ok = true;
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const float ex = (k & 1) ? 1.f : -1.f, ey = (k & 2) ? 1.f : -1.f;
-    const float px = xr + ex * hc + ey * hs;  // rotated corner
-    const float py = yr - ex * hs + ey * hc;
-    const float den = px + G.SO;
-    ok = ok && den > 1e-3f;
-    const float f = __fdividef(py * G.SD, den) * inv_det + off;
-    fmin = fminf(fmin, f);
-    fmax = fmaxf(fmax, f);
-  }
-  lo = (int)ceilf(fmin - 0.05f);
-  hi = (int)floorf(fmax + 0.05f);
-  return ok;
-}
-
 // Footprint sum of one voxel (Ax_cone_gpu.cu:247-269) for every thread of
 // the block: each block finds the detector window of its voxel tile, stages
 // the window's ray slopes and view values in shared memory, and every lane of
 // a warp then walks the same number of (bin) steps -- the warp's longest
 // footprint -- with the face tests evaluated branch-free, so lanes seeing
-// different rays do not serialise.  In the planar geometry each lane walks
-// only the bins of its pixel's shadow (inside the reference's window); the
-// bins it skips have chords of exactly 0, which add nothing unless a view
-// value is not finite, so a block whose window holds NaN/inf -- or an
-// axis-parallel ray, whose reference chord is not geometric -- walks the
-// whole window.  Pairs are accumulated in the reference's order (ib outer, ia
+// different rays do not serialise.  Each lane walks only the bins of its
+// voxel's shadow (shadow_bins / shadow_bins3, inside the reference's window);
+// the bins it skips have chords of exactly 0, which add nothing unless a view
+// value is not finite, so a block whose window holds NaN/inf, an
+// axis-parallel ray (whose reference chord is not geometric) or detector
+// coordinates off the uniform grid the shadow assumes walks the whole
+// window.  Pairs are accumulated in the reference's order (ib outer, ia
 // inner).  A block whose window does not fit the staging arrays (extreme
 // geometry) falls back to the direct per-pair computation.
 // Must be called by every thread of the block.
@@ -175,9 +144,12 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   bool narrow = true;
   bool allx = true, ally = true;  // every ray of the window x- / y-dominant
   if (staged) {
+    narrow = G.dy_det > 0.0f && (kPlanar || G.dz_det > 0.0f);
     for (int k = threadIdx.x; k < nA; k += kAtxThreads) {
-      const float4 A = ray_tab_a(G, G.y_det[amin + k]);
-      narrow = narrow && A.x != 0.0f && A.y != 0.0f;
+      const float yd = G.y_det[amin + k];
+      const float4 A = ray_tab_a(G, yd);
+      narrow = narrow && A.x != 0.0f && A.y != 0.0f &&
+               on_grid(yd, amin + k, D.na, G.dy_det);
       const bool xf = fabsf(A.x) > fabsf(A.y);
       allx = allx && xf;
       ally = ally && !xf;
@@ -191,6 +163,9 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
       narrow = narrow && isfinite(v);
       sh.ys[k] = v;
     }
+    if (!kPlanar)
+      for (int k = threadIdx.x; k < nB; k += kAtxThreads)
+        narrow = narrow && on_grid(G.z_det[bmin + k], bmin + k, D.nb, G.dz_det);
     narrow = __syncthreads_and(narrow);
     if (!kPlanar) {
       for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads)
@@ -205,16 +180,21 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   const float rx = G.cos_phi * (-G.SO) - w.xc;
   const float ry = G.sin_phi * (-G.SO) - w.yc;
   const float rz = 0.0f - w.zc;
-  int lo = w.a0, hi = w.a1;
-  if (kPlanar && narrow && has) {
-    int slo, shi;
-    if (shadow_bins(G, D, w.xc, w.yc, slo, shi)) {
+  int lo = w.a0, hi = w.a1, blo = w.b0, bhi = w.b1;
+  if (narrow && has) {
+    int slo, shi, tlo, thi;
+    if (kPlanar ? shadow_bins(G, D, w.xc, w.yc, slo, shi)
+                : shadow_bins3(G, D, w.xc, w.yc, w.zc, slo, shi, tlo, thi)) {
       lo = max(lo, slo);
       hi = min(hi, shi);
+      if (!kPlanar) {
+        blo = max(blo, tlo);
+        bhi = min(bhi, thi);
+      }
     }
   }
   const int cntA = has && lo <= hi ? hi - lo + 1 : 0;
-  const int cntB = has ? w.b1 - w.b0 + 1 : 0;
+  const int cntB = has && blo <= bhi ? bhi - blo + 1 : 0;
   const int kA = __reduce_max_sync(0xffffffffu, cntA);
   const int kB = __reduce_max_sync(0xffffffffu, cntB);
   const int a_off = lo - amin;
@@ -237,7 +217,7 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
   }
   for (int kb = 0; kb < kB; kb++) {
     const bool onb = kb < cntB;
-    const int ib = w.b0 + kb;
+    const int ib = blo + kb;
     const float c = kPlanar ? 0.0f : G.z_det[onb ? ib : bmin] - 0.0f;
     const int row = (onb ? ib - bmin : 0) * nA + a_off;
     for (int ka = 0; ka < kA; ka++) {
@@ -384,15 +364,21 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
         voxel_backproject(G, D, w, [&](long long i) { return cor[i]; }, acc, accl);
     } else {
       int lo = has ? w.a0 : 0, hi = has ? w.a1 : -1;
+      int blo = has ? w.b0 : 0, bhi = has ? w.b1 : -1;
       if (narrow && has) {
-        int slo, shi;
-        if (shadow_bins(G, D, w.xc, w.yc, slo, shi)) {
+        int slo, shi, tlo, thi;
+        if (kPlanar ? shadow_bins(G, D, w.xc, w.yc, slo, shi)
+                    : shadow_bins3(G, D, w.xc, w.yc, w.zc, slo, shi, tlo, thi)) {
           lo = max(lo, slo);
           hi = min(hi, shi);
+          if (!kPlanar) {
+            blo = max(blo, tlo);
+            bhi = min(bhi, thi);
+          }
         }
       }
       const int cntA = has && lo <= hi ? hi - lo + 1 : 0;
-      const int cntB = has ? w.b1 - w.b0 + 1 : 0;
+      const int cntB = has && blo <= bhi ? bhi - blo + 1 : 0;
       const int kA = __reduce_max_sync(0xffffffffu, cntA);
       const int kB =
           kPlanar ? (kA > 0 ? 1 : 0) : __reduce_max_sync(0xffffffffu, cntB);
@@ -400,7 +386,7 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
       const float rz = 0.0f - (has ? w.zc : 0.f);
       for (int kb = 0; kb < kB; kb++) {
         const bool onb = kb < cntB;
-        const int ib = w.b0 + kb;
+        const int ib = blo + kb;
         const float c = kPlanar ? 0.0f : (onb ? __ldg(G.z_det + ib) : 1.0f) - 0.0f;
         const int row = onb ? ib * D.na : 0;
         for (int ka = 0; ka < kA; ka++) {
@@ -446,8 +432,8 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
   const ViewGeo G = view_of(I, view);
   const float4 *tabA = I.tabA + (long long)view * D.na;
   const int vf = I.vflags[view];
-  const bool narrow = kPlanar && !(vf & kViewAxisParallel) && I.s->cor_finite &&
-                      G.z_det[0] == 0.0f;
+  const bool narrow = !(vf & kViewAxisParallel) && I.s->cor_finite &&
+                      (!kPlanar || G.z_det[0] == 0.0f);
   sart_atx_tiles<kPlanar, AX>(I, G, D, tabA, narrow);
 }
 
@@ -500,7 +486,7 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
   const float4 *__restrict__ tabC = I0.tabC;
   const int vf = I0.vflags[view];
   const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
-  const bool narrow = kPlanar && planar_ok && !(vf & kViewAxisParallel) && s_finite;
+  const bool narrow = planar_ok && !(vf & kViewAxisParallel) && s_finite;
   int ix, iy, iz;
   const bool valid = tile_voxel(D, ix, iy, iz);
   VoxelWin w;
@@ -537,15 +523,21 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
     }
   } else {
     int lo = has ? w.a0 : 0, hi = has ? w.a1 : -1;
+    int blo = has ? w.b0 : 0, bhi = has ? w.b1 : -1;
     if (narrow && has) {
-      int slo, shi;
-      if (shadow_bins(G, D, w.xc, w.yc, slo, shi)) {
+      int slo, shi, tlo, thi;
+      if (kPlanar ? shadow_bins(G, D, w.xc, w.yc, slo, shi)
+                  : shadow_bins3(G, D, w.xc, w.yc, w.zc, slo, shi, tlo, thi)) {
         lo = max(lo, slo);
         hi = min(hi, shi);
+        if (!kPlanar) {
+          blo = max(blo, tlo);
+          bhi = min(bhi, thi);
+        }
       }
     }
     const int cntA = has && lo <= hi ? hi - lo + 1 : 0;
-    const int cntB = has ? w.b1 - w.b0 + 1 : 0;
+    const int cntB = has && blo <= bhi ? bhi - blo + 1 : 0;
     const int kA = __reduce_max_sync(0xffffffffu, cntA);
     const int kB =
         kPlanar ? (kA > 0 ? 1 : 0) : __reduce_max_sync(0xffffffffu, cntB);
@@ -554,7 +546,7 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
     const float rz = 0.0f - (has ? w.zc : 0.f);
     for (int kb = 0; kb < kB; kb++) {
       const bool onb = kb < cntB;
-      const int ib = w.b0 + kb;
+      const int ib = blo + kb;
       const float c = kPlanar ? 0.0f : (onb ? __ldg(G.z_det + ib) : 1.0f) - 0.0f;
       const int row = onb ? ib * D.na : 0;
       for (int c0 = 0; c0 < kA; c0 += kPairChunk) {

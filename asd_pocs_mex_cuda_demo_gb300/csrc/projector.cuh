@@ -451,6 +451,94 @@ ASD_HD VoxelWin voxel_window(const ViewGeo &G,
   return w;
 }
 
+// ---------------------------------------------------------------------------
+// Shadows.  A ray that misses a voxel box by more than the rounding of the
+// face tests of find_l / find_l_3d (about 1e-4 voxel widths at these
+// distances) has no face hit, so its chord is exactly 0.  On a detector with
+// uniform bins (y_det[i] = (i - na/2 + 0.5) * dy_det, z_det likewise, as every
+// gateway call has) the rays that can meet the box are those whose bin
+// centres lie inside the bounding rectangle of the projections of the box's
+// corners; the functions below return that rectangle widened by 0.05 bin
+// (0.02-0.05 voxel widths at the voxel in these geometries), so every bin they
+// drop has a chord of exactly 0 -- provided no ray is axis-parallel (the
+// reference's chord ignores one coordinate there) and the view values are
+// finite (0 * inf is not 0).  The column of a point depends on its in-plane
+// position only, so the columns come from the four corners of the pixel; the
+// rows from all eight corners.  They return false (no narrowing) when a
+// corner is not in front of the source.
+// ---------------------------------------------------------------------------
+ASD_HD float hd_rcp(float x) {
+#ifdef __CUDA_ARCH__
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
+
+// Detector coordinate v of bin i on the uniform grid (i - n/2 + 0.5) * pitch,
+// to 1e-3 bin (the shadows' 0.05-bin margin absorbs that).
+ASD_HD bool on_grid(float v, int i, int n, float pitch) {
+  return fabsf(v - ((float)i - n * 0.5f + 0.5f) * pitch) <= 1e-3f * pitch;
+}
+
+ASD_HD bool shadow_bins(const ViewGeo &G, const Dims &D, float xc, float yc,
+                        int &lo, int &hi) {
+  const float xr = G.cos_phi * xc + G.sin_phi * yc;
+  const float yr = -G.sin_phi * xc + G.cos_phi * yc;
+  const float hc = 0.5f * G.cos_phi, hs = 0.5f * G.sin_phi;
+  const float inv_det = hd_rcp(G.dy_det);
+  const float off = D.na * 0.5f - 0.5f;
+  float fmin = 3.0e38f, fmax = -3.0e38f;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float ex = (k & 1) ? 1.f : -1.f, ey = (k & 2) ? 1.f : -1.f;
+    const float px = xr + ex * hc + ey * hs;  // rotated corner
+    const float py = yr - ex * hs + ey * hc;
+    const float den = px + G.SO;
+    ok = ok && den > 1e-3f;
+    const float f = fast_div(py * G.SD, den) * inv_det + off;
+    fmin = fminf(fmin, f);
+    fmax = fmaxf(fmax, f);
+  }
+  lo = (int)ceilf(fmin - 0.05f);
+  hi = (int)floorf(fmax + 0.05f);
+  return ok;
+}
+
+ASD_HD bool shadow_bins3(const ViewGeo &G, const Dims &D, float xc, float yc,
+                         float zc, int &alo, int &ahi, int &blo, int &bhi) {
+  const float xr = G.cos_phi * xc + G.sin_phi * yc;
+  const float yr = -G.sin_phi * xc + G.cos_phi * yc;
+  const float hc = 0.5f * G.cos_phi, hs = 0.5f * G.sin_phi;
+  const float inv_a = hd_rcp(G.dy_det), inv_b = hd_rcp(G.dz_det);
+  const float offa = D.na * 0.5f - 0.5f, offb = D.nb * 0.5f - 0.5f;
+  const float hz = 0.5f * G.dz;
+  const float zlo = (zc - hz) * inv_b, zhi = (zc + hz) * inv_b;
+  float umin = 3.0e38f, umax = -3.0e38f, vmin = 3.0e38f, vmax = -3.0e38f;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float ex = (k & 1) ? 1.f : -1.f, ey = (k & 2) ? 1.f : -1.f;
+    const float px = xr + ex * hc + ey * hs;
+    const float py = yr - ex * hs + ey * hc;
+    const float den = px + G.SO;
+    ok = ok && den > 1e-3f;
+    const float q = fast_div(G.SD, den);  // magnification at this corner
+    const float u = py * q * inv_a + offa;
+    const float v0 = zlo * q + offb, v1 = zhi * q + offb;
+    umin = fminf(umin, u);
+    umax = fmaxf(umax, u);
+    vmin = fminf(vmin, fminf(v0, v1));
+    vmax = fmaxf(vmax, fmaxf(v0, v1));
+  }
+  alo = (int)ceilf(umin - 0.05f);
+  ahi = (int)floorf(umax + 0.05f);
+  blo = (int)ceilf(vmin - 0.05f);
+  bhi = (int)floorf(vmax + 0.05f);
+  return ok;
+}
+
 // Sums l*y and l over the voxel's footprint (reference loop order: ib outer,
 // ia inner; Ax_cone_gpu.cu:255-269).
 template <class YLoad>

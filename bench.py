@@ -1,20 +1,26 @@
 #!/usr/bin/env python
 """ASD-POCS reconstructions per second on one GB300 (or N replicas).
 
-Workload (the sparse-view clinical-head-slice configuration): 512x512
-seeded random-ellipse phantoms (0-0.04 /mm), 60 views evenly spaced over
-360 deg, 888 detector bins at 1.0 mm, SID 541 / SDD 949 mm (voxel 0.9887 mm
-by the field-of-view rule), Poisson noise at I0 = 1e5 photons per bin,
-100 ASD-POCS iterations (20 TV steps each, alpha 0.2, alpha_red 0.95,
-r_max 0.95).  Synthetic seeded inputs stand in for real scans.
+Default workload (``--workload fan2d``, the sparse-view clinical head
+slice): 512x512 seeded random-ellipse phantoms (0-0.04 /mm), 60 views
+evenly spaced over 360 deg, 888 detector bins at 1.0 mm, SID 541 / SDD 949
+mm (voxel 0.9887 mm by the field-of-view rule), Poisson noise at I0 = 1e5
+photons per bin, 100 ASD-POCS iterations (20 TV steps each, alpha 0.2,
+alpha_red 0.95, r_max 0.95), a batch of 64 reconstructions per GPU.
 
-One step = one batch of --batch reconstructions run to completion from
-their sinograms.  ``value`` is device-resident throughput (inputs in HBM,
-CUDA events on the plan's stream); ``e2e`` runs the same batch through the
-C ABI with host buffers, the sinogram upload and the image download inside
-the timed region.  ``--impl reference`` times the reference's CPU path
-instead (its host build where present, else the C restatement of it), on
-all host cores, over a bounded sample of the same workload.
+``--workload cone3d``: one 256^3 modified Shepp-Logan volume (1 mm voxels,
+intensities scaled to 0.02 /mm so I0 = 5e4 photon statistics are
+meaningful), 360 projections over 360 deg on a 512x512 flat detector at 0.8
+mm, SID 1000 / SDD 1500 mm, 50 ASD-POCS iterations.
+
+Synthetic seeded inputs stand in for real scans.  One step = one batch of
+reconstructions run to completion from their sinograms.  ``value`` is
+device-resident throughput (inputs in HBM, CUDA events on the plan's
+stream); ``e2e`` runs the same batch through the C ABI with host buffers,
+the sinogram upload and the image download inside the timed region.
+``--impl reference`` times the reference's CPU path instead (its host build
+where present, else the C restatement of it), on all host cores, over a
+bounded sample of the same workload.
 """
 from __future__ import annotations
 
@@ -33,9 +39,30 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "ASD-POCS recons/s and p99 latency, batched/served vs plain, same GPU at matched RMSE"
-N_PIX, N_BINS, N_VIEWS, SO, OD, DET = 512, 888, 60, 541.0, 408.0, 1.0
-I0_PHOTONS = 1e5
-WORKLOAD = "2D fan-beam sparse-view ASD-POCS, 512^2, 60 views/360deg, 888 bins, I0=1e5, 100 it"
+
+WORKLOADS = {
+    "fan2d": dict(
+        label="2D fan-beam sparse-view ASD-POCS, 512^2, 60 views/360deg, 888 bins, "
+              "I0=1e5, 100 it",
+        nx=512, ny=512, nz=1, na=888, nb=1, nv=60, SO=541.0, OD=408.0, det=1.0,
+        vx=None, I0=1e5, iters=100, ng=20, batch=64, phantom="ellipses"),
+    "cone3d": dict(
+        label="3D cone-beam ASD-POCS, 256^3 Shepp-Logan, 360 views/360deg, 512x512 "
+              "detector at 0.8 mm, SID 1000 / SDD 1500, I0=5e4, 50 it",
+        nx=256, ny=256, nz=256, na=512, nb=512, nv=360, SO=1000.0, OD=500.0, det=0.8,
+        vx=1.0, I0=5e4, iters=50, ng=20, batch=1, phantom="shepp_logan"),
+}
+SHEPP_LOGAN_SCALE = 0.02  # 1/mm per unit phantom intensity (cone3d)
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per instance and
+# launch of each iteration kernel, from `ncu --set full --clock-control none`
+# captures of the 2D fan-beam workload at batch 16 (one shared-geometry
+# group); the traffic is one read of each instance's image, so it scales with
+# the batch.
+NCU_DRAM_PER_INSTANCE = {
+    "fan2d": {"sart_atx": 16.897e6 / 16, "sart_ax": 15.241e6 / 16,
+              "tv_step": 16.985e6 / 16},
+}
 
 
 def parse():
@@ -44,11 +71,18 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--batch", type=int, default=64)
-    ap.add_argument("--iters", type=int, default=100)
+    ap.add_argument("--workload", default="fan2d", choices=sorted(WORKLOADS))
+    ap.add_argument("--batch", type=int, default=None)
+    ap.add_argument("--iters", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    return ap.parse_args()
+    args = ap.parse_args()
+    W = dict(WORKLOADS[args.workload])
+    if args.batch is not None:
+        W["batch"] = args.batch
+    if args.iters is not None:
+        W["iters"] = args.iters
+    return args, W
 
 
 def dist_init(n):
@@ -79,51 +113,73 @@ def allmax(pg, v):
     return float(t.item())
 
 
-def para_for(seed):
+def voxel_size(W):
     from asd_pocs_mex_cuda_demo_gb300 import phantoms
 
-    vx = phantoms.fov_voxel_size(SO, OD, DET, N_BINS, N_PIX)
-    return dict(SO=SO, OD=OD, vxlsize=vx, detsize=DET, nx=N_PIX, ny=N_PIX, nz=1,
-                na=N_BINS, nb=1, maxnumIter=0, numOfgradients=20, alpha=0.2,
+    if W["vx"] is not None:
+        return W["vx"]
+    return phantoms.fov_voxel_size(W["SO"], W["OD"], W["det"], W["na"], W["nx"])
+
+
+def para_for(W):
+    return dict(SO=W["SO"], OD=W["OD"], vxlsize=voxel_size(W), detsize=W["det"],
+                nx=W["nx"], ny=W["ny"], nz=W["nz"], na=W["na"], nb=W["nb"],
+                maxnumIter=W["iters"], numOfgradients=W["ng"], alpha=0.2,
                 alpha_red=0.95, r_max=0.95, beta=1.0, beta_red=0.995)
 
 
-def make_inputs(B, iters, seed0, device):
-    """Seeded phantoms, their noiseless projections (GPU projector) and
-    Poisson-noise sinograms.  Setup only; not timed."""
+def phantom(W, seed):
+    from asd_pocs_mex_cuda_demo_gb300 import phantoms
+
+    if W["phantom"] == "ellipses":
+        return phantoms.random_ellipses(W["nx"], seed).astype(np.float32)
+    return (phantoms.shepp_logan_3d(W["nx"]) * SHEPP_LOGAN_SCALE).astype(np.float32)
+
+
+def make_inputs(W, seed0, device):
+    """Seeded phantoms, their projections (GPU projector, the launcher-level
+    geometry of the mex gateway) and Poisson-noise sinograms.  Setup only;
+    not timed.  Identical phantoms are generated once."""
     import torch
 
     from asd_pocs_mex_cuda_demo_gb300 import phantoms
     from asd_pocs_mex_cuda_demo_gb300._lib import check, load
 
     L = load()
-    phi = phantoms.views(N_VIEWS)
-    paras, Ps, I0s = [], [], []
+    B, na, nb, nv = W["batch"], W["na"], W["nb"], W["nv"]
+    nx, ny, nz = W["nx"], W["ny"], W["nz"]
+    phi = phantoms.views(nv)
+    vx = voxel_size(W)
+    sc = np.float32(vx)
+    det = np.float32(W["det"]) / sc
     st = torch.cuda.current_stream().cuda_stream
+    ydet = torch.tensor(((np.arange(na) - na / 2.0 + 0.5) * np.float64(det))
+                        .astype(np.float32), device=device)
+    zdet = torch.tensor(((np.arange(nb) - nb / 2.0 + 0.5) * np.float64(det))
+                        .astype(np.float32), device=device)
+    so, od = float(np.float32(W["SO"]) / sc), float(np.float32(W["OD"]) / sc)
+    paras, Ps, I0s = [], [], []
+    cache = {}
     for b in range(B):
-        p = para_for(seed0 + b)
-        p["maxnumIter"] = iters
-        x = phantoms.random_ellipses(N_PIX, seed0 + b).astype(np.float32)
-        xd = torch.tensor(x, device=device)
-        y = torch.empty(N_BINS * N_VIEWS, device=device)
-        sr = torch.empty(N_BINS, device=device)
-        vx = p["vxlsize"]
-        sc = np.float32(vx)
-        det = np.float32(DET) / sc
-        ydet = torch.tensor(((np.arange(N_BINS) - N_BINS / 2.0 + 0.5) * np.float64(det))
-                            .astype(np.float32), device=device)
-        zdet = torch.zeros(1, device=device)
-        for v, a in enumerate(phi):
-            ph = np.float32(-(a / 180.0 * np.pi))
-            check(L.asdpocs_ax_device(xd.data_ptr(), y.data_ptr() + 4 * N_BINS * v,
-                                      sr.data_ptr(), float(np.cos(ph)), float(np.sin(ph)),
-                                      ydet.data_ptr(), zdet.data_ptr(),
-                                      float(np.float32(SO) / sc), float(np.float32(OD) / sc),
-                                      float(sc), 1.0, N_PIX, N_PIX, 1, N_BINS, 1, st))
-        torch.cuda.synchronize()
-        P = phantoms.poisson_noise(y.cpu().numpy().astype(np.float64), I0_PHOTONS,
-                                   seed=1000 + seed0 + b)
-        paras.append(p)
+        seed = seed0 + b
+        key = seed if W["phantom"] == "ellipses" else 0
+        if key not in cache:
+            x = phantom(W, seed)
+            xd = torch.tensor(x, device=device)
+            y = torch.empty(na * nb * nv, device=device)
+            sr = torch.empty(na * nb, device=device)
+            for v, a in enumerate(phi):
+                ph = np.float32(-(a / 180.0 * np.pi))
+                check(L.asdpocs_ax_device(xd.data_ptr(), y.data_ptr() + 4 * na * nb * v,
+                                          sr.data_ptr(), float(np.cos(ph)), float(np.sin(ph)),
+                                          ydet.data_ptr(), zdet.data_ptr(), so, od,
+                                          float(sc), 1.0, nx, ny, nz, na, nb, st))
+            torch.cuda.synchronize()
+            cache = {key: (x, y.cpu().numpy().astype(np.float64))}
+            del xd, y, sr
+        x, clean = cache[key]
+        P = phantoms.poisson_noise(clean, W["I0"], seed=1000 + seed)
+        paras.append(para_for(W))
         Ps.append(P.astype(np.float32))
         I0s.append(x)
     return paras, [phi] * B, Ps, I0s
@@ -192,32 +248,71 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(paras, phis, Ps, sample_iters):
-    """The C restatement of the reference's CPU path (OpenMP, all host
-    threads) on one reconstruction of the workload, `sample_iters` iterations,
-    extrapolated to the full iteration count."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    kind = "port"
+    return oracle
+
+
+def cpu_sample_3d(W, impl, cores, views=2):
+    """Seconds per ASD-POCS iteration of the cone-beam workload on the host,
+    from a timed sample: `views` forward + backward projections and one 3D
+    TV step, scaled to nv views and ng steps (the SART vector updates, a few
+    passes over the volume per view, are left out, so the figure favours the
+    CPU)."""
+    oracle = _oracle()
+    from asd_pocs_mex_cuda_demo_gb300 import phantoms
+
+    nx, ny, nz, na, nb = W["nx"], W["ny"], W["nz"], W["na"], W["nb"]
+    x = phantom(W, 0)
+    phi = phantoms.views(W["nv"])
+    ax = oracle.ref_launch_ax if impl == "reference" else oracle.ax
+    atx = oracle.ref_launch_atx if impl == "reference" else oracle.atx
+    t_proj = 0.0
+    for v in range(views):
+        g = oracle.gateway_geometry(-phi[v] / 180 * np.pi, W["SO"], W["OD"], voxel_size(W),
+                                    W["det"], na, nb)
+        t = time.perf_counter()
+        y, _ = ax(x, g, nx, ny, nz, nthreads=cores)
+        atx(y, g, nx, ny, nz, nthreads=cores)
+        t_proj += time.perf_counter() - t
+    img = x.astype(np.float64).reshape((nx, ny, nz), order="F")
+    t = time.perf_counter()
+    oracle.tv(img, 0.01, 1, 1, nthreads=cores)
+    t_tv = time.perf_counter() - t
+    per_iter = t_proj / views * W["nv"] + t_tv * W["ng"]
+    sample = (f"{views} of {W['nv']} views (Ax+Atx) and 1 of {W['ng']} TV steps of one "
+              f"iteration, {t_proj + t_tv:.1f} s, scaled to {W['iters']} iterations")
+    return per_iter, sample
+
+
+def cpu_baseline(W, paras, phis, Ps, sample_iters):
+    """The C restatement of the reference's CPU path (OpenMP, all host
+    threads) on one reconstruction of the workload, sampled and extrapolated
+    to the full iteration count."""
     cores = os.cpu_count() or 1
+    if W["nz"] > 1:
+        per_iter, sample = cpu_sample_3d(W, "oracle", cores)
+        return {"value": 1.0 / (per_iter * W["iters"]), "unit": "recons/s", "cores": cores,
+                "kind": "port", "sample": sample}
+    oracle = _oracle()
     p = dict(paras[0], phi_vec=phis[0], maxnumIter=sample_iters)
-    P = Ps[0].astype(np.float64).reshape(N_BINS, N_VIEWS, order="F")
+    P = Ps[0].astype(np.float64).reshape(W["na"] * W["nb"], W["nv"], order="F")
     t = time.perf_counter()
     oracle.asdpocs(P, p, nthreads=cores)
     dt = time.perf_counter() - t
-    full = paras[0]["maxnumIter"]
-    per_recon = dt * full / sample_iters
-    return {"value": 1.0 / per_recon, "unit": "recons/s", "cores": cores, "kind": kind,
-            "sample": f"{sample_iters} of {full} ASD-POCS iterations of one 512^2 "
-                      f"reconstruction ({dt:.1f} s), extrapolated"}
+    per_recon = dt * W["iters"] / sample_iters
+    return {"value": 1.0 / per_recon, "unit": "recons/s", "cores": cores, "kind": "port",
+            "sample": f"{sample_iters} of {W['iters']} ASD-POCS iterations of one "
+                      f"{W['nx']}^2 reconstruction ({dt:.1f} s), extrapolated"}
 
 
 def main():
-    args = parse()
+    args, W = parse()
     rank, world, local, pg = dist_init(args.gpus)
     if args.impl == "reference":
-        return reference_arm(args, rank, world, pg)
+        return reference_arm(args, W, rank, world, pg)
     import torch
 
     import asd_pocs_mex_cuda_demo_gb300 as pkg
@@ -226,8 +321,10 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     pkg.load()
-    B, iters = args.batch, args.iters
-    paras, phis, Ps, I0s = make_inputs(B, iters, seed0=100 * rank, device=dev)
+    B, iters, nv, ng = W["batch"], W["iters"], W["nv"], W["ng"]
+    N = W["nx"] * W["ny"] * W["nz"]
+    M = W["na"] * W["nb"]
+    paras, phis, Ps, I0s = make_inputs(W, seed0=100 * rank, device=dev)
     stream = torch.cuda.Stream(device=dev)
     plan = pkg.Plan(paras, phis, stream=stream.cuda_stream)
     for b in range(B):
@@ -264,49 +361,64 @@ def main():
     ms = allmax(pg, statistics.mean(times))
     value = B * world / (ms / 1e3)
     rmse = [plan.stats(b)["RMSE"][-1] for b in range(B)]
-    kernels_per_step = iters * (2 * N_VIEWS + 1 + 2 * 20 + 1)
+    # per iteration: forward + backward step per view, after-sweep, one fused
+    # launch per TV step, finish
+    kernels_per_step = iters * (2 * nv + 1 + ng + 1)
 
     # ---- plain path (one reconstruction per plan, same kernels) for context
-    plain = pkg.Plan(paras[:1], phis[:1], stream=stream.cuda_stream)
-    plain.set_sinogram(0, Ps[0])
-    plain.set_reference(0, I0s[0])
-    plain.reset()
-    plain.run()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    plain.reset()
-    e0.record(stream)
-    plain.run(use_graph=True, sync=False)
-    e1.record(stream)
-    e1.synchronize()
-    plain_ms = e0.elapsed_time(e1)
-    plain_rmse = plain.stats(0)["RMSE"][-1]
-    plain_img = plain.image(0)
-    batch_img = plan.image(0)
-    plain.close()
+    plain_info = None
+    if B > 1:
+        plain = pkg.Plan(paras[:1], phis[:1], stream=stream.cuda_stream)
+        plain.set_sinogram(0, Ps[0])
+        plain.set_reference(0, I0s[0])
+        plain.reset()
+        plain.run()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        plain.reset()
+        e0.record(stream)
+        plain.run(use_graph=True, sync=False)
+        e1.record(stream)
+        e1.synchronize()
+        plain_ms = e0.elapsed_time(e1)
+        plain_rmse = plain.stats(0)["RMSE"][-1]
+        plain_img = plain.image(0)
+        batch_img = plan.image(0)
+        plain.close()
+        plain_info = {"recons_per_s": 1e3 / plain_ms, "ms_per_recon": plain_ms,
+                      "rmse": plain_rmse, "batched_rmse": rmse[0],
+                      "batch_equals_plain_bitwise": bool(np.array_equal(plain_img,
+                                                                        batch_img)),
+                      "batched_speedup": value / world / (1e3 / plain_ms)}
 
     # ---- per-kernel device times (CUDA events on the plan's stream)
-    vx = paras[0]["vxlsize"]
-    nnz = statistics.mean(roofline.nnz_per_view(a, SO, OD, vx, DET, N_PIX, N_PIX, 1,
-                                                N_BINS, 1) for a in phis[0][::6])
-    N, M = N_PIX * N_PIX, N_BINS
+    vx = voxel_size(W)
+    nnz = statistics.mean(
+        roofline.nnz_per_view(a, W["SO"], W["OD"], vx, W["det"], W["nx"], W["ny"], W["nz"],
+                              W["na"], W["nb"]) for a in phis[0][::max(1, nv // 10)])
+    reps = 30 if N * B <= (1 << 26) else 5
     plan.reset()
-    t_ax = plan.time_phase(0, 30)
-    t_atx = plan.time_phase(1, 30)
-    t_tv = plan.time_phase(2, 20)
+    t_ax = plan.time_phase(0, reps)
+    t_atx = plan.time_phase(1, reps)
+    t_tv = plan.time_phase(2, reps)
     plan.reset()
     kern = {
-        "sart_ax": {"ms": t_ax, "per_iter_ms": t_ax * N_VIEWS,
+        "sart_ax": {"ms": t_ax, "per_iter_ms": t_ax * nv,
                     "bytes": B * roofline.ax_bytes(nnz, M)},
-        "sart_atx": {"ms": t_atx, "per_iter_ms": t_atx * N_VIEWS,
+        "sart_atx": {"ms": t_atx, "per_iter_ms": t_atx * nv,
                      "bytes": B * roofline.atx_bytes(nnz, N)},
-        "tv_step": {"ms": t_tv, "per_iter_ms": t_tv * 20,
+        "tv_step": {"ms": t_tv, "per_iter_ms": t_tv * ng,
                     "bytes": B * roofline.tv_step_bytes(N)},
     }
+    for k in kern.values():
+        k["GBps"] = k["bytes"] / (k["ms"] / 1e3) / 1e9
+    ncu_dram = NCU_DRAM_PER_INSTANCE.get(args.workload, {})
+    for name, k in kern.items():
+        k["traffic"] = ncu_dram[name] * B if name in ncu_dram else None
     top = max(kern, key=lambda k: kern[k]["per_iter_ms"])
     peak, peak_kind = measured_peaks()
-    achieved = kern[top]["bytes"] / (kern[top]["ms"] / 1e3) / 1e9
+    achieved = kern[top]["GBps"]
     tot_iter = sum(k["per_iter_ms"] for k in kern.values())
 
     # ---- end to end through the C ABI with host buffers
@@ -323,48 +435,49 @@ def main():
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             for b in range(B):
-                check(L.asdpocs_plan_set_sinogram(plan._h, b, C.c_void_p(pinned_P[b].data_ptr()), 0))
+                check(L.asdpocs_plan_set_sinogram(plan._h, b,
+                                                  C.c_void_p(pinned_P[b].data_ptr()), 0))
             plan.reset()
             plan.run(use_graph=True, sync=False)
             for b in range(B):
-                check(L.asdpocs_plan_get_image(plan._h, b, C.c_void_p(out_img[b].data_ptr()), 0))
+                check(L.asdpocs_plan_get_image(plan._h, b, C.c_void_p(out_img[b].data_ptr()),
+                                               0))
             et.append(time.perf_counter() - t0)
         e_s = allmax(pg, statistics.mean(et))
         e2e = {"value": B * world / e_s, "unit": "recons/s",
-               "h2d_bytes_per_step": B * N_BINS * N_VIEWS * 4,
-               "d2h_bytes_per_step": B * N * 4}
+               "h2d_bytes_per_step": B * M * nv * 4, "d2h_bytes_per_step": B * N * 4}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(paras, phis, Ps, sample_iters=2)
+        cpu = cpu_baseline(W, paras, phis, Ps, sample_iters=64)
 
     if rank == 0:
+        dims = (f"{W['nx']}^2" if W["nz"] == 1 else f"{W['nx']}^3")
         line = {
             "metric": METRIC, "value": value, "unit": "recons/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded random-ellipse phantoms, Poisson noise)",
-            "config": {"workload": WORKLOAD, "batch_per_gpu": B, "iterations": iters,
-                       "nx": N_PIX, "views": N_VIEWS, "bins": N_BINS, "tv_steps": 20,
-                       "parallelism": f"replicas x{world}",
+            "dtype": "f32",
+            "data": "synthetic (seeded " + ("random-ellipse" if W["phantom"] == "ellipses"
+                                           else "Shepp-Logan") + " phantoms, Poisson noise)",
+            "config": {"workload": W["label"], "batch_per_gpu": B, "iterations": iters,
+                       "volume": dims, "views": nv, "bins": [W["na"], W["nb"]],
+                       "tv_steps": ng, "parallelism": f"replicas x{world}",
                        "l2": "256 MB buffer written between timed steps; resident set "
                              f"{plan.nbytes / 2**20:.0f} MB > 129 MB L2",
                        "graph": "one ASD-POCS iteration captured, replayed per iteration"},
-            "latency_ms": {"p50": ms, "p99": max(times),
+            "latency_ms": {"p50": statistics.median(times), "p99": max(times),
                            "note": "every reconstruction of a batch completes at the end "
                                    "of its step"},
-            "plain": {"recons_per_s": 1e3 / plain_ms, "ms_per_recon": plain_ms,
-                      "rmse": plain_rmse, "batched_rmse": rmse[0],
-                      "batch_equals_plain_bitwise": bool(np.array_equal(plain_img, batch_img)),
-                      "batched_speedup": value / world / (1e3 / plain_ms)},
+            "plain": plain_info,
             "rmse_vs_phantom": {"mean": float(np.mean(rmse)), "max": float(np.max(rmse))},
             "roofline": {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": None,
+                         "traffic": kern[top]["traffic"],
                          "bytes_per_launch": kern[top]["bytes"],
                          "ms_per_launch": kern[top]["ms"],
                          "share_of_iteration": kern[top]["per_iter_ms"] / tot_iter,
-                         "kernels": kern},
+                         "nnz_per_view": nnz, "kernels": kern},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clk,
@@ -374,45 +487,50 @@ def main():
     plan.close()
 
 
-def reference_arm(args, rank, world, pg):
+def reference_arm(args, W, rank, world, pg):
     """The reference's CPU implementation of the path on the host cores."""
     if rank != 0:
         return 0
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-
+    oracle = _oracle()
     from asd_pocs_mex_cuda_demo_gb300 import phantoms
 
     cores = os.cpu_count() or 1
     impl = "reference" if oracle.ref_available() else "oracle"
     kind = "reference" if impl == "reference" else "port"
-    p = para_for(0)
-    p["maxnumIter"] = 1
-    phi = phantoms.views(N_VIEWS)
-    x = phantoms.random_ellipses(N_PIX, 0)
-    P = np.zeros((N_BINS, N_VIEWS))
-    for v, a in enumerate(phi):
-        g = oracle.gateway_geometry(-a / 180 * np.pi, SO, OD, p["vxlsize"], DET, N_BINS, 1)
-        P[:, v] = oracle.ax(x.astype(np.float32), g, N_PIX, N_PIX, 1, nthreads=cores)[0]
-    P = phantoms.poisson_noise(P, I0_PHOTONS, seed=1000)
-    p["phi_vec"] = phi
-    for _ in range(args.warmup):
-        oracle.asdpocs(P, dict(p, maxnumIter=1), impl=impl, nthreads=cores)
     times = []
-    for _ in range(args.steps):
-        t = time.perf_counter()
-        oracle.asdpocs(P, dict(p, maxnumIter=1), impl=impl, nthreads=cores)
-        times.append(time.perf_counter() - t)
+    if W["nz"] > 1:
+        for _ in range(args.warmup):
+            cpu_sample_3d(W, impl, cores, views=1)
+        for _ in range(args.steps):
+            per_iter, sample = cpu_sample_3d(W, impl, cores, views=1)
+            times.append(per_iter)
+    else:
+        p = para_for(W)
+        phi = phantoms.views(W["nv"])
+        x = phantom(W, 0)
+        P = np.zeros((W["na"], W["nv"]))
+        for v, a in enumerate(phi):
+            g = oracle.gateway_geometry(-a / 180 * np.pi, W["SO"], W["OD"], p["vxlsize"],
+                                        W["det"], W["na"], 1)
+            P[:, v] = oracle.ax(x, g, W["nx"], W["ny"], 1, nthreads=cores)[0]
+        P = phantoms.poisson_noise(P, W["I0"], seed=1000)
+        p["phi_vec"] = phi
+        for _ in range(args.warmup):
+            oracle.asdpocs(P, dict(p, maxnumIter=1), impl=impl, nthreads=cores)
+        for _ in range(args.steps):
+            t = time.perf_counter()
+            oracle.asdpocs(P, dict(p, maxnumIter=1), impl=impl, nthreads=cores)
+            times.append(time.perf_counter() - t)
+        sample = (f"one of {W['iters']} ASD-POCS iterations per step ({W['nv']} views SART "
+                  f"+ {W['ng']} TV steps) of one {W['nx']}^2 reconstruction, extrapolated")
     per_iter = statistics.mean(times)
-    value = 1.0 / (per_iter * args.iters)
-    sample = (f"one of {args.iters} ASD-POCS iterations per step (60 views SART + 20 TV "
-              f"steps) of one 512^2 reconstruction, extrapolated")
+    value = 1.0 / (per_iter * W["iters"])
     print(json.dumps({
         "metric": METRIC, "impl": "reference", "value": value, "unit": "recons/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per_iter * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "iterations": args.iters},
+        "config": {"workload": W["label"], "iterations": W["iters"]},
         "cpu_baseline": {"value": value, "unit": "recons/s", "cores": cores, "kind": kind,
                          "sample": sample},
         "e2e": {"value": value, "unit": "recons/s", "h2d_bytes_per_step": 0,

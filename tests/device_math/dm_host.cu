@@ -8,7 +8,9 @@
 //              kernels' division-free ones (exact=0);
 //   dm_atx  -- Atx through the staged ray tables and the branch-free chords
 //              (ray_tab_a / ray_tab_c, chord_planar_bf / chord3_bf) as the
-//              kernels run it (staged=1), or the direct per-pair form.
+//              kernels run it (staged=1), the same restricted to each voxel's
+//              shadow (shadow_bins / shadow_bins3) under the kernels'
+//              conditions (staged=2), or the direct per-pair form.
 // Compiled with -ffp-contract=off so the host compiler fuses nothing.
 #include <string.h>
 
@@ -75,6 +77,16 @@ extern "C" void dm_atx(float *x, const float *yv, float *sc, float c, float s,
   if (!planar)
     for (long long k = 0; k < (long long)na * nb; k++)
       tC[k] = ray_tab_c(tA[k % na], zd[k / na]);
+  // the kernels narrow to the shadow only for views with no axis-parallel
+  // ray, finite values and bins on the uniform grid
+  bool narrow = staged == 2 && ddy > 0.0f && (planar || ddz > 0.0f);
+  for (int ia = 0; ia < na; ia++)
+    narrow = narrow && tA[ia].x != 0.0f && tA[ia].y != 0.0f &&
+             on_grid(yd[ia], ia, na, ddy);
+  for (int ib = 0; ib < nb && !planar; ib++)
+    narrow = narrow && on_grid(zd[ib], ib, nb, ddz);
+  for (long long k = 0; k < (long long)na * nb; k++)
+    narrow = narrow && isfinite(yv[k]);
   for (int iz = 0; iz < nz; iz++)
     for (int iy = 0; iy < ny; iy++)
       for (int ix = 0; ix < nx; ix++) {
@@ -87,9 +99,22 @@ extern "C" void dm_atx(float *x, const float *yv, float *sc, float c, float s,
           const float rx = G.cos_phi * (-G.SO) - w.xc;
           const float ry = G.sin_phi * (-G.SO) - w.yc;
           const float rz = 0.0f - w.zc;
-          for (int ib = w.b0; ib <= w.b1; ib++) {
+          int a0 = w.a0, a1 = w.a1, b0 = w.b0, b1 = w.b1;
+          if (narrow) {
+            int slo, shi, tlo, thi;
+            if (planar ? shadow_bins(G, D, w.xc, w.yc, slo, shi)
+                       : shadow_bins3(G, D, w.xc, w.yc, w.zc, slo, shi, tlo, thi)) {
+              a0 = a0 > slo ? a0 : slo;
+              a1 = a1 < shi ? a1 : shi;
+              if (!planar) {
+                b0 = b0 > tlo ? b0 : tlo;
+                b1 = b1 < thi ? b1 : thi;
+              }
+            }
+          }
+          for (int ib = b0; ib <= b1; ib++) {
             const float cc = zd[ib] - 0.0f;
-            for (int ia = w.a0; ia <= w.a1; ia++) {
+            for (int ia = a0; ia <= a1; ia++) {
               const long long k = (long long)ib * na + ia;
               float l;
               if (planar && tA[ia].x != 0.0f && tA[ia].y != 0.0f)

@@ -2,7 +2,8 @@
 against the oracle -- checks the float logic of the GPU code without a GPU.
 
 * Atx through the staged ray tables is bit-identical to the oracle (and so
-  to the reference), planar and 3D.
+  to the reference), planar and 3D, over the reference's whole footprint
+  window and over each voxel's shadow only (the kernels' narrowing).
 * Ax with one partial sum per ray and the reference's weight expressions is
   bit-identical; with the 32-lane split and xor-butterfly combination of the
   warp kernels, and their division-free weights, it stays within 1e-6.
@@ -51,6 +52,10 @@ CASES = [
     (40, 40, 1, 80, 2, 405.941, 500.31, 0.6),
     (24, 20, 12, 48, 24, 1000.0, 500.0, 3.2),
     (13, 11, 7, 27, 9, 300.0, 200.0, 1.3),
+    # cone beam shaped like 256^3 / 512^2 detector at 0.8 mm, SID 1000 / SDD 1500
+    # mm, scaled down (same magnification and bins per voxel)
+    (32, 32, 32, 64, 64, 1000.0, 500.0, 0.8 * 256 / 32),
+    (31, 33, 9, 60, 20, 1000.0, 500.0, 6.0),
 ]
 
 
@@ -75,7 +80,7 @@ def test_device_math_matches_oracle(dm, oracle_mod, case):
                 assert np.array_equal(y, yo) and np.array_equal(sr, so), a
             else:
                 assert rel_l2(y, yo) < 1e-6 and rel_l2(sr, so) < 1e-6, (a, exact)
-        for staged in (0, 1):
+        for staged in (0, 1, 2):
             b = np.zeros(nx * ny * nz, np.float32)
             sc = np.zeros(nx * ny * nz, np.float32)
             dm.dm_atx(_p(b), _p(yv), _p(sc), g["cos_phi"], g["sin_phi"], _p(yd), _p(zd),
