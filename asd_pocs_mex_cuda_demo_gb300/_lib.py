@@ -47,6 +47,16 @@ class Geometry(C.Structure):
                 ("vxlsize", C.c_double), ("detsize", C.c_double)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("slots_per_lane", C.c_int), ("hbm_budget_bytes", C.c_ulonglong),
+                ("inflight", C.c_int)]
+
+
+class JobTimes(C.Structure):
+    _fields_ = [("queued_ms", C.c_double), ("run_ms", C.c_double),
+                ("total_ms", C.c_double)]
+
+
 # (name, restype, argtypes) of every exported function
 SIGNATURES = [
     ("asdpocs_last_error", C.c_char_p, []),
@@ -95,6 +105,17 @@ SIGNATURES = [
     ("asdpocs_plan_sinogram_ptr", C.c_void_p, [C.c_void_p, C.c_int]),
     ("asdpocs_plan_image_ptr", C.c_void_p, [C.c_void_p, C.c_int]),
     ("asdpocs_plan_time_phase", C.c_int, [C.c_void_p, C.c_int, C.c_int, _D]),
+    ("asdpocs_server_config_default", None, [C.POINTER(ServerConfig)]),
+    ("asdpocs_server_create", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(ServerConfig)]),
+    ("asdpocs_server_submit", C.c_int, [C.c_void_p, C.POINTER(Geometry), _D,
+                                        C.POINTER(Options), _F, _F, _F,
+                                        C.POINTER(C.c_longlong)]),
+    ("asdpocs_server_poll", C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_int)]),
+    ("asdpocs_server_wait", C.c_int, [C.c_void_p, C.c_longlong, _F, C.POINTER(Stats), _D,
+                                      C.POINTER(JobTimes)]),
+    ("asdpocs_server_memory", C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong),
+                                        C.POINTER(C.c_ulonglong)]),
+    ("asdpocs_server_destroy", C.c_int, [C.c_void_p]),
     ("ASD_POCS_cuda", C.c_int, [_D, _D, C.POINTER(Geometry), C.POINTER(Options), _D, _D,
                                 _D, _D, C.POINTER(Stats)]),
     ("SART_cuda_inline", C.c_int, [_D, _D, C.POINTER(Geometry), C.c_double, _D, _D, _D]),

@@ -126,8 +126,11 @@ def SART_cuda_inline(P, para: dict):
 
 
 class Plan:
-    """A batch of device-resident ASD-POCS reconstructions sharing
-    nx, ny, nz, na, nb, nv (per-instance geometry values, angles and options).
+    """A batch of device-resident ASD-POCS reconstructions (per-instance
+    sizes, geometry values, angles and options).  Instances of one plan are
+    all 2-D (nz == nb == 1) or all cone-beam; the kernels run every instance
+    in one launch per step, each at its own sizes, and an instance gives the
+    same result bit for bit alone or in any batch.
 
     Data go in as float32 (host numpy arrays or device pointers as ints) and
     the whole iteration runs on the plan's CUDA stream, optionally replayed
@@ -139,19 +142,31 @@ class Plan:
         self.batch = len(paras)
         phis = [np.asarray(p, np.float64).ravel() for p in
                 (phi_vecs if isinstance(phi_vecs, (list, tuple)) else [phi_vecs] * self.batch)]
-        nv = phis[0].size
-        geoms = (Geometry * self.batch)(*[geometry_from_para(p, nv) for p in paras])
+        if len(phis) != self.batch:
+            raise AsdpocsError(1, "one phi_vec per instance")
+        geoms = (Geometry * self.batch)(*[geometry_from_para(p, ph.size)
+                                          for p, ph in zip(paras, phis)])
         opts = (Options * self.batch)(*[options_from_para(p) for p in paras])
         phi = np.ascontiguousarray(np.concatenate(phis))
-        self._g = geoms[0]
+        self._geoms = geoms
         self._opts = opts
         h = C.c_void_p()
         check(load().asdpocs_plan_create(C.byref(h), self.batch, geoms,
                                          phi.ctypes.data_as(_D), opts,
                                          int(hbm_budget_bytes), C.c_void_p(stream or None)))
         self._h = h
-        self.nx, self.ny, self.nz = self._g.nx, self._g.ny, self._g.nz
-        self.na, self.nb, self.nv = self._g.na, self._g.nb, self._g.nv
+        g0 = geoms[0]
+        # sizes of instance 0 (every instance of a uniform plan)
+        self.nx, self.ny, self.nz = g0.nx, g0.ny, g0.nz
+        self.na, self.nb, self.nv = g0.na, g0.nb, g0.nv
+
+    def voxels(self, inst: int) -> int:
+        g = self._geoms[inst]
+        return g.nx * g.ny * g.nz
+
+    def sinogram_size(self, inst: int) -> int:
+        g = self._geoms[inst]
+        return g.na * g.nb * g.nv
 
     @property
     def nbytes(self) -> int:
@@ -191,13 +206,13 @@ class Plan:
             check(getattr(L, fn)(self._h, inst, C.c_void_p(a.ctypes.data), 0))
 
     def set_sinogram(self, inst: int, P):
-        self._put("asdpocs_plan_set_sinogram", inst, P, self.na * self.nb * self.nv)
+        self._put("asdpocs_plan_set_sinogram", inst, P, self.sinogram_size(inst))
 
     def set_initial(self, inst: int, m0):
-        self._put("asdpocs_plan_set_initial", inst, m0, self.nx * self.ny * self.nz)
+        self._put("asdpocs_plan_set_initial", inst, m0, self.voxels(inst))
 
     def set_reference(self, inst: int, I0):
-        self._put("asdpocs_plan_set_reference", inst, I0, self.nx * self.ny * self.nz)
+        self._put("asdpocs_plan_set_reference", inst, I0, self.voxels(inst))
 
     def reset(self):
         check(load().asdpocs_plan_reset(self._h))
@@ -211,7 +226,7 @@ class Plan:
         check(load().asdpocs_plan_sync(self._h))
 
     def image(self, inst: int) -> np.ndarray:
-        out = np.empty(self.nx * self.ny * self.nz, np.float32)
+        out = np.empty(self.voxels(inst), np.float32)
         check(load().asdpocs_plan_get_image(self._h, inst, C.c_void_p(out.ctypes.data), 0))
         return out
 

@@ -32,6 +32,7 @@ UNITS = {
     "kernels_tv.cu": [],
     "host_api.cu": [],
     "noalloc.cu": [],
+    "server.cu": [],
 }
 
 

@@ -70,6 +70,9 @@ struct Scalars {
 };
 
 struct Inst {
+  Dims d;                    // this instance's volume and detector sizes
+  int nv;                    // and number of views (a plan's grids are sized
+                             // for its largest instance)
   ViewGeo g;                 // geometry (cos/sin filled per view from trig)
   const float2 *trig;        // [nv] (cos_phi, sin_phi) per view
   const float *P;            // sinogram, view-major, na*nb*nv
@@ -161,6 +164,24 @@ __device__ __forceinline__ int inst_block() {
   return blockIdx.x + gridDim.x * blockIdx.y;
 }
 __device__ __forceinline__ int inst_blocks() { return gridDim.x * gridDim.y; }
+
+// Batched kernels run every instance of a plan in one grid sized for its
+// largest instance.  A block keeps the (x, y) position it would have in a
+// grid sized for its own instance alone -- so its tiles, its index among the
+// instance's reduction partials and their number are the same as when the
+// instance runs alone, and so are the results, bit for bit -- and blocks
+// outside that grid have nothing to do.
+struct OwnBlock {
+  int bid, nblocks;  // bid < 0: outside the instance's own grid
+};
+__device__ __forceinline__ OwnBlock own_block(dim3 own) {
+  OwnBlock b;
+  b.nblocks = (int)(own.x * own.y);
+  b.bid = (blockIdx.x < own.x && blockIdx.y < own.y)
+              ? (int)(blockIdx.x + own.x * blockIdx.y)
+              : -1;
+  return b;
+}
 constexpr int kMaxReduceK = 4;          // values reduced together (partials sizing)
 
 }  // namespace asd

@@ -6,11 +6,12 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <new>
 #include <vector>
 
-#include "kernels.h"
+#include "instance.h"
 
 namespace asd {
 
@@ -382,14 +383,14 @@ struct asdpocs_plan_s {
   cudaStream_t st = nullptr;
   bool own_stream = false;
   int batch = 0;
-  Dims d{};
-  int nv = 0, max_iter = 0, max_ng = 0;
+  Dims d{};    // largest sizes over the instances (grids of the launches)
+  int nv = 0;  // largest number of views
+  int max_iter = 0, max_ng = 0;
   std::vector<asdpocs_geometry> geom;
   std::vector<asdpocs_options> opt;
   std::vector<Inst> h_inst;
   std::vector<int> has_ref;
-  std::vector<int> view_axis;  // per view: 1 / 2 / 0 (see launch_sart_atx)
-  bool shared = false;         // all instances share geometry and angles
+  bool shared = false;  // all instances share sizes, geometry and angles
   Inst *d_inst = nullptr;
   void *arena = nullptr;
   size_t bytes = 0;
@@ -399,19 +400,148 @@ struct asdpocs_plan_s {
 
 namespace asd {
 
-static int plan_enqueue_iteration(asdpocs_plan p) {
-  for (int v = 0; v < p->nv; v++) {
-    ASD_CUDA(launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st));
-    if (p->shared)
-      ASD_CUDA(launch_sart_atx_shared(p->d_inst, p->batch, p->d, v,
-                                      p->view_axis[v], p->st));
-    else
-      ASD_CUDA(launch_sart_atx(p->d_inst, p->batch, p->d, v, p->view_axis[v], p->st));
+int instance_kind(const asdpocs_geometry &g) {
+  return g.nz > 1 ? 2 : (g.nb > 1 ? 1 : 0);
+}
+
+int check_instance(const asdpocs_geometry &g, const asdpocs_options &o) {
+  if (int e = check_dims(g.nx, g.ny, g.nz, g.na, g.nb)) return e;
+  if (g.nv <= 0) return set_error(ASDPOCS_ERR_ARG, "nv must be positive");
+  if (o.maxnumIter < 0 || o.numOfgradients < 0)
+    return set_error(ASDPOCS_ERR_ARG, "negative iteration counts");
+  return 0;
+}
+
+InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
+                           size_t cor_floats) {
+  const Dims d{g.nx, g.ny, g.nz, g.na, g.nb};
+  const size_t N = (size_t)g.nx * g.ny * g.nz;
+  const size_t M = (size_t)g.na * g.nb;
+  const size_t per_img = align256(N * 4);
+  const size_t nblk = (size_t)reduce_blocks_for(d);
+  const bool proj3d = g.nz > 1 || g.nb > 1;
+  InstLayout o;
+  size_t off = 0;
+  o.P = off; off += align256(M * g.nv * 4);
+  o.m = off; off += per_img;
+  o.m_pre = off; off += per_img;
+  o.m_res = off; off += per_img;
+  o.m_k1 = off; off += per_img;
+  o.I0 = off; off += per_img;
+  o.tvb = off; off += per_img;
+  o.tvc = off; off += per_img;
+  o.cor = off; off += align256(cor_floats * 4);
+  o.tabA = off; off += align256((size_t)g.na * g.nv * 16);
+  o.vflags = off; off += align256((size_t)g.nv * 4);
+  o.tabC = off; off += align256(proj3d ? M * 16 : 16);
+  o.ydet = off; off += align256((size_t)g.na * 4);
+  o.zdet = off; off += align256((size_t)g.nb * 4);
+  o.trig = off; off += align256((size_t)g.nv * 8);
+  o.rmse = off; off += align256((size_t)(max_iter + 1) * 8);
+  o.part = off; off += align256(nblk * kMaxReduceK * 8);
+  o.cnt = off; off += 256;
+  o.scal = off; off += align256(sizeof(Scalars));
+  o.bytes = off;
+  return o;
+}
+
+cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,
+                          const asdpocs_geometry &g, const double *phi_deg,
+                          cudaStream_t st) {
+  I.d = Dims{g.nx, g.ny, g.nz, g.na, g.nb};
+  I.nv = g.nv;
+  GatewayGeo gg;
+  gateway_geometry(0.0, g.SO, g.OD, g.vxlsize, g.detsize, g.na, g.nb, gg);
+  I.g = with_constants(ViewGeo{0.f, 0.f, gg.SO, gg.OD, gg.scale, gg.det, gg.det,
+                               1.0f, (const float *)(b + o.ydet),
+                               (const float *)(b + o.zdet)});
+  std::vector<float2> trig(g.nv);
+  for (int v = 0; v < g.nv; v++) trig[v] = view_trig(phi_deg[v]);
+  I.trig = (const float2 *)(b + o.trig);
+  I.P = (const float *)(b + o.P);
+  I.m = (float *)(b + o.m);
+  I.m_pre = (float *)(b + o.m_pre);
+  I.m_res = (float *)(b + o.m_res);
+  I.m_k1 = (float *)(b + o.m_k1);
+  I.I0 = (float *)(b + o.I0);
+  I.tv_b = (float *)(b + o.tvb);
+  I.tv_c = (float *)(b + o.tvc);
+  I.cor = (float *)(b + o.cor);
+  I.cor_stride = 1;
+  I.tabA = (float4 *)(b + o.tabA);
+  I.vflags = (int *)(b + o.vflags);
+  I.tabC = (float4 *)(b + o.tabC);
+  I.rmse = (double *)(b + o.rmse);
+  I.partials = (double *)(b + o.part);
+  I.counter = (unsigned *)(b + o.cnt);
+  I.s = (Scalars *)(b + o.scal);
+  // pageable sources: staged before each call returns
+  cudaError_t e = cudaMemcpyAsync(b + o.ydet, gg.y_det.data(), (size_t)g.na * 4,
+                                  cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b + o.zdet, gg.z_det.data(), (size_t)g.nb * 4,
+                        cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b + o.trig, trig.data(), (size_t)g.nv * 8,
+                        cudaMemcpyHostToDevice, st);
+  return e;
+}
+
+Scalars initial_scalars(const asdpocs_options &o, bool has_ref) {
+  Scalars s;
+  memset(&s, 0, sizeof s);
+  s.alpha = o.alpha;
+  s.beta = o.beta;
+  s.beta_f = (float)o.beta;
+  s.alpha_red = o.alpha_red;
+  s.beta_red = o.beta_red;
+  s.r_max = o.r_max;
+  s.epsilon = o.epsilon;
+  s.stopRelChg = o.stopRelChg;
+  s.k = 1;
+  s.maxIter = o.maxnumIter;
+  s.ng = o.numOfgradients;
+  s.done = o.maxnumIter <= 0;
+  s.has_ref = has_ref;
+  return s;
+}
+
+cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st) {
+  const size_t bytes = (size_t)I.d.nx * I.d.ny * I.d.nz * 4;
+  cudaError_t e = cudaMemcpyAsync(I.m, I.m_k1, bytes, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(I.m_pre, I.m_k1, bytes, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(I.m_res, I.m_k1, bytes, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(I.counter, 0, 256, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(I.s, &s, sizeof s, cudaMemcpyHostToDevice, st);
+  return e;
+}
+
+}  // namespace asd
+
+namespace asd {
+
+cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
+                              int nv, int ng, bool shared, cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  for (int v = 0; v < nv && e == cudaSuccess; v++) {
+    e = launch_sart_ax(d_inst, batch, d, v, st);
+    if (e == cudaSuccess)
+      e = shared ? launch_sart_atx_shared(d_inst, batch, d, v, st)
+                 : launch_sart_atx(d_inst, batch, d, v, st);
   }
-  ASD_CUDA(launch_after_sweep(p->d_inst, p->batch, p->d, p->st));
-  for (int s = 0; s < p->max_ng; s++)
-    ASD_CUDA(launch_tv_step(p->d_inst, p->batch, p->d, s, p->max_ng, p->st));
-  ASD_CUDA(launch_finish_iter(p->d_inst, p->batch, p->d, p->max_ng, p->st));
+  if (e == cudaSuccess) e = launch_after_sweep(d_inst, batch, d, st);
+  for (int s = 0; s < ng && e == cudaSuccess; s++)
+    e = launch_tv_step(d_inst, batch, d, s, ng, st);
+  if (e == cudaSuccess) e = launch_finish_iter(d_inst, batch, d, ng, st);
+  return e;
+}
+
+static int plan_enqueue_iteration(asdpocs_plan p) {
+  ASD_CUDA(enqueue_iteration(p->d_inst, p->batch, p->d, p->nv, p->max_ng, p->shared,
+                             p->st));
   return 0;
 }
 
@@ -428,44 +558,52 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     return set_error(ASDPOCS_ERR_ARG, "bad plan arguments");
   *out = nullptr;
   const asdpocs_geometry &g0 = geom[0];
-  if (int e = check_dims(g0.nx, g0.ny, g0.nz, g0.na, g0.nb)) return e;
-  if (g0.nv <= 0) return set_error(ASDPOCS_ERR_ARG, "nv must be positive");
-  for (int i = 1; i < batch; i++) {
+  Dims dmax{0, 0, 0, 0, 0};
+  int nv_max = 0;
+  std::vector<size_t> phi_off(batch);
+  size_t phi_n = 0;
+  asdpocs_options dflt;
+  asdpocs_options_default(&dflt);
+  for (int i = 0; i < batch; i++) {
     const asdpocs_geometry &gi = geom[i];
-    if (gi.nx != g0.nx || gi.ny != g0.ny || gi.nz != g0.nz || gi.na != g0.na ||
-        gi.nb != g0.nb || gi.nv != g0.nv)
+    if (int e = check_instance(gi, opt ? opt[i] : dflt)) return e;
+    if (instance_kind(gi) != instance_kind(g0))
       return set_error(ASDPOCS_ERR_ARG,
-                       "instances of one plan must share nx,ny,nz,na,nb,nv");
+                       "instances of one plan must be all 2-D (nz == nb == 1), "
+                       "all single-slice, or all 3-D");
+    dmax.nx = std::max(dmax.nx, gi.nx);
+    dmax.ny = std::max(dmax.ny, gi.ny);
+    dmax.nz = std::max(dmax.nz, gi.nz);
+    dmax.na = std::max(dmax.na, gi.na);
+    dmax.nb = std::max(dmax.nb, gi.nb);
+    nv_max = std::max(nv_max, gi.nv);
+    phi_off[i] = phi_n;
+    phi_n += (size_t)gi.nv;
   }
   asdpocs_plan p = new (std::nothrow) asdpocs_plan_s;
   if (!p) return set_error(ASDPOCS_ERR_NOMEM, "host allocation");
   p->batch = batch;
-  p->d = Dims{g0.nx, g0.ny, g0.nz, g0.na, g0.nb};
-  p->nv = g0.nv;
+  p->d = dmax;
+  p->nv = nv_max;
   p->geom.assign(geom, geom + batch);
   p->opt.resize(batch);
   for (int i = 0; i < batch; i++) {
-    if (opt)
-      p->opt[i] = opt[i];
-    else
-      asdpocs_options_default(&p->opt[i]);
-    if (p->opt[i].maxnumIter < 0 || p->opt[i].numOfgradients < 0) {
-      delete p;
-      return set_error(ASDPOCS_ERR_ARG, "negative iteration counts");
-    }
+    p->opt[i] = opt ? opt[i] : dflt;
     if (p->opt[i].maxnumIter > p->max_iter) p->max_iter = p->opt[i].maxnumIter;
     if (p->opt[i].numOfgradients > p->max_ng)
       p->max_ng = p->opt[i].numOfgradients;
   }
   p->has_ref.assign(batch, 0);
-  // instances with identical geometry and view angles share the projector
-  // coefficients of every view
+  // instances with identical sizes, geometry and view angles share the
+  // projector coefficients of every view
   p->shared = batch > 1;
   for (int i = 1; i < batch && p->shared; i++) {
     const asdpocs_geometry &gi = geom[i];
-    p->shared = gi.SO == g0.SO && gi.OD == g0.OD && gi.vxlsize == g0.vxlsize &&
+    p->shared = gi.nx == g0.nx && gi.ny == g0.ny && gi.nz == g0.nz &&
+                gi.na == g0.na && gi.nb == g0.nb && gi.nv == g0.nv &&
+                gi.SO == g0.SO && gi.OD == g0.OD && gi.vxlsize == g0.vxlsize &&
                 gi.detsize == g0.detsize &&
-                memcmp(phi_vec_deg, phi_vec_deg + (size_t)i * g0.nv,
+                memcmp(phi_vec_deg, phi_vec_deg + phi_off[i],
                        sizeof(double) * (size_t)g0.nv) == 0;
   }
   if (getenv("ASDPOCS_NO_SHARED_GEOMETRY")) p->shared = false;
@@ -480,42 +618,18 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     }
     p->own_stream = true;
   }
-  // ---- arena layout (per instance) ----
-  const size_t N = (size_t)g0.nx * g0.ny * g0.nz;
-  const size_t M = (size_t)g0.na * g0.nb;
-  const size_t nblk = (size_t)reduce_blocks_for(p->d);
-  const size_t per_img = align256(N * 4);
+  // ---- arena: each instance's block at its own sizes ----
+  std::vector<InstLayout> lay(batch);
+  std::vector<size_t> base(batch);
   size_t off = 0;
-  struct Off {
-    size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, ydet, zdet, trig, rmse,
-        part, cnt, scal, tabA, tabC, vflags;
-  };
-  std::vector<Off> offs(batch);
   for (int i = 0; i < batch; i++) {
-    Off &o = offs[i];
-    o.P = off; off += align256(M * p->nv * 4);
-    o.m = off; off += per_img;
-    o.m_pre = off; off += per_img;
-    o.m_res = off; off += per_img;
-    o.m_k1 = off; off += per_img;
-    o.I0 = off; off += per_img;
-    o.tvb = off; off += per_img;
-    o.tvc = off; off += per_img;
+    const size_t M = (size_t)geom[i].na * geom[i].nb;
     // shared-geometry groups interleave their residuals in the buffer of
     // the group's first instance (kShareSlots values per ray)
-    o.cor = off;
-    off += align256((p->shared && i % kShareSlots == 0) ? M * 4 * kShareSlots
-                                                        : M * 4);
-    o.tabA = off; off += align256((size_t)g0.na * p->nv * 16);
-    o.vflags = off; off += align256((size_t)p->nv * 4);
-    o.tabC = off; off += align256((g0.nz > 1 || g0.nb > 1) ? M * 16 : 16);
-    o.ydet = off; off += align256((size_t)g0.na * 4);
-    o.zdet = off; off += align256((size_t)g0.nb * 4);
-    o.trig = off; off += align256((size_t)p->nv * 8);
-    o.rmse = off; off += align256((size_t)(p->max_iter + 1) * 8);
-    o.part = off; off += align256(nblk * kMaxReduceK * 8);
-    o.cnt = off; off += 256;
-    o.scal = off; off += align256(sizeof(Scalars));
+    lay[i] = layout_instance(geom[i], p->opt[i].maxnumIter,
+                             (p->shared && i % kShareSlots == 0) ? M * kShareSlots : M);
+    base[i] = off;
+    off += lay[i].bytes;
   }
   const size_t inst_off = off;
   off += align256(sizeof(Inst) * batch);
@@ -536,73 +650,20 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   char *b = (char *)p->arena;
   e = cudaMemsetAsync(b, 0, off, p->st);
   p->h_inst.resize(batch);
-  std::vector<float2> trig(p->nv);
   for (int i = 0; i < batch && e == cudaSuccess; i++) {
-    const Off &o = offs[i];
     Inst &I = p->h_inst[i];
-    GatewayGeo gg;
-    gateway_geometry(0.0, geom[i].SO, geom[i].OD, geom[i].vxlsize,
-                     geom[i].detsize, g0.na, g0.nb, gg);
-    I.g = with_constants(ViewGeo{0.f, 0.f, gg.SO, gg.OD, gg.scale, gg.det, gg.det,
-                                 1.0f, (const float *)(b + o.ydet),
-                                 (const float *)(b + o.zdet)});
-    for (int v = 0; v < p->nv; v++)
-      trig[v] = view_trig(phi_vec_deg[(size_t)i * p->nv + v]);
-    I.trig = (const float2 *)(b + o.trig);
-    I.P = (const float *)(b + o.P);
-    I.m = (float *)(b + o.m);
-    I.m_pre = (float *)(b + o.m_pre);
-    I.m_res = (float *)(b + o.m_res);
-    I.m_k1 = (float *)(b + o.m_k1);
-    I.I0 = (float *)(b + o.I0);
-    I.tv_b = (float *)(b + o.tvb);
-    I.tv_c = (float *)(b + o.tvc);
+    e = bind_instance(I, b + base[i], lay[i], geom[i], phi_vec_deg + phi_off[i], p->st);
     if (p->shared) {
-      I.cor = (float *)(b + offs[i - i % kShareSlots].cor) + i % kShareSlots;
+      const int g = i - i % kShareSlots;
+      I.cor = (float *)(b + base[g] + lay[g].cor) + i % kShareSlots;
       I.cor_stride = kShareSlots;
-    } else {
-      I.cor = (float *)(b + o.cor);
-      I.cor_stride = 1;
     }
-    I.tabA = (float4 *)(b + o.tabA);
-    I.vflags = (int *)(b + o.vflags);
-    I.tabC = (float4 *)(b + o.tabC);
-    I.rmse = (double *)(b + o.rmse);
-    I.partials = (double *)(b + o.part);
-    I.counter = (unsigned *)(b + o.cnt);
-    I.s = (Scalars *)(b + o.scal);
-    e = cudaMemcpyAsync(b + o.ydet, gg.y_det.data(), (size_t)g0.na * 4,
-                        cudaMemcpyHostToDevice, p->st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(b + o.zdet, gg.z_det.data(), (size_t)g0.nb * 4,
-                          cudaMemcpyHostToDevice, p->st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(b + o.trig, trig.data(), (size_t)p->nv * 8,
-                          cudaMemcpyHostToDevice, p->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);  // trig reused
   }
   p->d_inst = (Inst *)(b + inst_off);
   if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(),
                                             sizeof(Inst) * batch,
                                             cudaMemcpyHostToDevice, p->st);
   if (e == cudaSuccess) e = launch_view_tables(p->d_inst, batch, p->d, p->nv, p->st);
-  // per-view chord specialisation, valid when every instance agrees
-  std::vector<int> vf((size_t)p->nv);
-  p->view_axis.assign(p->nv, 0);
-  std::vector<int> acc((size_t)p->nv, 0);
-  for (int i = 0; i < batch && e == cudaSuccess; i++) {
-    e = cudaMemcpyAsync(vf.data(), p->h_inst[i].vflags, (size_t)p->nv * 4,
-                        cudaMemcpyDeviceToHost, p->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
-    for (int v = 0; v < p->nv; v++) acc[v] |= vf[v];
-  }
-  for (int v = 0; v < p->nv; v++) {
-    if (acc[v] & kViewAxisParallel) continue;
-    if (!(acc[v] & kViewNotX))
-      p->view_axis[v] = 1;
-    else if (!(acc[v] & kViewNotY))
-      p->view_axis[v] = 2;
-  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
   if (e != cudaSuccess) {
     asdpocs_plan_destroy(p);
@@ -625,6 +686,12 @@ int asdpocs_plan_destroy(asdpocs_plan p) {
 
 unsigned long long asdpocs_plan_bytes(asdpocs_plan p) {
   return p ? (unsigned long long)p->bytes : 0ULL;
+}
+
+// bytes of one image of instance `inst`
+static size_t inst_bytes(asdpocs_plan p, int inst) {
+  const Dims &d = p->h_inst[inst].d;
+  return (size_t)d.nx * d.ny * d.nz * 4;
 }
 
 static int plan_check(asdpocs_plan p, int inst) {
@@ -653,56 +720,32 @@ int asdpocs_plan_set_sinogram(asdpocs_plan p, int inst, const float *P,
   clear_error();
   if (int e = plan_check(p, inst)) return e;
   if (!P) return set_error(ASDPOCS_ERR_ARG, "null sinogram");
-  const size_t bytes = (size_t)p->d.na * p->d.nb * p->nv * 4;
-  return plan_put(p, (void *)p->h_inst[inst].P, P, bytes, where);
+  const Inst &I = p->h_inst[inst];
+  const size_t bytes = (size_t)I.d.na * I.d.nb * I.nv * 4;
+  return plan_put(p, (void *)I.P, P, bytes, where);
 }
 
 int asdpocs_plan_set_initial(asdpocs_plan p, int inst, const float *m0,
                              int where) {
   clear_error();
   if (int e = plan_check(p, inst)) return e;
-  const size_t bytes = (size_t)p->d.nx * p->d.ny * p->d.nz * 4;
-  return plan_put(p, p->h_inst[inst].m_k1, m0, bytes, where);
+  return plan_put(p, p->h_inst[inst].m_k1, m0, inst_bytes(p, inst), where);
 }
 
 int asdpocs_plan_set_reference(asdpocs_plan p, int inst, const float *I0,
                                int where) {
   clear_error();
   if (int e = plan_check(p, inst)) return e;
-  const size_t bytes = (size_t)p->d.nx * p->d.ny * p->d.nz * 4;
   p->has_ref[inst] = I0 != nullptr;
-  return plan_put(p, p->h_inst[inst].I0, I0, bytes, where);
+  return plan_put(p, p->h_inst[inst].I0, I0, inst_bytes(p, inst), where);
 }
 
 int asdpocs_plan_reset(asdpocs_plan p) {
   clear_error();
   if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
-  const size_t bytes = (size_t)p->d.nx * p->d.ny * p->d.nz * 4;
-  std::vector<Scalars> hs(p->batch);
-  for (int i = 0; i < p->batch; i++) {
-    const asdpocs_options &o = p->opt[i];
-    Scalars &s = hs[i];
-    memset(&s, 0, sizeof s);
-    s.alpha = o.alpha;
-    s.beta = o.beta;
-    s.beta_f = (float)o.beta;
-    s.alpha_red = o.alpha_red;
-    s.beta_red = o.beta_red;
-    s.r_max = o.r_max;
-    s.epsilon = o.epsilon;
-    s.stopRelChg = o.stopRelChg;
-    s.k = 1;
-    s.maxIter = o.maxnumIter;
-    s.ng = o.numOfgradients;
-    s.done = o.maxnumIter <= 0;
-    s.has_ref = p->has_ref[i];
-    const Inst &I = p->h_inst[i];
-    ASD_CUDA(cudaMemcpyAsync(I.m, I.m_k1, bytes, cudaMemcpyDeviceToDevice, p->st));
-    ASD_CUDA(cudaMemcpyAsync(I.m_pre, I.m_k1, bytes, cudaMemcpyDeviceToDevice, p->st));
-    ASD_CUDA(cudaMemcpyAsync(I.m_res, I.m_k1, bytes, cudaMemcpyDeviceToDevice, p->st));
-    ASD_CUDA(cudaMemsetAsync(I.counter, 0, 256, p->st));
-    ASD_CUDA(cudaMemcpyAsync(I.s, &s, sizeof s, cudaMemcpyHostToDevice, p->st));
-  }
+  for (int i = 0; i < p->batch; i++)
+    ASD_CUDA(reset_instance(p->h_inst[i], initial_scalars(p->opt[i], p->has_ref[i]),
+                            p->st));
   ASD_CUDA(cudaStreamSynchronize(p->st));
   return 0;
 }
@@ -745,8 +788,7 @@ int asdpocs_plan_get_image(asdpocs_plan p, int inst, float *m, int where) {
   clear_error();
   if (int e = plan_check(p, inst)) return e;
   if (!m) return set_error(ASDPOCS_ERR_ARG, "null output");
-  const size_t bytes = (size_t)p->d.nx * p->d.ny * p->d.nz * 4;
-  ASD_CUDA(cudaMemcpyAsync(m, p->h_inst[inst].m_res, bytes,
+  ASD_CUDA(cudaMemcpyAsync(m, p->h_inst[inst].m_res, inst_bytes(p, inst),
                            where ? cudaMemcpyDeviceToDevice
                                  : cudaMemcpyDeviceToHost,
                            p->st));
@@ -801,9 +843,8 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
       case 0: return launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
       case 1:
         return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, i % p->nv,
-                                                  p->view_axis[i % p->nv], p->st)
-                         : launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv,
-                                           p->view_axis[i % p->nv], p->st);
+                                                  p->st)
+                         : launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv, p->st);
       case 2: return launch_tv_step(p->d_inst, p->batch, p->d, 1 + i % (ng > 1 ? ng - 1 : 1),
                                     ng, p->st);
       default: return launch_after_sweep(p->d_inst, p->batch, p->d, p->st);

@@ -1,0 +1,52 @@
+// Device state of one reconstruction instance (internal): shared by the
+// batched plans and the serving queue.
+#pragma once
+#include "kernels.h"
+
+namespace asd {
+
+// Byte offsets of an instance's buffers inside its block of device memory
+// (each 256-byte aligned), at the instance's own sizes; `bytes` is the
+// block's size.
+struct InstLayout {
+  size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, ydet, zdet, trig, rmse,
+      part, cnt, scal, tabA, tabC, vflags, bytes;
+};
+
+// Kind of an instance: 0 = 2-D fan beam (nz == nb == 1), 1 = one slice with
+// detector rows (nz == 1, nb > 1), 2 = cone beam (nz > 1).  Instances that
+// run in one launch share a kind (their kernels are templated on it).
+int instance_kind(const asdpocs_geometry &g);
+
+// Sizes and counts of `g` checked (status and message set on failure).
+int check_instance(const asdpocs_geometry &g, const asdpocs_options &o);
+
+// Layout of an instance; cor_floats is the length of its residual buffer
+// (na*nb, or kShareSlots*na*nb for the first instance of a shared group).
+InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
+                           size_t cor_floats);
+
+// Points I at the block `b` laid out as `o` (own residual buffer, stride 1)
+// and uploads the instance's detector coordinates and view cosines/sines on
+// `st` (the host staging is released when the call returns).
+cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,
+                          const asdpocs_geometry &g, const double *phi_deg,
+                          cudaStream_t st);
+
+// Scalars of an instance before its first iteration (ASD_POCS_cuda.m:34-96
+// defaults already applied to `o`).
+Scalars initial_scalars(const asdpocs_options &o, bool has_ref);
+
+// Enqueues the start state of an instance on `st`: m, m_pre, m_res = m_k1,
+// a zero reduction ticket and the scalars (copied from `s`, which must stay
+// valid until the copy has run unless it is pageable host memory).
+cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st);
+
+// Enqueues one ASD-POCS iteration of `batch` instances on `st` (grids for
+// the largest sizes `d`, nv views, ng TV steps): per view the SART forward
+// and backward steps (shared-geometry backward step if `shared`), the
+// end-of-sweep scalars, the TV steps and the end of the iteration.
+cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
+                              int nv, int ng, bool shared, cudaStream_t st);
+
+}  // namespace asd

@@ -13,16 +13,19 @@ cudaError_t launch_ax(const float *x, float *y, float *sr, const ViewGeo &g,
 cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
                        const Dims &d, cudaStream_t st);
 
+// Batched launches take the plan's largest sizes `d` (each field the
+// maximum over its instances) for the grid; every instance reads its own
+// sizes from Inst::d, and instances of one plan are all planar (nz == nb ==
+// 1) or all not.
+//
 // Fused SART steps of view `view` for `batch` instances (ASD_POCS_cuda.m:
-// 116-131).  sart_ax: Ax of m, residual against P, dd2 accumulation, row
-// normalisation -> cor.  sart_atx: Atx of cor, column normalisation, update
-// m += beta*bp/sumC, positivity.
+// 116-131); instances with fewer views skip.  sart_ax: Ax of m, residual
+// against P, dd2 accumulation, row normalisation -> cor.  sart_atx: Atx of
+// cor, column normalisation, update m += beta*bp/sumC, positivity.
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
                            int view, cudaStream_t st);
-// axis: 1 (2) when every instance's rays of this view are x- (y-) dominant
-// and none is axis-parallel (view flags), else 0.
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, int axis, cudaStream_t st);
+                            int view, cudaStream_t st);
 
 // ---- TV and scalars (kernels_tv.cu) ----
 // FP64 / FP32 TV minimisation on device buffers (reference semantics).
@@ -46,11 +49,14 @@ cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
 
 int reduce_blocks_for(const Dims &d);
 
+// Copies Inst::s->done of n instances into the device array out[n].
+cudaError_t launch_gather_done(const Inst *insts, int n, int *out,
+                               cudaStream_t st);
+
 // Backward step for a batch whose instances share geometry and view angles:
 // chords computed once per voxel and applied to groups of instances.
 cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
-                                   const Dims &d, int view, int axis,
-                                   cudaStream_t st);
+                                   const Dims &d, int view, cudaStream_t st);
 
 // Ray slope tables and flags of every view (Inst::tabA, Inst::vflags, which
 // must be zeroed first), computed once per plan.

@@ -263,11 +263,13 @@ __device__ __forceinline__ ViewGeo view_of(const Inst &I, int view) {
 }
 
 // Ray slope tables of every view (Inst::tabA) and the view flags, once per
-// plan: grid (ceil(na/128), nv, instances).
+// plan: grid (ceil(na/128), nv, instances) for the largest na and nv.
 __global__ void __launch_bounds__(128)
-    k_view_tables(const Inst *__restrict__ insts, Dims D) {
+    k_view_tables(const Inst *__restrict__ insts) {
   const Inst &I = insts[blockIdx.z];
+  const Dims D = I.d;
   const int view = blockIdx.y;
+  if (view >= I.nv) return;
   const int ia = blockIdx.x * 128 + threadIdx.x;
   const ViewGeo G = view_of(I, view);
   int f = 0;
@@ -289,12 +291,15 @@ __global__ void __launch_bounds__(128)
 // backward step that follows.
 template <bool k3D>
 __global__ void __launch_bounds__(kAxThreads)
-    k_sart_ax(const Inst *__restrict__ insts, Dims D, int view) {
+    k_sart_ax(const Inst *__restrict__ insts, int view) {
   const Inst &I = insts[blockIdx.z];
-  if (((volatile int *)&I.s->done)[0]) return;
+  if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
+  const Dims D = I.d;
+  const long long nr = (long long)D.na * D.nb;
+  const OwnBlock ob = own_block(dim3((unsigned)((nr + kAxWarps - 1) / kAxWarps), 1));
+  if (ob.bid < 0) return;
   const ViewGeo G = view_of(I, view);
   const int lane = threadIdx.x & 31;
-  const long long nr = (long long)D.na * D.nb;
   const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
   float part[2] = {0.f, 0.f};  // dd2, non-finite residuals
   if (r < nr) {
@@ -315,8 +320,7 @@ __global__ void __launch_bounds__(kAxThreads)
     }
   }
   double tot[2];
-  if (grid_sum<kAxThreads, 2>(part, I.partials, I.counter, inst_block(),
-                              inst_blocks(), tot)) {
+  if (grid_sum<kAxThreads, 2>(part, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
     if (threadIdx.x == 0) {
       I.s->dd2_acc += tot[0];
       I.s->cor_finite = tot[1] == 0.0;
@@ -418,23 +422,34 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
 // ASD_POCS_cuda.m:125-131: [bProj,sumC]=Atx(cor); sumC(sumC==0)=1;
 // m = m + beta*(bProj./sumC); m(m<0)=0.
 // Reads the view's ray tables and residuals through the L1 cache, so no
-// block-wide staging or barrier is needed; each lane walks its footprint
-// (or, in the planar geometry when the view allows it, its pixel's shadow)
-// in warp-uniform steps, pairs accumulated in the reference's order.  AX != 0
-// (chosen by the host from the view flags, when every instance's rays of this
-// view share one dominant axis and none is axis-parallel) selects the
-// axis-specialised chord.
-template <bool kPlanar, int AX>
+// block-wide staging or barrier is needed; each lane walks its voxel's shadow
+// (or, when the view does not allow narrowing, the reference's window) in
+// warp-uniform steps, pairs accumulated in the reference's order.  In the
+// planar geometry a view whose rays share one dominant axis and include no
+// axis-parallel ray (the instance's view flags; a block-uniform branch) uses
+// the axis-specialised chord.
+template <bool kPlanar>
 __global__ void __launch_bounds__(kAtxThreads, 4)
-    k_sart_atx(const Inst *__restrict__ insts, Dims D, int view) {
+    k_sart_atx(const Inst *__restrict__ insts, int view) {
   const Inst &I = insts[blockIdx.z];
-  if (((volatile int *)&I.s->done)[0]) return;
+  if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
+  const Dims D = I.d;
+  if (own_block(group_grid(D.nx, D.ny, D.nz, 1)).bid < 0) return;
   const ViewGeo G = view_of(I, view);
   const float4 *tabA = I.tabA + (long long)view * D.na;
   const int vf = I.vflags[view];
   const bool narrow = !(vf & kViewAxisParallel) && I.s->cor_finite &&
                       (!kPlanar || G.z_det[0] == 0.0f);
-  sart_atx_tiles<kPlanar, AX>(I, G, D, tabA, narrow);
+  if constexpr (kPlanar) {
+    if (!(vf & (kViewAxisParallel | kViewNotX)))
+      sart_atx_tiles<true, 1>(I, G, D, tabA, narrow);
+    else if (!(vf & (kViewAxisParallel | kViewNotY)))
+      sart_atx_tiles<true, 2>(I, G, D, tabA, narrow);
+    else
+      sart_atx_tiles<true, 0>(I, G, D, tabA, narrow);
+  } else {
+    sart_atx_tiles<false, 0>(I, G, D, tabA, narrow);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -450,43 +465,13 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 constexpr int kShareGroup = kShareSlots;
 constexpr int kPairChunk = 4;
 
+// The voxel of this thread for the group (see k_sart_atx_shared).
 template <bool kPlanar, int AX>
-__global__ void __launch_bounds__(kAtxThreads, 2)
-    k_sart_atx_shared(const Inst *__restrict__ insts, int batch, Dims D,
-                      int view) {
-  __shared__ float *s_m[kShareGroup];
-  __shared__ float s_beta[kShareGroup];
-  __shared__ unsigned s_active;
-  __shared__ int s_finite;
-  const int g0 = blockIdx.z * kShareGroup;
-  const int gn = min(kShareGroup, batch - g0);
-  if (threadIdx.x == 0) {
-    s_active = 0u;
-    s_finite = 1;
-  }
-  __syncthreads();
-  if (threadIdx.x < gn) {
-    const Inst &Ib = insts[g0 + threadIdx.x];
-    const bool live = ((volatile int *)&Ib.s->done)[0] == 0;
-    s_m[threadIdx.x] = Ib.m;
-    s_beta[threadIdx.x] = Ib.s->beta_f;
-    if (live) {
-      atomicOr(&s_active, 1u << threadIdx.x);
-      if (!Ib.s->cor_finite) atomicAnd(&s_finite, 0);
-    }
-  }
-  __syncthreads();
-  const unsigned active = s_active;
-  if (!active) return;
-  const Inst &I0 = insts[g0];
-  const ViewGeo G = view_of(I0, view);
-  // the group's residuals, interleaved: ray r of slot b at corg[r*16 + b]
-  const float4 *__restrict__ corg = (const float4 *)I0.cor;
-  const float4 *__restrict__ tabA = I0.tabA + (long long)view * D.na;
-  const float4 *__restrict__ tabC = I0.tabC;
-  const int vf = I0.vflags[view];
-  const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
-  const bool narrow = planar_ok && !(vf & kViewAxisParallel) && s_finite;
+__device__ __forceinline__ void atx_shared_voxel(
+    const ViewGeo &G, const Dims &D, const float4 *__restrict__ corg,
+    const float4 *__restrict__ tabA, const float4 *__restrict__ tabC,
+    bool planar_ok, bool narrow, unsigned active, int gn,
+    float *const *s_m, const float *s_beta) {
   int ix, iy, iz;
   const bool valid = tile_voxel(D, ix, iy, iz);
   VoxelWin w;
@@ -598,6 +583,59 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
   }
 }
 
+template <bool kPlanar>
+__global__ void __launch_bounds__(kAtxThreads, 2)
+    k_sart_atx_shared(const Inst *__restrict__ insts, int batch, int view) {
+  __shared__ float *s_m[kShareGroup];
+  __shared__ float s_beta[kShareGroup];
+  __shared__ unsigned s_active;
+  __shared__ int s_finite;
+  const int g0 = blockIdx.z * kShareGroup;
+  const int gn = min(kShareGroup, batch - g0);
+  if (threadIdx.x == 0) {
+    s_active = 0u;
+    s_finite = 1;
+  }
+  __syncthreads();
+  if (threadIdx.x < gn) {
+    const Inst &Ib = insts[g0 + threadIdx.x];
+    const bool live = ((volatile int *)&Ib.s->done)[0] == 0;
+    s_m[threadIdx.x] = Ib.m;
+    s_beta[threadIdx.x] = Ib.s->beta_f;
+    if (live) {
+      atomicOr(&s_active, 1u << threadIdx.x);
+      if (!Ib.s->cor_finite) atomicAnd(&s_finite, 0);
+    }
+  }
+  __syncthreads();
+  const unsigned active = s_active;
+  if (!active) return;
+  const Inst &I0 = insts[g0];
+  const Dims D = I0.d;  // every instance of a shared-geometry plan
+  const ViewGeo G = view_of(I0, view);
+  // the group's residuals, interleaved: ray r of slot b at corg[r*16 + b]
+  const float4 *__restrict__ corg = (const float4 *)I0.cor;
+  const float4 *__restrict__ tabA = I0.tabA + (long long)view * D.na;
+  const float4 *__restrict__ tabC = I0.tabC;
+  const int vf = I0.vflags[view];
+  const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
+  const bool narrow = planar_ok && !(vf & kViewAxisParallel) && s_finite;
+  if constexpr (kPlanar) {
+    if (!(vf & (kViewAxisParallel | kViewNotX)))
+      atx_shared_voxel<true, 1>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
+                                gn, s_m, s_beta);
+    else if (!(vf & (kViewAxisParallel | kViewNotY)))
+      atx_shared_voxel<true, 2>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
+                                gn, s_m, s_beta);
+    else
+      atx_shared_voxel<true, 0>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
+                                gn, s_m, s_beta);
+  } else {
+    atx_shared_voxel<false, 0>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
+                               gn, s_m, s_beta);
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_ax(const float *x, float *y, float *sr, const ViewGeo &g,
@@ -624,45 +662,36 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
   if (d.nz > 1 || d.nb > 1)
-    k_sart_ax<true><<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, d, view);
+    k_sart_ax<true><<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, view);
   else
-    k_sart_ax<false><<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, d, view);
+    k_sart_ax<false><<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, view);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, int axis, cudaStream_t st) {
+                            int view, cudaStream_t st) {
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1 || d.nb > 1)
-    k_sart_atx<false, 0><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
-  else if (axis == 1)
-    k_sart_atx<true, 1><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
-  else if (axis == 2)
-    k_sart_atx<true, 2><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+    k_sart_atx<false><<<grid, kAtxThreads, 0, st>>>(insts, view);
   else
-    k_sart_atx<true, 0><<<grid, kAtxThreads, 0, st>>>(insts, d, view);
+    k_sart_atx<true><<<grid, kAtxThreads, 0, st>>>(insts, view);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
-                                   const Dims &d, int view, int axis,
-                                   cudaStream_t st) {
+                                   const Dims &d, int view, cudaStream_t st) {
   dim3 grid = tile_grid(d.nx, d.ny, d.nz, 1);
   grid.z = (batch + kShareGroup - 1) / kShareGroup;
   if (d.nz > 1 || d.nb > 1)
-    k_sart_atx_shared<false, 0><<<grid, kAtxThreads, 0, st>>>(insts, batch, d, view);
-  else if (axis == 1)
-    k_sart_atx_shared<true, 1><<<grid, kAtxThreads, 0, st>>>(insts, batch, d, view);
-  else if (axis == 2)
-    k_sart_atx_shared<true, 2><<<grid, kAtxThreads, 0, st>>>(insts, batch, d, view);
+    k_sart_atx_shared<false><<<grid, kAtxThreads, 0, st>>>(insts, batch, view);
   else
-    k_sart_atx_shared<true, 0><<<grid, kAtxThreads, 0, st>>>(insts, batch, d, view);
+    k_sart_atx_shared<true><<<grid, kAtxThreads, 0, st>>>(insts, batch, view);
   return cudaGetLastError();
 }
 
 cudaError_t launch_view_tables(const Inst *insts, int batch, const Dims &d,
                                int nv, cudaStream_t st) {
-  k_view_tables<<<dim3((d.na + 127) / 128, nv, batch), 128, 0, st>>>(insts, d);
+  k_view_tables<<<dim3((d.na + 127) / 128, nv, batch), 128, 0, st>>>(insts);
   return cudaGetLastError();
 }
 

@@ -275,10 +275,13 @@ __device__ __forceinline__ void finish_scalars(Scalars *s, double dg2) {
 // TV step, giving its step size alpha*d/||v||.
 template <bool k3D>
 __global__ void __launch_bounds__(kThreads)
-    k_after_sweep(const Inst *__restrict__ insts, Dims D) {
+    k_after_sweep(const Inst *__restrict__ insts) {
   __shared__ Tile<1, k3D> t;
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
+  const Dims D = I.d;
+  const OwnBlock ob = own_block(group_grid(D.nx, D.ny, D.nz, 1));
+  if (ob.bid < 0) return;
   const bool tv = I.s->ng > 0;
   const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
   float v[4] = {0.f, 0.f, 0.f, 0.f};
@@ -311,8 +314,7 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();  // the tile is reused by the next group member
   }
   double tot[4];
-  if (grid_sum<kThreads, 4>(v, I.partials, I.counter, inst_block(),
-                            inst_blocks(), tot)) {
+  if (grid_sum<kThreads, 4>(v, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
     if (threadIdx.x == 0) {
       Scalars *s = I.s;
       const double N = (double)D.nx * D.ny * D.nz;
@@ -339,13 +341,16 @@ __global__ void __launch_bounds__(kThreads)
 // image and to m_pre.
 template <bool k3D>
 __global__ void __launch_bounds__(kThreads)
-    k_tv_step(const Inst *__restrict__ insts, Dims D, int step) {
+    k_tv_step(const Inst *__restrict__ insts, int step) {
   __shared__ Tile<2, k3D> t2;
   __shared__ Tile<1, k3D> t1;
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
   if (step >= ng) return;
+  const Dims D = I.d;
+  const OwnBlock ob = own_block(group_grid(D.nx, D.ny, D.nz, 1));
+  if (ob.bid < 0) return;
   const bool last = step == ng - 1;
   const bool fused_finish = last && ng >= 2;
   const float coef = I.s->tv_coef_f;
@@ -396,8 +401,7 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();  // both tiles are reused by the next group member
   }
   double tot[1];
-  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, inst_block(),
-                            inst_blocks(), tot)) {
+  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
     if (threadIdx.x == 0) {
       Scalars *s = I.s;
       if (fused_finish) {
@@ -413,11 +417,14 @@ __global__ void __launch_bounds__(kThreads)
 // End of an iteration for instances whose last TV step did not finish it
 // (ng == 0 or ng == 1): positivity (after a TV step), dg, alpha/beta, k.
 __global__ void __launch_bounds__(kThreads)
-    k_finish_iter(const Inst *__restrict__ insts, Dims D) {
+    k_finish_iter(const Inst *__restrict__ insts) {
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
   if (ng >= 2) return;  // finished by the last TV step
+  const Dims D = I.d;
+  const OwnBlock ob = own_block(tile_grid(D.nx, D.ny, D.nz, 1));
+  if (ob.bid < 0) return;
   int ix, iy, iz;
   float v[1] = {0.f};
   if (tile_voxel(D.nx, D.ny, D.nz, ix, iy, iz)) {
@@ -434,13 +441,24 @@ __global__ void __launch_bounds__(kThreads)
     I.m_pre[i] = mn;
   }
   double tot[1];
-  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, inst_block(),
-                            inst_blocks(), tot)) {
+  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
     if (threadIdx.x == 0) finish_scalars(I.s, tot[0]);
   }
 }
 
+// Done flags of n instances (the serving queue's poll after an iteration).
+__global__ void k_gather_done(const Inst *__restrict__ insts, int n, int *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = ((volatile int *)&insts[i].s->done)[0];
+}
+
 }  // namespace
+
+cudaError_t launch_gather_done(const Inst *insts, int n, int *out,
+                               cudaStream_t st) {
+  k_gather_done<<<(n + 127) / 128, 128, 0, st>>>(insts, n, out);
+  return cudaGetLastError();
+}
 
 cudaError_t tv_minimize_f64(double *img, const double *img_old, double *wa,
                             double *wb, double *scal, double *partials,
@@ -467,9 +485,9 @@ cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
                                cudaStream_t st) {
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1)
-    k_after_sweep<true><<<grid, kThreads, 0, st>>>(insts, d);
+    k_after_sweep<true><<<grid, kThreads, 0, st>>>(insts);
   else
-    k_after_sweep<false><<<grid, kThreads, 0, st>>>(insts, d);
+    k_after_sweep<false><<<grid, kThreads, 0, st>>>(insts);
   return cudaGetLastError();
 }
 
@@ -478,17 +496,16 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
   (void)ng;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1)
-    k_tv_step<true><<<grid, kThreads, 0, st>>>(insts, d, step);
+    k_tv_step<true><<<grid, kThreads, 0, st>>>(insts, step);
   else
-    k_tv_step<false><<<grid, kThreads, 0, st>>>(insts, d, step);
+    k_tv_step<false><<<grid, kThreads, 0, st>>>(insts, step);
   return cudaGetLastError();
 }
 
 cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
                                int ng, cudaStream_t st) {
   (void)ng;
-  k_finish_iter<<<tile_grid(d.nx, d.ny, d.nz, batch), kThreads, 0, st>>>(insts,
-                                                                         d);
+  k_finish_iter<<<tile_grid(d.nx, d.ny, d.nz, batch), kThreads, 0, st>>>(insts);
   return cudaGetLastError();
 }
 

@@ -54,6 +54,16 @@ WORKLOADS = {
 }
 SHEPP_LOGAN_SCALE = 0.02  # 1/mm per unit phantom intensity (cone3d)
 
+# Serving stream (``--workload serve``): seeded Poisson arrivals of mixed jobs
+# through the serving queue.  The cone-beam jobs are scaled down from the
+# 128^3-512^3 / 180-720-projection range so that one GPU can keep up with
+# 20 arrivals per second at all.
+SERVE = dict(
+    label="serving stream: Poisson arrivals 20/s; 70% 2D fan-beam 512^2, 60-360 views, "
+          "20-100 it; 30% 3D cone-beam 64^3-128^3, 90-180 views on 2n x 2n detectors, "
+          "10-20 it",
+    jobs=120, rate=20.0, frac2d=0.7)
+
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per instance and
 # launch of each iteration kernel, from `ncu --set full --clock-control none`
 # captures of the 2D fan-beam workload at batch 16 (one shared-geometry
@@ -71,12 +81,18 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="fan2d", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="fan2d", choices=sorted(WORKLOADS) + ["serve"])
     ap.add_argument("--batch", type=int, default=None)
     ap.add_argument("--iters", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--jobs", type=int, default=None, help="serve: number of jobs")
     args = ap.parse_args()
+    if args.workload == "serve":
+        W = dict(SERVE)
+        if args.jobs is not None:
+            W["jobs"] = args.jobs
+        return args, W
     W = dict(WORKLOADS[args.workload])
     if args.batch is not None:
         W["batch"] = args.batch
@@ -312,7 +328,14 @@ def main():
     args, W = parse()
     rank, world, local, pg = dist_init(args.gpus)
     if args.impl == "reference":
+        if args.workload == "serve":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference has no serving path; its CPU path is timed "
+                              "on the fan2d and cone3d workloads"}))
+            return 0
         return reference_arm(args, W, rank, world, pg)
+    if args.workload == "serve":
+        return serve_main(args, W, rank, world, pg)
     import torch
 
     import asd_pocs_mex_cuda_demo_gb300 as pkg
@@ -485,6 +508,156 @@ def main():
         }
         print(json.dumps(line))
     plan.close()
+
+
+def serve_jobs(W, seed, device):
+    """The seeded job stream: arrival times, para structs, sinograms and
+    phantoms (projections by the GPU projector, Poisson noise)."""
+    import torch
+
+    from asd_pocs_mex_cuda_demo_gb300 import phantoms
+    from asd_pocs_mex_cuda_demo_gb300._lib import check, load
+
+    L = load()
+    st = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(seed)
+    cache3 = {}
+    jobs, t = [], 0.0
+    for k in range(W["jobs"]):
+        t += rng.exponential(1.0 / W["rate"])
+        if rng.random() < W["frac2d"]:
+            n, nz, na, nb = 512, 1, 888, 1
+            nv = int(rng.choice([60, 120, 180, 360]))
+            iters = int(rng.choice([20, 50, 100]))
+            SO, OD, det, I0 = 541.0, 408.0, 1.0, 1e5
+            vx = None
+            x = phantoms.random_ellipses(n, 5000 + k).astype(np.float32)
+        else:
+            n = int(rng.choice([64, 96, 128]))
+            nz, na, nb = n, 2 * n, 2 * n
+            nv = int(rng.choice([90, 120, 180]))
+            iters = int(rng.choice([10, 20]))
+            SO, OD, det, I0 = 1000.0, 500.0, 0.8 * 256 / n, 5e4
+            vx = 256.0 / n
+            if n not in cache3:
+                cache3[n] = (phantoms.shepp_logan_3d(n) * SHEPP_LOGAN_SCALE).astype(np.float32)
+            x = cache3[n]
+        Wj = dict(nx=n, ny=n, nz=nz, na=na, nb=nb, nv=nv, SO=SO, OD=OD, det=det, vx=vx,
+                  iters=iters, ng=20)
+        phi = phantoms.views(nv)
+        vxs = voxel_size(Wj)
+        sc = np.float32(vxs)
+        detv = np.float32(det) / sc
+        ydet = torch.tensor(((np.arange(na) - na / 2.0 + 0.5) * np.float64(detv))
+                            .astype(np.float32), device=device)
+        zdet = torch.tensor(((np.arange(nb) - nb / 2.0 + 0.5) * np.float64(detv))
+                            .astype(np.float32), device=device)
+        xd = torch.tensor(x, device=device)
+        y = torch.empty(na * nb * nv, device=device)
+        sr = torch.empty(na * nb, device=device)
+        for v, a in enumerate(phi):
+            ph = np.float32(-(a / 180.0 * np.pi))
+            check(L.asdpocs_ax_device(xd.data_ptr(), y.data_ptr() + 4 * na * nb * v,
+                                      sr.data_ptr(), float(np.cos(ph)), float(np.sin(ph)),
+                                      ydet.data_ptr(), zdet.data_ptr(),
+                                      float(np.float32(SO) / sc), float(np.float32(OD) / sc),
+                                      float(sc), 1.0, n, n, nz, na, nb, st))
+        torch.cuda.synchronize()
+        P = phantoms.poisson_noise(y.cpu().numpy().astype(np.float64), I0, seed=7000 + k)
+        para = dict(para_for(Wj), phi_vec=phi)
+        jobs.append(dict(t=t, para=para, P=P.astype(np.float32), x=x,
+                         kind="2d" if nz == 1 else "3d"))
+    return jobs
+
+
+def serve_main(args, W, rank, world, pg):
+    """Served throughput and latency of a seeded Poisson job stream, against
+    the same jobs run one at a time (plain, one-instance plans)."""
+    import torch
+
+    import asd_pocs_mex_cuda_demo_gb300 as pkg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    pkg.load()
+    jobs = serve_jobs(W, seed=31 + rank, device=dev)
+    # warm-up: one job of each kind through a server (graph captures, pools)
+    with pkg.Server() as srv:
+        for kind in ("2d", "3d"):
+            j = next((j for j in jobs if j["kind"] == kind), None)
+            if j is not None:
+                srv.wait(srv.submit(dict(j["para"], maxnumIter=1), j["P"]))
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    results = [None] * len(jobs)
+    barrier(pg)
+    clocks.start()
+    with pkg.Server(slots_per_lane=32) as srv:
+        ids = [None] * len(jobs)
+        t0 = time.perf_counter()
+
+        def feeder():
+            for k, j in enumerate(jobs):
+                dt = t0 + j["t"] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                ids[k] = srv.submit(j["para"], j["P"], I0=j["x"])
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        for k in range(len(jobs)):
+            while ids[k] is None:
+                time.sleep(0.0005)
+            results[k] = srv.wait(ids[k])
+        t_end = time.perf_counter()
+        th.join()
+        mem_peak = srv.memory()[1]
+    clk = clocks.stop()
+    makespan = allmax(pg, t_end - t0)
+    lat = np.array([r[2]["total_ms"] for r in results])
+    served = len(jobs) * world / makespan
+    # plain: the same jobs one at a time, each in its own one-instance plan
+    plain_s, equal = 0.0, True
+    stream = torch.cuda.Stream(device=dev)
+    for k, j in enumerate(jobs):
+        with pkg.Plan(j["para"], j["para"]["phi_vec"], stream=stream.cuda_stream) as pl:
+            pl.set_sinogram(0, j["P"])
+            pl.set_reference(0, j["x"])
+            pl.reset()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            pl.run(use_graph=True, sync=False)
+            e1.record(stream)
+            e1.synchronize()
+            plain_s += e0.elapsed_time(e1) / 1e3
+            equal = equal and bool(np.array_equal(pl.image(0), results[k][0]))
+    rm = [float(r[1]["RMSE"][-1]) for r in results]
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": served, "unit": "recons/s", "n_gpus": world,
+            "steps": 1, "warmup": 1, "ms_per_step": makespan * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded phantoms, Poisson noise, Poisson "
+                                    "arrivals)",
+            "config": {"workload": W["label"], "jobs": len(jobs), "rate_per_s": W["rate"],
+                       "jobs_2d": sum(j["kind"] == "2d" for j in jobs),
+                       "jobs_3d": sum(j["kind"] == "3d" for j in jobs),
+                       "parallelism": f"replicas x{world}",
+                       "timing": "host wall clock from the first arrival to the last "
+                                 "result; results copied to host memory"},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)),
+                           "p99": float(np.percentile(lat, 99)),
+                           "max": float(lat.max()),
+                           "queued_p50": float(np.percentile(
+                               [r[2]["queued_ms"] for r in results], 50))},
+            "plain": {"recons_per_s": len(jobs) / plain_s, "seconds": plain_s,
+                      "served_speedup": served / world / (len(jobs) / plain_s),
+                      "served_equals_plain_bitwise": equal},
+            "rmse_vs_phantom": {"mean": float(np.mean(rm)), "max": float(np.max(rm))},
+            "hbm_peak_bytes": int(mem_peak),
+            "clocks": clk,
+        }))
+    return 0
 
 
 def reference_arm(args, W, rank, world, pg):

@@ -169,10 +169,16 @@ typedef struct {
 
 typedef struct asdpocs_plan_s *asdpocs_plan;
 
-/* Create a plan for `batch` reconstructions that share nx,ny,nz,na,nb,nv.
- * geom[i], phi_vec_deg[i*nv..] and opt[i] are per instance (geom/opt may
- * point to one element when batch==1).  All device memory is allocated here;
- * hbm_budget_bytes (0 = no limit) rejects plans that would exceed it. */
+/* Create a plan for `batch` reconstructions (the batch descriptor: one
+ * geometry, angle list and option set per instance).  geom[i] and opt[i] are
+ * per instance and may differ in every field, sizes included, except that
+ * the instances are all 2-D (nz == nb == 1), all single-slice with nb > 1,
+ * or all 3-D (nz > 1).  phi_vec_deg holds the instances' angle lists one
+ * after the other (geom[0].nv values, then geom[1].nv, ...).  Each step of
+ * the iteration is one launch for the whole batch; an instance gives the
+ * same result, bit for bit, alone or in any batch.  All device memory is
+ * allocated here; hbm_budget_bytes (0 = no limit) rejects plans that would
+ * exceed it. */
 int asdpocs_plan_create(asdpocs_plan *plan, int batch,
                         const asdpocs_geometry *geom,
                         const double *phi_vec_deg,
@@ -184,7 +190,7 @@ unsigned long long asdpocs_plan_bytes(asdpocs_plan plan);
 
 /* Load instance data.  `where`: 0 = host pointer (copied on the plan's
  * stream), 1 = device pointer.  P: (na*nb) x nv float sinogram; m0 / I0:
- * nx*ny*nz (NULL = zeros / no RMSE). */
+ * nx*ny*nz (NULL = zeros / no RMSE); sizes are the instance's own. */
 int asdpocs_plan_set_sinogram(asdpocs_plan plan, int inst, const float *P,
                               int where);
 int asdpocs_plan_set_initial(asdpocs_plan plan, int inst, const float *m0,
@@ -234,6 +240,72 @@ int ASD_POCS_cuda(const double *P, const double *phi_vec_deg,
 int SART_cuda_inline(const double *P, const double *phi_vec_deg,
                      const asdpocs_geometry *geom, double lambda,
                      const double *m0, double *m_out, double *dataTolerance);
+
+/* ---------------------------------------------------------------------
+ * Serving queue (no counterpart in the reference, whose drivers run one
+ * reconstruction at a time).  Jobs of any geometry, view count and
+ * iteration budget are submitted at any time.  A worker thread admits them
+ * into free slots of device-resident lanes -- one lane per kind (2-D,
+ * single-slice, cone beam) and view-count class (views rounded up to a
+ * power of two), each on its own CUDA stream -- when the HBM budget has
+ * room, runs one ASD-POCS iteration of every job of a lane per launch
+ * sequence (a CUDA graph replayed while the lane's membership keeps its
+ * shape), retires jobs as they finish and admits waiting ones in their
+ * place, so jobs that arrive while others run join them on the device.
+ * Each job's result is bit-identical to the same job run alone in a plan.
+ * All calls are thread-safe.
+ * --------------------------------------------------------------------- */
+typedef struct asdpocs_server_s *asdpocs_server;
+
+typedef struct {
+  int slots_per_lane;                  /* concurrent jobs per lane (32)   */
+  unsigned long long hbm_budget_bytes; /* device bytes for job state;
+                                          0 = half the free memory       */
+  int inflight;                        /* iterations queued ahead per
+                                          lane (2)                        */
+} asdpocs_server_config;
+void asdpocs_server_config_default(asdpocs_server_config *cfg);
+
+enum {
+  ASDPOCS_JOB_QUEUED = 0,
+  ASDPOCS_JOB_RUNNING = 1,
+  ASDPOCS_JOB_DONE = 2,
+  ASDPOCS_JOB_FAILED = 3
+};
+
+/* Times of a finished job (host steady clock, milliseconds). */
+typedef struct {
+  double queued_ms; /* submission to admission  */
+  double run_ms;    /* admission to result ready */
+  double total_ms;  /* submission to result ready (the job's latency) */
+} asdpocs_job_times;
+
+/* Start the worker on the calling thread's current device (cfg NULL =
+ * defaults). */
+int asdpocs_server_create(asdpocs_server *server,
+                          const asdpocs_server_config *cfg);
+/* Queue a job: geometry, geom->nv view angles (degrees), options (NULL =
+ * defaults), sinogram P ((na*nb) x nv floats, host), optional initial image
+ * m0 and reference image I0 (nx*ny*nz floats, host; NULL = zeros / no
+ * RMSE).  The data are copied before the call returns.  A job larger than
+ * the whole HBM budget is rejected with ASDPOCS_ERR_NOMEM. */
+int asdpocs_server_submit(asdpocs_server server, const asdpocs_geometry *geom,
+                          const double *phi_vec_deg, const asdpocs_options *opt,
+                          const float *P, const float *m0, const float *I0,
+                          long long *job);
+/* Current state of a job (ASDPOCS_JOB_*). */
+int asdpocs_server_poll(asdpocs_server server, long long job, int *state);
+/* Wait for a job and take its results (image nx*ny*nz floats, stats, the
+ * per-iteration RMSE if a reference was given, times); any output may be
+ * NULL.  The job is released: a second wait on it is an error. */
+int asdpocs_server_wait(asdpocs_server server, long long job, float *m_res,
+                        asdpocs_stats *st, double *rmse,
+                        asdpocs_job_times *times);
+/* Device bytes held by admitted jobs now, and the peak so far. */
+int asdpocs_server_memory(asdpocs_server server, unsigned long long *in_use,
+                          unsigned long long *peak);
+/* Stop the worker (jobs not yet finished fail) and release everything. */
+int asdpocs_server_destroy(asdpocs_server server);
 
 #ifdef __cplusplus
 }

@@ -87,3 +87,26 @@ def test_device_math_matches_oracle(dm, oracle_mod, case):
                       g["SO"], g["OD"], g["scale"], g["det"], g["det"], 1.0, nx, ny, nz,
                       na, nb, staged)
             assert np.array_equal(b, bo) and np.array_equal(sc, co), (a, staged)
+
+
+@pytest.mark.parametrize("dims", [(48, 40, 1, 96, 1), (24, 20, 12, 48, 24)])
+def test_narrowing_off_grid_detector(dm, oracle_mod, dims):
+    """Detector coordinates off the uniform grid turn the shadow narrowing
+    off; the result stays bit-identical to the oracle."""
+    nx, ny, nz, na, nb = dims
+    SO, OD, det = 541.0, 408.0, 1.0
+    rng = np.random.default_rng(nx * nz)
+    vx = SO / (SO + OD) * det * na / nx
+    yv = rng.standard_normal(na * nb).astype(np.float32)
+    for a in (17.0, 133.0, 251.0):
+        g = oracle_mod.gateway_geometry(-a / 180 * np.pi, SO, OD, vx, det, na, nb)
+        yd = (g["y_det"] + rng.uniform(-0.3, 0.3, na) * g["det"]).astype(np.float32)
+        zd = (g["z_det"] * (1.07 if nb > 1 else 1.0)).astype(np.float32)
+        g["y_det"], g["z_det"] = yd, zd
+        bo, co = oracle_mod.atx(yv, g, nx, ny, nz)
+        b = np.zeros(nx * ny * nz, np.float32)
+        sc = np.zeros(nx * ny * nz, np.float32)
+        dm.dm_atx(_p(b), _p(yv), _p(sc), g["cos_phi"], g["sin_phi"], _p(yd), _p(zd),
+                  g["SO"], g["OD"], g["scale"], g["det"], g["det"], 1.0, nx, ny, nz, na, nb,
+                  2)
+        assert np.array_equal(b, bo) and np.array_equal(sc, co), a

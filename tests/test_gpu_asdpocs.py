@@ -182,3 +182,50 @@ def test_shared_geometry_batch_equals_alone_bitwise(gpu, monkeypatch):
             pl.run()
             for k in range(5):
                 assert np.array_equal(pl.image(k), alone[k]), (force_per_instance, k)
+
+
+def _uneven(seed, n, na, nv, iters, ng, SO=541.0, OD=408.0, det=1.0):
+    vx = phantoms.fov_voxel_size(SO, OD, det, na, n)
+    x = phantoms.random_ellipses(n, seed)
+    phi = phantoms.views(nv) + 0.5 * seed
+    para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, na=na, nb=1, detsize=det,
+                phi_vec=phi, maxnumIter=iters, numOfgradients=ng, alpha=0.002)
+    P = np.stack([pkg.Ax_cone_gpu(x.astype(np.float32), dict(para, phi=-a / 180 * np.pi))[0]
+                  for a in phi], axis=1)
+    return x, phantoms.poisson_noise(P, 1e5, seed), para
+
+
+def test_uneven_batch_equals_alone_bitwise(gpu, oracle_mod):
+    """One plan of instances with different image sizes, bins, view counts,
+    iteration counts and TV step counts (the batched uneven-slice pattern):
+    every step is one launch for all of them, and each result equals the
+    instance's run alone bit for bit and the oracle within the
+    reconstruction tolerance."""
+    insts = [_uneven(11, 48, 72, 12, 3, 20), _uneven(12, 80, 120, 30, 5, 5),
+             _uneven(13, 64, 96, 20, 2, 1), _uneven(14, 33, 50, 7, 4, 0),
+             _uneven(15, 80, 120, 30, 5, 5)]
+    alone = []
+    for x, P, para in insts:
+        with pkg.Plan(para, para["phi_vec"]) as pl:
+            pl.set_sinogram(0, P.ravel(order="F"))
+            pl.set_reference(0, x)
+            pl.reset()
+            pl.run()
+            alone.append((pl.image(0), pl.stats(0)))
+    paras = [i[2] for i in insts]
+    with pkg.Plan(paras, [p["phi_vec"] for p in paras]) as pl:
+        for k, (x, P, _) in enumerate(insts):
+            pl.set_sinogram(k, P.ravel(order="F"))
+            pl.set_reference(k, x)
+        for use_graph in (True, False):
+            pl.reset()
+            pl.run(use_graph=use_graph)
+            for k in range(len(insts)):
+                assert np.array_equal(pl.image(k), alone[k][0]), (use_graph, k)
+                s = pl.stats(k)
+                assert s["IterationNum"] == alone[k][1]["IterationNum"]
+                np.testing.assert_array_equal(s["RMSE"], alone[k][1]["RMSE"])
+    for k in (0, 1, 3):
+        _, P, para = insts[k]
+        mo, _ = oracle_mod.asdpocs(P, para)
+        assert rel_l2(alone[k][0], mo) < RECON_TOL, k

@@ -1,0 +1,92 @@
+"""Serving queue on the GPU: jobs of mixed kinds, sizes, view counts and
+iteration budgets submitted while others run; each result must equal the
+same reconstruction run alone in a Plan, bit for bit, and the device memory
+the jobs held must return to zero."""
+import time
+
+import numpy as np
+import pytest
+
+import asd_pocs_mex_cuda_demo_gb300 as pkg
+from asd_pocs_mex_cuda_demo_gb300 import phantoms
+
+pytestmark = pytest.mark.gpu
+
+
+def _job2d(seed, n, na, nv, iters, ng):
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = phantoms.fov_voxel_size(SO, OD, det, na, n)
+    x = phantoms.random_ellipses(n, seed).astype(np.float32)
+    phi = phantoms.views(nv) + 0.25 * seed
+    para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, na=na, nb=1, detsize=det,
+                phi_vec=phi, maxnumIter=iters, numOfgradients=ng, alpha=0.02)
+    P = np.stack([pkg.Ax_cone_gpu(x, dict(para, phi=-a / 180 * np.pi))[0] for a in phi],
+                 axis=1)
+    return x, phantoms.poisson_noise(P, 1e5, seed).astype(np.float32), para
+
+
+def _job3d(seed, n, na, nb, nv, iters):
+    SO, OD, det = 1000.0, 500.0, 0.8 * 256 / n
+    vx = 1.0 * 256 / n
+    x = (phantoms.shepp_logan_3d(n) * 0.02).astype(np.float32)
+    phi = phantoms.views(nv) + seed
+    para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=n, na=na, nb=nb, detsize=det,
+                phi_vec=phi, maxnumIter=iters, numOfgradients=3, alpha=0.02)
+    P = np.stack([pkg.Ax_cone_gpu(x, dict(para, phi=-a / 180 * np.pi))[0] for a in phi],
+                 axis=1)
+    return x, phantoms.poisson_noise(P, 5e4, seed).astype(np.float32), para
+
+
+def _alone(x, P, para):
+    with pkg.Plan(para, para["phi_vec"]) as pl:
+        pl.set_sinogram(0, P.ravel(order="F"))
+        pl.set_reference(0, x)
+        pl.reset()
+        pl.run()
+        return pl.image(0), pl.stats(0)
+
+
+def test_server_jobs_equal_alone(gpu):
+    jobs = [_job2d(1, 48, 72, 12, 3, 5), _job2d(2, 64, 96, 20, 4, 10),
+            _job2d(3, 40, 60, 9, 2, 0), _job3d(4, 16, 32, 24, 10, 2),
+            _job2d(5, 64, 96, 40, 3, 2), _job2d(6, 33, 50, 7, 5, 1),
+            _job3d(7, 20, 40, 30, 12, 3), _job2d(8, 48, 72, 12, 6, 20)]
+    ref = [_alone(*j) for j in jobs]
+    with pkg.Server(slots_per_lane=3) as srv:
+        ids = [srv.submit(para, P, I0=x) for x, P, para in jobs[:3]]
+        # later arrivals join while the first ones run
+        deadline = time.time() + 30
+        while srv.poll(ids[0]) == 0 and time.time() < deadline:
+            time.sleep(0.001)
+        ids += [srv.submit(para, P, I0=x) for x, P, para in jobs[3:]]
+        for k, j in enumerate(ids):
+            img, out, t = srv.wait(j)
+            assert np.array_equal(img, ref[k][0]), k
+            assert out["IterationNum"] == ref[k][1]["IterationNum"]
+            np.testing.assert_array_equal(out["RMSE"], ref[k][1]["RMSE"])
+            assert 0.0 <= t["queued_ms"] <= t["total_ms"] and t["run_ms"] > 0.0
+        in_use, peak = srv.memory()
+        assert in_use == 0 and peak > 0
+        with pytest.raises(pkg.AsdpocsError):
+            srv.wait(ids[0])  # released
+
+
+def test_server_budget_admission(gpu):
+    jobs = [_job2d(20 + s, 48, 72, 12, 3, 5) for s in range(4)]
+    ref = [_alone(*j) for j in jobs]
+    one = None
+    with pkg.Server() as probe:
+        j = probe.submit(jobs[0][2], jobs[0][1])
+        probe.wait(j)
+        one = probe.memory()[1]  # device bytes of one such job
+    # room for two jobs at a time: the others wait for memory, then run
+    with pkg.Server(slots_per_lane=8, hbm_budget_bytes=2 * one + one // 2) as srv:
+        ids = [srv.submit(para, P, I0=x) for x, P, para in jobs]
+        for k, j in enumerate(ids):
+            img, _, _ = srv.wait(j)
+            assert np.array_equal(img, ref[k][0]), k
+        assert srv.memory()[1] <= 2 * one
+    with pkg.Server(hbm_budget_bytes=one // 2) as srv:
+        with pytest.raises(pkg.AsdpocsError) as e:
+            srv.submit(jobs[0][2], jobs[0][1])
+        assert e.value.status == 3

@@ -61,11 +61,16 @@ def test_option_defaults_match_reference(lib):
     assert (o.maxnumIter, o.alpha, o.beta_red) == (7, 0.2, 1.0)
 
 
-def test_plan_rejects_mixed_shapes(lib):
+def test_plan_rejects_mixed_kinds(lib):
+    """Instances of one plan may differ in size but not in kind: 2-D fan
+    beam and cone beam need different kernels (rejected before any device
+    call)."""
     a = dict(PARA)
-    b = dict(PARA, nx=16)
-    with pytest.raises(pkg.AsdpocsError, match="must share"):
+    b = dict(PARA, nz=8, nb=4)
+    with pytest.raises(pkg.AsdpocsError, match="all 2-D"):
         pkg.Plan([a, b], [np.arange(1, 4.0), np.arange(1, 4.0)])
+    with pytest.raises(pkg.AsdpocsError, match="one phi_vec per instance"):
+        pkg.Plan([a, a], [np.arange(1, 4.0)])
 
 
 def test_phantoms():
