@@ -44,7 +44,7 @@ __device__ __forceinline__ void ax_warp(const ViewGeo &G, const Dims &D,
   if (D.nz == 1 && zd == 0.0f)
     ray_columns_planar_fast(R, lane, 32, ld, ys, ss);
   else
-    ray_columns<false>(R, lane, 32, ld, ys, ss);
+    ray_columns_fast<2>(R, lane, 32, ld, ys, ss);
   ys = warp_sum(ys);
   ss = warp_sum(ss);
 }

@@ -5,7 +5,8 @@
 //   dm_ax   -- Ax with the columns of a ray split over `lanes` partial sums
 //              combined by the same xor butterfly as the warp reduction,
 //              with the reference's weight expressions (exact=1) or the
-//              kernels' division-free ones (exact=0);
+//              kernels' division-free ones (exact=0: the kernels' grouped
+//              form, exact=2: the per-column form it must match);
 //   dm_atx  -- Atx through the staged ray tables and the branch-free chords
 //              (ray_tab_a / ray_tab_c, chord_planar_bf / chord3_bf) as the
 //              kernels run it (staged=1), the same restricted to each voxel's
@@ -39,14 +40,18 @@ extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,
     for (int l = 0; l < lanes; l++) {
       float a = 0.f, b = 0.f;
       auto ld = [&](long long i) { return x[i]; };
-      if (planar && exact)
+      if (planar && exact == 1)
         ray_columns_planar<true>(R, l, lanes, ld, a, b);
+      else if (planar && exact == 2)
+        ray_columns_planar<false>(R, l, lanes, ld, a, b);
       else if (planar)
         ray_columns_planar_fast(R, l, lanes, ld, a, b);
-      else if (exact)
+      else if (exact == 1)
         ray_columns<true>(R, l, lanes, ld, a, b);
-      else
+      else if (exact == 2)
         ray_columns<false>(R, l, lanes, ld, a, b);
+      else
+        ray_columns_fast<2>(R, l, lanes, ld, a, b);
       py[l] = a;
       ps[l] = b;
     }

@@ -8,10 +8,11 @@ test data, extracted by tests/golden/make_realdata.py):
   detector over 90 views of 180 degrees (a single-slice geometry with two
   detector rows), then reconstructed with its options for a few iterations.
 
-The GPU runs the image in FP32 where the oracle keeps FP64; at these
-settings a 1e-7 relative perturbation of the swine sinogram moves the FP64
-result by 4e-4, so the reconstructions are compared to 1e-2 and the data
-residual to 1e-3."""
+The GPU runs the image in FP32 where the oracle keeps FP64; at the swine
+settings a 1e-7 relative perturbation of the sinogram moves the FP64 result
+by 4e-4, so the reconstructions are compared to 1e-2 and the data residual
+to 1e-3 (the head slice's chaotic demo options are compared through their
+RMSE trajectory)."""
 import numpy as np
 import pytest
 
@@ -59,9 +60,17 @@ def test_head_slice_single_slice_geometry(gpu, oracle_mod):
         yo, _ = oracle_mod.ax(x, g, n, n, 1)
         assert rel_l2(y, yo) < 1e-5, a
         P[:, i] = y
+    # the demo's options (alpha 0.2) are chaotic here: a 1e-7 relative
+    # perturbation of P moves the FP64 image by 3e-2 but its RMSE trajectory
+    # by 5e-4; at alpha 0.002 the image moves by 2e-4
     run = dict(para, maxnumIter=4, alpha=0.2, alpha_red=0.95, beta_red=1.0, I0=I3d)
     m, out = pkg.ASD_POCS_cuda(P, run)
     mo, oo = oracle_mod.asdpocs(P, run)
-    assert rel_l2(m.ravel(order="F"), mo) < 1e-2
+    assert rel_l2(m.ravel(order="F"), mo) < 1e-1
     np.testing.assert_allclose(out["RMSE"], oo["RMSE"], rtol=1e-2)
     assert out["RMSE"][-1] < out["RMSE"][0]
+    run = dict(run, alpha=0.002)
+    m, out = pkg.ASD_POCS_cuda(P, run)
+    mo, oo = oracle_mod.asdpocs(P, run)
+    assert rel_l2(m.ravel(order="F"), mo) < 1e-2
+    np.testing.assert_allclose(out["RMSE"], oo["RMSE"], rtol=1e-3)
