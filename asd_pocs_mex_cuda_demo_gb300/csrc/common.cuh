@@ -88,6 +88,7 @@ struct Inst {
   float4 *tabA;              // ray slopes of every view, nv*na (ray_tab_a)
   int *vflags;               // per view: kViewAxisParallel | kViewNotX | kViewNotY
   float4 *tabC;              // 3D ray slopes of the current view, na*nb
+  int tabc_mode;             // who writes tabC in the forward step (kTabc*)
   double *rmse;              // [maxIter]
   double *partials;          // reduction partials [blocks * kMaxReduceK]
   unsigned *counter;         // reduction ticket
@@ -99,6 +100,12 @@ constexpr int kMaxPartials = 1 << 22;  // blocks per reduction (sanity bound)
 // Instances per group of the shared-geometry kernels; their residuals are
 // stored interleaved, cor[r * kShareSlots + slot].
 constexpr int kShareSlots = 16;
+
+// Inst::tabc_mode.  kTabcOwn: the instance writes its own table while it
+// runs.  Instances sharing geometry share one table: its writer
+// (kTabcShared) refreshes it every view even after it has finished, so the
+// others (kTabcNone) keep reading current slopes.
+constexpr int kTabcOwn = 0, kTabcShared = 1, kTabcNone = 2;
 
 // View flags (Inst::vflags): some ray of the view has no x (or no y)
 // extent; some ray is not x-dominant; some ray is not y-dominant.

@@ -413,16 +413,17 @@ int check_instance(const asdpocs_geometry &g, const asdpocs_options &o) {
 }
 
 InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
-                           size_t cor_floats) {
+                           size_t cor_floats, int parts) {
   const Dims d{g.nx, g.ny, g.nz, g.na, g.nb};
   const size_t N = (size_t)g.nx * g.ny * g.nz;
   const size_t M = (size_t)g.na * g.nb;
-  const size_t per_img = align256(N * 4);
+  const bool st = parts & kLayoutState, geo = parts & kLayoutGeometry;
+  const size_t per_img = st ? align256(N * 4) : 0;
   const size_t nblk = (size_t)reduce_blocks_for(d);
   const bool proj3d = g.nz > 1 || g.nb > 1;
   InstLayout o;
   size_t off = 0;
-  o.P = off; off += align256(M * g.nv * 4);
+  o.P = off; off += st ? align256(M * g.nv * 4) : 0;
   o.m = off; off += per_img;
   o.m_pre = off; off += per_img;
   o.m_res = off; off += per_img;
@@ -430,22 +431,37 @@ InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
   o.I0 = off; off += per_img;
   o.tvb = off; off += per_img;
   o.tvc = off; off += per_img;
-  o.cor = off; off += align256(cor_floats * 4);
-  o.tabA = off; off += align256((size_t)g.na * g.nv * 16);
-  o.vflags = off; off += align256((size_t)g.nv * 4);
-  o.tabC = off; off += align256(proj3d ? M * 16 : 16);
-  o.ydet = off; off += align256((size_t)g.na * 4);
-  o.zdet = off; off += align256((size_t)g.nb * 4);
-  o.trig = off; off += align256((size_t)g.nv * 8);
-  o.rmse = off; off += align256((size_t)(max_iter + 1) * 8);
-  o.part = off; off += align256(nblk * kMaxReduceK * 8);
-  o.cnt = off; off += 256;
-  o.scal = off; off += align256(sizeof(Scalars));
+  o.rmse = off; off += st ? align256((size_t)(max_iter + 1) * 8) : 0;
+  o.part = off; off += st ? align256(nblk * kMaxReduceK * 8) : 0;
+  o.cnt = off; off += st ? 256 : 0;
+  o.scal = off; off += st ? align256(sizeof(Scalars)) : 0;
+  o.cor = off; off += geo ? align256(cor_floats * 4) : 0;
+  o.tabA = off; off += geo ? align256((size_t)g.na * g.nv * 16) : 0;
+  o.vflags = off; off += geo ? align256((size_t)g.nv * 4) : 0;
+  o.tabC = off; off += geo ? align256(proj3d ? M * 16 : 16) : 0;
+  o.ydet = off; off += geo ? align256((size_t)g.na * 4) : 0;
+  o.zdet = off; off += geo ? align256((size_t)g.nb * 4) : 0;
+  o.trig = off; off += geo ? align256((size_t)g.nv * 8) : 0;
   o.bytes = off;
   return o;
 }
 
-cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,
+void bind_state(Inst &I, char *b, const InstLayout &o) {
+  I.P = (const float *)(b + o.P);
+  I.m = (float *)(b + o.m);
+  I.m_pre = (float *)(b + o.m_pre);
+  I.m_res = (float *)(b + o.m_res);
+  I.m_k1 = (float *)(b + o.m_k1);
+  I.I0 = (float *)(b + o.I0);
+  I.tv_b = (float *)(b + o.tvb);
+  I.tv_c = (float *)(b + o.tvc);
+  I.rmse = (double *)(b + o.rmse);
+  I.partials = (double *)(b + o.part);
+  I.counter = (unsigned *)(b + o.cnt);
+  I.s = (Scalars *)(b + o.scal);
+}
+
+cudaError_t bind_geometry(Inst &I, char *b, const InstLayout &o,
                           const asdpocs_geometry &g, const double *phi_deg,
                           cudaStream_t st) {
   I.d = Dims{g.nx, g.ny, g.nz, g.na, g.nb};
@@ -458,23 +474,12 @@ cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,
   std::vector<float2> trig(g.nv);
   for (int v = 0; v < g.nv; v++) trig[v] = view_trig(phi_deg[v]);
   I.trig = (const float2 *)(b + o.trig);
-  I.P = (const float *)(b + o.P);
-  I.m = (float *)(b + o.m);
-  I.m_pre = (float *)(b + o.m_pre);
-  I.m_res = (float *)(b + o.m_res);
-  I.m_k1 = (float *)(b + o.m_k1);
-  I.I0 = (float *)(b + o.I0);
-  I.tv_b = (float *)(b + o.tvb);
-  I.tv_c = (float *)(b + o.tvc);
   I.cor = (float *)(b + o.cor);
   I.cor_stride = 1;
   I.tabA = (float4 *)(b + o.tabA);
   I.vflags = (int *)(b + o.vflags);
   I.tabC = (float4 *)(b + o.tabC);
-  I.rmse = (double *)(b + o.rmse);
-  I.partials = (double *)(b + o.part);
-  I.counter = (unsigned *)(b + o.cnt);
-  I.s = (Scalars *)(b + o.scal);
+  I.tabc_mode = kTabcOwn;
   // pageable sources: staged before each call returns
   cudaError_t e = cudaMemcpyAsync(b + o.ydet, gg.y_det.data(), (size_t)g.na * 4,
                                   cudaMemcpyHostToDevice, st);
@@ -485,6 +490,13 @@ cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,
     e = cudaMemcpyAsync(b + o.trig, trig.data(), (size_t)g.nv * 8,
                         cudaMemcpyHostToDevice, st);
   return e;
+}
+
+cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,
+                          const asdpocs_geometry &g, const double *phi_deg,
+                          cudaStream_t st) {
+  bind_state(I, b, o);
+  return bind_geometry(I, b, o, g, phi_deg, st);
 }
 
 Scalars initial_scalars(const asdpocs_options &o, bool has_ref) {
@@ -657,6 +669,9 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
       const int g = i - i % kShareSlots;
       I.cor = (float *)(b + base[g] + lay[g].cor) + i % kShareSlots;
       I.cor_stride = kShareSlots;
+      // one ray-slope table for all: instance 0 refreshes it every view
+      I.tabC = (float4 *)(b + base[0] + lay[0].tabC);
+      I.tabc_mode = i == 0 ? kTabcShared : kTabcNone;
     }
   }
   p->d_inst = (Inst *)(b + inst_off);

@@ -21,14 +21,31 @@ int instance_kind(const asdpocs_geometry &g);
 // Sizes and counts of `g` checked (status and message set on failure).
 int check_instance(const asdpocs_geometry &g, const asdpocs_options &o);
 
-// Layout of an instance; cor_floats is the length of its residual buffer
-// (na*nb, or kShareSlots*na*nb for the first instance of a shared group).
-InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
-                           size_t cor_floats);
+// Parts of an instance's block: its state (sinogram, images, scalars,
+// reduction scratch) and its geometry (detector coordinates, view angles,
+// ray tables, residual buffer).  Instances that share geometry can keep one
+// geometry part between them.
+constexpr int kLayoutState = 1, kLayoutGeometry = 2;
 
-// Points I at the block `b` laid out as `o` (own residual buffer, stride 1)
-// and uploads the instance's detector coordinates and view cosines/sines on
-// `st` (the host staging is released when the call returns).
+// Layout of the parts `parts` of an instance (absent parts take no bytes);
+// cor_floats is the length of its residual buffer (na*nb, or kShareSlots
+// times that for the first instance of a shared group).
+InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
+                           size_t cor_floats,
+                           int parts = kLayoutState | kLayoutGeometry);
+
+// Points I's state pointers at the block `b` laid out as `o`.
+void bind_state(Inst &I, char *b, const InstLayout &o);
+
+// Points I's geometry at the block `b` laid out as `o` (own residual buffer,
+// stride 1, own ray-slope table) and uploads the detector coordinates and
+// view cosines/sines on `st` (the host staging is released when the call
+// returns).
+cudaError_t bind_geometry(Inst &I, char *b, const InstLayout &o,
+                          const asdpocs_geometry &g, const double *phi_deg,
+                          cudaStream_t st);
+
+// Both of the above for a block holding both parts.
 cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,
                           const asdpocs_geometry &g, const double *phi_deg,
                           cudaStream_t st);

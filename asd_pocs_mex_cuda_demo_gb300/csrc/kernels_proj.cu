@@ -288,12 +288,16 @@ __global__ void __launch_bounds__(128)
 // cor0=P(:,ii)-proj; dd2+=||cor0||^2; cor=cor0./sumR.
 // Also records whether every residual is finite (Scalars::cor_finite), and
 // for 3D geometry writes the view's per-ray slopes ray_tab_c for the
-// backward step that follows.
+// backward step that follows (Inst::tabc_mode: a shared table's writer does
+// so even after its own iterations have ended).
 template <bool k3D>
 __global__ void __launch_bounds__(kAxThreads)
     k_sart_ax(const Inst *__restrict__ insts, int view) {
   const Inst &I = insts[blockIdx.z];
-  if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
+  if (view >= I.nv) return;
+  const bool done = ((volatile int *)&I.s->done)[0] != 0;
+  const bool tabc = k3D && (I.tabc_mode == kTabcShared || (!done && I.tabc_mode == kTabcOwn));
+  if (done && !tabc) return;
   const Dims D = I.d;
   const long long nr = (long long)D.na * D.nb;
   const OwnBlock ob = own_block(dim3((unsigned)((nr + kAxWarps - 1) / kAxWarps), 1));
@@ -301,6 +305,11 @@ __global__ void __launch_bounds__(kAxThreads)
   const ViewGeo G = view_of(I, view);
   const int lane = threadIdx.x & 31;
   const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
+  if (tabc && lane == 0 && r < nr) {
+    const int ia = (int)(r % D.na), ib = (int)(r / D.na);
+    I.tabC[r] = ray_tab_c(I.tabA[(long long)view * D.na + ia], G.z_det[ib]);
+  }
+  if (done) return;  // the whole instance: no reduction
   float part[2] = {0.f, 0.f};  // dd2, non-finite residuals
   if (r < nr) {
     float ys, ss;
@@ -313,10 +322,6 @@ __global__ void __launch_bounds__(kAxThreads)
       I.cor[r * I.cor_stride] = cr;
       part[0] = c0 * c0;
       part[1] = isfinite(cr) ? 0.f : 1.f;
-      if (k3D) {
-        const int ia = (int)(r % D.na), ib = (int)(r / D.na);
-        I.tabC[r] = ray_tab_c(I.tabA[(long long)view * D.na + ia], G.z_det[ib]);
-      }
     }
   }
   double tot[2];

@@ -414,6 +414,96 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// 2-D TV step over the block's whole group of kTilesPerBlock tiles as one
+// 32 x 32 voxel tile: the source with a two-voxel halo (36 x 36) is staged
+// once, m' is evaluated once on the group plus a one-voxel halo (34 x 34),
+// and each thread then writes and differentiates its four voxels (rows
+// ty, ty+8, ty+16, ty+24 of the group -- the same voxels, in the same order,
+// as the tile-by-tile form, so the results are identical to it).  Per voxel
+// this stages 1.27 source values and evaluates m' 1.13 times, against 1.69
+// and 1.33 for one 32 x 8 tile at a time.
+constexpr int kGroupRows = kTileY * kTilesPerBlock;
+
+__global__ void __launch_bounds__(kThreads)
+    k_tv_step2d(const Inst *__restrict__ insts, int step) {
+  __shared__ float s2[kGroupRows + 4][kTileX + 4];
+  __shared__ float s1[kGroupRows + 2][kTileX + 2];
+  const Inst &I = insts[blockIdx.z];
+  if (inst_done(I)) return;
+  const int ng = I.s->ng;
+  if (step >= ng) return;
+  const Dims D = I.d;
+  const OwnBlock ob = own_block(group_grid(D.nx, D.ny, 1, 1));
+  if (ob.bid < 0) return;
+  const bool last = step == ng - 1;
+  const bool fused_finish = last && ng >= 2;
+  const float coef = I.s->tv_coef_f;
+  const float *src = tv_src(I, step);
+  float *dst = tv_dst(I, step);
+  const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
+  const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kGroupRows;
+  // source with a two-voxel halo, zero outside the image
+  for (int r = ty; r < kGroupRows + 4; r += kTileY) {
+    const int y = y0 - 2 + r;
+    const bool yin = y >= 0 && y < D.ny;
+    for (int c = tx; c < kTileX + 4; c += kTileX) {
+      const int x = x0 - 2 + c;
+      s2[r][c] = (yin && x >= 0 && x < D.nx) ? src[(unsigned)y * D.nx + x] : 0.f;
+    }
+  }
+  __syncthreads();
+  // m' on the group and a one-voxel halo (zero outside the image)
+  for (int r = ty; r < kGroupRows + 2; r += kTileY) {
+    const int y = y0 - 1 + r;
+    for (int c = tx; c < kTileX + 2; c += kTileX) {
+      const int x = x0 - 1 + c;
+      float val = 0.f;
+      if (y >= 0 && y < D.ny && x >= 0 && x < D.nx) {
+        const auto u = [&](int dx, int dy, int) { return s2[r + 1 + dy][c + 1 + dx]; };
+        val = u(0, 0, 0) - coef * tv_grad2<float>(u);
+      }
+      s1[r][c] = val;
+    }
+  }
+  __syncthreads();
+  float v[1] = {0.f};
+  for (int k = 0; k < kTilesPerBlock; k++) {
+    const int r = ty + kTileY * k;
+    const int ix = x0 + tx, iy = y0 + r;
+    if (ix < D.nx && iy < D.ny) {
+      const unsigned i = (unsigned)iy * D.nx + ix;
+      const auto u = [&](int dx, int dy, int) { return s1[r + 1 + dy][tx + 1 + dx]; };
+      const float mn = u(0, 0, 0);
+      if (fused_finish) {
+        const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
+        const float f0 = I.m[i];
+        const float dlt = mc - f0;
+        v[0] += dlt * dlt;
+        I.m[i] = mc;
+        I.m_pre[i] = mc;
+      } else {
+        dst[i] = mn;
+        if (!last) {
+          const float gr = tv_grad2<float>(u);
+          v[0] += gr * gr;
+        }
+      }
+    }
+  }
+  double tot[1];
+  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
+    if (threadIdx.x == 0) {
+      Scalars *s = I.s;
+      if (fused_finish) {
+        finish_scalars(s, tot[0]);
+      } else if (!last) {
+        s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
+        s->tv_coef_f = (float)s->tv_coef;
+      }
+    }
+  }
+}
+
 // End of an iteration for instances whose last TV step did not finish it
 // (ng == 0 or ng == 1): positivity (after a TV step), dg, alpha/beta, k.
 __global__ void __launch_bounds__(kThreads)
@@ -498,7 +588,7 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
   if (d.nz > 1)
     k_tv_step<true><<<grid, kThreads, 0, st>>>(insts, step);
   else
-    k_tv_step<false><<<grid, kThreads, 0, st>>>(insts, step);
+    k_tv_step2d<<<grid, kThreads, 0, st>>>(insts, step);
   return cudaGetLastError();
 }
 

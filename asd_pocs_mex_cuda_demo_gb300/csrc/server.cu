@@ -1,21 +1,25 @@
 // Serving queue: continuous batching of ASD-POCS jobs on one GPU (host code).
 //
-// A worker thread owns every CUDA call.  Jobs wait in a FIFO until the lane
-// of their kind and view-count class has a free slot and the HBM budget has
-// room for their state; admission allocates the job's block of device memory
-// (stream-ordered pool), uploads its data, computes its view tables, resets
-// its scalars and writes its descriptor into the lane's slot -- all on the
-// lane's stream, so it orders after the iterations already queued there.  A
-// lane runs one ASD-POCS iteration of all its slots per launch sequence
-// (dead slots point at scalars with done = 1 and exit at once), captured in
-// a CUDA graph that is re-captured only when a job needs larger grids, more
-// views or more TV steps than the captured one.  After each iteration a tiny
-// kernel gathers the slots' done flags into pinned memory; when the
-// worker sees a job done it enqueues the copies of its results, retires the
-// slot and frees the job's memory, again in stream order.  Because every
-// kernel computes an instance at its own sizes and reduces over its own
-// blocks (see OwnBlock), a job's result does not depend on the other jobs
-// sharing its launches.
+// A worker thread owns every CUDA call.  Jobs are routed to the lane of
+// their scan protocol -- identical sizes, geometry and view angles -- and
+// wait there until a slot is free and the HBM budget has room for their
+// state.  A lane owns the protocol's geometry (detector coordinates, view
+// angles, ray tables, the residuals of its slots interleaved in groups of
+// kShareSlots), computed once, so its backward step computes each chord once
+// per voxel for a whole group of jobs.  Admission allocates the job's state
+// (stream-ordered pool), uploads its data, resets its scalars and writes its
+// descriptor into the lane's slot, all on the lane's stream, so it orders
+// after the iterations already queued there.  A lane runs one ASD-POCS
+// iteration of all its slots per launch sequence (empty slots point at
+// scalars with done = 1 and exit at once), captured in a CUDA graph that is
+// re-captured only when a job needs more TV steps than the captured one.
+// After each iteration a tiny kernel gathers the slots' done flags into
+// pinned memory; when the worker sees a job done it enqueues the copies of
+// its results, empties the slot and frees the job's memory, again in stream
+// order.  Lanes run on their own streams, so different protocols overlap on
+// the device.  Every kernel computes an instance at its own sizes and
+// reduces over its own blocks, so a job's result does not depend on the
+// jobs sharing its launches.
 #include <string.h>
 
 #include <algorithm>
@@ -66,13 +70,16 @@ struct Flight {
 };
 
 struct Lane {
-  int kind = 0, nv_class = 0;
+  asdpocs_geometry g{};            // the protocol
+  std::vector<double> phi;
   cudaStream_t st = nullptr;
   int S = 0;
   Inst *d_inst = nullptr;          // S descriptors
   int *d_flags = nullptr;          // S done flags
   Scalars *d_dead = nullptr;       // scalars of an empty slot (done = 1)
-  Inst dead{};
+  char *geo = nullptr;             // the protocol's geometry block
+  Inst tmpl{};                     // geometry of every slot
+  std::vector<Inst> slot_desc;     // descriptor of each slot (host copy)
   std::vector<Job *> slot_job;
   int active = 0;
   std::deque<Job *> queue;
@@ -82,14 +89,14 @@ struct Lane {
   // captured iteration
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  Dims gd{0, 0, 0, 0, 0};
-  int gnv = 0, gng = 0;
+  int gng = -1;
 };
 
-int nv_class(int nv) {
-  int c = 0;
-  while ((1 << c) < nv) c++;
-  return c;
+// Key of a job's lane: its sizes, geometry and angles, byte for byte.
+std::string protocol_key(const asdpocs_geometry &g, const std::vector<double> &phi) {
+  std::string k((const char *)&g, sizeof g);
+  k.append((const char *)phi.data(), phi.size() * sizeof(double));
+  return k;
 }
 
 }  // namespace
@@ -106,7 +113,7 @@ struct asdpocs_server_s {
   long long next_id = 1;
   std::map<long long, std::unique_ptr<asd::Job>> jobs;
   std::deque<asd::Job *> pending;  // not yet assigned to a lane
-  std::map<int, std::unique_ptr<asd::Lane>> lanes;
+  std::map<std::string, std::unique_ptr<asd::Lane>> lanes;
   cudaMemPool_t pool = nullptr;  // the jobs' device memory
   unsigned long long budget = 0, in_use = 0, peak = 0;
 };
@@ -130,24 +137,43 @@ Dims inst_dims(const asdpocs_geometry &g) {
   return Dims{g.nx, g.ny, g.nz, g.na, g.nb};
 }
 
+// Slot s's descriptor when empty: the protocol's geometry with scalars that
+// say done.  Slot 0 refreshes the shared 3-D ray-slope table every view.
+Inst empty_slot(const Lane &L, int s) {
+  Inst I = L.tmpl;
+  I.s = L.d_dead;
+  const size_t M = (size_t)L.g.na * L.g.nb;
+  I.cor = L.tmpl.cor + (size_t)(s / kShareSlots) * M * kShareSlots + s % kShareSlots;
+  I.cor_stride = kShareSlots;
+  I.tabc_mode = s == 0 ? kTabcShared : kTabcNone;
+  return I;
+}
+
 bool lane_create(asdpocs_server sv, Lane &L) {
   L.S = sv->cfg.slots_per_lane;
+  const size_t M = (size_t)L.g.na * L.g.nb;
+  const int groups = (L.S + kShareSlots - 1) / kShareSlots;
   SV_CUDA(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking));
   SV_CUDA(cudaMalloc(&L.d_inst, sizeof(Inst) * L.S));
   SV_CUDA(cudaMalloc(&L.d_flags, sizeof(int) * L.S));
   SV_CUDA(cudaMalloc(&L.d_dead, sizeof(Scalars)));
+  const InstLayout gl =
+      layout_instance(L.g, 0, (size_t)groups * kShareSlots * M, kLayoutGeometry);
+  SV_CUDA(cudaMalloc(&L.geo, gl.bytes));
+  SV_CUDA(cudaMemsetAsync(L.geo, 0, gl.bytes, L.st));
   Scalars dead_s;
   memset(&dead_s, 0, sizeof dead_s);
   dead_s.done = 1;
   SV_CUDA(cudaMemcpyAsync(L.d_dead, &dead_s, sizeof dead_s, cudaMemcpyHostToDevice,
                           L.st));
-  memset(&L.dead, 0, sizeof L.dead);
-  L.dead.d = Dims{1, 1, 1, 1, 1};
-  L.dead.nv = 0;
-  L.dead.s = L.d_dead;
-  std::vector<Inst> all(L.S, L.dead);
-  SV_CUDA(cudaMemcpyAsync(L.d_inst, all.data(), sizeof(Inst) * L.S,
+  memset(&L.tmpl, 0, sizeof L.tmpl);
+  SV_CUDA(bind_geometry(L.tmpl, L.geo, gl, L.g, L.phi.data(), L.st));
+  L.slot_desc.resize(L.S);
+  for (int s = 0; s < L.S; s++) L.slot_desc[s] = empty_slot(L, s);
+  SV_CUDA(cudaMemcpyAsync(L.d_inst, L.slot_desc.data(), sizeof(Inst) * L.S,
                           cudaMemcpyHostToDevice, L.st));
+  // the protocol's ray tables and view flags, once, through slot 0
+  SV_CUDA(launch_view_tables(L.d_inst, 1, inst_dims(L.g), L.g.nv, L.st));
   L.slot_job.assign(L.S, nullptr);
   return true;
 }
@@ -167,6 +193,7 @@ void lane_destroy(Lane &L) {
   cudaFree(L.d_inst);
   cudaFree(L.d_flags);
   cudaFree(L.d_dead);
+  cudaFree(L.geo);
   if (L.st) cudaStreamDestroy(L.st);
 }
 
@@ -184,8 +211,9 @@ bool harvest(asdpocs_server sv, Lane &L, int s) {
     SV_CUDA(cudaMemcpyAsync(J->rmse, b + J->lay.rmse, (size_t)J->o.maxnumIter * 8,
                             cudaMemcpyDeviceToHost, L.st));
   SV_CUDA(cudaEventRecord(J->ev_done, L.st));
-  SV_CUDA(cudaMemcpyAsync(L.d_inst + s, &L.dead, sizeof(Inst), cudaMemcpyHostToDevice,
-                          L.st));
+  L.slot_desc[s] = empty_slot(L, s);
+  SV_CUDA(cudaMemcpyAsync(L.d_inst + s, &L.slot_desc[s], sizeof(Inst),
+                          cudaMemcpyHostToDevice, L.st));
   SV_CUDA(cudaFreeAsync(J->dev, L.st));
   J->dev = nullptr;
   sv->in_use -= J->lay.bytes;
@@ -205,9 +233,8 @@ bool admit(asdpocs_server sv, Lane &L, int s, Job *J) {
   sv->peak = std::max(sv->peak, sv->in_use);
   char *b = J->dev;
   SV_CUDA(cudaMemsetAsync(b, 0, J->lay.bytes, L.st));
-  Inst I;
-  memset(&I, 0, sizeof I);
-  SV_CUDA(bind_instance(I, b, J->lay, J->g, J->phi.data(), L.st));
+  Inst I = empty_slot(L, s);
+  bind_state(I, b, J->lay);
   // pageable sources are staged before each call returns
   SV_CUDA(cudaMemcpyAsync(b + J->lay.P, J->P.data(), J->P.size() * 4,
                           cudaMemcpyHostToDevice, L.st));
@@ -218,8 +245,9 @@ bool admit(asdpocs_server sv, Lane &L, int s, Job *J) {
     SV_CUDA(cudaMemcpyAsync(b + J->lay.I0, J->I0.data(), J->I0.size() * 4,
                             cudaMemcpyHostToDevice, L.st));
   SV_CUDA(reset_instance(I, initial_scalars(J->o, J->has_ref), L.st));
-  SV_CUDA(cudaMemcpyAsync(L.d_inst + s, &I, sizeof I, cudaMemcpyHostToDevice, L.st));
-  SV_CUDA(launch_view_tables(L.d_inst + s, 1, inst_dims(J->g), J->g.nv, L.st));
+  L.slot_desc[s] = I;
+  SV_CUDA(cudaMemcpyAsync(L.d_inst + s, &L.slot_desc[s], sizeof I,
+                          cudaMemcpyHostToDevice, L.st));
   std::vector<float>().swap(J->P);
   std::vector<float>().swap(J->m0);
   std::vector<float>().swap(J->I0);
@@ -231,37 +259,20 @@ bool admit(asdpocs_server sv, Lane &L, int s, Job *J) {
   return true;
 }
 
-// Grids, views and TV steps the lane's iteration must cover now.
-void lane_needs(const Lane &L, Dims &d, int &nv, int &ng) {
-  d = Dims{0, 0, 0, 0, 0};
-  nv = 0;
-  ng = 0;
-  for (const Job *J : L.slot_job) {
-    if (!J) continue;
-    d.nx = std::max(d.nx, J->g.nx);
-    d.ny = std::max(d.ny, J->g.ny);
-    d.nz = std::max(d.nz, J->g.nz);
-    d.na = std::max(d.na, J->g.na);
-    d.nb = std::max(d.nb, J->g.nb);
-    nv = std::max(nv, J->g.nv);
-    ng = std::max(ng, J->o.numOfgradients);
-  }
-}
-
 bool launch_iteration(asdpocs_server sv, Lane &L) {
-  Dims d;
-  int nv, ng;
-  lane_needs(L, d, nv, ng);
-  const bool fits = L.exec && d.nx <= L.gd.nx && d.ny <= L.gd.ny &&
-                    d.nz <= L.gd.nz && d.na <= L.gd.na && d.nb <= L.gd.nb &&
-                    nv <= L.gnv && ng <= L.gng;
-  if (!fits) {
+  int ng = 0;
+  for (const Job *J : L.slot_job)
+    if (J) ng = std::max(ng, J->o.numOfgradients);
+  if (!L.exec || ng > L.gng) {
+    // capture for the most TV steps seen so far; jobs with fewer skip the rest
+    ng = std::max(ng, L.gng);
     if (L.exec) cudaGraphExecDestroy(L.exec);
     if (L.graph) cudaGraphDestroy(L.graph);
     L.exec = nullptr;
     L.graph = nullptr;
     SV_CUDA(cudaStreamBeginCapture(L.st, cudaStreamCaptureModeThreadLocal));
-    const cudaError_t e = enqueue_iteration(L.d_inst, L.S, d, nv, ng, false, L.st);
+    const cudaError_t e =
+        enqueue_iteration(L.d_inst, L.S, inst_dims(L.g), L.g.nv, ng, true, L.st);
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(L.st, &g);
     if (e != cudaSuccess) {
@@ -271,8 +282,6 @@ bool launch_iteration(asdpocs_server sv, Lane &L) {
     SV_CUDA(e2);
     L.graph = g;
     SV_CUDA(cudaGraphInstantiate(&L.exec, L.graph, 0));
-    L.gd = d;
-    L.gnv = nv;
     L.gng = ng;
   }
   Flight f;
@@ -356,12 +365,12 @@ void worker_main(asdpocs_server sv) {
     while (!sv->pending.empty()) {
       Job *J = sv->pending.front();
       sv->pending.pop_front();
-      const int key = instance_kind(J->g) * 64 + nv_class(J->g.nv);
+      const std::string key = protocol_key(J->g, J->phi);
       auto it = sv->lanes.find(key);
       if (it == sv->lanes.end()) {
         std::unique_ptr<Lane> L(new Lane);
-        L->kind = instance_kind(J->g);
-        L->nv_class = nv_class(J->g.nv);
+        L->g = J->g;
+        L->phi = J->phi;
         if (!lane_create(sv, *L)) {
           ok = false;
           sv->lanes[key] = std::move(L);
@@ -477,7 +486,7 @@ int asdpocs_server_submit(asdpocs_server sv, const asdpocs_geometry *geom,
   if (int e = check_instance(J->g, J->o)) return e;
   const asdpocs_geometry &g = J->g;
   const size_t N = (size_t)g.nx * g.ny * g.nz;
-  J->lay = layout_instance(g, J->o.maxnumIter, (size_t)g.na * g.nb);
+  J->lay = layout_instance(g, J->o.maxnumIter, 0, kLayoutState);
   if (J->lay.bytes > sv->budget)
     return set_error(ASDPOCS_ERR_NOMEM,
                      "job needs %zu bytes, over the server's HBM budget of %llu",

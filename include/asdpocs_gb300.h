@@ -245,15 +245,16 @@ int SART_cuda_inline(const double *P, const double *phi_vec_deg,
  * Serving queue (no counterpart in the reference, whose drivers run one
  * reconstruction at a time).  Jobs of any geometry, view count and
  * iteration budget are submitted at any time.  A worker thread admits them
- * into free slots of device-resident lanes -- one lane per kind (2-D,
- * single-slice, cone beam) and view-count class (views rounded up to a
- * power of two), each on its own CUDA stream -- when the HBM budget has
- * room, runs one ASD-POCS iteration of every job of a lane per launch
- * sequence (a CUDA graph replayed while the lane's membership keeps its
- * shape), retires jobs as they finish and admits waiting ones in their
- * place, so jobs that arrive while others run join them on the device.
- * Each job's result is bit-identical to the same job run alone in a plan.
- * All calls are thread-safe.
+ * into free slots of device-resident lanes -- one lane per scan protocol
+ * (identical sizes, geometry and view angles), each on its own CUDA stream,
+ * its backward step computing each chord once for a group of its jobs --
+ * when the HBM budget has room, runs one ASD-POCS iteration of every job of
+ * a lane per launch sequence (a replayed CUDA graph), retires jobs as they
+ * finish and admits waiting ones in their place, so jobs that arrive while
+ * others run join them on the device.  Each job's result is bit-identical
+ * to the same job run alone in a plan.  The budget counts the jobs' state;
+ * a lane's geometry tables (a few MB) are held until the server is
+ * destroyed.  All calls are thread-safe.
  * --------------------------------------------------------------------- */
 typedef struct asdpocs_server_s *asdpocs_server;
 

@@ -229,3 +229,33 @@ def test_uneven_batch_equals_alone_bitwise(gpu, oracle_mod):
         _, P, para = insts[k]
         mo, _ = oracle_mod.asdpocs(P, para)
         assert rel_l2(alone[k][0], mo) < RECON_TOL, k
+
+
+def test_shared_geometry_cone_beam_instances_finishing_apart(gpu):
+    """Cone-beam instances sharing geometry share one per-view ray-slope
+    table; the instance that refreshes it keeps doing so after its own
+    iterations end, so the others' results still equal their runs alone."""
+    n, na, nb, nv = 20, 40, 30, 9
+    SO, OD, det, vx = 1000.0, 500.0, 10.24, 12.8
+    phi = phantoms.views(nv)
+    x = (phantoms.shepp_logan_3d(n) * 0.02).astype(np.float32)
+    base = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=n, na=na, nb=nb, detsize=det,
+                phi_vec=phi, numOfgradients=3, alpha=0.02)
+    P = np.stack([pkg.Ax_cone_gpu(x, dict(base, phi=-a / 180 * np.pi))[0] for a in phi],
+                 axis=1)
+    paras = [dict(base, maxnumIter=it) for it in (1, 3, 2, 4)]
+    Ps = [phantoms.poisson_noise(P, 5e4, 60 + k) for k in range(len(paras))]
+    alone = []
+    for para, Pk in zip(paras, Ps):
+        with pkg.Plan(para, phi) as pl:
+            pl.set_sinogram(0, Pk.ravel(order="F"))
+            pl.reset()
+            pl.run()
+            alone.append(pl.image(0))
+    with pkg.Plan(paras, [phi] * len(paras)) as pl:
+        for k, Pk in enumerate(Ps):
+            pl.set_sinogram(k, Pk.ravel(order="F"))
+        pl.reset()
+        pl.run()
+        for k in range(len(paras)):
+            assert np.array_equal(pl.image(k), alone[k]), k

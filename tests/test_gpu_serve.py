@@ -13,11 +13,13 @@ from asd_pocs_mex_cuda_demo_gb300 import phantoms
 pytestmark = pytest.mark.gpu
 
 
-def _job2d(seed, n, na, nv, iters, ng):
+def _job2d(seed, n, na, nv, iters, ng, shift=None):
+    """shift: view-angle offset; jobs with equal sizes and offset share a
+    scan protocol (and a lane of the server)."""
     SO, OD, det = 541.0, 408.0, 1.0
     vx = phantoms.fov_voxel_size(SO, OD, det, na, n)
     x = phantoms.random_ellipses(n, seed).astype(np.float32)
-    phi = phantoms.views(nv) + 0.25 * seed
+    phi = phantoms.views(nv) + (0.25 * seed if shift is None else shift)
     para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, na=na, nb=1, detsize=det,
                 phi_vec=phi, maxnumIter=iters, numOfgradients=ng, alpha=0.02)
     P = np.stack([pkg.Ax_cone_gpu(x, dict(para, phi=-a / 180 * np.pi))[0] for a in phi],
@@ -47,12 +49,14 @@ def _alone(x, P, para):
 
 
 def test_server_jobs_equal_alone(gpu):
-    jobs = [_job2d(1, 48, 72, 12, 3, 5), _job2d(2, 64, 96, 20, 4, 10),
+    # jobs 0, 4, 7 and 8 share one protocol, jobs 3 and 9 another (cone beam)
+    jobs = [_job2d(1, 48, 72, 12, 3, 5, shift=1.0), _job2d(2, 64, 96, 20, 4, 10),
             _job2d(3, 40, 60, 9, 2, 0), _job3d(4, 16, 32, 24, 10, 2),
-            _job2d(5, 64, 96, 40, 3, 2), _job2d(6, 33, 50, 7, 5, 1),
-            _job3d(7, 20, 40, 30, 12, 3), _job2d(8, 48, 72, 12, 6, 20)]
+            _job2d(5, 48, 72, 12, 2, 2, shift=1.0), _job2d(6, 33, 50, 7, 5, 1),
+            _job3d(7, 20, 40, 30, 12, 3), _job2d(8, 48, 72, 12, 6, 20, shift=1.0),
+            _job2d(9, 48, 72, 12, 1, 3, shift=1.0), _job3d(4, 16, 32, 24, 10, 4)]
     ref = [_alone(*j) for j in jobs]
-    with pkg.Server(slots_per_lane=3) as srv:
+    with pkg.Server(slots_per_lane=3) as srv:  # a fourth job of a protocol waits
         ids = [srv.submit(para, P, I0=x) for x, P, para in jobs[:3]]
         # later arrivals join while the first ones run
         deadline = time.time() + 30
