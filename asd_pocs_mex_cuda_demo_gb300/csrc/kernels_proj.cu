@@ -42,7 +42,7 @@ __device__ __forceinline__ void ax_warp(const ViewGeo &G, const Dims &D,
   ys = 0.f;
   ss = 0.f;
   if (D.nz == 1 && zd == 0.0f)
-    ray_columns_planar_fast(R, lane, 32, ld, ys, ss);
+    ray_columns_planar_fast<2>(R, lane, 32, ld, ys, ss);
   else
     ray_columns_fast<2>(R, lane, 32, ld, ys, ss);
   ys = warp_sum(ys);
@@ -393,24 +393,45 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
           kPlanar ? (kA > 0 ? 1 : 0) : __reduce_max_sync(0xffffffffu, cntB);
       const float rx = rx0 - (has ? w.xc : 0.f), ry = ry0 - (has ? w.yc : 0.f);
       const float rz = 0.0f - (has ? w.zc : 0.f);
-      for (int kb = 0; kb < kB; kb++) {
-        const bool onb = kb < cntB;
-        const int ib = blo + kb;
-        const float c = kPlanar ? 0.0f : (onb ? __ldg(G.z_det + ib) : 1.0f) - 0.0f;
-        const int row = onb ? ib * D.na : 0;
-        for (int ka = 0; ka < kA; ka++) {
-          const bool on = onb && ka < cntA;
-          const int ia = on ? lo + ka : 0;
+      if (kPlanar) {
+        for (int kb = 0; kb < kB; kb++) {
+          const bool onb = kb < cntB;
+          for (int ka = 0; ka < kA; ka++) {
+            const bool on = onb && ka < cntA;
+            const int ia = on ? lo + ka : 0;
+            const float4 A = __ldg(tabA + ia);
+            const float yv = on ? __ldg(cor + ia) : 0.f;
+            const float l = chord_sel<AX>(A, rx, ry, G.dz);
+            if (on) {
+              acc += l * yv;
+              accl += l;
+            }
+          }
+        }
+      } else {
+        // the voxel's (row, column) pairs as one sequence (rows outer, the
+        // reference's order), so a warp walks its longest sequence rather
+        // than its widest row times its tallest column
+        const int cnt = cntA * cntB;
+        const int kN = __reduce_max_sync(0xffffffffu, cnt);
+        int ka = 0, ib = blo;
+        for (int k = 0; k < kN; k++) {
+          const bool on = k < cnt;
+          const int ia = on ? lo + ka : 0, ibs = on ? ib : 0;
+          const int r = ibs * D.na + ia;
+          const float c = __ldg(G.z_det + ibs) - 0.0f;
           const float4 A = __ldg(tabA + ia);
-          const float yv = on ? __ldg(cor + row + ia) : 0.f;
-          float l;
-          if (kPlanar)
-            l = chord_sel<AX>(A, rx, ry, G.dz);
-          else
-            l = chord3_bf(A, __ldg(tabC + row + ia), c, rx, ry, rz, G.dz);
+          const float4 Cs = __ldg(tabC + r);
+          const float yv = on ? __ldg(cor + r) : 0.f;
+          const float l = AX == 0 ? chord3_bf(A, Cs, c, rx, ry, rz, G.dz)
+                                  : chord3_axis<AX == 1>(A, Cs, rx, ry, rz, G.dz);
           if (on) {
             acc += l * yv;
             accl += l;
+          }
+          if (++ka == cntA) {
+            ka = 0;
+            ib++;
           }
         }
       }
@@ -429,10 +450,10 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
 // Reads the view's ray tables and residuals through the L1 cache, so no
 // block-wide staging or barrier is needed; each lane walks its voxel's shadow
 // (or, when the view does not allow narrowing, the reference's window) in
-// warp-uniform steps, pairs accumulated in the reference's order.  In the
-// planar geometry a view whose rays share one dominant axis and include no
-// axis-parallel ray (the instance's view flags; a block-uniform branch) uses
-// the axis-specialised chord.
+// warp-uniform steps, pairs accumulated in the reference's order.  A view
+// whose rays share one dominant in-plane axis and include no axis-parallel
+// ray (the instance's view flags; a block-uniform branch) uses the
+// axis-specialised chord.
 template <bool kPlanar>
 __global__ void __launch_bounds__(kAtxThreads, 4)
     k_sart_atx(const Inst *__restrict__ insts, int view) {
@@ -445,16 +466,12 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
   const int vf = I.vflags[view];
   const bool narrow = !(vf & kViewAxisParallel) && I.s->cor_finite &&
                       (!kPlanar || G.z_det[0] == 0.0f);
-  if constexpr (kPlanar) {
-    if (!(vf & (kViewAxisParallel | kViewNotX)))
-      sart_atx_tiles<true, 1>(I, G, D, tabA, narrow);
-    else if (!(vf & (kViewAxisParallel | kViewNotY)))
-      sart_atx_tiles<true, 2>(I, G, D, tabA, narrow);
-    else
-      sart_atx_tiles<true, 0>(I, G, D, tabA, narrow);
-  } else {
-    sart_atx_tiles<false, 0>(I, G, D, tabA, narrow);
-  }
+  if (!(vf & (kViewAxisParallel | kViewNotX)))
+    sart_atx_tiles<kPlanar, 1>(I, G, D, tabA, narrow);
+  else if (!(vf & (kViewAxisParallel | kViewNotY)))
+    sart_atx_tiles<kPlanar, 2>(I, G, D, tabA, narrow);
+  else
+    sart_atx_tiles<kPlanar, 0>(I, G, D, tabA, narrow);
 }
 
 // ---------------------------------------------------------------------------
@@ -503,6 +520,7 @@ __device__ __forceinline__ void atx_shared_voxel(
           const long long r = (long long)ib * D.na + ia;
 #pragma unroll
           for (int q = 0; q < kShareGroup / 4; q++) {
+            if (!((active >> (4 * q)) & 0xFu)) continue;
             const float4 c4 = __ldg(corg + r * (kShareGroup / 4) + q);
             acc[4 * q] += l * c4.x;
             acc[4 * q + 1] += l * c4.y;
@@ -552,9 +570,12 @@ __device__ __forceinline__ void atx_shared_voxel(
           l[j] = 0.f;
           if (ka < kA) {  // warp-uniform
             const float4 A = __ldg(tabA + ia);
-            l[j] = kPlanar ? chord_sel<AX>(A, rx, ry, G.dz)
-                           : chord3_bf(A, __ldg(tabC + row + ia), c, rx, ry, rz,
-                                       G.dz);
+            if (kPlanar)
+              l[j] = chord_sel<AX>(A, rx, ry, G.dz);
+            else if (AX == 0)
+              l[j] = chord3_bf(A, __ldg(tabC + row + ia), c, rx, ry, rz, G.dz);
+            else
+              l[j] = chord3_axis<AX == 1>(A, __ldg(tabC + row + ia), rx, ry, rz, G.dz);
           }
           if (on[j]) accl += l[j];
         }
@@ -563,6 +584,9 @@ __device__ __forceinline__ void atx_shared_voxel(
           if (on[j]) {
 #pragma unroll
             for (int q = 0; q < kShareGroup / 4; q++) {
+              // quads of the group with no running instance are skipped
+              // (block-uniform); their accumulators are never read
+              if (!((active >> (4 * q)) & 0xFu)) continue;
               const float4 c4 = __ldg(corg + (long long)idx[j] * (kShareGroup / 4) + q);
               acc[4 * q] += l[j] * c4.x;
               acc[4 * q + 1] += l[j] * c4.y;
@@ -589,7 +613,7 @@ __device__ __forceinline__ void atx_shared_voxel(
 }
 
 template <bool kPlanar>
-__global__ void __launch_bounds__(kAtxThreads, 2)
+__global__ void __launch_bounds__(kAtxThreads, 3)
     k_sart_atx_shared(const Inst *__restrict__ insts, int batch, int view) {
   __shared__ float *s_m[kShareGroup];
   __shared__ float s_beta[kShareGroup];
@@ -625,20 +649,15 @@ __global__ void __launch_bounds__(kAtxThreads, 2)
   const int vf = I0.vflags[view];
   const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
   const bool narrow = planar_ok && !(vf & kViewAxisParallel) && s_finite;
-  if constexpr (kPlanar) {
-    if (!(vf & (kViewAxisParallel | kViewNotX)))
-      atx_shared_voxel<true, 1>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
-                                gn, s_m, s_beta);
-    else if (!(vf & (kViewAxisParallel | kViewNotY)))
-      atx_shared_voxel<true, 2>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
-                                gn, s_m, s_beta);
-    else
-      atx_shared_voxel<true, 0>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
-                                gn, s_m, s_beta);
-  } else {
-    atx_shared_voxel<false, 0>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
-                               gn, s_m, s_beta);
-  }
+  if (!(vf & (kViewAxisParallel | kViewNotX)))
+    atx_shared_voxel<kPlanar, 1>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
+                                 gn, s_m, s_beta);
+  else if (!(vf & (kViewAxisParallel | kViewNotY)))
+    atx_shared_voxel<kPlanar, 2>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
+                                 gn, s_m, s_beta);
+  else
+    atx_shared_voxel<kPlanar, 0>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
+                                 gn, s_m, s_beta);
 }
 
 }  // namespace

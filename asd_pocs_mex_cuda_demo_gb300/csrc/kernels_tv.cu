@@ -442,21 +442,28 @@ __global__ void __launch_bounds__(kThreads)
   float *dst = tv_dst(I, step);
   const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
   const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kGroupRows;
-  // source with a two-voxel halo, zero outside the image
-  for (int r = ty; r < kGroupRows + 4; r += kTileY) {
-    const int y = y0 - 2 + r;
-    const bool yin = y >= 0 && y < D.ny;
-    for (int c = tx; c < kTileX + 4; c += kTileX) {
-      const int x = x0 - 2 + c;
-      s2[r][c] = (yin && x >= 0 && x < D.nx) ? src[(unsigned)y * D.nx + x] : 0.f;
-    }
+  // Source with a two-voxel halo, zero outside the image.  The points are
+  // dealt to the threads in fixed-count unrolled rounds, so each thread has
+  // its loads (and below, its stencils) in flight together.
+  constexpr int W2 = kTileX + 4, N2 = W2 * (kGroupRows + 4);
+#pragma unroll
+  for (int j = 0; j < (N2 + kThreads - 1) / kThreads; j++) {
+    const int k = threadIdx.x + j * kThreads;
+    const int r = k / W2, c = k - r * W2;
+    const int y = y0 - 2 + r, x = x0 - 2 + c;
+    if (k < N2)
+      s2[r][c] = (y >= 0 && y < D.ny && x >= 0 && x < D.nx)
+                     ? src[(unsigned)y * D.nx + x] : 0.f;
   }
   __syncthreads();
   // m' on the group and a one-voxel halo (zero outside the image)
-  for (int r = ty; r < kGroupRows + 2; r += kTileY) {
-    const int y = y0 - 1 + r;
-    for (int c = tx; c < kTileX + 2; c += kTileX) {
-      const int x = x0 - 1 + c;
+  constexpr int W1 = kTileX + 2, N1 = W1 * (kGroupRows + 2);
+#pragma unroll
+  for (int j = 0; j < (N1 + kThreads - 1) / kThreads; j++) {
+    const int k = threadIdx.x + j * kThreads;
+    const int r = k / W1, c = k - r * W1;
+    const int y = y0 - 1 + r, x = x0 - 1 + c;
+    if (k < N1) {
       float val = 0.f;
       if (y >= 0 && y < D.ny && x >= 0 && x < D.nx) {
         const auto u = [&](int dx, int dy, int) { return s2[r + 1 + dy][c + 1 + dx]; };
@@ -467,6 +474,7 @@ __global__ void __launch_bounds__(kThreads)
   }
   __syncthreads();
   float v[1] = {0.f};
+#pragma unroll
   for (int k = 0; k < kTilesPerBlock; k++) {
     const int r = ty + kTileY * k;
     const int ix = x0 + tx, iy = y0 + r;

@@ -910,4 +910,46 @@ ASD_HD float chord3_bf(const float4 A, const float4 Cs, float c, float rx,
   return sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
 }
 
+// chord3_bf for a ray known to have a != 0, b != 0 and the given dominant
+// in-plane axis (XF: |a| > |b|): the same expressions, face order fixed.
+template <bool XF>
+ASD_HD float chord3_axis(const float4 A, const float4 Cs, float rx, float ry,
+                         float rz, float dz) {
+  const float hz = dz / 2.0f;
+  const float xt0 = A.z * (-rx) + ry, xu0 = A.z * 0.5f;
+  const float xt1 = Cs.x * (-rx) + rz, xu1 = Cs.x * 0.5f;
+  const float xmy = xt0 - xu0, xmz = xt1 - xu1, xpy = xt0 + xu0, xpz = xt1 + xu1;
+  const bool fxm = fabsf(xmy) <= 0.5f && fabsf(xmz) <= hz;
+  const bool fxp = fabsf(xpy) <= 0.5f && fabsf(xpz) <= hz;
+  const float yt0 = A.w * (-ry) + rx, yu0 = A.w * 0.5f;
+  const float yt1 = Cs.y * (-ry) + rz, yu1 = Cs.y * 0.5f;
+  const float ymx = yt0 - yu0, ymz = yt1 - yu1, ypx = yt0 + yu0, ypz = yt1 + yu1;
+  const bool fym = fabsf(ymx) <= 0.5f && fabsf(ymz) <= hz;
+  const bool fyp = fabsf(ypx) <= 0.5f && fabsf(ypz) <= hz;
+  const float zt0 = Cs.z * (-rz) + rx, zu0 = Cs.z * hz;
+  const float zt1 = Cs.w * (-rz) + ry, zu1 = Cs.w * hz;
+  const float zmx = zt0 - zu0, zmy = zt1 - zu1, zpx = zt0 + zu0, zpy = zt1 + zu1;
+  const bool fzm = fabsf(zmx) <= 0.5f && fabsf(zmy) <= 0.5f;
+  const bool fzp = fabsf(zpx) <= 0.5f && fabsf(zpy) <= 0.5f;
+  Pick2 p;
+  p.n = 0;
+  p.p0x = p.p0y = p.p0z = p.p1x = p.p1y = p.p1z = 0.f;
+  if (XF) {
+    p.take(fxm, -0.5f, xmy, xmz);
+    p.take(fxp, 0.5f, xpy, xpz);
+    p.take(fym, ymx, -0.5f, ymz);
+    p.take(fyp, ypx, 0.5f, ypz);
+  } else {
+    p.take(fym, ymx, -0.5f, ymz);
+    p.take(fyp, ypx, 0.5f, ypz);
+    p.take(fxm, -0.5f, xmy, xmz);
+    p.take(fxp, 0.5f, xpy, xpz);
+  }
+  p.take(fzm, zmx, zmy, -hz);
+  p.take(fzp, zpx, zpy, hz);
+  if (p.n < 2) return 0.0f;
+  const float e0 = p.p1x - p.p0x, e1 = p.p1y - p.p0y, e2 = p.p1z - p.p0z;
+  return sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
+}
+
 }  // namespace asd

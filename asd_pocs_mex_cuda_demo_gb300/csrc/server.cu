@@ -56,11 +56,14 @@ struct Job {
   InstLayout lay{};
   char *dev = nullptr;
   int slot = -1;
-  // results (pinned host memory, filled by stream-ordered copies)
+  // results (one pinned block from the server's pool, filled by
+  // stream-ordered copies): image, then RMSE, then the scalars
+  void *pin = nullptr;
+  size_t pin_cls = 0;
   float *img = nullptr;
   double *rmse = nullptr;
   Scalars *scal = nullptr;
-  cudaEvent_t ev_done = nullptr;
+  cudaEvent_t ev_done = nullptr;  // upload done, later results ready
 };
 
 struct Flight {
@@ -89,7 +92,7 @@ struct Lane {
   // captured iteration
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  int gng = -1;
+  int gng = -1, gbatch = 0;  // TV steps and slots the graph covers
 };
 
 // Key of a job's lane: its sizes, geometry and angles, byte for byte.
@@ -98,6 +101,36 @@ std::string protocol_key(const asdpocs_geometry &g, const std::vector<double> &p
   k.append((const char *)phi.data(), phi.size() * sizeof(double));
   return k;
 }
+
+// Pinned host blocks by power-of-two size class.  Blocks are allocated when
+// a class runs dry and kept until the server is destroyed: page-locking and
+// releasing host memory can stall every stream of the device, so neither
+// happens while jobs run once the pool has warmed up.
+struct PinnedPool {
+  std::map<size_t, std::vector<void *>> spare;
+  std::vector<void *> all;
+  cudaError_t get(size_t bytes, void *&p, size_t &cls) {
+    cls = 4096;
+    while (cls < bytes) cls <<= 1;
+    std::vector<void *> &v = spare[cls];
+    if (!v.empty()) {
+      p = v.back();
+      v.pop_back();
+      return cudaSuccess;
+    }
+    const cudaError_t e = cudaMallocHost(&p, cls);
+    if (e == cudaSuccess) all.push_back(p);
+    return e;
+  }
+  void put(void *p, size_t cls) {
+    if (p) spare[cls].push_back(p);
+  }
+  void release() {
+    for (void *p : all) cudaFreeHost(p);
+    all.clear();
+    spare.clear();
+  }
+};
 
 }  // namespace
 }  // namespace asd
@@ -115,6 +148,8 @@ struct asdpocs_server_s {
   std::deque<asd::Job *> pending;  // not yet assigned to a lane
   std::map<std::string, std::unique_ptr<asd::Lane>> lanes;
   cudaMemPool_t pool = nullptr;  // the jobs' device memory
+  cudaStream_t upload = nullptr; // admissions: allocation and data upload
+  asd::PinnedPool pinned;        // the jobs' result blocks
   unsigned long long budget = 0, in_use = 0, peak = 0;
 };
 
@@ -224,27 +259,36 @@ bool harvest(asdpocs_server sv, Lane &L, int s) {
 }
 
 bool admit(asdpocs_server sv, Lane &L, int s, Job *J) {
-  SV_CUDA(cudaMallocHost(&J->img, (size_t)J->g.nx * J->g.ny * J->g.nz * 4));
-  SV_CUDA(cudaMallocHost(&J->rmse, (size_t)std::max(J->o.maxnumIter, 1) * 8));
-  SV_CUDA(cudaMallocHost(&J->scal, sizeof(Scalars)));
+  const size_t N = (size_t)J->g.nx * J->g.ny * J->g.nz;
+  const size_t o_rmse = (N * 4 + 15) & ~(size_t)15;
+  const size_t o_scal = o_rmse + (size_t)std::max(J->o.maxnumIter, 1) * 8;
+  SV_CUDA(sv->pinned.get(o_scal + sizeof(Scalars), J->pin, J->pin_cls));
+  J->img = (float *)J->pin;
+  J->rmse = (double *)((char *)J->pin + o_rmse);
+  J->scal = (Scalars *)((char *)J->pin + o_scal);
   SV_CUDA(cudaEventCreateWithFlags(&J->ev_done, cudaEventDisableTiming));
-  SV_CUDA(cudaMallocFromPoolAsync((void **)&J->dev, J->lay.bytes, sv->pool, L.st));
+  // Allocation, upload and start state on the upload stream, which holds no
+  // iterations: the pageable copies are staged and return at once instead of
+  // waiting behind the lane's queued work.  The lane's stream then waits for
+  // them before the slot's descriptor changes.
+  SV_CUDA(cudaMallocFromPoolAsync((void **)&J->dev, J->lay.bytes, sv->pool, sv->upload));
   sv->in_use += J->lay.bytes;
   sv->peak = std::max(sv->peak, sv->in_use);
   char *b = J->dev;
-  SV_CUDA(cudaMemsetAsync(b, 0, J->lay.bytes, L.st));
+  SV_CUDA(cudaMemsetAsync(b, 0, J->lay.bytes, sv->upload));
   Inst I = empty_slot(L, s);
   bind_state(I, b, J->lay);
-  // pageable sources are staged before each call returns
   SV_CUDA(cudaMemcpyAsync(b + J->lay.P, J->P.data(), J->P.size() * 4,
-                          cudaMemcpyHostToDevice, L.st));
+                          cudaMemcpyHostToDevice, sv->upload));
   if (J->has_m0)
     SV_CUDA(cudaMemcpyAsync(b + J->lay.m_k1, J->m0.data(), J->m0.size() * 4,
-                            cudaMemcpyHostToDevice, L.st));
+                            cudaMemcpyHostToDevice, sv->upload));
   if (J->has_ref)
     SV_CUDA(cudaMemcpyAsync(b + J->lay.I0, J->I0.data(), J->I0.size() * 4,
-                            cudaMemcpyHostToDevice, L.st));
-  SV_CUDA(reset_instance(I, initial_scalars(J->o, J->has_ref), L.st));
+                            cudaMemcpyHostToDevice, sv->upload));
+  SV_CUDA(reset_instance(I, initial_scalars(J->o, J->has_ref), sv->upload));
+  SV_CUDA(cudaEventRecord(J->ev_done, sv->upload));
+  SV_CUDA(cudaStreamWaitEvent(L.st, J->ev_done, 0));
   L.slot_desc[s] = I;
   SV_CUDA(cudaMemcpyAsync(L.d_inst + s, &L.slot_desc[s], sizeof I,
                           cudaMemcpyHostToDevice, L.st));
@@ -260,19 +304,25 @@ bool admit(asdpocs_server sv, Lane &L, int s, Job *J) {
 }
 
 bool launch_iteration(asdpocs_server sv, Lane &L) {
-  int ng = 0;
-  for (const Job *J : L.slot_job)
-    if (J) ng = std::max(ng, J->o.numOfgradients);
-  if (!L.exec || ng > L.gng) {
-    // capture for the most TV steps seen so far; jobs with fewer skip the rest
+  int ng = 0, hw = 0;  // TV steps needed; slots up to the last occupied one
+  for (int s = 0; s < L.S; s++)
+    if (const Job *J = L.slot_job[s]) {
+      ng = std::max(ng, J->o.numOfgradients);
+      hw = s + 1;
+    }
+  if (!L.exec || ng > L.gng || hw > L.gbatch) {
+    // capture for the most TV steps and slots seen so far (jobs with fewer
+    // steps skip the rest; empty slots exit at once); admission fills the
+    // lowest free slot, so the occupied ones stay packed
     ng = std::max(ng, L.gng);
+    const int batch = std::min(L.S, std::max((hw + 3) & ~3, L.gbatch));
     if (L.exec) cudaGraphExecDestroy(L.exec);
     if (L.graph) cudaGraphDestroy(L.graph);
     L.exec = nullptr;
     L.graph = nullptr;
     SV_CUDA(cudaStreamBeginCapture(L.st, cudaStreamCaptureModeThreadLocal));
     const cudaError_t e =
-        enqueue_iteration(L.d_inst, L.S, inst_dims(L.g), L.g.nv, ng, true, L.st);
+        enqueue_iteration(L.d_inst, batch, inst_dims(L.g), L.g.nv, ng, true, L.st);
     cudaGraph_t g = nullptr;
     const cudaError_t e2 = cudaStreamEndCapture(L.st, &g);
     if (e != cudaSuccess) {
@@ -283,6 +333,7 @@ bool launch_iteration(asdpocs_server sv, Lane &L) {
     L.graph = g;
     SV_CUDA(cudaGraphInstantiate(&L.exec, L.graph, 0));
     L.gng = ng;
+    L.gbatch = batch;
   }
   Flight f;
   if (!L.spare.empty()) {
@@ -405,11 +456,10 @@ void worker_main(asdpocs_server sv) {
   }
 }
 
-void release_job(Job *J) {
-  if (J->img) cudaFreeHost(J->img);
-  if (J->rmse) cudaFreeHost(J->rmse);
-  if (J->scal) cudaFreeHost(J->scal);
+void release_job(asdpocs_server sv, Job *J) {
+  sv->pinned.put(J->pin, J->pin_cls);
   if (J->ev_done) cudaEventDestroy(J->ev_done);
+  J->pin = nullptr;
   J->img = nullptr;
   J->rmse = nullptr;
   J->scal = nullptr;
@@ -459,10 +509,11 @@ int asdpocs_server_create(asdpocs_server *out, const asdpocs_server_config *cfg)
     unsigned long long keep = sv->budget;
     e = cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
   }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->upload, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     if (sv->pool) cudaMemPoolDestroy(sv->pool);
     delete sv;
-    return cuda_status(e, "cudaMemPoolCreate");
+    return cuda_status(e, "server setup");
   }
   sv->worker = std::thread(worker_main, sv);
   *out = sv;
@@ -558,7 +609,7 @@ int asdpocs_server_wait(asdpocs_server sv, long long job, float *m_res,
       t->total_ms = ms_between(J->t_submit, J->t_done);
     }
   }
-  release_job(J);
+  release_job(sv, J);
   sv->jobs.erase(it);
   return rc;
 }
@@ -593,8 +644,10 @@ int asdpocs_server_destroy(asdpocs_server sv) {
       cudaFreeAsync(kv.second->dev, L != sv->lanes.end() ? L->second->st : 0);
     }
   for (auto &kv : sv->lanes) lane_destroy(*kv.second);
-  for (auto &kv : sv->jobs) release_job(kv.second.get());
+  for (auto &kv : sv->jobs) release_job(sv, kv.second.get());
   cudaDeviceSynchronize();
+  sv->pinned.release();
+  if (sv->upload) cudaStreamDestroy(sv->upload);
   if (sv->pool) cudaMemPoolDestroy(sv->pool);
   delete sv;
   return 0;
