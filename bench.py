@@ -570,34 +570,18 @@ def serve_jobs(W, seed, device):
     return jobs
 
 
-def serve_main(args, W, rank, world, pg):
-    """Served throughput and latency of a seeded Poisson job stream, against
-    the same jobs run one at a time (plain, one-instance plans)."""
-    import torch
-
-    import asd_pocs_mex_cuda_demo_gb300 as pkg
-
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    dev = torch.device("cuda", torch.cuda.current_device())
-    pkg.load()
-    jobs = serve_jobs(W, seed=31 + rank, device=dev)
-    # warm-up: one job of each kind through a server (graph captures, pools)
-    with pkg.Server() as srv:
-        for kind in ("2d", "3d"):
-            j = next((j for j in jobs if j["kind"] == kind), None)
-            if j is not None:
-                srv.wait(srv.submit(dict(j["para"], maxnumIter=1), j["P"]))
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+def serve_stream(pkg, jobs, rate_scale):
+    """Submit the job stream at its seeded arrival times (scaled by
+    1/rate_scale) from a feeder thread; returns (results, makespan s, peak
+    device bytes)."""
     results = [None] * len(jobs)
-    barrier(pg)
-    clocks.start()
     with pkg.Server(slots_per_lane=32) as srv:
         ids = [None] * len(jobs)
         t0 = time.perf_counter()
 
         def feeder():
             for k, j in enumerate(jobs):
-                dt = t0 + j["t"] - time.perf_counter()
+                dt = t0 + j["t"] / rate_scale - time.perf_counter()
                 if dt > 0:
                     time.sleep(dt)
                 ids[k] = srv.submit(j["para"], j["P"], I0=j["x"])
@@ -610,15 +594,35 @@ def serve_main(args, W, rank, world, pg):
             results[k] = srv.wait(ids[k])
         t_end = time.perf_counter()
         th.join()
-        mem_peak = srv.memory()[1]
-    clk = clocks.stop()
-    makespan = allmax(pg, t_end - t0)
+        peak = srv.memory()[1]
+    return results, t_end - t0, peak
+
+
+def latency_summary(results):
     lat = np.array([r[2]["total_ms"] for r in results])
-    served = len(jobs) * world / makespan
+    return {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+            "max": float(lat.max()),
+            "queued_p50": float(np.percentile([r[2]["queued_ms"] for r in results], 50))}
+
+
+def serve_main(args, W, rank, world, pg):
+    """Served throughput and latency of a seeded Poisson job stream, against
+    the same jobs run one at a time (plain, one-instance plans).  The stream
+    runs twice: at its specified rate (20 jobs/s, beyond what one GPU can
+    finish: throughput = capacity, latency grows with the backlog) and at 70%
+    of the throughput measured there (latency at a sustainable load)."""
+    import torch
+
+    import asd_pocs_mex_cuda_demo_gb300 as pkg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    pkg.load()
+    jobs = serve_jobs(W, seed=31 + rank, device=dev)
     # plain: the same jobs one at a time, each in its own one-instance plan
-    plain_s, equal = 0.0, True
+    plain_s, plain_img = 0.0, []
     stream = torch.cuda.Stream(device=dev)
-    for k, j in enumerate(jobs):
+    for j in jobs:
         with pkg.Plan(j["para"], j["para"]["phi_vec"], stream=stream.cuda_stream) as pl:
             pl.set_sinogram(0, j["P"])
             pl.set_reference(0, j["x"])
@@ -630,12 +634,28 @@ def serve_main(args, W, rank, world, pg):
             e1.record(stream)
             e1.synchronize()
             plain_s += e0.elapsed_time(e1) / 1e3
-            equal = equal and bool(np.array_equal(pl.image(0), results[k][0]))
-    rm = [float(r[1]["RMSE"][-1]) for r in results]
+            plain_img.append(pl.image(0))
+    # warm-up: one job of each kind through a server (graph captures, pools)
+    with pkg.Server() as srv:
+        for kind in ("2d", "3d"):
+            j = next((j for j in jobs if j["kind"] == kind), None)
+            if j is not None:
+                srv.wait(srv.submit(dict(j["para"], maxnumIter=1), j["P"]))
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    barrier(pg)
+    clocks.start()
+    res_a, span_a, peak_a = serve_stream(pkg, jobs, 1.0)
+    served = len(jobs) * world / allmax(pg, span_a)
+    scale = 0.7 * (len(jobs) / span_a) / W["rate"]
+    res_b, span_b, peak_b = serve_stream(pkg, jobs, scale)
+    clk = clocks.stop()
+    equal = all(np.array_equal(plain_img[k], res_a[k][0]) and
+                np.array_equal(plain_img[k], res_b[k][0]) for k in range(len(jobs)))
+    rm = [float(r[1]["RMSE"][-1]) for r in res_a]
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": served, "unit": "recons/s", "n_gpus": world,
-            "steps": 1, "warmup": 1, "ms_per_step": makespan * 1e3,
+            "steps": 1, "warmup": 1, "ms_per_step": span_a * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded phantoms, Poisson noise, Poisson "
                                     "arrivals)",
@@ -645,16 +665,17 @@ def serve_main(args, W, rank, world, pg):
                        "parallelism": f"replicas x{world}",
                        "timing": "host wall clock from the first arrival to the last "
                                  "result; results copied to host memory"},
-            "latency_ms": {"p50": float(np.percentile(lat, 50)),
-                           "p99": float(np.percentile(lat, 99)),
-                           "max": float(lat.max()),
-                           "queued_p50": float(np.percentile(
-                               [r[2]["queued_ms"] for r in results], 50))},
+            "latency_ms": dict(latency_summary(res_b),
+                               rate_per_s=W["rate"] * scale,
+                               note="stream replayed at 70% of the served throughput"),
+            "overload": dict(latency_summary(res_a), rate_per_s=W["rate"],
+                             note="the specified 20 jobs/s exceed one GPU's throughput: "
+                                  "latency grows with the backlog"),
             "plain": {"recons_per_s": len(jobs) / plain_s, "seconds": plain_s,
                       "served_speedup": served / world / (len(jobs) / plain_s),
                       "served_equals_plain_bitwise": equal},
             "rmse_vs_phantom": {"mean": float(np.mean(rm)), "max": float(np.max(rm))},
-            "hbm_peak_bytes": int(mem_peak),
+            "hbm_peak_bytes": int(max(peak_a, peak_b)),
             "clocks": clk,
         }))
     return 0
