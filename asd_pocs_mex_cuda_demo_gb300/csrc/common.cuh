@@ -85,6 +85,10 @@ struct Inst {
   float *cor;                // correction of the current view: element r at
   int cor_stride;            //   cor[r * cor_stride] (1, or kShareSlots when
                              //   a shared-geometry group interleaves them)
+  float *m_il;               // shared-geometry groups: the group's images
+                             //   during the SART sweep, voxel-major, slot
+                             //   minor (m_il[v * kShareSlots + slot]); the
+                             //   group's base, or nullptr
   float4 *tabA;              // ray slopes of every view, nv*na (ray_tab_a)
   int *vflags;               // per view: kViewAxisParallel | kViewNotX | kViewNotY
   float4 *tabC;              // 3D ray slopes of the current view, na*nb

@@ -413,7 +413,7 @@ int check_instance(const asdpocs_geometry &g, const asdpocs_options &o) {
 }
 
 InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
-                           size_t cor_floats, int parts) {
+                           size_t cor_floats, int parts, size_t il_floats) {
   const Dims d{g.nx, g.ny, g.nz, g.na, g.nb};
   const size_t N = (size_t)g.nx * g.ny * g.nz;
   const size_t M = (size_t)g.na * g.nb;
@@ -436,6 +436,7 @@ InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
   o.cnt = off; off += st ? 256 : 0;
   o.scal = off; off += st ? align256(sizeof(Scalars)) : 0;
   o.cor = off; off += geo ? align256(cor_floats * 4) : 0;
+  o.m_il = off; off += geo ? align256(il_floats * 4) : 0;
   o.tabA = off; off += geo ? align256((size_t)g.na * g.nv * 16) : 0;
   o.vflags = off; off += geo ? align256((size_t)g.nv * 4) : 0;
   o.tabC = off; off += geo ? align256(proj3d ? M * 16 : 16) : 0;
@@ -476,6 +477,7 @@ cudaError_t bind_geometry(Inst &I, char *b, const InstLayout &o,
   I.trig = (const float2 *)(b + o.trig);
   I.cor = (float *)(b + o.cor);
   I.cor_stride = 1;
+  I.m_il = nullptr;
   I.tabA = (float4 *)(b + o.tabA);
   I.vflags = (int *)(b + o.vflags);
   I.tabC = (float4 *)(b + o.tabC);
@@ -538,12 +540,15 @@ namespace asd {
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st) {
   cudaError_t e = cudaSuccess;
+  if (shared) e = launch_group_pack(d_inst, batch, d, 0, st);
   for (int v = 0; v < nv && e == cudaSuccess; v++) {
-    e = launch_sart_ax(d_inst, batch, d, v, st);
+    e = shared ? launch_sart_ax_shared(d_inst, batch, d, v, st)
+               : launch_sart_ax(d_inst, batch, d, v, st);
     if (e == cudaSuccess)
       e = shared ? launch_sart_atx_shared(d_inst, batch, d, v, st)
                  : launch_sart_atx(d_inst, batch, d, v, st);
   }
+  if (shared && e == cudaSuccess) e = launch_group_pack(d_inst, batch, d, 1, st);
   if (e == cudaSuccess) e = launch_after_sweep(d_inst, batch, d, st);
   for (int s = 0; s < ng && e == cudaSuccess; s++)
     e = launch_tv_step(d_inst, batch, d, s, ng, st);
@@ -638,8 +643,10 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     const size_t M = (size_t)geom[i].na * geom[i].nb;
     // shared-geometry groups interleave their residuals in the buffer of
     // the group's first instance (kShareSlots values per ray)
-    lay[i] = layout_instance(geom[i], p->opt[i].maxnumIter,
-                             (p->shared && i % kShareSlots == 0) ? M * kShareSlots : M);
+    const bool first = p->shared && i % kShareSlots == 0;
+    const size_t N = (size_t)geom[i].nx * geom[i].ny * geom[i].nz;
+    lay[i] = layout_instance(geom[i], p->opt[i].maxnumIter, first ? M * kShareSlots : M,
+                             kLayoutState | kLayoutGeometry, first ? N * kShareSlots : 0);
     base[i] = off;
     off += lay[i].bytes;
   }
@@ -669,6 +676,7 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
       const int g = i - i % kShareSlots;
       I.cor = (float *)(b + base[g] + lay[g].cor) + i % kShareSlots;
       I.cor_stride = kShareSlots;
+      I.m_il = (float *)(b + base[g] + lay[g].m_il);
       // one ray-slope table for all: instance 0 refreshes it every view
       I.tabC = (float4 *)(b + base[0] + lay[0].tabC);
       I.tabc_mode = i == 0 ? kTabcShared : kTabcNone;
@@ -855,7 +863,9 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   const int ng = p->max_ng > 0 ? p->max_ng : 1;
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {
-      case 0: return launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
+      case 0:
+        return p->shared ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, i % p->nv, p->st)
+                         : launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
       case 1:
         return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, i % p->nv,
                                                   p->st)

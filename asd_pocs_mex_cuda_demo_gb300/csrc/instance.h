@@ -9,8 +9,8 @@ namespace asd {
 // (each 256-byte aligned), at the instance's own sizes; `bytes` is the
 // block's size.
 struct InstLayout {
-  size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, ydet, zdet, trig, rmse,
-      part, cnt, scal, tabA, tabC, vflags, bytes;
+  size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, m_il, ydet, zdet, trig,
+      rmse, part, cnt, scal, tabA, tabC, vflags, bytes;
 };
 
 // Kind of an instance: 0 = 2-D fan beam (nz == nb == 1), 1 = one slice with
@@ -29,10 +29,13 @@ constexpr int kLayoutState = 1, kLayoutGeometry = 2;
 
 // Layout of the parts `parts` of an instance (absent parts take no bytes);
 // cor_floats is the length of its residual buffer (na*nb, or kShareSlots
-// times that for the first instance of a shared group).
+// times that for the first instance of a shared group) and il_floats that of
+// the interleaved images of a shared group (kShareSlots*N for the group's
+// first instance, else 0).
 InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
                            size_t cor_floats,
-                           int parts = kLayoutState | kLayoutGeometry);
+                           int parts = kLayoutState | kLayoutGeometry,
+                           size_t il_floats = 0);
 
 // Points I's state pointers at the block `b` laid out as `o`.
 void bind_state(Inst &I, char *b, const InstLayout &o);
@@ -61,8 +64,10 @@ cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st);
 
 // Enqueues one ASD-POCS iteration of `batch` instances on `st` (grids for
 // the largest sizes `d`, nv views, ng TV steps): per view the SART forward
-// and backward steps (shared-geometry backward step if `shared`), the
-// end-of-sweep scalars, the TV steps and the end of the iteration.
+// and backward steps, the end-of-sweep scalars, the TV steps and the end of
+// the iteration.  `shared`: the instances share geometry and angles and sit
+// in groups with interleaved images (Inst::m_il), packed before the sweep
+// and unpacked after it.
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st);
 

@@ -58,6 +58,16 @@ cudaError_t launch_gather_done(const Inst *insts, int n, int *out,
 cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
                                    const Dims &d, int view, cudaStream_t st);
 
+// Forward step for a batch whose instances share geometry and view angles:
+// the column march evaluated once per ray for groups of instances whose
+// images are interleaved (Inst::m_il) during the sweep.
+cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
+                                  int view, cudaStream_t st);
+// Copies the running instances' images into (unpack = 0) or out of
+// (unpack = 1) their group's interleaved images.
+cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,
+                              int unpack, cudaStream_t st);
+
 // Ray slope tables and flags of every view (Inst::tabA, Inst::vflags, which
 // must be zeroed first), computed once per plan.
 cudaError_t launch_view_tables(const Inst *insts, int batch, const Dims &d,

@@ -492,8 +492,8 @@ template <bool kPlanar, int AX>
 __device__ __forceinline__ void atx_shared_voxel(
     const ViewGeo &G, const Dims &D, const float4 *__restrict__ corg,
     const float4 *__restrict__ tabA, const float4 *__restrict__ tabC,
-    bool planar_ok, bool narrow, unsigned active, int gn,
-    float *const *s_m, const float *s_beta) {
+    bool planar_ok, bool narrow, unsigned active, int gn, float *m_il,
+    const float *s_beta) {
   int ix, iy, iz;
   const bool valid = tile_voxel(D, ix, iy, iz);
   VoxelWin w;
@@ -601,21 +601,29 @@ __device__ __forceinline__ void atx_shared_voxel(
   if (!valid) return;
   const float scv = accl * G.scale;
   const unsigned vi = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+  // the group's images, interleaved: four float4 per voxel
+  float4 *mg = (float4 *)m_il + (size_t)vi * (kShareGroup / 4);
 #pragma unroll
-  for (int b = 0; b < kShareGroup; b++) {
-    if (b < gn && ((active >> b) & 1u)) {
-      float *mb = s_m[b];
-      const float bp = acc[b] * G.scale;
-      const float mn = mb[vi] + s_beta[b] * __fdividef(bp, scv == 0.f ? 1.f : scv);
-      mb[vi] = mn < 0.f ? 0.f : mn;
+  for (int q = 0; q < kShareGroup / 4; q++) {
+    if (!((active >> (4 * q)) & 0xFu)) continue;
+    float4 m4 = mg[q];
+    float *mv = &m4.x;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int b = 4 * q + j;
+      if (b < gn && ((active >> b) & 1u)) {
+        const float bp = acc[b] * G.scale;
+        const float mn = mv[j] + s_beta[b] * __fdividef(bp, scv == 0.f ? 1.f : scv);
+        mv[j] = mn < 0.f ? 0.f : mn;
+      }
     }
+    mg[q] = m4;
   }
 }
 
 template <bool kPlanar>
 __global__ void __launch_bounds__(kAtxThreads, 3)
     k_sart_atx_shared(const Inst *__restrict__ insts, int batch, int view) {
-  __shared__ float *s_m[kShareGroup];
   __shared__ float s_beta[kShareGroup];
   __shared__ unsigned s_active;
   __shared__ int s_finite;
@@ -629,7 +637,6 @@ __global__ void __launch_bounds__(kAtxThreads, 3)
   if (threadIdx.x < gn) {
     const Inst &Ib = insts[g0 + threadIdx.x];
     const bool live = ((volatile int *)&Ib.s->done)[0] == 0;
-    s_m[threadIdx.x] = Ib.m;
     s_beta[threadIdx.x] = Ib.s->beta_f;
     if (live) {
       atomicOr(&s_active, 1u << threadIdx.x);
@@ -651,13 +658,202 @@ __global__ void __launch_bounds__(kAtxThreads, 3)
   const bool narrow = planar_ok && !(vf & kViewAxisParallel) && s_finite;
   if (!(vf & (kViewAxisParallel | kViewNotX)))
     atx_shared_voxel<kPlanar, 1>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
-                                 gn, s_m, s_beta);
+                                 gn, I0.m_il, s_beta);
   else if (!(vf & (kViewAxisParallel | kViewNotY)))
     atx_shared_voxel<kPlanar, 2>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
-                                 gn, s_m, s_beta);
+                                 gn, I0.m_il, s_beta);
   else
     atx_shared_voxel<kPlanar, 0>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
-                                 gn, s_m, s_beta);
+                                 gn, I0.m_il, s_beta);
+}
+
+// ---------------------------------------------------------------------------
+// Shared-geometry forward step: one warp per ray for a group of kShareGroup
+// instances.  The column march (cells and weights) is evaluated once per ray
+// and each piece reads the group's 16 voxel values with four float4 loads
+// from the interleaved images; every instance accumulates its pieces in the
+// order of k_sart_ax and sums lanes with the same butterfly, and its block
+// partials, reduction order and epilogue are those of k_sart_ax, so its
+// projection, residual, dd2 and flags are bit-identical to it.
+// ---------------------------------------------------------------------------
+template <bool k3D>
+__global__ void __launch_bounds__(kAxThreads)
+    k_sart_ax_shared(const Inst *__restrict__ insts, int batch, int view) {
+  __shared__ unsigned s_active;
+  __shared__ float s_part[2][kAxWarps][kShareGroup];
+  __shared__ int s_last[kShareGroup];
+  __shared__ int s_nlast;
+  const int g0 = blockIdx.z * kShareGroup;
+  const int gn = min(kShareGroup, batch - g0);
+  const Inst &I0 = insts[g0];
+  if (view >= I0.nv) return;
+  const Dims D = I0.d;
+  const long long nr = (long long)D.na * D.nb;
+  const OwnBlock ob = own_block(dim3((unsigned)((nr + kAxWarps - 1) / kAxWarps), 1));
+  if (ob.bid < 0) return;
+  if (threadIdx.x == 0) {
+    s_active = 0u;
+    s_nlast = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x < gn &&
+      ((volatile int *)&insts[g0 + threadIdx.x].s->done)[0] == 0)
+    atomicOr(&s_active, 1u << threadIdx.x);
+  __syncthreads();
+  const unsigned active = s_active;
+  const ViewGeo G = view_of(I0, view);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long r = (long long)blockIdx.x * kAxWarps + warp;
+  // cone beam: the plan's one ray-slope table, refreshed by group 0 every
+  // view whether or not its instances still run
+  if (k3D && blockIdx.z == 0 && lane == 0 && r < nr) {
+    const int ia = (int)(r % D.na), ib = (int)(r / D.na);
+    I0.tabC[r] = ray_tab_c(I0.tabA[(long long)view * D.na + ia], G.z_det[ib]);
+  }
+  if (!active) return;
+  float ys[kShareGroup];
+#pragma unroll
+  for (int b = 0; b < kShareGroup; b++) ys[b] = 0.f;
+  float ss = 0.f;
+  const float4 *__restrict__ mg = (const float4 *)I0.m_il;
+  if (r < nr) {
+    const int ia = (int)(r % D.na), ib = (int)(r / D.na);
+    const float zd = G.z_det[ib];
+    const RayMarch R = ray_setup(G, D, G.y_det[ia], zd);
+    const bool planar = D.nz == 1 && zd == 0.0f;
+    for (int iu = lane; iu < R.nu; iu += 32) {
+      constexpr int kP = 3;
+      unsigned id[kP];
+      float w[kP];
+      bool f[kP];
+      if (planar) {
+        unsigned i2[2];
+        float w2[2];
+        bool f2[2];
+        column_pieces_planar(R, iu, i2, w2, f2);
+        id[0] = i2[0], id[1] = i2[1], id[2] = 0u;
+        w[0] = w2[0], w[1] = w2[1], w[2] = 0.f;
+        f[0] = f2[0], f[1] = f2[1], f[2] = false;
+      } else {
+        column_pieces3(R, iu, id, w, f);
+      }
+#pragma unroll
+      for (int j = 0; j < kP; j++) {
+        if (!f[j]) continue;
+        const float4 *p = mg + (size_t)id[j] * (kShareGroup / 4);
+        float4 x[kShareGroup / 4];
+#pragma unroll
+        for (int q = 0; q < kShareGroup / 4; q++)
+          x[q] = ((active >> (4 * q)) & 0xFu) ? __ldg(p + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < kShareGroup / 4; q++) {
+          ys[4 * q] += w[j] * x[q].x;
+          ys[4 * q + 1] += w[j] * x[q].y;
+          ys[4 * q + 2] += w[j] * x[q].z;
+          ys[4 * q + 3] += w[j] * x[q].w;
+        }
+        ss += w[j];
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kShareGroup / 4; q++)
+    if ((active >> (4 * q)) & 0xFu) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) ys[4 * q + j] = warp_sum(ys[4 * q + j]);
+    }
+  ss = warp_sum(ss);
+  // lane b: the epilogue of k_sart_ax for instance g0 + b
+  float yb = 0.f;
+#pragma unroll
+  for (int b = 0; b < kShareGroup; b++)
+    if (lane == b) yb = ys[b];
+  float p0 = 0.f, p1 = 0.f;
+  if (lane < gn && ((active >> lane) & 1u) && r < nr) {
+    const Inst &Ib = insts[g0 + lane];
+    const float yv = yb * G.scale, srv = ss * G.scale;
+    const float c0 = Ib.P[(long long)view * nr + r] - yv;
+    const float cr = c0 / (srv == 0.f ? 1.f : srv);
+    Ib.cor[r * Ib.cor_stride] = cr;
+    p0 = c0 * c0;
+    p1 = isfinite(cr) ? 0.f : 1.f;
+  }
+  if (lane < kShareGroup) {
+    s_part[0][warp][lane] = p0;
+    s_part[1][warp][lane] = p1;
+  }
+  __syncthreads();
+  // per instance: the block total of k_sart_ax's block_sum_f (lane 0 of each
+  // warp the only nonzero value; warps combined as (w0 + w2) + (w1 + w3)),
+  // its partial, its ticket
+  static_assert(kAxWarps == 4, "block totals below follow block_sum_f for 4 warps");
+  if (threadIdx.x < gn && ((active >> threadIdx.x) & 1u)) {
+    const int b = threadIdx.x;
+    const Inst &Ib = insts[g0 + b];
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const float v = (s_part[k][0][b] + s_part[k][2][b]) + (s_part[k][1][b] + s_part[k][3][b]);
+      Ib.partials[(long long)ob.bid * 2 + k] = (double)v;
+    }
+    __threadfence();
+    if (atomicAdd(Ib.counter, 1u) == (unsigned)ob.nblocks - 1)
+      s_last[atomicAdd(&s_nlast, 1)] = b;
+  }
+  __syncthreads();
+  const int nlast = s_nlast;
+  if (nlast == 0) return;
+  __threadfence();
+  for (int i = 0; i < nlast; i++) {
+    const Inst &Ib = insts[g0 + s_last[i]];
+    double tot[2];
+    grid_sum_final<kAxThreads, 2>(Ib.partials, Ib.counter, ob.nblocks, tot);
+    if (threadIdx.x == 0) {
+      Ib.s->dd2_acc += tot[0];
+      Ib.s->cor_finite = tot[1] == 0.0;
+    }
+  }
+}
+
+// Copies the running instances of each shared-geometry group between their
+// own images (m) and the group's interleaved images (m_il): pack before the
+// SART sweep, unpack after it.  Grid (voxel blocks, 1, groups).
+__global__ void __launch_bounds__(256)
+    k_group_pack(const Inst *__restrict__ insts, int batch, int unpack) {
+  __shared__ float *s_m[kShareGroup];
+  __shared__ unsigned s_active;
+  const int g0 = blockIdx.z * kShareGroup;
+  const int gn = min(kShareGroup, batch - g0);
+  if (threadIdx.x == 0) s_active = 0u;
+  __syncthreads();
+  if (threadIdx.x < gn) {
+    const Inst &Ib = insts[g0 + threadIdx.x];
+    s_m[threadIdx.x] = Ib.m;
+    if (((volatile int *)&Ib.s->done)[0] == 0) atomicOr(&s_active, 1u << threadIdx.x);
+  }
+  __syncthreads();
+  const unsigned active = s_active;
+  const Dims D = insts[g0].d;
+  const long long n = (long long)D.nx * D.ny * D.nz;
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!active || v >= n) return;
+  float4 *mg = (float4 *)insts[g0].m_il + v * (kShareGroup / 4);
+#pragma unroll
+  for (int q = 0; q < kShareGroup / 4; q++) {
+    if (!((active >> (4 * q)) & 0xFu)) continue;
+    float4 x = unpack ? mg[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float *xv = &x.x;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int b = 4 * q + j;
+      if (b < gn && ((active >> b) & 1u)) {
+        if (unpack)
+          s_m[b][v] = xv[j];
+        else
+          xv[j] = s_m[b][v];
+      }
+    }
+    if (!unpack) mg[q] = x;
+  }
 }
 
 }  // namespace
@@ -710,6 +906,26 @@ cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
     k_sart_atx_shared<false><<<grid, kAtxThreads, 0, st>>>(insts, batch, view);
   else
     k_sart_atx_shared<true><<<grid, kAtxThreads, 0, st>>>(insts, batch, view);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
+                                  int view, cudaStream_t st) {
+  const long long nr = (long long)d.na * d.nb;
+  const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
+  const dim3 grid(blocks, 1, (batch + kShareGroup - 1) / kShareGroup);
+  if (d.nz > 1 || d.nb > 1)
+    k_sart_ax_shared<true><<<grid, kAxThreads, 0, st>>>(insts, batch, view);
+  else
+    k_sart_ax_shared<false><<<grid, kAxThreads, 0, st>>>(insts, batch, view);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,
+                              int unpack, cudaStream_t st) {
+  const long long n = (long long)d.nx * d.ny * d.nz;
+  const dim3 grid((unsigned)((n + 255) / 256), 1, (batch + kShareGroup - 1) / kShareGroup);
+  k_group_pack<<<grid, 256, 0, st>>>(insts, batch, unpack);
   return cudaGetLastError();
 }
 

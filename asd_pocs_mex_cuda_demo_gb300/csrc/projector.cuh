@@ -189,62 +189,70 @@ ASD_HD void ray_columns(const RayMarch &R, int first,
 // without control flow; a group of U columns is evaluated first, its
 // predicated loads are issued together, then the pieces are accumulated in
 // order, so a lane keeps up to 3U loads in flight.
+// The pieces of column iu for ray_columns_fast: at most three, in position
+// order (A, B, C), with their validity, evaluated without control flow.
+ASD_HD void column_pieces3(const RayMarch &R, int iu, unsigned (&id)[3],
+                           float (&w)[3], bool (&f)[3]) {
+  const bool pos1 = R.slope1 >= 0, pos2 = R.slope2 >= 0;
+  const bool zdiv = R.dz != 1.0f;
+  const float uu1 = (float)(iu - R.nu2);
+  const float uu2 = uu1 + 1;
+  const float ua = pos1 ? uu1 : uu2, ub = pos1 ? uu2 : uu1;
+  const float v1 = R.vs + R.slope1 * (ua - R.us) + R.nv2;
+  const float v2 = R.vs + R.slope1 * (ub - R.us) + R.nv2;
+  const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
+  const float q1 = 0.0f + R.slope2 * ((pos2 ? uu1 : uu2) - R.us);
+  const float q2 = 0.0f + R.slope2 * ((pos2 ? uu2 : uu1) - R.us);
+  const float w1 = (zdiv ? q1 / R.dz : q1) + R.nz2;
+  const float w2 = (zdiv ? q2 / R.dz : q2) + R.nz2;
+  const int cz1 = (int)floorf(w1), cz2 = (int)floorf(w2);
+  const bool vs = cv1 != cv2, zs = cz1 != cz2;
+  const bool vmid = cv2 > 0 && cv2 < R.nv, zmid = cz2 > 0 && cz2 < R.nz;
+  const bool in = iu < R.nu;
+  const bool vlo = in && (vs ? (vmid || cv2 == R.nv) : (cv1 >= 0 && cv1 <= R.nv - 1)) &&
+                   cv1 >= 0 && cv1 < R.nv;
+  const bool vhi = in && vs && (vmid || cv2 == 0) && cv2 >= 0 && cv2 < R.nv;
+  const bool zlo = (zs ? (zmid || cz2 == R.nz) : (cz1 >= 0 && cz1 <= R.nz - 1)) &&
+                   cz1 >= 0 && cz1 < R.nz;
+  const bool zhi = zs && (zmid || cz2 == 0) && cz2 >= 0 && cz2 < R.nz;
+  const float d = v2 - v1;
+  const float l = sqrtf((d * d + 1) * R.lfac);
+  const float rv = fast_div(cv2 - v1, d);
+  const float rz = fast_div(cz2 - w1, w2 - w1);
+  const unsigned base = (unsigned)iu * R.su;
+  const unsigned ilo = base + (unsigned)cv1 * R.sv;
+  const unsigned ihi = base + (unsigned)cv2 * R.sv;
+  const unsigned zl = (unsigned)cz1 * R.sz, zh = (unsigned)cz2 * R.sz;
+  const bool vfirst = !(rv > rz);  // both split: the v crossing comes first
+  // piece A: from the column entry
+  w[0] = !vs ? (zs ? rz * l : l) : (!zs ? rv * l : (vfirst ? rv : rz) * l);
+  id[0] = ilo + zl;
+  f[0] = vlo && zlo;
+  // piece B
+  w[1] = !vs ? (1 - rz) * l : (!zs ? (1 - rv) * l : (vfirst ? (rz - rv) : (rv - rz)) * l);
+  id[1] = !vs ? ilo + zh : (!zs ? ihi + zl : (vfirst ? ihi + zl : ilo + zh));
+  f[1] = !vs ? (zs && vlo && zhi)
+             : (!zs ? (vhi && zlo) : (vfirst ? (vhi && zlo) : (vlo && zhi)));
+  // piece C (both split)
+  w[2] = (vfirst ? (1 - rz) : (1 - rv)) * l;
+  id[2] = ihi + zh;
+  f[2] = vs && zs && vhi && zhi;
+}
+
+// The kernels' form of ray_columns<false> (same cells, weights and
+// accumulation order, so bit-identical to it): a group of U columns'
+// pieces is evaluated first, its predicated loads are issued together, then
+// the pieces are accumulated in order, so a lane keeps up to 3U loads in
+// flight.
 template <int U = 2, class Loader>
 ASD_HD void ray_columns_fast(const RayMarch &R, int first, int step, Loader ld,
                              float &ys, float &ss) {
-  const bool pos1 = R.slope1 >= 0, pos2 = R.slope2 >= 0;
-  const bool zdiv = R.dz != 1.0f;
   for (int iu0 = first; iu0 < R.nu; iu0 += U * step) {
     float w[U][3], x[U][3];
     unsigned id[U][3];
     bool f[U][3];
 #pragma unroll
-    for (int k = 0; k < U; k++) {
-      const int iu = iu0 + k * step;
-      const float uu1 = (float)(iu - R.nu2);
-      const float uu2 = uu1 + 1;
-      const float ua = pos1 ? uu1 : uu2, ub = pos1 ? uu2 : uu1;
-      const float v1 = R.vs + R.slope1 * (ua - R.us) + R.nv2;
-      const float v2 = R.vs + R.slope1 * (ub - R.us) + R.nv2;
-      const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
-      const float q1 = 0.0f + R.slope2 * ((pos2 ? uu1 : uu2) - R.us);
-      const float q2 = 0.0f + R.slope2 * ((pos2 ? uu2 : uu1) - R.us);
-      const float w1 = (zdiv ? q1 / R.dz : q1) + R.nz2;
-      const float w2 = (zdiv ? q2 / R.dz : q2) + R.nz2;
-      const int cz1 = (int)floorf(w1), cz2 = (int)floorf(w2);
-      const bool vs = cv1 != cv2, zs = cz1 != cz2;
-      const bool vmid = cv2 > 0 && cv2 < R.nv, zmid = cz2 > 0 && cz2 < R.nz;
-      const bool in = iu < R.nu;
-      const bool vlo = in && (vs ? (vmid || cv2 == R.nv) : (cv1 >= 0 && cv1 <= R.nv - 1)) &&
-                       cv1 >= 0 && cv1 < R.nv;
-      const bool vhi = in && vs && (vmid || cv2 == 0) && cv2 >= 0 && cv2 < R.nv;
-      const bool zlo = (zs ? (zmid || cz2 == R.nz) : (cz1 >= 0 && cz1 <= R.nz - 1)) &&
-                       cz1 >= 0 && cz1 < R.nz;
-      const bool zhi = zs && (zmid || cz2 == 0) && cz2 >= 0 && cz2 < R.nz;
-      const float d = v2 - v1;
-      const float l = sqrtf((d * d + 1) * R.lfac);
-      const float rv = fast_div(cv2 - v1, d);
-      const float rz = fast_div(cz2 - w1, w2 - w1);
-      const unsigned base = (unsigned)iu * R.su;
-      const unsigned ilo = base + (unsigned)cv1 * R.sv;
-      const unsigned ihi = base + (unsigned)cv2 * R.sv;
-      const unsigned zl = (unsigned)cz1 * R.sz, zh = (unsigned)cz2 * R.sz;
-      const bool vfirst = !(rv > rz);  // both split: the v crossing comes first
-      // piece A: from the column entry
-      w[k][0] = !vs ? (zs ? rz * l : l) : (!zs ? rv * l : (vfirst ? rv : rz) * l);
-      id[k][0] = ilo + zl;
-      f[k][0] = vlo && zlo;
-      // piece B
-      w[k][1] = !vs ? (1 - rz) * l
-                    : (!zs ? (1 - rv) * l : (vfirst ? (rz - rv) : (rv - rz)) * l);
-      id[k][1] = !vs ? ilo + zh : (!zs ? ihi + zl : (vfirst ? ihi + zl : ilo + zh));
-      f[k][1] = !vs ? (zs && vlo && zhi)
-                    : (!zs ? (vhi && zlo) : (vfirst ? (vhi && zlo) : (vlo && zhi)));
-      // piece C (both split)
-      w[k][2] = (vfirst ? (1 - rz) : (1 - rv)) * l;
-      id[k][2] = ihi + zh;
-      f[k][2] = vs && zs && vhi && zhi;
-    }
+    for (int k = 0; k < U; k++) column_pieces3(R, iu0 + k * step, id[k], w[k], f[k]);
 #pragma unroll
     for (int k = 0; k < U; k++)
 #pragma unroll
@@ -323,54 +331,58 @@ ASD_HD void ray_columns_planar(const RayMarch &R, int first,
 // U columns is evaluated first, then its (predicated) loads are issued
 // together, then the pieces are accumulated in order -- so a lane keeps 2U
 // loads in flight instead of waiting on each column in turn.
+// The pieces of column iu for ray_columns_planar_fast: the lower and the
+// upper row, with their validity, evaluated without control flow.
+ASD_HD void column_pieces_planar(const RayMarch &R, int iu, unsigned (&id)[2],
+                                 float (&w)[2], bool (&f)[2]) {
+  const bool pos = R.slope1 >= 0;
+  const float uu1 = (float)(iu - R.nu2);
+  const float uu2 = uu1 + 1;
+  const float ua = pos ? uu1 : uu2, ub = pos ? uu2 : uu1;
+  const float v1 = R.vs + R.slope1 * (ua - R.us) + R.nv2;
+  const float v2 = R.vs + R.slope1 * (ub - R.us) + R.nv2;
+  const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
+  const bool split = cv1 != cv2;
+  const bool mid = cv2 > 0 && cv2 < R.nv;
+  const bool in = iu < R.nu;
+  f[0] = in && cv1 >= 0 && cv1 < R.nv && (split ? (mid || cv2 == R.nv) : true);
+  f[1] = in && split && cv2 >= 0 && cv2 < R.nv && (mid || cv2 == 0);
+  const float d = v2 - v1;
+  const float l = sqrtf(d * d + 1);
+  const float rv = fast_div(cv2 - v1, d);
+  w[0] = split ? rv * l : l;
+  w[1] = (1 - rv) * l;
+  const unsigned base = (unsigned)iu * R.su;
+  id[0] = base + (unsigned)cv1 * R.sv;
+  id[1] = base + (unsigned)cv2 * R.sv;
+}
+
+// The kernels' form of ray_columns_planar<false>: the same cells, weights
+// and accumulation order, computed without control flow.  A group of U
+// columns is evaluated first, then its (predicated) loads are issued
+// together, then the pieces are accumulated in order -- so a lane keeps 2U
+// loads in flight instead of waiting on each column in turn.
 template <int U = 4, class Loader>
 ASD_HD void ray_columns_planar_fast(const RayMarch &R, int first, int step,
                                     Loader ld, float &ys, float &ss) {
-  const bool pos = R.slope1 >= 0;
   for (int iu0 = first; iu0 < R.nu; iu0 += U * step) {
-    float w_lo[U], w_hi[U], x_lo[U], x_hi[U];
-    unsigned i_lo[U], i_hi[U];
-    bool f_lo[U], f_hi[U];
+    float w[U][2], x[U][2];
+    unsigned id[U][2];
+    bool f[U][2];
 #pragma unroll
-    for (int k = 0; k < U; k++) {
-      const int iu = iu0 + k * step;
-      const float uu1 = (float)(iu - R.nu2);
-      const float uu2 = uu1 + 1;
-      const float ua = pos ? uu1 : uu2, ub = pos ? uu2 : uu1;
-      const float v1 = R.vs + R.slope1 * (ua - R.us) + R.nv2;
-      const float v2 = R.vs + R.slope1 * (ub - R.us) + R.nv2;
-      const int cv1 = (int)floorf(v1), cv2 = (int)floorf(v2);
-      const bool split = cv1 != cv2;
-      const bool mid = cv2 > 0 && cv2 < R.nv;
-      const bool in = iu < R.nu;
-      f_lo[k] = in && cv1 >= 0 && cv1 < R.nv &&
-                (split ? (mid || cv2 == R.nv) : true);
-      f_hi[k] = in && split && cv2 >= 0 && cv2 < R.nv && (mid || cv2 == 0);
-      const float d = v2 - v1;
-      const float l = sqrtf(d * d + 1);
-      const float rv = fast_div(cv2 - v1, d);
-      w_lo[k] = split ? rv * l : l;
-      w_hi[k] = (1 - rv) * l;
-      const unsigned base = (unsigned)iu * R.su;
-      i_lo[k] = base + (unsigned)cv1 * R.sv;
-      i_hi[k] = base + (unsigned)cv2 * R.sv;
-    }
+    for (int k = 0; k < U; k++) column_pieces_planar(R, iu0 + k * step, id[k], w[k], f[k]);
 #pragma unroll
-    for (int k = 0; k < U; k++) {
-      x_lo[k] = f_lo[k] ? ld(i_lo[k]) : 0.f;
-      x_hi[k] = f_hi[k] ? ld(i_hi[k]) : 0.f;
-    }
+    for (int k = 0; k < U; k++)
 #pragma unroll
-    for (int k = 0; k < U; k++) {
-      if (f_lo[k]) {
-        ys += w_lo[k] * x_lo[k];
-        ss += w_lo[k];
-      }
-      if (f_hi[k]) {
-        ys += w_hi[k] * x_hi[k];
-        ss += w_hi[k];
-      }
-    }
+      for (int j = 0; j < 2; j++) x[k][j] = f[k][j] ? ld(id[k][j]) : 0.f;
+#pragma unroll
+    for (int k = 0; k < U; k++)
+#pragma unroll
+      for (int j = 0; j < 2; j++)
+        if (f[k][j]) {
+          ys += w[k][j] * x[k][j];
+          ss += w[k][j];
+        }
   }
 }
 

@@ -40,6 +40,42 @@ __device__ __forceinline__ void block_sum_f(const float (&v)[K], float (&out)[K]
   __syncthreads();
 }
 
+// The last block's part of grid_sum: the FP64 totals of `nblocks` block
+// partials (K values each) in a fixed order -- each thread a strided
+// subset, a warp butterfly, then the warps in order -- and the ticket
+// reset.  Every thread of the block must call it; all get the totals.
+template <int NT, int K>
+__device__ __forceinline__ void grid_sum_final(const double *partials,
+                                               unsigned *counter, int nblocks,
+                                               double (&tot)[K]) {
+  __shared__ double sh[K * (NT / 32)];
+  __shared__ double bc[K];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double a = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += NT)
+      a += ((volatile const double *)partials)[(long long)b * K + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) sh[k * (NT / 32) + warp] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      double a = 0.0;
+      for (int w = 0; w < NT / 32; w++) a += sh[k * (NT / 32) + w];
+      bc[k] = a;
+    }
+    *counter = 0u;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; k++) tot[k] = bc[k];
+  __syncthreads();  // sh / bc may be reused by the next call
+}
+
 // Grid-wide deterministic sum of K values per thread over the blocks
 // bid = 0..nblocks-1 of one reduction (other grid dimensions select
 // independent reductions through `partials`/`counter`).  `partials` holds
@@ -51,7 +87,6 @@ __device__ __forceinline__ bool grid_sum(const float (&v)[K], double *partials,
                                          int nblocks, double (&tot)[K]) {
   static_assert(K <= kMaxReduceK, "partials are sized for kMaxReduceK values");
   __shared__ float shf[K * (NT / 32)];
-  __shared__ double sh[K * (NT / 32)];
   __shared__ bool last;
   float bs[K];
   block_sum_f<NT, K>(v, bs, shf);
@@ -65,31 +100,7 @@ __device__ __forceinline__ bool grid_sum(const float (&v)[K], double *partials,
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  // FP64 over the block partials (nblocks per reduction; few per thread)
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int k = 0; k < K; k++) {
-    double a = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += NT)
-      a += ((volatile double *)partials)[(long long)b * K + k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if (lane == 0) sh[k * (NT / 32) + warp] = a;
-  }
-  __syncthreads();
-  __shared__ double bc[K];
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < K; k++) {
-      double a = 0.0;
-      for (int w = 0; w < NT / 32; w++) a += sh[k * (NT / 32) + w];
-      bc[k] = a;
-    }
-    *counter = 0u;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < K; k++) tot[k] = bc[k];
+  grid_sum_final<NT, K>(partials, counter, nblocks, tot);
   return true;
 }
 

@@ -81,6 +81,7 @@ struct Lane {
   int *d_flags = nullptr;          // S done flags
   Scalars *d_dead = nullptr;       // scalars of an empty slot (done = 1)
   char *geo = nullptr;             // the protocol's geometry block
+  size_t geo_bytes = 0;
   Inst tmpl{};                     // geometry of every slot
   std::vector<Inst> slot_desc;     // descriptor of each slot (host copy)
   std::vector<Job *> slot_job;
@@ -178,23 +179,32 @@ Inst empty_slot(const Lane &L, int s) {
   Inst I = L.tmpl;
   I.s = L.d_dead;
   const size_t M = (size_t)L.g.na * L.g.nb;
+  const size_t N = (size_t)L.g.nx * L.g.ny * L.g.nz;
   I.cor = L.tmpl.cor + (size_t)(s / kShareSlots) * M * kShareSlots + s % kShareSlots;
   I.cor_stride = kShareSlots;
+  I.m_il = L.tmpl.m_il + (size_t)(s / kShareSlots) * N * kShareSlots;
   I.tabc_mode = s == 0 ? kTabcShared : kTabcNone;
   return I;
 }
 
 bool lane_create(asdpocs_server sv, Lane &L) {
-  L.S = sv->cfg.slots_per_lane;
+  // slots: as configured, but the lane's interleaved images (4 bytes per
+  // voxel and slot) within an eighth of the budget, in whole groups
+  const size_t vox = (size_t)L.g.nx * L.g.ny * L.g.nz;
+  const long long fit = (long long)(sv->budget / 8 / (vox * 4));
+  L.S = (int)std::min<long long>(sv->cfg.slots_per_lane,
+                                 std::max<long long>(kShareSlots, fit / kShareSlots * kShareSlots));
   const size_t M = (size_t)L.g.na * L.g.nb;
   const int groups = (L.S + kShareSlots - 1) / kShareSlots;
   SV_CUDA(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking));
   SV_CUDA(cudaMalloc(&L.d_inst, sizeof(Inst) * L.S));
   SV_CUDA(cudaMalloc(&L.d_flags, sizeof(int) * L.S));
   SV_CUDA(cudaMalloc(&L.d_dead, sizeof(Scalars)));
-  const InstLayout gl =
-      layout_instance(L.g, 0, (size_t)groups * kShareSlots * M, kLayoutGeometry);
+  const size_t N = (size_t)L.g.nx * L.g.ny * L.g.nz;
+  const InstLayout gl = layout_instance(L.g, 0, (size_t)groups * kShareSlots * M,
+                                        kLayoutGeometry, (size_t)groups * kShareSlots * N);
   SV_CUDA(cudaMalloc(&L.geo, gl.bytes));
+  L.geo_bytes = gl.bytes;  // outside the jobs' budget (bounded by the slots rule)
   SV_CUDA(cudaMemsetAsync(L.geo, 0, gl.bytes, L.st));
   Scalars dead_s;
   memset(&dead_s, 0, sizeof dead_s);
@@ -203,6 +213,7 @@ bool lane_create(asdpocs_server sv, Lane &L) {
                           L.st));
   memset(&L.tmpl, 0, sizeof L.tmpl);
   SV_CUDA(bind_geometry(L.tmpl, L.geo, gl, L.g, L.phi.data(), L.st));
+  L.tmpl.m_il = (float *)(L.geo + gl.m_il);
   L.slot_desc.resize(L.S);
   for (int s = 0; s < L.S; s++) L.slot_desc[s] = empty_slot(L, s);
   SV_CUDA(cudaMemcpyAsync(L.d_inst, L.slot_desc.data(), sizeof(Inst) * L.S,

@@ -252,9 +252,11 @@ int SART_cuda_inline(const double *P, const double *phi_vec_deg,
  * a lane per launch sequence (a replayed CUDA graph), retires jobs as they
  * finish and admits waiting ones in their place, so jobs that arrive while
  * others run join them on the device.  Each job's result is bit-identical
- * to the same job run alone in a plan.  The budget counts the jobs' state;
- * a lane's geometry tables (a few MB) are held until the server is
- * destroyed.  All calls are thread-safe.
+ * to the same job run alone in a plan.  The budget counts the jobs' state.
+ * A lane also holds its protocol's geometry tables and its slots'
+ * interleaved images (4 bytes per voxel and slot; a lane gets as many slots,
+ * in groups of 16, as fit in an eighth of the budget, at least 16) until the
+ * server is destroyed.  All calls are thread-safe.
  * --------------------------------------------------------------------- */
 typedef struct asdpocs_server_s *asdpocs_server;
 
