@@ -82,6 +82,9 @@ struct Inst {
   float *m_k1;               // TV distance reference (m0)
   float *I0;                 // reference image or nullptr
   float *tv_b, *tv_c;        // TV ping-pong buffers
+  float *tv_va, *tv_vb;      // 2-D TV: the stencil v of the image each step
+                             //   starts from (ping-pong), so the step's update
+                             //   reads it instead of recomputing it
   float *cor;                // correction of the current view: element r at
   int cor_stride;            //   cor[r * cor_stride] (1, or kShareSlots when
                              //   a shared-geometry group interleaves them)

@@ -431,6 +431,10 @@ InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
   o.I0 = off; off += per_img;
   o.tvb = off; off += per_img;
   o.tvc = off; off += per_img;
+  // 2-D: the TV stencil of the step's starting image (cone beam: unused)
+  const size_t per_v = (st && g.nz == 1) ? per_img : 0;
+  o.tvva = off; off += per_v;
+  o.tvvb = off; off += per_v;
   o.rmse = off; off += st ? align256((size_t)(max_iter + 1) * 8) : 0;
   o.part = off; off += st ? align256(nblk * kMaxReduceK * 8) : 0;
   o.cnt = off; off += st ? 256 : 0;
@@ -456,6 +460,8 @@ void bind_state(Inst &I, char *b, const InstLayout &o) {
   I.I0 = (float *)(b + o.I0);
   I.tv_b = (float *)(b + o.tvb);
   I.tv_c = (float *)(b + o.tvc);
+  I.tv_va = (float *)(b + o.tvva);
+  I.tv_vb = (float *)(b + o.tvvb);
   I.rmse = (double *)(b + o.rmse);
   I.partials = (double *)(b + o.part);
   I.counter = (unsigned *)(b + o.cnt);

@@ -9,7 +9,7 @@ namespace asd {
 // (each 256-byte aligned), at the instance's own sizes; `bytes` is the
 // block's size.
 struct InstLayout {
-  size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, m_il, ydet, zdet, trig,
+  size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, tvva, tvvb, cor, m_il, ydet, zdet, trig,
       rmse, part, cnt, scal, tabA, tabC, vflags, bytes;
 };
 

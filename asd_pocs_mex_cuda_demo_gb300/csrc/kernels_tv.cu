@@ -255,6 +255,10 @@ __device__ __forceinline__ const float *tv_src(const Inst &I, int step) {
 __device__ __forceinline__ float *tv_dst(const Inst &I, int step) {
   return (step & 1) ? I.tv_c : I.tv_b;
 }
+// 2-D: the stencil v of the image step `step` starts from
+__device__ __forceinline__ float *tv_v(const Inst &I, int step) {
+  return (step & 1) ? I.tv_vb : I.tv_va;
+}
 
 // End-of-iteration scalars (ASD_POCS_cuda.m:166-170) by the last block.
 __device__ __forceinline__ void finish_scalars(Scalars *s, double dg2) {
@@ -309,6 +313,7 @@ __global__ void __launch_bounds__(kThreads)
         const float gr =
             tv_grad<float>(TileAt<1, k3D>{t, tx + 1, ty + 1, k3D ? 1 : 0}, k3D);
         v[3] += gr * gr;
+        if (!k3D) I.tv_va[i] = gr;  // the first TV step's update reads it
       }
     }
     __syncthreads();  // the tile is reused by the next group member
@@ -415,18 +420,19 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // 2-D TV step over the block's whole group of kTilesPerBlock tiles as one
-// 32 x 32 voxel tile: the source with a two-voxel halo (36 x 36) is staged
-// once, m' is evaluated once on the group plus a one-voxel halo (34 x 34),
-// and each thread then writes and differentiates its four voxels (rows
-// ty, ty+8, ty+16, ty+24 of the group -- the same voxels, in the same order,
-// as the tile-by-tile form, so the results are identical to it).  Per voxel
-// this stages 1.27 source values and evaluates m' 1.13 times, against 1.69
-// and 1.33 for one 32 x 8 tile at a time.
+// 32 x 32 voxel tile.  The update m' = m - coef * v(m) needs the stencil v of
+// the step's starting image, which the previous step (or the end-of-sweep
+// kernel) evaluated for its norm and stored: the step reads m and v on the
+// group plus a one-voxel halo, forms m' there (34 x 34) without a stencil,
+// writes its four voxels per thread (rows ty, ty+8, ty+16, ty+24) and
+// evaluates one stencil per voxel -- v(m'), for the next norm, stored for the
+// next step.  The values are those of recomputing v here, so the results do
+// not change; the work per voxel drops from 2.13 stencils to one, for 8 more
+// bytes of traffic.
 constexpr int kGroupRows = kTileY * kTilesPerBlock;
 
 __global__ void __launch_bounds__(kThreads)
     k_tv_step2d(const Inst *__restrict__ insts, int step) {
-  __shared__ float s2[kGroupRows + 4][kTileX + 4];
   __shared__ float s1[kGroupRows + 2][kTileX + 2];
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
@@ -442,21 +448,14 @@ __global__ void __launch_bounds__(kThreads)
   float *dst = tv_dst(I, step);
   const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
   const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kGroupRows;
-  // Source with a two-voxel halo, zero outside the image.  The points are
-  // dealt to the threads in fixed-count unrolled rounds, so each thread has
-  // its loads (and below, its stencils) in flight together.
-  constexpr int W2 = kTileX + 4, N2 = W2 * (kGroupRows + 4);
-#pragma unroll
-  for (int j = 0; j < (N2 + kThreads - 1) / kThreads; j++) {
-    const int k = threadIdx.x + j * kThreads;
-    const int r = k / W2, c = k - r * W2;
-    const int y = y0 - 2 + r, x = x0 - 2 + c;
-    if (k < N2)
-      s2[r][c] = (y >= 0 && y < D.ny && x >= 0 && x < D.nx)
-                     ? src[(unsigned)y * D.nx + x] : 0.f;
-  }
-  __syncthreads();
-  // m' on the group and a one-voxel halo (zero outside the image)
+  // m' = m - coef * v(m) on the group and a one-voxel halo (zero outside the
+  // image), with v(m) read from the previous step (the end-of-sweep kernel
+  // for the first step): the same values the stencil would give, so no
+  // stencil is evaluated here.  The points are dealt to the threads in
+  // fixed-count unrolled rounds, so each thread has its loads in flight
+  // together.
+  const float *vin = tv_v(I, step);
+  float *vout = tv_v(I, step + 1);
   constexpr int W1 = kTileX + 2, N1 = W1 * (kGroupRows + 2);
 #pragma unroll
   for (int j = 0; j < (N1 + kThreads - 1) / kThreads; j++) {
@@ -466,8 +465,8 @@ __global__ void __launch_bounds__(kThreads)
     if (k < N1) {
       float val = 0.f;
       if (y >= 0 && y < D.ny && x >= 0 && x < D.nx) {
-        const auto u = [&](int dx, int dy, int) { return s2[r + 1 + dy][c + 1 + dx]; };
-        val = u(0, 0, 0) - coef * tv_grad2<float>(u);
+        const unsigned i = (unsigned)y * D.nx + x;
+        val = src[i] - coef * vin[i];
       }
       s1[r][c] = val;
     }
@@ -494,6 +493,7 @@ __global__ void __launch_bounds__(kThreads)
         if (!last) {
           const float gr = tv_grad2<float>(u);
           v[0] += gr * gr;
+          vout[i] = gr;  // the next step's update reads it
         }
       }
     }

@@ -66,12 +66,12 @@ SERVE = dict(
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per instance and
 # launch of each iteration kernel, from `ncu --set full --clock-control none`
-# captures of the 2D fan-beam workload at batch 16 (one shared-geometry
-# group); the traffic is one read of each instance's image, so it scales with
-# the batch.
+# captures of the 2D fan-beam workload at batch 64 (the shared-geometry
+# kernels); the traffic is about one read of each instance's image plus its
+# writes, so it scales with the batch.
 NCU_DRAM_PER_INSTANCE = {
-    "fan2d": {"sart_atx": 16.897e6 / 16, "sart_ax": 15.241e6 / 16,
-              "tv_step": 16.985e6 / 16},
+    "fan2d": {"sart_ax": 60.341e6 / 64, "sart_atx": 81.884e6 / 64,
+              "tv_step": 96.786e6 / 64},
 }
 
 
