@@ -676,9 +676,15 @@ __global__ void __launch_bounds__(kAtxThreads, 3)
 // partials, reduction order and epilogue are those of k_sart_ax, so its
 // projection, residual, dd2 and flags are bit-identical to it.
 // ---------------------------------------------------------------------------
+constexpr int kAxSplit = 2;  // warps sharing one ray of a group
+constexpr int kAxSharedThreads = kAxThreads * kAxSplit;
+
 template <bool k3D>
-__global__ void __launch_bounds__(kAxThreads)
+__global__ void __launch_bounds__(kAxSharedThreads)
     k_sart_ax_shared(const Inst *__restrict__ insts, int batch, int view) {
+  // warp w marches ray (w % kAxWarps) of the block for instances
+  // [(w / kAxWarps) * kPer, + kPer) of the group
+  constexpr int kPer = kShareGroup / kAxSplit, kQuads = kPer / 4;
   __shared__ unsigned s_active;
   __shared__ float s_part[2][kAxWarps][kShareGroup];
   __shared__ int s_last[kShareGroup];
@@ -703,20 +709,22 @@ __global__ void __launch_bounds__(kAxThreads)
   const unsigned active = s_active;
   const ViewGeo G = view_of(I0, view);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long r = (long long)blockIdx.x * kAxWarps + warp;
+  const int rw = warp % kAxWarps, part = warp / kAxWarps;
+  const long long r = (long long)blockIdx.x * kAxWarps + rw;
   // cone beam: the plan's one ray-slope table, refreshed by group 0 every
   // view whether or not its instances still run
-  if (k3D && blockIdx.z == 0 && lane == 0 && r < nr) {
+  if (k3D && blockIdx.z == 0 && part == 0 && lane == 0 && r < nr) {
     const int ia = (int)(r % D.na), ib = (int)(r / D.na);
     I0.tabC[r] = ray_tab_c(I0.tabA[(long long)view * D.na + ia], G.z_det[ib]);
   }
   if (!active) return;
-  float ys[kShareGroup];
+  const unsigned mine = (active >> (part * kPer)) & ((1u << kPer) - 1u);
+  float ys[kPer];
 #pragma unroll
-  for (int b = 0; b < kShareGroup; b++) ys[b] = 0.f;
+  for (int b = 0; b < kPer; b++) ys[b] = 0.f;
   float ss = 0.f;
-  const float4 *__restrict__ mg = (const float4 *)I0.m_il;
-  if (r < nr) {
+  const float4 *__restrict__ mg = (const float4 *)I0.m_il + part * kQuads;
+  if (r < nr && mine) {
     const int ia = (int)(r % D.na), ib = (int)(r / D.na);
     const float zd = G.z_det[ib];
     const RayMarch R = ray_setup(G, D, G.y_det[ia], zd);
@@ -741,12 +749,12 @@ __global__ void __launch_bounds__(kAxThreads)
       for (int j = 0; j < kP; j++) {
         if (!f[j]) continue;
         const float4 *p = mg + (size_t)id[j] * (kShareGroup / 4);
-        float4 x[kShareGroup / 4];
+        float4 x[kQuads];
 #pragma unroll
-        for (int q = 0; q < kShareGroup / 4; q++)
-          x[q] = ((active >> (4 * q)) & 0xFu) ? __ldg(p + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int q = 0; q < kQuads; q++)
+          x[q] = ((mine >> (4 * q)) & 0xFu) ? __ldg(p + q) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-        for (int q = 0; q < kShareGroup / 4; q++) {
+        for (int q = 0; q < kQuads; q++) {
           ys[4 * q] += w[j] * x[q].x;
           ys[4 * q + 1] += w[j] * x[q].y;
           ys[4 * q + 2] += w[j] * x[q].z;
@@ -757,20 +765,21 @@ __global__ void __launch_bounds__(kAxThreads)
     }
   }
 #pragma unroll
-  for (int q = 0; q < kShareGroup / 4; q++)
-    if ((active >> (4 * q)) & 0xFu) {
+  for (int q = 0; q < kQuads; q++)
+    if ((mine >> (4 * q)) & 0xFu) {
 #pragma unroll
       for (int j = 0; j < 4; j++) ys[4 * q + j] = warp_sum(ys[4 * q + j]);
     }
   ss = warp_sum(ss);
-  // lane b: the epilogue of k_sart_ax for instance g0 + b
+  // lane b: the epilogue of k_sart_ax for instance g0 + part * kPer + b
   float yb = 0.f;
 #pragma unroll
-  for (int b = 0; b < kShareGroup; b++)
+  for (int b = 0; b < kPer; b++)
     if (lane == b) yb = ys[b];
+  const int inst = part * kPer + lane;
   float p0 = 0.f, p1 = 0.f;
-  if (lane < gn && ((active >> lane) & 1u) && r < nr) {
-    const Inst &Ib = insts[g0 + lane];
+  if (lane < kPer && inst < gn && ((active >> inst) & 1u) && r < nr) {
+    const Inst &Ib = insts[g0 + inst];
     const float yv = yb * G.scale, srv = ss * G.scale;
     const float c0 = Ib.P[(long long)view * nr + r] - yv;
     const float cr = c0 / (srv == 0.f ? 1.f : srv);
@@ -778,14 +787,14 @@ __global__ void __launch_bounds__(kAxThreads)
     p0 = c0 * c0;
     p1 = isfinite(cr) ? 0.f : 1.f;
   }
-  if (lane < kShareGroup) {
-    s_part[0][warp][lane] = p0;
-    s_part[1][warp][lane] = p1;
+  if (lane < kPer) {
+    s_part[0][rw][inst] = p0;
+    s_part[1][rw][inst] = p1;
   }
   __syncthreads();
   // per instance: the block total of k_sart_ax's block_sum_f (lane 0 of each
-  // warp the only nonzero value; warps combined as (w0 + w2) + (w1 + w3)),
-  // its partial, its ticket
+  // of its 4 warps the only nonzero value; warps combined as
+  // (w0 + w2) + (w1 + w3)), its partial, its ticket
   static_assert(kAxWarps == 4, "block totals below follow block_sum_f for 4 warps");
   if (threadIdx.x < gn && ((active >> threadIdx.x) & 1u)) {
     const int b = threadIdx.x;
@@ -806,6 +815,7 @@ __global__ void __launch_bounds__(kAxThreads)
   for (int i = 0; i < nlast; i++) {
     const Inst &Ib = insts[g0 + s_last[i]];
     double tot[2];
+    // the final sum of k_sart_ax's reduction: its kAxThreads threads' order
     grid_sum_final<kAxThreads, 2>(Ib.partials, Ib.counter, ob.nblocks, tot);
     if (threadIdx.x == 0) {
       Ib.s->dd2_acc += tot[0];
@@ -915,9 +925,9 @@ cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
   const dim3 grid(blocks, 1, (batch + kShareGroup - 1) / kShareGroup);
   if (d.nz > 1 || d.nb > 1)
-    k_sart_ax_shared<true><<<grid, kAxThreads, 0, st>>>(insts, batch, view);
+    k_sart_ax_shared<true><<<grid, kAxSharedThreads, 0, st>>>(insts, batch, view);
   else
-    k_sart_ax_shared<false><<<grid, kAxThreads, 0, st>>>(insts, batch, view);
+    k_sart_ax_shared<false><<<grid, kAxSharedThreads, 0, st>>>(insts, batch, view);
   return cudaGetLastError();
 }
 

@@ -41,9 +41,10 @@ __device__ __forceinline__ void block_sum_f(const float (&v)[K], float (&out)[K]
 }
 
 // The last block's part of grid_sum: the FP64 totals of `nblocks` block
-// partials (K values each) in a fixed order -- each thread a strided
-// subset, a warp butterfly, then the warps in order -- and the ticket
-// reset.  Every thread of the block must call it; all get the totals.
+// partials (K values each) in a fixed order -- each of the first NT threads
+// a strided subset, a warp butterfly, then the warps in order -- and the
+// ticket reset.  Every thread of the block must call it (a block may have
+// more than NT threads; the others only wait); all get the totals.
 template <int NT, int K>
 __device__ __forceinline__ void grid_sum_final(const double *partials,
                                                unsigned *counter, int nblocks,
@@ -51,14 +52,16 @@ __device__ __forceinline__ void grid_sum_final(const double *partials,
   __shared__ double sh[K * (NT / 32)];
   __shared__ double bc[K];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const bool in = threadIdx.x < NT;  // warp-uniform (NT is a multiple of 32)
 #pragma unroll
   for (int k = 0; k < K; k++) {
     double a = 0.0;
-    for (int b = threadIdx.x; b < nblocks; b += NT)
-      a += ((volatile const double *)partials)[(long long)b * K + k];
+    if (in)
+      for (int b = threadIdx.x; b < nblocks; b += NT)
+        a += ((volatile const double *)partials)[(long long)b * K + k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if (lane == 0) sh[k * (NT / 32) + warp] = a;
+    if (lane == 0 && in) sh[k * (NT / 32) + warp] = a;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
