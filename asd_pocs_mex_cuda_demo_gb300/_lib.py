@@ -105,6 +105,10 @@ SIGNATURES = [
     ("asdpocs_plan_sinogram_ptr", C.c_void_p, [C.c_void_p, C.c_int]),
     ("asdpocs_plan_image_ptr", C.c_void_p, [C.c_void_p, C.c_int]),
     ("asdpocs_plan_time_phase", C.c_int, [C.c_void_p, C.c_int, C.c_int, _D]),
+    ("asdpocs_phantom_device", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _D, C.c_int,
+                                         C.c_double, C.c_void_p]),
+    ("asdpocs_poisson_noise_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong,
+                                               C.c_double, C.c_ulonglong, C.c_void_p]),
     ("asdpocs_server_config_default", None, [C.POINTER(ServerConfig)]),
     ("asdpocs_server_create", C.c_int, [C.POINTER(C.c_void_p), C.POINTER(ServerConfig)]),
     ("asdpocs_server_submit", C.c_int, [C.c_void_p, C.POINTER(Geometry), _D,

@@ -33,6 +33,7 @@ UNITS = {
     "host_api.cu": [],
     "noalloc.cu": [],
     "server.cu": [],
+    "phantom.cu": [],
 }
 
 

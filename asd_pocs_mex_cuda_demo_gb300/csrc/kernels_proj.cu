@@ -676,7 +676,7 @@ __global__ void __launch_bounds__(kAtxThreads, 3)
 // partials, reduction order and epilogue are those of k_sart_ax, so its
 // projection, residual, dd2 and flags are bit-identical to it.
 // ---------------------------------------------------------------------------
-constexpr int kAxSplit = 2;  // warps sharing one ray of a group
+constexpr int kAxSplit = 1;  // warps sharing one ray of a group (2 measured slower)
 constexpr int kAxSharedThreads = kAxThreads * kAxSplit;
 
 template <bool k3D>

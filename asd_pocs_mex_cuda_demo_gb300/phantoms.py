@@ -57,14 +57,30 @@ def ellipsoids(table, nx, ny, nz, zslices=None):
     gz = g[np.asarray(zslices)] if zslices is not None else g[:nz]
     # array index (r, c, k) -> point (x=g[c], y=g[r], z=g[k])
     Y, X, Z = np.meshgrid(gr, gc, gz, indexing="ij")
-    pts = np.stack([X.ravel(order="F"), Y.ravel(order="F"), Z.ravel(order="F")])
-    vol = np.zeros(pts.shape[1])
-    for A, a, b, c, x0, y0, z0, ph, th, ps in table:
-        q = _rot(np.deg2rad(ph), np.deg2rad(th), np.deg2rad(ps)) @ pts
-        inside = ((q[0] - x0) ** 2 / a ** 2 + (q[1] - y0) ** 2 / b ** 2
-                  + (q[2] - z0) ** 2 / c ** 2) <= 1
+    X, Y, Z = X.ravel(order="F"), Y.ravel(order="F"), Z.ravel(order="F")
+    vol = np.zeros(X.size)
+    # elementwise, one rounding per operation, in the order the device
+    # phantom (asdpocs_phantom_device) evaluates it
+    for row in ellipsoid_rows(table):
+        A, a, b, c, x0, y0, z0 = row[:7]
+        R = row[7:].reshape(3, 3)
+        q0 = R[0, 0] * X + R[0, 1] * Y + R[0, 2] * Z
+        q1 = R[1, 0] * X + R[1, 1] * Y + R[1, 2] * Z
+        q2 = R[2, 0] * X + R[2, 1] * Y + R[2, 2] * Z
+        inside = ((q0 - x0) ** 2 / (a * a) + (q1 - y0) ** 2 / (b * b)
+                  + (q2 - z0) ** 2 / (c * c)) <= 1
         vol[inside] += A
     return vol
+
+
+def ellipsoid_rows(table) -> np.ndarray:
+    """The table as the device phantom takes it: per ellipsoid A, a, b, c,
+    x0, y0, z0 and the 3 x 3 rotation (row-major), float64."""
+    rows = []
+    for A, a, b, c, x0, y0, z0, ph, th, ps in np.asarray(table, np.float64):
+        R = _rot(np.deg2rad(ph), np.deg2rad(th), np.deg2rad(ps))
+        rows.append(np.concatenate([[A, a, b, c, x0, y0, z0], R.ravel()]))
+    return np.array(rows, np.float64).reshape(-1, 16)
 
 
 def shepp_logan_3d(n: int) -> np.ndarray:
@@ -130,3 +146,33 @@ def poisson_noise(P: np.ndarray, I0: float, seed: int) -> np.ndarray:
     counts = rng.poisson(I0 * np.exp(-np.asarray(P, np.float64)))
     counts = np.maximum(counts, 1)
     return -np.log(counts / I0)
+
+
+# ----------------------------------------------------------------- device
+def ellipsoids_device(table, nx, ny, nz, out_ptr: int, scale: float = 1.0,
+                      stream: int = 0) -> None:
+    """The ellipsoid phantom of ``ellipsoids(table, nx, ny, nz) * scale`` as
+    float32, computed on the GPU into the device buffer at ``out_ptr``
+    (asdpocs_phantom_device; bit-identical to the host form)."""
+    import ctypes as C
+
+    from ._lib import check, load
+
+    rows = np.ascontiguousarray(ellipsoid_rows(table))
+    check(load().asdpocs_phantom_device(
+        C.c_void_p(out_ptr), int(nx), int(ny), int(nz),
+        rows.ctypes.data_as(C.POINTER(C.c_double)), int(rows.shape[0]), float(scale),
+        C.c_void_p(stream or None)))
+
+
+def poisson_noise_device(p_ptr: int, out_ptr: int, n: int, I0: float, seed: int,
+                         stream: int = 0) -> None:
+    """Poisson-noise sinogram on the GPU (asdpocs_poisson_noise_device): the
+    same model as ``poisson_noise``, from a counter-based generator."""
+    import ctypes as C
+
+    from ._lib import check, load
+
+    check(load().asdpocs_poisson_noise_device(C.c_void_p(p_ptr), C.c_void_p(out_ptr),
+                                              int(n), float(I0), int(seed),
+                                              C.c_void_p(stream or None)))

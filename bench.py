@@ -153,9 +153,10 @@ def phantom(W, seed):
 
 
 def make_inputs(W, seed0, device):
-    """Seeded phantoms, their projections (GPU projector, the launcher-level
-    geometry of the mex gateway) and Poisson-noise sinograms.  Setup only;
-    not timed.  Identical phantoms are generated once."""
+    """Seeded phantoms (the ellipsoid phantom generated on the device), their
+    projections (GPU projector, the launcher-level geometry of the mex
+    gateway) and Poisson-noise sinograms (device noise).  Setup only; not
+    timed.  Identical phantoms are generated once."""
     import torch
 
     from asd_pocs_mex_cuda_demo_gb300 import phantoms
@@ -180,8 +181,14 @@ def make_inputs(W, seed0, device):
         seed = seed0 + b
         key = seed if W["phantom"] == "ellipses" else 0
         if key not in cache:
-            x = phantom(W, seed)
-            xd = torch.tensor(x, device=device)
+            if W["phantom"] == "ellipses":
+                x = phantom(W, seed)
+                xd = torch.tensor(x, device=device)
+            else:  # the ellipsoid phantom, generated on the device
+                xd = torch.empty(nx * ny * nz, device=device)
+                phantoms.ellipsoids_device(phantoms.MODIFIED_SHEPP_LOGAN, nx, ny, nz,
+                                           xd.data_ptr(), scale=SHEPP_LOGAN_SCALE, stream=st)
+                x = xd.cpu().numpy()
             y = torch.empty(na * nb * nv, device=device)
             sr = torch.empty(na * nb, device=device)
             for v, a in enumerate(phi):
@@ -191,12 +198,15 @@ def make_inputs(W, seed0, device):
                                           ydet.data_ptr(), zdet.data_ptr(), so, od,
                                           float(sc), 1.0, nx, ny, nz, na, nb, st))
             torch.cuda.synchronize()
-            cache = {key: (x, y.cpu().numpy().astype(np.float64))}
-            del xd, y, sr
+            cache = {key: (x, y)}
+            del xd, sr
         x, clean = cache[key]
-        P = phantoms.poisson_noise(clean, W["I0"], seed=1000 + seed)
+        noisy = torch.empty_like(clean)  # Poisson noise on the device
+        phantoms.poisson_noise_device(clean.data_ptr(), noisy.data_ptr(), clean.numel(),
+                                      W["I0"], seed=1000 + seed, stream=st)
+        torch.cuda.synchronize()
         paras.append(para_for(W))
-        Ps.append(P.astype(np.float32))
+        Ps.append(noisy.cpu().numpy())
         I0s.append(x)
     return paras, [phi] * B, Ps, I0s
 
@@ -540,7 +550,10 @@ def serve_jobs(W, seed, device):
             SO, OD, det, I0 = 1000.0, 500.0, 0.8 * 256 / n, 5e4
             vx = 256.0 / n
             if n not in cache3:
-                cache3[n] = (phantoms.shepp_logan_3d(n) * SHEPP_LOGAN_SCALE).astype(np.float32)
+                xd3 = torch.empty(n * n * n, device=device)
+                phantoms.ellipsoids_device(phantoms.MODIFIED_SHEPP_LOGAN, n, n, n,
+                                           xd3.data_ptr(), scale=SHEPP_LOGAN_SCALE, stream=st)
+                cache3[n] = xd3.cpu().numpy()
             x = cache3[n]
         Wj = dict(nx=n, ny=n, nz=nz, na=na, nb=nb, nv=nv, SO=SO, OD=OD, det=det, vx=vx,
                   iters=iters, ng=20)
@@ -562,10 +575,11 @@ def serve_jobs(W, seed, device):
                                       ydet.data_ptr(), zdet.data_ptr(),
                                       float(np.float32(SO) / sc), float(np.float32(OD) / sc),
                                       float(sc), 1.0, n, n, nz, na, nb, st))
+        phantoms.poisson_noise_device(y.data_ptr(), y.data_ptr(), y.numel(), I0,
+                                      seed=7000 + k, stream=st)
         torch.cuda.synchronize()
-        P = phantoms.poisson_noise(y.cpu().numpy().astype(np.float64), I0, seed=7000 + k)
         para = dict(para_for(Wj), phi_vec=phi)
-        jobs.append(dict(t=t, para=para, P=P.astype(np.float32), x=x,
+        jobs.append(dict(t=t, para=para, P=y.cpu().numpy(), x=x,
                          kind="2d" if nz == 1 else "3d"))
     return jobs
 

@@ -242,6 +242,30 @@ int SART_cuda_inline(const double *P, const double *phi_vec_deg,
                      const double *m0, double *m_out, double *dataTolerance);
 
 /* ---------------------------------------------------------------------
+ * Device-side synthetic inputs (utilities/phantom3d.m semantics), so
+ * benchmark and serving inputs need no host round trip.
+ * --------------------------------------------------------------------- */
+
+/* vol_d[nx*ny*nz] (x fastest) = scale * the sum of the amplitudes of the
+ * ellipsoids containing each voxel's point on phantom3d.m's grid (n = the
+ * largest dimension, points in [-1, 1]; voxel (r, c, k) at x = g[c],
+ * y = g[r], z = g[k]).  ellipsoids: n_ellipsoids rows of 16 doubles --
+ * amplitude, semi-axes a, b, c, centre x0, y0, z0, then the 3 x 3 rotation
+ * row-major (q = R p) -- at most 32 rows.  FP64 with one rounding per
+ * operation, so the host restatement gives the same volume bit for bit.
+ * Asynchronous on `stream`. */
+int asdpocs_phantom_device(float *vol_d, int nx, int ny, int nz,
+                           const double *ellipsoids, int n_ellipsoids,
+                           double scale, void *stream);
+
+/* out_d[i] = -ln(max(k, 1) / I0) with k ~ Poisson(I0 * exp(-p_d[i])), from
+ * a counter-based generator keyed by `seed` (the value of element i depends
+ * on seed and i only).  out_d may equal p_d.  Asynchronous on `stream`. */
+int asdpocs_poisson_noise_device(const float *p_d, float *out_d, long long n,
+                                 double I0, unsigned long long seed,
+                                 void *stream);
+
+/* ---------------------------------------------------------------------
  * Serving queue (no counterpart in the reference, whose drivers run one
  * reconstruction at a time).  Jobs of any geometry, view count and
  * iteration budget are submitted at any time.  A worker thread admits them
