@@ -15,7 +15,6 @@ namespace asd {
 namespace {
 
 constexpr int kAxWarps = 4;             // rays per Ax block
-constexpr int kAxThreads = kAxWarps * 32;
 constexpr int kAtxThreads = kTileThreads;
 constexpr int kTabA = 512;              // detector columns staged per block
 constexpr int kTabC = 1536;             // 3D rays staged per block
@@ -31,35 +30,67 @@ int atx_blocks(const Dims &d) {
 }
 
 // ------------------------------------------------------------------- Ax
-// Partial sums of one ray in the lanes of a warp, reduced to every lane.
+// A ray's columns are dealt to kAxCols warps: lane l of warp part p takes
+// columns l + 32 p, l + 32 p + 32 kAxCols, ...  The parts' lane partials are
+// added in part order (through shared memory), then the lanes by the xor
+// butterfly.  Every forward kernel sums a ray this way, so a ray's total
+// does not depend on the kernel that computed it.
+constexpr int kAxCols = 2;
+constexpr int kAxBlock = kAxWarps * kAxCols * 32;  // threads per block
+
+// This lane's partial sums of ray r over its columns (no cross-lane sum).
 template <class Loader>
-__device__ __forceinline__ void ax_warp(const ViewGeo &G, const Dims &D,
-                                        long long r, int lane, Loader ld,
-                                        float &ys, float &ss) {
+__device__ __forceinline__ void ax_lane_partial(const ViewGeo &G, const Dims &D,
+                                                long long r, int first, Loader ld,
+                                                float &ys, float &ss) {
   const int ia = (int)(r % D.na), ib = (int)(r / D.na);
   const float zd = G.z_det[ib];
   const RayMarch R = ray_setup(G, D, G.y_det[ia], zd);
   ys = 0.f;
   ss = 0.f;
   if (D.nz == 1 && zd == 0.0f)
-    ray_columns_planar_fast<2>(R, lane, 32, ld, ys, ss);
+    ray_columns_planar_fast<2>(R, first, 32 * kAxCols, ld, ys, ss);
   else
-    ray_columns_fast<2>(R, lane, 32, ld, ys, ss);
-  ys = warp_sum(ys);
-  ss = warp_sum(ss);
+    ray_columns_fast<2>(R, first, 32 * kAxCols, ld, ys, ss);
 }
 
-__global__ void __launch_bounds__(kAxThreads)
+// The block's ray totals: each warp stores its lane partials of the K values
+// in sp[part][ray][k][lane]; after the barrier the part-0 warps add the parts
+// in order and sum their lanes.  Every thread of the block must call it.
+template <int K>
+__device__ __forceinline__ void ax_combine(float (&sp)[kAxCols][kAxWarps][K][32],
+                                           float (&v)[K], int part, int rw,
+                                           int lane) {
+#pragma unroll
+  for (int k = 0; k < K; k++) sp[part][rw][k][lane] = v[k];
+  __syncthreads();
+  if (part == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      float t = sp[0][rw][k][lane];
+#pragma unroll
+      for (int p = 1; p < kAxCols; p++) t += sp[p][rw][k][lane];
+      v[k] = warp_sum(t);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kAxBlock)
     k_ax(const float *__restrict__ x, float *__restrict__ y,
          float *__restrict__ sr, ViewGeo G, Dims D) {
-  const int lane = threadIdx.x & 31;
-  const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
-  if (r >= (long long)D.na * D.nb) return;  // whole warp exits together
-  float ys, ss;
-  ax_warp(G, D, r, lane, [&](unsigned i) { return __ldg(x + i); }, ys, ss);
-  if (lane == 0) {
-    y[r] = ys * G.scale;
-    sr[r] = ss * G.scale;
+  __shared__ float sp[kAxCols][kAxWarps][2][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rw = warp % kAxWarps, part = warp / kAxWarps;
+  const long long r = (long long)blockIdx.x * kAxWarps + rw;
+  const bool in = r < (long long)D.na * D.nb;
+  float v[2] = {0.f, 0.f};
+  if (in)
+    ax_lane_partial(G, D, r, lane + 32 * part,
+                    [&](unsigned i) { return __ldg(x + i); }, v[0], v[1]);
+  ax_combine<2>(sp, v, part, rw, lane);
+  if (in && part == 0 && lane == 0) {
+    y[r] = v[0] * G.scale;
+    sr[r] = v[1] * G.scale;
   }
 }
 
@@ -291,8 +322,9 @@ __global__ void __launch_bounds__(128)
 // backward step that follows (Inst::tabc_mode: a shared table's writer does
 // so even after its own iterations have ended).
 template <bool k3D>
-__global__ void __launch_bounds__(kAxThreads)
+__global__ void __launch_bounds__(kAxBlock)
     k_sart_ax(const Inst *__restrict__ insts, int view) {
+  __shared__ float sp[kAxCols][kAxWarps][2][32];
   const Inst &I = insts[blockIdx.z];
   if (view >= I.nv) return;
   const bool done = ((volatile int *)&I.s->done)[0] != 0;
@@ -303,29 +335,32 @@ __global__ void __launch_bounds__(kAxThreads)
   const OwnBlock ob = own_block(dim3((unsigned)((nr + kAxWarps - 1) / kAxWarps), 1));
   if (ob.bid < 0) return;
   const ViewGeo G = view_of(I, view);
-  const int lane = threadIdx.x & 31;
-  const long long r = (long long)blockIdx.x * kAxWarps + (threadIdx.x >> 5);
-  if (tabc && lane == 0 && r < nr) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rw = warp % kAxWarps, part = warp / kAxWarps;
+  const long long r = (long long)blockIdx.x * kAxWarps + rw;
+  if (tabc && part == 0 && lane == 0 && r < nr) {
     const int ia = (int)(r % D.na), ib = (int)(r / D.na);
     I.tabC[r] = ray_tab_c(I.tabA[(long long)view * D.na + ia], G.z_det[ib]);
   }
   if (done) return;  // the whole instance: no reduction
-  float part[2] = {0.f, 0.f};  // dd2, non-finite residuals
+  float v[2] = {0.f, 0.f};
   if (r < nr) {
-    float ys, ss;
     const float *m = I.m;
-    ax_warp(G, D, r, lane, [&](unsigned i) { return m[i]; }, ys, ss);
-    if (lane == 0) {
-      const float yv = ys * G.scale, srv = ss * G.scale;
-      const float c0 = I.P[(long long)view * nr + r] - yv;
-      const float cr = c0 / (srv == 0.f ? 1.f : srv);
-      I.cor[r * I.cor_stride] = cr;
-      part[0] = c0 * c0;
-      part[1] = isfinite(cr) ? 0.f : 1.f;
-    }
+    ax_lane_partial(G, D, r, lane + 32 * part, [&](unsigned i) { return m[i]; }, v[0],
+                    v[1]);
+  }
+  ax_combine<2>(sp, v, part, rw, lane);
+  float pt[2] = {0.f, 0.f};  // dd2, non-finite residuals
+  if (r < nr && part == 0 && lane == 0) {
+    const float yv = v[0] * G.scale, srv = v[1] * G.scale;
+    const float c0 = I.P[(long long)view * nr + r] - yv;
+    const float cr = c0 / (srv == 0.f ? 1.f : srv);
+    I.cor[r * I.cor_stride] = cr;
+    pt[0] = c0 * c0;
+    pt[1] = isfinite(cr) ? 0.f : 1.f;
   }
   double tot[2];
-  if (grid_sum<kAxThreads, 2>(part, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
+  if (grid_sum<kAxBlock, 2>(pt, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
     if (threadIdx.x == 0) {
       I.s->dd2_acc += tot[0];
       I.s->cor_finite = tot[1] == 0.0;
@@ -485,7 +520,7 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 // reference's order, so the result is bit-identical to k_sart_atx.
 // ---------------------------------------------------------------------------
 constexpr int kShareGroup = kShareSlots;
-constexpr int kPairChunk = 4;
+constexpr int kPairChunk = 2;
 
 // The voxel of this thread for the group (see k_sart_atx_shared).
 template <bool kPlanar, int AX>
@@ -622,7 +657,7 @@ __device__ __forceinline__ void atx_shared_voxel(
 }
 
 template <bool kPlanar>
-__global__ void __launch_bounds__(kAtxThreads, 3)
+__global__ void __launch_bounds__(kAtxThreads, 4)
     k_sart_atx_shared(const Inst *__restrict__ insts, int batch, int view) {
   __shared__ float s_beta[kShareGroup];
   __shared__ unsigned s_active;
@@ -676,16 +711,12 @@ __global__ void __launch_bounds__(kAtxThreads, 3)
 // partials, reduction order and epilogue are those of k_sart_ax, so its
 // projection, residual, dd2 and flags are bit-identical to it.
 // ---------------------------------------------------------------------------
-constexpr int kAxSplit = 1;  // warps sharing one ray of a group (2 measured slower)
-constexpr int kAxSharedThreads = kAxThreads * kAxSplit;
-
 template <bool k3D>
-__global__ void __launch_bounds__(kAxSharedThreads)
+__global__ void __launch_bounds__(kAxBlock)
     k_sart_ax_shared(const Inst *__restrict__ insts, int batch, int view) {
-  // warp w marches ray (w % kAxWarps) of the block for instances
-  // [(w / kAxWarps) * kPer, + kPer) of the group
-  constexpr int kPer = kShareGroup / kAxSplit, kQuads = kPer / 4;
+  constexpr int kQuads = kShareGroup / 4;
   __shared__ unsigned s_active;
+  __shared__ float sp[kAxCols][kAxWarps][kShareGroup + 1][32];
   __shared__ float s_part[2][kAxWarps][kShareGroup];
   __shared__ int s_last[kShareGroup];
   __shared__ int s_nlast;
@@ -718,18 +749,16 @@ __global__ void __launch_bounds__(kAxSharedThreads)
     I0.tabC[r] = ray_tab_c(I0.tabA[(long long)view * D.na + ia], G.z_det[ib]);
   }
   if (!active) return;
-  const unsigned mine = (active >> (part * kPer)) & ((1u << kPer) - 1u);
-  float ys[kPer];
+  float v[kShareGroup + 1];  // the instances' sums, then the weights' sum
 #pragma unroll
-  for (int b = 0; b < kPer; b++) ys[b] = 0.f;
-  float ss = 0.f;
-  const float4 *__restrict__ mg = (const float4 *)I0.m_il + part * kQuads;
-  if (r < nr && mine) {
+  for (int b = 0; b <= kShareGroup; b++) v[b] = 0.f;
+  const float4 *__restrict__ mg = (const float4 *)I0.m_il;
+  if (r < nr) {
     const int ia = (int)(r % D.na), ib = (int)(r / D.na);
     const float zd = G.z_det[ib];
     const RayMarch R = ray_setup(G, D, G.y_det[ia], zd);
     const bool planar = D.nz == 1 && zd == 0.0f;
-    for (int iu = lane; iu < R.nu; iu += 32) {
+    for (int iu = lane + 32 * part; iu < R.nu; iu += 32 * kAxCols) {
       constexpr int kP = 3;
       unsigned id[kP];
       float w[kP];
@@ -748,52 +777,45 @@ __global__ void __launch_bounds__(kAxSharedThreads)
 #pragma unroll
       for (int j = 0; j < kP; j++) {
         if (!f[j]) continue;
-        const float4 *p = mg + (size_t)id[j] * (kShareGroup / 4);
+        const float4 *p = mg + (size_t)id[j] * kQuads;
         float4 x[kQuads];
 #pragma unroll
         for (int q = 0; q < kQuads; q++)
-          x[q] = ((mine >> (4 * q)) & 0xFu) ? __ldg(p + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+          x[q] = ((active >> (4 * q)) & 0xFu) ? __ldg(p + q) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int q = 0; q < kQuads; q++) {
-          ys[4 * q] += w[j] * x[q].x;
-          ys[4 * q + 1] += w[j] * x[q].y;
-          ys[4 * q + 2] += w[j] * x[q].z;
-          ys[4 * q + 3] += w[j] * x[q].w;
+          v[4 * q] += w[j] * x[q].x;
+          v[4 * q + 1] += w[j] * x[q].y;
+          v[4 * q + 2] += w[j] * x[q].z;
+          v[4 * q + 3] += w[j] * x[q].w;
         }
-        ss += w[j];
+        v[kShareGroup] += w[j];
       }
     }
   }
-#pragma unroll
-  for (int q = 0; q < kQuads; q++)
-    if ((mine >> (4 * q)) & 0xFu) {
-#pragma unroll
-      for (int j = 0; j < 4; j++) ys[4 * q + j] = warp_sum(ys[4 * q + j]);
-    }
-  ss = warp_sum(ss);
-  // lane b: the epilogue of k_sart_ax for instance g0 + part * kPer + b
+  ax_combine<kShareGroup + 1>(sp, v, part, rw, lane);
+  // part-0 lane b: the epilogue of k_sart_ax for instance g0 + b
   float yb = 0.f;
 #pragma unroll
-  for (int b = 0; b < kPer; b++)
-    if (lane == b) yb = ys[b];
-  const int inst = part * kPer + lane;
+  for (int b = 0; b < kShareGroup; b++)
+    if (lane == b) yb = v[b];
   float p0 = 0.f, p1 = 0.f;
-  if (lane < kPer && inst < gn && ((active >> inst) & 1u) && r < nr) {
-    const Inst &Ib = insts[g0 + inst];
-    const float yv = yb * G.scale, srv = ss * G.scale;
+  if (part == 0 && lane < gn && ((active >> lane) & 1u) && r < nr) {
+    const Inst &Ib = insts[g0 + lane];
+    const float yv = yb * G.scale, srv = v[kShareGroup] * G.scale;
     const float c0 = Ib.P[(long long)view * nr + r] - yv;
     const float cr = c0 / (srv == 0.f ? 1.f : srv);
     Ib.cor[r * Ib.cor_stride] = cr;
     p0 = c0 * c0;
     p1 = isfinite(cr) ? 0.f : 1.f;
   }
-  if (lane < kPer) {
-    s_part[0][rw][inst] = p0;
-    s_part[1][rw][inst] = p1;
+  if (part == 0 && lane < kShareGroup) {
+    s_part[0][rw][lane] = p0;
+    s_part[1][rw][lane] = p1;
   }
   __syncthreads();
-  // per instance: the block total of k_sart_ax's block_sum_f (lane 0 of each
-  // of its 4 warps the only nonzero value; warps combined as
+  // per instance: the block total of k_sart_ax's block_sum_f (lane 0 of the
+  // part-0 warps 0..3 the only nonzero values; combined as
   // (w0 + w2) + (w1 + w3)), its partial, its ticket
   static_assert(kAxWarps == 4, "block totals below follow block_sum_f for 4 warps");
   if (threadIdx.x < gn && ((active >> threadIdx.x) & 1u)) {
@@ -801,8 +823,8 @@ __global__ void __launch_bounds__(kAxSharedThreads)
     const Inst &Ib = insts[g0 + b];
 #pragma unroll
     for (int k = 0; k < 2; k++) {
-      const float v = (s_part[k][0][b] + s_part[k][2][b]) + (s_part[k][1][b] + s_part[k][3][b]);
-      Ib.partials[(long long)ob.bid * 2 + k] = (double)v;
+      const float t = (s_part[k][0][b] + s_part[k][2][b]) + (s_part[k][1][b] + s_part[k][3][b]);
+      Ib.partials[(long long)ob.bid * 2 + k] = (double)t;
     }
     __threadfence();
     if (atomicAdd(Ib.counter, 1u) == (unsigned)ob.nblocks - 1)
@@ -815,8 +837,8 @@ __global__ void __launch_bounds__(kAxSharedThreads)
   for (int i = 0; i < nlast; i++) {
     const Inst &Ib = insts[g0 + s_last[i]];
     double tot[2];
-    // the final sum of k_sart_ax's reduction: its kAxThreads threads' order
-    grid_sum_final<kAxThreads, 2>(Ib.partials, Ib.counter, ob.nblocks, tot);
+    // the final sum of k_sart_ax's reduction (its kAxBlock threads' order)
+    grid_sum_final<kAxBlock, 2>(Ib.partials, Ib.counter, ob.nblocks, tot);
     if (threadIdx.x == 0) {
       Ib.s->dd2_acc += tot[0];
       Ib.s->cor_finite = tot[1] == 0.0;
@@ -873,7 +895,7 @@ cudaError_t launch_ax(const float *x, float *y, float *sr, const ViewGeo &g,
   const long long nr = (long long)d.na * d.nb;
   if (nr == 0) return cudaSuccess;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
-  k_ax<<<blocks, kAxThreads, 0, st>>>(x, y, sr, g, d);
+  k_ax<<<blocks, kAxBlock, 0, st>>>(x, y, sr, g, d);
   return cudaGetLastError();
 }
 
@@ -892,9 +914,9 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
   if (d.nz > 1 || d.nb > 1)
-    k_sart_ax<true><<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, view);
+    k_sart_ax<true><<<dim3(blocks, 1, batch), kAxBlock, 0, st>>>(insts, view);
   else
-    k_sart_ax<false><<<dim3(blocks, 1, batch), kAxThreads, 0, st>>>(insts, view);
+    k_sart_ax<false><<<dim3(blocks, 1, batch), kAxBlock, 0, st>>>(insts, view);
   return cudaGetLastError();
 }
 
@@ -925,9 +947,9 @@ cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
   const dim3 grid(blocks, 1, (batch + kShareGroup - 1) / kShareGroup);
   if (d.nz > 1 || d.nb > 1)
-    k_sart_ax_shared<true><<<grid, kAxSharedThreads, 0, st>>>(insts, batch, view);
+    k_sart_ax_shared<true><<<grid, kAxBlock, 0, st>>>(insts, batch, view);
   else
-    k_sart_ax_shared<false><<<grid, kAxSharedThreads, 0, st>>>(insts, batch, view);
+    k_sart_ax_shared<false><<<grid, kAxBlock, 0, st>>>(insts, batch, view);
   return cudaGetLastError();
 }
 

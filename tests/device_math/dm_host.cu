@@ -37,6 +37,8 @@ extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,
     const int ia = (int)(r % na), ib = (int)(r / na);
     const RayMarch R = ray_setup(G, D, yd[ia], zd[ib]);
     const bool planar = nz == 1 && zd[ib] == 0.0f;
+    py.assign(lanes, 0.f);
+    ps.assign(lanes, 0.f);
     for (int l = 0; l < lanes; l++) {
       float a = 0.f, b = 0.f;
       auto ld = [&](long long i) { return x[i]; };
@@ -55,10 +57,22 @@ extern "C" void dm_ax(const float *x, float *y, float *sr, float c, float s,
       py[l] = a;
       ps[l] = b;
     }
+    // more than 32 partials: kAxCols warps share the ray's columns; their
+    // lane partials are added in part order before the lanes are summed
+    if (lanes > 32) {
+      for (int l = 0; l < 32; l++)
+        for (int q = 1; q < lanes / 32; q++) {
+          py[l] += py[l + 32 * q];
+          ps[l] += ps[l + 32 * q];
+        }
+      py.resize(32);
+      ps.resize(32);
+    }
+    const int nl = lanes > 32 ? 32 : lanes;
     // xor butterfly (warp_sum): every lane ends with the same total
-    for (int o = lanes / 2; o > 0; o >>= 1) {
+    for (int o = nl / 2; o > 0; o >>= 1) {
       std::vector<float> ny_(py), ns_(ps);
-      for (int l = 0; l < lanes; l++) {
+      for (int l = 0; l < nl; l++) {
         ny_[l] = py[l] + py[l ^ o];
         ns_[l] = ps[l] + ps[l ^ o];
       }

@@ -259,3 +259,58 @@ def test_shared_geometry_cone_beam_instances_finishing_apart(gpu):
         pl.run()
         for k in range(len(paras)):
             assert np.array_equal(pl.image(k), alone[k]), k
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1, 3, 1), (3, 17, 1, 1, 1), (17, 9, 5, 33, 7)])
+def test_plan_edge_shapes_vs_oracle(gpu, oracle_mod, dims):
+    """Degenerate and odd sizes (a single voxel, a single bin, odd cone-beam
+    sizes) through the whole device iteration, against the oracle."""
+    nx, ny, nz, na, nb = dims
+    SO, OD, det = 300.0, 200.0, 1.3
+    vx = phantoms.fov_voxel_size(SO, OD, det, max(na, 2), nx)
+    rng = np.random.default_rng(sum(dims))
+    phi = phantoms.views(6) + 3.0
+    para = dict(SO=SO, OD=OD, vxlsize=vx, nx=nx, ny=ny, nz=nz, na=na, nb=nb, detsize=det,
+                phi_vec=phi, maxnumIter=3, numOfgradients=4, alpha=0.002)
+    P = rng.random((na * nb, len(phi)))
+    m, out = pkg.ASD_POCS_cuda(P, para)
+    mo, oo = oracle_mod.asdpocs(P, para)
+    assert out["IterationNum"] == oo["IterationNum"]
+    assert rel_l2(m.ravel(order="F"), mo) < 1e-4 or np.abs(m.ravel(order="F") - mo).max() < 1e-6
+
+
+def test_zero_iterations_returns_initial_image(gpu):
+    n, na = 16, 24
+    para = dict(SO=541.0, OD=408.0, vxlsize=phantoms.fov_voxel_size(541, 408, 1.0, na, n),
+                nx=n, ny=n, nz=1, na=na, nb=1, detsize=1.0, phi_vec=phantoms.views(5),
+                maxnumIter=0)
+    m0 = np.random.default_rng(3).random((n, n))
+    m, out = pkg.ASD_POCS_cuda(np.ones((na, 5)), dict(para, m0=m0))
+    assert out["IterationNum"] == 0
+    assert np.array_equal(m.ravel(order="F"), m0.ravel(order="F").astype(np.float32))
+
+
+def test_shared_geometry_groups_with_remainder(gpu):
+    """37 instances of one protocol: two full groups of 16 and one of 5, each
+    result equal to its run alone."""
+    n, na, nv = 16, 24, 8
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = phantoms.fov_voxel_size(SO, OD, det, na, n)
+    phi = phantoms.views(nv)
+    rng = np.random.default_rng(11)
+    paras = [dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, na=na, nb=1, detsize=det,
+                  phi_vec=phi, maxnumIter=int(rng.integers(1, 4)),
+                  numOfgradients=int(rng.integers(0, 4)), alpha=0.02) for _ in range(37)]
+    Ps = [rng.random(na * nv).astype(np.float32) for _ in range(37)]
+    with pkg.Plan(paras, [phi] * 37) as pl:
+        for k, P in enumerate(Ps):
+            pl.set_sinogram(k, P)
+        pl.reset()
+        pl.run()
+        batch = [pl.image(k) for k in range(37)]
+    for k in (0, 15, 16, 31, 32, 36):
+        with pkg.Plan(paras[k], phi) as pl:
+            pl.set_sinogram(0, Ps[k])
+            pl.reset()
+            pl.run()
+            assert np.array_equal(pl.image(0), batch[k]), k
