@@ -34,8 +34,10 @@ int atx_blocks(const Dims &d) {
 // columns l + 32 p, l + 32 p + 32 kAxCols, ...  The parts' lane partials are
 // added in part order (through shared memory), then the lanes by the xor
 // butterfly.  Every forward kernel sums a ray this way, so a ray's total
-// does not depend on the kernel that computed it.
-constexpr int kAxCols = 2;
+// does not depend on the kernel that computed it.  One warp per ray
+// measured fastest for batches and cone beam (two: 14 % slower for a batch
+// of 64 and 27 % for 256^3, 7 % faster for one 512^2 instance).
+constexpr int kAxCols = 1;
 constexpr int kAxBlock = kAxWarps * kAxCols * 32;  // threads per block
 
 // This lane's partial sums of ray r over its columns (no cross-lane sum).
@@ -61,6 +63,11 @@ template <int K>
 __device__ __forceinline__ void ax_combine(float (&sp)[kAxCols][kAxWarps][K][32],
                                            float (&v)[K], int part, int rw,
                                            int lane) {
+  if constexpr (kAxCols == 1) {
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = warp_sum(v[k]);
+    return;
+  }
 #pragma unroll
   for (int k = 0; k < K; k++) sp[part][rw][k][lane] = v[k];
   __syncthreads();

@@ -419,95 +419,146 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// 2-D TV step over the block's whole group of kTilesPerBlock tiles as one
-// 32 x 32 voxel tile.  The update m' = m - coef * v(m) needs the stencil v of
-// the step's starting image, which the previous step (or the end-of-sweep
-// kernel) evaluated for its norm and stored: the step reads m and v on the
-// group plus a one-voxel halo, forms m' there (34 x 34) without a stencil,
-// writes its four voxels per thread (rows ty, ty+8, ty+16, ty+24) and
-// evaluates one stencil per voxel -- v(m'), for the next norm, stored for the
-// next step.  The values are those of recomputing v here, so the results do
-// not change; the work per voxel drops from 2.13 stencils to one, for 8 more
-// bytes of traffic.
+// 2-D TV step.  A group is the block's kTilesPerBlock tiles as one 32 x 32
+// voxel tile.  The update m' = m - coef * v(m) needs the stencil v of the
+// step's starting image, which the previous step (or the end-of-sweep
+// kernel) evaluated for its norm and stored, so a group stages m and v on
+// the group plus a one-voxel halo (34 x 34), forms m' there without a
+// stencil, writes its four voxels per thread (rows ty, ty+8, ty+16, ty+24)
+// and evaluates one stencil per voxel -- v(m'), for the next norm, stored for
+// the next step.  The values are those of recomputing v here.
+//
+// A block walks `per_block` consecutive groups of its instance, staging the
+// next group's halo with cp.async (zero-filled outside the image) while it
+// evaluates the current one, and leaves one partial per group; the last
+// block of the instance sums the partials in group order.  The result is
+// therefore the same for every `per_block`, which the host picks from the
+// batch size (long-lived blocks for large batches, one group per block for
+// one instance).
 constexpr int kGroupRows = kTileY * kTilesPerBlock;
+constexpr int kHaloW = kTileX + 2, kHaloH = kGroupRows + 2, kHaloN = kHaloW * kHaloH;
+constexpr int kHaloRounds = (kHaloN + kThreads - 1) / kThreads;
+
+__device__ __forceinline__ void cp_async4(float *smem, const float *gmem, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem),
+               "r"(valid ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
 
 __global__ void __launch_bounds__(kThreads)
-    k_tv_step2d(const Inst *__restrict__ insts, int step) {
-  __shared__ float s1[kGroupRows + 2][kTileX + 2];
+    k_tv_step2d(const Inst *__restrict__ insts, int step, int per_block) {
+  __shared__ float sm[2][kHaloH][kHaloW];  // m on the halo region, then m'
+  __shared__ float sv[2][kHaloH][kHaloW];  // v(m) on the halo region
+  __shared__ float shf[kThreads / 32];
+  __shared__ int s_last;
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
   if (step >= ng) return;
   const Dims D = I.d;
-  const OwnBlock ob = own_block(group_grid(D.nx, D.ny, 1, 1));
-  if (ob.bid < 0) return;
+  const dim3 gg = group_grid(D.nx, D.ny, 1, 1);
+  const int G = (int)(gg.x * gg.y);
+  const int nb = (G + per_block - 1) / per_block;
+  if ((int)blockIdx.x >= nb) return;
+  const int g_begin = blockIdx.x * per_block, g_end = min(G, g_begin + per_block);
   const bool last = step == ng - 1;
   const bool fused_finish = last && ng >= 2;
   const float coef = I.s->tv_coef_f;
   const float *src = tv_src(I, step);
   float *dst = tv_dst(I, step);
-  const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
-  const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kGroupRows;
-  // m' = m - coef * v(m) on the group and a one-voxel halo (zero outside the
-  // image), with v(m) read from the previous step (the end-of-sweep kernel
-  // for the first step): the same values the stencil would give, so no
-  // stencil is evaluated here.  The points are dealt to the threads in
-  // fixed-count unrolled rounds, so each thread has its loads in flight
-  // together.
   const float *vin = tv_v(I, step);
   float *vout = tv_v(I, step + 1);
-  constexpr int W1 = kTileX + 2, N1 = W1 * (kGroupRows + 2);
+  const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
+  auto stage = [&](int g, int buf) {
+    const int x0 = (g % (int)gg.x) * kTileX, y0 = (g / (int)gg.x) * kGroupRows;
 #pragma unroll
-  for (int j = 0; j < (N1 + kThreads - 1) / kThreads; j++) {
-    const int k = threadIdx.x + j * kThreads;
-    const int r = k / W1, c = k - r * W1;
-    const int y = y0 - 1 + r, x = x0 - 1 + c;
-    if (k < N1) {
-      float val = 0.f;
-      if (y >= 0 && y < D.ny && x >= 0 && x < D.nx) {
-        const unsigned i = (unsigned)y * D.nx + x;
-        val = src[i] - coef * vin[i];
+    for (int j = 0; j < kHaloRounds; j++) {
+      const int k = threadIdx.x + j * kThreads;
+      if (k < kHaloN) {
+        const int r = k / kHaloW, c = k - r * kHaloW;
+        const int y = y0 - 1 + r, x = x0 - 1 + c;
+        const bool in = y >= 0 && y < D.ny && x >= 0 && x < D.nx;
+        const unsigned i = in ? (unsigned)y * D.nx + x : 0u;
+        cp_async4(&sm[buf][r][c], src + i, in);
+        cp_async4(&sv[buf][r][c], vin + i, in);
       }
-      s1[r][c] = val;
     }
-  }
-  __syncthreads();
-  float v[1] = {0.f};
+    cp_async_commit();
+  };
+  stage(g_begin, 0);
+  for (int g = g_begin; g < g_end; g++) {
+    const int buf = (g - g_begin) & 1;
+    cp_async_wait_all();
+    __syncthreads();
+    // m' = m - coef * v in place (zero outside the image: staged as zeros)
 #pragma unroll
-  for (int k = 0; k < kTilesPerBlock; k++) {
-    const int r = ty + kTileY * k;
-    const int ix = x0 + tx, iy = y0 + r;
-    if (ix < D.nx && iy < D.ny) {
-      const unsigned i = (unsigned)iy * D.nx + ix;
-      const auto u = [&](int dx, int dy, int) { return s1[r + 1 + dy][tx + 1 + dx]; };
-      const float mn = u(0, 0, 0);
-      if (fused_finish) {
-        const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
-        const float f0 = I.m[i];
-        const float dlt = mc - f0;
-        v[0] += dlt * dlt;
-        I.m[i] = mc;
-        I.m_pre[i] = mc;
-      } else {
-        dst[i] = mn;
-        if (!last) {
-          const float gr = tv_grad2<float>(u);
-          v[0] += gr * gr;
-          vout[i] = gr;  // the next step's update reads it
+    for (int j = 0; j < kHaloRounds; j++) {
+      const int k = threadIdx.x + j * kThreads;
+      if (k < kHaloN) {
+        const int r = k / kHaloW, c = k - r * kHaloW;
+        sm[buf][r][c] = sm[buf][r][c] - coef * sv[buf][r][c];
+      }
+    }
+    __syncthreads();
+    // the next group's halo arrives while this one is evaluated (its buffer
+    // was last read two groups ago, before the barrier above)
+    if (g + 1 < g_end) stage(g + 1, buf ^ 1);
+    const int x0 = (g % (int)gg.x) * kTileX, y0 = (g / (int)gg.x) * kGroupRows;
+    float v = 0.f;
+#pragma unroll
+    for (int k = 0; k < kTilesPerBlock; k++) {
+      const int r = ty + kTileY * k;
+      const int ix = x0 + tx, iy = y0 + r;
+      if (ix < D.nx && iy < D.ny) {
+        const unsigned i = (unsigned)iy * D.nx + ix;
+        const auto u = [&](int dx, int dy, int) { return sm[buf][r + 1 + dy][tx + 1 + dx]; };
+        const float mn = u(0, 0, 0);
+        if (fused_finish) {
+          const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
+          const float f0 = I.m[i];
+          const float dlt = mc - f0;
+          v += dlt * dlt;
+          I.m[i] = mc;
+          I.m_pre[i] = mc;
+        } else {
+          dst[i] = mn;
+          if (!last) {
+            const float gr = tv_grad2<float>(u);
+            v += gr * gr;
+            vout[i] = gr;  // the next step's update reads it
+          }
         }
       }
     }
+    // this group's partial (block_sum_f ends with a barrier)
+    const float vv[1] = {v};
+    float bs[1];
+    block_sum_f<kThreads, 1>(vv, bs, shf);
+    if (threadIdx.x == 0) I.partials[g] = (double)bs[0];
   }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(I.counter, 1u) == (unsigned)nb - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
   double tot[1];
-  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
-    if (threadIdx.x == 0) {
-      Scalars *s = I.s;
-      if (fused_finish) {
-        finish_scalars(s, tot[0]);
-      } else if (!last) {
-        s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
-        s->tv_coef_f = (float)s->tv_coef;
-      }
+  grid_sum_final<kThreads, 1>(I.partials, I.counter, G, tot);
+  if (threadIdx.x == 0) {
+    Scalars *s = I.s;
+    if (fused_finish) {
+      finish_scalars(s, tot[0]);
+    } else if (!last) {
+      s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
+      s->tv_coef_f = (float)s->tv_coef;
     }
   }
 }
@@ -593,10 +644,17 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
                            int step, int ng, cudaStream_t st) {
   (void)ng;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
-  if (d.nz > 1)
+  if (d.nz > 1) {
     k_tv_step<true><<<grid, kThreads, 0, st>>>(insts, step);
-  else
-    k_tv_step2d<<<grid, kThreads, 0, st>>>(insts, step);
+  } else {
+    // groups per block: about two waves of 8 resident blocks per SM over the
+    // batch, one group per block for small batches
+    const long long groups = (long long)grid.x * grid.y;
+    const long long per = groups * batch / (2LL * 152 * 8);
+    const int per_block = (int)(per < 1 ? 1 : (per > 16 ? 16 : per));
+    const dim3 g2((unsigned)((groups + per_block - 1) / per_block), 1, batch);
+    k_tv_step2d<<<g2, kThreads, 0, st>>>(insts, step, per_block);
+  }
   return cudaGetLastError();
 }
 

@@ -72,7 +72,7 @@ def test_device_math_matches_oracle(dm, oracle_mod, case):
         yo, so = oracle_mod.ax(x, g, nx, ny, nz)
         bo, co = oracle_mod.atx(yv, g, nx, ny, nz)
         outs = {}
-        for lanes, exact in ((1, 1), (64, 1), (64, 0), (64, 2)):
+        for lanes, exact in ((1, 1), (32, 1), (32, 0), (32, 2)):
             y = np.zeros(na * nb, np.float32)
             sr = np.zeros(na * nb, np.float32)
             dm.dm_ax(_p(x), _p(y), _p(sr), g["cos_phi"], g["sin_phi"], _p(yd), _p(zd),
