@@ -106,7 +106,7 @@ constexpr int kMaxPartials = 1 << 22;  // blocks per reduction (sanity bound)
 
 // Instances per group of the shared-geometry kernels; their residuals are
 // stored interleaved, cor[r * kShareSlots + slot].
-constexpr int kShareSlots = 16;
+constexpr int kShareSlots = 8;
 
 // Inst::tabc_mode.  kTabcOwn: the instance writes its own table while it
 // runs.  Instances sharing geometry share one table: its writer

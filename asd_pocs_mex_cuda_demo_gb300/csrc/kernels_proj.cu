@@ -643,7 +643,7 @@ __device__ __forceinline__ void atx_shared_voxel(
   if (!valid) return;
   const float scv = accl * G.scale;
   const unsigned vi = ((unsigned)iz * D.ny + iy) * D.nx + ix;
-  // the group's images, interleaved: four float4 per voxel
+  // the group's images, interleaved: kShareGroup / 4 float4 per voxel
   float4 *mg = (float4 *)m_il + (size_t)vi * (kShareGroup / 4);
 #pragma unroll
   for (int q = 0; q < kShareGroup / 4; q++) {
@@ -691,7 +691,7 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
   const Inst &I0 = insts[g0];
   const Dims D = I0.d;  // every instance of a shared-geometry plan
   const ViewGeo G = view_of(I0, view);
-  // the group's residuals, interleaved: ray r of slot b at corg[r*16 + b]
+  // the group's residuals, interleaved: ray r of slot b at corg[r*kShareGroup + b]
   const float4 *__restrict__ corg = (const float4 *)I0.cor;
   const float4 *__restrict__ tabA = I0.tabA + (long long)view * D.na;
   const float4 *__restrict__ tabC = I0.tabC;
@@ -712,7 +712,7 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 // ---------------------------------------------------------------------------
 // Shared-geometry forward step: one warp per ray for a group of kShareGroup
 // instances.  The column march (cells and weights) is evaluated once per ray
-// and each piece reads the group's 16 voxel values with four float4 loads
+// and each piece reads the group's voxel values with kShareGroup / 4 float4 loads
 // from the interleaved images; every instance accumulates its pieces in the
 // order of k_sart_ax and sums lanes with the same butterfly, and its block
 // partials, reduction order and epilogue are those of k_sart_ax, so its

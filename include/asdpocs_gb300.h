@@ -279,7 +279,7 @@ int asdpocs_poisson_noise_device(const float *p_d, float *out_d, long long n,
  * to the same job run alone in a plan.  The budget counts the jobs' state.
  * A lane also holds its protocol's geometry tables and its slots'
  * interleaved images (4 bytes per voxel and slot; a lane gets as many slots,
- * in groups of 16, as fit in an eighth of the budget, at least 16) until the
+ * in groups of 8, as fit in an eighth of the budget, at least 8) until the
  * server is destroyed.  All calls are thread-safe.
  * --------------------------------------------------------------------- */
 typedef struct asdpocs_server_s *asdpocs_server;

@@ -291,7 +291,7 @@ def test_zero_iterations_returns_initial_image(gpu):
 
 
 def test_shared_geometry_groups_with_remainder(gpu):
-    """37 instances of one protocol: two full groups of 16 and one of 5, each
+    """37 instances of one protocol: full groups and a partial last one, each
     result equal to its run alone."""
     n, na, nv = 16, 24, 8
     SO, OD, det = 541.0, 408.0, 1.0
@@ -308,7 +308,7 @@ def test_shared_geometry_groups_with_remainder(gpu):
         pl.reset()
         pl.run()
         batch = [pl.image(k) for k in range(37)]
-    for k in (0, 15, 16, 31, 32, 36):
+    for k in (0, 7, 8, 15, 16, 31, 32, 35, 36):
         with pkg.Plan(paras[k], phi) as pl:
             pl.set_sinogram(0, Ps[k])
             pl.reset()
