@@ -64,6 +64,15 @@ SERVE = dict(
           "10-20 it",
     jobs=120, rate=20.0, frac2d=0.7)
 
+# Batched uneven slices (``--workload uneven``): one plan of 64 fan-beam
+# instances with sizes, view counts and bins drawn per instance -- every step
+# one launch for all of them -- against the same instances run one at a time.
+UNEVEN = dict(
+    label="batched uneven 2D: 64 slices, sizes {256,384,512,768}^2, views "
+          "{60,120,360,720}, bins 1.5 n, seeded random-ellipse phantoms, 20 it",
+    batch=64, iters=20, ng=20, sizes=(256, 384, 512, 768), views=(60, 120, 360, 720),
+    SO=541.0, OD=408.0, det=1.0, I0=1e5)
+
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per instance and
 # launch of each iteration kernel, from `ncu --set full --clock-control none`
 # captures of the 2D fan-beam workload at batch 64 (the shared-geometry
@@ -81,7 +90,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="fan2d", choices=sorted(WORKLOADS) + ["serve"])
+    ap.add_argument("--workload", default="fan2d",
+                    choices=sorted(WORKLOADS) + ["serve", "uneven"])
     ap.add_argument("--batch", type=int, default=None)
     ap.add_argument("--iters", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
@@ -92,6 +102,13 @@ def parse():
         W = dict(SERVE)
         if args.jobs is not None:
             W["jobs"] = args.jobs
+        return args, W
+    if args.workload == "uneven":
+        W = dict(UNEVEN)
+        if args.batch is not None:
+            W["batch"] = args.batch
+        if args.iters is not None:
+            W["iters"] = args.iters
         return args, W
     W = dict(WORKLOADS[args.workload])
     if args.batch is not None:
@@ -338,14 +355,16 @@ def main():
     args, W = parse()
     rank, world, local, pg = dist_init(args.gpus)
     if args.impl == "reference":
-        if args.workload == "serve":
+        if args.workload in ("serve", "uneven"):
             print(json.dumps({"impl": "reference", "unavailable":
-                              "the reference has no serving path; its CPU path is timed "
-                              "on the fan2d and cone3d workloads"}))
+                              "the reference runs one reconstruction at a time; its CPU "
+                              "path is timed on the fan2d and cone3d workloads"}))
             return 0
         return reference_arm(args, W, rank, world, pg)
     if args.workload == "serve":
         return serve_main(args, W, rank, world, pg)
+    if args.workload == "uneven":
+        return uneven_main(args, W, rank, world, pg)
     import torch
 
     import asd_pocs_mex_cuda_demo_gb300 as pkg
@@ -690,6 +709,116 @@ def serve_main(args, W, rank, world, pg):
                       "served_equals_plain_bitwise": equal},
             "rmse_vs_phantom": {"mean": float(np.mean(rm)), "max": float(np.max(rm))},
             "hbm_peak_bytes": int(max(peak_a, peak_b)),
+            "clocks": clk,
+        }))
+    return 0
+
+
+def uneven_main(args, W, rank, world, pg):
+    """One heterogeneous plan of W["batch"] seeded slices against the same
+    slices run one at a time (plain plans); images compared bit for bit."""
+    import torch
+
+    import asd_pocs_mex_cuda_demo_gb300 as pkg
+    from asd_pocs_mex_cuda_demo_gb300 import phantoms
+    from asd_pocs_mex_cuda_demo_gb300._lib import check, load
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dev = torch.device("cuda", torch.cuda.current_device())
+    L = load()
+    st = torch.cuda.current_stream().cuda_stream
+    rng = np.random.default_rng(17 + rank)
+    paras, Ps, xs = [], [], []
+    for k in range(W["batch"]):
+        n = int(rng.choice(W["sizes"]))
+        nv = int(rng.choice(W["views"]))
+        na = int(round(1.5 * n))
+        Wk = dict(nx=n, ny=n, nz=1, na=na, nb=1, nv=nv, SO=W["SO"], OD=W["OD"], det=W["det"],
+                  vx=None, iters=W["iters"], ng=W["ng"])
+        vx = voxel_size(Wk)
+        sc = np.float32(vx)
+        detv = np.float32(W["det"]) / sc
+        phi = phantoms.views(nv)
+        x = phantoms.random_ellipses(n, 9000 + k).astype(np.float32)
+        xd = torch.tensor(x, device=dev)
+        ydet = torch.tensor(((np.arange(na) - na / 2.0 + 0.5) * np.float64(detv))
+                            .astype(np.float32), device=dev)
+        zdet = torch.zeros(1, device=dev)
+        y = torch.empty(na * nv, device=dev)
+        sr = torch.empty(na, device=dev)
+        for v, a in enumerate(phi):
+            ph = np.float32(-(a / 180.0 * np.pi))
+            check(L.asdpocs_ax_device(xd.data_ptr(), y.data_ptr() + 4 * na * v, sr.data_ptr(),
+                                      float(np.cos(ph)), float(np.sin(ph)), ydet.data_ptr(),
+                                      zdet.data_ptr(), float(np.float32(W["SO"]) / sc),
+                                      float(np.float32(W["OD"]) / sc), float(sc), 1.0, n, n, 1,
+                                      na, 1, st))
+        phantoms.poisson_noise_device(y.data_ptr(), y.data_ptr(), y.numel(), W["I0"],
+                                      seed=11000 + k, stream=st)
+        torch.cuda.synchronize()
+        paras.append(dict(para_for(Wk), phi_vec=phi))
+        Ps.append(y.cpu().numpy())
+        xs.append(x)
+    stream = torch.cuda.Stream(device=dev)
+    plan = pkg.Plan(paras, [p["phi_vec"] for p in paras], stream=stream.cuda_stream)
+    for k in range(W["batch"]):
+        plan.set_sinogram(k, Ps[k])
+        plan.set_reference(k, xs[k])
+    for _ in range(args.warmup):
+        plan.reset()
+        plan.run(use_graph=True)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    times = []
+    barrier(pg)
+    clocks.start()
+    flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        plan.reset()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.run(use_graph=True, sync=False)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    ms = allmax(pg, statistics.mean(times))
+    batch_img = [plan.image(k) for k in range(W["batch"])]
+    rm = [float(plan.stats(k)["RMSE"][-1]) for k in range(W["batch"])]
+    plan.close()
+    plain_ms, equal = 0.0, True
+    for k in range(W["batch"]):
+        with pkg.Plan(paras[k], paras[k]["phi_vec"], stream=stream.cuda_stream) as pl:
+            pl.set_sinogram(0, Ps[k])
+            pl.set_reference(0, xs[k])
+            pl.reset()
+            pl.run()
+            pl.reset()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            pl.run(use_graph=True, sync=False)
+            e1.record(stream)
+            e1.synchronize()
+            plain_ms += e0.elapsed_time(e1)
+            equal = equal and bool(np.array_equal(pl.image(0), batch_img[k]))
+    value = W["batch"] * world / (ms / 1e3)
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "recons/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded random-ellipse phantoms, Poisson noise)",
+            "config": {"workload": W["label"], "batch_per_gpu": W["batch"],
+                       "iterations": W["iters"], "parallelism": f"replicas x{world}",
+                       "storage": "FP32 (BF16/FP16 storage is not built)",
+                       "l2": "256 MB buffer written between timed steps"},
+            "plain": {"recons_per_s": W["batch"] / (plain_ms / 1e3), "ms_total": plain_ms,
+                      "batched_speedup": value / world / (W["batch"] / (plain_ms / 1e3)),
+                      "batch_equals_plain_bitwise": equal},
+            "rmse_vs_phantom": {"mean": float(np.mean(rm)), "max": float(np.max(rm))},
             "clocks": clk,
         }))
     return 0
