@@ -429,15 +429,26 @@ __global__ void __launch_bounds__(kThreads)
 // the next step.  The values are those of recomputing v here.
 //
 // A block walks `per_block` consecutive groups of its instance, staging the
-// next group's halo with cp.async (zero-filled outside the image) while it
-// evaluates the current one, and leaves one partial per group; the last
-// block of the instance sums the partials in group order.  The result is
-// therefore the same for every `per_block`, which the host picks from the
-// batch size (long-lived blocks for large batches, one group per block for
-// one instance).
+// next group's halo while it evaluates the current one, and leaves one
+// partial per group; the last block of the instance sums the partials in
+// group order, so the result is the same for every `per_block` (picked by
+// the host from the batch size).  Staging is by TMA when the instance has
+// tensor maps (nx a multiple of 4): one thread issues two 2-D tile loads
+// (m and v, box 40 x 34 from column x0 - 4, 16-byte aligned; zeros outside
+// the image) completing on an mbarrier, which every thread waits on with a
+// bounded number of tries -- past it the block records a fault and goes on.
+// Otherwise each thread stages its share with 4-byte cp.async (zero-filled
+// outside the image).
 constexpr int kGroupRows = kTileY * kTilesPerBlock;
 constexpr int kHaloW = kTileX + 2, kHaloH = kGroupRows + 2, kHaloN = kHaloW * kHaloH;
 constexpr int kHaloRounds = (kHaloN + kThreads - 1) / kThreads;
+constexpr int kBoxX0 = 3;  // column of x0 - 1 in the staged box (box starts at x0 - 4)
+static_assert(kTmBoxW == kTileX + 8 && kTmBoxH == kHaloH, "TMA box covers the halo");
+constexpr unsigned kTmBytes = 2u * kTmBoxW * kTmBoxH * 4u;  // m and v boxes
+// a box's slot in shared memory, rounded up to the 128-byte alignment of
+// tensor copies
+constexpr int kBoxFloats = (kTmBoxW * kTmBoxH + 31) / 32 * 32;
+constexpr int kWaitTries = 1 << 20;
 
 __device__ __forceinline__ void cp_async4(float *smem, const float *gmem, bool valid) {
   const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
@@ -451,11 +462,49 @@ __device__ __forceinline__ void cp_async_commit() {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// true when the phase with the given parity has completed; false after
+// kWaitTries attempts
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
+  const unsigned a = smem_u32(bar);
+  for (int i = 0; i < kWaitTries; i++) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(float *dst, const CUtensorMap *map, int x, int y,
+                                            unsigned long long *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];\n" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
 
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 5)
     k_tv_step2d(const Inst *__restrict__ insts, int step, int per_block) {
-  __shared__ float sm[2][kHaloH][kHaloW];  // m on the halo region, then m'
-  __shared__ float sv[2][kHaloH][kHaloW];  // v(m) on the halo region
+  // [stage][m | v][row][column]: m (then m' in place) and v(m) of a group's
+  // halo region at columns kBoxX0 .. kBoxX0 + 33
+  __shared__ alignas(128) float tile[2][2][kBoxFloats];
+  __shared__ alignas(8) unsigned long long bar[2];
   __shared__ float shf[kThreads / 32];
   __shared__ int s_last;
   const Inst &I = insts[blockIdx.z];
@@ -475,9 +524,28 @@ __global__ void __launch_bounds__(kThreads)
   float *dst = tv_dst(I, step);
   const float *vin = tv_v(I, step);
   float *vout = tv_v(I, step + 1);
+  const int tm_m = step == 0 ? kTmM : ((step & 1) ? kTmB : kTmC);
+  const int tm_v = (step & 1) ? kTmVb : kTmVa;
+  const bool tma = I.tmap != nullptr;  // block-uniform
   const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
-  auto stage = [&](int g, int buf) {
-    const int x0 = (g % (int)gg.x) * kTileX, y0 = (g / (int)gg.x) * kGroupRows;
+  auto group_origin = [&](int g, int &x0, int &y0) {
+    x0 = (g % (int)gg.x) * kTileX;
+    y0 = (g / (int)gg.x) * kGroupRows;
+  };
+  auto stage = [&](int g, int st) {
+    int x0, y0;
+    group_origin(g, x0, y0);
+    if (tma) {
+      if (threadIdx.x == 0) {
+        // the buffer's previous contents were written by this block's
+        // threads (generic proxy) before the barrier that precedes this call
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        mbar_expect_tx(&bar[st], kTmBytes);
+        tma_load_2d(tile[st][0], I.tmap + tm_m, x0 - 4, y0 - 1, &bar[st]);
+        tma_load_2d(tile[st][1], I.tmap + tm_v, x0 - 4, y0 - 1, &bar[st]);
+      }
+      return;
+    }
 #pragma unroll
     for (int j = 0; j < kHaloRounds; j++) {
       const int k = threadIdx.x + j * kThreads;
@@ -486,31 +554,57 @@ __global__ void __launch_bounds__(kThreads)
         const int y = y0 - 1 + r, x = x0 - 1 + c;
         const bool in = y >= 0 && y < D.ny && x >= 0 && x < D.nx;
         const unsigned i = in ? (unsigned)y * D.nx + x : 0u;
-        cp_async4(&sm[buf][r][c], src + i, in);
-        cp_async4(&sv[buf][r][c], vin + i, in);
+        cp_async4(&tile[st][0][r * kTmBoxW + kBoxX0 + c], src + i, in);
+        cp_async4(&tile[st][1][r * kTmBoxW + kBoxX0 + c], vin + i, in);
       }
     }
     cp_async_commit();
   };
+  if (tma && threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(I.tmap + tm_m)
+                 : "memory");
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(I.tmap + tm_v)
+                 : "memory");
+  }
+  __syncthreads();
   stage(g_begin, 0);
   for (int g = g_begin; g < g_end; g++) {
-    const int buf = (g - g_begin) & 1;
-    cp_async_wait_all();
-    __syncthreads();
+    const int i = g - g_begin, st = i & 1;
+    if (tma) {
+      const unsigned parity = (unsigned)(i >> 1) & 1u;
+      if (!__syncthreads_and(mbar_wait(&bar[st], parity))) {
+        // the only copy in flight is this group's: record the fault, give it
+        // one more bounded wait and leave the groups (the instance's sums
+        // still close, so the launch ends normally)
+        if (threadIdx.x == 0) {
+          if (I.fault) atomicOr(I.fault, kFaultTmaWait);
+          mbar_wait(&bar[st], parity);
+        }
+        __syncthreads();
+        break;
+      }
+    } else {
+      cp_async_wait_all();
+      __syncthreads();
+    }
     // m' = m - coef * v in place (zero outside the image: staged as zeros)
 #pragma unroll
     for (int j = 0; j < kHaloRounds; j++) {
       const int k = threadIdx.x + j * kThreads;
       if (k < kHaloN) {
-        const int r = k / kHaloW, c = k - r * kHaloW;
-        sm[buf][r][c] = sm[buf][r][c] - coef * sv[buf][r][c];
+        const int r = k / kHaloW, c = r * kTmBoxW + kBoxX0 + k - r * kHaloW;
+        tile[st][0][c] = tile[st][0][c] - coef * tile[st][1][c];
       }
     }
     __syncthreads();
     // the next group's halo arrives while this one is evaluated (its buffer
     // was last read two groups ago, before the barrier above)
-    if (g + 1 < g_end) stage(g + 1, buf ^ 1);
-    const int x0 = (g % (int)gg.x) * kTileX, y0 = (g / (int)gg.x) * kGroupRows;
+    if (g + 1 < g_end) stage(g + 1, st ^ 1);
+    int x0, y0;
+    group_origin(g, x0, y0);
     float v = 0.f;
 #pragma unroll
     for (int k = 0; k < kTilesPerBlock; k++) {
@@ -518,7 +612,9 @@ __global__ void __launch_bounds__(kThreads)
       const int ix = x0 + tx, iy = y0 + r;
       if (ix < D.nx && iy < D.ny) {
         const unsigned i = (unsigned)iy * D.nx + ix;
-        const auto u = [&](int dx, int dy, int) { return sm[buf][r + 1 + dy][tx + 1 + dx]; };
+        const auto u = [&](int dx, int dy, int) {
+          return tile[st][0][(r + 1 + dy) * kTmBoxW + kBoxX0 + tx + 1 + dx];
+        };
         const float mn = u(0, 0, 0);
         if (fused_finish) {
           const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
