@@ -12,6 +12,7 @@
 // previous kernel.  The end-of-sweep kernel provides ||v|| of the first
 // step; the last step also applies the positivity constraint and the
 // alpha/beta step control.
+#include <type_traits>
 #include "kernels.h"
 #include "reduce.cuh"
 
@@ -62,6 +63,45 @@ __device__ __forceinline__ T tv_grad2(const U &u) {
   return g1 + g2 + g3;
 }
 
+// FP32 form of the 2-D stencil with every rounding explicit, so that a
+// kernel holding its terms in registers reproduces it bit for bit.  With
+// dx = f(x,y) - f(x-1,y), dy = f(x,y) - f(x,y-1) at a voxel, its terms are
+//   r1 = 1/sqrt(eps + dx^2 + dy^2),  g1 = (dx + dy) * r1,  q = dx * r1,
+//   r3 = 1/sqrt(eps + dy^2 + dx^2),  t = dy * r3
+// and v(x,y) = (g1(x,y) - q(x+1,y)) - t(x,y+1): the reference's second term
+// is the right neighbour's q (same differences, same sum order) and its
+// third the lower neighbour's t (its sum in the other order).  1/sqrt is
+// the approximate reciprocal square root; den >= eps is never subnormal, so
+// flushing subnormals changes nothing.
+__device__ __forceinline__ float tv_rsqrt(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+struct Tv2Terms {
+  float g1, q, t;
+};
+__device__ __forceinline__ Tv2Terms tv2_terms(float dx, float dy) {
+  const float eps = tv_eps<float>();
+  const float r1 = tv_rsqrt(__fmaf_rn(dy, dy, __fmaf_rn(dx, dx, eps)));
+  const float r3 = tv_rsqrt(__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, eps)));
+  return Tv2Terms{__fmul_rn(__fadd_rn(dx, dy), r1), __fmul_rn(dx, r1), __fmul_rn(dy, r3)};
+}
+__device__ __forceinline__ float tv2_combine(float g1, float q_right, float t_below) {
+  return __fsub_rn(__fsub_rn(g1, q_right), t_below);
+}
+template <class U>
+__device__ __forceinline__ float tv_grad2f(const U &u) {
+  const float c0 = u(0, 0, 0);
+  const float xm = u(-1, 0, 0), ym = u(0, -1, 0);
+  const float xp = u(1, 0, 0), yp = u(0, 1, 0);
+  const float xpym = u(1, -1, 0), xmyp = u(-1, 1, 0);
+  const Tv2Terms here = tv2_terms(__fsub_rn(c0, xm), __fsub_rn(c0, ym));
+  const Tv2Terms right = tv2_terms(__fsub_rn(xp, c0), __fsub_rn(xp, xpym));
+  const Tv2Terms below = tv2_terms(__fsub_rn(yp, xmyp), __fsub_rn(yp, c0));
+  return tv2_combine(here.g1, right.q, below.t);
+}
+
 // imgTVGradMin3D.cpp:114-140 (image index x + y*Nx + z*Nx*Ny).
 template <class T, class U>
 __device__ __forceinline__ T tv_grad3(const U &u) {
@@ -85,7 +125,11 @@ __device__ __forceinline__ T tv_grad3(const U &u) {
 
 template <class T, class U>
 __device__ __forceinline__ T tv_grad(const U &u, bool is3d) {
-  return is3d ? tv_grad3<T>(u) : tv_grad2<T>(u);
+  if (is3d) return tv_grad3<T>(u);
+  if constexpr (std::is_same<T, float>::value)
+    return tv_grad2f(u);
+  else
+    return tv_grad2<T>(u);
 }
 
 // Global-memory accessor with zero padding (standalone entry points).
@@ -626,7 +670,7 @@ __global__ void __launch_bounds__(kThreads, 5)
         } else {
           dst[i] = mn;
           if (!last) {
-            const float gr = tv_grad2<float>(u);
+            const float gr = tv_grad2f(u);
             v += gr * gr;
             vout[i] = gr;  // the next step's update reads it
           }
@@ -654,6 +698,222 @@ __global__ void __launch_bounds__(kThreads, 5)
       finish_scalars(s, tot[0]);
     } else if (!last) {
       s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
+      s->tv_coef_f = (float)s->tv_coef;
+    }
+  }
+}
+
+// 2-D TV step as column walks.  A warp owns a strip of 64 image columns
+// (lane l: columns xs - 2 + 2l and the next) and walks down it a row at a
+// time, holding everything in registers: each new row of m gives, with one
+// shuffle from each neighbour lane, the stencil terms of that row
+// (tv2_terms), which complete v(m) one row up; m' = m - coef * v(m) follows
+// (zero outside the image), and the same walk over the rows of m' completes
+// v(m') two rows up.  The lanes at the strip's edges only feed their
+// neighbours, so a strip writes its 60 middle columns (strips overlap by
+// four columns) and a walk over output rows [y0, y1) reads rows
+// y0 - 2 .. y1 + 1.  A step reads m once and writes m' once (8 bytes per
+// voxel) and evaluates two stencils per voxel, both in registers.
+//
+// ||v(m')||^2 (or, in the last step, the positivity-change norm) is summed
+// per band of 32 output rows of a strip -- lanes in row order, then an xor
+// butterfly -- and the walk that finishes last sums the band partials of
+// the instance in order; walks of `bands` consecutive bands (chosen by the
+// host from the batch size) therefore give the same bits for every choice.
+constexpr int kWalkWarps = 4;
+constexpr int kWalkOut = 60;   // output columns of a strip
+constexpr int kBandRows = 32;  // output rows of a partial
+constexpr int kWalkAhead = 4;  // rows loaded ahead of the one in use
+
+__host__ __device__ __forceinline__ int walk_strips(int nx) {
+  return (nx + kWalkOut - 1) / kWalkOut;
+}
+__host__ __device__ __forceinline__ int walk_bands(int ny) {
+  return (ny + kBandRows - 1) / kBandRows;
+}
+
+// The running stencil of one field along a walk: the previous row's values
+// and its partly combined v, (g1 - q_right), waiting for the row below.
+struct WalkField {
+  float pa, pb;  // previous row, columns a and b
+  float ca, cb;  // g1 - q_right of the previous row
+  // Takes row j (fa, fb); returns v of row j - 1 in va, vb.
+  __device__ __forceinline__ void push(float fa, float fb, float &va, float &vb) {
+    const float fl = __shfl_up_sync(0xffffffffu, fb, 1);  // column a - 1
+    const Tv2Terms ta = tv2_terms(__fsub_rn(fa, fl), __fsub_rn(fa, pa));
+    const Tv2Terms tb = tv2_terms(__fsub_rn(fb, fa), __fsub_rn(fb, pb));
+    const float qr = __shfl_down_sync(0xffffffffu, ta.q, 1);  // q of column b + 1
+    va = __fsub_rn(ca, ta.t);
+    vb = __fsub_rn(cb, tb.t);
+    ca = __fsub_rn(ta.g1, tb.q);
+    cb = __fsub_rn(tb.g1, qr);
+    pa = fa;
+    pb = fb;
+  }
+};
+
+// kMode 0: m' and ||v(m')||^2; 1: m' only (the single, last step);
+// 2: the last of several steps -- positivity, the change norm, and m' into
+// the image and m_pre.  kPair: nx is even, so a lane's two columns are both
+// inside or both outside the image and 8-byte aligned (one access each).
+template <int kMode, bool kPair>
+__device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1, int xa,
+                                        int strip, int S, float coef) {
+  const Dims D = I.d;
+  const int lane = threadIdx.x & 31;
+  const float *src = tv_src(I, step);
+  float *dst = tv_dst(I, step);
+  const bool ina = xa >= 0 && xa < D.nx, inb = xa + 1 >= 0 && xa + 1 < D.nx;
+  const bool outl = lane >= 1 && lane <= 30;
+  const bool outa = outl && ina, outb = outl && inb;
+  const int jl0 = y0 - 2, jl1 = min(D.ny, y1 + 2);  // rows of m read
+  const int j1 = y1 + 2;                            // rows walked: jl0 .. j1 - 1
+  auto load = [&](int j, float &a, float &b) {
+    const bool r = j >= max(jl0, 0) && j < jl1;
+    const int i = j * D.nx + xa;
+    if (kPair) {
+      const float2 v = (r && ina) ? __ldg((const float2 *)(src + i)) : make_float2(0.f, 0.f);
+      a = v.x;
+      b = v.y;
+    } else {
+      a = (r && ina) ? __ldg(src + i) : 0.f;
+      b = (r && inb) ? __ldg(src + i + 1) : 0.f;
+    }
+  };
+  float ra[kWalkAhead], rb[kWalkAhead];
+#pragma unroll
+  for (int k = 0; k < kWalkAhead; k++) load(jl0 + k, ra[k], rb[k]);
+  WalkField f1{0.f, 0.f, 0.f, 0.f}, f2{0.f, 0.f, 0.f, 0.f};
+  float acc = 0.f;
+  for (int j0 = jl0; j0 < j1; j0 += kWalkAhead) {
+#pragma unroll
+    for (int k = 0; k < kWalkAhead; k++) {
+      const int j = j0 + k;
+      const float ma = ra[k], mb = rb[k];
+      load(j + kWalkAhead, ra[k], rb[k]);
+      // v(m) of row j - 1, then m' of row j - 1 (zero outside the image)
+      const float m1a = f1.pa, m1b = f1.pb;
+      float va, vb;
+      f1.push(ma, mb, va, vb);
+      const int o1 = j - 1;
+      const bool row1 = o1 >= 0 && o1 < D.ny;
+      const float pa = (row1 && ina) ? __fmaf_rn(-coef, va, m1a) : 0.f;
+      const float pb = (row1 && inb) ? __fmaf_rn(-coef, vb, m1b) : 0.f;
+      const bool out1 = o1 >= y0 && o1 < y1;  // warp-uniform
+      if (kMode == 2) {
+        if (out1) {
+          const int i = o1 * D.nx + xa;
+          const float mca = pa < 0.f ? 0.f : pa;  // imgTVGradMin.cpp:110-116
+          const float mcb = pb < 0.f ? 0.f : pb;
+          if (kPair) {
+            if (outa) {
+              const float2 f0 = *(const float2 *)(I.m + i);
+              const float da = mca - f0.x, db = mcb - f0.y;
+              acc += da * da;
+              acc += db * db;
+              *(float2 *)(I.m + i) = make_float2(mca, mcb);
+              *(float2 *)(I.m_pre + i) = make_float2(mca, mcb);
+            }
+          } else {
+            if (outa) {
+              const float d = mca - I.m[i];
+              acc += d * d;
+              I.m[i] = mca;
+              I.m_pre[i] = mca;
+            }
+            if (outb) {
+              const float d = mcb - I.m[i + 1];
+              acc += d * d;
+              I.m[i + 1] = mcb;
+              I.m_pre[i + 1] = mcb;
+            }
+          }
+        }
+      } else {
+        if (out1) {
+          const int i = o1 * D.nx + xa;
+          if (kPair) {
+            if (outa) *(float2 *)(dst + i) = make_float2(pa, pb);
+          } else {
+            if (outa) dst[i] = pa;
+            if (outb) dst[i + 1] = pb;
+          }
+        }
+        if (kMode == 0) {
+          // v(m') of row j - 2
+          float wa, wb;
+          f2.push(pa, pb, wa, wb);
+          const int o2 = j - 2;
+          if (o2 >= y0 && o2 < y1) {
+            if (outa) acc += wa * wa;
+            if (outb) acc += wb * wb;
+          }
+        }
+      }
+      // the band of the row just accumulated is complete: one partial
+      if (kMode != 1) {
+        const int o = kMode == 2 ? o1 : j - 2;
+        if (o >= y0 && o < y1 && ((o + 1) % kBandRows == 0 || o + 1 == y1)) {
+#pragma unroll
+          for (int w = 16; w > 0; w >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, w);
+          if (lane == 0) I.partials[(o / kBandRows) * S + strip] = (double)acc;
+          acc = 0.f;
+        }
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kWalkWarps * 32, 8)
+    k_tv_walk2d(const Inst *__restrict__ insts, int step, int bands) {
+  const Inst &I = insts[blockIdx.z];
+  if (inst_done(I)) return;
+  const int ng = I.s->ng;
+  if (step >= ng) return;
+  const Dims D = I.d;
+  const int S = walk_strips(D.nx), NB = walk_bands(D.ny);
+  const int per_strip = (NB + bands - 1) / bands;
+  const int walks = S * per_strip;
+  const int w = blockIdx.x * kWalkWarps + (threadIdx.x >> 5);
+  if (w >= walks) return;  // warp-uniform
+  const int lane = threadIdx.x & 31;
+  const int strip = w % S, b0 = (w / S) * bands;
+  const int y0 = b0 * kBandRows, y1 = min(D.ny, (b0 + bands) * kBandRows);
+  const int xa = strip * kWalkOut - 2 + 2 * lane;
+  const bool last = step == ng - 1;
+  const float coef = I.s->tv_coef_f;
+  const bool pair = (D.nx & 1) == 0;
+  if (!last)
+    pair ? tv_walk<0, true>(I, step, y0, y1, xa, strip, S, coef)
+         : tv_walk<0, false>(I, step, y0, y1, xa, strip, S, coef);
+  else if (ng == 1)
+    pair ? tv_walk<1, true>(I, step, y0, y1, xa, strip, S, coef)
+         : tv_walk<1, false>(I, step, y0, y1, xa, strip, S, coef);
+  else
+    pair ? tv_walk<2, true>(I, step, y0, y1, xa, strip, S, coef)
+         : tv_walk<2, false>(I, step, y0, y1, xa, strip, S, coef);
+  if (last && ng == 1) return;  // nothing to sum: k_finish_iter ends the iteration
+  // the walk that finishes last sums the instance's band partials
+  unsigned ticket = 0;
+  if (lane == 0) {
+    __threadfence();
+    ticket = atomicAdd(I.counter, 1u);
+  }
+  ticket = __shfl_sync(0xffffffffu, ticket, 0);
+  if (ticket != (unsigned)walks - 1) return;
+  __threadfence();
+  const int P = S * NB;
+  double a = 0.0;
+  for (int p = lane; p < P; p += 32) a += ((volatile const double *)I.partials)[p];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane == 0) {
+    *I.counter = 0u;
+    Scalars *s = I.s;
+    if (last) {
+      finish_scalars(s, a);
+    } else {
+      s->tv_coef = s->alpha * s->d_tv / sqrt(a);
       s->tv_coef_f = (float)s->tv_coef;
     }
   }
@@ -743,13 +1003,15 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
   if (d.nz > 1) {
     k_tv_step<true><<<grid, kThreads, 0, st>>>(insts, step);
   } else {
-    // groups per block: about two waves of 8 resident blocks per SM over the
-    // batch, one group per block for small batches
-    const long long groups = (long long)grid.x * grid.y;
-    const long long per = groups * batch / (2LL * 152 * 8);
-    const int per_block = (int)(per < 1 ? 1 : (per > 16 ? 16 : per));
-    const dim3 g2((unsigned)((groups + per_block - 1) / per_block), 1, batch);
-    k_tv_step2d<<<g2, kThreads, 0, st>>>(insts, step, per_block);
+    // bands per walk: the batch's walks within about one wave of 32
+    // resident warps per SM, one band per walk for small batches
+    const long long units = (long long)walk_strips(d.nx) * walk_bands(d.ny);
+    const long long cap = 152LL * 32;
+    const long long per = (units * batch + cap - 1) / cap;
+    const int bands = (int)(per < 1 ? 1 : (per > walk_bands(d.ny) ? walk_bands(d.ny) : per));
+    const long long walks = (long long)walk_strips(d.nx) * ((walk_bands(d.ny) + bands - 1) / bands);
+    const dim3 g2((unsigned)((walks + kWalkWarps - 1) / kWalkWarps), 1, batch);
+    k_tv_walk2d<<<g2, kWalkWarps * 32, 0, st>>>(insts, step, bands);
   }
   return cudaGetLastError();
 }
