@@ -1,6 +1,5 @@
 // Shared definitions of the asdpocs_gb300 library (internal).
 #pragma once
-#include <cuda.h>  // CUtensorMap (the type only; no driver calls here)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -83,7 +82,6 @@ struct Inst {
   float *m_k1;               // TV distance reference (m0)
   float *I0;                 // reference image or nullptr
   float *tv_b, *tv_c;        // TV ping-pong buffers
-  float *tv_va, *tv_vb;      // 2-D TV: the stencil v of the image each step
                              //   starts from (ping-pong), so the step's update
                              //   reads it instead of recomputing it
   float *cor;                // correction of the current view: element r at
@@ -98,8 +96,6 @@ struct Inst {
   float4 *tabC;              // 3D ray slopes of the current view, na*nb
   int tabc_mode;             // who writes tabC in the forward step (kTabc*)
   double *rmse;              // [maxIter]
-  const CUtensorMap *tmap;   // 2-D TV halo tiles (kTm*), or nullptr
-  unsigned *fault;           // set when a bounded device wait gives up
   double *partials;          // reduction partials [blocks * kMaxReduceK]
   unsigned *counter;         // reduction ticket
   Scalars *s;
@@ -116,16 +112,6 @@ constexpr int kShareSlots = 8;
 // (kTabcShared) refreshes it every view even after it has finished, so the
 // others (kTabcNone) keep reading current slopes.
 constexpr int kTabcOwn = 0, kTabcShared = 1, kTabcNone = 2;
-
-// Inst::tmap: TMA descriptors of an instance's 2-D TV buffers, in this
-// order; each describes the nx x ny image with a box of kTmBoxW x kTmBoxH
-// floats (a 32 x 32 voxel group with its one-voxel halo, widened to a
-// 16-byte-aligned start column).
-constexpr int kTmM = 0, kTmB = 1, kTmC = 2, kTmVa = 3, kTmVb = 4, kTmCount = 5;
-constexpr int kTmBoxW = 40, kTmBoxH = 34;
-
-// Inst::fault codes
-constexpr unsigned kFaultTmaWait = 1u;
 
 // View flags (Inst::vflags): some ray of the view has no x (or no y)
 // extent; some ray is not x-dominant; some ray is not y-dominant.

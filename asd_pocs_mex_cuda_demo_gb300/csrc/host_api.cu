@@ -393,7 +393,6 @@ struct asdpocs_plan_s {
   bool shared = false;  // all instances share sizes, geometry and angles
   Inst *d_inst = nullptr;
   void *arena = nullptr;
-  unsigned *d_fault = nullptr;  // bounded device waits that gave up (kFault*)
   size_t bytes = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -432,16 +431,10 @@ InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
   o.I0 = off; off += per_img;
   o.tvb = off; off += per_img;
   o.tvc = off; off += per_img;
-  // 2-D: the TV stencil of the step's starting image (cone beam: unused)
-  const size_t per_v = (st && g.nz == 1) ? per_img : 0;
-  o.tvva = off; off += per_v;
-  o.tvvb = off; off += per_v;
   o.rmse = off; off += st ? align256((size_t)(max_iter + 1) * 8) : 0;
   o.part = off; off += st ? align256(nblk * kMaxReduceK * 8) : 0;
   o.cnt = off; off += st ? 256 : 0;
   o.scal = off; off += st ? align256(sizeof(Scalars)) : 0;
-  o.tmaps = (st && g.nz == 1 && g.nx % 4 == 0) ? kTmCount : 0;
-  o.tmap = off; off += align256((size_t)o.tmaps * sizeof(CUtensorMap));
   o.cor = off; off += geo ? align256(cor_floats * 4) : 0;
   o.m_il = off; off += geo ? align256(il_floats * 4) : 0;
   o.tabA = off; off += geo ? align256((size_t)g.na * g.nv * 16) : 0;
@@ -463,64 +456,10 @@ void bind_state(Inst &I, char *b, const InstLayout &o) {
   I.I0 = (float *)(b + o.I0);
   I.tv_b = (float *)(b + o.tvb);
   I.tv_c = (float *)(b + o.tvc);
-  I.tv_va = (float *)(b + o.tvva);
-  I.tv_vb = (float *)(b + o.tvvb);
   I.rmse = (double *)(b + o.rmse);
   I.partials = (double *)(b + o.part);
   I.counter = (unsigned *)(b + o.cnt);
   I.s = (Scalars *)(b + o.scal);
-  I.tmap = nullptr;
-}
-
-// cuTensorMapEncodeTiled, resolved from the driver on first use (the
-// library links the runtime only)
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                  const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion,
-                                  CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn encode_tiled() {
-  static const EncodeTiledFn fn = [] {
-    void *f = nullptr;
-    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
-                                         cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess)
-      f = nullptr;
-    return (EncodeTiledFn)f;
-  }();
-  return fn;
-}
-
-cudaError_t bind_tensor_maps(Inst &I, char *b, const InstLayout &o, cudaStream_t st) {
-  I.tmap = nullptr;
-  if (o.tmaps != kTmCount || getenv("ASDPOCS_NO_TMA")) return cudaSuccess;
-  const EncodeTiledFn enc = encode_tiled();
-  if (!enc) return cudaSuccess;
-  // 2-D fp32 images, row pitch nx * 4 bytes; boxes of the halo staging,
-  // zeros outside the image
-  const cuuint64_t dim[2] = {(cuuint64_t)I.d.nx, (cuuint64_t)I.d.ny};
-  const cuuint64_t pitch[1] = {(cuuint64_t)I.d.nx * 4};
-  const cuuint32_t box[2] = {kTmBoxW, kTmBoxH}, unit[2] = {1, 1};
-  const float *buf[kTmCount];
-  buf[kTmM] = I.m;
-  buf[kTmB] = I.tv_b;
-  buf[kTmC] = I.tv_c;
-  buf[kTmVa] = I.tv_va;
-  buf[kTmVb] = I.tv_vb;
-  CUtensorMap maps[kTmCount];
-  for (int k = 0; k < kTmCount; k++)
-    if (enc(&maps[k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)buf[k], dim, pitch, box,
-            unit, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return cudaSuccess;
-  // pageable source: staged before the call returns
-  const cudaError_t e =
-      cudaMemcpyAsync(b + o.tmap, maps, sizeof maps, cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) I.tmap = (const CUtensorMap *)(b + o.tmap);
-  return e;
 }
 
 cudaError_t bind_geometry(Inst &I, char *b, const InstLayout &o,
@@ -559,9 +498,7 @@ cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,
                           const asdpocs_geometry &g, const double *phi_deg,
                           cudaStream_t st) {
   bind_state(I, b, o);
-  cudaError_t e = bind_geometry(I, b, o, g, phi_deg, st);
-  if (e == cudaSuccess) e = bind_tensor_maps(I, b, o, st);
-  return e;
+  return bind_geometry(I, b, o, g, phi_deg, st);
 }
 
 Scalars initial_scalars(const asdpocs_options &o, bool has_ref) {
@@ -715,8 +652,6 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   }
   const size_t inst_off = off;
   off += align256(sizeof(Inst) * batch);
-  const size_t fault_off = off;
-  off += 256;
   p->bytes = off;
   if (hbm_budget_bytes && off > hbm_budget_bytes) {
     if (p->own_stream) cudaStreamDestroy(p->st);
@@ -733,7 +668,6 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   }
   char *b = (char *)p->arena;
   e = cudaMemsetAsync(b, 0, off, p->st);
-  p->d_fault = (unsigned *)(b + fault_off);
   p->h_inst.resize(batch);
   for (int i = 0; i < batch && e == cudaSuccess; i++) {
     Inst &I = p->h_inst[i];
@@ -747,7 +681,6 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
       I.tabC = (float4 *)(b + base[0] + lay[0].tabC);
       I.tabc_mode = i == 0 ? kTabcShared : kTabcNone;
     }
-    I.fault = p->d_fault;
   }
   p->d_inst = (Inst *)(b + inst_off);
   if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(),
@@ -867,23 +800,11 @@ int asdpocs_plan_run(asdpocs_plan p, int use_graph) {
   return 0;
 }
 
-// ASDPOCS_ERR_TIMEOUT when a kernel's bounded wait gave up since the plan
-// was created (the stream's work must have completed)
-static int plan_fault_check(asdpocs_plan p) {
-  unsigned f = 0;
-  ASD_CUDA(cudaMemcpy(&f, p->d_fault, sizeof f, cudaMemcpyDeviceToHost));
-  if (f & kFaultTmaWait)
-    return set_error(ASDPOCS_ERR_TIMEOUT,
-                     "a TV step's tile copy did not complete within its wait limit");
-  if (f) return set_error(ASDPOCS_ERR_TIMEOUT, "device wait gave up (0x%x)", f);
-  return 0;
-}
-
 int asdpocs_plan_sync(asdpocs_plan p) {
   clear_error();
   if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
   ASD_CUDA(cudaStreamSynchronize(p->st));
-  return plan_fault_check(p);
+  return 0;
 }
 
 int asdpocs_plan_get_image(asdpocs_plan p, int inst, float *m, int where) {
@@ -910,7 +831,6 @@ int asdpocs_plan_get_stats(asdpocs_plan p, int inst, asdpocs_stats *st,
                              (size_t)p->opt[inst].maxnumIter * 8,
                              cudaMemcpyDeviceToHost, p->st));
   ASD_CUDA(cudaStreamSynchronize(p->st));
-  if (int e = plan_fault_check(p)) return e;
   if (st) {
     st->IterationNum = s.iterations;
     st->dataTolerance = s.dd2;

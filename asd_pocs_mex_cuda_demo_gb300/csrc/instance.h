@@ -9,9 +9,8 @@ namespace asd {
 // (each 256-byte aligned), at the instance's own sizes; `bytes` is the
 // block's size.
 struct InstLayout {
-  size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, tvva, tvvb, cor, m_il, ydet, zdet, trig,
-      rmse, part, cnt, scal, tabA, tabC, vflags, tmap, bytes;
-  int tmaps;  // tensor maps of the 2-D TV step's buffers at `tmap` (0 or kTmCount)
+  size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, m_il, ydet, zdet, trig,
+      rmse, part, cnt, scal, tabA, tabC, vflags, bytes;
 };
 
 // Kind of an instance: 0 = 2-D fan beam (nz == nb == 1), 1 = one slice with
@@ -48,13 +47,6 @@ void bind_state(Inst &I, char *b, const InstLayout &o);
 cudaError_t bind_geometry(Inst &I, char *b, const InstLayout &o,
                           const asdpocs_geometry &g, const double *phi_deg,
                           cudaStream_t st);
-
-// Encodes the tensor maps of the 2-D TV step's buffers (2-D instances with
-// nx a multiple of 4: rows 16-byte aligned) into the block `b` on `st` and
-// points I.tmap at them; leaves I.tmap null -- the step then stages by
-// cp.async -- when the layout has none, the driver cannot encode them or
-// ASDPOCS_NO_TMA is set.  Needs I's state pointers (bind_state).
-cudaError_t bind_tensor_maps(Inst &I, char *b, const InstLayout &o, cudaStream_t st);
 
 // Both of the above for a block holding both parts.
 cudaError_t bind_instance(Inst &I, char *b, const InstLayout &o,

@@ -2,16 +2,16 @@
 // the per-iteration ASD-POCS scalar steps (ASD_POCS_cuda.m:137-170), sm_103a.
 //
 // Device-resident path (FP32 image, FP64 scalars): one kernel per TV step.
-// A block stages its 32x8 voxel tile of the current image with a halo of two
-// voxels in shared memory (zero outside the image, as the reference's padded
-// copy), computes the updated image m' = m - (alpha*d/||v||) v on the tile
-// plus a one-voxel halo, writes the tile of m', and evaluates the stencil of
-// m' on the tile for the next step's ||v'||^2 (deterministic grid sum).  A
-// step therefore reads the image once and writes it once (8 bytes per voxel)
-// and the ||v|| that every step needs before it can update comes out of the
-// previous kernel.  The end-of-sweep kernel provides ||v|| of the first
-// step; the last step also applies the positivity constraint and the
-// alpha/beta step control.
+// A step computes the updated image m' = m - (alpha*d/||v||) v(m) (zero
+// outside the image, as the reference's padded copy), writes it, and
+// evaluates the stencil of m' for the next step's ||v'||^2 (deterministic
+// grid sum) -- so it reads the image once and writes it once (8 bytes per
+// voxel), and the ||v|| that every step needs before it can update comes out
+// of the previous kernel.  Cone beam: a block stages its 32x8 voxel tile
+// with a halo of two voxels in shared memory.  2-D: warps walk down strips
+// of columns with the stencils in registers (k_tv_walk2d).  The end-of-sweep
+// kernel provides ||v|| of the first step; the last step also applies the
+// positivity constraint and the alpha/beta step control.
 #include <type_traits>
 #include "kernels.h"
 #include "reduce.cuh"
@@ -299,10 +299,6 @@ __device__ __forceinline__ const float *tv_src(const Inst &I, int step) {
 __device__ __forceinline__ float *tv_dst(const Inst &I, int step) {
   return (step & 1) ? I.tv_c : I.tv_b;
 }
-// 2-D: the stencil v of the image step `step` starts from
-__device__ __forceinline__ float *tv_v(const Inst &I, int step) {
-  return (step & 1) ? I.tv_vb : I.tv_va;
-}
 
 // End-of-iteration scalars (ASD_POCS_cuda.m:166-170) by the last block.
 __device__ __forceinline__ void finish_scalars(Scalars *s, double dg2) {
@@ -357,7 +353,6 @@ __global__ void __launch_bounds__(kThreads)
         const float gr =
             tv_grad<float>(TileAt<1, k3D>{t, tx + 1, ty + 1, k3D ? 1 : 0}, k3D);
         v[3] += gr * gr;
-        if (!k3D) I.tv_va[i] = gr;  // the first TV step's update reads it
       }
     }
     __syncthreads();  // the tile is reused by the next group member
@@ -459,246 +454,6 @@ __global__ void __launch_bounds__(kThreads)
         s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
         s->tv_coef_f = (float)s->tv_coef;
       }
-    }
-  }
-}
-
-// 2-D TV step.  A group is the block's kTilesPerBlock tiles as one 32 x 32
-// voxel tile.  The update m' = m - coef * v(m) needs the stencil v of the
-// step's starting image, which the previous step (or the end-of-sweep
-// kernel) evaluated for its norm and stored, so a group stages m and v on
-// the group plus a one-voxel halo (34 x 34), forms m' there without a
-// stencil, writes its four voxels per thread (rows ty, ty+8, ty+16, ty+24)
-// and evaluates one stencil per voxel -- v(m'), for the next norm, stored for
-// the next step.  The values are those of recomputing v here.
-//
-// A block walks `per_block` consecutive groups of its instance, staging the
-// next group's halo while it evaluates the current one, and leaves one
-// partial per group; the last block of the instance sums the partials in
-// group order, so the result is the same for every `per_block` (picked by
-// the host from the batch size).  Staging is by TMA when the instance has
-// tensor maps (nx a multiple of 4): one thread issues two 2-D tile loads
-// (m and v, box 40 x 34 from column x0 - 4, 16-byte aligned; zeros outside
-// the image) completing on an mbarrier, which every thread waits on with a
-// bounded number of tries -- past it the block records a fault and goes on.
-// Otherwise each thread stages its share with 4-byte cp.async (zero-filled
-// outside the image).
-constexpr int kGroupRows = kTileY * kTilesPerBlock;
-constexpr int kHaloW = kTileX + 2, kHaloH = kGroupRows + 2, kHaloN = kHaloW * kHaloH;
-constexpr int kHaloRounds = (kHaloN + kThreads - 1) / kThreads;
-constexpr int kBoxX0 = 3;  // column of x0 - 1 in the staged box (box starts at x0 - 4)
-static_assert(kTmBoxW == kTileX + 8 && kTmBoxH == kHaloH, "TMA box covers the halo");
-constexpr unsigned kTmBytes = 2u * kTmBoxW * kTmBoxH * 4u;  // m and v boxes
-// a box's slot in shared memory, rounded up to the 128-byte alignment of
-// tensor copies
-constexpr int kBoxFloats = (kTmBoxW * kTmBoxH + 31) / 32 * 32;
-constexpr int kWaitTries = 1 << 20;
-
-__device__ __forceinline__ void cp_async4(float *smem, const float *gmem, bool valid) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(gmem),
-               "r"(valid ? 4 : 0)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;\n" ::: "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-}
-__device__ __forceinline__ unsigned smem_u32(const void *p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-// true when the phase with the given parity has completed; false after
-// kWaitTries attempts
-__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, unsigned parity) {
-  const unsigned a = smem_u32(bar);
-  for (int i = 0; i < kWaitTries; i++) {
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        " selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (ok) return true;
-  }
-  return false;
-}
-__device__ __forceinline__ void tma_load_2d(float *dst, const CUtensorMap *map, int x, int y,
-                                            unsigned long long *bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%2, %3}], [%4];\n" ::"r"(smem_u32(dst)),
-      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-
-__global__ void __launch_bounds__(kThreads, 5)
-    k_tv_step2d(const Inst *__restrict__ insts, int step, int per_block) {
-  // [stage][m | v][row][column]: m (then m' in place) and v(m) of a group's
-  // halo region at columns kBoxX0 .. kBoxX0 + 33
-  __shared__ alignas(128) float tile[2][2][kBoxFloats];
-  __shared__ alignas(8) unsigned long long bar[2];
-  __shared__ float shf[kThreads / 32];
-  __shared__ int s_last;
-  const Inst &I = insts[blockIdx.z];
-  if (inst_done(I)) return;
-  const int ng = I.s->ng;
-  if (step >= ng) return;
-  const Dims D = I.d;
-  const dim3 gg = group_grid(D.nx, D.ny, 1, 1);
-  const int G = (int)(gg.x * gg.y);
-  const int nb = (G + per_block - 1) / per_block;
-  if ((int)blockIdx.x >= nb) return;
-  const int g_begin = blockIdx.x * per_block, g_end = min(G, g_begin + per_block);
-  const bool last = step == ng - 1;
-  const bool fused_finish = last && ng >= 2;
-  const float coef = I.s->tv_coef_f;
-  const float *src = tv_src(I, step);
-  float *dst = tv_dst(I, step);
-  const float *vin = tv_v(I, step);
-  float *vout = tv_v(I, step + 1);
-  const int tm_m = step == 0 ? kTmM : ((step & 1) ? kTmB : kTmC);
-  const int tm_v = (step & 1) ? kTmVb : kTmVa;
-  const bool tma = I.tmap != nullptr;  // block-uniform
-  const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
-  auto group_origin = [&](int g, int &x0, int &y0) {
-    x0 = (g % (int)gg.x) * kTileX;
-    y0 = (g / (int)gg.x) * kGroupRows;
-  };
-  auto stage = [&](int g, int st) {
-    int x0, y0;
-    group_origin(g, x0, y0);
-    if (tma) {
-      if (threadIdx.x == 0) {
-        // the buffer's previous contents were written by this block's
-        // threads (generic proxy) before the barrier that precedes this call
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        mbar_expect_tx(&bar[st], kTmBytes);
-        tma_load_2d(tile[st][0], I.tmap + tm_m, x0 - 4, y0 - 1, &bar[st]);
-        tma_load_2d(tile[st][1], I.tmap + tm_v, x0 - 4, y0 - 1, &bar[st]);
-      }
-      return;
-    }
-#pragma unroll
-    for (int j = 0; j < kHaloRounds; j++) {
-      const int k = threadIdx.x + j * kThreads;
-      if (k < kHaloN) {
-        const int r = k / kHaloW, c = k - r * kHaloW;
-        const int y = y0 - 1 + r, x = x0 - 1 + c;
-        const bool in = y >= 0 && y < D.ny && x >= 0 && x < D.nx;
-        const unsigned i = in ? (unsigned)y * D.nx + x : 0u;
-        cp_async4(&tile[st][0][r * kTmBoxW + kBoxX0 + c], src + i, in);
-        cp_async4(&tile[st][1][r * kTmBoxW + kBoxX0 + c], vin + i, in);
-      }
-    }
-    cp_async_commit();
-  };
-  if (tma && threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(I.tmap + tm_m)
-                 : "memory");
-    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(I.tmap + tm_v)
-                 : "memory");
-  }
-  __syncthreads();
-  stage(g_begin, 0);
-  for (int g = g_begin; g < g_end; g++) {
-    const int i = g - g_begin, st = i & 1;
-    if (tma) {
-      const unsigned parity = (unsigned)(i >> 1) & 1u;
-      if (!__syncthreads_and(mbar_wait(&bar[st], parity))) {
-        // the only copy in flight is this group's: record the fault, give it
-        // one more bounded wait and leave the groups (the instance's sums
-        // still close, so the launch ends normally)
-        if (threadIdx.x == 0) {
-          if (I.fault) atomicOr(I.fault, kFaultTmaWait);
-          mbar_wait(&bar[st], parity);
-        }
-        __syncthreads();
-        break;
-      }
-    } else {
-      cp_async_wait_all();
-      __syncthreads();
-    }
-    // m' = m - coef * v in place (zero outside the image: staged as zeros)
-#pragma unroll
-    for (int j = 0; j < kHaloRounds; j++) {
-      const int k = threadIdx.x + j * kThreads;
-      if (k < kHaloN) {
-        const int r = k / kHaloW, c = r * kTmBoxW + kBoxX0 + k - r * kHaloW;
-        tile[st][0][c] = tile[st][0][c] - coef * tile[st][1][c];
-      }
-    }
-    __syncthreads();
-    // the next group's halo arrives while this one is evaluated (its buffer
-    // was last read two groups ago, before the barrier above)
-    if (g + 1 < g_end) stage(g + 1, st ^ 1);
-    int x0, y0;
-    group_origin(g, x0, y0);
-    float v = 0.f;
-#pragma unroll
-    for (int k = 0; k < kTilesPerBlock; k++) {
-      const int r = ty + kTileY * k;
-      const int ix = x0 + tx, iy = y0 + r;
-      if (ix < D.nx && iy < D.ny) {
-        const unsigned i = (unsigned)iy * D.nx + ix;
-        const auto u = [&](int dx, int dy, int) {
-          return tile[st][0][(r + 1 + dy) * kTmBoxW + kBoxX0 + tx + 1 + dx];
-        };
-        const float mn = u(0, 0, 0);
-        if (fused_finish) {
-          const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
-          const float f0 = I.m[i];
-          const float dlt = mc - f0;
-          v += dlt * dlt;
-          I.m[i] = mc;
-          I.m_pre[i] = mc;
-        } else {
-          dst[i] = mn;
-          if (!last) {
-            const float gr = tv_grad2f(u);
-            v += gr * gr;
-            vout[i] = gr;  // the next step's update reads it
-          }
-        }
-      }
-    }
-    // this group's partial (block_sum_f ends with a barrier)
-    const float vv[1] = {v};
-    float bs[1];
-    block_sum_f<kThreads, 1>(vv, bs, shf);
-    if (threadIdx.x == 0) I.partials[g] = (double)bs[0];
-  }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    s_last = atomicAdd(I.counter, 1u) == (unsigned)nb - 1;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  double tot[1];
-  grid_sum_final<kThreads, 1>(I.partials, I.counter, G, tot);
-  if (threadIdx.x == 0) {
-    Scalars *s = I.s;
-    if (fused_finish) {
-      finish_scalars(s, tot[0]);
-    } else if (!last) {
-      s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
-      s->tv_coef_f = (float)s->tv_coef;
     }
   }
 }

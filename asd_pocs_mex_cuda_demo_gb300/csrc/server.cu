@@ -78,7 +78,7 @@ struct Lane {
   cudaStream_t st = nullptr;
   int S = 0;
   Inst *d_inst = nullptr;          // S descriptors
-  int *d_flags = nullptr;          // S done flags, then the lane's fault word
+  int *d_flags = nullptr;          // S done flags
   Scalars *d_dead = nullptr;       // scalars of an empty slot (done = 1)
   char *geo = nullptr;             // the protocol's geometry block
   size_t geo_bytes = 0;
@@ -178,7 +178,6 @@ Dims inst_dims(const asdpocs_geometry &g) {
 Inst empty_slot(const Lane &L, int s) {
   Inst I = L.tmpl;
   I.s = L.d_dead;
-  I.fault = (unsigned *)(L.d_flags + L.S);
   const size_t M = (size_t)L.g.na * L.g.nb;
   const size_t N = (size_t)L.g.nx * L.g.ny * L.g.nz;
   I.cor = L.tmpl.cor + (size_t)(s / kShareSlots) * M * kShareSlots + s % kShareSlots;
@@ -199,8 +198,7 @@ bool lane_create(asdpocs_server sv, Lane &L) {
   const int groups = (L.S + kShareSlots - 1) / kShareSlots;
   SV_CUDA(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking));
   SV_CUDA(cudaMalloc(&L.d_inst, sizeof(Inst) * L.S));
-  SV_CUDA(cudaMalloc(&L.d_flags, sizeof(int) * (L.S + 1)));
-  SV_CUDA(cudaMemsetAsync(L.d_flags, 0, sizeof(int) * (L.S + 1), L.st));
+  SV_CUDA(cudaMalloc(&L.d_flags, sizeof(int) * L.S));
   SV_CUDA(cudaMalloc(&L.d_dead, sizeof(Scalars)));
   const size_t N = (size_t)L.g.nx * L.g.ny * L.g.nz;
   const InstLayout gl = layout_instance(L.g, 0, (size_t)groups * kShareSlots * M,
@@ -291,7 +289,6 @@ bool admit(asdpocs_server sv, Lane &L, int s, Job *J) {
   SV_CUDA(cudaMemsetAsync(b, 0, J->lay.bytes, sv->upload));
   Inst I = empty_slot(L, s);
   bind_state(I, b, J->lay);
-  SV_CUDA(bind_tensor_maps(I, b, J->lay, sv->upload));
   SV_CUDA(cudaMemcpyAsync(b + J->lay.P, J->P.data(), J->P.size() * 4,
                           cudaMemcpyHostToDevice, sv->upload));
   if (J->has_m0)
@@ -355,14 +352,14 @@ bool launch_iteration(asdpocs_server sv, Lane &L) {
     L.spare.pop_back();
   } else {
     SV_CUDA(cudaEventCreateWithFlags(&f.ev, cudaEventDisableTiming));
-    SV_CUDA(cudaMallocHost(&f.flags, sizeof(int) * (L.S + 1)));
+    SV_CUDA(cudaMallocHost(&f.flags, sizeof(int) * L.S));
   }
   f.owner.assign(L.S, 0);
   for (int s = 0; s < L.S; s++)
     if (L.slot_job[s]) f.owner[s] = L.slot_job[s]->id;
   SV_CUDA(cudaGraphLaunch(L.exec, L.st));
   SV_CUDA(launch_gather_done(L.d_inst, L.S, L.d_flags, L.st));
-  SV_CUDA(cudaMemcpyAsync(f.flags, L.d_flags, sizeof(int) * (L.S + 1),
+  SV_CUDA(cudaMemcpyAsync(f.flags, L.d_flags, sizeof(int) * L.S,
                           cudaMemcpyDeviceToHost, L.st));
   SV_CUDA(cudaEventRecord(f.ev, L.st));
   L.inflight.push_back(std::move(f));
@@ -393,11 +390,6 @@ bool lane_step(asdpocs_server sv, Lane &L, bool &progress) {
     const cudaError_t q = cudaEventQuery(f.ev);
     if (q == cudaErrorNotReady) break;
     SV_CUDA(q);
-    if (f.flags[L.S]) {
-      if (sv->error.empty())
-        sv->error = "a TV step's tile copy did not complete within its wait limit";
-      return false;
-    }
     for (int s = 0; s < L.S; s++) {
       // the flag belongs to the job that held the slot when the iteration
       // was queued; act on it only if that job still holds it

@@ -316,14 +316,17 @@ def test_shared_geometry_groups_with_remainder(gpu):
             assert np.array_equal(pl.image(0), batch[k]), k
 
 
-@pytest.mark.parametrize("nx,ny,batch", [(256, 256, 80), (100, 70, 3), (36, 20, 2),
-                                         (4, 3, 2), (50, 30, 2)])
-def test_tv_staging_by_tensor_copies_equals_cp_async(gpu, monkeypatch, nx, ny, batch):
-    """The 2-D TV step stages its tiles by TMA tensor copies when the rows are
-    16-byte aligned (nx % 4 == 0) and by cp.async otherwise or when
-    ASDPOCS_NO_TMA is set; both give the same bits, at any number of groups
-    per block (256 x 256 at batch 80 walks two groups per block), with boxes
-    partly or wholly outside small images."""
+@pytest.mark.parametrize("nx,ny,batch,check", [
+    (384, 384, 60, (0, 59)),   # 84 strip bands x 60: two bands per walk in the batch
+    (121, 70, 3, (0, 2)),      # odd nx: per-column accesses; ragged strips and bands
+    (36, 20, 2, (1,)),         # one strip, one band
+    (4, 3, 2, (0,)),
+    (1, 5, 2, (1,)),
+])
+def test_tv_walks_batch_equals_alone(gpu, nx, ny, batch, check):
+    """The 2-D TV step walks strips of 60 output columns in bands of 32 rows,
+    several bands per walk when the batch is large; each instance's result
+    is the same bits as its run alone (one band per walk)."""
     na, nv = 48, 8
     SO, OD, det = 541.0, 408.0, 1.0
     vx = phantoms.fov_voxel_size(SO, OD, det, na, max(nx, ny))
@@ -332,18 +335,16 @@ def test_tv_staging_by_tensor_copies_equals_cp_async(gpu, monkeypatch, nx, ny, b
                 phi_vec=phi, maxnumIter=2, numOfgradients=3, alpha=0.05)
     rng = np.random.default_rng(nx * 1000 + ny)
     Ps = [rng.random(na * nv).astype(np.float32) for _ in range(batch)]
-
-    def run():
-        with pkg.Plan([para] * batch, [phi] * batch) as pl:
-            for k, P in enumerate(Ps):
-                pl.set_sinogram(k, P)
+    with pkg.Plan([para] * batch, [phi] * batch) as pl:
+        for k, P in enumerate(Ps):
+            pl.set_sinogram(k, P)
+        pl.reset()
+        pl.run()
+        out = [pl.image(k) for k in range(batch)]
+    for k in check:
+        with pkg.Plan(para, phi) as pl:
+            pl.set_sinogram(0, Ps[k])
             pl.reset()
             pl.run()
-            return [pl.image(k) for k in range(batch)]
-
-    tma = run()
-    monkeypatch.setenv("ASDPOCS_NO_TMA", "1")
-    plain = run()
-    for k in range(batch):
-        assert np.array_equal(tma[k], plain[k]), k
-        assert np.isfinite(tma[k]).all()
+            assert np.array_equal(pl.image(0), out[k]), k
+        assert np.isfinite(out[k]).all()
