@@ -66,13 +66,14 @@ __device__ __forceinline__ T tv_grad2(const U &u) {
 // FP32 form of the 2-D stencil with every rounding explicit, so that a
 // kernel holding its terms in registers reproduces it bit for bit.  With
 // dx = f(x,y) - f(x-1,y), dy = f(x,y) - f(x,y-1) at a voxel, its terms are
-//   r1 = 1/sqrt(eps + dx^2 + dy^2),  g1 = (dx + dy) * r1,  q = dx * r1,
-//   r3 = 1/sqrt(eps + dy^2 + dx^2),  t = dy * r3
-// and v(x,y) = (g1(x,y) - q(x+1,y)) - t(x,y+1): the reference's second term
-// is the right neighbour's q (same differences, same sum order) and its
-// third the lower neighbour's t (its sum in the other order).  1/sqrt is
-// the approximate reciprocal square root; den >= eps is never subnormal, so
-// flushing subnormals changes nothing.
+//   r = 1/sqrt(eps + dx^2 + dy^2),  g1 = (dx + dy) * r,  q = dx * r,
+//   t = dy * r
+// and v(x,y) = (g1(x,y) - q(x+1,y)) - t(x,y+1): the reference's second and
+// third terms (FP64 there) are the right neighbour's q and the lower
+// neighbour's t -- the same differences under the same square root, whose
+// two squares the reference sums in the other order for the third.  1/sqrt
+// is the approximate reciprocal square root; den >= eps is never
+// subnormal, so flushing subnormals changes nothing.
 __device__ __forceinline__ float tv_rsqrt(float x) {
   float r;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
@@ -83,9 +84,8 @@ struct Tv2Terms {
 };
 __device__ __forceinline__ Tv2Terms tv2_terms(float dx, float dy) {
   const float eps = tv_eps<float>();
-  const float r1 = tv_rsqrt(__fmaf_rn(dy, dy, __fmaf_rn(dx, dx, eps)));
-  const float r3 = tv_rsqrt(__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, eps)));
-  return Tv2Terms{__fmul_rn(__fadd_rn(dx, dy), r1), __fmul_rn(dx, r1), __fmul_rn(dy, r3)};
+  const float r = tv_rsqrt(__fmaf_rn(dy, dy, __fmaf_rn(dx, dx, eps)));
+  return Tv2Terms{__fmul_rn(__fadd_rn(dx, dy), r), __fmul_rn(dx, r), __fmul_rn(dy, r)};
 }
 __device__ __forceinline__ float tv2_combine(float g1, float q_right, float t_below) {
   return __fsub_rn(__fsub_rn(g1, q_right), t_below);
@@ -478,7 +478,11 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kWalkWarps = 4;
 constexpr int kWalkOut = 60;   // output columns of a strip
 constexpr int kBandRows = 32;  // output rows of a partial
-constexpr int kWalkAhead = 4;  // rows loaded ahead of the one in use
+constexpr int kWalkChunk = 4;  // rows per chunk (a band ends at a chunk's end)
+constexpr int kWalkRing = 16;  // rows of m in flight per warp (shared-memory ring)
+static_assert(4 % kWalkChunk == 0, "bands and the steady chunks line up");
+static_assert(kWalkRing % kWalkChunk == 0 && (kWalkRing & (kWalkRing - 1)) == 0,
+              "a chunk's rows sit in consecutive ring slots");
 
 __host__ __device__ __forceinline__ int walk_strips(int nx) {
   return (nx + kWalkOut - 1) / kWalkOut;
@@ -511,9 +515,24 @@ struct WalkField {
 // 2: the last of several steps -- positivity, the change norm, and m' into
 // the image and m_pre.  kPair: nx is even, so a lane's two columns are both
 // inside or both outside the image and 8-byte aligned (one access each).
+// 4- and 8-byte asynchronous copies into shared memory, zero-filled when
+// `valid` is false (nothing is read then; `gmem` must still be mapped)
+__device__ __forceinline__ void cp_async_4(float *smem, const float *gmem, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(smem)),
+               "l"(gmem), "r"(valid ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_8(float *smem, const float *gmem, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(smem)),
+               "l"(gmem), "r"(valid ? 8 : 0)
+               : "memory");
+}
+
 template <int kMode, bool kPair>
 __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1, int xa,
-                                        int strip, int S, float coef) {
+                                        int strip, int S, float coef, float2 *ring) {
   const Dims D = I.d;
   const int lane = threadIdx.x & 31;
   const float *src = tv_src(I, step);
@@ -523,104 +542,130 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
   const bool outa = outl && ina, outb = outl && inb;
   const int jl0 = y0 - 2, jl1 = min(D.ny, y1 + 2);  // rows of m read
   const int j1 = y1 + 2;                            // rows walked: jl0 .. j1 - 1
-  auto load = [&](int j, float &a, float &b) {
-    const bool r = j >= max(jl0, 0) && j < jl1;
-    const int i = j * D.nx + xa;
+  const float coef_a = ina ? coef : 0.f, coef_b = inb ? coef : 0.f;
+  // Rows of m stream through a ring of kWalkRing rows per warp (each lane
+  // its two columns), copied asynchronously kWalkRing - 1 rows ahead of the
+  // one in use and zero-filled outside the image and the walk; one copy
+  // group per row, so "row j has landed" is a fixed wait depth.
+  float2 *const my = ring + lane;  // slot s of this lane: my[32 * s]
+  const float *la = src + (ina ? xa : 0), *lb = src + (inb ? xa + 1 : 0);
+  auto fetch = [&](int j, int slot) {
+    const bool r = (unsigned)j < (unsigned)jl1;  // 0 <= j < jl1
+    const int off = r ? j * D.nx : 0;
+    float *d = (float *)(my + 32 * slot);
     if (kPair) {
-      const float2 v = (r && ina) ? __ldg((const float2 *)(src + i)) : make_float2(0.f, 0.f);
-      a = v.x;
-      b = v.y;
+      cp_async_8(d, la + off, r && ina);
     } else {
-      a = (r && ina) ? __ldg(src + i) : 0.f;
-      b = (r && inb) ? __ldg(src + i + 1) : 0.f;
+      cp_async_4(d, la + off, r && ina);
+      cp_async_4(d + 1, lb + off, r && inb);
     }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
-  float ra[kWalkAhead], rb[kWalkAhead];
-#pragma unroll
-  for (int k = 0; k < kWalkAhead; k++) load(jl0 + k, ra[k], rb[k]);
+  for (int k = 0; k < kWalkRing - 1; k++) fetch(jl0 + k, k);
   WalkField f1{0.f, 0.f, 0.f, 0.f}, f2{0.f, 0.f, 0.f, 0.f};
   float acc = 0.f;
-  for (int j0 = jl0; j0 < j1; j0 += kWalkAhead) {
+  // one partial from the band whose last output row is o
+  auto flush = [&](int o) {
 #pragma unroll
-    for (int k = 0; k < kWalkAhead; k++) {
-      const int j = j0 + k;
-      const float ma = ra[k], mb = rb[k];
-      load(j + kWalkAhead, ra[k], rb[k]);
-      // v(m) of row j - 1, then m' of row j - 1 (zero outside the image)
-      const float m1a = f1.pa, m1b = f1.pb;
-      float va, vb;
-      f1.push(ma, mb, va, vb);
-      const int o1 = j - 1;
+    for (int w = 16; w > 0; w >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, w);
+    if (lane == 0) I.partials[(o / kBandRows) * S + strip] = (double)acc;
+    acc = 0.f;
+  };
+  // row j of m in: v(m) and m' of row j - 1, v(m') of row j - 2
+  // rslot: ring slot of row j; its predecessor's slot receives row j + 15
+  auto walk_row = [&](auto checked, int j, int rslot) {
+    constexpr bool kC = decltype(checked)::value;
+    fetch(j + kWalkRing - 1, (rslot + kWalkRing - 1) & (kWalkRing - 1));
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(kWalkRing - 1) : "memory");
+    const float2 mab = my[32 * rslot];
+    const float m1a = f1.pa, m1b = f1.pb;
+    float va, vb;
+    f1.push(mab.x, mab.y, va, vb);
+    const int o1 = j - 1;
+    float pa, pb;
+    if (kC) {
       const bool row1 = o1 >= 0 && o1 < D.ny;
-      const float pa = (row1 && ina) ? __fmaf_rn(-coef, va, m1a) : 0.f;
-      const float pb = (row1 && inb) ? __fmaf_rn(-coef, vb, m1b) : 0.f;
-      const bool out1 = o1 >= y0 && o1 < y1;  // warp-uniform
-      if (kMode == 2) {
-        if (out1) {
-          const int i = o1 * D.nx + xa;
-          const float mca = pa < 0.f ? 0.f : pa;  // imgTVGradMin.cpp:110-116
-          const float mcb = pb < 0.f ? 0.f : pb;
-          if (kPair) {
-            if (outa) {
-              const float2 f0 = *(const float2 *)(I.m + i);
-              const float da = mca - f0.x, db = mcb - f0.y;
-              acc += da * da;
-              acc += db * db;
-              *(float2 *)(I.m + i) = make_float2(mca, mcb);
-              *(float2 *)(I.m_pre + i) = make_float2(mca, mcb);
-            }
-          } else {
-            if (outa) {
-              const float d = mca - I.m[i];
-              acc += d * d;
-              I.m[i] = mca;
-              I.m_pre[i] = mca;
-            }
-            if (outb) {
-              const float d = mcb - I.m[i + 1];
-              acc += d * d;
-              I.m[i + 1] = mcb;
-              I.m_pre[i + 1] = mcb;
-            }
+      pa = (row1 && ina) ? __fmaf_rn(-coef, va, m1a) : 0.f;
+      pb = (row1 && inb) ? __fmaf_rn(-coef, vb, m1b) : 0.f;
+    } else {
+      pa = __fmaf_rn(-coef_a, va, m1a);
+      pb = __fmaf_rn(-coef_b, vb, m1b);
+    }
+    const bool out1 = !kC || (o1 >= y0 && o1 < y1);  // warp-uniform
+    if (kMode == 2) {
+      if (out1) {
+        const int i = o1 * D.nx + xa;
+        const float mca = pa < 0.f ? 0.f : pa;  // imgTVGradMin.cpp:110-116
+        const float mcb = pb < 0.f ? 0.f : pb;
+        if (kPair) {
+          if (outa) {
+            const float2 f0 = *(const float2 *)(I.m + i);
+            const float da = mca - f0.x, db = mcb - f0.y;
+            acc += da * da;
+            acc += db * db;
+            *(float2 *)(I.m + i) = make_float2(mca, mcb);
+            *(float2 *)(I.m_pre + i) = make_float2(mca, mcb);
           }
-        }
-      } else {
-        if (out1) {
-          const int i = o1 * D.nx + xa;
-          if (kPair) {
-            if (outa) *(float2 *)(dst + i) = make_float2(pa, pb);
-          } else {
-            if (outa) dst[i] = pa;
-            if (outb) dst[i + 1] = pb;
+        } else {
+          if (outa) {
+            const float d = mca - I.m[i];
+            acc += d * d;
+            I.m[i] = mca;
+            I.m_pre[i] = mca;
           }
-        }
-        if (kMode == 0) {
-          // v(m') of row j - 2
-          float wa, wb;
-          f2.push(pa, pb, wa, wb);
-          const int o2 = j - 2;
-          if (o2 >= y0 && o2 < y1) {
-            if (outa) acc += wa * wa;
-            if (outb) acc += wb * wb;
+          if (outb) {
+            const float d = mcb - I.m[i + 1];
+            acc += d * d;
+            I.m[i + 1] = mcb;
+            I.m_pre[i + 1] = mcb;
           }
         }
       }
-      // the band of the row just accumulated is complete: one partial
-      if (kMode != 1) {
-        const int o = kMode == 2 ? o1 : j - 2;
-        if (o >= y0 && o < y1 && ((o + 1) % kBandRows == 0 || o + 1 == y1)) {
-#pragma unroll
-          for (int w = 16; w > 0; w >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, w);
-          if (lane == 0) I.partials[(o / kBandRows) * S + strip] = (double)acc;
-          acc = 0.f;
+    } else {
+      if (out1) {
+        const int i = o1 * D.nx + xa;
+        if (kPair) {
+          if (outa) *(float2 *)(dst + i) = make_float2(pa, pb);
+        } else {
+          if (outa) dst[i] = pa;
+          if (outb) dst[i + 1] = pb;
+        }
+      }
+      if (kMode == 0) {
+        float wa, wb;
+        f2.push(pa, pb, wa, wb);
+        const int o2 = j - 2;
+        if (!kC || (o2 >= y0 && o2 < y1)) {
+          if (outa) acc += wa * wa;
+          if (outb) acc += wb * wb;
         }
       }
     }
+    if (kC && kMode != 1) {
+      const int o = kMode == 2 ? o1 : j - 2;
+      if (o >= y0 && o < y1 && ((o + 1) % kBandRows == 0 || o + 1 == y1)) flush(o);
+    }
+  };
+  // steady chunks: outputs of rows j0 - 2 .. j0 + 1 all inside [y0, y1 - 1)
+  for (int j0 = jl0; j0 < j1; j0 += kWalkChunk) {
+    const int s0 = (j0 - jl0) & (kWalkRing - 1);  // chunks never wrap the ring
+    if (kMode == 0 && j0 >= y0 + 2 && j0 <= y1 - 3) {
+#pragma unroll
+      for (int k = 0; k < kWalkChunk; k++) walk_row(std::false_type(), j0 + k, s0 + k);
+      // bands start at multiples of 32 (so does y0) and steady chunks at
+      // y0 - 2 plus a multiple of 4: a band can only end at a chunk's end
+      if ((j0 + 2) % kBandRows == 0) flush(j0 + 1);
+    } else {
+#pragma unroll
+      for (int k = 0; k < kWalkChunk; k++) walk_row(std::true_type(), j0 + k, s0 + k);
+    }
   }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");  // the ring's last copies
 }
 
 __global__ void __launch_bounds__(kWalkWarps * 32, 8)
     k_tv_walk2d(const Inst *__restrict__ insts, int step, int bands) {
+  __shared__ float2 ring[kWalkWarps][kWalkRing * 32];
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
@@ -639,14 +684,14 @@ __global__ void __launch_bounds__(kWalkWarps * 32, 8)
   const float coef = I.s->tv_coef_f;
   const bool pair = (D.nx & 1) == 0;
   if (!last)
-    pair ? tv_walk<0, true>(I, step, y0, y1, xa, strip, S, coef)
-         : tv_walk<0, false>(I, step, y0, y1, xa, strip, S, coef);
+    pair ? tv_walk<0, true>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5])
+         : tv_walk<0, false>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5]);
   else if (ng == 1)
-    pair ? tv_walk<1, true>(I, step, y0, y1, xa, strip, S, coef)
-         : tv_walk<1, false>(I, step, y0, y1, xa, strip, S, coef);
+    pair ? tv_walk<1, true>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5])
+         : tv_walk<1, false>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5]);
   else
-    pair ? tv_walk<2, true>(I, step, y0, y1, xa, strip, S, coef)
-         : tv_walk<2, false>(I, step, y0, y1, xa, strip, S, coef);
+    pair ? tv_walk<2, true>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5])
+         : tv_walk<2, false>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5]);
   if (last && ng == 1) return;  // nothing to sum: k_finish_iter ends the iteration
   // the walk that finishes last sums the instance's band partials
   unsigned ticket = 0;
