@@ -432,7 +432,8 @@ InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
   o.tvb = off; off += per_img;
   o.tvc = off; off += per_img;
   o.rmse = off; off += st ? align256((size_t)(max_iter + 1) * 8) : 0;
-  o.part = off; off += st ? align256(nblk * kMaxReduceK * 8) : 0;
+  const size_t nparts = std::max(nblk * kMaxReduceK, (size_t)tv_partials_for(d));
+  o.part = off; off += st ? align256(nparts * 8) : 0;
   o.cnt = off; off += st ? 256 : 0;
   o.scal = off; off += st ? align256(sizeof(Scalars)) : 0;
   o.cor = off; off += geo ? align256(cor_floats * 4) : 0;

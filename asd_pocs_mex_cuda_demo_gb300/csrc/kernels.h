@@ -48,6 +48,8 @@ cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
                                int ng, cudaStream_t st);
 
 int reduce_blocks_for(const Dims &d);
+// Reduction partials of the 2-D TV step (one per strip and band of rows).
+int tv_partials_for(const Dims &d);
 
 // Copies Inst::s->done of n instances into the device array out[n].
 cudaError_t launch_gather_done(const Inst *insts, int n, int *out,

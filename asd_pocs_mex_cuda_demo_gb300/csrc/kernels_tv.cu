@@ -28,9 +28,6 @@ constexpr int kThreads = kTileThreads;
 __device__ __forceinline__ double tv_q(double num, double den) {
   return num / sqrt(den);
 }
-__device__ __forceinline__ float tv_q(float num, float den) {
-  return num * rsqrtf(den);
-}
 
 template <class T>
 __device__ __forceinline__ T tv_eps();
@@ -123,9 +120,48 @@ __device__ __forceinline__ T tv_grad3(const U &u) {
   return g1 + g2 + g3 + g4;
 }
 
+// FP32 form of the 3-D stencil with every rounding explicit.  At a voxel
+// with differences dx, dy, dz to its -x, -y, -z neighbours,
+//   r = 1/sqrt(eps + dx^2 + dy^2 + dz^2)
+// and the reference's four terms are
+//   v = (((6c - 2(xm + ym + zm)) r + (2c - 2zp) r(+z)) + (2c - 2yp) r(+y))
+//       + (2c - 2xp) r(+x):
+// the denominators of its second to fourth terms are those of the +z, +y
+// and +x neighbours' first terms, in the same order.
+__device__ __forceinline__ float tv3_r(float dx, float dy, float dz) {
+  return tv_rsqrt(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, tv_eps<float>()))));
+}
+__device__ __forceinline__ float tv3_combine(float c, float xm, float ym, float zm, float xp,
+                                             float yp, float zp, float r, float rx, float ry,
+                                             float rz) {
+  const float c2 = __fmul_rn(2.f, c);
+  const float g1 = __fmul_rn(
+      __fsub_rn(__fmul_rn(6.f, c), __fmul_rn(2.f, __fadd_rn(__fadd_rn(xm, ym), zm))), r);
+  const float g2 = __fmul_rn(__fsub_rn(c2, __fmul_rn(2.f, zp)), rz);
+  const float g3 = __fmul_rn(__fsub_rn(c2, __fmul_rn(2.f, yp)), ry);
+  const float g4 = __fmul_rn(__fsub_rn(c2, __fmul_rn(2.f, xp)), rx);
+  return __fadd_rn(__fadd_rn(__fadd_rn(g1, g2), g3), g4);
+}
+template <class U>
+__device__ __forceinline__ float tv_grad3f(const U &u) {
+  const float c = u(0, 0, 0);
+  const float xm = u(-1, 0, 0), ym = u(0, -1, 0), zm = u(0, 0, -1);
+  const float xp = u(1, 0, 0), yp = u(0, 1, 0), zp = u(0, 0, 1);
+  const float r = tv3_r(__fsub_rn(c, xm), __fsub_rn(c, ym), __fsub_rn(c, zm));
+  const float rx = tv3_r(__fsub_rn(xp, c), __fsub_rn(xp, u(1, -1, 0)), __fsub_rn(xp, u(1, 0, -1)));
+  const float ry = tv3_r(__fsub_rn(yp, u(-1, 1, 0)), __fsub_rn(yp, c), __fsub_rn(yp, u(0, 1, -1)));
+  const float rz = tv3_r(__fsub_rn(zp, u(-1, 0, 1)), __fsub_rn(zp, u(0, -1, 1)), __fsub_rn(zp, c));
+  return tv3_combine(c, xm, ym, zm, xp, yp, zp, r, rx, ry, rz);
+}
+
 template <class T, class U>
 __device__ __forceinline__ T tv_grad(const U &u, bool is3d) {
-  if (is3d) return tv_grad3<T>(u);
+  if (is3d) {
+    if constexpr (std::is_same<T, float>::value)
+      return tv_grad3f(u);
+    else
+      return tv_grad3<T>(u);
+  }
   if constexpr (std::is_same<T, float>::value)
     return tv_grad2f(u);
   else
@@ -378,90 +414,12 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// TV step `step` (imgTVGradMin.cpp:62-108): m' = m - tv_coef*v(m) into the
-// other buffer, and ||v(m')|| for the next step.  The last step (when there
-// are at least two, so that it reads a work buffer) also does the work of
-// k_finish_iter: positivity, dg, alpha/beta, and writes m' back to the
-// image and to m_pre.
-template <bool k3D>
-__global__ void __launch_bounds__(kThreads)
-    k_tv_step(const Inst *__restrict__ insts, int step) {
-  __shared__ Tile<2, k3D> t2;
-  __shared__ Tile<1, k3D> t1;
-  const Inst &I = insts[blockIdx.z];
-  if (inst_done(I)) return;
-  const int ng = I.s->ng;
-  if (step >= ng) return;
-  const Dims D = I.d;
-  const OwnBlock ob = own_block(group_grid(D.nx, D.ny, D.nz, 1));
-  if (ob.bid < 0) return;
-  const bool last = step == ng - 1;
-  const bool fused_finish = last && ng >= 2;
-  const float coef = I.s->tv_coef_f;
-  const float *src = tv_src(I, step);
-  float *dst = tv_dst(I, step);
-  const int tx = threadIdx.x % kTileX, ty = threadIdx.x / kTileX;
-  float v[1] = {0.f};
-  for (int g = 0; g < kTilesPerBlock; g++) {
-    int x0, y0, z;
-    if (!group_tile(D.ny, D.nz, g, x0, y0, z)) break;
-    load_tile(t2, src, D, x0, y0, z);
-    __syncthreads();
-    // m' on the tile and a one-voxel halo (zero outside the image)
-    {
-      constexpr int W = Tile<1, k3D>::W, Hh = Tile<1, k3D>::Hh, Dd = Tile<1, k3D>::D;
-      for (int k = threadIdx.x; k < W * Hh * Dd; k += kThreads) {
-        const int hx = k % W, hy = (k / W) % Hh, hz = k / (W * Hh);
-        const int x = x0 - 1 + hx, y = y0 - 1 + hy, zz = k3D ? z - 1 + hz : z;
-        float val = 0.f;
-        if (x >= 0 && y >= 0 && zz >= 0 && x < D.nx && y < D.ny && zz < D.nz) {
-          const TileAt<2, k3D> u{t2, hx + 1, hy + 1, k3D ? hz + 1 : 0};
-          val = u(0, 0, 0) - coef * tv_grad<float>(u, k3D);
-        }
-        t1.v[hz][hy][hx] = val;
-      }
-    }
-    __syncthreads();
-    const int ix = x0 + tx, iy = y0 + ty;
-    if (ix < D.nx && iy < D.ny) {
-      const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
-      const TileAt<1, k3D> u{t1, tx + 1, ty + 1, k3D ? 1 : 0};
-      const float mn = u(0, 0, 0);
-      if (fused_finish) {
-        const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin.cpp:110-116
-        const float f0 = I.m[i];
-        const float dlt = mc - f0;
-        v[0] += dlt * dlt;
-        I.m[i] = mc;
-        I.m_pre[i] = mc;
-      } else {
-        dst[i] = mn;
-        if (!last) {
-          const float gr = tv_grad<float>(u, k3D);
-          v[0] += gr * gr;
-        }
-      }
-    }
-    __syncthreads();  // both tiles are reused by the next group member
-  }
-  double tot[1];
-  if (grid_sum<kThreads, 1>(v, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
-    if (threadIdx.x == 0) {
-      Scalars *s = I.s;
-      if (fused_finish) {
-        finish_scalars(s, tot[0]);
-      } else if (!last) {
-        s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
-        s->tv_coef_f = (float)s->tv_coef;
-      }
-    }
-  }
-}
-
-// 2-D TV step as column walks.  A warp owns a strip of 64 image columns
-// (lane l: columns xs - 2 + 2l and the next) and walks down it a row at a
-// time, holding everything in registers: each new row of m gives, with one
-// shuffle from each neighbour lane, the stencil terms of that row
+// 2-D TV step (imgTVGradMin.cpp:62-116: m' = m - alpha*d*v(m)/||v(m)||,
+// positivity after the last step) as column walks.  A warp owns a strip of
+// 64 image columns (lane l: columns xs - 2 + 2l and the next) and walks
+// down it a row at a time, holding everything in registers: each new row
+// of m gives, with one shuffle from each neighbour lane, the stencil terms
+// of that row
 // (tv2_terms), which complete v(m) one row up; m' = m - coef * v(m) follows
 // (zero outside the image), and the same walk over the rows of m' completes
 // v(m') two rows up.  The lanes at the strip's edges only feed their
@@ -471,16 +429,16 @@ __global__ void __launch_bounds__(kThreads)
 // voxel) and evaluates two stencils per voxel, both in registers.
 //
 // ||v(m')||^2 (or, in the last step, the positivity-change norm) is summed
-// per band of 32 output rows of a strip -- lanes in row order, then an xor
+// per band of 16 output rows of a strip -- lanes in row order, then an xor
 // butterfly -- and the walk that finishes last sums the band partials of
 // the instance in order; walks of `bands` consecutive bands (chosen by the
 // host from the batch size) therefore give the same bits for every choice.
 constexpr int kWalkWarps = 4;
 constexpr int kWalkOut = 60;   // output columns of a strip
-constexpr int kBandRows = 32;  // output rows of a partial
+constexpr int kBandRows = 16;  // output rows of a partial
 constexpr int kWalkChunk = 4;  // rows per chunk (a band ends at a chunk's end)
 constexpr int kWalkRing = 16;  // rows of m in flight per warp (shared-memory ring)
-static_assert(4 % kWalkChunk == 0, "bands and the steady chunks line up");
+static_assert(4 % kWalkChunk == 0 && kBandRows % 4 == 0, "bands and the steady chunks line up");
 static_assert(kWalkRing % kWalkChunk == 0 && (kWalkRing & (kWalkRing - 1)) == 0,
               "a chunk's rows sit in consecutive ring slots");
 
@@ -719,6 +677,217 @@ __global__ void __launch_bounds__(kWalkWarps * 32, 8)
   }
 }
 
+// Cone-beam TV step (imgTVGradMin3D.cpp:83-170) as z walks (2.5-D
+// blocking).  A block owns a tile of
+// 32 x 16 output voxels in (x, y) and walks down z through a range of
+// slices.  Each slice of m is staged with a two-voxel halo (36 x 20, zero
+// outside the image) into a ring of four slices by cp.async, two slices
+// ahead.  Per slice k the block forms, on shrinking halo regions:
+//   A  r(k) = 1/sqrt(eps + dx^2 + dy^2 + dz^2) of m       (35 x 19)
+//   B  v(m) of slice k - 1 from m and r (tv3_combine), and
+//      m' = m - coef v(m), zero outside the image          (34 x 18)
+//   C  r'(k - 1) of m'                                      (33 x 17)
+//   D  v(m') of slice k - 2 on the tile: ||v(m')||^2, and m' written out.
+// so each voxel is read once and written once, with four passes of stencil
+// arithmetic over slightly larger regions instead of five full stencils.
+// ||v(m')||^2 (or the last step's positivity-change norm) is summed per
+// tile and slab of 16 slices, and the block that finishes last sums the
+// slab partials in order; walks of `slabs` consecutive slabs (host-chosen)
+// give the same bits for every choice.
+constexpr int kZTX = 32, kZTY = 16;                 // output tile
+constexpr int kZW = kZTX + 4, kZH = kZTY + 4;       // staged slice with halo 2
+constexpr int kZSlab = 16;                          // slices of a partial
+constexpr int kZThreads = 256;
+static_assert(kZTX * kZTY == 2 * kZThreads, "two tile voxels per thread");
+
+__host__ __device__ __forceinline__ int zwalk_tiles_x(int nx) { return (nx + kZTX - 1) / kZTX; }
+__host__ __device__ __forceinline__ int zwalk_tiles_y(int ny) { return (ny + kZTY - 1) / kZTY; }
+__host__ __device__ __forceinline__ int zwalk_slabs(int nz) { return (nz + kZSlab - 1) / kZSlab; }
+
+// kMode as in tv_walk: 0 m' and ||v(m')||^2; 1 m' only; 2 the finishing step.
+template <int kMode>
+__device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0, int z0,
+                                         int z1, float coef, float &acc, int tile, int ntiles,
+                                         float (*sm)[kZH][kZW], float (*sr)[kZH][kZW],
+                                         float (*sp)[kZH][kZW], float (*sq)[kZH][kZW],
+                                         float *shf) {
+  const Dims D = I.d;
+  const float *src = tv_src(I, step);
+  float *dst = tv_dst(I, step);
+  const int tid = threadIdx.x;
+  const long long plane = (long long)D.nx * D.ny;
+  auto stage = [&](int z) {  // slice z into ring slot z & 3
+    float(*m)[kZW] = sm[z & 3];
+    const bool zin = z >= 0 && z < D.nz;
+    for (int i = tid; i < kZW * kZH; i += kZThreads) {
+      const int yy = i / kZW, xx = i - yy * kZW;
+      const int gx = x0 - 2 + xx, gy = y0 - 2 + yy;
+      const bool in = zin && gx >= 0 && gx < D.nx && gy >= 0 && gy < D.ny;
+      const float *g = in ? src + (z * plane + (long long)gy * D.nx + gx) : src;
+      const unsigned sa = (unsigned)__cvta_generic_to_shared(&m[yy][xx]);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(g),
+                   "r"(in ? 4 : 0)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  auto inside = [&](int xx, int yy, int z) {
+    const int gx = x0 - 2 + xx, gy = y0 - 2 + yy;
+    return gx >= 0 && gx < D.nx && gy >= 0 && gy < D.ny && z >= 0 && z < D.nz;
+  };
+  // r of field f (slices a = current, b = previous) over [lo, 36) x [lo, 20)
+  // minus `cut` on the high side
+  auto pass_r = [&](const float(*f)[kZW], const float(*fb)[kZW], float(*r)[kZW], int lo,
+                    int wx, int wy) {
+    for (int i = tid; i < wx * wy; i += kZThreads) {
+      const int yy = lo + i / wx, xx = lo + i % wx;
+      const float c = f[yy][xx];
+      r[yy][xx] = tv3_r(__fsub_rn(c, f[yy][xx - 1]), __fsub_rn(c, f[yy - 1][xx]),
+                        __fsub_rn(c, fb[yy][xx]));
+    }
+  };
+  auto vat = [&](const float(*fm)[kZW], const float(*f)[kZW], const float(*fp)[kZW],
+                 const float(*r)[kZW], const float(*rp)[kZW], int yy, int xx) {
+    return tv3_combine(f[yy][xx], f[yy][xx - 1], f[yy - 1][xx], fm[yy][xx], f[yy][xx + 1],
+                       f[yy + 1][xx], fp[yy][xx], r[yy][xx], r[yy][xx + 1], r[yy + 1][xx],
+                       rp[yy][xx]);
+  };
+  auto flush = [&](int z) {  // the slab of output slice z is complete
+    const float vv[1] = {acc};
+    float bs[1];
+    block_sum_f<kZThreads, 1>(vv, bs, shf);
+    if (tid == 0) I.partials[(long long)(z / kZSlab) * ntiles + tile] = (double)bs[0];
+    acc = 0.f;
+  };
+  // slices z0 - 2 and z0 - 1 staged; then one slice ahead of use
+  stage(z0 - 2);
+  stage(z0 - 1);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  __syncthreads();
+  stage(z0);
+  pass_r(sm[(z0 - 1) & 3], sm[(z0 - 2) & 3], sr[(z0 - 1) & 1], 1, kZW - 1, kZH - 1);
+  const int kend = kMode == 0 ? z1 + 1 : z1;
+  for (int k = z0; k <= kend; k++) {
+    if (k + 1 <= kend) stage(k + 1);
+    else asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // slice k landed
+    __syncthreads();
+    // A: r(k)
+    pass_r(sm[k & 3], sm[(k - 1) & 3], sr[k & 1], 1, kZW - 1, kZH - 1);
+    __syncthreads();
+    // B: v(m) and m' of slice k - 1
+    const float(*m0)[kZW] = sm[(k - 2) & 3];
+    const float(*m1)[kZW] = sm[(k - 1) & 3];
+    const float(*m2)[kZW] = sm[k & 3];
+    const float(*r1)[kZW] = sr[(k - 1) & 1];
+    const float(*r2)[kZW] = sr[k & 1];
+    const int zb = k - 1;
+    if (kMode == 0) {
+      float(*mp)[kZW] = sp[zb % 3 < 0 ? zb % 3 + 3 : zb % 3];
+      for (int i = tid; i < (kZW - 2) * (kZH - 2); i += kZThreads) {
+        const int yy = 1 + i / (kZW - 2), xx = 1 + i % (kZW - 2);
+        const float v = vat(m0, m1, m2, r1, r2, yy, xx);
+        mp[yy][xx] = inside(xx, yy, zb) ? __fmaf_rn(-coef, v, m1[yy][xx]) : 0.f;
+      }
+    } else if (zb >= z0 && zb < z1) {
+      // the single or finishing step: m' on the tile only
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int xx = 2 + tid % kZTX, yy = 2 + tid / kZTX + h * (kZTY / 2);
+        if (!inside(xx, yy, zb)) continue;
+        const float mn = __fmaf_rn(-coef, vat(m0, m1, m2, r1, r2, yy, xx), m1[yy][xx]);
+        const long long gi = zb * plane + (long long)(y0 - 2 + yy) * D.nx + (x0 - 2 + xx);
+        if (kMode == 1) {
+          dst[gi] = mn;
+        } else {
+          const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin3D.cpp positivity
+          const float d = mc - I.m[gi];
+          acc += d * d;
+          I.m[gi] = mc;
+          I.m_pre[gi] = mc;
+        }
+      }
+      if (kMode == 2 && ((zb + 1) % kZSlab == 0 || zb + 1 == z1)) flush(zb);
+    }
+    // the next step's staging overwrites slice k - 2's ring slot
+    __syncthreads();
+    if (kMode != 0) continue;
+    // C: r'(k - 1) (needs m' of k - 2, computed one step earlier)
+    const int zc = k - 1;
+    if (zc >= z0) {
+      pass_r(sp[zc % 3], sp[(zc + 2) % 3], sq[zc & 1], 2, kZW - 3, kZH - 3);
+    }
+    __syncthreads();
+    // D: v(m') of slice k - 2 on the tile, m' written out
+    const int zd = k - 2;
+    if (zd >= z0) {
+      const float(*p0)[kZW] = sp[(zd + 2) % 3];
+      const float(*p1)[kZW] = sp[zd % 3];
+      const float(*p2)[kZW] = sp[(zd + 1) % 3];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int xx = 2 + tid % kZTX, yy = 2 + tid / kZTX + h * (kZTY / 2);
+        if (!inside(xx, yy, zd)) continue;
+        const long long gi = zd * plane + (long long)(y0 - 2 + yy) * D.nx + (x0 - 2 + xx);
+        dst[gi] = p1[yy][xx];
+        const float w = vat(p0, p1, p2, sq[zd & 1], sq[(zd + 1) & 1], yy, xx);
+        acc += w * w;
+      }
+      if ((zd + 1) % kZSlab == 0 || zd + 1 == z1) flush(zd);
+    }
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kZThreads)
+    k_tv_walk3d(const Inst *__restrict__ insts, int step, int slabs) {
+  __shared__ float sm[4][kZH][kZW], sr[2][kZH][kZW], sp[3][kZH][kZW], sq[2][kZH][kZW];
+  __shared__ float shf[kZThreads / 32];
+  __shared__ int s_last;
+  const Inst &I = insts[blockIdx.z];
+  if (inst_done(I)) return;
+  const int ng = I.s->ng;
+  if (step >= ng) return;
+  const Dims D = I.d;
+  const int TXn = zwalk_tiles_x(D.nx), TYn = zwalk_tiles_y(D.ny), NS = zwalk_slabs(D.nz);
+  const int ntiles = TXn * TYn;
+  const int per_tile = (NS + slabs - 1) / slabs;
+  const int walks = ntiles * per_tile;
+  const int w = blockIdx.x;
+  if (w >= walks) return;
+  const int tile = w % ntiles, s0 = (w / ntiles) * slabs;
+  const int x0 = (tile % TXn) * kZTX, y0 = (tile / TXn) * kZTY;
+  const int z0 = s0 * kZSlab, z1 = min(D.nz, (s0 + slabs) * kZSlab);
+  const bool last = step == ng - 1;
+  const float coef = I.s->tv_coef_f;
+  float acc = 0.f;
+  if (!last)
+    tv_zwalk<0>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sm, sr, sp, sq, shf);
+  else if (ng == 1)
+    tv_zwalk<1>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sm, sr, sp, sq, shf);
+  else
+    tv_zwalk<2>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sm, sr, sp, sq, shf);
+  if (last && ng == 1) return;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(I.counter, 1u) == (unsigned)walks - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double tot[1];
+  grid_sum_final<kZThreads, 1>(I.partials, I.counter, ntiles * NS, tot);
+  if (threadIdx.x == 0) {
+    Scalars *s = I.s;
+    if (last) {
+      finish_scalars(s, tot[0]);
+    } else {
+      s->tv_coef = s->alpha * s->d_tv / sqrt(tot[0]);
+      s->tv_coef_f = (float)s->tv_coef;
+    }
+  }
+}
+
 // End of an iteration for instances whose last TV step did not finish it
 // (ng == 0 or ng == 1): positivity (after a TV step), dg, alpha/beta, k.
 __global__ void __launch_bounds__(kThreads)
@@ -801,10 +970,19 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
   (void)ng;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1) {
-    k_tv_step<true><<<grid, kThreads, 0, st>>>(insts, step);
+    // slabs per walk: the batch's walks within about one wave of 7 resident
+    // blocks per SM (32 KB of slices each)
+    const long long tiles = (long long)zwalk_tiles_x(d.nx) * zwalk_tiles_y(d.ny);
+    const long long units = tiles * zwalk_slabs(d.nz);
+    const long long cap = 152LL * 7;
+    const long long per = (units * batch + cap - 1) / cap;
+    const int slabs = (int)(per < 1 ? 1 : (per > zwalk_slabs(d.nz) ? zwalk_slabs(d.nz) : per));
+    const long long walks = tiles * ((zwalk_slabs(d.nz) + slabs - 1) / slabs);
+    k_tv_walk3d<<<dim3((unsigned)walks, 1, batch), kZThreads, 0, st>>>(insts, step, slabs);
   } else {
     // bands per walk: the batch's walks within about one wave of 32
-    // resident warps per SM, one band per walk for small batches
+    // resident warps per SM; one band (16 rows) per walk for small batches,
+    // which keeps a single instance's step spread over many warps
     const long long units = (long long)walk_strips(d.nx) * walk_bands(d.ny);
     const long long cap = 152LL * 32;
     const long long per = (units * batch + cap - 1) / cap;
@@ -814,6 +992,11 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
     k_tv_walk2d<<<g2, kWalkWarps * 32, 0, st>>>(insts, step, bands);
   }
   return cudaGetLastError();
+}
+
+int tv_partials_for(const Dims &d) {
+  return d.nz > 1 ? zwalk_tiles_x(d.nx) * zwalk_tiles_y(d.ny) * zwalk_slabs(d.nz)
+                  : walk_strips(d.nx) * walk_bands(d.ny);
 }
 
 cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,

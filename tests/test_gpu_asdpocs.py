@@ -317,14 +317,14 @@ def test_shared_geometry_groups_with_remainder(gpu):
 
 
 @pytest.mark.parametrize("nx,ny,batch,check", [
-    (384, 384, 60, (0, 59)),   # 84 strip bands x 60: two bands per walk in the batch
+    (384, 384, 60, (0, 59)),   # 168 strip bands x 60: three bands per walk in the batch
     (121, 70, 3, (0, 2)),      # odd nx: per-column accesses; ragged strips and bands
     (36, 20, 2, (1,)),         # one strip, one band
     (4, 3, 2, (0,)),
     (1, 5, 2, (1,)),
 ])
 def test_tv_walks_batch_equals_alone(gpu, nx, ny, batch, check):
-    """The 2-D TV step walks strips of 60 output columns in bands of 32 rows,
+    """The 2-D TV step walks strips of 60 output columns in bands of 16 rows,
     several bands per walk when the batch is large; each instance's result
     is the same bits as its run alone (one band per walk)."""
     na, nv = 48, 8
@@ -342,6 +342,32 @@ def test_tv_walks_batch_equals_alone(gpu, nx, ny, batch, check):
         pl.run()
         out = [pl.image(k) for k in range(batch)]
     for k in check:
+        with pkg.Plan(para, phi) as pl:
+            pl.set_sinogram(0, Ps[k])
+            pl.reset()
+            pl.run()
+            assert np.array_equal(pl.image(0), out[k]), k
+        assert np.isfinite(out[k]).all()
+
+
+def test_tv_zwalks_batch_equals_alone(gpu):
+    """The cone-beam TV step walks 32 x 16 tiles down z in slabs of 16
+    slices, two slabs per walk in this batch (18 tiles x 3 slabs x 20) and
+    one alone; each instance's result is the same bits either way."""
+    nx, ny, nz, na, nb, nv, batch = 96, 96, 40, 48, 48, 6, 20
+    SO, OD, det = 1000.0, 500.0, 1.6
+    phi = phantoms.views(nv)
+    para = dict(SO=SO, OD=OD, vxlsize=1.0, nx=nx, ny=ny, nz=nz, na=na, nb=nb, detsize=det,
+                phi_vec=phi, maxnumIter=2, numOfgradients=3, alpha=0.05)
+    rng = np.random.default_rng(5)
+    Ps = [rng.random(na * nb * nv).astype(np.float32) for _ in range(batch)]
+    with pkg.Plan([para] * batch, [phi] * batch) as pl:
+        for k, P in enumerate(Ps):
+            pl.set_sinogram(k, P)
+        pl.reset()
+        pl.run()
+        out = [pl.image(k) for k in range(batch)]
+    for k in (0, batch - 1):
         with pkg.Plan(para, phi) as pl:
             pl.set_sinogram(0, Ps[k])
             pl.reset()
