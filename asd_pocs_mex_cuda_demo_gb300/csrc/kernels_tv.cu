@@ -678,27 +678,28 @@ __global__ void __launch_bounds__(kWalkWarps * 32, 8)
 }
 
 // Cone-beam TV step (imgTVGradMin3D.cpp:83-170) as z walks (2.5-D
-// blocking).  A block owns a tile of
-// 32 x 16 output voxels in (x, y) and walks down z through a range of
-// slices.  Each slice of m is staged with a two-voxel halo (36 x 20, zero
-// outside the image) into a ring of four slices by cp.async, two slices
-// ahead.  Per slice k the block forms, on shrinking halo regions:
-//   A  r(k) = 1/sqrt(eps + dx^2 + dy^2 + dz^2) of m       (35 x 19)
+// blocking).  A block of 16 warps owns a tile of 28 x 28 output voxels in
+// (x, y) and walks down z through a range of slices.  Each slice of m is
+// staged with a two-voxel halo (32 x 32: lane l holds column x0 - 2 + l,
+// warp w rows w and w + 16; zeros outside the image) into a ring of four
+// slices by cp.async, one slice ahead.  Per slice k the block forms, on
+// shrinking halo regions:
+//   A  r(k) = 1/sqrt(eps + dx^2 + dy^2 + dz^2) of m       ([1, 32)^2)
 //   B  v(m) of slice k - 1 from m and r (tv3_combine), and
-//      m' = m - coef v(m), zero outside the image          (34 x 18)
-//   C  r'(k - 1) of m'                                      (33 x 17)
-//   D  v(m') of slice k - 2 on the tile: ||v(m')||^2, and m' written out.
+//      m' = m - coef v(m), zero outside the image          ([1, 31)^2)
+//   C  r'(k - 1) of m'                                      ([2, 31)^2)
+//   D  v(m') of slice k - 2 on the tile: ||v(m')||^2, and m' written out
 // so each voxel is read once and written once, with four passes of stencil
 // arithmetic over slightly larger regions instead of five full stencils.
 // ||v(m')||^2 (or the last step's positivity-change norm) is summed per
 // tile and slab of 16 slices, and the block that finishes last sums the
 // slab partials in order; walks of `slabs` consecutive slabs (host-chosen)
 // give the same bits for every choice.
-constexpr int kZTX = 32, kZTY = 16;                 // output tile
+constexpr int kZTX = 28, kZTY = 28;                 // output tile
 constexpr int kZW = kZTX + 4, kZH = kZTY + 4;       // staged slice with halo 2
 constexpr int kZSlab = 16;                          // slices of a partial
-constexpr int kZThreads = 256;
-static_assert(kZTX * kZTY == 2 * kZThreads, "two tile voxels per thread");
+constexpr int kZThreads = 512;
+static_assert(kZW == 32 && kZH == 2 * (kZThreads / 32), "lane = column, two rows per warp");
 
 __host__ __device__ __forceinline__ int zwalk_tiles_x(int nx) { return (nx + kZTX - 1) / kZTX; }
 __host__ __device__ __forceinline__ int zwalk_tiles_y(int ny) { return (ny + kZTY - 1) / kZTY; }
@@ -714,66 +715,77 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
   const Dims D = I.d;
   const float *src = tv_src(I, step);
   float *dst = tv_dst(I, step);
-  const int tid = threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long plane = (long long)D.nx * D.ny;
+  const int gx = x0 - 2 + lane;
+  const bool colin = gx >= 0 && gx < D.nx;
+  int gy[2];
+  bool in2[2];  // this thread's staged voxels lie inside the image in (x, y)
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    gy[h] = y0 - 2 + warp + 16 * h;
+    in2[h] = colin && gy[h] >= 0 && gy[h] < D.ny;
+  }
+  auto zin = [&](int z) { return z >= 0 && z < D.nz; };
   auto stage = [&](int z) {  // slice z into ring slot z & 3
-    float(*m)[kZW] = sm[z & 3];
-    const bool zin = z >= 0 && z < D.nz;
-    for (int i = tid; i < kZW * kZH; i += kZThreads) {
-      const int yy = i / kZW, xx = i - yy * kZW;
-      const int gx = x0 - 2 + xx, gy = y0 - 2 + yy;
-      const bool in = zin && gx >= 0 && gx < D.nx && gy >= 0 && gy < D.ny;
-      const float *g = in ? src + (z * plane + (long long)gy * D.nx + gx) : src;
-      const unsigned sa = (unsigned)__cvta_generic_to_shared(&m[yy][xx]);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const bool in = in2[h] && zin(z);
+      const float *g = in ? src + (z * plane + (long long)gy[h] * D.nx + gx) : src;
+      const unsigned sa = (unsigned)__cvta_generic_to_shared(&sm[z & 3][warp + 16 * h][lane]);
       asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(g),
                    "r"(in ? 4 : 0)
                    : "memory");
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
-  auto inside = [&](int xx, int yy, int z) {
-    const int gx = x0 - 2 + xx, gy = y0 - 2 + yy;
-    return gx >= 0 && gx < D.nx && gy >= 0 && gy < D.ny && z >= 0 && z < D.nz;
-  };
-  // r of field f (slices a = current, b = previous) over [lo, 36) x [lo, 20)
-  // minus `cut` on the high side
+  // r of field f (previous slice fb) on [lo, hi)^2
   auto pass_r = [&](const float(*f)[kZW], const float(*fb)[kZW], float(*r)[kZW], int lo,
-                    int wx, int wy) {
-    for (int i = tid; i < wx * wy; i += kZThreads) {
-      const int yy = lo + i / wx, xx = lo + i % wx;
-      const float c = f[yy][xx];
-      r[yy][xx] = tv3_r(__fsub_rn(c, f[yy][xx - 1]), __fsub_rn(c, f[yy - 1][xx]),
-                        __fsub_rn(c, fb[yy][xx]));
+                    int hi) {
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int yy = warp + 16 * h;
+      if (yy < lo || yy >= hi || lane < lo || lane >= hi) continue;
+      const float c = f[yy][lane];
+      r[yy][lane] = tv3_r(__fsub_rn(c, f[yy][lane - 1]), __fsub_rn(c, f[yy - 1][lane]),
+                          __fsub_rn(c, fb[yy][lane]));
     }
   };
   auto vat = [&](const float(*fm)[kZW], const float(*f)[kZW], const float(*fp)[kZW],
-                 const float(*r)[kZW], const float(*rp)[kZW], int yy, int xx) {
-    return tv3_combine(f[yy][xx], f[yy][xx - 1], f[yy - 1][xx], fm[yy][xx], f[yy][xx + 1],
-                       f[yy + 1][xx], fp[yy][xx], r[yy][xx], r[yy][xx + 1], r[yy + 1][xx],
-                       rp[yy][xx]);
+                 const float(*r)[kZW], const float(*rp)[kZW], int yy) {
+    return tv3_combine(f[yy][lane], f[yy][lane - 1], f[yy - 1][lane], fm[yy][lane],
+                       f[yy][lane + 1], f[yy + 1][lane], fp[yy][lane], r[yy][lane],
+                       r[yy][lane + 1], r[yy + 1][lane], rp[yy][lane]);
   };
   auto flush = [&](int z) {  // the slab of output slice z is complete
     const float vv[1] = {acc};
     float bs[1];
     block_sum_f<kZThreads, 1>(vv, bs, shf);
-    if (tid == 0) I.partials[(long long)(z / kZSlab) * ntiles + tile] = (double)bs[0];
+    if (threadIdx.x == 0) I.partials[(long long)(z / kZSlab) * ntiles + tile] = (double)bs[0];
     acc = 0.f;
   };
-  // slices z0 - 2 and z0 - 1 staged; then one slice ahead of use
+  auto ring3 = [](int z) { return (z % 3 + 3) % 3; };
+  // an output voxel of this thread: tile rows and columns [2, 30)
+  auto outvox = [&](int h) {
+    const int yy = warp + 16 * h;
+    return yy >= 2 && yy < kZH - 2 && lane >= 2 && lane < kZW - 2 && in2[h];
+  };
   stage(z0 - 2);
   stage(z0 - 1);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   __syncthreads();
   stage(z0);
-  pass_r(sm[(z0 - 1) & 3], sm[(z0 - 2) & 3], sr[(z0 - 1) & 1], 1, kZW - 1, kZH - 1);
+  pass_r(sm[(z0 - 1) & 3], sm[(z0 - 2) & 3], sr[(z0 - 1) & 1], 1, kZW);
   const int kend = kMode == 0 ? z1 + 1 : z1;
   for (int k = z0; k <= kend; k++) {
-    if (k + 1 <= kend) stage(k + 1);
-    else asm volatile("cp.async.commit_group;\n" ::: "memory");
+    if (k + 1 <= kend)
+      stage(k + 1);
+    else
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
     asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // slice k landed
     __syncthreads();
     // A: r(k)
-    pass_r(sm[k & 3], sm[(k - 1) & 3], sr[k & 1], 1, kZW - 1, kZH - 1);
+    pass_r(sm[k & 3], sm[(k - 1) & 3], sr[k & 1], 1, kZW);
     __syncthreads();
     // B: v(m) and m' of slice k - 1
     const float(*m0)[kZW] = sm[(k - 2) & 3];
@@ -783,24 +795,26 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
     const float(*r2)[kZW] = sr[k & 1];
     const int zb = k - 1;
     if (kMode == 0) {
-      float(*mp)[kZW] = sp[zb % 3 < 0 ? zb % 3 + 3 : zb % 3];
-      for (int i = tid; i < (kZW - 2) * (kZH - 2); i += kZThreads) {
-        const int yy = 1 + i / (kZW - 2), xx = 1 + i % (kZW - 2);
-        const float v = vat(m0, m1, m2, r1, r2, yy, xx);
-        mp[yy][xx] = inside(xx, yy, zb) ? __fmaf_rn(-coef, v, m1[yy][xx]) : 0.f;
+      float(*mp)[kZW] = sp[ring3(zb)];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        const int yy = warp + 16 * h;
+        if (yy < 1 || yy >= kZH - 1 || lane < 1 || lane >= kZW - 1) continue;
+        const float v = vat(m0, m1, m2, r1, r2, yy);
+        mp[yy][lane] = (in2[h] && zin(zb)) ? __fmaf_rn(-coef, v, m1[yy][lane]) : 0.f;
       }
     } else if (zb >= z0 && zb < z1) {
       // the single or finishing step: m' on the tile only
 #pragma unroll
       for (int h = 0; h < 2; h++) {
-        const int xx = 2 + tid % kZTX, yy = 2 + tid / kZTX + h * (kZTY / 2);
-        if (!inside(xx, yy, zb)) continue;
-        const float mn = __fmaf_rn(-coef, vat(m0, m1, m2, r1, r2, yy, xx), m1[yy][xx]);
-        const long long gi = zb * plane + (long long)(y0 - 2 + yy) * D.nx + (x0 - 2 + xx);
+        if (!outvox(h)) continue;
+        const int yy = warp + 16 * h;
+        const float mn = __fmaf_rn(-coef, vat(m0, m1, m2, r1, r2, yy), m1[yy][lane]);
+        const long long gi = zb * plane + (long long)gy[h] * D.nx + gx;
         if (kMode == 1) {
           dst[gi] = mn;
         } else {
-          const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin3D.cpp positivity
+          const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin3D.cpp:163-170
           const float d = mc - I.m[gi];
           acc += d * d;
           I.m[gi] = mc;
@@ -814,23 +828,20 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
     if (kMode != 0) continue;
     // C: r'(k - 1) (needs m' of k - 2, computed one step earlier)
     const int zc = k - 1;
-    if (zc >= z0) {
-      pass_r(sp[zc % 3], sp[(zc + 2) % 3], sq[zc & 1], 2, kZW - 3, kZH - 3);
-    }
+    if (zc >= z0) pass_r(sp[ring3(zc)], sp[ring3(zc - 1)], sq[zc & 1], 2, kZW - 1);
     __syncthreads();
     // D: v(m') of slice k - 2 on the tile, m' written out
     const int zd = k - 2;
     if (zd >= z0) {
-      const float(*p0)[kZW] = sp[(zd + 2) % 3];
-      const float(*p1)[kZW] = sp[zd % 3];
-      const float(*p2)[kZW] = sp[(zd + 1) % 3];
+      const float(*p0)[kZW] = sp[ring3(zd - 1)];
+      const float(*p1)[kZW] = sp[ring3(zd)];
+      const float(*p2)[kZW] = sp[ring3(zd + 1)];
 #pragma unroll
       for (int h = 0; h < 2; h++) {
-        const int xx = 2 + tid % kZTX, yy = 2 + tid / kZTX + h * (kZTY / 2);
-        if (!inside(xx, yy, zd)) continue;
-        const long long gi = zd * plane + (long long)(y0 - 2 + yy) * D.nx + (x0 - 2 + xx);
-        dst[gi] = p1[yy][xx];
-        const float w = vat(p0, p1, p2, sq[zd & 1], sq[(zd + 1) & 1], yy, xx);
+        if (!outvox(h)) continue;
+        const int yy = warp + 16 * h;
+        dst[zd * plane + (long long)gy[h] * D.nx + gx] = p1[yy][lane];
+        const float w = vat(p0, p1, p2, sq[zd & 1], sq[(zd + 1) & 1], yy);
         acc += w * w;
       }
       if ((zd + 1) % kZSlab == 0 || zd + 1 == z1) flush(zd);
@@ -970,11 +981,11 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
   (void)ng;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1) {
-    // slabs per walk: the batch's walks within about one wave of 7 resident
-    // blocks per SM (32 KB of slices each)
+    // slabs per walk: the batch's walks within about one wave of 2 resident
+    // blocks per SM (16 warps and 44 KB of slices each)
     const long long tiles = (long long)zwalk_tiles_x(d.nx) * zwalk_tiles_y(d.ny);
     const long long units = tiles * zwalk_slabs(d.nz);
-    const long long cap = 152LL * 7;
+    const long long cap = 152LL * 2;
     const long long per = (units * batch + cap - 1) / cap;
     const int slabs = (int)(per < 1 ? 1 : (per > zwalk_slabs(d.nz) ? zwalk_slabs(d.nz) : per));
     const long long walks = tiles * ((zwalk_slabs(d.nz) + slabs - 1) / slabs);
