@@ -248,6 +248,20 @@ class Plan:
         check(load().asdpocs_plan_time_phase(self._h, int(phase), int(reps), C.byref(ms)))
         return ms.value
 
+    def autotune(self, reps: int = 20):
+        """Times the TV step at each candidate walk length and keeps the
+        fastest (results do not depend on it); returns (walk, ms per step),
+        walk 0 meaning the batch-size rule.  Leaves the reconstruction state
+        unchanged."""
+        w, ms = C.c_int(), C.c_double()
+        check(load().asdpocs_plan_autotune(self._h, int(reps), C.byref(w), C.byref(ms)))
+        return w.value, ms.value
+
+    def set_tv_walk(self, walk: int):
+        """Pins the TV walk length (bands or slabs per walk; 0: the
+        batch-size rule)."""
+        check(load().asdpocs_plan_set_tv_walk(self._h, int(walk)))
+
     def sinogram_ptr(self, inst: int) -> int:
         return int(load().asdpocs_plan_sinogram_ptr(self._h, inst))
 

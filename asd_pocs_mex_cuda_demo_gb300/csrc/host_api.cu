@@ -391,6 +391,7 @@ struct asdpocs_plan_s {
   std::vector<Inst> h_inst;
   std::vector<int> has_ref;
   bool shared = false;  // all instances share sizes, geometry and angles
+  int tv_walk = 0;      // TV walk length (0: from the batch size)
   Inst *d_inst = nullptr;
   void *arena = nullptr;
   size_t bytes = 0;
@@ -539,7 +540,8 @@ cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st) {
 namespace asd {
 
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
-                              int nv, int ng, bool shared, cudaStream_t st) {
+                              int nv, int ng, bool shared, cudaStream_t st,
+                              int tv_walk) {
   cudaError_t e = cudaSuccess;
   if (shared) e = launch_group_pack(d_inst, batch, d, 0, st);
   for (int v = 0; v < nv && e == cudaSuccess; v++) {
@@ -552,14 +554,14 @@ cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
   if (shared && e == cudaSuccess) e = launch_group_pack(d_inst, batch, d, 1, st);
   if (e == cudaSuccess) e = launch_after_sweep(d_inst, batch, d, st);
   for (int s = 0; s < ng && e == cudaSuccess; s++)
-    e = launch_tv_step(d_inst, batch, d, s, ng, st);
+    e = launch_tv_step(d_inst, batch, d, s, ng, st, tv_walk);
   if (e == cudaSuccess) e = launch_finish_iter(d_inst, batch, d, ng, st);
   return e;
 }
 
 static int plan_enqueue_iteration(asdpocs_plan p) {
   ASD_CUDA(enqueue_iteration(p->d_inst, p->batch, p->d, p->nv, p->max_ng, p->shared,
-                             p->st));
+                             p->st, p->tv_walk));
   return 0;
 }
 
@@ -872,7 +874,7 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
                                                   p->st)
                          : launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv, p->st);
       case 2: return launch_tv_step(p->d_inst, p->batch, p->d, 1 + i % (ng > 1 ? ng - 1 : 1),
-                                    ng, p->st);
+                                    ng, p->st, p->tv_walk);
       default: return launch_after_sweep(p->d_inst, p->batch, p->d, p->st);
     }
   };
@@ -887,6 +889,64 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   cudaEventDestroy(e1);
   ASD_CUDA(e);
   *avg_ms = (double)ms / reps;
+  return 0;
+}
+
+static void plan_drop_graph(asdpocs_plan p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = nullptr;
+  p->graph = nullptr;
+}
+
+int asdpocs_plan_set_tv_walk(asdpocs_plan p, int walk) {
+  clear_error();
+  if (!p || walk < 0) return set_error(ASDPOCS_ERR_ARG, "bad walk length");
+  if (walk != p->tv_walk) plan_drop_graph(p);  // the captured launches change
+  p->tv_walk = walk;
+  return 0;
+}
+
+int asdpocs_plan_autotune(asdpocs_plan p, int reps, int *walk, double *ms) {
+  clear_error();
+  if (!p || reps <= 0) return set_error(ASDPOCS_ERR_ARG, "bad autotune arguments");
+  if (p->max_ng < 2) {
+    if (walk) *walk = p->tv_walk;
+    if (ms) *ms = 0.0;
+    return 0;
+  }
+  std::vector<int> cand{0};
+  const int wmax = tv_walk_max(p->d);
+  for (int w = 1; w < wmax; w *= 2) cand.push_back(w);
+  cand.push_back(wmax);
+  cudaEvent_t e0, e1;
+  ASD_CUDA(cudaEventCreate(&e0));
+  ASD_CUDA(cudaEventCreate(&e1));
+  int best = 0;
+  float best_ms = 0.f;
+  cudaError_t e = cudaSuccess;
+  for (size_t c = 0; c < cand.size() && e == cudaSuccess; c++) {
+    // step 0 of ng >= 2 steps: reads the image, writes tv_b and the step
+    // size (both rewritten every iteration)
+    e = launch_tv_step(p->d_inst, p->batch, p->d, 0, p->max_ng, p->st, cand[c]);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, p->st);
+    for (int r = 0; r < reps && e == cudaSuccess; r++)
+      e = launch_tv_step(p->d_inst, p->batch, p->d, 0, p->max_ng, p->st, cand[c]);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, p->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    if (e == cudaSuccess && (c == 0 || t < best_ms)) {
+      best_ms = t;
+      best = cand[c];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ASD_CUDA(e);
+  if (int rc = asdpocs_plan_set_tv_walk(p, best)) return rc;
+  if (walk) *walk = best;
+  if (ms) *ms = (double)best_ms / reps;
   return 0;
 }
 

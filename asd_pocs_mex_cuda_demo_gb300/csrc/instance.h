@@ -69,6 +69,7 @@ cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st);
 // in groups with interleaved images (Inst::m_il), packed before the sweep
 // and unpacked after it.
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
-                              int nv, int ng, bool shared, cudaStream_t st);
+                              int nv, int ng, bool shared, cudaStream_t st,
+                              int tv_walk = 0);
 
 }  // namespace asd

@@ -42,8 +42,12 @@ cudaError_t tv_minimize_f32(float *img, const float *img_old, float *work_a,
 cudaError_t launch_iter_begin(const Inst *insts, int batch, cudaStream_t st);
 cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
                                cudaStream_t st);
+// `walk`: bands (2-D) or slabs (3-D) per walk of the TV step; 0 picks it
+// from the batch size.  Results do not depend on it.
 cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
-                           int step, int ng, cudaStream_t st);
+                           int step, int ng, cudaStream_t st, int walk = 0);
+// Largest useful `walk` for images of size d (the bands or slabs of one).
+int tv_walk_max(const Dims &d);
 cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
                                int ng, cudaStream_t st);
 

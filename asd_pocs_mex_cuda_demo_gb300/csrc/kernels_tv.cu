@@ -976,8 +976,12 @@ cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
   return cudaGetLastError();
 }
 
+int tv_walk_max(const Dims &d) {
+  return d.nz > 1 ? zwalk_slabs(d.nz) : walk_bands(d.ny);
+}
+
 cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
-                           int step, int ng, cudaStream_t st) {
+                           int step, int ng, cudaStream_t st, int walk) {
   (void)ng;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1) {
@@ -986,7 +990,7 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
     const long long tiles = (long long)zwalk_tiles_x(d.nx) * zwalk_tiles_y(d.ny);
     const long long units = tiles * zwalk_slabs(d.nz);
     const long long cap = 152LL * 2;
-    const long long per = (units * batch + cap - 1) / cap;
+    const long long per = walk > 0 ? walk : (units * batch + cap - 1) / cap;
     const int slabs = (int)(per < 1 ? 1 : (per > zwalk_slabs(d.nz) ? zwalk_slabs(d.nz) : per));
     const long long walks = tiles * ((zwalk_slabs(d.nz) + slabs - 1) / slabs);
     k_tv_walk3d<<<dim3((unsigned)walks, 1, batch), kZThreads, 0, st>>>(insts, step, slabs);
@@ -996,7 +1000,7 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
     // which keeps a single instance's step spread over many warps
     const long long units = (long long)walk_strips(d.nx) * walk_bands(d.ny);
     const long long cap = 152LL * 32;
-    const long long per = (units * batch + cap - 1) / cap;
+    const long long per = walk > 0 ? walk : (units * batch + cap - 1) / cap;
     const int bands = (int)(per < 1 ? 1 : (per > walk_bands(d.ny) ? walk_bands(d.ny) : per));
     const long long walks = (long long)walk_strips(d.nx) * ((walk_bands(d.ny) + bands - 1) / bands);
     const dim3 g2((unsigned)((walks + kWalkWarps - 1) / kWalkWarps), 1, batch);

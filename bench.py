@@ -75,12 +75,14 @@ UNEVEN = dict(
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per instance and
 # launch of each iteration kernel, from `ncu --set full --clock-control none`
-# captures of the 2D fan-beam workload at batch 64 (the shared-geometry
-# kernels); the traffic is about one read of each instance's image plus its
-# writes, so it scales with the batch.
+# captures: the 2D fan-beam workload at batch 64 (the shared-geometry
+# kernels and the column-walk TV step) and the cone-beam workload (one
+# volume).  The traffic is about one read of each instance's image or volume
+# plus its writes, so it scales with the batch.
 NCU_DRAM_PER_INSTANCE = {
-    "fan2d": {"sart_ax": 60.341e6 / 64, "sart_atx": 81.884e6 / 64,
-              "tv_step": 96.786e6 / 64},
+    "fan2d": {"sart_ax": 60.94e6 / 64, "sart_atx": 80.41e6 / 64,
+              "tv_step": 90.55e6 / 64},
+    "cone3d": {"sart_ax": 71.55e6, "sart_atx": 80.01e6, "tv_step": 91.60e6},
 }
 
 
@@ -383,6 +385,10 @@ def main():
         plan.set_sinogram(b, Ps[b])
         plan.set_reference(b, I0s[b])
     flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)  # > L2 (129 MB)
+    # the TV step's walk length, timed on this batch (results do not depend
+    # on it); untimed, like the graph capture
+    plan.reset()
+    tv_walk, tv_walk_ms = plan.autotune(reps=20)
 
     def step():
         plan.reset()
@@ -517,7 +523,10 @@ def main():
                        "tv_steps": ng, "parallelism": f"replicas x{world}",
                        "l2": "256 MB buffer written between timed steps; resident set "
                              f"{plan.nbytes / 2**20:.0f} MB > 129 MB L2",
-                       "graph": "one ASD-POCS iteration captured, replayed per iteration"},
+                       "graph": "one ASD-POCS iteration captured, replayed per iteration",
+                       "tv_walk": {"autotuned": tv_walk, "ms_per_step": tv_walk_ms,
+                                   "note": "bands (2-D) or slabs (3-D) of 16 per walk; "
+                                           "0 = the batch-size rule"}},
             "latency_ms": {"p50": statistics.median(times), "p99": max(times),
                            "note": "every reconstruction of a batch completes at the end "
                                    "of its step"},

@@ -218,6 +218,22 @@ int asdpocs_plan_get_stats(asdpocs_plan plan, int inst, asdpocs_stats *st,
 float *asdpocs_plan_sinogram_ptr(asdpocs_plan plan, int inst);
 float *asdpocs_plan_image_ptr(asdpocs_plan plan, int inst);
 
+/* Autotuner for the TV step's work partition: the walk length in bands of
+ * 16 rows per column walk (2-D) or slabs of 16 slices per z walk (3-D).
+ * Times the first TV step of every running instance, `reps` launches per
+ * candidate (the batch-size rule, then 1, 2, 4, ... up to a whole image),
+ * on the plan's stream, and keeps the fastest for later runs.  Every walk
+ * length gives the same bits (the norm is summed per band or slab in a
+ * fixed order).  The first TV step reads the image and writes a scratch
+ * buffer, so the reconstruction state is unchanged: call it after
+ * asdpocs_plan_reset() and before a run.  *walk (may be NULL) receives the
+ * choice (0: the batch-size rule), *ms (may be NULL) its time per step.
+ * Plans with fewer than two TV steps per iteration keep the rule. */
+int asdpocs_plan_autotune(asdpocs_plan plan, int reps, int *walk, double *ms);
+/* Pins the TV walk length (0: the batch-size rule; larger values are
+ * clipped to a whole image). */
+int asdpocs_plan_set_tv_walk(asdpocs_plan plan, int walk);
+
 /* Profiling hook: average device time (ms, CUDA events on the plan's
  * stream) of `reps` back-to-back launches of one phase kernel for the whole
  * batch.  phase: 0 = SART forward step (Ax + residual), 1 = SART backward

@@ -374,3 +374,32 @@ def test_tv_zwalks_batch_equals_alone(gpu):
             pl.run()
             assert np.array_equal(pl.image(0), out[k]), k
         assert np.isfinite(out[k]).all()
+
+
+@pytest.mark.parametrize("shape", [(200, 150, 1), (60, 44, 40)])
+def test_tv_walk_length_and_autotune_do_not_change_results(gpu, shape):
+    """Every TV walk length (bands of 16 rows in 2-D, slabs of 16 slices in
+    3-D) gives the same bits; the autotuner picks one of them and leaves the
+    reconstruction state as it was."""
+    nx, ny, nz = shape
+    na, nb, nv = 64, (1 if nz == 1 else 48), 6
+    phi = phantoms.views(nv)
+    para = dict(SO=1000.0, OD=500.0, vxlsize=1.0, nx=nx, ny=ny, nz=nz, na=na, nb=nb,
+                detsize=1.6, phi_vec=phi, maxnumIter=2, numOfgradients=4, alpha=0.05)
+    P = np.random.default_rng(nz).random(na * nb * nv).astype(np.float32)
+    out = {}
+    with pkg.Plan(para, phi) as pl:
+        pl.set_sinogram(0, P)
+        for walk in (0, 1, 2, 3, 100):
+            pl.set_tv_walk(walk)
+            pl.reset()
+            pl.run()
+            out[walk] = pl.image(0)
+        pl.reset()
+        w, ms = pl.autotune(reps=3)
+        assert w >= 0 and ms > 0
+        pl.run()
+        tuned = pl.image(0)
+    for walk, img in out.items():
+        assert np.array_equal(img, out[0]), walk
+    assert np.array_equal(tuned, out[0])
