@@ -925,13 +925,16 @@ int asdpocs_plan_autotune(asdpocs_plan p, int reps, int *walk, double *ms) {
   int best = 0;
   float best_ms = 0.f;
   cudaError_t e = cudaSuccess;
+  // steps 0, 1, ..., ng - 2, 1, ... as in an iteration, each reading the
+  // previous one's output; never the last step, so only the work buffers
+  // and the step size (both rewritten every iteration) change
+  const int ng = p->max_ng;
+  auto step_of = [&](int r) { return ng > 2 ? (r == 0 ? 0 : 1 + (r - 1) % (ng - 2)) : 0; };
   for (size_t c = 0; c < cand.size() && e == cudaSuccess; c++) {
-    // step 0 of ng >= 2 steps: reads the image, writes tv_b and the step
-    // size (both rewritten every iteration)
-    e = launch_tv_step(p->d_inst, p->batch, p->d, 0, p->max_ng, p->st, cand[c]);  // warm-up
+    e = launch_tv_step(p->d_inst, p->batch, p->d, 0, ng, p->st, cand[c]);  // warm-up
     if (e == cudaSuccess) e = cudaEventRecord(e0, p->st);
     for (int r = 0; r < reps && e == cudaSuccess; r++)
-      e = launch_tv_step(p->d_inst, p->batch, p->d, 0, p->max_ng, p->st, cand[c]);
+      e = launch_tv_step(p->d_inst, p->batch, p->d, step_of(r), ng, p->st, cand[c]);
     if (e == cudaSuccess) e = cudaEventRecord(e1, p->st);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     float t = 0.f;

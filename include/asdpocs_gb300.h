@@ -220,13 +220,14 @@ float *asdpocs_plan_image_ptr(asdpocs_plan plan, int inst);
 
 /* Autotuner for the TV step's work partition: the walk length in bands of
  * 16 rows per column walk (2-D) or slabs of 16 slices per z walk (3-D).
- * Times the first TV step of every running instance, `reps` launches per
- * candidate (the batch-size rule, then 1, 2, 4, ... up to a whole image),
- * on the plan's stream, and keeps the fastest for later runs.  Every walk
- * length gives the same bits (the norm is summed per band or slab in a
- * fixed order).  The first TV step reads the image and writes a scratch
- * buffer, so the reconstruction state is unchanged: call it after
- * asdpocs_plan_reset() and before a run.  *walk (may be NULL) receives the
+ * Times `reps` TV steps per candidate (the batch-size rule, then 1, 2, 4,
+ * ... up to a whole image) on the plan's stream -- steps 0, 1, ..., ng - 2,
+ * 1, ..., each reading the previous one's output as in an iteration -- and
+ * keeps the fastest for later runs.  Every walk length gives the same bits
+ * (the norm is summed per band or slab in a fixed order).  The timed steps
+ * read the image and write only work buffers and the step size, so the
+ * reconstruction state is unchanged: call it after asdpocs_plan_reset()
+ * and before a run.  *walk (may be NULL) receives the
  * choice (0: the batch-size rule), *ms (may be NULL) its time per step.
  * Plans with fewer than two TV steps per iteration keep the rule. */
 int asdpocs_plan_autotune(asdpocs_plan plan, int reps, int *walk, double *ms);
