@@ -437,7 +437,7 @@ constexpr int kWalkWarps = 4;
 constexpr int kWalkOut = 60;   // output columns of a strip
 constexpr int kBandRows = 16;  // output rows of a partial
 constexpr int kWalkChunk = 4;  // rows per chunk (a band ends at a chunk's end)
-constexpr int kWalkRing = 16;  // rows of m in flight per warp (shared-memory ring)
+constexpr int kWalkRing = 8;  // rows of m in flight per warp (shared-memory ring)
 static_assert(4 % kWalkChunk == 0 && kBandRows % 4 == 0, "bands and the steady chunks line up");
 static_assert(kWalkRing % kWalkChunk == 0 && (kWalkRing & (kWalkRing - 1)) == 0,
               "a chunk's rows sit in consecutive ring slots");
@@ -490,11 +490,13 @@ __device__ __forceinline__ void cp_async_8(float *smem, const float *gmem, bool 
 
 template <int kMode, bool kPair>
 __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1, int xa,
-                                        int strip, int S, float coef, float2 *ring) {
+                                        int strip, int S, float coef, float2 *ring,
+                                        float2 *ring0) {
   const Dims D = I.d;
   const int lane = threadIdx.x & 31;
   const float *src = tv_src(I, step);
   float *dst = tv_dst(I, step);
+  float *const im = I.m, *const impre = I.m_pre;
   const bool ina = xa >= 0 && xa < D.nx, inb = xa + 1 >= 0 && xa + 1 < D.nx;
   const bool outl = lane >= 1 && lane <= 30;
   const bool outa = outl && ina, outb = outl && inb;
@@ -505,17 +507,27 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
   // its two columns), copied asynchronously kWalkRing - 1 rows ahead of the
   // one in use and zero-filled outside the image and the walk; one copy
   // group per row, so "row j has landed" is a fixed wait depth.
+  // The finishing step (kMode 2) also streams the rows of the pre-TV image
+  // (the positivity-change norm's reference) through a second ring.
   float2 *const my = ring + lane;  // slot s of this lane: my[32 * s]
+  float2 *const my0 = ring0 + lane;
   const float *la = src + (ina ? xa : 0), *lb = src + (inb ? xa + 1 : 0);
+  const float *l0a = im + (ina ? xa : 0), *l0b = im + (inb ? xa + 1 : 0);
   auto fetch = [&](int j, int slot) {
     const bool r = (unsigned)j < (unsigned)jl1;  // 0 <= j < jl1
     const int off = r ? j * D.nx : 0;
     float *d = (float *)(my + 32 * slot);
+    float *d0 = (float *)(my0 + 32 * slot);
     if (kPair) {
       cp_async_8(d, la + off, r && ina);
+      if (kMode == 2) cp_async_8(d0, l0a + off, r && ina);
     } else {
       cp_async_4(d, la + off, r && ina);
       cp_async_4(d + 1, lb + off, r && inb);
+      if (kMode == 2) {
+        cp_async_4(d0, l0a + off, r && ina);
+        cp_async_4(d0 + 1, l0b + off, r && inb);
+      }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
@@ -530,9 +542,14 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
     acc = 0.f;
   };
   // row j of m in: v(m) and m' of row j - 1, v(m') of row j - 2
-  // rslot: ring slot of row j; its predecessor's slot receives row j + 15
+  // rslot: ring slot of row j; its predecessor's slot receives row
+  // j + kWalkRing - 1
   auto walk_row = [&](auto checked, int j, int rslot) {
     constexpr bool kC = decltype(checked)::value;
+    // the pre-TV image at output row j - 1 (landed a row ago), read before
+    // its slot receives row j + kWalkRing - 1
+    const float2 f0 = kMode == 2 ? my0[32 * ((rslot + kWalkRing - 1) & (kWalkRing - 1))]
+                                 : make_float2(0.f, 0.f);
     fetch(j + kWalkRing - 1, (rslot + kWalkRing - 1) & (kWalkRing - 1));
     asm volatile("cp.async.wait_group %0;\n" ::"n"(kWalkRing - 1) : "memory");
     const float2 mab = my[32 * rslot];
@@ -557,25 +574,24 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
         const float mcb = pb < 0.f ? 0.f : pb;
         if (kPair) {
           if (outa) {
-            const float2 f0 = *(const float2 *)(I.m + i);
             const float da = mca - f0.x, db = mcb - f0.y;
             acc += da * da;
             acc += db * db;
-            *(float2 *)(I.m + i) = make_float2(mca, mcb);
-            *(float2 *)(I.m_pre + i) = make_float2(mca, mcb);
+            *(float2 *)(im + i) = make_float2(mca, mcb);
+            *(float2 *)(impre + i) = make_float2(mca, mcb);
           }
         } else {
           if (outa) {
-            const float d = mca - I.m[i];
+            const float d = mca - f0.x;
             acc += d * d;
-            I.m[i] = mca;
-            I.m_pre[i] = mca;
+            im[i] = mca;
+            impre[i] = mca;
           }
           if (outb) {
-            const float d = mcb - I.m[i + 1];
+            const float d = mcb - f0.y;
             acc += d * d;
-            I.m[i + 1] = mcb;
-            I.m_pre[i + 1] = mcb;
+            im[i + 1] = mcb;
+            impre[i + 1] = mcb;
           }
         }
       }
@@ -623,7 +639,7 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
 
 __global__ void __launch_bounds__(kWalkWarps * 32, 8)
     k_tv_walk2d(const Inst *__restrict__ insts, int step, int bands) {
-  __shared__ float2 ring[kWalkWarps][kWalkRing * 32];
+  __shared__ float2 ring[kWalkWarps][kWalkRing * 32], ring0[kWalkWarps][kWalkRing * 32];
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
@@ -641,15 +657,16 @@ __global__ void __launch_bounds__(kWalkWarps * 32, 8)
   const bool last = step == ng - 1;
   const float coef = I.s->tv_coef_f;
   const bool pair = (D.nx & 1) == 0;
+  float2 *const rg = ring[threadIdx.x >> 5], *const rg0 = ring0[threadIdx.x >> 5];
   if (!last)
-    pair ? tv_walk<0, true>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5])
-         : tv_walk<0, false>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5]);
+    pair ? tv_walk<0, true>(I, step, y0, y1, xa, strip, S, coef, rg, rg0)
+         : tv_walk<0, false>(I, step, y0, y1, xa, strip, S, coef, rg, rg0);
   else if (ng == 1)
-    pair ? tv_walk<1, true>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5])
-         : tv_walk<1, false>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5]);
+    pair ? tv_walk<1, true>(I, step, y0, y1, xa, strip, S, coef, rg, rg0)
+         : tv_walk<1, false>(I, step, y0, y1, xa, strip, S, coef, rg, rg0);
   else
-    pair ? tv_walk<2, true>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5])
-         : tv_walk<2, false>(I, step, y0, y1, xa, strip, S, coef, ring[threadIdx.x >> 5]);
+    pair ? tv_walk<2, true>(I, step, y0, y1, xa, strip, S, coef, rg, rg0)
+         : tv_walk<2, false>(I, step, y0, y1, xa, strip, S, coef, rg, rg0);
   if (last && ng == 1) return;  // nothing to sum: k_finish_iter ends the iteration
   // the walk that finishes last sums the instance's band partials
   unsigned ticket = 0;
@@ -715,6 +732,7 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
   const Dims D = I.d;
   const float *src = tv_src(I, step);
   float *dst = tv_dst(I, step);
+  float *const im = I.m, *const impre = I.m_pre;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long plane = (long long)D.nx * D.ny;
   const int gx = x0 - 2 + lane;
@@ -778,6 +796,14 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
   pass_r(sm[(z0 - 1) & 3], sm[(z0 - 2) & 3], sr[(z0 - 1) & 1], 1, kZW);
   const int kend = kMode == 0 ? z1 + 1 : z1;
   for (int k = z0; k <= kend; k++) {
+    // the finishing step's pre-TV image at this thread's voxels of slice
+    // k - 1, loaded early so the load overlaps the wait and pass A
+    float f0[2] = {0.f, 0.f};
+    if (kMode == 2 && k - 1 >= z0 && k - 1 < z1) {
+#pragma unroll
+      for (int h = 0; h < 2; h++)
+        if (outvox(h)) f0[h] = im[(k - 1) * plane + (long long)gy[h] * D.nx + gx];
+    }
     if (k + 1 <= kend)
       stage(k + 1);
     else
@@ -815,10 +841,10 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
           dst[gi] = mn;
         } else {
           const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin3D.cpp:163-170
-          const float d = mc - I.m[gi];
+          const float d = mc - f0[h];
           acc += d * d;
-          I.m[gi] = mc;
-          I.m_pre[gi] = mc;
+          im[gi] = mc;
+          impre[gi] = mc;
         }
       }
       if (kMode == 2 && ((zb + 1) % kZSlab == 0 || zb + 1 == z1)) flush(zb);
