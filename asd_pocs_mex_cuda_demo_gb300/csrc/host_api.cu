@@ -385,7 +385,7 @@ struct asdpocs_plan_s {
   int batch = 0;
   Dims d{};    // largest sizes over the instances (grids of the launches)
   int nv = 0;  // largest number of views
-  int max_iter = 0, max_ng = 0;
+  int max_iter = 0, max_ng = 0, min_ng = 0;
   std::vector<asdpocs_geometry> geom;
   std::vector<asdpocs_options> opt;
   std::vector<Inst> h_inst;
@@ -541,7 +541,7 @@ namespace asd {
 
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk) {
+                              int tv_walk, bool finish) {
   cudaError_t e = cudaSuccess;
   if (shared) e = launch_group_pack(d_inst, batch, d, 0, st);
   for (int v = 0; v < nv && e == cudaSuccess; v++) {
@@ -555,13 +555,13 @@ cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
   if (e == cudaSuccess) e = launch_after_sweep(d_inst, batch, d, st);
   for (int s = 0; s < ng && e == cudaSuccess; s++)
     e = launch_tv_step(d_inst, batch, d, s, ng, st, tv_walk);
-  if (e == cudaSuccess) e = launch_finish_iter(d_inst, batch, d, ng, st);
+  if (e == cudaSuccess && finish) e = launch_finish_iter(d_inst, batch, d, ng, st);
   return e;
 }
 
 static int plan_enqueue_iteration(asdpocs_plan p) {
   ASD_CUDA(enqueue_iteration(p->d_inst, p->batch, p->d, p->nv, p->max_ng, p->shared,
-                             p->st, p->tv_walk));
+                             p->st, p->tv_walk, p->min_ng < 2));
   return 0;
 }
 
@@ -612,6 +612,8 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     if (p->opt[i].maxnumIter > p->max_iter) p->max_iter = p->opt[i].maxnumIter;
     if (p->opt[i].numOfgradients > p->max_ng)
       p->max_ng = p->opt[i].numOfgradients;
+    if (i == 0 || p->opt[i].numOfgradients < p->min_ng)
+      p->min_ng = p->opt[i].numOfgradients;
   }
   p->has_ref.assign(batch, 0);
   // instances with identical sizes, geometry and view angles share the

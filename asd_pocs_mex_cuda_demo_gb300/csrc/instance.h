@@ -68,8 +68,11 @@ cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st);
 // the iteration.  `shared`: the instances share geometry and angles and sit
 // in groups with interleaved images (Inst::m_il), packed before the sweep
 // and unpacked after it.
+// `finish`: some instance may run fewer than two TV steps, so the
+// end-of-iteration kernel is needed (otherwise the last TV step ends every
+// instance's iteration and the launch is skipped).
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk = 0);
+                              int tv_walk = 0, bool finish = true);
 
 }  // namespace asd

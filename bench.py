@@ -419,9 +419,11 @@ def main():
     ms = allmax(pg, statistics.mean(times))
     value = B * world / (ms / 1e3)
     rmse = [plan.stats(b)["RMSE"][-1] for b in range(B)]
-    # per iteration: forward + backward step per view, after-sweep, one fused
-    # launch per TV step, finish
-    kernels_per_step = iters * (2 * nv + 1 + ng + 1)
+    # per iteration: forward + backward step per view, after-sweep, one launch
+    # per TV step (the last also ends the iteration when ng >= 2, else an
+    # end-of-iteration launch), and for a batch sharing one geometry the
+    # interleave / de-interleave of the images around the sweep
+    kernels_per_step = iters * (2 * nv + 1 + ng + (1 if ng < 2 else 0) + (2 if B > 1 else 0))
 
     # ---- plain path (one reconstruction per plan, same kernels) for context
     plain_info = None
