@@ -664,8 +664,10 @@ __device__ __forceinline__ void atx_shared_voxel(
   }
 }
 
+// 4 blocks per SM for fan beams; 5 for cone beams (measured 3 % faster at
+// 128^3, 6 % slower for fan beams, whose extra spills cost more)
 template <bool kPlanar>
-__global__ void __launch_bounds__(kAtxThreads, 4)
+__global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 5)
     k_sart_atx_shared(const Inst *__restrict__ insts, int batch, int view) {
   __shared__ float s_beta[kShareGroup];
   __shared__ unsigned s_active;
@@ -720,13 +722,15 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 // projection, residual, dd2 and flags are bit-identical to it.
 // ---------------------------------------------------------------------------
 // columns per round of loads in the shared forward step: two for fan beams
-// (measured 6 % faster than one at 80 registers); one for cone beams, whose
-// three pieces per column already keep six loads in flight
+// (measured 6 % faster than one); one for cone beams, whose three pieces per
+// column already keep six loads in flight.  Blocks per SM: 6 for fan beams
+// (72 registers, no spills), 8 for cone beams (64 registers: 10 % faster
+// than 6 at 128^3).
 template <bool k3D>
 constexpr int kAxShareU = k3D ? 1 : 2;
 
 template <bool k3D>
-__global__ void __launch_bounds__(kAxBlock, 6)
+__global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
     k_sart_ax_shared(const Inst *__restrict__ insts, int batch, int view) {
   constexpr int kQuads = kShareGroup / 4;
   __shared__ unsigned s_active;
