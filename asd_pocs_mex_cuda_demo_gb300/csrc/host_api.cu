@@ -433,7 +433,9 @@ InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
   o.tvb = off; off += per_img;
   o.tvc = off; off += per_img;
   o.rmse = off; off += st ? align256((size_t)(max_iter + 1) * 8) : 0;
-  const size_t nparts = std::max(nblk * kMaxReduceK, (size_t)tv_partials_for(d));
+  // block partials of the projector and tile kernels; the 2-D walks keep four
+  // values per strip and band
+  const size_t nparts = std::max(nblk * kMaxReduceK, (size_t)tv_partials_for(d) * 4);
   o.part = off; off += st ? align256(nparts * 8) : 0;
   o.cnt = off; off += st ? 256 : 0;
   o.scal = off; off += st ? align256(sizeof(Scalars)) : 0;

@@ -52,7 +52,8 @@ cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
                                int ng, cudaStream_t st);
 
 int reduce_blocks_for(const Dims &d);
-// Reduction partials of the 2-D TV step (one per strip and band of rows).
+// Strips x bands of the 2-D walks (the TV steps keep one partial for each,
+// the end of the sweep four), or tiles x slabs of the cone-beam TV step.
 int tv_partials_for(const Dims &d);
 
 // Copies Inst::s->done of n instances into the device array out[n].

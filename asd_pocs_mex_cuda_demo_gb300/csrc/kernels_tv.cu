@@ -350,6 +350,25 @@ __device__ __forceinline__ void finish_scalars(Scalars *s, double dg2) {
   }
 }
 
+// The sweep's scalars from the totals of (m - m_pre)^2, (m - m_k1)^2,
+// (m - I0)^2 and v(m)^2 (ASD_POCS_cuda.m:137-149, imgTVGradMin.cpp:57-60).
+__device__ __forceinline__ void sweep_scalars(const Inst &I, const double (&tot)[4]) {
+  Scalars *s = I.s;
+  const double N = (double)I.d.nx * I.d.ny * I.d.nz;
+  s->dd2 = s->dd2_acc;
+  s->dd2_acc = 0.0;
+  s->dp = sqrt(tot[0]);
+  if (s->has_ref) I.rmse[s->k - 1] = sqrt(tot[2] / N);
+  s->iterations = s->k;
+  if (s->dp / N <= s->stopRelChg) {
+    s->done = 1;
+  } else {
+    s->d_tv = sqrt(tot[1]);
+    s->tv_coef = s->alpha * s->d_tv / sqrt(tot[3]);
+    s->tv_coef_f = (float)s->tv_coef;
+  }
+}
+
 // After the SART sweep (ASD_POCS_cuda.m:137-149): dd, m_res, RMSE, dp and the
 // stop test; d = ||m - m_k1|| (imgTVGradMin.cpp:57-60) and ||v|| of the first
 // TV step, giving its step size alpha*d/||v||.
@@ -395,22 +414,7 @@ __global__ void __launch_bounds__(kThreads)
   }
   double tot[4];
   if (grid_sum<kThreads, 4>(v, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
-    if (threadIdx.x == 0) {
-      Scalars *s = I.s;
-      const double N = (double)D.nx * D.ny * D.nz;
-      s->dd2 = s->dd2_acc;
-      s->dd2_acc = 0.0;
-      s->dp = sqrt(tot[0]);
-      if (s->has_ref) I.rmse[s->k - 1] = sqrt(tot[2] / N);
-      s->iterations = s->k;
-      if (s->dp / N <= s->stopRelChg) {
-        s->done = 1;
-      } else {
-        s->d_tv = sqrt(tot[1]);
-        s->tv_coef = s->alpha * s->d_tv / sqrt(tot[3]);
-        s->tv_coef_f = (float)s->tv_coef;
-      }
-    }
+    if (threadIdx.x == 0) sweep_scalars(I, tot);
   }
 }
 
@@ -691,6 +695,138 @@ __global__ void __launch_bounds__(kWalkWarps * 32, 8)
       s->tv_coef = s->alpha * s->d_tv / sqrt(a);
       s->tv_coef_f = (float)s->tv_coef;
     }
+  }
+}
+
+// End of the SART sweep for 2-D instances as column walks (the work of
+// k_after_sweep<false>): the same strips, bands and ring as k_tv_walk2d,
+// streaming m, m_pre, m_k1 and the reference image I0 through four rings.
+// Each output voxel copies m to m_res and adds (m - m_pre)^2, (m - m_k1)^2,
+// (m - I0)^2 and v(m)^2 (tv2_terms, the TV step's own stencil) to its
+// band's four partials; the walk that finishes last sums them in order and
+// sets the iteration's scalars (ASD_POCS_cuda.m:137-149).
+template <bool kPair>
+__device__ __forceinline__ void sweep_walk(const Inst &I, int y0, int y1, int xa, int strip,
+                                           int S, bool tv, float2 (*ring)[kWalkRing * 32]) {
+  const Dims D = I.d;
+  const int lane = threadIdx.x & 31;
+  const bool ina = xa >= 0 && xa < D.nx, inb = xa + 1 >= 0 && xa + 1 < D.nx;
+  const bool outl = lane >= 1 && lane <= 30;
+  const bool outa = outl && ina, outb = outl && inb;
+  const bool ref = I.I0 != nullptr;
+  float *const mres = I.m_res;
+  const float *srcs[4] = {I.m, I.m_pre, I.m_k1, ref ? I.I0 : I.m};
+  const int jl0 = y0 - 1, jl1 = min(D.ny, y1 + 1);  // rows read
+  auto fetch = [&](int j, int slot) {
+    const bool r = (unsigned)j < (unsigned)jl1;
+    const int off = r ? j * D.nx : 0;
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      float *d = (float *)&ring[a][32 * slot + lane];
+      const float *g = srcs[a] + off;
+      if (kPair) {
+        cp_async_8(d, g + (ina ? xa : 0), r && ina);
+      } else {
+        cp_async_4(d, g + (ina ? xa : 0), r && ina);
+        cp_async_4(d + 1, g + (inb ? xa + 1 : 0), r && inb);
+      }
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  for (int k = 0; k < kWalkRing - 1; k++) fetch(jl0 + k, k);
+  WalkField f1{0.f, 0.f, 0.f, 0.f};
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  const int ntot = y1 + 1 - jl0;  // rows jl0 .. y1
+  for (int n = 0; n < ntot; n++) {
+    const int j = jl0 + n, slot = n & (kWalkRing - 1);
+    const int oslot = (slot + kWalkRing - 1) & (kWalkRing - 1);  // row j - 1
+    // row j - 1's other arrays, read before that slot receives row
+    // j + kWalkRing - 1
+    const float2 mo = ring[0][32 * oslot + lane];
+    const float2 pre = ring[1][32 * oslot + lane];
+    const float2 k1 = ring[2][32 * oslot + lane];
+    const float2 i0 = ring[3][32 * oslot + lane];
+    fetch(j + kWalkRing - 1, oslot);
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(kWalkRing - 1) : "memory");
+    const float2 m = ring[0][32 * slot + lane];
+    float va = 0.f, vb = 0.f;
+    if (tv) f1.push(m.x, m.y, va, vb);  // warp-uniform
+    const int o = j - 1;
+    if (o < y0 || o >= y1) continue;  // warp-uniform
+    const int i = o * D.nx + xa;
+    auto add = [&](float mv, float pv, float kv, float iv, float v) {
+      const float a = mv - pv, b = mv - kv;
+      acc[0] += a * a;
+      acc[1] += b * b;
+      if (ref) {
+        const float c = mv - iv;
+        acc[2] += c * c;
+      }
+      acc[3] += v * v;
+    };
+    if (outa) {
+      add(mo.x, pre.x, k1.x, i0.x, va);
+      if (!kPair) mres[i] = mo.x;
+    }
+    if (outb) {
+      add(mo.y, pre.y, k1.y, i0.y, vb);
+      if (!kPair) mres[i + 1] = mo.y;
+    }
+    if (kPair && outa) *(float2 *)(mres + i) = mo;
+    if ((o + 1) % kBandRows == 0 || o + 1 == y1) {
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+#pragma unroll
+        for (int w = 16; w > 0; w >>= 1) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], w);
+        if (lane == 0) I.partials[((long long)(o / kBandRows) * S + strip) * 4 + k] = (double)acc[k];
+        acc[k] = 0.f;
+      }
+    }
+  }
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kWalkWarps * 32)
+    k_after_sweep_walk2d(const Inst *__restrict__ insts, int bands) {
+  __shared__ float2 ring[kWalkWarps][4][kWalkRing * 32];
+  const Inst &I = insts[blockIdx.z];
+  if (inst_done(I)) return;
+  const Dims D = I.d;
+  const int S = walk_strips(D.nx), NB = walk_bands(D.ny);
+  const int per_strip = (NB + bands - 1) / bands;
+  const int walks = S * per_strip;
+  const int w = blockIdx.x * kWalkWarps + (threadIdx.x >> 5);
+  if (w >= walks) return;  // warp-uniform
+  const int lane = threadIdx.x & 31;
+  const int strip = w % S, b0 = (w / S) * bands;
+  const int y0 = b0 * kBandRows, y1 = min(D.ny, (b0 + bands) * kBandRows);
+  const int xa = strip * kWalkOut - 2 + 2 * lane;
+  const bool tv = I.s->ng > 0;
+  if ((D.nx & 1) == 0)
+    sweep_walk<true>(I, y0, y1, xa, strip, S, tv, ring[threadIdx.x >> 5]);
+  else
+    sweep_walk<false>(I, y0, y1, xa, strip, S, tv, ring[threadIdx.x >> 5]);
+  unsigned ticket = 0;
+  if (lane == 0) {
+    __threadfence();
+    ticket = atomicAdd(I.counter, 1u);
+  }
+  ticket = __shfl_sync(0xffffffffu, ticket, 0);
+  if (ticket != (unsigned)walks - 1) return;
+  __threadfence();
+  const int P = S * NB;
+  double tot[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    double a = 0.0;
+    for (int p = lane; p < P; p += 32) a += ((volatile const double *)I.partials)[p * 4 + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    tot[k] = a;
+  }
+  if (lane == 0) {
+    *I.counter = 0u;
+    sweep_scalars(I, tot);
   }
 }
 
@@ -995,10 +1131,19 @@ cudaError_t launch_iter_begin(const Inst *, int, cudaStream_t) {
 cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
                                cudaStream_t st) {
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
-  if (d.nz > 1)
+  if (d.nz > 1) {
     k_after_sweep<true><<<grid, kThreads, 0, st>>>(insts);
-  else
-    k_after_sweep<false><<<grid, kThreads, 0, st>>>(insts);
+  } else {
+    // one band per walk up to a wave of walks (24 resident warps per SM at
+    // 80 registers), then longer walks
+    const long long units = (long long)walk_strips(d.nx) * walk_bands(d.ny);
+    const long long cap = 152LL * 24;
+    const long long per = (units * batch + cap - 1) / cap;
+    const int bands = (int)(per < 1 ? 1 : (per > walk_bands(d.ny) ? walk_bands(d.ny) : per));
+    const long long walks = (long long)walk_strips(d.nx) * ((walk_bands(d.ny) + bands - 1) / bands);
+    k_after_sweep_walk2d<<<dim3((unsigned)((walks + kWalkWarps - 1) / kWalkWarps), 1, batch),
+                           kWalkWarps * 32, 0, st>>>(insts, bands);
+  }
   return cudaGetLastError();
 }
 
