@@ -51,10 +51,13 @@ __device__ __forceinline__ void ax_lane_partial(const ViewGeo &G, const Dims &D,
   const RayMarch R = ray_setup(G, D, G.y_det[ia], zd);
   ys = 0.f;
   ss = 0.f;
+  // fan beams: the loads of two columns per round; cone beams: one (its
+  // three pieces per column already keep loads in flight; two measured 6 %
+  // slower at 256^3)
   if (D.nz == 1 && zd == 0.0f)
     ray_columns_planar_fast<2>(R, first, 32 * kAxCols, ld, ys, ss);
   else
-    ray_columns_fast<2>(R, first, 32 * kAxCols, ld, ys, ss);
+    ray_columns_fast<1>(R, first, 32 * kAxCols, ld, ys, ss);
 }
 
 // The block's ray totals: each warp stores its lane partials of the K values
