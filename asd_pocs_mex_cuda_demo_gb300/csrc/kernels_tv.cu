@@ -7,11 +7,11 @@
 // evaluates the stencil of m' for the next step's ||v'||^2 (deterministic
 // grid sum) -- so it reads the image once and writes it once (8 bytes per
 // voxel), and the ||v|| that every step needs before it can update comes out
-// of the previous kernel.  Cone beam: a block stages its 32x8 voxel tile
-// with a halo of two voxels in shared memory.  2-D: warps walk down strips
-// of columns with the stencils in registers (k_tv_walk2d).  The end-of-sweep
-// kernel provides ||v|| of the first step; the last step also applies the
-// positivity constraint and the alpha/beta step control.
+// of the previous kernel.  2-D: warps walk down strips of columns with the
+// stencils in registers (k_tv_walk2d).  Cone beam: blocks walk down z over
+// (x, y) tiles with the slices staged in shared memory (k_tv_walk3d).  The
+// end-of-sweep kernel provides ||v|| of the first step; the last step also
+// applies the positivity constraint and the alpha/beta step control.
 #include <type_traits>
 #include "kernels.h"
 #include "reduce.cuh"
