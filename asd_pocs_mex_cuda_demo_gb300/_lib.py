@@ -79,6 +79,12 @@ SIGNATURES = [
                                      C.c_int, C.c_void_p]),
     ("Ax_cone_gpu", C.c_int, [_F, C.c_longlong, C.POINTER(Para), _F, _F]),
     ("Atx_cone_gpu", C.c_int, [_F, C.c_longlong, C.POINTER(Para), _F, _F]),
+    ("asdpocs_adjoint_check_para", C.c_int, [_F, C.c_longlong, _F, C.c_longlong,
+                                             C.POINTER(Para), _D]),
+    ("asdpocs_adjoint_check", C.c_int, [_F, _F, C.c_float, C.c_float, _F, _F, C.c_float,
+                                        C.c_float, C.c_float, C.c_float, C.c_float,
+                                        C.c_float, C.c_int, C.c_int, C.c_int, C.c_int,
+                                        C.c_int, _D]),
     ("imgTVGradMin", C.c_int, [_D, _D, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int,
                                _D]),
     ("imgTVGradMin3D", C.c_int, [_D, _D, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,

@@ -190,6 +190,90 @@ static int ax_host(const float *X, float *y, float *sr, float cos_phi,
   return 0;
 }
 
+}  // extern "C"
+
+namespace asd {
+namespace {
+
+constexpr int kDotThreads = 256, kDotBlocks = 152 * 4;
+
+// FP64 partial dot products of a and b, one per block, each over a fixed
+// grid-stride subset and summed in a fixed order.
+__global__ void __launch_bounds__(kDotThreads)
+    k_dot_f64(const float *__restrict__ a, const float *__restrict__ b, long long n,
+              double *__restrict__ partials) {
+  __shared__ double sh[kDotThreads / 32];
+  double s = 0.0;
+  for (long long i = (long long)blockIdx.x * kDotThreads + threadIdx.x; i < n;
+       i += (long long)kDotBlocks * kDotThreads)
+    s += (double)a[i] * (double)b[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kDotThreads / 32; w++) t += sh[w];
+    partials[blockIdx.x] = t;
+  }
+}
+
+// out = the block partials summed in block order (one thread)
+__global__ void k_sum_f64(const double *__restrict__ partials, int n, double *out) {
+  double t = 0.0;
+  for (int i = 0; i < n; i++) t += partials[i];
+  *out = t;
+}
+
+}  // namespace
+}  // namespace asd
+
+extern "C" {
+
+int asdpocs_adjoint_check(const float *X, const float *yv, float cos_phi, float sin_phi,
+                          const float *y_det, const float *z_det, float SO, float OD,
+                          float scale, float dy_det, float dz_det, float dz, int nx,
+                          int ny, int nz, int na, int nb, double dots[2]) {
+  clear_error();
+  if (int e = check_dims(nx, ny, nz, na, nb)) return e;
+  if (!X || !yv || !y_det || !z_det || !dots)
+    return set_error(ASDPOCS_ERR_ARG, "null pointer");
+  const size_t N = (size_t)nx * ny * nz, M = (size_t)na * nb;
+  const size_t oX = 0, oY = oX + align256(N * 4), oAx = oY + align256(M * 4),
+               oSr = oAx + align256(M * 4), oAty = oSr + align256(M * 4),
+               oSc = oAty + align256(N * 4), oA = oSc + align256(N * 4),
+               oB = oA + align256((size_t)na * 4), oP = oB + align256((size_t)nb * 4),
+               oD = oP + align256((size_t)kDotBlocks * 8), tot = oD + 256;
+  Workspace *w;
+  if (int e = ws_acquire(w, tot)) return e;
+  std::lock_guard<std::mutex> lk(w->mu);
+  char *b = (char *)w->buf;
+  ASD_CUDA(cudaMemcpyAsync(b + oX, X, N * 4, cudaMemcpyHostToDevice, w->st));
+  ASD_CUDA(cudaMemcpyAsync(b + oY, yv, M * 4, cudaMemcpyHostToDevice, w->st));
+  ASD_CUDA(cudaMemcpyAsync(b + oA, y_det, (size_t)na * 4, cudaMemcpyHostToDevice, w->st));
+  ASD_CUDA(cudaMemcpyAsync(b + oB, z_det, (size_t)nb * 4, cudaMemcpyHostToDevice, w->st));
+  const ViewGeo g = with_constants(ViewGeo{cos_phi, sin_phi, SO, OD, scale, dy_det, dz_det,
+                                           dz, (const float *)(b + oA),
+                                           (const float *)(b + oB)});
+  const Dims d{nx, ny, nz, na, nb};
+  ASD_CUDA(launch_ax((const float *)(b + oX), (float *)(b + oAx), (float *)(b + oSr), g, d,
+                     w->st));
+  ASD_CUDA(launch_atx((float *)(b + oAty), (const float *)(b + oY), (float *)(b + oSc), g, d,
+                      w->st));
+  double *part = (double *)(b + oP), *dd = (double *)(b + oD);
+  k_dot_f64<<<kDotBlocks, kDotThreads, 0, w->st>>>((const float *)(b + oAx),
+                                                   (const float *)(b + oY), (long long)M,
+                                                   part);
+  k_sum_f64<<<1, 1, 0, w->st>>>(part, kDotBlocks, dd);
+  k_dot_f64<<<kDotBlocks, kDotThreads, 0, w->st>>>((const float *)(b + oX),
+                                                   (const float *)(b + oAty), (long long)N,
+                                                   part);
+  k_sum_f64<<<1, 1, 0, w->st>>>(part, kDotBlocks, dd + 1);
+  ASD_CUDA(cudaGetLastError());
+  ASD_CUDA(cudaMemcpyAsync(dots, dd, 16, cudaMemcpyDeviceToHost, w->st));
+  ASD_CUDA(cudaStreamSynchronize(w->st));
+  return 0;
+}
+
 static int atx_host(float *X, const float *yv, float *sc, float cos_phi,
                     float sin_phi, const float *y_det, const float *z_det,
                     float SO, float OD, float scale, float dy_det, float dz_det,
@@ -254,6 +338,23 @@ int Ax_cone_gpu(const float *X, long long numel_X, const asdpocs_para *para,
   return ax_host(X, y, sr, g.cos_phi, g.sin_phi, g.y_det.data(), g.z_det.data(),
                  g.SO, g.OD, g.scale, 1.0f, para->nx, para->ny, para->nz,
                  para->na, para->nb);
+}
+
+int asdpocs_adjoint_check_para(const float *X, long long numel_X, const float *Y,
+                               long long numel_Y, const asdpocs_para *para,
+                               double dots[2]) {
+  clear_error();
+  if (int e = check_para(para)) return e;
+  if (numel_X != (long long)para->nx * para->ny * para->nz)
+    return set_error(ASDPOCS_ERR_ARG, "Error size of input argument X!");
+  if (numel_Y != (long long)para->na * para->nb)
+    return set_error(ASDPOCS_ERR_ARG, "Error size of input argument Y!");
+  GatewayGeo g;
+  gateway_geometry(para->phi, para->SO, para->OD, para->vxlsize, para->detsize,
+                   para->na, para->nb, g);
+  return asdpocs_adjoint_check(X, Y, g.cos_phi, g.sin_phi, g.y_det.data(), g.z_det.data(),
+                               g.SO, g.OD, g.scale, g.det, g.det, 1.0f, para->nx,
+                               para->ny, para->nz, para->na, para->nb, dots);
 }
 
 int Atx_cone_gpu(const float *Y, long long numel_Y, const asdpocs_para *para,

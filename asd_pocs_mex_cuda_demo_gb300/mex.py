@@ -93,6 +93,19 @@ def Atx_cone_gpu(Y, para, *extra):
     return x, sc
 
 
+def adjoint_check(X, Y, para):
+    """(<Ax, Y>, <X, A^T Y>) of the view described by para, accumulated in
+    FP64 on the GPU: the two agree to the FP32 rounding of the projections."""
+    p = _para(para)
+    x = _flat_single(X)
+    yv = _flat_single(Y)
+    dots = np.zeros(2)
+    check(load().asdpocs_adjoint_check_para(x.ctypes.data_as(_F), x.size,
+                                            yv.ctypes.data_as(_F), yv.size, C.byref(p),
+                                            dots.ctypes.data_as(_D)))
+    return float(dots[0]), float(dots[1])
+
+
 def _tv_args(I, I0, ndim):
     I = np.asarray(I)
     if I.dtype != np.float64:

@@ -84,6 +84,16 @@ int asdpocs_atx_device(float *x_d, const float *y_d, float *sc_d,
                        float dy_det, float dz_det, float dz, int nx, int ny,
                        int nz, int na, int nb, void *stream);
 
+/* Adjoint consistency of one view's projector pair, the launcher-level
+ * arguments as above (all pointers on the host): dots[0] = <A x, y> and
+ * dots[1] = <x, A^T y>, both accumulated in FP64 on the GPU in a fixed
+ * order.  A and A^T carry the same `scale`, so the two agree to the FP32
+ * rounding of the projections.  Synchronous. */
+int asdpocs_adjoint_check(const float *X, const float *y, float cos_phi, float sin_phi,
+                          const float *y_det, const float *z_det, float SO, float OD,
+                          float scale, float dy_det, float dz_det, float dz, int nx,
+                          int ny, int nz, int na, int nb, double dots[2]);
+
 /* ------------------------------------------------------------------ */
 /* mex-level entry points (the para struct as a C struct)              */
 /* ------------------------------------------------------------------ */
@@ -105,6 +115,13 @@ int Ax_cone_gpu(const float *X, long long numel_X, const asdpocs_para *para,
  * numel_Y is checked against na*nb.  x, sc have nx*ny*nz elements. */
 int Atx_cone_gpu(const float *Y, long long numel_Y, const asdpocs_para *para,
                  float *x, float *sc);
+
+/* The adjoint check (asdpocs_adjoint_check) of the view described by para:
+ * dots[0] = <Ax_cone_gpu(X), Y>, dots[1] = <X, Atx_cone_gpu(Y)>, FP64 on the
+ * GPU.  numel checks as above. */
+int asdpocs_adjoint_check_para(const float *X, long long numel_X, const float *Y,
+                               long long numel_Y, const asdpocs_para *para,
+                               double dots[2]);
 
 /* I2 = imgTVGradMin(I, alpha, nTVIter, pos[, I0])   (imgTVGradMin.cpp:16-140)
  * I: rowN x colN double, column-major; img_old may be NULL (zeros).

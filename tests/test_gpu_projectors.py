@@ -183,3 +183,24 @@ def test_axis_parallel_central_ray(gpu, oracle_mod, angle):
                 detsize=det, na=na, nb=1)
     b, sc = pkg.Atx_cone_gpu(yv, para)
     assert np.array_equal(b, bo) and np.array_equal(sc, co)
+
+
+@pytest.mark.parametrize("dims", [(128, 128, 1, 256, 1), (48, 40, 24, 64, 48)])
+def test_adjoint_check_on_gpu(gpu, dims):
+    """<Ax, y> and <x, A^T y> accumulated in FP64 on the GPU agree, and match
+    the host FP64 dots of the GPU projections."""
+    nx, ny, nz, na, nb = dims
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = SO / (SO + OD) * det * na / max(nx, ny)
+    rng = np.random.default_rng(nz)
+    x = rng.random(nx * ny * nz).astype(np.float32)
+    yv = rng.random(na * nb).astype(np.float32)
+    for a in (13.0, 200.0):
+        para = dict(SO=SO, OD=OD, vxlsize=vx, nx=nx, ny=ny, nz=nz, phi=-a / 180 * np.pi,
+                    detsize=det, na=na, nb=nb)
+        lhs, rhs = pkg.adjoint_check(x, yv, para)
+        assert abs(lhs - rhs) / abs(lhs) < 2e-5
+        Ax, _ = pkg.Ax_cone_gpu(x, para)
+        Aty, _ = pkg.Atx_cone_gpu(yv, para)
+        assert abs(lhs - float(np.dot(Ax.astype(np.float64), yv))) <= 1e-9 * abs(lhs)
+        assert abs(rhs - float(np.dot(x.astype(np.float64), Aty))) <= 1e-9 * abs(rhs)
