@@ -969,15 +969,19 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   ASD_CUDA(cudaEventCreate(&e0));
   ASD_CUDA(cudaEventCreate(&e1));
   const int ng = p->max_ng > 0 ? p->max_ng : 1;
+  // projector steps: views spread evenly over the scan (a view's cost
+  // depends on its angle)
+  auto view_of_rep = [&](int i) { return (int)(((long long)i * p->nv / reps) % p->nv); };
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {
       case 0:
-        return p->shared ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, i % p->nv, p->st)
-                         : launch_sart_ax(p->d_inst, p->batch, p->d, i % p->nv, p->st);
+        return p->shared
+                   ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, view_of_rep(i), p->st)
+                   : launch_sart_ax(p->d_inst, p->batch, p->d, view_of_rep(i), p->st);
       case 1:
-        return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, i % p->nv,
-                                                  p->st)
-                         : launch_sart_atx(p->d_inst, p->batch, p->d, i % p->nv, p->st);
+        return p->shared
+                   ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, view_of_rep(i), p->st)
+                   : launch_sart_atx(p->d_inst, p->batch, p->d, view_of_rep(i), p->st);
       case 2: return launch_tv_step(p->d_inst, p->batch, p->d, 1 + i % (ng > 1 ? ng - 1 : 1),
                                     ng, p->st, p->tv_walk);
       default: return launch_after_sweep(p->d_inst, p->batch, p->d, p->st);
