@@ -188,7 +188,11 @@ def test_axis_parallel_central_ray(gpu, oracle_mod, angle):
 @pytest.mark.parametrize("dims", [(128, 128, 1, 256, 1), (48, 40, 24, 64, 48)])
 def test_adjoint_check_on_gpu(gpu, dims):
     """<Ax, y> and <x, A^T y> accumulated in FP64 on the GPU agree, and match
-    the host FP64 dots of the GPU projections."""
+    the host FP64 dots of the GPU projections.  In 2-D the reference's
+    forward march and backprojector use the same exact intersection lengths
+    (agreement to FP32 rounding); in 3-D its forward march approximates
+    them (a piecewise column march against find_l_3d's exact chords), so
+    the pair is adjoint to about 1e-4 only."""
     nx, ny, nz, na, nb = dims
     SO, OD, det = 541.0, 408.0, 1.0
     vx = SO / (SO + OD) * det * na / max(nx, ny)
@@ -199,7 +203,7 @@ def test_adjoint_check_on_gpu(gpu, dims):
         para = dict(SO=SO, OD=OD, vxlsize=vx, nx=nx, ny=ny, nz=nz, phi=-a / 180 * np.pi,
                     detsize=det, na=na, nb=nb)
         lhs, rhs = pkg.adjoint_check(x, yv, para)
-        assert abs(lhs - rhs) / abs(lhs) < 2e-5
+        assert abs(lhs - rhs) / abs(lhs) < (2e-5 if nz == 1 else 5e-4)
         Ax, _ = pkg.Ax_cone_gpu(x, para)
         Aty, _ = pkg.Atx_cone_gpu(yv, para)
         assert abs(lhs - float(np.dot(Ax.astype(np.float64), yv))) <= 1e-9 * abs(lhs)
