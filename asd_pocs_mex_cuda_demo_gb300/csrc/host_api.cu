@@ -972,28 +972,48 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   // projector steps: views spread evenly over the scan (a view's cost
   // depends on its angle)
   auto view_of_rep = [&](int i) { return (int)(((long long)i * p->nv / reps) % p->nv); };
+  auto ax = [&](int v) {
+    return p->shared ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, v, p->st)
+                     : launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st);
+  };
+  auto atx = [&](int v) {
+    return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, v, p->st)
+                     : launch_sart_atx(p->d_inst, p->batch, p->d, v, p->st);
+  };
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {
-      case 0:
-        return p->shared
-                   ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, view_of_rep(i), p->st)
-                   : launch_sart_ax(p->d_inst, p->batch, p->d, view_of_rep(i), p->st);
-      case 1:
-        return p->shared
-                   ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, view_of_rep(i), p->st)
-                   : launch_sart_atx(p->d_inst, p->batch, p->d, view_of_rep(i), p->st);
+      case 0: return ax(view_of_rep(i));
       case 2: return launch_tv_step(p->d_inst, p->batch, p->d, 1 + i % (ng > 1 ? ng - 1 : 1),
                                     ng, p->st, p->tv_walk);
       default: return launch_after_sweep(p->d_inst, p->batch, p->d, p->st);
     }
   };
-  cudaError_t e = launch(0);  // warm-up
-  if (e == cudaSuccess) e = cudaEventRecord(e0, p->st);
-  for (int i = 0; i < reps && e == cudaSuccess; i++) e = launch(i);
-  if (e == cudaSuccess) e = cudaEventRecord(e1, p->st);
-  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  cudaError_t e = cudaSuccess;
   float ms = 0.f;
-  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (phase == 1) {
+    // the backward step reads what the forward step of its view leaves (the
+    // residuals, the ray-slope table, their finiteness), and its cost
+    // depends on it: each timed launch follows its view's untimed forward
+    // step
+    for (int i = 0; i < reps && e == cudaSuccess; i++) {
+      const int v = view_of_rep(i);
+      e = ax(v);
+      if (e == cudaSuccess) e = cudaEventRecord(e0, p->st);
+      if (e == cudaSuccess) e = atx(v);
+      if (e == cudaSuccess) e = cudaEventRecord(e1, p->st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float t = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+      ms += t;
+    }
+  } else {
+    e = launch(0);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(e0, p->st);
+    for (int i = 0; i < reps && e == cudaSuccess; i++) e = launch(i);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, p->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   ASD_CUDA(e);

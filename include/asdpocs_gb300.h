@@ -255,8 +255,10 @@ int asdpocs_plan_set_tv_walk(asdpocs_plan plan, int walk);
 /* Profiling hook: average device time (ms, CUDA events on the plan's
  * stream) of `reps` back-to-back launches of one phase kernel for the whole
  * batch.  phase: 0 = SART forward step (Ax + residual), 1 = SART backward
- * step (Atx + update), both at `reps` views spread evenly over the scan,
- * 2 = one TV step (norm pass + update pass), 3 = end-of-sweep scalars.  The launches modify the plan's state: call
+ * step (Atx + update; each timed launch follows its view's untimed
+ * forward step, whose residuals and tables it reads), both at `reps` views
+ * spread evenly over the scan, 2 = one TV step (norm pass + update pass),
+ * 3 = end-of-sweep scalars.  The launches modify the plan's state: call
  * asdpocs_plan_reset() before the next run. */
 int asdpocs_plan_time_phase(asdpocs_plan plan, int phase, int reps,
                             double *avg_ms);
