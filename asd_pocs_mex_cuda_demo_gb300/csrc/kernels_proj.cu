@@ -70,18 +70,18 @@ __device__ __forceinline__ void ax_combine(float (&sp)[kAxCols][kAxWarps][K][32]
   if constexpr (kAxCols == 1) {
 #pragma unroll
     for (int k = 0; k < K; k++) v[k] = warp_sum(v[k]);
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int k = 0; k < K; k++) sp[part][rw][k][lane] = v[k];
-  __syncthreads();
-  if (part == 0) {
+    for (int k = 0; k < K; k++) sp[part][rw][k][lane] = v[k];
+    __syncthreads();
+    if (part == 0) {
 #pragma unroll
-    for (int k = 0; k < K; k++) {
-      float t = sp[0][rw][k][lane];
+      for (int k = 0; k < K; k++) {
+        float t = sp[0][rw][k][lane];
 #pragma unroll
-      for (int p = 1; p < kAxCols; p++) t += sp[p][rw][k][lane];
-      v[k] = warp_sum(t);
+        for (int p = 1; p < kAxCols; p++) t += sp[p][rw][k][lane];
+        v[k] = warp_sum(t);
+      }
     }
   }
 }
