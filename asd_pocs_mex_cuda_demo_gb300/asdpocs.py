@@ -257,6 +257,11 @@ class Plan:
         check(load().asdpocs_plan_autotune(self._h, int(reps), C.byref(w), C.byref(ms)))
         return w.value, ms.value
 
+    @property
+    def streams(self) -> int:
+        """Sub-batches run concurrently on their own streams."""
+        return int(load().asdpocs_plan_streams(self._h))
+
     def set_tv_walk(self, walk: int):
         """Pins the TV walk length (bands or slabs per walk; 0: the
         batch-size rule)."""

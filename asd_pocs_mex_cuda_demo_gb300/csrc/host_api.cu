@@ -479,6 +479,23 @@ void asdpocs_options_default(asdpocs_options *o) {
 // ======================================================================
 // Plans: batched, device-resident ASD-POCS
 // ======================================================================
+namespace asd {
+// A plan's batch runs as one or two sub-batches, each on its own stream with
+// its own captured iteration, so that the forward, backward and TV kernels
+// of one sub-batch overlap those of the other (each kernel alone leaves the
+// GPU partly idle: it is bound by latency, not by a unit's throughput).
+// Instances never read each other's state, so results do not change.
+struct SubBatch {
+  int first = 0, count = 0;  // instances [first, first + count)
+  Dims d{};                  // largest sizes of these instances
+  int nv = 0, max_ng = 0, min_ng = 0;
+  cudaStream_t st = nullptr;  // the plan's stream when there is one sub-batch
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t done = nullptr;
+};
+}  // namespace asd
+
 struct asdpocs_plan_s {
   int device = 0;
   cudaStream_t st = nullptr;
@@ -496,8 +513,8 @@ struct asdpocs_plan_s {
   Inst *d_inst = nullptr;
   void *arena = nullptr;
   size_t bytes = 0;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  std::vector<asd::SubBatch> subs;
+  cudaEvent_t fork = nullptr;  // orders the sub-batches after the plan's stream
 };
 
 namespace asd {
@@ -662,10 +679,54 @@ cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
   return e;
 }
 
-static int plan_enqueue_iteration(asdpocs_plan p) {
-  ASD_CUDA(enqueue_iteration(p->d_inst, p->batch, p->d, p->nv, p->max_ng, p->shared,
-                             p->st, p->tv_walk, p->min_ng < 2));
+// One iteration of sub-batch s on its stream.
+static int plan_enqueue_sub(asdpocs_plan p, const SubBatch &s) {
+  ASD_CUDA(enqueue_iteration(p->d_inst + s.first, s.count, s.d, s.nv, s.max_ng, p->shared,
+                             s.st, p->tv_walk, s.min_ng < 2));
   return 0;
+}
+
+// Splits the batch: two sub-batches once it holds two groups of shared
+// geometry (the split falls on a group boundary), else one on the plan's
+// stream.  Sizes, view and TV-step counts per sub-batch.
+static int plan_make_subs(asdpocs_plan p) {
+  const int nsub = p->batch >= 2 * kShareSlots ? 2 : 1;
+  const int c0 = nsub == 1 ? p->batch
+                           : (p->batch / 2 + kShareSlots - 1) / kShareSlots * kShareSlots;
+  p->subs.assign(nsub, SubBatch{});
+  for (int k = 0; k < nsub; k++) {
+    SubBatch &s = p->subs[k];
+    s.first = k == 0 ? 0 : c0;
+    s.count = k == 0 ? c0 : p->batch - c0;
+    for (int i = s.first; i < s.first + s.count; i++) {
+      const asdpocs_geometry &g = p->geom[i];
+      s.d.nx = std::max(s.d.nx, g.nx);
+      s.d.ny = std::max(s.d.ny, g.ny);
+      s.d.nz = std::max(s.d.nz, g.nz);
+      s.d.na = std::max(s.d.na, g.na);
+      s.d.nb = std::max(s.d.nb, g.nb);
+      s.nv = std::max(s.nv, g.nv);
+      const int ng = p->opt[i].numOfgradients;
+      s.max_ng = std::max(s.max_ng, ng);
+      s.min_ng = i == s.first ? ng : std::min(s.min_ng, ng);
+    }
+    if (nsub == 1) {
+      s.st = p->st;
+    } else {
+      ASD_CUDA(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+      ASD_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+    }
+  }
+  if (nsub > 1) ASD_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
+  return 0;
+}
+
+// First instance of the sub-batch holding instance i.
+static int plan_sub_first(asdpocs_plan p, int i) {
+  int f = 0;
+  for (const SubBatch &s : p->subs)
+    if (i >= s.first) f = s.first;
+  return f;
 }
 
 }  // namespace asd
@@ -743,6 +804,10 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     }
     p->own_stream = true;
   }
+  if (int rc = plan_make_subs(p)) {
+    asdpocs_plan_destroy(p);
+    return rc;
+  }
   // ---- arena: each instance's block at its own sizes ----
   std::vector<InstLayout> lay(batch);
   std::vector<size_t> base(batch);
@@ -785,9 +850,11 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
       I.cor = (float *)(b + base[g] + lay[g].cor) + i % kShareSlots;
       I.cor_stride = kShareSlots;
       I.m_il = (float *)(b + base[g] + lay[g].m_il);
-      // one ray-slope table for all: instance 0 refreshes it every view
-      I.tabC = (float4 *)(b + base[0] + lay[0].tabC);
-      I.tabc_mode = i == 0 ? kTabcShared : kTabcNone;
+      // one ray-slope table per sub-batch: its first instance refreshes it
+      // every view (the sub-batches run different views at a time)
+      const int f = plan_sub_first(p, i);
+      I.tabC = (float4 *)(b + base[f] + lay[f].tabC);
+      I.tabc_mode = i == f ? kTabcShared : kTabcNone;
     }
   }
   p->d_inst = (Inst *)(b + inst_off);
@@ -806,8 +873,16 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
 
 int asdpocs_plan_destroy(asdpocs_plan p) {
   if (!p) return 0;
-  if (p->exec) cudaGraphExecDestroy(p->exec);
-  if (p->graph) cudaGraphDestroy(p->graph);
+  for (SubBatch &s : p->subs) {
+    if (s.exec) cudaGraphExecDestroy(s.exec);
+    if (s.graph) cudaGraphDestroy(s.graph);
+    if (s.st && s.st != p->st) {
+      cudaStreamSynchronize(s.st);
+      cudaStreamDestroy(s.st);
+    }
+    if (s.done) cudaEventDestroy(s.done);
+  }
+  if (p->fork) cudaEventDestroy(p->fork);
   if (p->st) cudaStreamSynchronize(p->st);
   if (p->arena) cudaFree(p->arena);
   if (p->own_stream && p->st) cudaStreamDestroy(p->st);
@@ -886,24 +961,38 @@ int asdpocs_plan_run(asdpocs_plan p, int use_graph) {
   if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
   if (p->max_iter <= 0) return 0;
   if (use_graph) {
-    if (!p->exec) {
-      ASD_CUDA(cudaStreamBeginCapture(p->st, cudaStreamCaptureModeThreadLocal));
-      const int rc = plan_enqueue_iteration(p);
+    for (SubBatch &s : p->subs) {
+      if (s.exec) continue;
+      ASD_CUDA(cudaStreamBeginCapture(s.st, cudaStreamCaptureModeThreadLocal));
+      const int rc = plan_enqueue_sub(p, s);
       cudaGraph_t g = nullptr;
-      const cudaError_t e = cudaStreamEndCapture(p->st, &g);
+      const cudaError_t e = cudaStreamEndCapture(s.st, &g);
       if (rc) {
         if (g) cudaGraphDestroy(g);
         return rc;
       }
       ASD_CUDA(e);
-      p->graph = g;
-      ASD_CUDA(cudaGraphInstantiate(&p->exec, p->graph, 0));
+      s.graph = g;
+      ASD_CUDA(cudaGraphInstantiate(&s.exec, s.graph, 0));
     }
-    for (int k = 0; k < p->max_iter; k++)
-      ASD_CUDA(cudaGraphLaunch(p->exec, p->st));
-  } else {
-    for (int k = 0; k < p->max_iter; k++)
-      if (int rc = plan_enqueue_iteration(p)) return rc;
+  }
+  const bool multi = p->subs.size() > 1;
+  if (multi) {  // the sub-batches start after the work queued on the plan's stream
+    ASD_CUDA(cudaEventRecord(p->fork, p->st));
+    for (SubBatch &s : p->subs) ASD_CUDA(cudaStreamWaitEvent(s.st, p->fork, 0));
+  }
+  for (int k = 0; k < p->max_iter; k++)
+    for (SubBatch &s : p->subs) {
+      if (use_graph)
+        ASD_CUDA(cudaGraphLaunch(s.exec, s.st));
+      else if (int rc = plan_enqueue_sub(p, s))
+        return rc;
+    }
+  if (multi) {  // and the plan's stream continues after both
+    for (SubBatch &s : p->subs) {
+      ASD_CUDA(cudaEventRecord(s.done, s.st));
+      ASD_CUDA(cudaStreamWaitEvent(p->st, s.done, 0));
+    }
   }
   return 0;
 }
@@ -1022,11 +1111,15 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
 }
 
 static void plan_drop_graph(asdpocs_plan p) {
-  if (p->exec) cudaGraphExecDestroy(p->exec);
-  if (p->graph) cudaGraphDestroy(p->graph);
-  p->exec = nullptr;
-  p->graph = nullptr;
+  for (SubBatch &s : p->subs) {
+    if (s.exec) cudaGraphExecDestroy(s.exec);
+    if (s.graph) cudaGraphDestroy(s.graph);
+    s.exec = nullptr;
+    s.graph = nullptr;
+  }
 }
+
+int asdpocs_plan_streams(asdpocs_plan p) { return p ? (int)p->subs.size() : 0; }
 
 int asdpocs_plan_set_tv_walk(asdpocs_plan p, int walk) {
   clear_error();

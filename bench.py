@@ -423,7 +423,9 @@ def main():
     # per TV step (the last also ends the iteration when ng >= 2, else an
     # end-of-iteration launch), and for a batch sharing one geometry the
     # interleave / de-interleave of the images around the sweep
-    kernels_per_step = iters * (2 * nv + 1 + ng + (1 if ng < 2 else 0) + (2 if B > 1 else 0))
+    # (once per sub-batch: the plan runs two concurrently for large batches)
+    kernels_per_step = (plan.streams * iters *
+                        (2 * nv + 1 + ng + (1 if ng < 2 else 0) + (2 if B > 1 else 0)))
 
     # ---- plain path (one reconstruction per plan, same kernels) for context
     plain_info = None

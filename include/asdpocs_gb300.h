@@ -252,6 +252,13 @@ int asdpocs_plan_autotune(asdpocs_plan plan, int reps, int *walk, double *ms);
  * clipped to a whole image). */
 int asdpocs_plan_set_tv_walk(asdpocs_plan plan, int walk);
 
+/* Number of sub-batches the plan runs concurrently, each on its own stream
+ * with its own captured iteration (2 once the batch holds 16 instances,
+ * else 1); asdpocs_plan_run orders them after the plan's stream and the
+ * plan's stream after them.  Every launch of an iteration is issued once
+ * per sub-batch. */
+int asdpocs_plan_streams(asdpocs_plan plan);
+
 /* Profiling hook: average device time (ms, CUDA events on the plan's
  * stream) of `reps` back-to-back launches of one phase kernel for the whole
  * batch.  phase: 0 = SART forward step (Ax + residual), 1 = SART backward
