@@ -686,18 +686,22 @@ static int plan_enqueue_sub(asdpocs_plan p, const SubBatch &s) {
   return 0;
 }
 
-// Splits the batch: two sub-batches once it holds two groups of shared
-// geometry (the split falls on a group boundary), else one on the plan's
-// stream.  Sizes, view and TV-step counts per sub-batch.
+// Splits the batch into up to kMaxSubBatches sub-batches of whole groups
+// (kShareSlots instances), at least kSubGroups groups each; a single
+// sub-batch runs on the plan's stream.  Sizes, view and TV-step counts per
+// sub-batch.
+constexpr int kMaxSubBatches = 2, kSubGroups = 1;
 static int plan_make_subs(asdpocs_plan p) {
-  const int nsub = p->batch >= 2 * kShareSlots ? 2 : 1;
-  const int c0 = nsub == 1 ? p->batch
-                           : (p->batch / 2 + kShareSlots - 1) / kShareSlots * kShareSlots;
+  // whole groups per sub-batch, at least kSubGroups of them
+  const int groups = (p->batch + kShareSlots - 1) / kShareSlots;
+  const int want = std::max(1, std::min(kMaxSubBatches, groups / kSubGroups));
+  const int per = (groups + want - 1) / want * kShareSlots;  // instances per sub-batch
+  const int nsub = (p->batch + per - 1) / per;
   p->subs.assign(nsub, SubBatch{});
   for (int k = 0; k < nsub; k++) {
     SubBatch &s = p->subs[k];
-    s.first = k == 0 ? 0 : c0;
-    s.count = k == 0 ? c0 : p->batch - c0;
+    s.first = k * per;
+    s.count = std::min(p->batch, (k + 1) * per) - s.first;
     for (int i = s.first; i < s.first + s.count; i++) {
       const asdpocs_geometry &g = p->geom[i];
       s.d.nx = std::max(s.d.nx, g.nx);
