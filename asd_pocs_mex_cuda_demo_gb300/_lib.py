@@ -114,6 +114,7 @@ SIGNATURES = [
     ("asdpocs_plan_autotune", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), _D]),
     ("asdpocs_plan_set_tv_walk", C.c_int, [C.c_void_p, C.c_int]),
     ("asdpocs_plan_streams", C.c_int, [C.c_void_p]),
+    ("asdpocs_plan_chord_slots", C.c_int, [C.c_void_p]),
     ("asdpocs_phantom_device", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _D, C.c_int,
                                          C.c_double, C.c_void_p]),
     ("asdpocs_poisson_noise_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong,

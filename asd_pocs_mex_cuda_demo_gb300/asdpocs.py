@@ -262,6 +262,12 @@ class Plan:
         """Sub-batches run concurrently on their own streams."""
         return int(load().asdpocs_plan_streams(self._h))
 
+    @property
+    def chord_slots(self) -> int:
+        """Chord slots per voxel of the backward step's chord tables (2-D
+        shared-geometry plans), 0 when the plan computes chords every step."""
+        return int(load().asdpocs_plan_chord_slots(self._h))
+
     def set_tv_walk(self, walk: int):
         """Pins the TV walk length (bands or slabs per walk; 0: the
         batch-size rule)."""

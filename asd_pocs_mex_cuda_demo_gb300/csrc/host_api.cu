@@ -515,6 +515,9 @@ struct asdpocs_plan_s {
   size_t bytes = 0;
   std::vector<asd::SubBatch> subs;
   cudaEvent_t fork = nullptr;  // orders the sub-batches after the plan's stream
+  int *chtab = nullptr;        // backward-step chord tables (2-D shared plans)
+  int chK = 0;                 // their slots per voxel and view
+  unsigned long long budget = 0;  // HBM budget of the plan (0: none)
 };
 
 namespace asd {
@@ -604,6 +607,8 @@ cudaError_t bind_geometry(Inst &I, char *b, const InstLayout &o,
   I.vflags = (int *)(b + o.vflags);
   I.tabC = (float4 *)(b + o.tabC);
   I.tabc_mode = kTabcOwn;
+  I.chtab = nullptr;
+  I.chK = 0;
   // pageable sources: staged before each call returns
   cudaError_t e = cudaMemcpyAsync(b + o.ydet, gg.y_det.data(), (size_t)g.na * 4,
                                   cudaMemcpyHostToDevice, st);
@@ -737,6 +742,60 @@ static int plan_sub_first(asdpocs_plan p, int i) {
 
 extern "C" {
 
+// Backward-step chord tables of a 2-D shared-geometry plan (Inst::chtab): a
+// counting pass for the slots per voxel, then the filling pass.  A plan
+// without them (a voxel with more pairs than kChordMaxSlots, tables over the
+// plan's HBM budget, or no memory left) computes its chords in every step,
+// with the same results.
+static cudaError_t plan_chord_tables(asdpocs_plan p) {
+  const Dims &d = p->d;
+  if (d.nz != 1 || d.nb != 1 || (long long)d.na >= (1LL << 24) || p->nv > 65535)
+    return cudaSuccess;
+  int *kmax = nullptr;
+  if (cudaMalloc(&kmax, 2 * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();  // out of memory is not sticky: run without tables
+    return cudaSuccess;
+  }
+  int hk[2] = {0, 0};
+  cudaError_t e = cudaMemsetAsync(kmax, 0, sizeof(hk), p->st);
+  if (e == cudaSuccess) e = launch_atx_chords(p->d_inst, d, p->nv, 0, nullptr, kmax, p->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(hk, kmax, sizeof(hk), cudaMemcpyDeviceToHost, p->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  const int K = hk[0];
+  const size_t bytes = atx_chord_words(d, p->nv, K) * sizeof(int);
+  int *tab = nullptr;
+  if (e == cudaSuccess && K > 0 && K <= atx_chord_max_slots() &&
+      (!p->budget || p->bytes + bytes <= p->budget)) {
+    if (cudaMalloc(&tab, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      tab = nullptr;
+    }
+  }
+  if (tab) {
+    e = launch_atx_chords(p->d_inst, d, p->nv, K, tab, kmax, p->st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(hk, kmax, sizeof(hk), cudaMemcpyDeviceToHost, p->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+    if (e == cudaSuccess && hk[1] == 0) {
+      for (Inst &I : p->h_inst) {
+        I.chtab = tab;
+        I.chK = K;
+      }
+      e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(), sizeof(Inst) * p->batch,
+                          cudaMemcpyHostToDevice, p->st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+      p->chtab = tab;  // freed with the plan
+      p->chK = K;
+      p->bytes += bytes;
+      tab = nullptr;
+    }
+  }
+  if (tab) cudaFree(tab);
+  cudaFree(kmax);
+  return e;
+}
+
 int asdpocs_plan_create(asdpocs_plan *out, int batch,
                         const asdpocs_geometry *geom,
                         const double *phi_vec_deg, const asdpocs_options *opt,
@@ -771,6 +830,7 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   asdpocs_plan p = new (std::nothrow) asdpocs_plan_s;
   if (!p) return set_error(ASDPOCS_ERR_NOMEM, "host allocation");
   p->batch = batch;
+  p->budget = hbm_budget_bytes;
   p->d = dmax;
   p->nv = nv_max;
   p->geom.assign(geom, geom + batch);
@@ -867,6 +927,8 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
                                             cudaMemcpyHostToDevice, p->st);
   if (e == cudaSuccess) e = launch_view_tables(p->d_inst, batch, p->d, p->nv, p->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  if (e == cudaSuccess && p->shared && !getenv("ASDPOCS_NO_CHORD_TABLE"))
+    e = plan_chord_tables(p);
   if (e != cudaSuccess) {
     asdpocs_plan_destroy(p);
     return cuda_status(e, "plan setup");
@@ -889,6 +951,7 @@ int asdpocs_plan_destroy(asdpocs_plan p) {
   if (p->fork) cudaEventDestroy(p->fork);
   if (p->st) cudaStreamSynchronize(p->st);
   if (p->arena) cudaFree(p->arena);
+  if (p->chtab) cudaFree(p->chtab);
   if (p->own_stream && p->st) cudaStreamDestroy(p->st);
   delete p;
   return 0;
@@ -1124,6 +1187,8 @@ static void plan_drop_graph(asdpocs_plan p) {
 }
 
 int asdpocs_plan_streams(asdpocs_plan p) { return p ? (int)p->subs.size() : 0; }
+
+int asdpocs_plan_chord_slots(asdpocs_plan p) { return p ? p->chK : 0; }
 
 int asdpocs_plan_set_tv_walk(asdpocs_plan p, int walk) {
   clear_error();

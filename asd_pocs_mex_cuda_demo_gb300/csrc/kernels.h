@@ -61,7 +61,8 @@ cudaError_t launch_gather_done(const Inst *insts, int n, int *out,
                                cudaStream_t st);
 
 // Backward step for a batch whose instances share geometry and view angles:
-// chords computed once per voxel and applied to groups of instances.
+// chords computed once per voxel and applied to groups of instances (read
+// from the plan's chord tables, Inst::chtab, where it has them).
 cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
                                    const Dims &d, int view, cudaStream_t st);
 
@@ -74,6 +75,16 @@ cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
 // (unpack = 1) their group's interleaved images.
 cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,
                               int unpack, cudaStream_t st);
+
+// Backward-step chord tables of a 2-D shared-geometry plan (Inst::chtab),
+// from the plan's first instance, whose view tables must be built.  K == 0
+// counts: the largest number of pairs of a voxel goes to kmax[0] (zeroed
+// first).  K > 0 fills `tabs` (atx_chord_words(d, nv, K) ints) and sets
+// kmax[1] if a voxel has more than K pairs.
+cudaError_t launch_atx_chords(const Inst *insts, const Dims &d, int nv, int K,
+                              int *tabs, int *kmax, cudaStream_t st);
+size_t atx_chord_words(const Dims &d, int nv, int K);
+int atx_chord_max_slots();
 
 // Ray slope tables and flags of every view (Inst::tabA, Inst::vflags, which
 // must be zeroed first), computed once per plan.

@@ -535,6 +535,34 @@ constexpr int kShareGroup = kShareSlots;
 // than 2 for cone-beam groups, the same for fan beams)
 constexpr int kPairChunk = 1;
 
+// SART update of one voxel for the group (ASD_POCS_cuda.m:128-134):
+// m += beta * (Atx(cor) * scale) / (sumC * scale), sumC == 0 -> 1, then
+// positivity.  accl is the voxel's chord sum, acc[b] slot b's weighted sum.
+__device__ __forceinline__ void atx_shared_apply(const ViewGeo &G, unsigned vi,
+                                                 float accl, const float *acc,
+                                                 unsigned active, int gn, float *m_il,
+                                                 const float *s_beta) {
+  const float scv = accl * G.scale;
+  // the group's images, interleaved: kShareGroup / 4 float4 per voxel
+  float4 *mg = (float4 *)m_il + (size_t)vi * (kShareGroup / 4);
+#pragma unroll
+  for (int q = 0; q < kShareGroup / 4; q++) {
+    if (!((active >> (4 * q)) & 0xFu)) continue;
+    float4 m4 = mg[q];
+    float *mv = &m4.x;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int b = 4 * q + j;
+      if (b < gn && ((active >> b) & 1u)) {
+        const float bp = acc[b] * G.scale;
+        const float mn = mv[j] + s_beta[b] * __fdividef(bp, scv == 0.f ? 1.f : scv);
+        mv[j] = mn < 0.f ? 0.f : mn;
+      }
+    }
+    mg[q] = m4;
+  }
+}
+
 // The voxel of this thread for the group (see k_sart_atx_shared).
 template <bool kPlanar, int AX>
 __device__ __forceinline__ void atx_shared_voxel(
@@ -647,15 +675,163 @@ __device__ __forceinline__ void atx_shared_voxel(
     }
   }
   if (!valid) return;
-  const float scv = accl * G.scale;
-  const unsigned vi = ((unsigned)iz * D.ny + iy) * D.nx + ix;
-  // the group's images, interleaved: kShareGroup / 4 float4 per voxel
+  atx_shared_apply(G, ((unsigned)iz * D.ny + iy) * D.nx + ix, accl, acc, active, gn,
+                   m_il, s_beta);
+}
+
+// ---------------------------------------------------------------------------
+// Chord tables of 2-D shared-geometry plans.  The chords of the backward step
+// depend on the geometry and the view only, so a plan whose instances share
+// them computes every view's chords once (k_atx_chords) and its backward
+// steps read them instead of repeating the window, shadow and face tests of
+// find_l for every group and iteration.  Per view the table holds, for voxel
+// vi = iy * nx + ix of the N = nx * ny voxels:
+//   hdr[vi]          (count << 24) | first ray, 0 for no pair
+//   sum[vi]          the voxel's chord sum (float bits)
+//   ch[k * N + vi]   chord of pair k < count (ray first + k)
+// in that order, (2 + chK) * N words per view.  The pairs, their chords and
+// the chord sum are those of the narrow form of atx_shared_voxel, in the same
+// order and from the same functions, so the backward step gives the same
+// bits with or without the table.  Views with an axis-parallel ray have no
+// table (their pairs need the full window); the step also keeps the direct
+// form when a residual is not finite (0 * inf is not 0).
+// ---------------------------------------------------------------------------
+constexpr int kChordMaxSlots = 32;
+
+__host__ __device__ __forceinline__ size_t chord_view_words(const Dims &d, int K) {
+  return (size_t)(2 + K) * (size_t)d.nx * (size_t)d.ny;
+}
+
+// Pairs of this voxel: the reference's window narrowed to the voxel's shadow.
+template <int AX>
+__device__ __forceinline__ void chords_voxel(const ViewGeo &G, const Dims &D,
+                                             const float4 *__restrict__ tabA,
+                                             bool valid, int ix, int iy, int K,
+                                             int *tab, int *kmax) {
+  const VoxelWin w = voxel_window(G, D, ix, iy, 0);
+  const bool has = valid && w.a0 <= w.a1 && w.b0 <= w.b1;
+  int lo = has ? w.a0 : 0, hi = has ? w.a1 : -1;
+  if (has) {
+    int slo, shi;
+    if (shadow_bins(G, D, w.xc, w.yc, slo, shi)) {
+      lo = max(lo, slo);
+      hi = min(hi, shi);
+    }
+  }
+  const int cnt = has && lo <= hi ? hi - lo + 1 : 0;
+  if (K == 0) {  // counting pass
+    const int m = __reduce_max_sync(0xffffffffu, cnt);
+    if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(kmax, m);
+    return;
+  }
+  if (!valid) return;
+  const size_t N = (size_t)D.nx * D.ny, vi = (size_t)iy * D.nx + ix;
+  if (cnt > K) {  // cannot happen after the counting pass; the host drops the table
+    atomicOr(kmax + 1, 1);
+    return;
+  }
+  const float rx = G.cos_phi * (-G.SO) - w.xc;
+  const float ry = G.sin_phi * (-G.SO) - w.yc;
+  float *ch = (float *)(tab + 2 * N) + vi;
+  float accl = 0.f;
+  for (int ka = 0; ka < cnt; ka++) {
+    const float l = chord_sel<AX>(__ldg(tabA + lo + ka), rx, ry, G.dz);
+    accl += l;
+    ch[(size_t)ka * N] = l;
+  }
+  tab[vi] = cnt ? (int)(((unsigned)cnt << 24) | (unsigned)(w.b0 * D.na + lo)) : 0;
+  tab[N + vi] = __float_as_int(accl);
+}
+
+// Counting (K == 0: the largest pair count into kmax[0]) or filling pass over
+// every view of the plan's first instance: grid (x tiles, y tiles, views).
+__global__ void __launch_bounds__(kAtxThreads)
+    k_atx_chords(const Inst *__restrict__ insts, int K, int *tabs, int *kmax) {
+  const Inst &I0 = insts[0];
+  const Dims D = I0.d;
+  const int view = blockIdx.z;
+  if (view >= I0.nv) return;
+  const ViewGeo G = view_of(I0, view);
+  const int vf = I0.vflags[view];
+  if ((vf & kViewAxisParallel) || G.z_det[0] != 0.0f) return;  // no table
+  int ix, iy, iz;
+  const bool valid = tile_voxel(D, ix, iy, iz);  // the whole warp goes on
+  const float4 *__restrict__ tabA = I0.tabA + (long long)view * D.na;
+  int *tab = tabs ? tabs + (size_t)view * chord_view_words(D, K) : nullptr;
+  if (!(vf & kViewNotX))
+    chords_voxel<1>(G, D, tabA, valid, ix, iy, K, tab, kmax);
+  else if (!(vf & kViewNotY))
+    chords_voxel<2>(G, D, tabA, valid, ix, iy, K, tab, kmax);
+  else
+    chords_voxel<0>(G, D, tabA, valid, ix, iy, K, tab, kmax);
+}
+
+// The voxel of this thread for the group, from the view's chord table: the
+// pairs, chords and accumulation order of atx_shared_voxel's narrow form,
+// and its update (atx_shared_apply).  Everything that does not depend on the
+// header -- the group's image values, the chord sum and the first
+// kChordPre chord slots -- is loaded together up front, so a warp waits for
+// DRAM once; the residuals it then reads are the view's few kB, in L1.
+// (A kernel of its own for this path, 48 registers and 5 blocks per SM with
+// the direct form out of line, measured 14 % slower: more long-scoreboard
+// stalls, fewer L1 hits.)
+constexpr int kChordPre = 4;
+
+__device__ __forceinline__ void atx_shared_voxel_tab(
+    const ViewGeo &G, const Dims &D, const float4 *__restrict__ corg,
+    const int *__restrict__ tab, int K, unsigned active, int gn, float *m_il,
+    const float *s_beta) {
+  int ix, iy, iz;
+  const bool valid = tile_voxel(D, ix, iy, iz);
+  const size_t N = (size_t)D.nx * D.ny;
+  const unsigned vi = valid ? (unsigned)iy * D.nx + ix : 0u;
+  const float *__restrict__ ch = (const float *)(tab + 2 * N) + vi;
   float4 *mg = (float4 *)m_il + (size_t)vi * (kShareGroup / 4);
+  int h = 0;
+  float accl = 0.f;
+  float pre[kChordPre];
+  float4 m4[kShareGroup / 4];
+#pragma unroll
+  for (int k = 0; k < kChordPre; k++) pre[k] = 0.f;
+  if (valid) {
+    h = __ldg(tab + vi);
+    accl = __int_as_float(__ldg(tab + N + vi));
+#pragma unroll
+    for (int k = 0; k < kChordPre; k++)
+      if (k < K) pre[k] = __ldg(ch + (size_t)k * N);  // slot k < K exists
+#pragma unroll
+    for (int q = 0; q < kShareGroup / 4; q++)
+      if ((active >> (4 * q)) & 0xFu) m4[q] = mg[q];
+  }
+  const int cnt = (int)((unsigned)h >> 24), first = h & 0xffffff;
+  const int kA = __reduce_max_sync(0xffffffffu, cnt);
+  float acc[kShareGroup];
+#pragma unroll
+  for (int b = 0; b < kShareGroup; b++) acc[b] = 0.f;
+  auto pair = [&](int ka, float l) {
+    const long long r = first + ka;
+#pragma unroll
+    for (int q = 0; q < kShareGroup / 4; q++) {
+      if (!((active >> (4 * q)) & 0xFu)) continue;
+      const float4 c4 = __ldg(corg + r * (kShareGroup / 4) + q);
+      acc[4 * q] += l * c4.x;
+      acc[4 * q + 1] += l * c4.y;
+      acc[4 * q + 2] += l * c4.z;
+      acc[4 * q + 3] += l * c4.w;
+    }
+  };
+#pragma unroll
+  for (int ka = 0; ka < kChordPre; ka++)
+    if (ka < kA && ka < cnt) pair(ka, pre[ka]);
+  for (int ka = kChordPre; ka < kA; ka++)
+    if (ka < cnt) pair(ka, __ldg(ch + (size_t)ka * N));
+  if (!valid) return;
+  // atx_shared_apply with the image values already loaded
+  const float scv = accl * G.scale;
 #pragma unroll
   for (int q = 0; q < kShareGroup / 4; q++) {
     if (!((active >> (4 * q)) & 0xFu)) continue;
-    float4 m4 = mg[q];
-    float *mv = &m4.x;
+    float *mv = &m4[q].x;
 #pragma unroll
     for (int j = 0; j < 4; j++) {
       const int b = 4 * q + j;
@@ -665,7 +841,7 @@ __device__ __forceinline__ void atx_shared_voxel(
         mv[j] = mn < 0.f ? 0.f : mn;
       }
     }
-    mg[q] = m4;
+    mg[q] = m4[q];
   }
 }
 
@@ -706,7 +882,10 @@ __global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 5)
   const int vf = I0.vflags[view];
   const bool planar_ok = !kPlanar || G.z_det[0] == 0.0f;
   const bool narrow = planar_ok && !(vf & kViewAxisParallel) && s_finite;
-  if (!(vf & (kViewAxisParallel | kViewNotX)))
+  if (kPlanar && narrow && I0.chtab)
+    atx_shared_voxel_tab(G, D, corg, I0.chtab + (size_t)view * chord_view_words(D, I0.chK),
+                         I0.chK, active, gn, I0.m_il, s_beta);
+  else if (!(vf & (kViewAxisParallel | kViewNotX)))
     atx_shared_voxel<kPlanar, 1>(G, D, corg, tabA, tabC, planar_ok, narrow, active,
                                  gn, I0.m_il, s_beta);
   else if (!(vf & (kViewAxisParallel | kViewNotY)))
@@ -1011,6 +1190,21 @@ cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,
   k_group_pack<<<grid, 256, 0, st>>>(insts, batch, unpack);
   return cudaGetLastError();
 }
+
+cudaError_t launch_atx_chords(const Inst *insts, const Dims &d, int nv, int K,
+                              int *tabs, int *kmax, cudaStream_t st) {
+  if (K < 0 || K > kChordMaxSlots || (K > 0 && !tabs) || d.nz != 1 || d.nb != 1)
+    return cudaErrorInvalidValue;
+  dim3 grid = tile_grid(d.nx, d.ny, 1, nv);
+  k_atx_chords<<<grid, kAtxThreads, 0, st>>>(insts, K, tabs, kmax);
+  return cudaGetLastError();
+}
+
+size_t atx_chord_words(const Dims &d, int nv, int K) {
+  return chord_view_words(d, K) * (size_t)nv;
+}
+
+int atx_chord_max_slots() { return kChordMaxSlots; }
 
 cudaError_t launch_view_tables(const Inst *insts, int batch, const Dims &d,
                                int nv, cudaStream_t st) {

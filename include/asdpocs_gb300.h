@@ -259,6 +259,18 @@ int asdpocs_plan_set_tv_walk(asdpocs_plan plan, int walk);
  * per sub-batch. */
 int asdpocs_plan_streams(asdpocs_plan plan);
 
+/* Chord slots per voxel of the plan's backward-step chord tables, 0 when it
+ * has none.  A plan of 2-D instances sharing geometry and view angles
+ * computes the chords of every (voxel, ray) pair of every view once, at
+ * creation, and its backward steps read them (2 + slots words per voxel and
+ * view, counted in asdpocs_plan_bytes; results are the same bits as without
+ * them).  Plans whose voxels have more than 32 pairs, or whose tables would
+ * exceed hbm_budget_bytes or the free memory, compute the chords in every
+ * step; so does every plan when ASDPOCS_NO_CHORD_TABLE is set at creation.
+ * Replaces nothing in the reference, whose Atx_cone_mf_gpu_new
+ * (Ax_cone_gpu.cu:299-331) recomputes the chords in every call. */
+int asdpocs_plan_chord_slots(asdpocs_plan plan);
+
 /* Profiling hook: average device time (ms, CUDA events on the plan's
  * stream) of `reps` back-to-back launches of one phase kernel for the whole
  * batch.  phase: 0 = SART forward step (Ax + residual), 1 = SART backward

@@ -403,3 +403,42 @@ def test_tv_walk_length_and_autotune_do_not_change_results(gpu, shape):
     for walk, img in out.items():
         assert np.array_equal(img, out[0]), walk
     assert np.array_equal(tuned, out[0])
+
+
+@pytest.mark.parametrize("n,na,det,vx,nv,span,table", [
+    (96, 160, 1.0, None, 24, 360.0, True),   # fan beam like the 512^2 protocol, scaled down
+    (40, 41, 1.0, None, 8, 360.0, True),     # odd na: the 90-degree views' central rays are axis-parallel
+    (50, 64, 1.0, None, 13, 200.0, True),    # nx not a multiple of the 32-voxel tiles
+    (24, 400, 0.01, 0.5, 6, 180.0, False),   # ~120 bins per voxel: more pairs than a table holds
+])
+def test_chord_tables_do_not_change_results(gpu, monkeypatch, n, na, det, vx, nv, span,
+                                            table):
+    """2-D shared-geometry plans read the backward step's chords from tables
+    built once per plan; every image equals the plan's without the tables, and
+    a residual that is not finite (a sinogram with inf) takes the direct form
+    in both."""
+    SO, OD = 541.0, 408.0
+    vx = vx or phantoms.fov_voxel_size(SO, OD, det, na, n)
+    phi = phantoms.views(nv, span)
+    para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, na=na, nb=1, detsize=det,
+                phi_vec=phi, maxnumIter=3, numOfgradients=3, alpha=0.02)
+    rng = np.random.default_rng(n + na)
+    B = 11
+    Ps = [rng.random(na * nv).astype(np.float32) for _ in range(B)]
+    Ps[4][7] = np.inf
+
+    def run():
+        with pkg.Plan([para] * B, [phi] * B) as pl:
+            for k, P in enumerate(Ps):
+                pl.set_sinogram(k, P)
+            pl.reset()
+            pl.run()
+            return [pl.image(k) for k in range(B)], pl.nbytes, pl.chord_slots
+
+    with_tab, bytes_tab, slots = run()
+    monkeypatch.setenv("ASDPOCS_NO_CHORD_TABLE", "1")
+    without, bytes_direct, slots_direct = run()
+    assert (slots > 0) == table and slots_direct == 0  # whether the tables were built
+    assert bytes_tab - bytes_direct == (2 + slots) * n * n * nv * 4 * (slots > 0)
+    for k in range(B):
+        assert np.array_equal(with_tab[k], without[k], equal_nan=True), k
