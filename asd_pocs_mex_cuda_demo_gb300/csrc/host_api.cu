@@ -227,6 +227,52 @@ __global__ void k_sum_f64(const double *__restrict__ partials, int n, double *ou
 }  // namespace
 }  // namespace asd
 
+namespace asd {
+
+cudaError_t build_chord_tables(const Inst *d_inst, const Dims &d, int nv,
+                               size_t max_bytes, cudaStream_t st, int **tab_out,
+                               int *K_out, size_t *bytes_out) {
+  *tab_out = nullptr;
+  *K_out = 0;
+  *bytes_out = 0;
+  if (d.nz != 1 || d.nb != 1 || (long long)d.na >= (1LL << 24) || nv > 65535)
+    return cudaSuccess;
+  int *kmax = nullptr;
+  if (cudaMalloc(&kmax, 2 * sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();  // out of memory is not sticky: go on without tables
+    return cudaSuccess;
+  }
+  int hk[2] = {0, 0};
+  cudaError_t e = cudaMemsetAsync(kmax, 0, sizeof(hk), st);
+  if (e == cudaSuccess) e = launch_atx_chords(d_inst, d, nv, 0, nullptr, kmax, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hk, kmax, sizeof(hk), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  const int K = hk[0];
+  const size_t bytes = atx_chord_words(d, nv, K) * sizeof(int);
+  int *tab = nullptr;
+  if (e == cudaSuccess && K > 0 && K <= atx_chord_max_slots() && bytes <= max_bytes &&
+      cudaMalloc(&tab, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    tab = nullptr;
+  }
+  if (tab) {
+    e = launch_atx_chords(d_inst, d, nv, K, tab, kmax, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hk, kmax, sizeof(hk), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess && hk[1] == 0) {
+      *tab_out = tab;
+      *K_out = K;
+      *bytes_out = bytes;
+      tab = nullptr;
+    }
+  }
+  if (tab) cudaFree(tab);
+  cudaFree(kmax);
+  return e;
+}
+
+}  // namespace asd
+
 extern "C" {
 
 int asdpocs_adjoint_check(const float *X, const float *yv, float cos_phi, float sin_phi,
@@ -742,57 +788,26 @@ static int plan_sub_first(asdpocs_plan p, int i) {
 
 extern "C" {
 
-// Backward-step chord tables of a 2-D shared-geometry plan (Inst::chtab): a
-// counting pass for the slots per voxel, then the filling pass.  A plan
-// without them (a voxel with more pairs than kChordMaxSlots, tables over the
-// plan's HBM budget, or no memory left) computes its chords in every step,
-// with the same results.
+
+// The plan's chord tables (see build_chord_tables), within its HBM budget;
+// every instance's descriptor points at them.
 static cudaError_t plan_chord_tables(asdpocs_plan p) {
-  const Dims &d = p->d;
-  if (d.nz != 1 || d.nb != 1 || (long long)d.na >= (1LL << 24) || p->nv > 65535)
-    return cudaSuccess;
-  int *kmax = nullptr;
-  if (cudaMalloc(&kmax, 2 * sizeof(int)) != cudaSuccess) {
-    cudaGetLastError();  // out of memory is not sticky: run without tables
-    return cudaSuccess;
+  size_t room = (size_t)-1;
+  if (p->budget) room = p->budget > p->bytes ? (size_t)(p->budget - p->bytes) : 0;
+  int *tab = nullptr, K = 0;
+  size_t bytes = 0;
+  cudaError_t e = build_chord_tables(p->d_inst, p->d, p->nv, room, p->st, &tab, &K, &bytes);
+  if (!tab) return e;
+  p->chtab = tab;  // freed with the plan
+  p->chK = K;
+  p->bytes += bytes;
+  for (Inst &I : p->h_inst) {
+    I.chtab = tab;
+    I.chK = K;
   }
-  int hk[2] = {0, 0};
-  cudaError_t e = cudaMemsetAsync(kmax, 0, sizeof(hk), p->st);
-  if (e == cudaSuccess) e = launch_atx_chords(p->d_inst, d, p->nv, 0, nullptr, kmax, p->st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(hk, kmax, sizeof(hk), cudaMemcpyDeviceToHost, p->st);
+  e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(), sizeof(Inst) * p->batch,
+                      cudaMemcpyHostToDevice, p->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
-  const int K = hk[0];
-  const size_t bytes = atx_chord_words(d, p->nv, K) * sizeof(int);
-  int *tab = nullptr;
-  if (e == cudaSuccess && K > 0 && K <= atx_chord_max_slots() &&
-      (!p->budget || p->bytes + bytes <= p->budget)) {
-    if (cudaMalloc(&tab, bytes) != cudaSuccess) {
-      cudaGetLastError();
-      tab = nullptr;
-    }
-  }
-  if (tab) {
-    e = launch_atx_chords(p->d_inst, d, p->nv, K, tab, kmax, p->st);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(hk, kmax, sizeof(hk), cudaMemcpyDeviceToHost, p->st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
-    if (e == cudaSuccess && hk[1] == 0) {
-      for (Inst &I : p->h_inst) {
-        I.chtab = tab;
-        I.chK = K;
-      }
-      e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(), sizeof(Inst) * p->batch,
-                          cudaMemcpyHostToDevice, p->st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
-      p->chtab = tab;  // freed with the plan
-      p->chK = K;
-      p->bytes += bytes;
-      tab = nullptr;
-    }
-  }
-  if (tab) cudaFree(tab);
-  cudaFree(kmax);
   return e;
 }
 

@@ -75,4 +75,16 @@ cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
                               int tv_walk = 0, bool finish = true);
 
+// Backward-step chord tables (Inst::chtab) of instances sharing 2-D geometry
+// and view angles, from d_inst[0], whose view tables are built: a counting
+// pass for the slots per voxel, then a filling pass, synchronous on `st`.
+// Leaves *tab_out null (and returns cudaSuccess) when the instances are not
+// 2-D, a voxel has more than 32 pairs, the tables would take more than
+// max_bytes, or the allocation fails; the caller then computes chords in
+// every step.  The caller frees *tab_out (cudaFree) and sets the
+// descriptors' chtab and chK.
+cudaError_t build_chord_tables(const Inst *d_inst, const Dims &d, int nv,
+                               size_t max_bytes, cudaStream_t st, int **tab_out,
+                               int *K_out, size_t *bytes_out);
+
 }  // namespace asd

@@ -20,6 +20,7 @@
 // the device.  Every kernel computes an instance at its own sizes and
 // reduces over its own blocks, so a job's result does not depend on the
 // jobs sharing its launches.
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -82,6 +83,8 @@ struct Lane {
   Scalars *d_dead = nullptr;       // scalars of an empty slot (done = 1)
   char *geo = nullptr;             // the protocol's geometry block
   size_t geo_bytes = 0;
+  int *chtab = nullptr;            // backward-step chord tables (2-D protocols)
+  size_t chtab_bytes = 0;
   Inst tmpl{};                     // geometry of every slot
   std::vector<Inst> slot_desc;     // descriptor of each slot (host copy)
   std::vector<Job *> slot_job;
@@ -152,6 +155,7 @@ struct asdpocs_server_s {
   cudaStream_t upload = nullptr; // admissions: allocation and data upload
   asd::PinnedPool pinned;        // the jobs' result blocks
   unsigned long long budget = 0, in_use = 0, peak = 0;
+  unsigned long long chord_bytes = 0;  // the lanes' chord tables
 };
 
 namespace asd {
@@ -220,6 +224,23 @@ bool lane_create(asdpocs_server sv, Lane &L) {
                           cudaMemcpyHostToDevice, L.st));
   // the protocol's ray tables and view flags, once, through slot 0
   SV_CUDA(launch_view_tables(L.d_inst, 1, inst_dims(L.g), L.g.nv, L.st));
+  // and a 2-D protocol's backward-step chord tables: every lane's together
+  // within a quarter of the budget (outside the jobs' share, like the
+  // geometry block); without them the lane computes chords in every step
+  const unsigned long long room =
+      sv->budget / 4 > sv->chord_bytes ? sv->budget / 4 - sv->chord_bytes : 0;
+  int K = 0;
+  if (!getenv("ASDPOCS_NO_CHORD_TABLE"))
+    SV_CUDA(build_chord_tables(L.d_inst, inst_dims(L.g), L.g.nv, (size_t)room, L.st,
+                               &L.chtab, &K, &L.chtab_bytes));
+  if (L.chtab) {
+    sv->chord_bytes += L.chtab_bytes;
+    L.tmpl.chtab = L.chtab;
+    L.tmpl.chK = K;
+    for (int s = 0; s < L.S; s++) L.slot_desc[s] = empty_slot(L, s);
+    SV_CUDA(cudaMemcpyAsync(L.d_inst, L.slot_desc.data(), sizeof(Inst) * L.S,
+                            cudaMemcpyHostToDevice, L.st));
+  }
   L.slot_job.assign(L.S, nullptr);
   return true;
 }
@@ -240,6 +261,7 @@ void lane_destroy(Lane &L) {
   cudaFree(L.d_flags);
   cudaFree(L.d_dead);
   cudaFree(L.geo);
+  if (L.chtab) cudaFree(L.chtab);
   if (L.st) cudaStreamDestroy(L.st);
 }
 
