@@ -335,7 +335,9 @@ int asdpocs_poisson_noise_device(const float *p_d, float *out_d, long long n,
  * A lane also holds its protocol's geometry tables and its slots'
  * interleaved images (4 bytes per voxel and slot; a lane gets as many slots,
  * in groups of 8, as fit in an eighth of the budget, at least 8) until the
- * server is destroyed.  All calls are thread-safe.
+ * server is destroyed; a 2-D lane also holds its protocol's backward-step
+ * chord tables (see asdpocs_plan_chord_slots), every lane's together within
+ * a quarter of the budget.  All calls are thread-safe.
  * --------------------------------------------------------------------- */
 typedef struct asdpocs_server_s *asdpocs_server;
 
