@@ -265,7 +265,8 @@ class Plan:
     @property
     def chord_slots(self) -> int:
         """Chord slots per voxel of the backward step's chord tables (2-D
-        shared-geometry plans), 0 when the plan computes chords every step."""
+        plans of one instance or of instances sharing geometry), 0 when the
+        plan computes chords every step."""
         return int(load().asdpocs_plan_chord_slots(self._h))
 
     def set_tv_walk(self, walk: int):

@@ -95,8 +95,9 @@ struct Inst {
   int *vflags;               // per view: kViewAxisParallel | kViewNotX | kViewNotY
   float4 *tabC;              // 3D ray slopes of the current view, na*nb
   int tabc_mode;             // who writes tabC in the forward step (kTabc*)
-  const int *chtab;          // 2-D shared-geometry plans: the backward step's
-                             //   chords of every view (k_atx_chords), or nullptr
+  const int *chtab;          // 2-D plans of one instance or sharing geometry:
+                             //   the backward step's chords of every view
+                             //   (k_atx_chords), or nullptr
   int chK;                   //   chord slots per voxel and view in chtab
   double *rmse;              // [maxIter]
   double *partials;          // reduction partials [blocks * kMaxReduceK]

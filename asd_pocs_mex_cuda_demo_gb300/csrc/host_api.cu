@@ -789,8 +789,9 @@ static int plan_sub_first(asdpocs_plan p, int i) {
 extern "C" {
 
 
-// The plan's chord tables (see build_chord_tables), within its HBM budget;
-// every instance's descriptor points at them.
+// The chord tables of a plan of one instance or of instances sharing
+// geometry (see build_chord_tables), within its HBM budget; every instance's
+// descriptor points at them.
 static cudaError_t plan_chord_tables(asdpocs_plan p) {
   size_t room = (size_t)-1;
   if (p->budget) room = p->budget > p->bytes ? (size_t)(p->budget - p->bytes) : 0;
@@ -942,7 +943,7 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
                                             cudaMemcpyHostToDevice, p->st);
   if (e == cudaSuccess) e = launch_view_tables(p->d_inst, batch, p->d, p->nv, p->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
-  if (e == cudaSuccess && p->shared && !getenv("ASDPOCS_NO_CHORD_TABLE"))
+  if (e == cudaSuccess && (p->shared || batch == 1) && !getenv("ASDPOCS_NO_CHORD_TABLE"))
     e = plan_chord_tables(p);
   if (e != cudaSuccess) {
     asdpocs_plan_destroy(p);

@@ -390,6 +390,78 @@ __device__ __forceinline__ float chord_sel(const float4 A, float rx, float ry,
 }
 
 // Backward step over this block's tile group (see k_sart_atx).
+// ---------------------------------------------------------------------------
+// Chord tables of 2-D plans (one instance, or instances sharing geometry and
+// view angles).  The chords of the backward step depend on the geometry and
+// the view only, so such a plan computes every view's chords once
+// (k_atx_chords) and its backward steps read them instead of repeating the
+// window, shadow and face tests of find_l for every group and iteration.  Per view the table holds, for voxel
+// vi = iy * nx + ix of the N = nx * ny voxels:
+//   hdr[vi]          (count << 24) | first ray, 0 for no pair
+//   sum[vi]          the voxel's chord sum (float bits)
+//   ch[k * N + vi]   chord of pair k < count (ray first + k)
+// in that order, (2 + chK) * N words per view.  The pairs, their chords and
+// the chord sum are those of the narrow form of the backward steps
+// (sart_atx_tiles, atx_shared_voxel), in the same order and from the same
+// functions, so they give the same bits with or without the table.  Views with an axis-parallel ray have no
+// table (their pairs need the full window); the step also keeps the direct
+// form when a residual is not finite (0 * inf is not 0).
+// ---------------------------------------------------------------------------
+constexpr int kChordMaxSlots = 32;
+// chord slots a thread loads with the table header, before it knows its count
+constexpr int kChordPre = 4;
+
+__host__ __device__ __forceinline__ size_t chord_view_words(const Dims &d, int K) {
+  return (size_t)(2 + K) * (size_t)d.nx * (size_t)d.ny;
+}
+
+// Backward step over this block's tile group from the view's chord table
+// (2-D, narrow form; see sart_atx_tiles): the image value, header, chord sum
+// and first kChordPre chords of a voxel are loaded together, then its
+// residuals (L1) in the pairs' order.
+__device__ __forceinline__ void sart_atx_tiles_tab(const Inst &I, const ViewGeo &G,
+                                                   const Dims &D, const int *__restrict__ tab,
+                                                   int K) {
+  const float beta = I.s->beta_f;
+  float *m = I.m;
+  const float *__restrict__ cor = I.cor;
+  const size_t N = (size_t)D.nx * D.ny;
+  for (int t = 0; t < kTilesPerBlock; t++) {
+    int x0, y0, iz;
+    if (!group_tile(D.ny, D.nz, t, x0, y0, iz)) break;
+    const int ix = x0 + threadIdx.x % kTileX, iy = y0 + threadIdx.x / kTileX;
+    const bool valid = ix < D.nx && iy < D.ny;
+    const unsigned vi = valid ? (unsigned)iy * D.nx + ix : 0u;
+    const float *__restrict__ ch = (const float *)(tab + 2 * N) + vi;
+    int h = 0;
+    float accl = 0.f, mv = 0.f;
+    float pre[kChordPre];
+#pragma unroll
+    for (int k = 0; k < kChordPre; k++) pre[k] = 0.f;
+    if (valid) {
+      h = __ldg(tab + vi);
+      accl = __int_as_float(__ldg(tab + N + vi));
+#pragma unroll
+      for (int k = 0; k < kChordPre; k++)
+        if (k < K) pre[k] = __ldg(ch + (size_t)k * N);  // slot k < K exists
+      mv = m[vi];
+    }
+    const int cnt = (int)((unsigned)h >> 24), first = h & 0xffffff;
+    const int kA = __reduce_max_sync(0xffffffffu, cnt);
+    float acc = 0.f;
+#pragma unroll
+    for (int ka = 0; ka < kChordPre; ka++)
+      if (ka < kA && ka < cnt) acc += pre[ka] * __ldg(cor + first + ka);
+    for (int ka = kChordPre; ka < kA; ka++)
+      if (ka < cnt) acc += __ldg(ch + (size_t)ka * N) * __ldg(cor + first + ka);
+    if (valid) {
+      const float bp = acc * G.scale, scv = accl * G.scale;
+      const float mn = mv + beta * __fdividef(bp, scv == 0.f ? 1.f : scv);
+      m[vi] = mn < 0.f ? 0.f : mn;
+    }
+  }
+}
+
 template <bool kPlanar, int AX>
 __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
                                                const Dims &D,
@@ -512,7 +584,9 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
   const int vf = I.vflags[view];
   const bool narrow = !(vf & kViewAxisParallel) && I.s->cor_finite &&
                       (!kPlanar || G.z_det[0] == 0.0f);
-  if (!(vf & (kViewAxisParallel | kViewNotX)))
+  if (kPlanar && narrow && I.chtab)
+    sart_atx_tiles_tab(I, G, D, I.chtab + (size_t)view * chord_view_words(D, I.chK), I.chK);
+  else if (!(vf & (kViewAxisParallel | kViewNotX)))
     sart_atx_tiles<kPlanar, 1>(I, G, D, tabA, narrow);
   else if (!(vf & (kViewAxisParallel | kViewNotY)))
     sart_atx_tiles<kPlanar, 2>(I, G, D, tabA, narrow);
@@ -679,29 +753,6 @@ __device__ __forceinline__ void atx_shared_voxel(
                    m_il, s_beta);
 }
 
-// ---------------------------------------------------------------------------
-// Chord tables of 2-D shared-geometry plans.  The chords of the backward step
-// depend on the geometry and the view only, so a plan whose instances share
-// them computes every view's chords once (k_atx_chords) and its backward
-// steps read them instead of repeating the window, shadow and face tests of
-// find_l for every group and iteration.  Per view the table holds, for voxel
-// vi = iy * nx + ix of the N = nx * ny voxels:
-//   hdr[vi]          (count << 24) | first ray, 0 for no pair
-//   sum[vi]          the voxel's chord sum (float bits)
-//   ch[k * N + vi]   chord of pair k < count (ray first + k)
-// in that order, (2 + chK) * N words per view.  The pairs, their chords and
-// the chord sum are those of the narrow form of atx_shared_voxel, in the same
-// order and from the same functions, so the backward step gives the same
-// bits with or without the table.  Views with an axis-parallel ray have no
-// table (their pairs need the full window); the step also keeps the direct
-// form when a residual is not finite (0 * inf is not 0).
-// ---------------------------------------------------------------------------
-constexpr int kChordMaxSlots = 32;
-
-__host__ __device__ __forceinline__ size_t chord_view_words(const Dims &d, int K) {
-  return (size_t)(2 + K) * (size_t)d.nx * (size_t)d.ny;
-}
-
 // Pairs of this voxel: the reference's window narrowed to the voxel's shadow.
 template <int AX>
 __device__ __forceinline__ void chords_voxel(const ViewGeo &G, const Dims &D,
@@ -775,7 +826,6 @@ __global__ void __launch_bounds__(kAtxThreads)
 // (A kernel of its own for this path, 48 registers and 5 blocks per SM with
 // the direct form out of line, measured 14 % slower: more long-scoreboard
 // stalls, fewer L1 hits.)
-constexpr int kChordPre = 4;
 
 __device__ __forceinline__ void atx_shared_voxel_tab(
     const ViewGeo &G, const Dims &D, const float4 *__restrict__ corg,

@@ -413,10 +413,10 @@ def test_tv_walk_length_and_autotune_do_not_change_results(gpu, shape):
 ])
 def test_chord_tables_do_not_change_results(gpu, monkeypatch, n, na, det, vx, nv, span,
                                             table):
-    """2-D shared-geometry plans read the backward step's chords from tables
-    built once per plan; every image equals the plan's without the tables, and
-    a residual that is not finite (a sinogram with inf) takes the direct form
-    in both."""
+    """2-D plans of one instance or of instances sharing geometry read the
+    backward step's chords from tables built once per plan; every image
+    equals the plan's without the tables, and a residual that is not finite
+    (a sinogram with inf) takes the direct form in both."""
     SO, OD = 541.0, 408.0
     vx = vx or phantoms.fov_voxel_size(SO, OD, det, na, n)
     phi = phantoms.views(nv, span)
@@ -427,18 +427,22 @@ def test_chord_tables_do_not_change_results(gpu, monkeypatch, n, na, det, vx, nv
     Ps = [rng.random(na * nv).astype(np.float32) for _ in range(B)]
     Ps[4][7] = np.inf
 
-    def run():
-        with pkg.Plan([para] * B, [phi] * B) as pl:
-            for k, P in enumerate(Ps):
-                pl.set_sinogram(k, P)
+    def run(b):  # b instances (1: the per-instance kernels)
+        with pkg.Plan([para] * b, [phi] * b) as pl:
+            for k in range(b):
+                pl.set_sinogram(k, Ps[k])
             pl.reset()
             pl.run()
-            return [pl.image(k) for k in range(B)], pl.nbytes, pl.chord_slots
+            return [pl.image(k) for k in range(b)], pl.nbytes, pl.chord_slots
 
-    with_tab, bytes_tab, slots = run()
+    with_tab, bytes_tab, slots = run(B)
+    alone_tab, _, slots1 = run(1)
     monkeypatch.setenv("ASDPOCS_NO_CHORD_TABLE", "1")
-    without, bytes_direct, slots_direct = run()
+    without, bytes_direct, slots_direct = run(B)
+    alone, _, _ = run(1)
     assert (slots > 0) == table and slots_direct == 0  # whether the tables were built
+    assert slots1 == slots
     assert bytes_tab - bytes_direct == (2 + slots) * n * n * nv * 4 * (slots > 0)
     for k in range(B):
         assert np.array_equal(with_tab[k], without[k], equal_nan=True), k
+    assert np.array_equal(alone_tab[0], alone[0]) and np.array_equal(alone[0], without[0])
