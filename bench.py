@@ -536,8 +536,8 @@ def main():
                        "plan": {"create_ms": plan_ms, "chord_slots": slots,
                                 "chord_table_mb": chord_mb,
                                 "note": "created once per scan protocol, outside the timed "
-                                        "region (view tables and, for 2-D shared geometry, "
-                                        "the backward step's chord tables)"},
+                                        "region (view tables and, for 2-D plans, the "
+                                        "backward step's chord tables)"},
                        "tv_walk": {"autotuned": tv_walk, "ms_per_step": tv_walk_ms,
                                    "note": "bands (2-D) or slabs (3-D) of 16 per walk; "
                                            "0 = the batch-size rule"}},
