@@ -562,7 +562,9 @@ struct asdpocs_plan_s {
   std::vector<asd::SubBatch> subs;
   cudaEvent_t fork = nullptr;  // orders the sub-batches after the plan's stream
   int *chtab = nullptr;        // backward-step chord tables (2-D shared plans)
-  int chK = 0;                 // their slots per voxel and view
+  int chK = 0;                 // their slots per voxel and view (the largest
+                               // over the instances' own tables)
+  std::vector<int *> inst_tabs;  // instances' own tables (2-D, geometry apart)
   unsigned long long budget = 0;  // HBM budget of the plan (0: none)
 };
 
@@ -812,6 +814,41 @@ static cudaError_t plan_chord_tables(asdpocs_plan p) {
   return e;
 }
 
+// Instances of different 2-D geometry: a table per instance, in instance
+// order, until the tables reach half the free device memory or the plan's
+// HBM budget; the instances left without one compute their chords in every
+// step.
+static cudaError_t plan_instance_chord_tables(asdpocs_plan p) {
+  size_t free_b = 0, total_b = 0;
+  cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+  if (e != cudaSuccess) return e;
+  size_t room = free_b / 2;
+  if (p->budget)
+    room = std::min(room, p->budget > p->bytes ? (size_t)(p->budget - p->bytes) : (size_t)0);
+  bool any = false;
+  for (int i = 0; i < p->batch && e == cudaSuccess; i++) {
+    const asdpocs_geometry &g = p->geom[i];
+    int *tab = nullptr, K = 0;
+    size_t bytes = 0;
+    e = build_chord_tables(p->d_inst + i, Dims{g.nx, g.ny, g.nz, g.na, g.nb}, g.nv, room,
+                           p->st, &tab, &K, &bytes);
+    if (!tab) continue;
+    p->inst_tabs.push_back(tab);  // freed with the plan
+    p->chK = std::max(p->chK, K);
+    p->bytes += bytes;
+    room -= bytes;
+    p->h_inst[i].chtab = tab;
+    p->h_inst[i].chK = K;
+    any = true;
+  }
+  if (e == cudaSuccess && any) {
+    e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(), sizeof(Inst) * p->batch,
+                        cudaMemcpyHostToDevice, p->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  }
+  return e;
+}
+
 int asdpocs_plan_create(asdpocs_plan *out, int batch,
                         const asdpocs_geometry *geom,
                         const double *phi_vec_deg, const asdpocs_options *opt,
@@ -943,8 +980,8 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
                                             cudaMemcpyHostToDevice, p->st);
   if (e == cudaSuccess) e = launch_view_tables(p->d_inst, batch, p->d, p->nv, p->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
-  if (e == cudaSuccess && (p->shared || batch == 1) && !getenv("ASDPOCS_NO_CHORD_TABLE"))
-    e = plan_chord_tables(p);
+  if (e == cudaSuccess && !getenv("ASDPOCS_NO_CHORD_TABLE"))
+    e = p->shared || batch == 1 ? plan_chord_tables(p) : plan_instance_chord_tables(p);
   if (e != cudaSuccess) {
     asdpocs_plan_destroy(p);
     return cuda_status(e, "plan setup");
@@ -968,6 +1005,7 @@ int asdpocs_plan_destroy(asdpocs_plan p) {
   if (p->st) cudaStreamSynchronize(p->st);
   if (p->arena) cudaFree(p->arena);
   if (p->chtab) cudaFree(p->chtab);
+  for (int *t : p->inst_tabs) cudaFree(t);
   if (p->own_stream && p->st) cudaStreamDestroy(p->st);
   delete p;
   return 0;

@@ -259,10 +259,11 @@ int asdpocs_plan_set_tv_walk(asdpocs_plan plan, int walk);
  * per sub-batch. */
 int asdpocs_plan_streams(asdpocs_plan plan);
 
-/* Chord slots per voxel of the plan's backward-step chord tables, 0 when it
- * has none.  A plan of one 2-D instance, or of 2-D instances sharing
- * geometry and view angles, computes the chords of every (voxel, ray) pair
- * of every view once, at
+/* Chord slots per voxel of the plan's backward-step chord tables (the
+ * largest over its instances' tables), 0 when it has none.  A plan of 2-D
+ * instances computes the chords of every (voxel, ray) pair of every view
+ * once -- one table for instances sharing geometry and view angles, else one
+ * per instance while the tables stay within half the free memory -- at
  * creation, and its backward steps read them (2 + slots words per voxel and
  * view, counted in asdpocs_plan_bytes; results are the same bits as without
  * them).  Plans whose voxels have more than 32 pairs, or whose tables would

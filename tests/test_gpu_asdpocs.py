@@ -446,3 +446,29 @@ def test_chord_tables_do_not_change_results(gpu, monkeypatch, n, na, det, vx, nv
     for k in range(B):
         assert np.array_equal(with_tab[k], without[k], equal_nan=True), k
     assert np.array_equal(alone_tab[0], alone[0]) and np.array_equal(alone[0], without[0])
+
+
+def test_chord_tables_per_instance_in_uneven_plans(gpu, monkeypatch):
+    """A plan of 2-D instances with different sizes, bins and views builds a
+    chord table per instance; every image equals the plan's without them."""
+    shapes = [(40, 60, 9), (33, 50, 7), (64, 96, 12)]
+    paras, Ps = [], []
+    for s, (n, na, nv) in enumerate(shapes):
+        x, P, para = _uneven(70 + s, n, na, nv, 3, 3)
+        paras.append(para)
+        Ps.append(P)
+
+    def run():
+        with pkg.Plan(paras, [p["phi_vec"] for p in paras]) as pl:
+            for k, P in enumerate(Ps):
+                pl.set_sinogram(k, P.ravel(order="F"))
+            pl.reset()
+            pl.run()
+            return [pl.image(k) for k in range(len(Ps))], pl.chord_slots
+
+    with_tab, slots = run()
+    monkeypatch.setenv("ASDPOCS_NO_CHORD_TABLE", "1")
+    without, slots_direct = run()
+    assert slots > 0 and slots_direct == 0
+    for k in range(len(Ps)):
+        assert np.array_equal(with_tab[k], without[k]), k
