@@ -791,12 +791,23 @@ static int plan_sub_first(asdpocs_plan p, int i) {
 extern "C" {
 
 
+// Device bytes the plan's chord tables may take: half the free memory, and
+// what is left of the plan's HBM budget.
+static cudaError_t plan_chord_room(asdpocs_plan p, size_t &room) {
+  size_t free_b = 0, total_b = 0;
+  const cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+  room = free_b / 2;
+  if (p->budget)
+    room = std::min(room, p->budget > p->bytes ? (size_t)(p->budget - p->bytes) : (size_t)0);
+  return e;
+}
+
 // The chord tables of a plan of one instance or of instances sharing
-// geometry (see build_chord_tables), within its HBM budget; every instance's
-// descriptor points at them.
+// geometry (see build_chord_tables); every instance's descriptor points at
+// them.
 static cudaError_t plan_chord_tables(asdpocs_plan p) {
-  size_t room = (size_t)-1;
-  if (p->budget) room = p->budget > p->bytes ? (size_t)(p->budget - p->bytes) : 0;
+  size_t room = 0;
+  if (cudaError_t e0 = plan_chord_room(p, room)) return e0;
   int *tab = nullptr, K = 0;
   size_t bytes = 0;
   cudaError_t e = build_chord_tables(p->d_inst, p->d, p->nv, room, p->st, &tab, &K, &bytes);
@@ -815,16 +826,12 @@ static cudaError_t plan_chord_tables(asdpocs_plan p) {
 }
 
 // Instances of different 2-D geometry: a table per instance, in instance
-// order, until the tables reach half the free device memory or the plan's
-// HBM budget; the instances left without one compute their chords in every
-// step.
+// order, while they fit (plan_chord_room); the instances left without one
+// compute their chords in every step.
 static cudaError_t plan_instance_chord_tables(asdpocs_plan p) {
-  size_t free_b = 0, total_b = 0;
-  cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+  size_t room = 0;
+  cudaError_t e = plan_chord_room(p, room);
   if (e != cudaSuccess) return e;
-  size_t room = free_b / 2;
-  if (p->budget)
-    room = std::min(room, p->budget > p->bytes ? (size_t)(p->budget - p->bytes) : (size_t)0);
   bool any = false;
   for (int i = 0; i < p->batch && e == cudaSuccess; i++) {
     const asdpocs_geometry &g = p->geom[i];

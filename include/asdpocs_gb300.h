@@ -263,12 +263,13 @@ int asdpocs_plan_streams(asdpocs_plan plan);
  * largest over its instances' tables), 0 when it has none.  A plan of 2-D
  * instances computes the chords of every (voxel, ray) pair of every view
  * once -- one table for instances sharing geometry and view angles, else one
- * per instance while the tables stay within half the free memory -- at
- * creation, and its backward steps read them (2 + slots words per voxel and
- * view, counted in asdpocs_plan_bytes; results are the same bits as without
- * them).  Plans whose voxels have more than 32 pairs, or whose tables would
- * exceed hbm_budget_bytes or the free memory, compute the chords in every
- * step; so does every plan when ASDPOCS_NO_CHORD_TABLE is set at creation.
+ * per instance -- at creation, and its backward steps read them (2 + slots
+ * words per voxel and view, counted in asdpocs_plan_bytes; results are the
+ * same bits as without them).  The tables stay within half the free device
+ * memory and what is left of hbm_budget_bytes; instances whose tables do not
+ * fit, or whose voxels have more than 32 pairs, compute the chords in every
+ * step, and so does every plan when ASDPOCS_NO_CHORD_TABLE is set at
+ * creation.
  * Replaces nothing in the reference, whose Atx_cone_mf_gpu_new
  * (Ax_cone_gpu.cu:299-331) recomputes the chords in every call. */
 int asdpocs_plan_chord_slots(asdpocs_plan plan);
