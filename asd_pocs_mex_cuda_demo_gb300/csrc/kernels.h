@@ -76,8 +76,9 @@ cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
 cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,
                               int unpack, cudaStream_t st);
 
-// Backward-step chord tables of a 2-D shared-geometry plan (Inst::chtab),
-// from the plan's first instance, whose view tables must be built.  K == 0
+// Backward-step chord tables (Inst::chtab) of the 2-D instance insts[0]
+// (and of the instances sharing its geometry), whose view tables must be
+// built.  K == 0
 // counts: the largest number of pairs of a voxel goes to kmax[0] (zeroed
 // first).  K > 0 fills `tabs` (atx_chord_words(d, nv, K) ints) and sets
 // kmax[1] if a voxel has more than K pairs.

@@ -391,21 +391,23 @@ __device__ __forceinline__ float chord_sel(const float4 A, float rx, float ry,
 
 // Backward step over this block's tile group (see k_sart_atx).
 // ---------------------------------------------------------------------------
-// Chord tables of 2-D plans (one instance, or instances sharing geometry and
-// view angles).  The chords of the backward step depend on the geometry and
-// the view only, so such a plan computes every view's chords once
-// (k_atx_chords) and its backward steps read them instead of repeating the
-// window, shadow and face tests of find_l for every group and iteration.  Per view the table holds, for voxel
-// vi = iy * nx + ix of the N = nx * ny voxels:
+// Chord tables of 2-D plans.  The chords of the backward step depend on the
+// geometry and the view only, so a plan computes every view's chords once
+// (k_atx_chords; one table for instances sharing geometry and view angles,
+// else one per instance) and its backward steps read them instead of
+// repeating the window, shadow and face tests of find_l for every group and
+// iteration.  Per view the table holds, for voxel vi = iy * nx + ix of the
+// N = nx * ny voxels:
 //   hdr[vi]          (count << 24) | first ray, 0 for no pair
 //   sum[vi]          the voxel's chord sum (float bits)
 //   ch[k * N + vi]   chord of pair k < count (ray first + k)
 // in that order, (2 + chK) * N words per view.  The pairs, their chords and
 // the chord sum are those of the narrow form of the backward steps
 // (sart_atx_tiles, atx_shared_voxel), in the same order and from the same
-// functions, so they give the same bits with or without the table.  Views with an axis-parallel ray have no
-// table (their pairs need the full window); the step also keeps the direct
-// form when a residual is not finite (0 * inf is not 0).
+// functions, so they give the same bits with or without the table.  Views
+// with an axis-parallel ray have no table (their pairs need the full
+// window); the steps also keep the direct form when a residual is not
+// finite (0 * inf is not 0).
 // ---------------------------------------------------------------------------
 constexpr int kChordMaxSlots = 32;
 // chord slots a thread loads with the table header, before it knows its count
@@ -795,7 +797,8 @@ __device__ __forceinline__ void chords_voxel(const ViewGeo &G, const Dims &D,
 }
 
 // Counting (K == 0: the largest pair count into kmax[0]) or filling pass over
-// every view of the plan's first instance: grid (x tiles, y tiles, views).
+// every view of the instance insts[0] (the first of instances sharing
+// geometry, or one instance): grid (x tiles, y tiles, views).
 __global__ void __launch_bounds__(kAtxThreads)
     k_atx_chords(const Inst *__restrict__ insts, int K, int *tabs, int *kmax) {
   const Inst &I0 = insts[0];
