@@ -154,3 +154,117 @@ extern "C" void dm_atx(float *x, const float *yv, float *sc, float c, float s,
         sc[idx] = accl * scale;
       }
 }
+
+// Chord tables of the 2-D backward step, as k_atx_chords lays them out for
+// one view -- header (count << 24 | first ray), chord sum, then K slot
+// planes of N chords -- from the same window, shadow and chord functions,
+// the chord function picked per view (every ray x-dominant, every ray
+// y-dominant, or the general form) as the kernels pick it.  dm_chord_count
+// returns the view's largest pair count, 0 when the view has an
+// axis-parallel ray (no table); dm_atx_table builds the table with K slots
+// and replays it the way the backward steps read it (pairs of a voxel in
+// slot order), giving Atx and its chord sums; it returns 0, or -1 when a
+// voxel has more than K pairs.
+namespace {
+struct PlanarView {
+  ViewGeo G;
+  Dims D;
+  std::vector<float4> tA;
+  int ax = -1;  // 1: x-dominant rays, 2: y-dominant, 0: mixed; -1: no table
+};
+
+PlanarView planar_view(float c, float s, const float *yd, const float *zd, float SO,
+                       float OD, float scale, float ddy, int nx, int ny, int na) {
+  PlanarView v{geo(c, s, yd, zd, SO, OD, scale, ddy, ddy, 1.0f), Dims{nx, ny, 1, na, 1},
+               std::vector<float4>(na), -1};
+  bool par = false, allx = true, ally = true;
+  for (int ia = 0; ia < na; ia++) {
+    const float4 A = ray_tab_a(v.G, yd[ia]);
+    v.tA[ia] = A;
+    par = par || A.x == 0.0f || A.y == 0.0f;
+    const bool xf = fabsf(A.x) > fabsf(A.y);
+    allx = allx && xf;
+    ally = ally && !xf;
+  }
+  if (!par && zd[0] == 0.0f) v.ax = allx ? 1 : (ally ? 2 : 0);
+  return v;
+}
+
+// The pairs of voxel (ix, iy): first ray and count, as chords_voxel finds them.
+void voxel_pairs(const PlanarView &v, int ix, int iy, int &first, int &cnt, float &rx,
+                 float &ry) {
+  const VoxelWin w = voxel_window(v.G, v.D, ix, iy, 0);
+  const bool has = w.a0 <= w.a1 && w.b0 <= w.b1;
+  int lo = has ? w.a0 : 0, hi = has ? w.a1 : -1;
+  if (has) {
+    int slo, shi;
+    if (shadow_bins(v.G, v.D, w.xc, w.yc, slo, shi)) {
+      lo = lo > slo ? lo : slo;
+      hi = hi < shi ? hi : shi;
+    }
+  }
+  cnt = has && lo <= hi ? hi - lo + 1 : 0;
+  first = has ? w.b0 * v.D.na + lo : 0;
+  rx = v.G.cos_phi * (-v.G.SO) - w.xc;
+  ry = v.G.sin_phi * (-v.G.SO) - w.yc;
+}
+
+float view_chord(const PlanarView &v, int ia, float rx, float ry) {
+  const float4 A = v.tA[ia];
+  if (v.ax == 1) return chord_planar_axis<true>(A, rx, ry);
+  if (v.ax == 2) return chord_planar_axis<false>(A, rx, ry);
+  return chord_planar_bf(A, rx, ry, v.G.dz);
+}
+}  // namespace
+
+extern "C" int dm_chord_count(float c, float s, const float *yd, float SO, float OD,
+                              float ddy, int nx, int ny, int na) {
+  const float zd0 = 0.0f;
+  const PlanarView v = planar_view(c, s, yd, &zd0, SO, OD, 1.0f, ddy, nx, ny, na);
+  if (v.ax < 0) return 0;
+  int K = 0;
+  for (int iy = 0; iy < ny; iy++)
+    for (int ix = 0; ix < nx; ix++) {
+      int first, cnt;
+      float rx, ry;
+      voxel_pairs(v, ix, iy, first, cnt, rx, ry);
+      K = cnt > K ? cnt : K;
+    }
+  return K;
+}
+
+extern "C" int dm_atx_table(float *x, const float *yv, float *sc, float c, float s,
+                            const float *yd, float SO, float OD, float scale, float ddy,
+                            int nx, int ny, int na, int K) {
+  const float zd0 = 0.0f;
+  const PlanarView v = planar_view(c, s, yd, &zd0, SO, OD, scale, ddy, nx, ny, na);
+  const size_t N = (size_t)nx * ny;
+  std::vector<int> tab((size_t)(2 + K) * N, 0);
+  float *ch = (float *)(tab.data() + 2 * N);
+  for (int iy = 0; iy < ny; iy++)  // the filling pass
+    for (int ix = 0; ix < nx; ix++) {
+      const size_t vi = (size_t)iy * nx + ix;
+      int first, cnt;
+      float rx, ry;
+      voxel_pairs(v, ix, iy, first, cnt, rx, ry);
+      if (cnt > K) return -1;
+      float accl = 0.f;
+      for (int k = 0; k < cnt; k++) {
+        const float l = view_chord(v, first + k, rx, ry);
+        accl += l;
+        ch[(size_t)k * N + vi] = l;
+      }
+      tab[vi] = cnt ? (int)(((unsigned)cnt << 24) | (unsigned)first) : 0;
+      memcpy(&tab[N + vi], &accl, 4);
+    }
+  for (size_t vi = 0; vi < N; vi++) {  // the backward step's reading
+    const int h = tab[vi];
+    const int cnt = (int)((unsigned)h >> 24), first = h & 0xffffff;
+    float acc = 0.f, accl;
+    memcpy(&accl, &tab[N + vi], 4);
+    for (int k = 0; k < cnt; k++) acc += ch[(size_t)k * N + vi] * yv[first + k];
+    x[vi] = acc * scale;
+    sc[vi] = accl * scale;
+  }
+  return 0;
+}

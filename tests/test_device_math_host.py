@@ -3,7 +3,8 @@ against the oracle -- checks the float logic of the GPU code without a GPU.
 
 * Atx through the staged ray tables is bit-identical to the oracle (and so
   to the reference), planar and 3D, over the reference's whole footprint
-  window and over each voxel's shadow only (the kernels' narrowing).
+  window and over each voxel's shadow only (the kernels' narrowing); so is
+  2-D Atx read back from a chord table in the layout of the plans' tables.
 * Ax with one partial sum per ray and the reference's weight expressions is
   bit-identical; with the 32-lane split and xor-butterfly combination of the
   warp kernels, and their division-free weights, it stays within 1e-6.
@@ -39,6 +40,12 @@ def dm():
     L.dm_atx.argtypes = [F, F, F, C.c_float, C.c_float, F, F, C.c_float, C.c_float,
                          C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
                          C.c_int, C.c_int, C.c_int, C.c_int]
+    L.dm_chord_count.argtypes = [C.c_float, C.c_float, F, C.c_float, C.c_float, C.c_float,
+                                 C.c_int, C.c_int, C.c_int]
+    L.dm_chord_count.restype = C.c_int
+    L.dm_atx_table.argtypes = [F, F, F, C.c_float, C.c_float, F, C.c_float, C.c_float,
+                               C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.dm_atx_table.restype = C.c_int
     return L
 
 
@@ -114,3 +121,51 @@ def test_narrowing_off_grid_detector(dm, oracle_mod, dims):
                   g["SO"], g["OD"], g["scale"], g["det"], g["det"], 1.0, nx, ny, nz, na, nb,
                   2)
         assert np.array_equal(b, bo) and np.array_equal(sc, co), a
+
+
+@pytest.mark.parametrize("dims", [(64, 64, 128), (17, 23, 41), (50, 31, 77)])
+def test_chord_table_layout_matches_oracle(dm, oracle_mod, dims):
+    """The 2-D chord table (header, chord sum, slot planes), filled from each
+    voxel's shadow and read back in slot order, gives the oracle's Atx and
+    chord sums bit for bit; views with an axis-parallel ray have none."""
+    nx, ny, na = dims
+    SO, OD, det = 541.0, 408.0, 1.0
+    vx = SO / (SO + OD) * det * na / nx
+    yv = np.random.default_rng(na).standard_normal(na).astype(np.float32)
+    tables = 0
+    for a in (0.0, 30.0, 45.0, 90.0, 200.0, 333.3):
+        g = oracle_mod.gateway_geometry(-a / 180 * np.pi, SO, OD, vx, det, na, 1)
+        yd = g["y_det"].copy()
+        K = dm.dm_chord_count(g["cos_phi"], g["sin_phi"], _p(yd), g["SO"], g["OD"],
+                              g["det"], nx, ny, na)
+        if K == 0:  # an axis-parallel central ray (odd na at 0 and 90 degrees)
+            assert na % 2 == 1 and a in (0.0, 90.0)
+            continue
+        tables += 1
+        bo, co = oracle_mod.atx(yv, g, nx, ny, 1)
+        b = np.zeros(nx * ny, np.float32)
+        sc = np.zeros(nx * ny, np.float32)
+        assert dm.dm_atx_table(_p(b), _p(yv), _p(sc), g["cos_phi"], g["sin_phi"], _p(yd),
+                               g["SO"], g["OD"], g["scale"], g["det"], nx, ny, na, K) == 0
+        assert np.array_equal(b, bo) and np.array_equal(sc, co), a
+        # one slot fewer than the largest count does not hold every voxel
+        assert dm.dm_atx_table(_p(b), _p(yv), _p(sc), g["cos_phi"], g["sin_phi"], _p(yd),
+                               g["SO"], g["OD"], g["scale"], g["det"], nx, ny, na,
+                               K - 1) == -1
+    assert tables >= 4
+
+
+def test_chord_slots_of_the_512_fan_beam_protocol(dm, oracle_mod):
+    """512^2 voxels of 0.9887 mm, 888 bins of 1 mm, SID 541 / SDD 949 mm, 60
+    views: the largest number of pairs of a voxel is 8, the slots (and the
+    600 MB of tables) that the GPU plan builds for this protocol."""
+    nx = ny = 512
+    na, SO, OD, det, vx = 888, 541.0, 408.0, 1.0, 0.9887
+    K = 0
+    for a in np.arange(1, 61) * 6.0:
+        g = oracle_mod.gateway_geometry(-a / 180 * np.pi, SO, OD, vx, det, na, 1)
+        yd = g["y_det"].copy()
+        K = max(K, dm.dm_chord_count(g["cos_phi"], g["sin_phi"], _p(yd), g["SO"], g["OD"],
+                                     g["det"], nx, ny, na))
+    assert K == 8
+    assert (2 + K) * nx * ny * 60 * 4 / 2**20 == 600.0
