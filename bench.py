@@ -76,11 +76,12 @@ UNEVEN = dict(
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per instance and
 # launch of each iteration kernel, from `ncu --set full --clock-control none`
 # captures: the 2D fan-beam workload at batch 64 (the shared-geometry
-# kernels and the column-walk TV step) and the cone-beam workload (one
-# volume).  The traffic is about one read of each instance's image or volume
-# plus its writes, so it scales with the batch.
+# kernels and the column-walk TV step; the backward step reading its chord
+# tables, captured on a launch of 32 instances) and the cone-beam workload
+# (one volume).  The traffic is about one read of each instance's image or
+# volume plus its writes, so it scales with the batch.
 NCU_DRAM_PER_INSTANCE = {
-    "fan2d": {"sart_ax": 60.94e6 / 64, "sart_atx": 80.41e6 / 64,
+    "fan2d": {"sart_ax": 60.94e6 / 64, "sart_atx": 40.13e6 / 32,
               "tv_step": 90.55e6 / 64},
     "cone3d": {"sart_ax": 71.55e6, "sart_atx": 80.01e6, "tv_step": 91.60e6},
 }
