@@ -40,6 +40,9 @@ def dm():
     L.dm_atx.argtypes = [F, F, F, C.c_float, C.c_float, F, F, C.c_float, C.c_float,
                          C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
                          C.c_int, C.c_int, C.c_int, C.c_int]
+    L.dm_atx3_zcol.argtypes = [F, F, F, C.c_float, C.c_float, F, F, C.c_float, C.c_float,
+                               C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
+                               C.c_int, C.c_int, C.c_int]
     L.dm_chord_count.argtypes = [C.c_float, C.c_float, F, C.c_float, C.c_float, C.c_float,
                                  C.c_int, C.c_int, C.c_int]
     L.dm_chord_count.restype = C.c_int
@@ -169,3 +172,25 @@ def test_chord_slots_of_the_512_fan_beam_protocol(dm, oracle_mod):
                                      g["det"], nx, ny, na))
     assert K == 8
     assert (2 + K) * nx * ny * 60 * 4 / 2**20 == 600.0
+
+
+@pytest.mark.parametrize("case", [c for c in CASES if c[2] > 1], ids=lambda c: str(c[:5]))
+def test_cone_beam_z_column_walk_matches_oracle(dm, oracle_mod, case):
+    """The cone-beam backward step walked down each voxel column, with the
+    window's and shadow's columns, the corners' magnifications and the
+    in-plane face tests computed once per column, gives the oracle's Atx
+    and chord sums bit for bit (the form planned for the cone-beam kernel)."""
+    nx, ny, nz, na, nb, SO, OD, det = case
+    rng = np.random.default_rng(3 * nx + nz)
+    vx = SO / (SO + OD) * det * na / nx
+    yv = rng.standard_normal(na * nb).astype(np.float32)
+    for a in [0.0, 45.0, 90.0, 200.0] + rng.uniform(0, 360, 4).tolist():
+        g = oracle_mod.gateway_geometry(-a / 180 * np.pi, SO, OD, vx, det, na, nb)
+        yd, zd = g["y_det"].copy(), g["z_det"].copy()
+        bo, co = oracle_mod.atx(yv, g, nx, ny, nz)
+        b = np.zeros(nx * ny * nz, np.float32)
+        sc = np.zeros(nx * ny * nz, np.float32)
+        dm.dm_atx3_zcol(_p(b), _p(yv), _p(sc), g["cos_phi"], g["sin_phi"], _p(yd), _p(zd),
+                        g["SO"], g["OD"], g["scale"], g["det"], g["det"], 1.0, nx, ny, nz,
+                        na, nb)
+        assert np.array_equal(b, bo) and np.array_equal(sc, co), a
