@@ -131,6 +131,13 @@ __host__ __device__ inline dim3 tile_grid(int nx, int ny, int nz, int batch) {
               batch);
 }
 
+// Launch rows of a tile grid: (ny / kTileY rounded up) * nz, at most 65535
+// (the GPU's grid y limit).  The TV entry points reject images beyond it.
+constexpr long long kMaxGridRows = 65535;
+__host__ __device__ inline long long tile_rows(int ny, int nz) {
+  return (long long)((ny + kTileY - 1) / kTileY) * nz;
+}
+
 // Voxel of this thread; true if inside the volume.
 __device__ __forceinline__ bool tile_voxel(int nx, int ny, int nz, int &ix,
                                            int &iy, int &iz) {

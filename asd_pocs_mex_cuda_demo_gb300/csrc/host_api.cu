@@ -106,6 +106,18 @@ static int ws_acquire(Workspace *&w, size_t bytes) {
 
 static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// The TV entry points' image limit: its tile grid must launch (see tile_rows).
+static int check_tv_dims(int nx, int ny, int nz) {
+  if (nx <= 0 || ny <= 0 || nz <= 0)
+    return set_error(ASDPOCS_ERR_ARG, "bad image dimensions");
+  if (tile_rows(ny, nz) > kMaxGridRows)
+    return set_error(ASDPOCS_ERR_ARG,
+                     "image of %d x %d x %d needs %lld tile rows (ceil(ny/8)*nz), over "
+                     "the limit of %lld",
+                     nx, ny, nz, tile_rows(ny, nz), kMaxGridRows);
+  return 0;
+}
+
 static int check_dims(int nx, int ny, int nz, int na, int nb) {
   if (nx <= 0 || ny <= 0 || nz <= 0 || na <= 0 || nb <= 0)
     return set_error(ASDPOCS_ERR_ARG,
@@ -329,9 +341,12 @@ static int atx_host(float *X, const float *yv, float *sc, float cos_phi,
   if (!X || !yv || !sc || !y_det || !z_det)
     return set_error(ASDPOCS_ERR_ARG, "null pointer");
   const size_t N = (size_t)nx * ny * nz, M = (size_t)na * nb;
+  const Dims d{nx, ny, nz, na, nb};
+  // cone beams: the view's ray tables for the z-column backward step
+  const size_t zs = nz > 1 ? atx_zcol_scratch_bytes(d) : 0;
   const size_t oX = 0, oS = align256(N * 4), oY = oS + align256(N * 4),
                oA = oY + align256(M * 4), oB = oA + align256((size_t)na * 4),
-               tot = oB + align256((size_t)nb * 4);
+               oT = oB + align256((size_t)nb * 4), tot = oT + zs;
   Workspace *w;
   if (int e = ws_acquire(w, tot)) return e;
   std::lock_guard<std::mutex> lk(w->mu);
@@ -342,8 +357,12 @@ static int atx_host(float *X, const float *yv, float *sc, float cos_phi,
   const ViewGeo g = with_constants(ViewGeo{cos_phi, sin_phi, SO, OD, scale,
                                            dy_det, dz_det, dz, (const float *)(b + oA),
                                            (const float *)(b + oB)});
-  Dims d{nx, ny, nz, na, nb};
-  ASD_CUDA(launch_atx((float *)(b + oX), (const float *)(b + oY), (float *)(b + oS), g, d, w->st));
+  if (nz > 1)
+    ASD_CUDA(launch_atx_zcol((float *)(b + oX), (const float *)(b + oY), (float *)(b + oS), g,
+                             d, b + oT, w->st));
+  else
+    ASD_CUDA(launch_atx((float *)(b + oX), (const float *)(b + oY), (float *)(b + oS), g, d,
+                        w->st));
   ASD_CUDA(cudaMemcpyAsync(X, b + oX, N * 4, cudaMemcpyDeviceToHost, w->st));
   ASD_CUDA(cudaMemcpyAsync(sc, b + oS, N * 4, cudaMemcpyDeviceToHost, w->st));
   ASD_CUDA(cudaStreamSynchronize(w->st));
@@ -425,8 +444,7 @@ static int tv_host(const T *img, T *out, int nx, int ny, int nz, double alpha,
                    int n, int pos, const T *old) {
   clear_error();
   if (!img || !out) return set_error(ASDPOCS_ERR_ARG, "null pointer");
-  if (nx <= 0 || ny <= 0 || nz <= 0)
-    return set_error(ASDPOCS_ERR_ARG, "bad image dimensions");
+  if (int e = check_tv_dims(nx, ny, nz)) return e;
   const size_t N = (size_t)nx * ny * nz;
   const size_t tiles = (size_t)((nx + 31) / 32) * ((ny + 7) / 8) * nz;
   const size_t oI = 0, oO = align256(N * sizeof(T)), oA = oO + align256(N * sizeof(T)),
@@ -485,8 +503,7 @@ int asdpocs_tv_device(float *img_d, const float *img_old_d, int nx, int ny,
                       void *stream) {
   clear_error();
   if (!img_d) return set_error(ASDPOCS_ERR_ARG, "null pointer");
-  if (nx <= 0 || ny <= 0 || nz <= 0)
-    return set_error(ASDPOCS_ERR_ARG, "bad image dimensions");
+  if (int e = check_tv_dims(nx, ny, nz)) return e;
   const size_t N = (size_t)nx * ny * nz;
   const size_t tiles = (size_t)((nx + 31) / 32) * ((ny + 7) / 8) * nz;
   const size_t oA = 0, oB = align256(N * 4), oS = oB + align256(N * 4),
@@ -555,6 +572,7 @@ struct asdpocs_plan_s {
   std::vector<Inst> h_inst;
   std::vector<int> has_ref;
   bool shared = false;  // all instances share sizes, geometry and angles
+  bool zcol = true;     // cone beams: z-column backward step (else per voxel)
   int tv_walk = 0;      // TV walk length (0: from the batch size)
   Inst *d_inst = nullptr;
   void *arena = nullptr;
@@ -714,7 +732,7 @@ namespace asd {
 
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk, bool finish) {
+                              int tv_walk, bool finish, bool zcol) {
   cudaError_t e = cudaSuccess;
   if (shared) e = launch_group_pack(d_inst, batch, d, 0, st);
   for (int v = 0; v < nv && e == cudaSuccess; v++) {
@@ -722,7 +740,7 @@ cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                : launch_sart_ax(d_inst, batch, d, v, st);
     if (e == cudaSuccess)
       e = shared ? launch_sart_atx_shared(d_inst, batch, d, v, st)
-                 : launch_sart_atx(d_inst, batch, d, v, st);
+                 : launch_sart_atx(d_inst, batch, d, v, st, zcol);
   }
   if (shared && e == cudaSuccess) e = launch_group_pack(d_inst, batch, d, 1, st);
   if (e == cudaSuccess) e = launch_after_sweep(d_inst, batch, d, st);
@@ -735,7 +753,7 @@ cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
 // One iteration of sub-batch s on its stream.
 static int plan_enqueue_sub(asdpocs_plan p, const SubBatch &s) {
   ASD_CUDA(enqueue_iteration(p->d_inst + s.first, s.count, s.d, s.nv, s.max_ng, p->shared,
-                             s.st, p->tv_walk, s.min_ng < 2));
+                             s.st, p->tv_walk, s.min_ng < 2, p->zcol));
   return 0;
 }
 
@@ -917,6 +935,12 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
                        sizeof(double) * (size_t)g0.nv) == 0;
   }
   if (getenv("ASDPOCS_NO_SHARED_GEOMETRY")) p->shared = false;
+  // ASDPOCS_CONE_ATX=voxel: the per-voxel form of the cone-beam backward step
+  // (same results; kept for comparison)
+  {
+    const char *f = getenv("ASDPOCS_CONE_ATX");
+    p->zcol = !(f && strcmp(f, "voxel") == 0);
+  }
   cudaGetDevice(&p->device);
   if (stream) {
     p->st = (cudaStream_t)stream;

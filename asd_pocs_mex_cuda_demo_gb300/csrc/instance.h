@@ -71,9 +71,10 @@ cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st);
 // `finish`: some instance may run fewer than two TV steps, so the
 // end-of-iteration kernel is needed (otherwise the last TV step ends every
 // instance's iteration and the launch is skipped).
+// `zcol`: cone-beam backward steps walk voxel columns (launch_sart_atx).
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk = 0, bool finish = true);
+                              int tv_walk = 0, bool finish = true, bool zcol = true);
 
 // Backward-step chord tables (Inst::chtab) of instances sharing 2-D geometry
 // and view angles, from d_inst[0], whose view tables are built: a counting

@@ -13,6 +13,13 @@ cudaError_t launch_ax(const float *x, float *y, float *sr, const ViewGeo &g,
 cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
                        const Dims &d, cudaStream_t st);
 
+// Atx of one cone-beam view (nz > 1) walked down voxel columns, bit-identical
+// to launch_atx; `scratch` holds the view's ray tables
+// (atx_zcol_scratch_bytes(d) bytes, 256-byte aligned).
+size_t atx_zcol_scratch_bytes(const Dims &d);
+cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &g,
+                            const Dims &d, void *scratch, cudaStream_t st);
+
 // Batched launches take the plan's largest sizes `d` (each field the
 // maximum over its instances) for the grid; every instance reads its own
 // sizes from Inst::d, and instances of one plan are all planar (nz == nb ==
@@ -24,8 +31,10 @@ cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
 // cor, column normalisation, update m += beta*bp/sumC, positivity.
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
                            int view, cudaStream_t st);
+// Cone beams (nz > 1) walk voxel columns (k_sart_atx_zcol) unless `zcol`
+// is false (the per-voxel form; bit-identical).
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, cudaStream_t st);
+                            int view, cudaStream_t st, bool zcol = true);
 
 // ---- TV and scalars (kernels_tv.cu) ----
 // FP64 / FP32 TV minimisation on device buffers (reference semantics).

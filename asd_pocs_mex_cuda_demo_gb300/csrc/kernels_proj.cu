@@ -597,6 +597,230 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 }
 
 // ---------------------------------------------------------------------------
+// Cone-beam backward step per voxel column (z-column form).  A thread owns a
+// segment of kZSeg voxels of one (x, y) column and walks it down z.  What
+// does not depend on z is computed once per segment (zcol_setup): the
+// footprint window's columns and magnification, the shadow's columns and its
+// corners' magnifications, and for each detector column of the shadow the
+// in-plane part of the x and y face tests (col_faces, kept in shared memory,
+// a thread reading only its own slots).  Each voxel then finds its rows
+// (zcol_rows) and evaluates only the z parts of the face tests
+// (chord3_col).  Pairs run as one sequence per voxel, rows outer (the
+// reference's order), a warp walking its longest sequence; the voxels of a
+// warp are 32 neighbours along x at the same z, so image reads and writes
+// are coalesced.  Views that do not allow narrowing (an axis-parallel ray, a
+// residual that is not finite) take the per-voxel form with the reference's
+// whole window.  Columns whose shadow is wider than kZColA detector columns
+// evaluate their chords from the ray tables (chord3_bf).
+// Grid: (x tiles of 32, y tiles of 8 x segments, instances).
+// ---------------------------------------------------------------------------
+constexpr int kZSeg = 32;   // voxels of a column per thread
+constexpr int kZColA = 8;   // detector columns of a shadow kept per thread
+
+struct ZColShared {
+  float4 pts[kZColA][kAtxThreads];   // F1, F2 in-plane points
+  unsigned bits[kZColA][kAtxThreads];
+};
+
+__host__ __device__ inline dim3 zcol_grid(int nx, int ny, int nz, int batch) {
+  return dim3((nx + kTileX - 1) / kTileX,
+              ((ny + kTileY - 1) / kTileY) * ((nz + kZSeg - 1) / kZSeg), batch);
+}
+
+// This thread's column and segment [z0, z1) for an instance of sizes D;
+// false when the block lies outside the instance's own grid.
+__device__ __forceinline__ bool zcol_thread(const Dims &D, int &ix, int &iy, int &z0,
+                                            int &z1) {
+  const int ty = (D.ny + kTileY - 1) / kTileY, ns = (D.nz + kZSeg - 1) / kZSeg;
+  if ((int)blockIdx.x * kTileX >= D.nx || (int)blockIdx.y >= ty * ns) return false;
+  const int seg = blockIdx.y / ty, yt = blockIdx.y - seg * ty;
+  ix = blockIdx.x * kTileX + threadIdx.x % kTileX;
+  iy = yt * kTileY + threadIdx.x / kTileX;
+  z0 = seg * kZSeg;
+  z1 = min(z0 + kZSeg, D.nz);
+  return true;
+}
+
+// Walks this thread's segment.  pair(r, l, on) takes the chord l of ray r
+// (pairs in the reference's order; on == false for a lane past its own
+// pairs), voxel(idx) ends a voxel; begin(idx) starts it (prefetches).
+template <class Begin, class Pair, class Voxel>
+__device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
+                                              const float4 *__restrict__ tabA,
+                                              const float4 *__restrict__ tabC,
+                                              bool narrow, int ix, int iy, int z0, int z1,
+                                              ZColShared &sh, Begin begin, Pair pair,
+                                              Voxel voxel) {
+  const bool valid = ix < D.nx && iy < D.ny;
+  const float hz = G.dz / 2.0f;
+  if (!narrow) {
+    // the per-voxel form over the reference's window (no warp-wide steps)
+    if (!valid) return;
+    for (int iz = z0; iz < z1; iz++) {
+      const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+      begin(idx);
+      const VoxelWin w = voxel_window(G, D, ix, iy, iz);
+      const float rx = G.cos_phi * (-G.SO) - w.xc, ry = G.sin_phi * (-G.SO) - w.yc;
+      const float rz = 0.0f - w.zc;
+      for (int ib = w.b0; ib <= w.b1; ib++) {
+        const float c = __ldg(G.z_det + ib) - 0.0f;
+        for (int ia = w.a0; ia <= w.a1; ia++) {
+          const int r = ib * D.na + ia;
+          pair(r, chord3_bf(__ldg(tabA + ia), __ldg(tabC + r), c, rx, ry, rz, G.dz), true);
+        }
+      }
+      voxel(idx);
+    }
+    return;
+  }
+  const int t = threadIdx.x;
+  ZCol col;
+  int cntA = 0;
+  bool wide = false;
+  col.lo = 0;
+  col.rx = col.ry = 0.f;
+  if (valid) {
+    col = zcol_setup(G, D, ix, iy, true);
+    cntA = col.lo <= col.hi ? col.hi - col.lo + 1 : 0;
+    wide = cntA > kZColA;
+    if (!wide)
+      for (int k = 0; k < cntA; k++) {
+        const ColFaces f = col_faces(__ldg(tabA + col.lo + k), col.rx, col.ry);
+        sh.pts[k][t] = make_float4(f.p1x, f.p1y, f.p2x, f.p2y);
+        sh.bits[k][t] = f.bits;
+      }
+  }
+  for (int iz = z0; iz < z1; iz++) {
+    const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+    if (valid) begin(idx);
+    float zc = 0.f;
+    int blo = 0, bhi = -1;
+    const bool has = valid && zcol_rows(G, D, col, iz, zc, blo, bhi);
+    const int cntB = has && blo <= bhi ? bhi - blo + 1 : 0;
+    const int cnt = cntA * cntB;
+    const int kN = __reduce_max_sync(0xffffffffu, cnt);
+    const float rz = 0.0f - zc;
+    int ka = 0, ib = blo;
+    for (int k = 0; k < kN; k++) {
+      const bool on = k < cnt;
+      const int kk = on ? ka : 0;
+      const int ia = on ? col.lo + ka : 0;
+      const int r = (on ? ib : 0) * D.na + ia;
+      const float4 Cs = __ldg(tabC + r);
+      float l;
+      if (!wide) {
+        const float4 p = sh.pts[kk][t];
+        const ColFaces f{p.x, p.y, p.z, p.w, sh.bits[kk][t]};
+        if (f.bits & kCfMany)
+          l = (f.bits & kCfXF) ? chord3_axis<true>(__ldg(tabA + ia), Cs, col.rx, col.ry, rz, G.dz)
+                               : chord3_axis<false>(__ldg(tabA + ia), Cs, col.rx, col.ry, rz, G.dz);
+        else
+          l = chord3_col(f, Cs, col.rx, col.ry, rz, hz);
+      } else {
+        l = chord3_bf(__ldg(tabA + ia), Cs, 0.0f, col.rx, col.ry, rz, G.dz);
+      }
+      pair(r, l, on);
+      if (++ka == cntA) {
+        ka = 0;
+        ib++;
+      }
+    }
+    if (valid) voxel(idx);
+  }
+}
+
+// SART backward step of cone-beam instances (see k_sart_atx) in z columns.
+__global__ void __launch_bounds__(kAtxThreads, 4)
+    k_sart_atx_zcol(const Inst *__restrict__ insts, int view) {
+  __shared__ ZColShared sh;
+  const Inst &I = insts[blockIdx.z];
+  if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
+  const Dims D = I.d;
+  int ix, iy, z0, z1;
+  if (!zcol_thread(D, ix, iy, z0, z1)) return;
+  const ViewGeo G = view_of(I, view);
+  const float4 *tabA = I.tabA + (long long)view * D.na;
+  const bool narrow = !(I.vflags[view] & kViewAxisParallel) && I.s->cor_finite;
+  const float beta = I.s->beta_f;
+  float *m = I.m;
+  const float *__restrict__ cor = I.cor;
+  float acc = 0.f, accl = 0.f, mv = 0.f;
+  atx_zcol_walk(
+      G, D, tabA, I.tabC, narrow, ix, iy, z0, z1, sh,
+      [&](unsigned idx) {
+        mv = m[idx];
+        acc = 0.f;
+        accl = 0.f;
+      },
+      [&](int r, float l, bool on) {
+        const float yv = on ? __ldg(cor + r) : 0.f;
+        if (on) {
+          acc += l * yv;
+          accl += l;
+        }
+      },
+      [&](unsigned idx) {
+        const float bp = acc * G.scale, scv = accl * G.scale;
+        const float mn = mv + beta * __fdividef(bp, scv == 0.f ? 1.f : scv);
+        m[idx] = mn < 0.f ? 0.f : mn;
+      });
+}
+
+// Ray tables of one view for the standalone backward step (launcher path):
+// tabA[na], tabC[na*nb] and, in flag[0], whether the view forbids narrowing
+// (flag[0] set unless every ray has both in-plane components, the bins lie
+// on the uniform grid and every value is finite; flag[0] must be 0 before
+// the launch).
+__global__ void __launch_bounds__(256)
+    k_view_tab3(const float *__restrict__ yv, float4 *tabA, float4 *tabC, int *flag,
+                ViewGeo G, Dims D) {
+  const long long nr = (long long)D.na * D.nb;
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool ok = true;
+  if (r < nr) {
+    const int ia = (int)(r % D.na), ib = (int)(r / D.na);
+    const float yd = G.y_det[ia], zd = G.z_det[ib];
+    const float4 A = ray_tab_a(G, yd);
+    if (ib == 0) tabA[ia] = A;
+    tabC[r] = ray_tab_c(A, zd);
+    ok = A.x != 0.0f && A.y != 0.0f && on_grid(yd, ia, D.na, G.dy_det) &&
+         on_grid(zd, ib, D.nb, G.dz_det) && isfinite(yv[r]) && G.dy_det > 0.0f &&
+         G.dz_det > 0.0f;
+  }
+  if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
+}
+
+// Standalone cone-beam backward step (Ax_cone_gpu.cu:214-271) in z columns,
+// from the tables of k_view_tab3.
+__global__ void __launch_bounds__(kAtxThreads, 4)
+    k_atx_zcol(float *__restrict__ x, const float *__restrict__ yv, float *__restrict__ sc,
+               const float4 *__restrict__ tabA, const float4 *__restrict__ tabC,
+               const int *__restrict__ flag, ViewGeo G, Dims D) {
+  __shared__ ZColShared sh;
+  int ix, iy, z0, z1;
+  if (!zcol_thread(D, ix, iy, z0, z1)) return;
+  const bool narrow = flag[0] == 0;
+  float acc = 0.f, accl = 0.f;
+  atx_zcol_walk(
+      G, D, tabA, tabC, narrow, ix, iy, z0, z1, sh,
+      [&](unsigned) {
+        acc = 0.f;
+        accl = 0.f;
+      },
+      [&](int r, float l, bool on) {
+        const float v = on ? __ldg(yv + r) : 0.f;
+        if (on) {
+          acc += l * v;
+          accl += l;
+        }
+      },
+      [&](unsigned idx) {
+        x[idx] = acc * G.scale;
+        sc[idx] = accl * G.scale;
+      });
+}
+
+// ---------------------------------------------------------------------------
 // Shared-geometry backward step: when every instance of a plan has the same
 // geometry and view angles, the chords of a (voxel, bin) pair are the same
 // for all of them.  A block then handles one voxel tile for a group of
@@ -1190,6 +1414,27 @@ cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
   return cudaGetLastError();
 }
 
+size_t atx_zcol_scratch_bytes(const Dims &d) {
+  const size_t a = ((size_t)d.na * sizeof(float4) + 255) & ~(size_t)255;
+  const size_t c = ((size_t)d.na * d.nb * sizeof(float4) + 255) & ~(size_t)255;
+  return a + c + 256;
+}
+
+cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &g,
+                            const Dims &d, void *scratch, cudaStream_t st) {
+  char *b = (char *)scratch;
+  float4 *tabA = (float4 *)b;
+  float4 *tabC = (float4 *)(b + (((size_t)d.na * sizeof(float4) + 255) & ~(size_t)255));
+  int *flag = (int *)(b + atx_zcol_scratch_bytes(d) - 256);
+  cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const long long nr = (long long)d.na * d.nb;
+  k_view_tab3<<<(unsigned)((nr + 255) / 256), 256, 0, st>>>(y, tabA, tabC, flag, g, d);
+  k_atx_zcol<<<zcol_grid(d.nx, d.ny, d.nz, 1), kAtxThreads, 0, st>>>(x, y, sc, tabA, tabC,
+                                                                     flag, g, d);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
                            int view, cudaStream_t st) {
   const long long nr = (long long)d.na * d.nb;
@@ -1202,9 +1447,11 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
 }
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, cudaStream_t st) {
+                            int view, cudaStream_t st, bool zcol) {
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
-  if (d.nz > 1 || d.nb > 1)
+  if (d.nz > 1 && zcol)
+    k_sart_atx_zcol<<<zcol_grid(d.nx, d.ny, d.nz, batch), kAtxThreads, 0, st>>>(insts, view);
+  else if (d.nz > 1 || d.nb > 1)
     k_sart_atx<false><<<grid, kAtxThreads, 0, st>>>(insts, view);
   else
     k_sart_atx<true><<<grid, kAtxThreads, 0, st>>>(insts, view);

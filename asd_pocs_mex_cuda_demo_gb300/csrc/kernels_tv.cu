@@ -269,7 +269,8 @@ cudaError_t tv_minimize(T *img, const T *old, T *wa, T *wb, double *scal,
                         int nz, double alpha, int n_iter, int pos,
                         cudaStream_t st) {
   const dim3 grid = tile_grid(nx, ny, nz, 1);
-  if ((long long)grid.x * grid.y > kMaxPartials) return cudaErrorInvalidValue;
+  if ((long long)grid.x * grid.y > kMaxPartials || tile_rows(ny, nz) > kMaxGridRows)
+    return cudaErrorInvalidValue;
   k_tv_dist<T><<<grid, kThreads, 0, st>>>(img, old, nx, ny, nz, scal, partials,
                                           counter);
   const T *src = img;

@@ -12,7 +12,8 @@
 // passes the image (in/out) and the reference image.
 //
 // Limits: at most kMaxVoxels voxels (nx*ny*nz <= 1,048,576, e.g. 1024^2 or
-// 128^2 x 64) and kMaxTiles 32x8 voxel tiles; larger images are rejected.
+// 128^2 x 64), kMaxTiles 32x8 voxel tiles and 65535 tile rows
+// (ceil(ny/8)*nz, the GPU's grid limit); other images are rejected.
 // All calls share the one array: calls that overlap on the GPU (different
 // streams, or several host threads) race on it and corrupt each other.
 // The first call on a device looks up the array's device address (with that
@@ -81,6 +82,11 @@ extern "C" int asdpocs_tv_device_noalloc(float *img_d, const float *img_old_d,
                      "image needs %zu tiles, over the %zu-tile limit of the "
                      "allocation-free TV entry point",
                      tiles, kMaxTiles);
+  if (tile_rows(ny, nz) > kMaxGridRows)
+    return set_error(ASDPOCS_ERR_ARG,
+                     "image needs %lld tile rows (ceil(ny/8)*nz), over the limit of "
+                     "%lld of the allocation-free TV entry point",
+                     tile_rows(ny, nz), kMaxGridRows);
   char *b = nullptr;
   if (int e = scratch_address(&b)) return e;
   cudaStream_t st = (cudaStream_t)stream;

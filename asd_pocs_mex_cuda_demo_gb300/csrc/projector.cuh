@@ -969,4 +969,195 @@ ASD_HD float chord3_axis(const float4 A, const float4 Cs, float rx, float ry,
   return sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
 }
 
+// ---------------------------------------------------------------------------
+// Cone-beam backward step per voxel column (z-column form).
+//
+// For a voxel column (ix, iy) and a detector column ia, the x and y face
+// tests of find_l_3d (Ax_cone_gpu.cu:120-209) split into an in-plane part --
+// the face point's in-plane coordinate t0 -/+ u0 and its |.| <= 1/2 test,
+// which depend on the ray's in-plane slopes and the column only -- and a z
+// part, t1 -/+ u1 and its |.| <= dz/2 test, which depends on the voxel's z.
+// ColFaces keeps the in-plane part of one (column, detector column): the
+// first two x/y faces, in the reference's face order, whose in-plane test
+// passes.  Faces whose in-plane test fails can never be hits, so a voxel's
+// hits are, in order, F1 and F2 (if their z tests pass), then the z- and z+
+// faces: chord3_col takes the first two of those four, which is the
+// reference's first-two-hits rule.  When three or four in-plane tests pass
+// (a ray through a column corner, to within rounding) the column keeps
+// kCfMany and its pairs use chord3_axis.  Every face value is the reference
+// expression, rounded as there, so the chord is find_l_3d's bit for bit.
+// Requires a != 0 and b != 0 (no axis-parallel ray).
+// ---------------------------------------------------------------------------
+constexpr unsigned kCfV1 = 1u, kCfV2 = 2u;    // F1 / F2 exists
+constexpr unsigned kCfY1 = 4u, kCfY2 = 8u;    // F1 / F2 is a y face
+constexpr unsigned kCfU1 = 16u, kCfU2 = 32u;  // F1 / F2 is an upper face
+constexpr unsigned kCfMany = 64u;             // three or more in-plane hits
+constexpr unsigned kCfXF = 128u;              // |a| > |b| (x faces first)
+
+struct ColFaces {
+  float p1x, p1y, p2x, p2y;  // in-plane coordinates of F1 and F2
+  unsigned bits;
+};
+
+// In-plane part of the x/y face tests of ray A (ray_tab_a) for the voxel
+// column whose centre is the source minus (rx, ry).
+ASD_HD ColFaces col_faces(const float4 A, float rx, float ry) {
+  const float xt0 = A.z * (-rx) + ry, xu0 = A.z * 0.5f;
+  const float xmy = xt0 - xu0, xpy = xt0 + xu0;
+  const float yt0 = A.w * (-ry) + rx, yu0 = A.w * 0.5f;
+  const float ymx = yt0 - yu0, ypx = yt0 + yu0;
+  const bool fxm = fabsf(xmy) <= 0.5f, fxp = fabsf(xpy) <= 0.5f;
+  const bool fym = fabsf(ymx) <= 0.5f, fyp = fabsf(ypx) <= 0.5f;
+  const bool xf = fabsf(A.x) > fabsf(A.y);
+  // the four faces in the reference's order, each (pass, x, y, bits)
+  const bool pass[4] = {xf ? fxm : fym, xf ? fxp : fyp, xf ? fym : fxm, xf ? fyp : fxp};
+  const float px[4] = {xf ? -0.5f : ymx, xf ? 0.5f : ypx, xf ? ymx : -0.5f, xf ? ypx : 0.5f};
+  const float py[4] = {xf ? xmy : -0.5f, xf ? xpy : 0.5f, xf ? -0.5f : xmy, xf ? 0.5f : xpy};
+  // face k: bit 0 = upper, bit 1 = y face
+  const unsigned kind[4] = {xf ? 0u : 2u, xf ? 1u : 3u, xf ? 2u : 0u, xf ? 3u : 1u};
+  ColFaces f;
+  f.p1x = f.p1y = f.p2x = f.p2y = 0.f;
+  unsigned k1 = 0, k2 = 0;
+  int n = 0;
+  // taken from the last face to the first: a passing face becomes F1 and
+  // pushes the previous F1 to F2
+#pragma unroll
+  for (int k = 3; k >= 0; k--) {
+    const bool p = pass[k];
+    f.p2x = p ? f.p1x : f.p2x;
+    f.p2y = p ? f.p1y : f.p2y;
+    k2 = p ? k1 : k2;
+    f.p1x = p ? px[k] : f.p1x;
+    f.p1y = p ? py[k] : f.p1y;
+    k1 = p ? kind[k] : k1;
+    n += p ? 1 : 0;
+  }
+  f.bits = (n >= 1 ? kCfV1 : 0u) | (n >= 2 ? kCfV2 : 0u) | ((k1 & 2u) ? kCfY1 : 0u) |
+           ((k2 & 2u) ? kCfY2 : 0u) | ((k1 & 1u) ? kCfU1 : 0u) | ((k2 & 1u) ? kCfU2 : 0u) |
+           (n > 2 ? kCfMany : 0u) | (xf ? kCfXF : 0u);
+  return f;
+}
+
+// find_l_3d of ray (A, Cs) and the voxel at (rx, ry, rz) from the source,
+// given the column's ColFaces f (without kCfMany).  hz = dz / 2.
+ASD_HD float chord3_col(const ColFaces &f, const float4 Cs, float rx, float ry,
+                        float rz, float hz) {
+  const unsigned bits = f.bits;
+  // z parts of F1 and F2: t1 -/+ u1 with t1 = s * (-r) + rz, u1 = s * (1/2),
+  // s = c/a (x faces) or c/b (y faces)
+  const float c1 = (bits & kCfY1) ? Cs.y : Cs.x, r1 = (bits & kCfY1) ? ry : rx;
+  const float t1 = c1 * (-r1) + rz, u1 = c1 * 0.5f;
+  const float z1 = (bits & kCfU1) ? t1 + u1 : t1 - u1;
+  const float c2 = (bits & kCfY2) ? Cs.y : Cs.x, r2 = (bits & kCfY2) ? ry : rx;
+  const float t2 = c2 * (-r2) + rz, u2 = c2 * 0.5f;
+  const float z2 = (bits & kCfU2) ? t2 + u2 : t2 - u2;
+  const bool h1 = (bits & kCfV1) && fabsf(z1) <= hz;
+  const bool h2 = (bits & kCfV2) && fabsf(z2) <= hz;
+  // z faces
+  const float zt0 = Cs.z * (-rz) + rx, zu0 = Cs.z * hz;
+  const float zt1 = Cs.w * (-rz) + ry, zu1 = Cs.w * hz;
+  const float zmx = zt0 - zu0, zmy = zt1 - zu1, zpx = zt0 + zu0, zpy = zt1 + zu1;
+  const bool fzm = fabsf(zmx) <= 0.5f && fabsf(zmy) <= 0.5f;
+  const bool fzp = fabsf(zpx) <= 0.5f && fabsf(zpy) <= 0.5f;
+  const int n = (h1 ? 1 : 0) + (h2 ? 1 : 0) + (fzm ? 1 : 0) + (fzp ? 1 : 0);
+  // first z hit
+  const float qx = fzm ? zmx : zpx, qy = fzm ? zmy : zpy, qz = fzm ? -hz : hz;
+  // first hit: F1, else F2, else the first z hit
+  const float ax = h1 ? f.p1x : (h2 ? f.p2x : qx);
+  const float ay = h1 ? f.p1y : (h2 ? f.p2y : qy);
+  const float az = h1 ? z1 : (h2 ? z2 : qz);
+  // second hit: F2 after F1; the first z hit after one face; z+ after z-
+  const bool both = h1 && h2, one = h1 != h2;
+  const float bx = both ? f.p2x : (one ? qx : zpx);
+  const float by = both ? f.p2y : (one ? qy : zpy);
+  const float bz = both ? z2 : (one ? qz : hz);
+  const float e0 = bx - ax, e1 = by - ay, e2 = bz - az;
+  return n >= 2 ? sqrtf(e0 * e0 + e1 * e1 + e2 * e2) : 0.0f;
+}
+
+// Per-column part of the footprint (voxel_window's columns and its
+// magnification, shadow_bins3's columns and its corners' magnifications);
+// zcol_rows then gives each voxel's rows.  Same expressions as voxel_window
+// and shadow_bins3, so the same pairs.
+struct ZCol {
+  float xc, yc, rx, ry, ta, tb;
+  float q[4];      // magnification at the four corners (shadow rows)
+  int a0, a1;      // window columns (clamped)
+  int lo, hi;      // window columns narrowed to the shadow
+  bool ok;         // every corner in front of the source (shadow usable)
+};
+
+ASD_HD ZCol zcol_setup(const ViewGeo &G, const Dims &D, int ix, int iy, bool narrow) {
+  ZCol c;
+  const int na2 = D.na / 2, nx2 = D.nx / 2, ny2 = D.ny / 2;
+  c.yc = (float)(iy - ny2) + 0.5f;
+  c.xc = (float)(ix - nx2) + 0.5f;
+  const float xr = G.cos_phi * c.xc + G.sin_phi * c.yc;
+  const float yr = -G.sin_phi * c.xc + G.cos_phi * c.yc;
+  c.ta = G.SD / ((xr + G.SO) * G.dy_det);
+  c.tb = G.dz_det != G.dy_det ? G.SD / ((xr + G.SO) * G.dz_det) : c.ta;
+  const int amax = (int)floorf((yr + 1) * c.ta + na2);
+  const int amin = (int)floorf((yr - 1) * c.ta + na2);
+  c.a0 = amin > 0 ? amin : 0;
+  c.a1 = amax < D.na - 1 ? amax : D.na - 1;
+  const float hc = 0.5f * G.cos_phi, hs = 0.5f * G.sin_phi;
+  const float inv_a = hd_rcp(G.dy_det);
+  const float offa = D.na * 0.5f - 0.5f;
+  float umin = 3.0e38f, umax = -3.0e38f;
+  bool ok = true;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const float ex = (k & 1) ? 1.f : -1.f, ey = (k & 2) ? 1.f : -1.f;
+    const float px = xr + ex * hc + ey * hs;
+    const float py = yr - ex * hs + ey * hc;
+    const float den = px + G.SO;
+    ok = ok && den > 1e-3f;
+    c.q[k] = fast_div(G.SD, den);
+    const float u = py * c.q[k] * inv_a + offa;
+    umin = fminf(umin, u);
+    umax = fmaxf(umax, u);
+  }
+  c.ok = narrow && ok;
+  c.lo = c.a0;
+  c.hi = c.a1;
+  if (c.ok) {
+    const int alo = (int)ceilf(umin - 0.05f), ahi = (int)floorf(umax + 0.05f);
+    c.lo = c.lo > alo ? c.lo : alo;
+    c.hi = c.hi < ahi ? c.hi : ahi;
+  }
+  c.rx = G.cos_phi * (-G.SO) - c.xc;
+  c.ry = G.sin_phi * (-G.SO) - c.yc;
+  return c;
+}
+
+// Rows [blo, bhi] of voxel iz of column c (the window's rows narrowed to the
+// shadow's); false when the reference's window is empty.
+ASD_HD bool zcol_rows(const ViewGeo &G, const Dims &D, const ZCol &c, int iz, float &zc,
+                      int &blo, int &bhi) {
+  const int nb2 = D.nb / 2, nz2 = D.nz / 2;
+  zc = ((float)(iz - nz2) + 0.5f) * G.dz;
+  const int bmax = (int)floorf((zc + G.dwin) * c.tb + nb2);
+  const int bmin = (int)floorf((zc - G.dwin) * c.tb + nb2);
+  blo = bmin > 0 ? bmin : 0;
+  bhi = bmax < D.nb - 1 ? bmax : D.nb - 1;
+  const bool has = c.a0 <= c.a1 && blo <= bhi;
+  if (has && c.ok) {
+    const float hz = 0.5f * G.dz;
+    const float inv_b = hd_rcp(G.dz_det);
+    const float offb = D.nb * 0.5f - 0.5f;
+    const float zlo = (zc - hz) * inv_b, zhi = (zc + hz) * inv_b;
+    float vmin = 3.0e38f, vmax = -3.0e38f;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const float v0 = zlo * c.q[k] + offb, v1 = zhi * c.q[k] + offb;
+      vmin = fminf(vmin, fminf(v0, v1));
+      vmax = fmaxf(vmax, fmaxf(v0, v1));
+    }
+    const int tlo = (int)ceilf(vmin - 0.05f), thi = (int)floorf(vmax + 0.05f);
+    blo = blo > tlo ? blo : tlo;
+    bhi = bhi < thi ? bhi : thi;
+  }
+  return has;
+}
+
 }  // namespace asd

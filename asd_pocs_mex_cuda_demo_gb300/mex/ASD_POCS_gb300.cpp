@@ -32,10 +32,30 @@ static double field(const mxArray *para, const char *name, double dflt,
   return mxGetScalar(f);
 }
 
+// A real double array (MATLAB's default class), as the reconstruction reads
+// its elements as doubles.
+static bool real_double(const mxArray *a) {
+  return mxGetClassID(a) == mxDOUBLE_CLASS && !mxIsComplex(a);
+}
+
+// Optional image field (para.m0, para.I0): NULL when absent or empty, else it
+// must be a real double array of nx*ny*nz elements.
+static const double *image_field(const mxArray *para, const char *name, size_t N) {
+  const mxArray *f = mxGetField(para, 0, name);
+  if (!f || mxGetNumberOfElements(f) == 0) return NULL;
+  if (!real_double(f) || mxGetNumberOfElements(f) != N) {
+    char msg[112];
+    snprintf(msg, sizeof msg, "parameter.%s must be a real double array of nx*ny*nz elements!",
+             name);
+    mexErrMsgTxt(msg);
+  }
+  return mxGetPr(f);
+}
+
 void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
   if (nrhs != 2) mexErrMsgTxt("Error usage! [m_res,out] = ASD_POCS_gb300(P, para)");
   const mxArray *P = prhs[0], *para = prhs[1];
-  if (mxGetClassID(P) != mxDOUBLE_CLASS) mexErrMsgTxt("P must be double");
+  if (!real_double(P)) mexErrMsgTxt("P must be a real double matrix");
   asdpocs_geometry g;
   g.nx = (int)field(para, "nx", 0, true);
   g.ny = (int)field(para, "ny", 0, true);
@@ -48,9 +68,14 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
   g.detsize = field(para, "detsize", 0, true);
   const mxArray *phi = mxGetField(para, 0, "phi_vec");
   if (!phi) mexErrMsgTxt("Error input argument parameter.phi_vec!");
+  if (!real_double(phi)) mexErrMsgTxt("parameter.phi_vec must be a real double vector!");
   g.nv = (int)mxGetN(P);
   if ((int)mxGetNumberOfElements(phi) != g.nv)
     mexErrMsgTxt("Size of Projection and phi_vec mismatch!");  // ASD_POCS_cuda.m:97-100
+  // one column of na*nb rays per view: the reference's P(:,ii) - proj
+  // (ASD_POCS_cuda.m:121) fails on any other row count
+  if (g.na <= 0 || g.nb <= 0 || mxGetM(P) != (size_t)g.na * (size_t)g.nb)
+    mexErrMsgTxt("Matrix dimensions must agree: P must have na*nb rows!");
   asdpocs_options o;
   asdpocs_options_default(&o);
   o.maxnumIter = (int)field(para, "maxnumIter", o.maxnumIter, false);
@@ -62,22 +87,19 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[]) {
   o.r_max = field(para, "r_max", o.r_max, false);
   o.epsilon = field(para, "epsilon", o.epsilon, false);
   o.stopRelChg = field(para, "stopRelChg", o.stopRelChg, false);
-  const mxArray *m0 = mxGetField(para, 0, "m0");
-  const mxArray *I0 = mxGetField(para, 0, "I0");
   const size_t N = (size_t)g.nx * g.ny * g.nz;
+  const double *m0 = image_field(para, "m0", N);
+  const double *I0 = image_field(para, "I0", N);
   mwSize dims[3] = {(mwSize)g.nx, (mwSize)g.ny, (mwSize)g.nz};
   plhs[0] = mxCreateNumericArray(3, dims, mxDOUBLE_CLASS, mxREAL);
   std::vector<double> rmse((size_t)(o.maxnumIter > 0 ? o.maxnumIter : 1));
   asdpocs_stats st;
   const int rc = ASD_POCS_cuda(
-      mxGetPr(P), mxGetPr(phi), &g, &o,
-      (m0 && mxGetNumberOfElements(m0) == N) ? mxGetPr(m0) : NULL,
-      (I0 && mxGetNumberOfElements(I0) == N) ? mxGetPr(I0) : NULL,
-      mxGetPr(plhs[0]), rmse.data(), &st);
+      mxGetPr(P), mxGetPr(phi), &g, &o, m0, I0, mxGetPr(plhs[0]), rmse.data(), &st);
   if (rc != 0) mexErrMsgTxt(asdpocs_last_error());
   if (nlhs > 1) {
     const char *names[] = {"IterationNum", "dataTolerance", "beta", "alpha", "RMSE"};
-    const int nf = (I0 && mxGetNumberOfElements(I0) == N) ? 5 : 4;
+    const int nf = I0 ? 5 : 4;
     plhs[1] = mxCreateStructMatrix(1, 1, nf, names);
     mxSetField(plhs[1], 0, "IterationNum", mxCreateDoubleScalar(st.IterationNum));
     mxSetField(plhs[1], 0, "dataTolerance", mxCreateDoubleScalar(st.dataTolerance));

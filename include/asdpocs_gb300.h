@@ -144,7 +144,8 @@ int asdpocs_tv_device(float *img_d, const float *img_old_d, int nx, int ny,
  * loop that must not stall on an allocation: the work images and reduction
  * scratch live in a fixed array of about 8.5 MB that every GPU loading the
  * library holds until exit.  Images are limited to nx*ny*nz <= 1,048,576
- * voxels (larger ones are rejected with ASDPOCS_ERR_ARG).  Asynchronous on
+ * voxels, to 65,536 tiles of 32 x 8 voxels and to 65,535 tile rows
+ * (ceil(ny/8) * nz); others are rejected with ASDPOCS_ERR_ARG.  Asynchronous on
  * `stream`; the first call on a device looks up the array's address and
  * should come before any stream capture.  All calls share the array, so
  * calls that overlap on the GPU race. */

@@ -2,9 +2,9 @@
 # Host build of the reference's OWN projector, gateway and TV sources -- the
 # strongest parity pin for the oracle (test infrastructure only).
 #
-# Compiles, straight from the reference checkout (default /root/reference,
-# override with ASDPOCS_REFERENCE_DIR), without copying any source into the
-# repository:
+# Compiles, straight from the reference checkout (ASDPOCS_REFERENCE_DIR, else
+# a checkout named "reference" beside the repository), without copying any
+# source into the repository:
 #   * src/AxAtx/Ax_cone_gpu.cu lines 1-297 and 339-776 (device functions and
 #     kernels; the cudaMalloc launchers are replaced by oracle/ref_shim_tail.inc)
 #     with the host shim oracle/ref_shim_head.h, as one translation unit;
@@ -17,7 +17,7 @@
 # prebuilt library).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${ASDPOCS_REFERENCE_DIR:-/root/reference}"
+REF="${ASDPOCS_REFERENCE_DIR:-$HERE/../../reference}"
 OUT="$HERE/_ref"
 CU="$REF/src/AxAtx/Ax_cone_gpu.cu"
 if [ ! -f "$CU" ]; then

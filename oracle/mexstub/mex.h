@@ -32,6 +32,7 @@ size_t mxGetN(const mxArray *a);
 size_t mxGetNumberOfElements(const mxArray *a);
 const mwSize *mxGetDimensions(const mxArray *a);
 mxClassID mxGetClassID(const mxArray *a);
+bool mxIsComplex(const mxArray *a);
 mxArray *mxGetField(const mxArray *s, mwIndex i, const char *name);
 mxArray *mxCreateDoubleMatrix(mwSize m, mwSize n, mxComplexity c);
 mxArray *mxCreateNumericMatrix(mwSize m, mwSize n, mxClassID cls,

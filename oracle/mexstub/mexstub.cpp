@@ -50,6 +50,8 @@ size_t mxGetN(const mxArray *a) {
 size_t mxGetNumberOfElements(const mxArray *a) { return numel(a); }
 const mwSize *mxGetDimensions(const mxArray *a) { return a->dims.data(); }
 mxClassID mxGetClassID(const mxArray *a) { return a->cls; }
+// stand-in arrays are always real
+bool mxIsComplex(const mxArray *) { return false; }
 mxArray *mxGetField(const mxArray *s, mwIndex, const char *name) {
   for (size_t i = 0; i < s->names.size(); i++)
     if (s->names[i] == name) return s->fields[i];

@@ -8,6 +8,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
+# The reference checkout, for the tests that read its sources or data where
+# it exists: ASDPOCS_REFERENCE_DIR, else a checkout named "reference" beside
+# the repository.
+REFERENCE = os.environ.get("ASDPOCS_REFERENCE_DIR") or os.path.join(
+    os.path.dirname(ROOT), "reference")
 
 
 def pytest_configure(config):

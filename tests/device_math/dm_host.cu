@@ -14,8 +14,8 @@
 //              conditions (staged=2), or the direct per-pair form;
 //   dm_chord_count / dm_atx_table -- the 2-D chord tables' layout, filled
 //              and read back;
-//   dm_atx3_zcol -- the cone-beam backward step walked down voxel columns
-//              (the form planned for the cone-beam kernel).
+//   dm_atx3_zcol -- the cone-beam backward step walked down voxel columns,
+//              as the z-column kernel runs it.
 // Compiled with -ffp-contract=off so the host compiler fuses nothing.
 #include <string.h>
 
@@ -273,76 +273,14 @@ extern "C" int dm_atx_table(float *x, const float *yv, float *sc, float c, float
   return 0;
 }
 
-// dm_atx3_zcol -- the cone-beam backward step as a walk down each (x, y)
-// voxel column, the form planned for the cone-beam kernel: what does not
-// depend on z is computed once per column -- the window's columns and its
-// magnification (one division), the shadow's columns and the four corners'
-// magnifications (four divisions), and for every detector column of the
-// shadow the in-plane parts of the x and y face tests -- and each voxel of
-// the column then needs its rows (multiply-adds) and the z parts of the face
-// tests.  The expressions are those of voxel_window, shadow_bins3 and
-// chord3_bf, split where they do not depend on z, so the result must be the
-// per-voxel form's bit for bit.  Narrowing conditions as dm_atx (staged=2).
-namespace {
-struct InPlane3 {
-  float xmy, xpy, ymx, ypx;
-  bool ixm, ixp, iym, iyp;
-};
-
-InPlane3 inplane3(const float4 A, float rx, float ry) {
-  InPlane3 p;
-  const float xt0 = A.z * (-rx) + ry, xu0 = A.z * 0.5f;
-  p.xmy = xt0 - xu0;
-  p.xpy = xt0 + xu0;
-  p.ixm = fabsf(p.xmy) <= 0.5f;
-  p.ixp = fabsf(p.xpy) <= 0.5f;
-  const float yt0 = A.w * (-ry) + rx, yu0 = A.w * 0.5f;
-  p.ymx = yt0 - yu0;
-  p.ypx = yt0 + yu0;
-  p.iym = fabsf(p.ymx) <= 0.5f;
-  p.iyp = fabsf(p.ypx) <= 0.5f;
-  return p;
-}
-
-// chord3_bf for a ray with a != 0 and b != 0, from its in-plane parts.
-float chord3_z(const float4 A, const InPlane3 &p, const float4 Cs, float rx, float ry,
-               float rz, float dz) {
-  const float hz = dz / 2.0f;
-  const float xt1 = Cs.x * (-rx) + rz, xu1 = Cs.x * 0.5f;
-  const float xmz = xt1 - xu1, xpz = xt1 + xu1;
-  const bool fxm = p.ixm && fabsf(xmz) <= hz;
-  const bool fxp = p.ixp && fabsf(xpz) <= hz;
-  const float yt1 = Cs.y * (-ry) + rz, yu1 = Cs.y * 0.5f;
-  const float ymz = yt1 - yu1, ypz = yt1 + yu1;
-  const bool fym = p.iym && fabsf(ymz) <= hz;
-  const bool fyp = p.iyp && fabsf(ypz) <= hz;
-  const float zt0 = Cs.z * (-rz) + rx, zu0 = Cs.z * hz;
-  const float zt1 = Cs.w * (-rz) + ry, zu1 = Cs.w * hz;
-  const float zmx = zt0 - zu0, zmy = zt1 - zu1, zpx = zt0 + zu0, zpy = zt1 + zu1;
-  const bool fzm = fabsf(zmx) <= 0.5f && fabsf(zmy) <= 0.5f;
-  const bool fzp = fabsf(zpx) <= 0.5f && fabsf(zpy) <= 0.5f;
-  Pick2Rev q;
-  q.n = 0;
-  q.p0x = q.p0y = q.p0z = q.p1x = q.p1y = q.p1z = 0.f;
-  q.put(fzp, zpx, zpy, hz);
-  q.put(fzm, zmx, zmy, -hz);
-  if (fabsf(A.x) > fabsf(A.y)) {
-    q.put(fyp, p.ypx, 0.5f, ypz);
-    q.put(fym, p.ymx, -0.5f, ymz);
-    q.put(fxp, 0.5f, p.xpy, xpz);
-    q.put(fxm, -0.5f, p.xmy, xmz);
-  } else {
-    q.put(fxp, 0.5f, p.xpy, xpz);
-    q.put(fxm, -0.5f, p.xmy, xmz);
-    q.put(fyp, p.ypx, 0.5f, ypz);
-    q.put(fym, p.ymx, -0.5f, ymz);
-  }
-  if (q.n < 2) return 0.0f;
-  const float e0 = q.p1x - q.p0x, e1 = q.p1y - q.p0y, e2 = q.p1z - q.p0z;
-  return sqrtf(e0 * e0 + e1 * e1 + e2 * e2);
-}
-}  // namespace
-
+// dm_atx3_zcol -- the cone-beam backward step walked down each (x, y) voxel
+// column as the z-column kernel runs it: the window's and shadow's columns,
+// the corners' magnifications and, for every detector column of the shadow,
+// the in-plane part of the x and y face tests (col_faces) once per column;
+// each voxel then needs its rows (zcol_rows) and the z parts of the face
+// tests (chord3_col).  Columns with three or more in-plane hits use
+// chord3_axis.  Narrowing conditions as dm_atx (staged=2); views that do not
+// allow narrowing take the per-voxel form.
 extern "C" void dm_atx3_zcol(float *x, const float *yv, float *sc, float c, float s,
                              const float *yd, const float *zd, float SO, float OD,
                              float scale, float ddy, float ddz, float dz, int nx, int ny,
@@ -357,80 +295,36 @@ extern "C" void dm_atx3_zcol(float *x, const float *yv, float *sc, float c, floa
     narrow = narrow && tA[ia].x != 0.0f && tA[ia].y != 0.0f && on_grid(yd[ia], ia, na, ddy);
   for (int ib = 0; ib < nb; ib++) narrow = narrow && on_grid(zd[ib], ib, nb, ddz);
   for (long long k = 0; k < (long long)na * nb; k++) narrow = narrow && isfinite(yv[k]);
-  const int na2 = na / 2, nb2 = nb / 2, nx2 = nx / 2, ny2 = ny / 2, nz2 = nz / 2;
-  const float hz = 0.5f * G.dz;
-  const float inv_a = hd_rcp(G.dy_det), inv_b = hd_rcp(G.dz_det);
-  const float offa = na * 0.5f - 0.5f, offb = nb * 0.5f - 0.5f;
-  std::vector<InPlane3> ip(na);
+  if (!narrow) {
+    dm_atx(x, yv, sc, c, s, yd, zd, SO, OD, scale, ddy, ddz, dz, nx, ny, nz, na, nb, 1);
+    return;
+  }
+  const float hz = dz / 2.0f;
+  std::vector<ColFaces> cf(na);
   for (int iy = 0; iy < ny; iy++)
     for (int ix = 0; ix < nx; ix++) {
-      // ---- once per column: voxel_window's columns and magnification
-      const float yc = (float)(iy - ny2) + 0.5f, xc = (float)(ix - nx2) + 0.5f;
-      const float xr = G.cos_phi * xc + G.sin_phi * yc;
-      const float yr = -G.sin_phi * xc + G.cos_phi * yc;
-      const float ta = G.SD / ((xr + G.SO) * G.dy_det);
-      const float tb = G.dz_det != G.dy_det ? G.SD / ((xr + G.SO) * G.dz_det) : ta;
-      const int amax = (int)floorf((yr + 1) * ta + na2);
-      const int amin = (int)floorf((yr - 1) * ta + na2);
-      const int a0 = amin > 0 ? amin : 0, a1 = amax < na - 1 ? amax : na - 1;
-      // shadow_bins3's columns and its corners' magnifications
-      const float hc = 0.5f * G.cos_phi, hs = 0.5f * G.sin_phi;
-      float q[4], umin = 3.0e38f, umax = -3.0e38f;
-      bool ok = true;
-      for (int k = 0; k < 4; k++) {
-        const float ex = (k & 1) ? 1.f : -1.f, ey = (k & 2) ? 1.f : -1.f;
-        const float px = xr + ex * hc + ey * hs;
-        const float py = yr - ex * hs + ey * hc;
-        const float den = px + G.SO;
-        ok = ok && den > 1e-3f;
-        q[k] = fast_div(G.SD, den);
-        const float u = py * q[k] * inv_a + offa;
-        umin = fminf(umin, u);
-        umax = fmaxf(umax, u);
-      }
-      int lo = a0, hi = a1;
-      const bool nar = narrow && ok;
-      if (nar) {
-        const int alo = (int)ceilf(umin - 0.05f), ahi = (int)floorf(umax + 0.05f);
-        lo = lo > alo ? lo : alo;
-        hi = hi < ahi ? hi : ahi;
-      }
-      const float rx = G.cos_phi * (-G.SO) - xc;
-      const float ry = G.sin_phi * (-G.SO) - yc;
-      for (int ia = lo; ia <= hi; ia++) ip[ia] = inplane3(tA[ia], rx, ry);
-      // ---- per voxel of the column: rows and the z parts
+      const ZCol col = zcol_setup(G, D, ix, iy, true);
+      const int cntA = col.lo <= col.hi ? col.hi - col.lo + 1 : 0;
+      for (int k = 0; k < cntA; k++) cf[k] = col_faces(tA[col.lo + k], col.rx, col.ry);
       for (int iz = 0; iz < nz; iz++) {
-        const float zc = ((float)(iz - nz2) + 0.5f) * G.dz;
-        const int bmax = (int)floorf((zc + G.dwin) * tb + nb2);
-        const int bmin = (int)floorf((zc - G.dwin) * tb + nb2);
-        int blo = bmin > 0 ? bmin : 0, bhi = bmax < nb - 1 ? bmax : nb - 1;
-        float acc = 0.f, accl = 0.f;
-        const bool has = a0 <= a1 && blo <= bhi;
-        if (has && nar) {
-          const float zlo = (zc - hz) * inv_b, zhi = (zc + hz) * inv_b;
-          float vmin = 3.0e38f, vmax = -3.0e38f;
-          for (int k = 0; k < 4; k++) {
-            const float v0 = zlo * q[k] + offb, v1 = zhi * q[k] + offb;
-            vmin = fminf(vmin, fminf(v0, v1));
-            vmax = fmaxf(vmax, fmaxf(v0, v1));
-          }
-          const int tlo = (int)ceilf(vmin - 0.05f), thi = (int)floorf(vmax + 0.05f);
-          blo = blo > tlo ? blo : tlo;
-          bhi = bhi < thi ? bhi : thi;
-        }
+        float zc;
+        int blo, bhi;
+        const bool has = zcol_rows(G, D, col, iz, zc, blo, bhi);
+        const int cntB = has && blo <= bhi ? bhi - blo + 1 : 0;
         const float rz = 0.0f - zc;
-        if (has)
-          for (int ib = blo; ib <= bhi; ib++) {
-            const float cc = zd[ib] - 0.0f;
-            for (int ia = lo; ia <= hi; ia++) {
-              const long long k = (long long)ib * na + ia;
-              const float4 A = tA[ia];
-              const float l = (A.x != 0.0f && A.y != 0.0f)
-                                  ? chord3_z(A, ip[ia], tC[k], rx, ry, rz, dz)
-                                  : chord3_bf(A, tC[k], cc, rx, ry, rz, dz);
-              acc += l * yv[k];
-              accl += l;
-            }
+        float acc = 0.f, accl = 0.f;
+        for (int kb = 0; kb < (has ? cntB : 0); kb++)
+          for (int ka = 0; ka < cntA; ka++) {
+            const long long r = (long long)(blo + kb) * na + col.lo + ka;
+            const ColFaces &f = cf[ka];
+            float l;
+            if (f.bits & kCfMany)
+              l = (f.bits & kCfXF) ? chord3_axis<true>(tA[col.lo + ka], tC[r], col.rx, col.ry, rz, dz)
+                                   : chord3_axis<false>(tA[col.lo + ka], tC[r], col.rx, col.ry, rz, dz);
+            else
+              l = chord3_col(f, tC[r], col.rx, col.ry, rz, hz);
+            acc += l * yv[r];
+            accl += l;
           }
         const long long idx = ((long long)iz * ny + iy) * nx + ix;
         x[idx] = acc * scale;

@@ -37,6 +37,10 @@ def extract(ref_root):
 
 
 if __name__ == "__main__":
+    # the reference checkout: an argument, ASDPOCS_REFERENCE_DIR, else a
+    # checkout named "reference" beside the repository
     root = (sys.argv[1] if len(sys.argv) > 1
-            else os.environ.get("ASDPOCS_REFERENCE_DIR", "/root/reference"))
+            else os.environ.get("ASDPOCS_REFERENCE_DIR")
+            or os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(HERE))),
+                            "reference"))
     np.savez_compressed(os.path.join(HERE, "realdata.npz"), **extract(root))

@@ -15,7 +15,9 @@ STUB = os.path.join(ROOT, "oracle", "mexstub")
 GW = os.path.join(ROOT, "asd_pocs_mex_cuda_demo_gb300", "mex")
 LIBDIR = os.path.join(ROOT, "asd_pocs_mex_cuda_demo_gb300", "lib")
 OUT = os.path.join(HERE, "_build")
-REF = os.environ.get("ASDPOCS_REFERENCE_DIR", "/root/reference")
+# the reference checkout: ASDPOCS_REFERENCE_DIR, else "reference" beside the repository
+REF = os.environ.get("ASDPOCS_REFERENCE_DIR") or os.path.join(os.path.dirname(ROOT),
+                                                                "reference")
 
 GATEWAYS = [("imgTVGradMin_gb300.cpp", "gw_tv2d"), ("imgTVGradMin3D_gb300.cpp", "gw_tv3d"),
             ("ASD_POCS_gb300.cpp", "gw_asdpocs")]

@@ -7,7 +7,7 @@ import subprocess
 
 import pytest
 
-from conftest import ROOT
+from conftest import REFERENCE, ROOT
 
 
 def _declared():
@@ -58,7 +58,7 @@ def test_launcher_signatures_match_reference_arity():
 
 
 def test_ref_signatures_in_reference_source_if_present():
-    ref = "/root/reference/src/AxAtx/Ax_cone_gpu.cu"
+    ref = os.path.join(REFERENCE, "src", "AxAtx", "Ax_cone_gpu.cu")
     if not os.path.exists(ref):
         pytest.skip("reference checkout not on this machine")
     src = open(ref, encoding="latin-1").read()

@@ -40,6 +40,13 @@ def test_tv_argument_checks(lib):
         pkg.imgTVGradMin3D(np.zeros((4, 4, 1)), 0.1, 2, 1)
 
 
+def test_tv_rejects_images_beyond_one_launch(lib):
+    """A thin volume whose TV tile grid would need more than 65535 launch rows
+    (ceil(ny/8) * nz) is rejected with a clear message before device work."""
+    with pytest.raises(pkg.AsdpocsError, match="tile rows"):
+        pkg.imgTVGradMin3D(np.zeros((4, 1, 65536)), 0.1, 2, 1)
+
+
 def test_bad_dimensions_are_rejected_before_device_work(lib):
     p = dict(PARA, nx=0)
     with pytest.raises(pkg.AsdpocsError, match="dimensions must be positive"):

@@ -35,6 +35,21 @@ def test_gateway_argument_errors_without_gpu(gw):
         m.call(fns["asdpocs"], [np.zeros((4, 2))], nlhs=2)
     with pytest.raises(RuntimeError, match="parameter.SO"):
         m.call(fns["asdpocs"], [np.zeros((4, 2)), dict(nx=2, ny=2, nz=1, na=4, nb=1)], nlhs=2)
+    para = dict(nx=2, ny=2, nz=1, na=4, nb=1, SO=541.0, OD=408.0, vxlsize=1.0, detsize=1.0,
+                phi_vec=[0.0, 90.0])
+    # a sinogram with too few rows for na*nb rays per view is refused before
+    # anything reads it (the reference fails on P(:,ii) - proj)
+    with pytest.raises(RuntimeError, match="na\\*nb rows"):
+        m.call(fns["asdpocs"], [np.zeros((3, 2)), para], nlhs=2)
+    with pytest.raises(RuntimeError, match="real double matrix"):
+        m.call(fns["asdpocs"], [np.zeros((4, 2), np.float32), para], nlhs=2)
+    with pytest.raises(RuntimeError, match="phi_vec mismatch"):
+        m.call(fns["asdpocs"], [np.zeros((4, 3)), para], nlhs=2)
+    # m0 / I0 of the wrong size are refused, not silently ignored
+    for name in ("m0", "I0"):
+        with pytest.raises(RuntimeError, match=f"parameter.{name} must be"):
+            m.call(fns["asdpocs"], [np.zeros((4, 2)), dict(para, **{name: np.ones(3)})],
+                   nlhs=2)
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(harness.REF, "src", "AxAtx",

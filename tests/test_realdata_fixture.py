@@ -8,9 +8,8 @@ import sys
 import numpy as np
 import pytest
 
+from conftest import REFERENCE as REF
 from conftest import ROOT, golden
-
-REF = os.environ.get("ASDPOCS_REFERENCE_DIR", "/root/reference")
 
 
 def test_swine_constants_match_driver():

@@ -56,3 +56,9 @@ def test_noalloc_tv_rejects_images_over_its_limit(gpu):
     with pytest.raises(AsdpocsError, match="1048576-voxel limit"):
         check(L.asdpocs_tv_device_noalloc(big.data_ptr(), None, 1025, 1024, 1, 0.2, 3, 1,
                                           torch.cuda.current_stream().cuda_stream))
+    # a thin image within the voxel and tile limits whose tile rows
+    # (ceil(ny/8) * nz = 65536) exceed what one launch can hold
+    thin = torch.zeros(16 * 65536, device=gpu)
+    with pytest.raises(AsdpocsError, match="tile rows"):
+        check(L.asdpocs_tv_device_noalloc(thin.data_ptr(), None, 16, 1, 65536, 0.2, 3, 1,
+                                          torch.cuda.current_stream().cuda_stream))
