@@ -17,9 +17,10 @@ from ._lib import AsdpocsError, load  # noqa: F401
 from .asdpocs import ASD_POCS_cuda, Plan, SART_cuda_inline  # noqa: F401
 from .serve import Server  # noqa: F401
 from .mex import (Atx_cone_gpu, Atx_cone_mf_gpu_new, Ax_cone_gpu,  # noqa: F401
-                  Ax_cone_mf_gpu_new, MexError, adjoint_check, imgTVGradMin,
-                  imgTVGradMin3D)
+                  Ax_cone_mf_gpu_new, Ax_siddon_mf_gpu, MexError, adjoint_check,
+                  imgTVGradMin, imgTVGradMin3D)
 
 __all__ = ["Ax_cone_gpu", "Atx_cone_gpu", "imgTVGradMin", "imgTVGradMin3D",
            "ASD_POCS_cuda", "SART_cuda_inline", "Plan", "Server", "Ax_cone_mf_gpu_new",
-           "Atx_cone_mf_gpu_new", "MexError", "AsdpocsError", "load", "adjoint_check"]
+           "Atx_cone_mf_gpu_new", "Ax_siddon_mf_gpu", "MexError", "AsdpocsError", "load",
+           "adjoint_check"]

@@ -32,7 +32,13 @@ class Options(C.Structure):
     _fields_ = [("maxnumIter", C.c_int), ("numOfgradients", C.c_int),
                 ("alpha", C.c_double), ("alpha_red", C.c_double), ("beta", C.c_double),
                 ("beta_red", C.c_double), ("r_max", C.c_double), ("epsilon", C.c_double),
-                ("stopRelChg", C.c_double)]
+                ("stopRelChg", C.c_double), ("sino_storage", C.c_int), ("ax_mode", C.c_int)]
+
+
+# asdpocs_options.sino_storage: device storage of the sinogram
+SINO_STORAGE = {"f32": 0, "f16": 1, "bf16": 2}
+# asdpocs_options.ax_mode: forward projection of the SART steps
+AX_MODE = {"reference": 0, "exact": 1}
 
 
 class Stats(C.Structure):
@@ -72,6 +78,13 @@ SIGNATURES = [
                                     C.c_float, C.c_void_p, C.c_void_p, C.c_float,
                                     C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
                                     C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("asdpocs_ax_siddon", C.c_int, [_F, _F, _F, C.c_float, C.c_float, _F, _F, C.c_float,
+                                    C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
+                                    C.c_int, C.c_int, C.c_int]),
+    ("asdpocs_ax_siddon_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
+                                           C.c_float, C.c_void_p, C.c_void_p, C.c_float,
+                                           C.c_float, C.c_float, C.c_float, C.c_int,
+                                           C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     ("asdpocs_atx_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_float,
                                      C.c_float, C.c_void_p, C.c_void_p, C.c_float,
                                      C.c_float, C.c_float, C.c_float, C.c_float,
@@ -95,6 +108,7 @@ SIGNATURES = [
                                             C.c_int, C.c_double, C.c_int, C.c_int,
                                             C.c_void_p]),
     ("asdpocs_options_default", None, [C.POINTER(Options)]),
+    ("asdpocs_store_sinogram", C.c_int, [C.c_void_p, C.c_void_p, C.c_ulonglong, C.c_int]),
     ("asdpocs_plan_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int,
                                       C.POINTER(Geometry), _D, C.POINTER(Options),
                                       C.c_ulonglong, C.c_void_p]),

@@ -13,7 +13,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import AsdpocsError, Geometry, Options, Stats, check, load
+from ._lib import AX_MODE, SINO_STORAGE, AsdpocsError, Geometry, Options, Stats, check, load
 
 _D = C.POINTER(C.c_double)
 _EPS = float(np.finfo(np.float64).eps)
@@ -37,6 +37,12 @@ def options_from_para(para: dict) -> Options:
     o.r_max = float(get("r_max", 0.95))
     o.epsilon = float(get("epsilon", _EPS))
     o.stopRelChg = float(get("stopRelChg", _EPS))
+    # not in the reference: "f32" (default), "f16" or "bf16" device storage of P
+    s = get("sino_storage", "f32")
+    o.sino_storage = SINO_STORAGE[s] if isinstance(s, str) else int(s)
+    # not in the reference: "reference" column march (default) or "exact" Siddon
+    a = get("ax_mode", "reference")
+    o.ax_mode = AX_MODE[a] if isinstance(a, str) else int(a)
     return o
 
 
@@ -275,7 +281,9 @@ class Plan:
         check(load().asdpocs_plan_set_tv_walk(self._h, int(walk)))
 
     def sinogram_ptr(self, inst: int) -> int:
-        return int(load().asdpocs_plan_sinogram_ptr(self._h, inst))
+        """Device pointer of the instance's FP32 sinogram; 0 for FP16 / BF16
+        storage (load those through set_sinogram)."""
+        return int(load().asdpocs_plan_sinogram_ptr(self._h, inst) or 0)
 
     def image_ptr(self, inst: int) -> int:
         return int(load().asdpocs_plan_image_ptr(self._h, inst))

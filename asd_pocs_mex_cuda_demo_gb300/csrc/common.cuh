@@ -1,5 +1,7 @@
 // Shared definitions of the asdpocs_gb300 library (internal).
 #pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -75,7 +77,8 @@ struct Inst {
                              // for its largest instance)
   ViewGeo g;                 // geometry (cos/sin filled per view from trig)
   const float2 *trig;        // [nv] (cos_phi, sin_phi) per view
-  const float *P;            // sinogram, view-major, na*nb*nv
+  const void *P;             // sinogram, view-major, na*nb*nv, stored as
+  int p_fmt;                 //   ASDPOCS_STORE_F32 / _F16 / _BF16 (sino_at)
   float *m;                  // current image (A)
   float *m_pre;              // image at sweep start
   float *m_res;              // post-SART snapshot (returned image)
@@ -104,6 +107,18 @@ struct Inst {
   unsigned *counter;         // reduction ticket
   Scalars *s;
 };
+
+// Sinogram value i of an instance, widened to FP32 from its storage.
+__device__ __forceinline__ float sino_at(const Inst &I, long long i) {
+  if (I.p_fmt == ASDPOCS_STORE_F16) return __half2float(((const __half *)I.P)[i]);
+  if (I.p_fmt == ASDPOCS_STORE_BF16) return __bfloat162float(((const __nv_bfloat16 *)I.P)[i]);
+  return ((const float *)I.P)[i];
+}
+
+// Bytes of one stored sinogram value.
+__host__ __device__ inline size_t sino_elem_bytes(int fmt) {
+  return fmt == ASDPOCS_STORE_F32 ? 4 : 2;
+}
 
 constexpr int kMaxPartials = 1 << 22;  // blocks per reduction (sanity bound)
 

@@ -140,11 +140,10 @@ int asdpocs_last_status(void) { return g_status; }
 const char *asdpocs_version(void) { return "asdpocs_gb300 0.1 (sm_103a)"; }
 
 // ------------------------------------------------------------ projectors
-int asdpocs_ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
-                      float sin_phi, const float *y_det_d,
-                      const float *z_det_d, float SO, float OD, float scale,
-                      float dz, int nx, int ny, int nz, int na, int nb,
-                      void *stream) {
+static int ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
+                     float sin_phi, const float *y_det_d, const float *z_det_d, float SO,
+                     float OD, float scale, float dz, int nx, int ny, int nz, int na,
+                     int nb, void *stream, bool exact) {
   clear_error();
   if (int e = check_dims(nx, ny, nz, na, nb)) return e;
   if (!x_d || !y_d || !sr_d || !y_det_d || !z_det_d)
@@ -152,8 +151,28 @@ int asdpocs_ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
   const ViewGeo g = with_constants(
       ViewGeo{cos_phi, sin_phi, SO, OD, scale, 0.f, 0.f, dz, y_det_d, z_det_d});
   Dims d{nx, ny, nz, na, nb};
-  ASD_CUDA(launch_ax(x_d, y_d, sr_d, g, d, (cudaStream_t)stream));
+  if (exact)
+    ASD_CUDA(launch_ax_siddon(x_d, y_d, sr_d, g, d, (cudaStream_t)stream));
+  else
+    ASD_CUDA(launch_ax(x_d, y_d, sr_d, g, d, (cudaStream_t)stream));
   return 0;
+}
+
+int asdpocs_ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
+                      float sin_phi, const float *y_det_d,
+                      const float *z_det_d, float SO, float OD, float scale,
+                      float dz, int nx, int ny, int nz, int na, int nb,
+                      void *stream) {
+  return ax_device(x_d, y_d, sr_d, cos_phi, sin_phi, y_det_d, z_det_d, SO, OD, scale, dz, nx,
+                   ny, nz, na, nb, stream, false);
+}
+
+int asdpocs_ax_siddon_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
+                             float sin_phi, const float *y_det_d, const float *z_det_d,
+                             float SO, float OD, float scale, float dz, int nx, int ny,
+                             int nz, int na, int nb, void *stream) {
+  return ax_device(x_d, y_d, sr_d, cos_phi, sin_phi, y_det_d, z_det_d, SO, OD, scale, dz, nx,
+                   ny, nz, na, nb, stream, true);
 }
 
 int asdpocs_atx_device(float *x_d, const float *y_d, float *sc_d,
@@ -175,7 +194,7 @@ int asdpocs_atx_device(float *x_d, const float *y_d, float *sc_d,
 static int ax_host(const float *X, float *y, float *sr, float cos_phi,
                    float sin_phi, const float *y_det, const float *z_det,
                    float SO, float OD, float scale, float dz, int nx, int ny,
-                   int nz, int na, int nb) {
+                   int nz, int na, int nb, bool exact = false) {
   clear_error();
   if (int e = check_dims(nx, ny, nz, na, nb)) return e;
   if (!X || !y || !sr || !y_det || !z_det)
@@ -195,7 +214,12 @@ static int ax_host(const float *X, float *y, float *sr, float cos_phi,
                                            0.f, dz, (const float *)(b + oA),
                                            (const float *)(b + oB)});
   Dims d{nx, ny, nz, na, nb};
-  ASD_CUDA(launch_ax((const float *)(b + oX), (float *)(b + oY), (float *)(b + oS), g, d, w->st));
+  if (exact)
+    ASD_CUDA(launch_ax_siddon((const float *)(b + oX), (float *)(b + oY), (float *)(b + oS), g,
+                              d, w->st));
+  else
+    ASD_CUDA(launch_ax((const float *)(b + oX), (float *)(b + oY), (float *)(b + oS), g, d,
+                       w->st));
   ASD_CUDA(cudaMemcpyAsync(y, b + oY, M * 4, cudaMemcpyDeviceToHost, w->st));
   ASD_CUDA(cudaMemcpyAsync(sr, b + oS, M * 4, cudaMemcpyDeviceToHost, w->st));
   ASD_CUDA(cudaStreamSynchronize(w->st));
@@ -377,6 +401,14 @@ void Ax_cone_mf_gpu_new(float *X, float *y, float *sr, float cos_phi,
           nz, na, nb);
 }
 
+int asdpocs_ax_siddon(const float *X, float *y, float *sr, float cos_phi,
+                      float sin_phi, const float *y_det, const float *z_det,
+                      float SO, float OD, float scale, float dz, int nx, int ny,
+                      int nz, int na, int nb) {
+  return ax_host(X, y, sr, cos_phi, sin_phi, y_det, z_det, SO, OD, scale, dz, nx, ny, nz,
+                 na, nb, true);
+}
+
 void Atx_cone_mf_gpu_new(float *X, float *y, float *sc, float cos_phi,
                          float sin_phi, float *y_det, float *z_det, float SO,
                          float OD, float scale, float dy_det, float dz_det,
@@ -535,6 +567,17 @@ void asdpocs_options_default(asdpocs_options *o) {
   o->r_max = 0.95;
   o->epsilon = 2.220446049250313e-16;
   o->stopRelChg = 2.220446049250313e-16;
+  o->sino_storage = ASDPOCS_STORE_F32;
+  o->ax_mode = ASDPOCS_AX_REFERENCE;
+}
+
+int asdpocs_store_sinogram(const float *in, void *out, unsigned long long n, int storage) {
+  clear_error();
+  if (n && (!in || !out)) return set_error(ASDPOCS_ERR_ARG, "null pointer");
+  if (storage < ASDPOCS_STORE_F32 || storage > ASDPOCS_STORE_BF16)
+    return set_error(ASDPOCS_ERR_ARG, "unknown sinogram storage %d", storage);
+  store_sinogram_host(in, out, (size_t)n, storage);
+  return 0;
 }
 
 }  // extern "C"
@@ -573,6 +616,7 @@ struct asdpocs_plan_s {
   std::vector<int> has_ref;
   bool shared = false;  // all instances share sizes, geometry and angles
   bool zcol = true;     // cone beams: z-column backward step (else per voxel)
+  bool exact = false;   // forward steps: exact Siddon projection (ax_mode)
   int tv_walk = 0;      // TV walk length (0: from the batch size)
   Inst *d_inst = nullptr;
   void *arena = nullptr;
@@ -592,8 +636,56 @@ int instance_kind(const asdpocs_geometry &g) {
   return g.nz > 1 ? 2 : (g.nb > 1 ? 1 : 0);
 }
 
+// FP32 to FP16, round to nearest with ties to even (IEEE 754 binary16).
+static uint16_t f32_to_f16(float f) {
+  uint32_t x;
+  memcpy(&x, &f, 4);
+  const uint32_t sign = (x >> 16) & 0x8000u;
+  const uint32_t ax = x & 0x7fffffffu;
+  if (ax > 0x7f800000u) return (uint16_t)(sign | 0x7e00u | ((ax >> 13) & 0x3ffu));  // NaN
+  if (ax >= 0x477ff000u) return (uint16_t)(sign | 0x7c00u);  // rounds to inf (or is inf)
+  if (ax >= 0x38800000u) {  // normal half: rebias the exponent, round 13 bits
+    const uint32_t m = ax - 0x38000000u;  // exponent 127 -> 15
+    const uint32_t r = (m >> 13) + (((m >> 12) & 1u) & (((m & 0xfffu) != 0) | ((m >> 13) & 1u)));
+    return (uint16_t)(sign | r);
+  }
+  if (ax < 0x33000000u) return (uint16_t)sign;  // below half the smallest subnormal
+  // subnormal half: value = mant * 2^-24 with the implicit bit restored
+  const uint32_t e = ax >> 23;              // 102 .. 112
+  const uint32_t mant = (ax & 0x7fffffu) | 0x800000u;
+  const uint32_t shift = 126 - e;           // bits dropped: 14 .. 24
+  const uint32_t q = mant >> shift, rem = mant & ((1u << shift) - 1u), half = 1u << (shift - 1);
+  const uint32_t r = q + ((rem > half) || (rem == half && (q & 1u)) ? 1u : 0u);
+  return (uint16_t)(sign | r);
+}
+
+// FP32 to BF16, round to nearest with ties to even; NaN stays NaN.
+static uint16_t f32_to_bf16(float f) {
+  uint32_t x;
+  memcpy(&x, &f, 4);
+  if ((x & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((x >> 16) | 0x40u);
+  const uint32_t r = x + 0x7fffu + ((x >> 16) & 1u);
+  return (uint16_t)(r >> 16);
+}
+
+void store_sinogram_host(const float *in, void *out, size_t n, int fmt) {
+  if (fmt == ASDPOCS_STORE_F32) {
+    memcpy(out, in, n * 4);
+    return;
+  }
+  uint16_t *o = (uint16_t *)out;
+  if (fmt == ASDPOCS_STORE_F16)
+    for (size_t i = 0; i < n; i++) o[i] = f32_to_f16(in[i]);
+  else
+    for (size_t i = 0; i < n; i++) o[i] = f32_to_bf16(in[i]);
+}
+
 int check_instance(const asdpocs_geometry &g, const asdpocs_options &o) {
   if (int e = check_dims(g.nx, g.ny, g.nz, g.na, g.nb)) return e;
+  if (o.sino_storage < ASDPOCS_STORE_F32 || o.sino_storage > ASDPOCS_STORE_BF16)
+    return set_error(ASDPOCS_ERR_ARG, "unknown sinogram storage %d", o.sino_storage);
+  if (o.ax_mode != ASDPOCS_AX_REFERENCE && o.ax_mode != ASDPOCS_AX_EXACT)
+    return set_error(ASDPOCS_ERR_ARG, "unknown forward mode %d", o.ax_mode);
   if (g.nv <= 0) return set_error(ASDPOCS_ERR_ARG, "nv must be positive");
   if (o.maxnumIter < 0 || o.numOfgradients < 0)
     return set_error(ASDPOCS_ERR_ARG, "negative iteration counts");
@@ -601,7 +693,8 @@ int check_instance(const asdpocs_geometry &g, const asdpocs_options &o) {
 }
 
 InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
-                           size_t cor_floats, int parts, size_t il_floats) {
+                           size_t cor_floats, int parts, size_t il_floats,
+                           int sino_storage) {
   const Dims d{g.nx, g.ny, g.nz, g.na, g.nb};
   const size_t N = (size_t)g.nx * g.ny * g.nz;
   const size_t M = (size_t)g.na * g.nb;
@@ -611,7 +704,8 @@ InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
   const bool proj3d = g.nz > 1 || g.nb > 1;
   InstLayout o;
   size_t off = 0;
-  o.P = off; off += st ? align256(M * g.nv * 4) : 0;
+  o.p_fmt = sino_storage;
+  o.P = off; off += st ? align256(M * g.nv * sino_elem_bytes(sino_storage)) : 0;
   o.m = off; off += per_img;
   o.m_pre = off; off += per_img;
   o.m_res = off; off += per_img;
@@ -639,7 +733,8 @@ InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
 }
 
 void bind_state(Inst &I, char *b, const InstLayout &o) {
-  I.P = (const float *)(b + o.P);
+  I.P = (const void *)(b + o.P);
+  I.p_fmt = o.p_fmt;
   I.m = (float *)(b + o.m);
   I.m_pre = (float *)(b + o.m_pre);
   I.m_res = (float *)(b + o.m_res);
@@ -732,12 +827,12 @@ namespace asd {
 
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk, bool finish, bool zcol) {
+                              int tv_walk, bool finish, bool zcol, bool exact) {
   cudaError_t e = cudaSuccess;
   if (shared) e = launch_group_pack(d_inst, batch, d, 0, st);
   for (int v = 0; v < nv && e == cudaSuccess; v++) {
     e = shared ? launch_sart_ax_shared(d_inst, batch, d, v, st)
-               : launch_sart_ax(d_inst, batch, d, v, st);
+               : launch_sart_ax(d_inst, batch, d, v, st, exact);
     if (e == cudaSuccess)
       e = shared ? launch_sart_atx_shared(d_inst, batch, d, v, st)
                  : launch_sart_atx(d_inst, batch, d, v, st, zcol);
@@ -753,7 +848,7 @@ cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
 // One iteration of sub-batch s on its stream.
 static int plan_enqueue_sub(asdpocs_plan p, const SubBatch &s) {
   ASD_CUDA(enqueue_iteration(p->d_inst + s.first, s.count, s.d, s.nv, s.max_ng, p->shared,
-                             s.st, p->tv_walk, s.min_ng < 2, p->zcol));
+                             s.st, p->tv_walk, s.min_ng < 2, p->zcol, p->exact));
   return 0;
 }
 
@@ -934,6 +1029,16 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
                 memcmp(phi_vec_deg, phi_vec_deg + phi_off[i],
                        sizeof(double) * (size_t)g0.nv) == 0;
   }
+  // forward mode: one per plan; the shared-geometry forward step runs the
+  // reference's march only, so exact plans run every instance on its own
+  for (int i = 0; i < batch; i++)
+    if (p->opt[i].ax_mode != p->opt[0].ax_mode) {
+      delete p;
+      return set_error(ASDPOCS_ERR_ARG,
+                       "the instances of a plan must share one forward mode (ax_mode)");
+    }
+  p->exact = p->opt[0].ax_mode == ASDPOCS_AX_EXACT;
+  if (p->exact) p->shared = false;
   if (getenv("ASDPOCS_NO_SHARED_GEOMETRY")) p->shared = false;
   // ASDPOCS_CONE_ATX=voxel: the per-voxel form of the cone-beam backward step
   // (same results; kept for comparison)
@@ -967,7 +1072,8 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     const bool first = p->shared && i % kShareSlots == 0;
     const size_t N = (size_t)geom[i].nx * geom[i].ny * geom[i].nz;
     lay[i] = layout_instance(geom[i], p->opt[i].maxnumIter, first ? M * kShareSlots : M,
-                             kLayoutState | kLayoutGeometry, first ? N * kShareSlots : 0);
+                             kLayoutState | kLayoutGeometry, first ? N * kShareSlots : 0,
+                             p->opt[i].sino_storage);
     base[i] = off;
     off += lay[i].bytes;
   }
@@ -1079,8 +1185,17 @@ int asdpocs_plan_set_sinogram(asdpocs_plan p, int inst, const float *P,
   if (int e = plan_check(p, inst)) return e;
   if (!P) return set_error(ASDPOCS_ERR_ARG, "null sinogram");
   const Inst &I = p->h_inst[inst];
-  const size_t bytes = (size_t)I.d.na * I.d.nb * I.nv * 4;
-  return plan_put(p, (void *)I.P, P, bytes, where);
+  const size_t n = (size_t)I.d.na * I.d.nb * I.nv;
+  if (I.p_fmt == ASDPOCS_STORE_F32) return plan_put(p, (void *)I.P, P, n * 4, where);
+  // FP16 / BF16 storage: rounded on the device from a device sinogram, on
+  // the host from a host one (the same bits either way)
+  if (where) {
+    ASD_CUDA(launch_store_sinogram(P, (void *)I.P, n, I.p_fmt, p->st));
+    return 0;
+  }
+  std::vector<uint16_t> h(n);
+  store_sinogram_host(P, h.data(), n, I.p_fmt);
+  return plan_put(p, (void *)I.P, h.data(), n * 2, 0);
 }
 
 int asdpocs_plan_set_initial(asdpocs_plan p, int inst, const float *m0,
@@ -1192,6 +1307,13 @@ int asdpocs_plan_get_stats(asdpocs_plan p, int inst, asdpocs_stats *st,
 }
 
 float *asdpocs_plan_sinogram_ptr(asdpocs_plan p, int inst) {
+  if (p && inst >= 0 && inst < p->batch && p->h_inst[inst].p_fmt != ASDPOCS_STORE_F32) {
+    set_error(ASDPOCS_ERR_STATE,
+              "instance %d stores its sinogram in 16 bits: load it with "
+              "asdpocs_plan_set_sinogram",
+              inst);
+    return nullptr;
+  }
   if (plan_check(p, inst)) return nullptr;
   return (float *)p->h_inst[inst].P;
 }
@@ -1215,11 +1337,11 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   auto view_of_rep = [&](int i) { return (int)(((long long)i * p->nv / reps) % p->nv); };
   auto ax = [&](int v) {
     return p->shared ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, v, p->st)
-                     : launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st);
+                     : launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st, p->exact);
   };
   auto atx = [&](int v) {
     return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, v, p->st)
-                     : launch_sart_atx(p->d_inst, p->batch, p->d, v, p->st);
+                     : launch_sart_atx(p->d_inst, p->batch, p->d, v, p->st, p->zcol);
   };
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {

@@ -11,6 +11,7 @@ namespace asd {
 struct InstLayout {
   size_t P, m, m_pre, m_res, m_k1, I0, tvb, tvc, cor, m_il, ydet, zdet, trig,
       rmse, part, cnt, scal, tabA, tabC, vflags, bytes;
+  int p_fmt;  // sinogram storage (ASDPOCS_STORE_*)
 };
 
 // Kind of an instance: 0 = 2-D fan beam (nz == nb == 1), 1 = one slice with
@@ -32,10 +33,15 @@ constexpr int kLayoutState = 1, kLayoutGeometry = 2;
 // times that for the first instance of a shared group) and il_floats that of
 // the interleaved images of a shared group (kShareSlots*N for the group's
 // first instance, else 0).
+// sino_storage: the sinogram's storage (ASDPOCS_STORE_*, 2 or 4 bytes a value).
 InstLayout layout_instance(const asdpocs_geometry &g, int max_iter,
                            size_t cor_floats,
                            int parts = kLayoutState | kLayoutGeometry,
-                           size_t il_floats = 0);
+                           size_t il_floats = 0, int sino_storage = ASDPOCS_STORE_F32);
+
+// Host copy of a job's sinogram in its storage: n FP32 values rounded as
+// asdpocs_store_sinogram does, into out (n * sino_elem_bytes(fmt) bytes).
+void store_sinogram_host(const float *in, void *out, size_t n, int fmt);
 
 // Points I's state pointers at the block `b` laid out as `o`.
 void bind_state(Inst &I, char *b, const InstLayout &o);
@@ -71,10 +77,12 @@ cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st);
 // `finish`: some instance may run fewer than two TV steps, so the
 // end-of-iteration kernel is needed (otherwise the last TV step ends every
 // instance's iteration and the launch is skipped).
-// `zcol`: cone-beam backward steps walk voxel columns (launch_sart_atx).
+// `zcol`: cone-beam backward steps walk voxel columns (launch_sart_atx);
+// `exact`: forward steps use the exact projection (launch_sart_ax).
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk = 0, bool finish = true, bool zcol = true);
+                              int tv_walk = 0, bool finish = true, bool zcol = true,
+                              bool exact = false);
 
 // Backward-step chord tables (Inst::chtab) of instances sharing 2-D geometry
 // and view angles, from d_inst[0], whose view tables are built: a counting

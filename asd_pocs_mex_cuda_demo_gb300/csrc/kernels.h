@@ -9,6 +9,10 @@ namespace asd {
 // Ax of one view: y, sr (na*nb) from x.
 cudaError_t launch_ax(const float *x, float *y, float *sr, const ViewGeo &g,
                       const Dims &d, cudaStream_t st);
+// Exact Ax of one view (Siddon's method: FP64 crossing parameters, FP32
+// lengths and sums) instead of the reference's column march.
+cudaError_t launch_ax_siddon(const float *x, float *y, float *sr, const ViewGeo &g,
+                             const Dims &d, cudaStream_t st);
 // Atx of one view: x, sc (nx*ny*nz) from y.
 cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
                        const Dims &d, cudaStream_t st);
@@ -20,6 +24,10 @@ size_t atx_zcol_scratch_bytes(const Dims &d);
 cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &g,
                             const Dims &d, void *scratch, cudaStream_t st);
 
+// Stores n FP32 sinogram values (device) as `fmt` (ASDPOCS_STORE_*) at dst.
+cudaError_t launch_store_sinogram(const float *src, void *dst, size_t n, int fmt,
+                                  cudaStream_t st);
+
 // Batched launches take the plan's largest sizes `d` (each field the
 // maximum over its instances) for the grid; every instance reads its own
 // sizes from Inst::d, and instances of one plan are all planar (nz == nb ==
@@ -29,8 +37,9 @@ cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &
 // 116-131); instances with fewer views skip.  sart_ax: Ax of m, residual
 // against P, dd2 accumulation, row normalisation -> cor.  sart_atx: Atx of
 // cor, column normalisation, update m += beta*bp/sumC, positivity.
+// `exact`: the forward step uses the exact projection (launch_ax_siddon).
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
-                           int view, cudaStream_t st);
+                           int view, cudaStream_t st, bool exact = false);
 // Cone beams (nz > 1) walk voxel columns (k_sart_atx_zcol) unless `zcol`
 // is false (the per-voxel form; bit-identical).
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,

@@ -6,6 +6,7 @@
 // the detector window its 32x8 voxel tile projects to, computes the slopes
 // of those rays once (two divisions per detector column, four per 3D ray),
 // then every (voxel, bin) pair reads them instead of dividing again.
+#include <algorithm>
 #include <type_traits>
 #include "kernels.h"
 #include "projector.cuh"
@@ -102,6 +103,25 @@ __global__ void __launch_bounds__(kAxBlock)
   if (in && part == 0 && lane == 0) {
     y[r] = v[0] * G.scale;
     sr[r] = v[1] * G.scale;
+  }
+}
+
+// Exact forward projection (siddon_columns): one warp per ray, lanes over
+// the columns of its dominant in-plane axis, the butterfly sum of k_ax.
+__global__ void __launch_bounds__(kAxBlock)
+    k_ax_siddon(const float *__restrict__ x, float *__restrict__ y,
+                float *__restrict__ sr, ViewGeo G, Dims D) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long r = (long long)blockIdx.x * kAxWarps + warp;
+  if (r >= (long long)D.na * D.nb) return;  // the whole warp
+  const SidRay R = siddon_setup(G, D, G.y_det[r % D.na], G.z_det[r / D.na]);
+  float ys = 0.f, ss = 0.f;
+  siddon_columns(R, lane, 32, [&](unsigned i) { return __ldg(x + i); }, ys, ss);
+  ys = warp_sum(ys);
+  ss = warp_sum(ss);
+  if (lane == 0) {
+    y[r] = ys * G.scale;
+    sr[r] = ss * G.scale;
   }
 }
 
@@ -331,8 +351,9 @@ __global__ void __launch_bounds__(128)
 // Also records whether every residual is finite (Scalars::cor_finite), and
 // for 3D geometry writes the view's per-ray slopes ray_tab_c for the
 // backward step that follows (Inst::tabc_mode: a shared table's writer does
-// so even after its own iterations have ended).
-template <bool k3D>
+// so even after its own iterations have ended).  kExact: the projection is
+// the exact one (siddon_columns) instead of the reference's column march.
+template <bool k3D, bool kExact>
 __global__ void __launch_bounds__(kAxBlock)
     k_sart_ax(const Inst *__restrict__ insts, int view) {
   __shared__ float sp[kAxCols][kAxWarps][2][32];
@@ -357,14 +378,20 @@ __global__ void __launch_bounds__(kAxBlock)
   float v[2] = {0.f, 0.f};
   if (r < nr) {
     const float *m = I.m;
-    ax_lane_partial(G, D, r, lane + 32 * part, [&](unsigned i) { return m[i]; }, v[0],
-                    v[1]);
+    if constexpr (kExact) {
+      const SidRay R = siddon_setup(G, D, G.y_det[r % D.na], G.z_det[r / D.na]);
+      siddon_columns(R, lane + 32 * part, 32 * kAxCols, [&](unsigned i) { return m[i]; },
+                     v[0], v[1]);
+    } else {
+      ax_lane_partial(G, D, r, lane + 32 * part, [&](unsigned i) { return m[i]; }, v[0],
+                      v[1]);
+    }
   }
   ax_combine<2>(sp, v, part, rw, lane);
   float pt[2] = {0.f, 0.f};  // dd2, non-finite residuals
   if (r < nr && part == 0 && lane == 0) {
     const float yv = v[0] * G.scale, srv = v[1] * G.scale;
-    const float c0 = I.P[(long long)view * nr + r] - yv;
+    const float c0 = sino_at(I, (long long)view * nr + r) - yv;
     const float cr = c0 / (srv == 0.f ? 1.f : srv);
     I.cor[r * I.cor_stride] = cr;
     pt[0] = c0 * c0;
@@ -1308,7 +1335,7 @@ __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
   if (part == 0 && lane < gn && ((active >> lane) & 1u) && r < nr) {
     const Inst &Ib = insts[gi + lane];
     const float yv = yb * G.scale, srv = v[kS] * G.scale;
-    const float c0 = Ib.P[(long long)view * nr + r] - yv;
+    const float c0 = sino_at(Ib, (long long)view * nr + r) - yv;
     const float cr = c0 / (srv == 0.f ? 1.f : srv);
     Ib.cor[r * Ib.cor_stride] = cr;
     p0 = c0 * c0;
@@ -1348,6 +1375,19 @@ __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
       Ib.s->dd2_acc += tot[0];
       Ib.s->cor_finite = tot[1] == 0.0;
     }
+  }
+}
+
+// Rounds an FP32 sinogram to FP16 / BF16 storage (round to nearest, ties to
+// even: the same bits as asdpocs_store_sinogram on the host).
+__global__ void __launch_bounds__(256)
+    k_store_sinogram(const float *__restrict__ src, void *dst, long long n, int fmt) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (fmt == ASDPOCS_STORE_F16)
+      ((__half *)dst)[i] = __float2half_rn(src[i]);
+    else
+      ((__nv_bfloat16 *)dst)[i] = __float2bfloat16_rn(src[i]);
   }
 }
 
@@ -1414,6 +1454,16 @@ cudaError_t launch_atx(float *x, const float *y, float *sc, const ViewGeo &g,
   return cudaGetLastError();
 }
 
+cudaError_t launch_store_sinogram(const float *src, void *dst, size_t n, int fmt,
+                                  cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  if (fmt == ASDPOCS_STORE_F32)
+    return cudaMemcpyAsync(dst, src, n * 4, cudaMemcpyDeviceToDevice, st);
+  const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 64);
+  k_store_sinogram<<<blocks, 256, 0, st>>>(src, dst, (long long)n, fmt);
+  return cudaGetLastError();
+}
+
 size_t atx_zcol_scratch_bytes(const Dims &d) {
   const size_t a = ((size_t)d.na * sizeof(float4) + 255) & ~(size_t)255;
   const size_t c = ((size_t)d.na * d.nb * sizeof(float4) + 255) & ~(size_t)255;
@@ -1436,13 +1486,31 @@ cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &
 }
 
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
-                           int view, cudaStream_t st) {
+                           int view, cudaStream_t st, bool exact) {
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
-  if (d.nz > 1 || d.nb > 1)
-    k_sart_ax<true><<<dim3(blocks, 1, batch), kAxBlock, 0, st>>>(insts, view);
-  else
-    k_sart_ax<false><<<dim3(blocks, 1, batch), kAxBlock, 0, st>>>(insts, view);
+  const dim3 grid(blocks, 1, batch);
+  const bool p3 = d.nz > 1 || d.nb > 1;
+  if (exact) {
+    if (p3)
+      k_sart_ax<true, true><<<grid, kAxBlock, 0, st>>>(insts, view);
+    else
+      k_sart_ax<false, true><<<grid, kAxBlock, 0, st>>>(insts, view);
+  } else {
+    if (p3)
+      k_sart_ax<true, false><<<grid, kAxBlock, 0, st>>>(insts, view);
+    else
+      k_sart_ax<false, false><<<grid, kAxBlock, 0, st>>>(insts, view);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ax_siddon(const float *x, float *y, float *sr, const ViewGeo &g,
+                             const Dims &d, cudaStream_t st) {
+  const long long nr = (long long)d.na * d.nb;
+  if (nr == 0) return cudaSuccess;
+  k_ax_siddon<<<(unsigned)((nr + kAxWarps - 1) / kAxWarps), kAxBlock, 0, st>>>(x, y, sr, g,
+                                                                                d);
   return cudaGetLastError();
 }
 

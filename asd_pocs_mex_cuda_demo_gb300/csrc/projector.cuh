@@ -386,6 +386,142 @@ ASD_HD void ray_columns_planar_fast(const RayMarch &R, int first, int step,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Exact forward projection (Siddon's method): the intersection length of the
+// ray with every voxel it crosses, not the reference's column march (whose
+// 3-D splits approximate them; its 2-D march is already exact).  The ray runs
+// from the source to the bin centre in voxel units; the volume spans
+// [-(n/2), n - n/2) along x and y and [-(nz/2), nz - nz/2) * dz along z.  The
+// parameters of the plane crossings are FP64 (as in an FP64 Siddon
+// reference), each segment's length is rounded to FP32 and the sums are
+// FP32.  The lanes of a warp share the ray's columns along its dominant
+// in-plane axis u; inside a column a merge walk over the planes of the other
+// axes yields the segments in order, each in the cell of its midpoint.
+// Fan beams (nz == nb == 1) are traced in the plane (two axes).
+// ---------------------------------------------------------------------------
+struct SidRay {
+  double p0[3], d[3], inv[3], lo[3], h[3];
+  double amin, amax, L;  // in-volume parameter range; |d|
+  int n[3];
+  int naxes, du;         // 2 (fan beam) or 3; the dominant in-plane axis
+  bool hit;
+};
+
+ASD_HD SidRay siddon_setup(const ViewGeo &G, const Dims &D, float ydet, float zdet) {
+  SidRay s;
+  const bool planar = D.nz == 1 && D.nb == 1;
+  s.naxes = planar ? 2 : 3;
+  s.p0[0] = (double)G.cos_phi * -(double)G.SO;
+  s.p0[1] = (double)G.sin_phi * -(double)G.SO;
+  s.p0[2] = 0.0;
+  const double p1[3] = {(double)G.cos_phi * G.OD - (double)G.sin_phi * ydet,
+                        (double)G.sin_phi * G.OD + (double)G.cos_phi * ydet,
+                        planar ? 0.0 : (double)zdet};
+  s.n[0] = D.nx;
+  s.n[1] = D.ny;
+  s.n[2] = D.nz;
+  s.h[0] = 1.0;
+  s.h[1] = 1.0;
+  s.h[2] = G.dz;
+  s.lo[0] = (double)(0 - D.nx / 2);
+  s.lo[1] = (double)(0 - D.ny / 2);
+  s.lo[2] = (double)(0 - D.nz / 2) * G.dz;
+  s.amin = 0.0;
+  s.amax = 1.0;
+  s.hit = true;
+  double L2 = 0.0;
+  for (int k = 0; k < 3; k++) {
+    const double dk = k < s.naxes ? p1[k] - s.p0[k] : 0.0;
+    s.d[k] = dk;
+    s.inv[k] = dk != 0.0 ? 1.0 / dk : 0.0;
+    if (k >= s.naxes) continue;
+    L2 += dk * dk;
+    const double b0 = s.lo[k], b1 = s.lo[k] + s.n[k] * s.h[k];
+    if (dk == 0.0) {
+      if (s.p0[k] < b0 || s.p0[k] > b1) s.hit = false;
+      continue;
+    }
+    double t0 = (b0 - s.p0[k]) / dk, t1 = (b1 - s.p0[k]) / dk;
+    if (t0 > t1) {
+      const double t = t0;
+      t0 = t1;
+      t1 = t;
+    }
+    if (t0 > s.amin) s.amin = t0;
+    if (t1 < s.amax) s.amax = t1;
+  }
+  s.L = sqrt(L2);
+  s.du = fabs(s.d[0]) >= fabs(s.d[1]) ? 0 : 1;
+  s.hit = s.hit && s.amax > s.amin && s.d[s.du] != 0.0;
+  return s;
+}
+
+// Adds the exact segments of columns first, first + step, ... of ray R's
+// dominant axis to (ys, ss): ys += l * x[voxel], ss += l, l in FP32.
+template <class Loader>
+ASD_HD void siddon_columns(const SidRay &R, int first, int step, Loader ld, float &ys,
+                           float &ss) {
+  if (!R.hit) return;
+  const int du = R.du;
+  const unsigned sx = 1u, sy = (unsigned)R.n[0], sz = (unsigned)R.n[0] * (unsigned)R.n[1];
+  for (int iu = first; iu < R.n[du]; iu += step) {
+    const double ta = (R.lo[du] + iu - R.p0[du]) * R.inv[du];
+    const double tb = (R.lo[du] + (iu + 1) - R.p0[du]) * R.inv[du];
+    double t = fmax(fmin(ta, tb), R.amin);
+    const double tend = fmin(fmax(ta, tb), R.amax);
+    if (!(tend > t)) continue;
+    // the other axes: cell at the column entry, sign of travel, parameter
+    // of the next plane crossed
+    int cell[3], sgn[3];
+    double tn[3];
+    for (int k = 0; k < 3; k++) {
+      cell[k] = 0;
+      sgn[k] = 0;
+      tn[k] = 1.0e300;
+      if (k == du || k >= R.naxes) continue;
+      const double pos = (R.p0[k] + t * R.d[k] - R.lo[k]) / R.h[k];
+      int c = (int)floor(pos);
+      if (R.d[k] == 0.0) {
+        cell[k] = c;
+        continue;
+      }
+      sgn[k] = R.d[k] > 0.0 ? 1 : -1;
+      if (sgn[k] < 0 && (double)c == pos) c -= 1;  // on a plane, moving down
+      // the next plane ahead; a plane whose crossing rounds to at or before t
+      // (the entry lies on it) is already behind: the cell is past it
+      double tk = (R.lo[k] + (sgn[k] > 0 ? c + 1 : c) * R.h[k] - R.p0[k]) * R.inv[k];
+      for (int g = 0; g < 2 && tk <= t; g++) {
+        c += sgn[k];
+        tk = (R.lo[k] + (sgn[k] > 0 ? c + 1 : c) * R.h[k] - R.p0[k]) * R.inv[k];
+      }
+      cell[k] = c;
+      tn[k] = tk;
+    }
+    cell[du] = iu;
+    // merge walk over the crossings inside the column
+    for (int guard = 0; guard < 4 * (R.n[0] + R.n[1] + R.n[2]) + 8; guard++) {
+      const double tm = fmin(tend, fmin(tn[0], fmin(tn[1], tn[2])));
+      const float l = (float)((tm - t) * R.L);
+      bool in = l > 0.0f;
+      for (int k = 0; k < R.naxes; k++) in = in && cell[k] >= 0 && cell[k] < R.n[k];
+      if (in) {
+        const unsigned idx = (unsigned)cell[0] * sx + (unsigned)cell[1] * sy +
+                             (R.naxes == 3 ? (unsigned)cell[2] * sz : 0u);
+        ys += l * ld(idx);
+        ss += l;
+      }
+      if (tm >= tend) break;
+      for (int k = 0; k < 3; k++)
+        if (tn[k] == tm) {
+          cell[k] += sgn[k];
+          const int plane = sgn[k] > 0 ? cell[k] + 1 : cell[k];
+          tn[k] = (R.lo[k] + plane * R.h[k] - R.p0[k]) * R.inv[k];
+        }
+      t = tm;
+    }
+  }
+}
+
 // Warp-wide sum; the xor butterfly leaves bit-identical totals in every lane
 // (IEEE addition is commutative).
 __device__ __forceinline__ float warp_sum(float v) {

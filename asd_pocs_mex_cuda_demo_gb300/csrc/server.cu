@@ -51,6 +51,7 @@ struct Job {
   asdpocs_options o{};
   std::vector<double> phi;
   std::vector<float> P, m0, I0;  // host copies, dropped after upload
+  std::vector<uint16_t> P16;     // the sinogram in FP16 / BF16 storage
   bool has_m0 = false, has_ref = false;
   int state = ASDPOCS_JOB_QUEUED;
   Clock::time_point t_submit, t_admit, t_done;
@@ -311,8 +312,12 @@ bool admit(asdpocs_server sv, Lane &L, int s, Job *J) {
   SV_CUDA(cudaMemsetAsync(b, 0, J->lay.bytes, sv->upload));
   Inst I = empty_slot(L, s);
   bind_state(I, b, J->lay);
-  SV_CUDA(cudaMemcpyAsync(b + J->lay.P, J->P.data(), J->P.size() * 4,
-                          cudaMemcpyHostToDevice, sv->upload));
+  if (J->lay.p_fmt == ASDPOCS_STORE_F32)
+    SV_CUDA(cudaMemcpyAsync(b + J->lay.P, J->P.data(), J->P.size() * 4,
+                            cudaMemcpyHostToDevice, sv->upload));
+  else
+    SV_CUDA(cudaMemcpyAsync(b + J->lay.P, J->P16.data(), J->P16.size() * 2,
+                            cudaMemcpyHostToDevice, sv->upload));
   if (J->has_m0)
     SV_CUDA(cudaMemcpyAsync(b + J->lay.m_k1, J->m0.data(), J->m0.size() * 4,
                             cudaMemcpyHostToDevice, sv->upload));
@@ -326,6 +331,7 @@ bool admit(asdpocs_server sv, Lane &L, int s, Job *J) {
   SV_CUDA(cudaMemcpyAsync(L.d_inst + s, &L.slot_desc[s], sizeof I,
                           cudaMemcpyHostToDevice, L.st));
   std::vector<float>().swap(J->P);
+  std::vector<uint16_t>().swap(J->P16);
   std::vector<float>().swap(J->m0);
   std::vector<float>().swap(J->I0);
   J->state = ASDPOCS_JOB_RUNNING;
@@ -568,15 +574,25 @@ int asdpocs_server_submit(asdpocs_server sv, const asdpocs_geometry *geom,
   else
     asdpocs_options_default(&J->o);
   if (int e = check_instance(J->g, J->o)) return e;
+  if (J->o.ax_mode != ASDPOCS_AX_REFERENCE)
+    return set_error(ASDPOCS_ERR_ARG,
+                     "the serving queue runs the reference forward mode only; "
+                     "run exact-mode jobs in a plan");
   const asdpocs_geometry &g = J->g;
   const size_t N = (size_t)g.nx * g.ny * g.nz;
-  J->lay = layout_instance(g, J->o.maxnumIter, 0, kLayoutState);
+  J->lay = layout_instance(g, J->o.maxnumIter, 0, kLayoutState, 0, J->o.sino_storage);
   if (J->lay.bytes > sv->budget)
     return set_error(ASDPOCS_ERR_NOMEM,
                      "job needs %zu bytes, over the server's HBM budget of %llu",
                      J->lay.bytes, sv->budget);
   J->phi.assign(phi_vec_deg, phi_vec_deg + g.nv);
-  J->P.assign(P, P + (size_t)g.na * g.nb * g.nv);
+  const size_t nP = (size_t)g.na * g.nb * g.nv;
+  if (J->o.sino_storage == ASDPOCS_STORE_F32) {
+    J->P.assign(P, P + nP);
+  } else {  // rounded once here, uploaded at half the bytes
+    J->P16.resize(nP);
+    store_sinogram_host(P, J->P16.data(), nP, J->o.sino_storage);
+  }
   if (m0) {
     J->m0.assign(m0, m0 + N);
     J->has_m0 = true;

@@ -167,6 +167,21 @@ def Ax_cone_mf_gpu_new(X, y, sr, cos_phi, sin_phi, y_det, z_det, SO, OD, scale, 
     check(L.asdpocs_last_status())
 
 
+def Ax_siddon_mf_gpu(X, y, sr, cos_phi, sin_phi, y_det, z_det, SO, OD, scale, dz,
+                     nx, ny, nz, na, nb):
+    """Exact (Siddon) forward projection with Ax_cone_mf_gpu_new's arguments:
+    the length of each ray inside every voxel it crosses (asdpocs_ax_siddon;
+    host memory, synchronous)."""
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (X, y_det, z_det)]
+    for out in (y, sr):
+        if out.dtype != np.float32 or not out.flags.c_contiguous or out.size < na * nb:
+            raise ValueError("outputs must be contiguous float32 arrays of na*nb")
+    check(load().asdpocs_ax_siddon(arrs[0].ctypes.data_as(_F), y.ctypes.data_as(_F),
+                                   sr.ctypes.data_as(_F), cos_phi, sin_phi,
+                                   arrs[1].ctypes.data_as(_F), arrs[2].ctypes.data_as(_F),
+                                   SO, OD, scale, dz, nx, ny, nz, na, nb))
+
+
 def Atx_cone_mf_gpu_new(X, y, sc, cos_phi, sin_phi, y_det, z_det, SO, OD, scale, dy_det,
                         dz_det, dz, nx, ny, nz, na, nb):
     """Launcher-level backprojection: X, sc (outputs, nx*ny*nz float32) from

@@ -76,6 +76,22 @@ int asdpocs_ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
                       float dz, int nx, int ny, int nz, int na, int nb,
                       void *stream);
 
+/* Exact forward projection (no counterpart in the reference, whose 3-D
+ * column march approximates the voxel chords): Siddon's method, the length
+ * of the ray inside every voxel it crosses, with FP64 plane-crossing
+ * parameters, FP32 lengths and FP32 sums.  Same arguments and outputs as
+ * Ax_cone_mf_gpu_new (host buffers, synchronous) / asdpocs_ax_device (device
+ * buffers, asynchronous on `stream`).  In 2-D it agrees with the reference
+ * march to FP32 rounding. */
+int asdpocs_ax_siddon(const float *X, float *y, float *sr, float cos_phi,
+                      float sin_phi, const float *y_det, const float *z_det,
+                      float SO, float OD, float scale, float dz, int nx, int ny,
+                      int nz, int na, int nb);
+int asdpocs_ax_siddon_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,
+                             float sin_phi, const float *y_det_d, const float *z_det_d,
+                             float SO, float OD, float scale, float dz, int nx, int ny,
+                             int nz, int na, int nb, void *stream);
+
 /* Same computation as Atx_cone_mf_gpu_new on device buffers (x_d, sc_d
  * outputs, y_d input).  Asynchronous. */
 int asdpocs_atx_device(float *x_d, const float *y_d, float *sc_d,
@@ -157,7 +173,27 @@ int asdpocs_tv_device_noalloc(float *img_d, const float *img_old_d, int nx,
 /* ASD-POCS reconstruction jobs (device resident)                      */
 /* ------------------------------------------------------------------ */
 
-/* Option set of ASD_POCS_cuda.m:20-96 (defaults via asdpocs_options_default). */
+/* Device storage of a job's sinogram (asdpocs_options.sino_storage).  The
+ * reference keeps P in double and passes single-precision views to the GPU
+ * (Ax_main_test.cpp:45); here it is stored once on the device in FP32 or, to
+ * halve its bytes, rounded to nearest (ties to even) to FP16 or BF16.  Every
+ * read widens it to FP32; ray sums, residuals and images stay FP32 and the
+ * step-control scalars FP64. */
+enum {
+  ASDPOCS_STORE_F32 = 0,
+  ASDPOCS_STORE_F16 = 1, /* 11-bit significand, range 6e-5 .. 65504 */
+  ASDPOCS_STORE_BF16 = 2 /* 8-bit significand, FP32's range        */
+};
+
+/* Forward projection of the SART steps (asdpocs_options.ax_mode): the
+ * reference's column march (Ax_cone_gpu.cu:339-776) or the exact Siddon
+ * projection of asdpocs_ax_siddon (no counterpart in the reference). */
+enum { ASDPOCS_AX_REFERENCE = 0, ASDPOCS_AX_EXACT = 1 };
+
+/* Option set of ASD_POCS_cuda.m:20-96 (defaults via asdpocs_options_default),
+ * plus the sinogram storage and the forward mode (no counterpart in the
+ * reference).  The instances of one plan share one ax_mode; the serving
+ * queue runs ASDPOCS_AX_REFERENCE jobs only. */
 typedef struct {
   int maxnumIter;       /* 5      */
   int numOfgradients;   /* ng, 20 */
@@ -168,8 +204,16 @@ typedef struct {
   double r_max;         /* 0.95   */
   double epsilon;       /* eps    */
   double stopRelChg;    /* eps    */
+  int sino_storage;     /* ASDPOCS_STORE_F32 */
+  int ax_mode;          /* ASDPOCS_AX_REFERENCE */
 } asdpocs_options;
 void asdpocs_options_default(asdpocs_options *opt);
+
+/* Rounds n FP32 values to the sinogram storage `storage` (2 bytes each for
+ * FP16 / BF16, 4 for FP32), as the plans and the serving queue store them:
+ * round to nearest, ties to even; NaN stays NaN, overflow gives inf. */
+int asdpocs_store_sinogram(const float *in, void *out, unsigned long long n,
+                           int storage);
 
 /* Per-reconstruction outputs (the `out` struct of ASD_POCS_cuda.m:173-180). */
 typedef struct {
@@ -207,8 +251,9 @@ int asdpocs_plan_destroy(asdpocs_plan plan);
 unsigned long long asdpocs_plan_bytes(asdpocs_plan plan);
 
 /* Load instance data.  `where`: 0 = host pointer (copied on the plan's
- * stream), 1 = device pointer.  P: (na*nb) x nv float sinogram; m0 / I0:
- * nx*ny*nz (NULL = zeros / no RMSE); sizes are the instance's own. */
+ * stream), 1 = device pointer.  P: (na*nb) x nv float sinogram, rounded to
+ * the instance's sino_storage; m0 / I0: nx*ny*nz (NULL = zeros / no RMSE);
+ * sizes are the instance's own. */
 int asdpocs_plan_set_sinogram(asdpocs_plan plan, int inst, const float *P,
                               int where);
 int asdpocs_plan_set_initial(asdpocs_plan plan, int inst, const float *m0,
@@ -232,7 +277,9 @@ int asdpocs_plan_get_image(asdpocs_plan plan, int inst, float *m, int where);
 int asdpocs_plan_get_stats(asdpocs_plan plan, int inst, asdpocs_stats *st,
                            double *rmse);
 /* Device pointer of an instance's sinogram / result image (for zero-copy
- * pipelines). */
+ * pipelines).  The sinogram pointer exists only for FP32 storage (NULL with
+ * ASDPOCS_ERR_STATE otherwise: load FP16 / BF16 sinograms through
+ * asdpocs_plan_set_sinogram, which rounds them). */
 float *asdpocs_plan_sinogram_ptr(asdpocs_plan plan, int inst);
 float *asdpocs_plan_image_ptr(asdpocs_plan plan, int inst);
 

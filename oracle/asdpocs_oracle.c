@@ -646,6 +646,25 @@ long long orc_siddon_nnz(float cos_phi, float sin_phi, const float *y_det,
   return c.n;
 }
 
+/* The FP64 Siddon projection in the driver's forward-projector form (FP32
+ * outputs): the oracle of the library's exact forward mode. */
+void orc_ax_siddon_for_driver(const float *x, float *y, float *sr, float c, float s,
+                              const float *yd, const float *zd, float SO, float OD,
+                              float sc, float dz, int nx, int ny, int nz, int na, int nb,
+                              int nt) {
+  (void)nt;
+  const long M = (long)na * nb;
+  double *yy = (double *)malloc(sizeof(double) * (size_t)M);
+  double *ss = (double *)malloc(sizeof(double) * (size_t)M);
+  orc_siddon_ax_f64(x, yy, ss, c, s, yd, zd, SO, OD, sc, dz, nx, ny, nz, na, nb);
+  for (long i = 0; i < M; i++) {
+    y[i] = (float)yy[i];
+    sr[i] = (float)ss[i];
+  }
+  free(yy);
+  free(ss);
+}
+
 /* ------------------------------------------------------------------------ */
 /* ASD-POCS driver (ASD_POCS_cuda.m:97-182), FP64 image state                 */
 /* ------------------------------------------------------------------------ */

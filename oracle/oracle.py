@@ -266,8 +266,10 @@ def make_params(para: dict, nv: int) -> AsdParams:
 
 def asdpocs(P, para, impl="oracle", nthreads=0):
     """ASD_POCS_cuda(P, para) with FP64 image state.  ``impl`` selects the
-    projector/TV code: ``"oracle"`` (restatement) or ``"reference"`` (the
-    reference's host build).  Returns (m_res flat, out dict)."""
+    projector/TV code: ``"oracle"`` (restatement), ``"reference"`` (the
+    reference's host build) or ``"siddon"`` (the restatement with the FP64
+    Siddon forward projection, the oracle of the exact forward mode).
+    Returns (m_res flat, out dict)."""
     P = np.asfortranarray(np.asarray(P, np.float64))
     nv = P.shape[1]
     phi = _f64(np.asarray(para["phi_vec"], np.float64).ravel())
@@ -288,6 +290,8 @@ def asdpocs(P, para, impl="oracle", nthreads=0):
         R = ref()
         fns = tuple(C.cast(getattr(R, n), C.c_void_p)
                     for n in ("ref_ax_for_driver", "ref_atx_for_driver", "ref_tv_for_driver"))
+    elif impl == "siddon":
+        fns = (C.cast(lib().orc_ax_siddon_for_driver, C.c_void_p), None, None)
     lib().orc_asdpocs_with(_dp(Pflat), _dp(phi), C.byref(p), _dp(m0), _dp(I0), _dp(m_res),
                            _dp(rmse), C.byref(out), nthreads, *fns)
     res = dict(IterationNum=out.iterations, dataTolerance=out.dataTolerance,

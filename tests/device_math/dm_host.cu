@@ -15,7 +15,9 @@
 //   dm_chord_count / dm_atx_table -- the 2-D chord tables' layout, filled
 //              and read back;
 //   dm_atx3_zcol -- the cone-beam backward step walked down voxel columns,
-//              as the z-column kernel runs it.
+//              as the z-column kernel runs it;
+//   dm_ax_siddon -- the exact (Siddon) forward projection, its columns split
+//              over `lanes` partial sums combined by the warp butterfly.
 // Compiled with -ffp-contract=off so the host compiler fuses nothing.
 #include <string.h>
 
@@ -331,4 +333,33 @@ extern "C" void dm_atx3_zcol(float *x, const float *yv, float *sc, float c, floa
         sc[idx] = accl * scale;
       }
     }
+}
+
+extern "C" void dm_ax_siddon(const float *x, float *y, float *sr, float c, float s,
+                             const float *yd, const float *zd, float SO, float OD,
+                             float scale, float dz, int nx, int ny, int nz, int na, int nb,
+                             int lanes) {
+  const ViewGeo G = geo(c, s, yd, zd, SO, OD, scale, 0.f, 0.f, dz);
+  const Dims D{nx, ny, nz, na, nb};
+  std::vector<float> py(lanes), ps(lanes);
+  for (long long r = 0; r < (long long)na * nb; r++) {
+    const SidRay R = siddon_setup(G, D, yd[r % na], zd[r / na]);
+    for (int l = 0; l < lanes; l++) {
+      float a = 0.f, b = 0.f;
+      siddon_columns(R, l, lanes, [&](unsigned i) { return x[i]; }, a, b);
+      py[l] = a;
+      ps[l] = b;
+    }
+    for (int o = lanes / 2; o > 0; o >>= 1) {
+      std::vector<float> ny_(py), ns_(ps);
+      for (int l = 0; l < lanes; l++) {
+        ny_[l] = py[l] + py[l ^ o];
+        ns_[l] = ps[l] + ps[l ^ o];
+      }
+      py.swap(ny_);
+      ps.swap(ns_);
+    }
+    y[r] = py[0] * G.scale;
+    sr[r] = ps[0] * G.scale;
+  }
 }

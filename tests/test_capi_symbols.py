@@ -45,6 +45,11 @@ def test_python_signatures_cover_header():
 
 def test_version_and_error_state_without_gpu(lib):
     assert b"sm_103a" in lib.asdpocs_version()
+    # a refused call sets the calling thread's status and message; the next
+    # successful call clears them
+    assert lib.asdpocs_store_sinogram(None, None, 4, 0) == 1
+    assert lib.asdpocs_last_status() == 1 and b"null" in lib.asdpocs_last_error()
+    assert lib.asdpocs_store_sinogram(None, None, 0, 0) == 0
     assert lib.asdpocs_last_status() == 0
 
 

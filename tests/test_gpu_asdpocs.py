@@ -509,3 +509,54 @@ def test_cone_beam_z_column_step_equals_per_voxel_step(gpu, monkeypatch, dims):
         zc, vox = run(None, ps), run("voxel", ps)
         for a, b in zip(zc, vox):
             assert np.array_equal(a, b), rel_l2(a, b)
+
+
+@pytest.mark.parametrize("dims", [(64, 64, 1, 128, 1, 1.0), (20, 20, 20, 40, 30, 10.24)])
+def test_exact_forward_mode_reconstruction_vs_oracle(gpu, oracle_mod, dims):
+    """A plan with ax_mode="exact" (SART forward steps through the exact
+    Siddon projection) against the oracle's ASD-POCS driver with the FP64
+    Siddon forward projector; a batch of exact instances of different sizes
+    gives each instance's image alone, bit for bit."""
+    nx, ny, nz, na, nb, det = dims
+    SO, OD = (541.0, 408.0) if nz == 1 else (1000.0, 500.0)
+    vx = phantoms.fov_voxel_size(SO, OD, det, na, nx)
+    x = (phantoms.shepp_logan_2d(nx) if nz == 1 else phantoms.shepp_logan_3d(nx) * 0.02)
+    x = x.astype(np.float32)
+    phi = phantoms.views(9)
+    para = dict(SO=SO, OD=OD, vxlsize=vx, nx=nx, ny=ny, nz=nz, na=na, nb=nb, detsize=det,
+                phi_vec=phi, maxnumIter=3, numOfgradients=5, alpha=0.002, ax_mode="exact")
+    P = np.stack([oracle_mod.siddon_ax(x, oracle_mod.gateway_geometry(
+        -a / 180 * np.pi, SO, OD, vx, det, na, nb), nx, ny, nz)[0] for a in phi], axis=1)
+    m, out = pkg.ASD_POCS_cuda(P, dict(para, I0=x))
+    mo, oo = oracle_mod.asdpocs(P, dict(para, I0=x.astype(np.float64)), impl="siddon")
+    assert out["IterationNum"] == oo["IterationNum"]
+    assert rel_l2(m.ravel(order="F"), mo) < RECON_TOL, rel_l2(m.ravel(order="F"), mo)
+    np.testing.assert_allclose(out["RMSE"], oo["RMSE"], rtol=1e-4)
+    # a batch: this instance and a smaller one, both exact
+    other = dict(para, nx=nx - 3, na=na - 5)
+    Po = np.random.default_rng(1).random(((na - 5) * nb, len(phi))).astype(np.float32)
+    alone = []
+    for pa, Pk in ((para, P), (other, Po)):
+        with pkg.Plan(pa, phi) as pl:
+            pl.set_sinogram(0, np.asarray(Pk, np.float32).ravel(order="F"))
+            pl.reset()
+            pl.run()
+            alone.append(pl.image(0))
+    with pkg.Plan([para, other], [phi, phi]) as pl:
+        for k, Pk in enumerate((P, Po)):
+            pl.set_sinogram(k, np.asarray(Pk, np.float32).ravel(order="F"))
+        pl.reset()
+        pl.run()
+        for k in range(2):
+            assert np.array_equal(pl.image(k), alone[k]), k
+
+
+def test_exact_mode_rules(gpu):
+    """One forward mode per plan; the serving queue refuses exact-mode jobs."""
+    para = dict(SO=541.0, OD=408.0, vxlsize=1.0, nx=16, ny=16, nz=1, na=32, nb=1,
+                detsize=1.0, phi_vec=phantoms.views(4), maxnumIter=1)
+    with pytest.raises(pkg.AsdpocsError, match="one forward mode"):
+        pkg.Plan([para, dict(para, ax_mode="exact")], [para["phi_vec"]] * 2)
+    with pkg.Server() as srv:
+        with pytest.raises(pkg.AsdpocsError, match="reference forward mode only"):
+            srv.submit(dict(para, ax_mode="exact"), np.zeros((32, 4), np.float32))
