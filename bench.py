@@ -100,20 +100,24 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--jobs", type=int, default=None, help="serve: number of jobs")
+    ap.add_argument("--storage", default=None, choices=["f32", "f16", "bf16"],
+                    help="device storage of the sinograms (default f32; uneven: f16)")
+    ap.add_argument("--ax-mode", default="reference", choices=["reference", "exact"],
+                    help="forward projection of the SART steps")
     args = ap.parse_args()
     if args.workload == "serve":
-        W = dict(SERVE)
+        W = dict(SERVE, storage=args.storage or "f32", ax_mode="reference")
         if args.jobs is not None:
             W["jobs"] = args.jobs
         return args, W
     if args.workload == "uneven":
-        W = dict(UNEVEN)
+        W = dict(UNEVEN, storage=args.storage or "f16", ax_mode=args.ax_mode)
         if args.batch is not None:
             W["batch"] = args.batch
         if args.iters is not None:
             W["iters"] = args.iters
         return args, W
-    W = dict(WORKLOADS[args.workload])
+    W = dict(WORKLOADS[args.workload], storage=args.storage or "f32", ax_mode=args.ax_mode)
     if args.batch is not None:
         W["batch"] = args.batch
     if args.iters is not None:
@@ -161,7 +165,38 @@ def para_for(W):
     return dict(SO=W["SO"], OD=W["OD"], vxlsize=voxel_size(W), detsize=W["det"],
                 nx=W["nx"], ny=W["ny"], nz=W["nz"], na=W["na"], nb=W["nb"],
                 maxnumIter=W["iters"], numOfgradients=W["ng"], alpha=0.2,
-                alpha_red=0.95, r_max=0.95, beta=1.0, beta_red=0.995)
+                alpha_red=0.95, r_max=0.95, beta=1.0, beta_red=0.995,
+                sino_storage=W.get("storage", "f32"), ax_mode=W.get("ax_mode", "reference"))
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu model")):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+def base_config(W, world):
+    """The workload as both arms (this library, the reference's CPU path)
+    report it."""
+    dims = (f"{W['nx']}^2" if W["nz"] == 1 else f"{W['nx']}^3")
+    return {"workload": W["label"], "batch_per_gpu": W["batch"], "iterations": W["iters"],
+            "volume": dims, "views": W["nv"], "bins": [W["na"], W["nb"]],
+            "tv_steps": W["ng"], "parallelism": f"replicas x{world}",
+            "storage": W.get("storage", "f32"), "ax_mode": W.get("ax_mode", "reference"),
+            "l2": "a 256 MB buffer (> 129 MB L2) is written between timed GPU steps"}
 
 
 def phantom(W, seed):
@@ -333,25 +368,30 @@ def cpu_sample_3d(W, impl, cores, views=2):
     return per_iter, sample
 
 
-def cpu_baseline(W, paras, phis, Ps, sample_iters):
+def cpu_baseline(W, paras, phis, Ps, I0s, sample_iters):
     """The C restatement of the reference's CPU path (OpenMP, all host
     threads) on one reconstruction of the workload, sampled and extrapolated
-    to the full iteration count."""
+    to the full iteration count.  For fan beams the sample is instance 0's
+    first `sample_iters` iterations (FP64 image state); its image and RMSE
+    trajectory are returned for the comparison with the GPU."""
     cores = os.cpu_count() or 1
     if W["nz"] > 1:
         per_iter, sample = cpu_sample_3d(W, "oracle", cores)
         return {"value": 1.0 / (per_iter * W["iters"]), "unit": "recons/s", "cores": cores,
-                "kind": "port", "sample": sample}
+                "cpu": cpu_model(), "kind": "port", "sample": sample}, None
     oracle = _oracle()
-    p = dict(paras[0], phi_vec=phis[0], maxnumIter=sample_iters)
+    p = dict(paras[0], phi_vec=phis[0], maxnumIter=sample_iters,
+             I0=I0s[0].astype(np.float64))
     P = Ps[0].astype(np.float64).reshape(W["na"] * W["nb"], W["nv"], order="F")
     t = time.perf_counter()
-    oracle.asdpocs(P, p, nthreads=cores)
+    m, out = oracle.asdpocs(P, p, nthreads=cores)
     dt = time.perf_counter() - t
     per_recon = dt * W["iters"] / sample_iters
-    return {"value": 1.0 / per_recon, "unit": "recons/s", "cores": cores, "kind": "port",
-            "sample": f"{sample_iters} of {W['iters']} ASD-POCS iterations of one "
-                      f"{W['nx']}^2 reconstruction ({dt:.1f} s), extrapolated"}
+    return ({"value": 1.0 / per_recon, "unit": "recons/s", "cores": cores,
+             "cpu": cpu_model(), "kind": "port",
+             "sample": f"{sample_iters} of {W['iters']} ASD-POCS iterations of one "
+                       f"{W['nx']}^2 reconstruction ({dt:.1f} s), extrapolated"},
+            (m, out["RMSE"]))
 
 
 def main():
@@ -425,6 +465,7 @@ def main():
     ms = allmax(pg, statistics.mean(times))
     value = B * world / (ms / 1e3)
     rmse = [plan.stats(b)["RMSE"][-1] for b in range(B)]
+    batch_img = plan.image(0)  # before the phase timing below resets the plan
     # per iteration: forward + backward step per view, after-sweep, one launch
     # per TV step (the last also ends the iteration when ng >= 2, else an
     # end-of-iteration launch), and for a batch sharing one geometry the
@@ -433,7 +474,45 @@ def main():
     kernels_per_step = (plan.streams * iters *
                         (2 * nv + 1 + ng + (1 if ng < 2 else 0) + (2 if B > 1 else 0)))
 
-    # ---- plain path (one reconstruction per plan, same kernels) for context
+    # ---- per-kernel device times (CUDA events on the plan's stream)
+    vx = voxel_size(W)
+    nnz = statistics.mean(
+        roofline.nnz_per_view(a, W["SO"], W["OD"], vx, W["det"], W["nx"], W["ny"], W["nz"],
+                              W["na"], W["nb"]) for a in phis[0][::max(1, nv // 10)])
+    peak, peak_kind = measured_peaks()
+    ncu_dram = NCU_DRAM_PER_INSTANCE.get(args.workload, {})
+
+    def phase_times(pl, nb_inst, reps):
+        """Per-launch device times of the three iteration kernels of plan
+        pl (nb_inst instances), their algorithmic bytes and fractions of
+        the measured HBM peak."""
+        pl.reset()
+        t_ax, t_atx, t_tv = (pl.time_phase(k, reps) for k in (0, 1, 2))
+        pl.reset()
+        kern = {
+            "sart_ax": {"ms": t_ax, "per_iter_ms": t_ax * nv,
+                        "bytes": nb_inst * roofline.ax_bytes(nnz, M)},
+            "sart_atx": {"ms": t_atx, "per_iter_ms": t_atx * nv,
+                         "bytes": nb_inst * roofline.atx_bytes(nnz, N)},
+            "tv_step": {"ms": t_tv, "per_iter_ms": t_tv * ng,
+                        "bytes": nb_inst * roofline.tv_step_bytes(N)},
+        }
+        for k in kern.values():
+            k["GBps"] = k["bytes"] / (k["ms"] / 1e3) / 1e9
+            k["frac"] = k["GBps"] / peak
+        return kern
+
+    reps = 30 if N * B <= (1 << 26) else 5
+    kern = phase_times(plan, B, reps)
+    for name, k in kern.items():
+        k["traffic"] = ncu_dram[name] * B if name in ncu_dram else None
+    top = max(kern, key=lambda k: kern[k]["per_iter_ms"])
+    achieved = kern[top]["GBps"]
+    tot_iter = sum(k["per_iter_ms"] for k in kern.values())
+
+    # ---- plain path: the same reconstruction one at a time (a one-instance
+    # plan, same kernel families), timed several times, with its own
+    # per-kernel roofline
     plain_info = None
     if B > 1:
         plain = pkg.Plan(paras[:1], phis[:1], stream=stream.cuda_stream)
@@ -442,52 +521,36 @@ def main():
         plain.reset()
         plain.run()
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        plain.reset()
-        e0.record(stream)
-        plain.run(use_graph=True, sync=False)
-        e1.record(stream)
-        e1.synchronize()
-        plain_ms = e0.elapsed_time(e1)
+        plain_times = []
+        for _ in range(7):
+            flush.zero_()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            plain.reset()
+            e0.record(stream)
+            plain.run(use_graph=True, sync=False)
+            e1.record(stream)
+            e1.synchronize()
+            plain_times.append(e0.elapsed_time(e1))
+        plain_ms = statistics.median(plain_times)
         plain_rmse = plain.stats(0)["RMSE"][-1]
         plain_img = plain.image(0)
-        batch_img = plan.image(0)
+        pk = phase_times(plain, 1, 30)
+        plain_iter_ms = plain_ms / iters
         plain.close()
-        plain_info = {"recons_per_s": 1e3 / plain_ms, "ms_per_recon": plain_ms,
+        plain_info = {"recons_per_s": 1e3 / plain_ms, "ms_per_recon_p50": plain_ms,
+                      "ms_per_recon_all": plain_times, "runs": len(plain_times),
                       "rmse": plain_rmse, "batched_rmse": rmse[0],
                       "batch_equals_plain_bitwise": bool(np.array_equal(plain_img,
                                                                         batch_img)),
-                      "batched_speedup": value / world / (1e3 / plain_ms)}
-
-    # ---- per-kernel device times (CUDA events on the plan's stream)
-    vx = voxel_size(W)
-    nnz = statistics.mean(
-        roofline.nnz_per_view(a, W["SO"], W["OD"], vx, W["det"], W["nx"], W["ny"], W["nz"],
-                              W["na"], W["nb"]) for a in phis[0][::max(1, nv // 10)])
-    reps = 30 if N * B <= (1 << 26) else 5
-    plan.reset()
-    t_ax = plan.time_phase(0, reps)
-    t_atx = plan.time_phase(1, reps)
-    t_tv = plan.time_phase(2, reps)
-    plan.reset()
-    kern = {
-        "sart_ax": {"ms": t_ax, "per_iter_ms": t_ax * nv,
-                    "bytes": B * roofline.ax_bytes(nnz, M)},
-        "sart_atx": {"ms": t_atx, "per_iter_ms": t_atx * nv,
-                     "bytes": B * roofline.atx_bytes(nnz, N)},
-        "tv_step": {"ms": t_tv, "per_iter_ms": t_tv * ng,
-                    "bytes": B * roofline.tv_step_bytes(N)},
-    }
-    for k in kern.values():
-        k["GBps"] = k["bytes"] / (k["ms"] / 1e3) / 1e9
-    ncu_dram = NCU_DRAM_PER_INSTANCE.get(args.workload, {})
-    for name, k in kern.items():
-        k["traffic"] = ncu_dram[name] * B if name in ncu_dram else None
-    top = max(kern, key=lambda k: kern[k]["per_iter_ms"])
-    peak, peak_kind = measured_peaks()
-    achieved = kern[top]["GBps"]
-    tot_iter = sum(k["per_iter_ms"] for k in kern.values())
+                      "batched_speedup": value / world / (1e3 / plain_ms),
+                      "kernels": pk,
+                      "iteration_ms": plain_iter_ms,
+                      "kernel_share_of_iteration": sum(k["per_iter_ms"] for k in pk.values())
+                      / plain_iter_ms,
+                      "note": "one reconstruction per plan; per-kernel fractions are "
+                              "algorithmic bytes / event-timed launch / measured HBM peak"}
 
     # ---- end to end through the C ABI with host buffers
     e2e = None
@@ -512,12 +575,36 @@ def main():
                                                0))
             et.append(time.perf_counter() - t0)
         e_s = allmax(pg, statistics.mean(et))
+        esz = 4 if W["storage"] == "f32" else 2  # rounded on the host before the copy
         e2e = {"value": B * world / e_s, "unit": "recons/s",
-               "h2d_bytes_per_step": B * M * nv * 4, "d2h_bytes_per_step": B * N * 4}
+               "h2d_bytes_per_step": B * M * nv * esz, "d2h_bytes_per_step": B * N * 4}
 
-    cpu = None
+    cpu, cpu_vs_gpu = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline(W, paras, phis, Ps, sample_iters=64)
+        sample_iters = 64
+        cpu, ref_run = cpu_baseline(W, paras, phis, Ps, I0s, sample_iters)
+        if ref_run is not None:
+            # instance 0 for the same iterations on the GPU (a one-instance
+            # plan), against the oracle's FP64-state run
+            m_o, rmse_o = ref_run
+            with pkg.Plan(dict(paras[0], maxnumIter=sample_iters), phis[:1],
+                          stream=stream.cuda_stream) as pl:
+                pl.set_sinogram(0, Ps[0])
+                pl.set_reference(0, I0s[0])
+                pl.reset()
+                pl.run()
+                m_g, rmse_g = pl.image(0), pl.stats(0)["RMSE"]
+            d = np.abs(np.asarray(rmse_g) / np.asarray(rmse_o) - 1)
+            cpu_vs_gpu = {
+                "instance": 0, "iterations": sample_iters,
+                "rmse_oracle_last": float(rmse_o[-1]), "rmse_gpu_last": float(rmse_g[-1]),
+                "rmse_trajectory_max_rel_diff": float(d.max()),
+                "rmse_trajectory_mean_rel_diff": float(d.mean()),
+                "image_rel_l2": float(np.linalg.norm(m_g.astype(np.float64) - m_o)
+                                      / np.linalg.norm(m_o)),
+                "note": "alpha 0.2: the iteration is chaotic (a 1e-7 change of P moves "
+                        "the FP64 image by ~3e-2), so the RMSE trajectory is the "
+                        "comparable quantity; well-conditioned settings agree to 2e-4"}
 
     if rank == 0:
         dims = (f"{W['nx']}^2" if W["nz"] == 1 else f"{W['nx']}^3")
@@ -528,20 +615,17 @@ def main():
             "dtype": "f32",
             "data": "synthetic (seeded " + ("random-ellipse" if W["phantom"] == "ellipses"
                                            else "Shepp-Logan") + " phantoms, Poisson noise)",
-            "config": {"workload": W["label"], "batch_per_gpu": B, "iterations": iters,
-                       "volume": dims, "views": nv, "bins": [W["na"], W["nb"]],
-                       "tv_steps": ng, "parallelism": f"replicas x{world}",
-                       "l2": "256 MB buffer written between timed steps; resident set "
-                             f"{plan.nbytes / 2**20:.0f} MB > 129 MB L2",
-                       "graph": "one ASD-POCS iteration captured, replayed per iteration",
-                       "plan": {"create_ms": plan_ms, "chord_slots": slots,
-                                "chord_table_mb": chord_mb,
-                                "note": "created once per scan protocol, outside the timed "
-                                        "region (view tables and, for 2-D plans, the "
-                                        "backward step's chord tables)"},
-                       "tv_walk": {"autotuned": tv_walk, "ms_per_step": tv_walk_ms,
-                                   "note": "bands (2-D) or slabs (3-D) of 16 per walk; "
-                                           "0 = the batch-size rule"}},
+            "config": base_config(W, world),
+            "details": {"resident_mb": plan.nbytes / 2**20,
+                        "graph": "one ASD-POCS iteration captured, replayed per iteration",
+                        "plan": {"create_ms": plan_ms, "chord_slots": slots,
+                                 "chord_table_mb": chord_mb,
+                                 "note": "created once per scan protocol, outside the timed "
+                                         "region (view tables and, for 2-D plans, the "
+                                         "backward step's chord tables)"},
+                        "tv_walk": {"autotuned": tv_walk, "ms_per_step": tv_walk_ms,
+                                    "note": "bands (2-D) or slabs (3-D) of 16 per walk; "
+                                            "0 = the batch-size rule"}},
             "latency_ms": {"p50": statistics.median(times), "p99": max(times),
                            "note": "every reconstruction of a batch completes at the end "
                                    "of its step"},
@@ -555,6 +639,7 @@ def main():
                          "share_of_iteration": kern[top]["per_iter_ms"] / tot_iter,
                          "nnz_per_view": nnz, "kernels": kern},
             "cpu_baseline": cpu,
+            "cpu_vs_gpu": cpu_vs_gpu,
             "e2e": e2e,
             "clocks": clk,
             "gpu_launches": kernels_per_step * args.steps,
@@ -599,7 +684,7 @@ def serve_jobs(W, seed, device):
                 cache3[n] = xd3.cpu().numpy()
             x = cache3[n]
         Wj = dict(nx=n, ny=n, nz=nz, na=na, nb=nb, nv=nv, SO=SO, OD=OD, det=det, vx=vx,
-                  iters=iters, ng=20)
+                  iters=iters, ng=20, storage=W["storage"])
         phi = phantoms.views(nv)
         vxs = voxel_size(Wj)
         sc = np.float32(vxs)
@@ -739,8 +824,11 @@ def serve_main(args, W, rank, world, pg):
 
 
 def uneven_main(args, W, rank, world, pg):
-    """One heterogeneous plan of W["batch"] seeded slices against the same
-    slices run one at a time (plain plans); images compared bit for bit."""
+    """One heterogeneous plan of W["batch"] seeded slices, sinograms stored as
+    W["storage"], against the same slices run one at a time in FP32 (plain
+    plans): images compared bit for bit when the storage is FP32, else the
+    RMSE against the phantoms; the smallest slice is also reconstructed by
+    the FP64 oracle."""
     import torch
 
     import asd_pocs_mex_cuda_demo_gb300 as pkg
@@ -780,7 +868,7 @@ def uneven_main(args, W, rank, world, pg):
         phantoms.poisson_noise_device(y.data_ptr(), y.data_ptr(), y.numel(), W["I0"],
                                       seed=11000 + k, stream=st)
         torch.cuda.synchronize()
-        paras.append(dict(para_for(Wk), phi_vec=phi))
+        paras.append(dict(para_for(dict(Wk, storage=W["storage"])), phi_vec=phi))
         Ps.append(y.cpu().numpy())
         xs.append(x)
     stream = torch.cuda.Stream(device=dev)
@@ -812,9 +900,10 @@ def uneven_main(args, W, rank, world, pg):
     batch_img = [plan.image(k) for k in range(W["batch"])]
     rm = [float(plan.stats(k)["RMSE"][-1]) for k in range(W["batch"])]
     plan.close()
-    plain_ms, equal = 0.0, True
+    plain_ms, equal, plain_img, plain_rm = 0.0, True, [], []
     for k in range(W["batch"]):
-        with pkg.Plan(paras[k], paras[k]["phi_vec"], stream=stream.cuda_stream) as pl:
+        pk = dict(paras[k], sino_storage="f32")  # the FP32 plain loop
+        with pkg.Plan(pk, pk["phi_vec"], stream=stream.cuda_stream) as pl:
             pl.set_sinogram(0, Ps[k])
             pl.set_reference(0, xs[k])
             pl.reset()
@@ -827,8 +916,31 @@ def uneven_main(args, W, rank, world, pg):
             e1.record(stream)
             e1.synchronize()
             plain_ms += e0.elapsed_time(e1)
-            equal = equal and bool(np.array_equal(pl.image(0), batch_img[k]))
+            plain_img.append(pl.image(0))
+            plain_rm.append(float(pl.stats(0)["RMSE"][-1]))
+            equal = equal and bool(np.array_equal(plain_img[-1], batch_img[k]))
     value = W["batch"] * world / (ms / 1e3)
+    rr = np.abs(np.array(rm) / np.array(plain_rm) - 1)
+    # the smallest slice through the FP64 oracle (same iterations, exact P)
+    oracle_check = None
+    if rank == 0 and not args.no_cpu:
+        k0 = min(range(W["batch"]), key=lambda k: paras[k]["nx"] ** 2 * len(paras[k]["phi_vec"]))
+        oracle = _oracle()
+        p0 = dict(paras[k0], I0=xs[k0].astype(np.float64))
+        P0 = Ps[k0].astype(np.float64).reshape(paras[k0]["na"], -1, order="F")
+        t = time.perf_counter()
+        m_o, out_o = oracle.asdpocs(P0, p0, nthreads=os.cpu_count() or 1)
+        oracle_check = {
+            "instance": k0, "size": paras[k0]["nx"], "views": len(paras[k0]["phi_vec"]),
+            "oracle_s": time.perf_counter() - t,
+            "rmse_oracle_fp64": float(out_o["RMSE"][-1]),
+            "rmse_batched": rm[k0], "rmse_plain_fp32": plain_rm[k0],
+            "image_rel_l2_batched": float(np.linalg.norm(batch_img[k0] - m_o)
+                                          / np.linalg.norm(m_o)),
+            "image_rel_l2_plain_fp32": float(np.linalg.norm(plain_img[k0] - m_o)
+                                             / np.linalg.norm(m_o)),
+            "note": "alpha 0.2 makes the iteration chaotic: compare the RMSE; images "
+                    "agree only to ~1e-2 even between FP32 runs"}
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": "recons/s", "n_gpus": world,
@@ -837,12 +949,17 @@ def uneven_main(args, W, rank, world, pg):
             "data": "synthetic (seeded random-ellipse phantoms, Poisson noise)",
             "config": {"workload": W["label"], "batch_per_gpu": W["batch"],
                        "iterations": W["iters"], "parallelism": f"replicas x{world}",
-                       "storage": "FP32 (BF16/FP16 storage is not built)",
+                       "storage": f"sinograms {W['storage'].upper()} on the device (FP32 "
+                                  "sums and images, FP64 scalars); plain loop FP32",
                        "l2": "256 MB buffer written between timed steps"},
             "plain": {"recons_per_s": W["batch"] / (plain_ms / 1e3), "ms_total": plain_ms,
                       "batched_speedup": value / world / (W["batch"] / (plain_ms / 1e3)),
-                      "batch_equals_plain_bitwise": equal},
-            "rmse_vs_phantom": {"mean": float(np.mean(rm)), "max": float(np.max(rm))},
+                      "batch_equals_plain_bitwise": equal,
+                      "rmse_rel_diff_vs_plain_fp32": {"max": float(rr.max()),
+                                                      "mean": float(rr.mean())}},
+            "rmse_vs_phantom": {"mean": float(np.mean(rm)), "max": float(np.max(rm)),
+                                "plain_fp32_mean": float(np.mean(plain_rm))},
+            "oracle_check": oracle_check,
             "clocks": clk,
         }))
     return 0
@@ -891,9 +1008,9 @@ def reference_arm(args, W, rank, world, pg):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per_iter * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": W["label"], "iterations": W["iters"]},
+        "config": base_config(W, world),
         "cpu_baseline": {"value": value, "unit": "recons/s", "cores": cores, "kind": kind,
-                         "sample": sample},
+                         "cpu": cpu_model(), "sample": sample},
         "e2e": {"value": value, "unit": "recons/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }))
