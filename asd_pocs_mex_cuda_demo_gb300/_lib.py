@@ -10,7 +10,9 @@ import os
 import threading
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_PKG, "lib", "libasdpocs_gb300.so")
+# ASDPOCS_LIB=checked loads the bounds-checked build (build(checked=True))
+LIB_PATH = os.path.join(_PKG, "lib", "libasdpocs_gb300_checked.so"
+                        if os.environ.get("ASDPOCS_LIB") == "checked" else "libasdpocs_gb300.so")
 
 _F = C.POINTER(C.c_float)
 _D = C.POINTER(C.c_double)
@@ -68,6 +70,7 @@ SIGNATURES = [
     ("asdpocs_last_error", C.c_char_p, []),
     ("asdpocs_last_status", C.c_int, []),
     ("asdpocs_version", C.c_char_p, []),
+    ("asdpocs_checked_errors", C.c_int, [C.POINTER(C.c_ulonglong), C.POINTER(C.c_longlong)]),
     ("Ax_cone_mf_gpu_new", None, [_F, _F, _F, C.c_float, C.c_float, _F, _F, C.c_float,
                                   C.c_float, C.c_float, C.c_float, C.c_int, C.c_int,
                                   C.c_int, C.c_int, C.c_int]),
@@ -139,6 +142,7 @@ SIGNATURES = [
                                         C.POINTER(Options), _F, _F, _F,
                                         C.POINTER(C.c_longlong)]),
     ("asdpocs_server_poll", C.c_int, [C.c_void_p, C.c_longlong, C.POINTER(C.c_int)]),
+    ("asdpocs_server_cancel", C.c_int, [C.c_void_p, C.c_longlong]),
     ("asdpocs_server_wait", C.c_int, [C.c_void_p, C.c_longlong, _F, C.POINTER(Stats), _D,
                                       C.POINTER(JobTimes)]),
     ("asdpocs_server_memory", C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong),

@@ -10,6 +10,46 @@
 namespace asd {
 
 // ---------------------------------------------------------------------------
+// Bounds-checked builds (compiled with -DASDPOCS_CHECKED, the library
+// libasdpocs_gb300_checked.so).  Every volume, sinogram, residual and table
+// index of the projector and TV kernels goes through ASD_IN(i, n) before its
+// access: an index outside [0, n) is counted in a device word of the
+// translation unit (the first one kept with its extent) and the access is
+// skipped -- a load gives 0, a store is dropped -- so a bad index never
+// faults or traps.  asdpocs_checked_errors reads and clears the words.  In
+// the normal build ASD_IN is `true` and costs nothing.
+// ---------------------------------------------------------------------------
+#ifdef ASDPOCS_CHECKED
+static __device__ unsigned long long g_oob_count;
+static __device__ long long g_oob_first[2];  // first bad index and its extent
+__device__ __forceinline__ bool asd_in(long long i, long long n) {
+  if (i >= 0 && i < n) return true;
+  if (atomicAdd(&g_oob_count, 1ull) == 0ull) {
+    g_oob_first[0] = i;
+    g_oob_first[1] = n;
+  }
+  return false;
+}
+#define ASD_IN(i, n) ::asd::asd_in((long long)(i), (long long)(n))
+// Reads and clears this translation unit's words: count, first index, extent.
+#define ASD_CHECKED_READER(name)                                                   \
+  cudaError_t name(unsigned long long *count, long long *first) {                \
+    unsigned long long c = 0, z = 0;                                             \
+    long long f[2] = {0, 0}, zf[2] = {0, 0};                                     \
+    cudaError_t e = cudaMemcpyFromSymbol(&c, g_oob_count, sizeof c);             \
+    if (e == cudaSuccess) e = cudaMemcpyFromSymbol(f, g_oob_first, sizeof f);    \
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_oob_count, &z, sizeof z);     \
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_oob_first, zf, sizeof zf);    \
+    *count = c;                                                                  \
+    first[0] = f[0];                                                             \
+    first[1] = f[1];                                                             \
+    return e;                                                                    \
+  }
+#else
+#define ASD_IN(i, n) true
+#endif
+
+// ---------------------------------------------------------------------------
 // Error reporting (thread-local last error, as returned by asdpocs_last_error)
 // ---------------------------------------------------------------------------
 int set_error(int status, const char *fmt, ...);

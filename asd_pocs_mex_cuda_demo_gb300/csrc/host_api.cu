@@ -137,7 +137,34 @@ extern "C" {
 
 const char *asdpocs_last_error(void) { return g_msg; }
 int asdpocs_last_status(void) { return g_status; }
-const char *asdpocs_version(void) { return "asdpocs_gb300 0.1 (sm_103a)"; }
+const char *asdpocs_version(void) {
+#ifdef ASDPOCS_CHECKED
+  return "asdpocs_gb300 0.2 (sm_103a, bounds-checked)";
+#else
+  return "asdpocs_gb300 0.2 (sm_103a)";
+#endif
+}
+
+int asdpocs_checked_errors(unsigned long long *count, long long first[2]) {
+  clear_error();
+  if (!count || !first) return set_error(ASDPOCS_ERR_ARG, "null pointer");
+#ifdef ASDPOCS_CHECKED
+  ASD_CUDA(cudaDeviceSynchronize());
+  unsigned long long cp = 0, ct = 0;
+  long long fp[2] = {0, 0}, ft[2] = {0, 0};
+  ASD_CUDA(checked_take_proj(&cp, fp));
+  ASD_CUDA(checked_take_tv(&ct, ft));
+  *count = cp + ct;
+  first[0] = cp ? fp[0] : ft[0];
+  first[1] = cp ? fp[1] : ft[1];
+  return 0;
+#else
+  *count = 0;
+  first[0] = first[1] = 0;
+  return set_error(ASDPOCS_ERR_STATE,
+                   "not a bounds-checked build (libasdpocs_gb300_checked.so has the checks)");
+#endif
+}
 
 // ------------------------------------------------------------ projectors
 static int ax_device(const float *x_d, float *y_d, float *sr_d, float cos_phi,

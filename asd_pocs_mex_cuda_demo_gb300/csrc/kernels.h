@@ -24,6 +24,13 @@ size_t atx_zcol_scratch_bytes(const Dims &d);
 cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &g,
                             const Dims &d, void *scratch, cudaStream_t st);
 
+#ifdef ASDPOCS_CHECKED
+// Bounds-checked builds: read and clear the out-of-range counts (and the
+// first bad index with its extent) of the projector and TV kernels.
+cudaError_t checked_take_proj(unsigned long long *count, long long *first);
+cudaError_t checked_take_tv(unsigned long long *count, long long *first);
+#endif
+
 // Stores n FP32 sinogram values (device) as `fmt` (ASDPOCS_STORE_*) at dst.
 cudaError_t launch_store_sinogram(const float *src, void *dst, size_t n, int fmt,
                                   cudaStream_t st);

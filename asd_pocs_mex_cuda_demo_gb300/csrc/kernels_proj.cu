@@ -26,6 +26,12 @@ __device__ __forceinline__ bool tile_voxel(const Dims &D, int &ix, int &iy,
   return asd::tile_voxel(D.nx, D.ny, D.nz, ix, iy, iz);
 }
 
+// Extents of an instance's volume (nx*ny*nz) and view (na*nb), for ASD_IN.
+__device__ __forceinline__ long long nvox(const Dims &D) {
+  return (long long)D.nx * D.ny * D.nz;
+}
+__device__ __forceinline__ long long nray(const Dims &D) { return (long long)D.na * D.nb; }
+
 int atx_blocks(const Dims &d) {
   const dim3 g = tile_grid(d.nx, d.ny, d.nz, 1);
   return (int)(g.x * g.y);
@@ -98,9 +104,10 @@ __global__ void __launch_bounds__(kAxBlock)
   float v[2] = {0.f, 0.f};
   if (in)
     ax_lane_partial(G, D, r, lane + 32 * part,
-                    [&](unsigned i) { return __ldg(x + i); }, v[0], v[1]);
+                    [&](unsigned i) { return ASD_IN(i, nvox(D)) ? __ldg(x + i) : 0.f; },
+                    v[0], v[1]);
   ax_combine<2>(sp, v, part, rw, lane);
-  if (in && part == 0 && lane == 0) {
+  if (in && part == 0 && lane == 0 && ASD_IN(r, nray(D))) {
     y[r] = v[0] * G.scale;
     sr[r] = v[1] * G.scale;
   }
@@ -116,7 +123,8 @@ __global__ void __launch_bounds__(kAxBlock)
   if (r >= (long long)D.na * D.nb) return;  // the whole warp
   const SidRay R = siddon_setup(G, D, G.y_det[r % D.na], G.z_det[r / D.na]);
   float ys = 0.f, ss = 0.f;
-  siddon_columns(R, lane, 32, [&](unsigned i) { return __ldg(x + i); }, ys, ss);
+  siddon_columns(R, lane, 32,
+                 [&](unsigned i) { return ASD_IN(i, nvox(D)) ? __ldg(x + i) : 0.f; }, ys, ss);
   ys = warp_sum(ys);
   ss = warp_sum(ss);
   if (lane == 0) {
@@ -221,7 +229,8 @@ __device__ __forceinline__ void atx_block_sum(const ViewGeo &G, const Dims &D,
     ally = __syncthreads_and(ally);
     for (int k = threadIdx.x; k < nA * nB; k += kAtxThreads) {
       const int r = kPlanar ? 0 : k / nA, c = kPlanar ? k : k - r * nA;
-      const float v = yl((long long)(bmin + r) * D.na + amin + c);
+      const long long yi = (long long)(bmin + r) * D.na + amin + c;
+      const float v = ASD_IN(yi, nray(D)) ? yl(yi) : 0.f;
       narrow = narrow && isfinite(v);
       sh.ys[k] = v;
     }
@@ -308,9 +317,11 @@ __global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 3)
   const bool valid = tile_voxel(D, ix, iy, iz);
   float acc, accl;
   atx_block_sum<kPlanar>(G, D, valid, ix, iy, iz, sh,
-                         [&](long long i) { return __ldg(yv + i); }, acc, accl);
+                         [&](long long i) { return ASD_IN(i, nray(D)) ? __ldg(yv + i) : 0.f; },
+                         acc, accl);
   if (!valid) return;
   const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+  if (!ASD_IN(idx, nvox(D))) return;
   x[idx] = acc * G.scale;
   sc[idx] = accl * G.scale;
 }
@@ -370,7 +381,7 @@ __global__ void __launch_bounds__(kAxBlock)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int rw = warp % kAxWarps, part = warp / kAxWarps;
   const long long r = (long long)blockIdx.x * kAxWarps + rw;
-  if (tabc && part == 0 && lane == 0 && r < nr) {
+  if (tabc && part == 0 && lane == 0 && r < nr && ASD_IN(r, nr)) {
     const int ia = (int)(r % D.na), ib = (int)(r / D.na);
     I.tabC[r] = ray_tab_c(I.tabA[(long long)view * D.na + ia], G.z_det[ib]);
   }
@@ -380,10 +391,11 @@ __global__ void __launch_bounds__(kAxBlock)
     const float *m = I.m;
     if constexpr (kExact) {
       const SidRay R = siddon_setup(G, D, G.y_det[r % D.na], G.z_det[r / D.na]);
-      siddon_columns(R, lane + 32 * part, 32 * kAxCols, [&](unsigned i) { return m[i]; },
-                     v[0], v[1]);
+      siddon_columns(R, lane + 32 * part, 32 * kAxCols,
+                     [&](unsigned i) { return ASD_IN(i, nvox(D)) ? m[i] : 0.f; }, v[0], v[1]);
     } else {
-      ax_lane_partial(G, D, r, lane + 32 * part, [&](unsigned i) { return m[i]; }, v[0],
+      ax_lane_partial(G, D, r, lane + 32 * part,
+                      [&](unsigned i) { return ASD_IN(i, nvox(D)) ? m[i] : 0.f; }, v[0],
                       v[1]);
     }
   }
@@ -391,9 +403,10 @@ __global__ void __launch_bounds__(kAxBlock)
   float pt[2] = {0.f, 0.f};  // dd2, non-finite residuals
   if (r < nr && part == 0 && lane == 0) {
     const float yv = v[0] * G.scale, srv = v[1] * G.scale;
-    const float c0 = sino_at(I, (long long)view * nr + r) - yv;
+    const long long pi = (long long)view * nr + r;
+    const float c0 = (ASD_IN(pi, nr * I.nv) ? sino_at(I, pi) : 0.f) - yv;
     const float cr = c0 / (srv == 0.f ? 1.f : srv);
-    I.cor[r * I.cor_stride] = cr;
+    if (ASD_IN(r, nr)) I.cor[r * I.cor_stride] = cr;
     pt[0] = c0 * c0;
     pt[1] = isfinite(cr) ? 0.f : 1.f;
   }
@@ -467,7 +480,7 @@ __device__ __forceinline__ void sart_atx_tiles_tab(const Inst &I, const ViewGeo 
     float pre[kChordPre];
 #pragma unroll
     for (int k = 0; k < kChordPre; k++) pre[k] = 0.f;
-    if (valid) {
+    if (valid && ASD_IN(vi, N)) {
       h = __ldg(tab + vi);
       accl = __int_as_float(__ldg(tab + N + vi));
 #pragma unroll
@@ -477,13 +490,15 @@ __device__ __forceinline__ void sart_atx_tiles_tab(const Inst &I, const ViewGeo 
     }
     const int cnt = (int)((unsigned)h >> 24), first = h & 0xffffff;
     const int kA = __reduce_max_sync(0xffffffffu, cnt);
+    const long long M = nray(D);
     float acc = 0.f;
 #pragma unroll
     for (int ka = 0; ka < kChordPre; ka++)
-      if (ka < kA && ka < cnt) acc += pre[ka] * __ldg(cor + first + ka);
+      if (ka < kA && ka < cnt && ASD_IN(first + ka, M)) acc += pre[ka] * __ldg(cor + first + ka);
     for (int ka = kChordPre; ka < kA; ka++)
-      if (ka < cnt) acc += __ldg(ch + (size_t)ka * N) * __ldg(cor + first + ka);
-    if (valid) {
+      if (ka < cnt && ASD_IN(ka, K) && ASD_IN(first + ka, M))
+        acc += __ldg(ch + (size_t)ka * N) * __ldg(cor + first + ka);
+    if (valid && ASD_IN(vi, N)) {
       const float bp = acc * G.scale, scv = accl * G.scale;
       const float mn = mv + beta * __fdividef(bp, scv == 0.f ? 1.f : scv);
       m[vi] = mn < 0.f ? 0.f : mn;
@@ -517,7 +532,9 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
     if (!planar_ok) {
       // planar kernel on a geometry with z_det != 0: direct per-pair form
       if (valid)
-        voxel_backproject(G, D, w, [&](long long i) { return cor[i]; }, acc, accl);
+        voxel_backproject(G, D, w,
+                          [&](long long i) { return ASD_IN(i, nray(D)) ? cor[i] : 0.f; }, acc,
+                          accl);
     } else {
       int lo = has ? w.a0 : 0, hi = has ? w.a1 : -1;
       int blo = has ? w.b0 : 0, bhi = has ? w.b1 : -1;
@@ -546,8 +563,8 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
           for (int ka = 0; ka < kA; ka++) {
             const bool on = onb && ka < cntA;
             const int ia = on ? lo + ka : 0;
-            const float4 A = __ldg(tabA + ia);
-            const float yv = on ? __ldg(cor + ia) : 0.f;
+            const float4 A = ASD_IN(ia, D.na) ? __ldg(tabA + ia) : make_float4(1.f, 1.f, 1.f, 1.f);
+            const float yv = on && ASD_IN(ia, nray(D)) ? __ldg(cor + ia) : 0.f;
             const float l = chord_sel<AX>(A, rx, ry, G.dz);
             if (on) {
               acc += l * yv;
@@ -566,10 +583,11 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
           const bool on = k < cnt;
           const int ia = on ? lo + ka : 0, ibs = on ? ib : 0;
           const int r = ibs * D.na + ia;
-          const float c = __ldg(G.z_det + ibs) - 0.0f;
-          const float4 A = __ldg(tabA + ia);
-          const float4 Cs = __ldg(tabC + r);
-          const float yv = on ? __ldg(cor + r) : 0.f;
+          const bool ok = ASD_IN(ibs, D.nb) && ASD_IN(ia, D.na) && ASD_IN(r, nray(D));
+          const float c = (ok ? __ldg(G.z_det + ibs) : 0.f) - 0.0f;
+          const float4 A = ok ? __ldg(tabA + ia) : make_float4(1.f, 1.f, 1.f, 1.f);
+          const float4 Cs = ok ? __ldg(tabC + r) : make_float4(0.f, 0.f, 0.f, 0.f);
+          const float yv = on && ok ? __ldg(cor + r) : 0.f;
           const float l = AX == 0 ? chord3_bf(A, Cs, c, rx, ry, rz, G.dz)
                                   : chord3_axis<AX == 1>(A, Cs, rx, ry, rz, G.dz);
           if (on) {
@@ -583,9 +601,9 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
         }
       }
     }
-    if (valid) {
+    const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+    if (valid && ASD_IN(idx, nvox(D))) {
       const float bp = acc * G.scale, scv = accl * G.scale;
-      const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
       const float mn = m[idx] + beta * __fdividef(bp, scv == 0.f ? 1.f : scv);
       m[idx] = mn < 0.f ? 0.f : mn;
     }
@@ -685,14 +703,16 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
     if (!valid) return;
     for (int iz = z0; iz < z1; iz++) {
       const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+      if (!ASD_IN(idx, nvox(D))) continue;
       begin(idx);
       const VoxelWin w = voxel_window(G, D, ix, iy, iz);
       const float rx = G.cos_phi * (-G.SO) - w.xc, ry = G.sin_phi * (-G.SO) - w.yc;
       const float rz = 0.0f - w.zc;
       for (int ib = w.b0; ib <= w.b1; ib++) {
-        const float c = __ldg(G.z_det + ib) - 0.0f;
+        const float c = (ASD_IN(ib, D.nb) ? __ldg(G.z_det + ib) : 0.f) - 0.0f;
         for (int ia = w.a0; ia <= w.a1; ia++) {
           const int r = ib * D.na + ia;
+          if (!(ASD_IN(ia, D.na) && ASD_IN(r, nray(D)))) continue;
           pair(r, chord3_bf(__ldg(tabA + ia), __ldg(tabC + r), c, rx, ry, rz, G.dz), true);
         }
       }
@@ -712,6 +732,7 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
     wide = cntA > kZColA;
     if (!wide)
       for (int k = 0; k < cntA; k++) {
+        if (!ASD_IN(col.lo + k, D.na)) continue;
         const ColFaces f = col_faces(__ldg(tabA + col.lo + k), col.rx, col.ry);
         sh.pts[k][t] = make_float4(f.p1x, f.p1y, f.p2x, f.p2y);
         sh.bits[k][t] = f.bits;
@@ -719,7 +740,8 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
   }
   for (int iz = z0; iz < z1; iz++) {
     const unsigned idx = ((unsigned)iz * D.ny + iy) * D.nx + ix;
-    if (valid) begin(idx);
+    const bool vin = valid && ASD_IN(idx, nvox(D));
+    if (vin) begin(idx);
     float zc = 0.f;
     int blo = 0, bhi = -1;
     const bool has = valid && zcol_rows(G, D, col, iz, zc, blo, bhi);
@@ -733,7 +755,8 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
       const int kk = on ? ka : 0;
       const int ia = on ? col.lo + ka : 0;
       const int r = (on ? ib : 0) * D.na + ia;
-      const float4 Cs = __ldg(tabC + r);
+      const bool rin = ASD_IN(r, nray(D)) && ASD_IN(ia, D.na);
+      const float4 Cs = rin ? __ldg(tabC + r) : make_float4(0.f, 0.f, 0.f, 0.f);
       float l;
       if (!wide) {
         const float4 p = sh.pts[kk][t];
@@ -746,13 +769,13 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
       } else {
         l = chord3_bf(__ldg(tabA + ia), Cs, 0.0f, col.rx, col.ry, rz, G.dz);
       }
-      pair(r, l, on);
+      pair(r, l, on && rin);
       if (++ka == cntA) {
         ka = 0;
         ib++;
       }
     }
-    if (valid) voxel(idx);
+    if (vin) voxel(idx);
   }
 }
 
@@ -808,8 +831,8 @@ __global__ void __launch_bounds__(256)
     const int ia = (int)(r % D.na), ib = (int)(r / D.na);
     const float yd = G.y_det[ia], zd = G.z_det[ib];
     const float4 A = ray_tab_a(G, yd);
-    if (ib == 0) tabA[ia] = A;
-    tabC[r] = ray_tab_c(A, zd);
+    if (ib == 0 && ASD_IN(ia, D.na)) tabA[ia] = A;
+    if (ASD_IN(r, nr)) tabC[r] = ray_tab_c(A, zd);
     ok = A.x != 0.0f && A.y != 0.0f && on_grid(yd, ia, D.na, G.dy_det) &&
          on_grid(zd, ib, D.nb, G.dz_det) && isfinite(yv[r]) && G.dy_det > 0.0f &&
          G.dz_det > 0.0f;
@@ -924,7 +947,8 @@ __device__ __forceinline__ void atx_shared_voxel(
 #pragma unroll
           for (int q = 0; q < kShareGroup / 4; q++) {
             if (!((active >> (4 * q)) & 0xFu)) continue;
-            const float4 c4 = __ldg(corg + r * (kShareGroup / 4) + q);
+            const float4 c4 = ASD_IN(r, nray(D)) ? __ldg(corg + r * (kShareGroup / 4) + q)
+                                                 : make_float4(0.f, 0.f, 0.f, 0.f);
             acc[4 * q] += l * c4.x;
             acc[4 * q + 1] += l * c4.y;
             acc[4 * q + 2] += l * c4.z;
@@ -958,7 +982,8 @@ __device__ __forceinline__ void atx_shared_voxel(
     for (int kb = 0; kb < kB; kb++) {
       const bool onb = kb < cntB;
       const int ib = blo + kb;
-      const float c = kPlanar ? 0.0f : (onb ? __ldg(G.z_det + ib) : 1.0f) - 0.0f;
+      const float c =
+          kPlanar ? 0.0f : ((onb && ASD_IN(ib, D.nb)) ? __ldg(G.z_det + ib) : 1.0f) - 0.0f;
       const int row = onb ? ib * D.na : 0;
       for (int c0 = 0; c0 < kA; c0 += kPairChunk) {
         float l[kPairChunk];
@@ -972,13 +997,15 @@ __device__ __forceinline__ void atx_shared_voxel(
           idx[j] = row + ia;
           l[j] = 0.f;
           if (ka < kA) {  // warp-uniform
-            const float4 A = __ldg(tabA + ia);
+            const bool okr = ASD_IN(ia, D.na) && ASD_IN(row + ia, nray(D));
+            const float4 A = okr ? __ldg(tabA + ia) : make_float4(1.f, 1.f, 1.f, 1.f);
             if (kPlanar)
               l[j] = chord_sel<AX>(A, rx, ry, G.dz);
             else if (AX == 0)
-              l[j] = chord3_bf(A, __ldg(tabC + row + ia), c, rx, ry, rz, G.dz);
+              l[j] = okr ? chord3_bf(A, __ldg(tabC + row + ia), c, rx, ry, rz, G.dz) : 0.f;
             else
-              l[j] = chord3_axis<AX == 1>(A, __ldg(tabC + row + ia), rx, ry, rz, G.dz);
+              l[j] = okr ? chord3_axis<AX == 1>(A, __ldg(tabC + row + ia), rx, ry, rz, G.dz)
+                         : 0.f;
           }
           if (on[j]) accl += l[j];
         }
@@ -990,7 +1017,9 @@ __device__ __forceinline__ void atx_shared_voxel(
               // quads of the group with no running instance are skipped
               // (block-uniform); their accumulators are never read
               if (!((active >> (4 * q)) & 0xFu)) continue;
-              const float4 c4 = __ldg(corg + (long long)idx[j] * (kShareGroup / 4) + q);
+              const float4 c4 = ASD_IN(idx[j], nray(D))
+                                    ? __ldg(corg + (long long)idx[j] * (kShareGroup / 4) + q)
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
               acc[4 * q] += l[j] * c4.x;
               acc[4 * q + 1] += l[j] * c4.y;
               acc[4 * q + 2] += l[j] * c4.z;
@@ -1002,8 +1031,9 @@ __device__ __forceinline__ void atx_shared_voxel(
     }
   }
   if (!valid) return;
-  atx_shared_apply(G, ((unsigned)iz * D.ny + iy) * D.nx + ix, accl, acc, active, gn,
-                   m_il, s_beta);
+  const unsigned vi = ((unsigned)iz * D.ny + iy) * D.nx + ix;
+  if (!ASD_IN(vi, nvox(D))) return;
+  atx_shared_apply(G, vi, accl, acc, active, gn, m_il, s_beta);
 }
 
 // Pairs of this voxel: the reference's window narrowed to the voxel's shadow.
@@ -1036,9 +1066,11 @@ __device__ __forceinline__ void chords_voxel(const ViewGeo &G, const Dims &D,
   }
   const float rx = G.cos_phi * (-G.SO) - w.xc;
   const float ry = G.sin_phi * (-G.SO) - w.yc;
+  if (!ASD_IN(vi, N)) return;
   float *ch = (float *)(tab + 2 * N) + vi;
   float accl = 0.f;
   for (int ka = 0; ka < cnt; ka++) {
+    if (!(ASD_IN(lo + ka, D.na) && ASD_IN(ka, K))) continue;
     const float l = chord_sel<AX>(__ldg(tabA + lo + ka), rx, ry, G.dz);
     accl += l;
     ch[(size_t)ka * N] = l;
@@ -1097,7 +1129,7 @@ __device__ __forceinline__ void atx_shared_voxel_tab(
   float4 m4[kShareGroup / 4];
 #pragma unroll
   for (int k = 0; k < kChordPre; k++) pre[k] = 0.f;
-  if (valid) {
+  if (valid && ASD_IN(vi, N)) {
     h = __ldg(tab + vi);
     accl = __int_as_float(__ldg(tab + N + vi));
 #pragma unroll
@@ -1114,6 +1146,7 @@ __device__ __forceinline__ void atx_shared_voxel_tab(
   for (int b = 0; b < kShareGroup; b++) acc[b] = 0.f;
   auto pair = [&](int ka, float l) {
     const long long r = first + ka;
+    if (!ASD_IN(r, nray(D))) return;
 #pragma unroll
     for (int q = 0; q < kShareGroup / 4; q++) {
       if (!((active >> (4 * q)) & 0xFu)) continue;
@@ -1128,8 +1161,8 @@ __device__ __forceinline__ void atx_shared_voxel_tab(
   for (int ka = 0; ka < kChordPre; ka++)
     if (ka < kA && ka < cnt) pair(ka, pre[ka]);
   for (int ka = kChordPre; ka < kA; ka++)
-    if (ka < cnt) pair(ka, __ldg(ch + (size_t)ka * N));
-  if (!valid) return;
+    if (ka < cnt && ASD_IN(ka, K)) pair(ka, __ldg(ch + (size_t)ka * N));
+  if (!valid || !ASD_IN(vi, N)) return;
   // atx_shared_apply with the image values already loaded
   const float scv = accl * G.scale;
 #pragma unroll
@@ -1260,7 +1293,7 @@ __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
   const long long r = (long long)blockIdx.x * kAxWarps + rw;
   // cone beam: the plan's one ray-slope table, refreshed by group 0 every
   // view whether or not its instances still run
-  if (k3D && blockIdx.z == 0 && part == 0 && lane == 0 && r < nr) {
+  if (k3D && blockIdx.z == 0 && part == 0 && lane == 0 && r < nr && ASD_IN(r, nr)) {
     const int ia = (int)(r % D.na), ib = (int)(r / D.na);
     I0.tabC[r] = ray_tab_c(I0.tabA[(long long)view * D.na + ia], G.z_det[ib]);
   }
@@ -1297,6 +1330,7 @@ __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
 #pragma unroll
           for (int j = 0; j < kP; j++) {
             const float4 *p = mg + (size_t)id[u][j] * kQuads + q0;
+            f[u][j] = f[u][j] && ASD_IN(id[u][j], nvox(D));
 #pragma unroll
             for (int q = 0; q < kQ; q++)
               x[u][j][q] = (f[u][j] && ((active >> (4 * q)) & 0xFu))
@@ -1335,9 +1369,10 @@ __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
   if (part == 0 && lane < gn && ((active >> lane) & 1u) && r < nr) {
     const Inst &Ib = insts[gi + lane];
     const float yv = yb * G.scale, srv = v[kS] * G.scale;
-    const float c0 = sino_at(Ib, (long long)view * nr + r) - yv;
+    const long long pi = (long long)view * nr + r;
+    const float c0 = (ASD_IN(pi, nr * Ib.nv) ? sino_at(Ib, pi) : 0.f) - yv;
     const float cr = c0 / (srv == 0.f ? 1.f : srv);
-    Ib.cor[r * Ib.cor_stride] = cr;
+    if (ASD_IN(r, nr)) Ib.cor[r * Ib.cor_stride] = cr;
     p0 = c0 * c0;
     p1 = isfinite(cr) ? 0.f : 1.f;
   }
@@ -1579,6 +1614,10 @@ cudaError_t launch_view_tables(const Inst *insts, int batch, const Dims &d,
   k_view_tables<<<dim3((d.na + 127) / 128, nv, batch), 128, 0, st>>>(insts);
   return cudaGetLastError();
 }
+
+#ifdef ASDPOCS_CHECKED
+ASD_CHECKED_READER(checked_take_proj)
+#endif
 
 int reduce_blocks_for(const Dims &d) {
   const long long nr = (long long)d.na * d.nb;

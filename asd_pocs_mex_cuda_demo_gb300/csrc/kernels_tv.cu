@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kThreads)
   T v = T(0);
   if (tile_voxel(nx, ny, nz, ix, iy, iz)) {
     const long long i = ((long long)iz * ny + iy) * nx + ix;
-    const T d = img[i] - (old ? old[i] : T(0));
+    const T d = ASD_IN(i, (long long)nx * ny * nz) ? img[i] - (old ? old[i] : T(0)) : T(0);
     v = d * d;
   }
   double tot;
@@ -241,6 +241,7 @@ __global__ void __launch_bounds__(kThreads)
   if (!tile_voxel(nx, ny, nz, ix, iy, iz)) return;
   const T g = tv_grad<T>(GlobalAt<T>{src, nx, ny, nz, ix, iy, iz}, nz >= 2);
   const long long i = ((long long)iz * ny + iy) * nx + ix;
+  if (!ASD_IN(i, (long long)nx * ny * nz)) return;
   T r;
   if (sizeof(T) == 8) {
     r = (T)((double)src[i] - alpha * scal[0] * (double)g / scal[1]);
@@ -320,8 +321,10 @@ __device__ __forceinline__ void load_tile(Tile<H, k3D> &t, const float *src,
     const int tx = k % W, ty = (k / W) % Hh, tz = k / (W * Hh);
     const int x = x0 - H + tx, y = y0 - H + ty, zz = k3D ? z - H + tz : z;
     float v = 0.f;
-    if (x >= 0 && y >= 0 && zz >= 0 && x < D.nx && y < D.ny && zz < D.nz)
-      v = src[((unsigned)zz * D.ny + y) * D.nx + x];
+    const long long si = ((long long)zz * D.ny + y) * D.nx + x;
+    if (x >= 0 && y >= 0 && zz >= 0 && x < D.nx && y < D.ny && zz < D.nz &&
+        ASD_IN(si, (long long)D.nx * D.ny * D.nz))
+      v = src[si];
     t.v[tz][ty][tx] = v;
   }
 }
@@ -393,8 +396,8 @@ __global__ void __launch_bounds__(kThreads)
       __syncthreads();
     }
     const int ix = x0 + tx, iy = y0 + ty;
-    if (ix < D.nx && iy < D.ny) {
-      const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
+    const unsigned i = ((unsigned)z * D.ny + iy) * D.nx + ix;
+    if (ix < D.nx && iy < D.ny && ASD_IN(i, (long long)D.nx * D.ny * D.nz)) {
       const float m = I.m[i];
       I.m_res[i] = m;
       const float a = m - I.m_pre[i];
@@ -508,6 +511,7 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
   const int jl0 = y0 - 2, jl1 = min(D.ny, y1 + 2);  // rows of m read
   const int j1 = y1 + 2;                            // rows walked: jl0 .. j1 - 1
   const float coef_a = ina ? coef : 0.f, coef_b = inb ? coef : 0.f;
+  const long long N2 = (long long)D.nx * D.ny;  // bounds-checked builds
   // Rows of m stream through a ring of kWalkRing rows per warp (each lane
   // its two columns), copied asynchronously kWalkRing - 1 rows ahead of the
   // one in use and zero-filled outside the image and the walk; one copy
@@ -523,15 +527,18 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
     const int off = r ? j * D.nx : 0;
     float *d = (float *)(my + 32 * slot);
     float *d0 = (float *)(my0 + 32 * slot);
+    const bool va = r && ina && ASD_IN((long long)off + xa, N2) &&
+                    (!kPair || ASD_IN((long long)off + xa + 1, N2));
+    const bool vb = r && inb && ASD_IN((long long)off + xa + 1, N2);
     if (kPair) {
-      cp_async_8(d, la + off, r && ina);
-      if (kMode == 2) cp_async_8(d0, l0a + off, r && ina);
+      cp_async_8(d, la + off, va);
+      if (kMode == 2) cp_async_8(d0, l0a + off, va);
     } else {
-      cp_async_4(d, la + off, r && ina);
-      cp_async_4(d + 1, lb + off, r && inb);
+      cp_async_4(d, la + off, va);
+      cp_async_4(d + 1, lb + off, vb);
       if (kMode == 2) {
-        cp_async_4(d0, l0a + off, r && ina);
-        cp_async_4(d0 + 1, l0b + off, r && inb);
+        cp_async_4(d0, l0a + off, va);
+        cp_async_4(d0 + 1, l0b + off, vb);
       }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -578,7 +585,7 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
         const float mca = pa < 0.f ? 0.f : pa;  // imgTVGradMin.cpp:110-116
         const float mcb = pb < 0.f ? 0.f : pb;
         if (kPair) {
-          if (outa) {
+          if (outa && ASD_IN(i + 1, N2) && ASD_IN(i, N2)) {
             const float da = mca - f0.x, db = mcb - f0.y;
             acc += da * da;
             acc += db * db;
@@ -586,13 +593,13 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
             *(float2 *)(impre + i) = make_float2(mca, mcb);
           }
         } else {
-          if (outa) {
+          if (outa && ASD_IN(i, N2)) {
             const float d = mca - f0.x;
             acc += d * d;
             im[i] = mca;
             impre[i] = mca;
           }
-          if (outb) {
+          if (outb && ASD_IN(i + 1, N2)) {
             const float d = mcb - f0.y;
             acc += d * d;
             im[i + 1] = mcb;
@@ -604,10 +611,10 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
       if (out1) {
         const int i = o1 * D.nx + xa;
         if (kPair) {
-          if (outa) *(float2 *)(dst + i) = make_float2(pa, pb);
+          if (outa && ASD_IN(i, N2) && ASD_IN(i + 1, N2)) *(float2 *)(dst + i) = make_float2(pa, pb);
         } else {
-          if (outa) dst[i] = pa;
-          if (outb) dst[i + 1] = pb;
+          if (outa && ASD_IN(i, N2)) dst[i] = pa;
+          if (outb && ASD_IN(i + 1, N2)) dst[i + 1] = pb;
         }
       }
       if (kMode == 0) {
@@ -718,18 +725,22 @@ __device__ __forceinline__ void sweep_walk(const Inst &I, int y0, int y1, int xa
   float *const mres = I.m_res;
   const float *srcs[4] = {I.m, I.m_pre, I.m_k1, ref ? I.I0 : I.m};
   const int jl0 = y0 - 1, jl1 = min(D.ny, y1 + 1);  // rows read
+  const long long N2 = (long long)D.nx * D.ny;       // bounds-checked builds
   auto fetch = [&](int j, int slot) {
     const bool r = (unsigned)j < (unsigned)jl1;
     const int off = r ? j * D.nx : 0;
+    const bool va = r && ina && ASD_IN((long long)off + xa, N2) &&
+                    (!kPair || ASD_IN((long long)off + xa + 1, N2));
+    const bool vb = r && inb && ASD_IN((long long)off + xa + 1, N2);
 #pragma unroll
     for (int a = 0; a < 4; a++) {
       float *d = (float *)&ring[a][32 * slot + lane];
       const float *g = srcs[a] + off;
       if (kPair) {
-        cp_async_8(d, g + (ina ? xa : 0), r && ina);
+        cp_async_8(d, g + (ina ? xa : 0), va);
       } else {
-        cp_async_4(d, g + (ina ? xa : 0), r && ina);
-        cp_async_4(d + 1, g + (inb ? xa + 1 : 0), r && inb);
+        cp_async_4(d, g + (ina ? xa : 0), va);
+        cp_async_4(d + 1, g + (inb ? xa + 1 : 0), vb);
       }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -767,13 +778,13 @@ __device__ __forceinline__ void sweep_walk(const Inst &I, int y0, int y1, int xa
     };
     if (outa) {
       add(mo.x, pre.x, k1.x, i0.x, va);
-      if (!kPair) mres[i] = mo.x;
+      if (!kPair && ASD_IN(i, N2)) mres[i] = mo.x;
     }
     if (outb) {
       add(mo.y, pre.y, k1.y, i0.y, vb);
-      if (!kPair) mres[i + 1] = mo.y;
+      if (!kPair && ASD_IN(i + 1, N2)) mres[i + 1] = mo.y;
     }
-    if (kPair && outa) *(float2 *)(mres + i) = mo;
+    if (kPair && outa && ASD_IN(i, N2) && ASD_IN(i + 1, N2)) *(float2 *)(mres + i) = mo;
     if ((o + 1) % kBandRows == 0 || o + 1 == y1) {
 #pragma unroll
       for (int k = 0; k < 4; k++) {
@@ -885,8 +896,9 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
   auto stage = [&](int z) {  // slice z into ring slot z & 3
 #pragma unroll
     for (int h = 0; h < 2; h++) {
-      const bool in = in2[h] && zin(z);
-      const float *g = in ? src + (z * plane + (long long)gy[h] * D.nx + gx) : src;
+      const long long gi = z * plane + (long long)gy[h] * D.nx + gx;
+      const bool in = in2[h] && zin(z) && ASD_IN(gi, plane * D.nz);
+      const float *g = in ? src + gi : src;
       const unsigned sa = (unsigned)__cvta_generic_to_shared(&sm[z & 3][warp + 16 * h][lane]);
       asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(g),
                    "r"(in ? 4 : 0)
@@ -939,7 +951,10 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
     if (kMode == 2 && k - 1 >= z0 && k - 1 < z1) {
 #pragma unroll
       for (int h = 0; h < 2; h++)
-        if (outvox(h)) f0[h] = im[(k - 1) * plane + (long long)gy[h] * D.nx + gx];
+        if (outvox(h)) {
+          const long long gi = (k - 1) * plane + (long long)gy[h] * D.nx + gx;
+          f0[h] = ASD_IN(gi, plane * D.nz) ? im[gi] : 0.f;
+        }
     }
     if (k + 1 <= kend)
       stage(k + 1);
@@ -974,6 +989,7 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
         const int yy = warp + 16 * h;
         const float mn = __fmaf_rn(-coef, vat(m0, m1, m2, r1, r2, yy), m1[yy][lane]);
         const long long gi = zb * plane + (long long)gy[h] * D.nx + gx;
+        if (!ASD_IN(gi, plane * D.nz)) continue;
         if (kMode == 1) {
           dst[gi] = mn;
         } else {
@@ -1003,7 +1019,8 @@ __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0
       for (int h = 0; h < 2; h++) {
         if (!outvox(h)) continue;
         const int yy = warp + 16 * h;
-        dst[zd * plane + (long long)gy[h] * D.nx + gx] = p1[yy][lane];
+        const long long gi = zd * plane + (long long)gy[h] * D.nx + gx;
+        if (ASD_IN(gi, plane * D.nz)) dst[gi] = p1[yy][lane];
         const float w = vat(p0, p1, p2, sq[zd & 1], sq[(zd + 1) & 1], yy);
         acc += w * w;
       }
@@ -1192,5 +1209,9 @@ cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
   k_finish_iter<<<tile_grid(d.nx, d.ny, d.nz, batch), kThreads, 0, st>>>(insts);
   return cudaGetLastError();
 }
+
+#ifdef ASDPOCS_CHECKED
+ASD_CHECKED_READER(checked_take_tv)
+#endif
 
 }  // namespace asd

@@ -53,6 +53,7 @@ struct Job {
   std::vector<float> P, m0, I0;  // host copies, dropped after upload
   std::vector<uint16_t> P16;     // the sinogram in FP16 / BF16 storage
   bool has_m0 = false, has_ref = false;
+  bool cancel = false;  // asdpocs_server_cancel on a running job
   int state = ASDPOCS_JOB_QUEUED;
   Clock::time_point t_submit, t_admit, t_done;
   InstLayout lay{};
@@ -394,6 +395,25 @@ bool launch_iteration(asdpocs_server sv, Lane &L) {
   return true;
 }
 
+// A cancelled running job leaves slot s: the slot's descriptor is emptied and
+// the job's memory freed, both in the order of the lane's stream (after the
+// iterations already queued, which may still use it); no results are copied.
+bool drop(asdpocs_server sv, Lane &L, int s) {
+  Job *J = L.slot_job[s];
+  L.slot_desc[s] = empty_slot(L, s);
+  SV_CUDA(cudaMemcpyAsync(L.d_inst + s, &L.slot_desc[s], sizeof(Inst),
+                          cudaMemcpyHostToDevice, L.st));
+  SV_CUDA(cudaFreeAsync(J->dev, L.st));
+  J->dev = nullptr;
+  sv->in_use -= J->lay.bytes;
+  L.slot_job[s] = nullptr;
+  L.active--;
+  J->state = ASDPOCS_JOB_CANCELLED;
+  J->t_done = Clock::now();
+  sv->cv_done.notify_all();
+  return true;
+}
+
 // One pass over a lane; returns false on a CUDA error.  `progress` is set
 // when something changed.
 bool lane_step(asdpocs_server sv, Lane &L, bool &progress) {
@@ -429,6 +449,13 @@ bool lane_step(asdpocs_server sv, Lane &L, bool &progress) {
     L.inflight.pop_front();
     progress = true;
   }
+  // cancelled running jobs
+  for (int s = 0; s < L.S; s++)
+    if (Job *J = L.slot_job[s])
+      if (J->cancel && J->state == ASDPOCS_JOB_RUNNING) {
+        if (!drop(sv, L, s)) return false;
+        progress = true;
+      }
   // admissions (FIFO per lane, within the HBM budget)
   while (!L.queue.empty()) {
     Job *J = L.queue.front();
@@ -623,6 +650,45 @@ int asdpocs_server_poll(asdpocs_server sv, long long job, int *state) {
   return 0;
 }
 
+int asdpocs_server_cancel(asdpocs_server sv, long long job) {
+  clear_error();
+  if (!sv) return set_error(ASDPOCS_ERR_ARG, "null server");
+  std::lock_guard<std::mutex> lk(sv->mu);
+  auto it = sv->jobs.find(job);
+  if (it == sv->jobs.end()) return set_error(ASDPOCS_ERR_ARG, "unknown job %lld", job);
+  Job *J = it->second.get();
+  if (J->state == ASDPOCS_JOB_QUEUED) {
+    // still on the server's pending list or in its lane's queue: drop it there
+    auto p = std::find(sv->pending.begin(), sv->pending.end(), J);
+    if (p != sv->pending.end()) {
+      sv->pending.erase(p);
+    } else {
+      auto L = sv->lanes.find(protocol_key(J->g, J->phi));
+      if (L != sv->lanes.end()) {
+        auto q = std::find(L->second->queue.begin(), L->second->queue.end(), J);
+        if (q != L->second->queue.end()) L->second->queue.erase(q);
+      }
+    }
+    J->state = ASDPOCS_JOB_CANCELLED;
+    J->t_done = Clock::now();
+    sv->cv_done.notify_all();
+    return 0;
+  }
+  if (J->state == ASDPOCS_JOB_RUNNING) {
+    auto L = sv->lanes.find(protocol_key(J->g, J->phi));
+    const bool in_slot = L != sv->lanes.end() && J->slot >= 0 &&
+                         J->slot < (int)L->second->slot_job.size() &&
+                         L->second->slot_job[J->slot] == J;
+    if (in_slot) {
+      J->cancel = true;  // the worker empties the slot
+      sv->cv_work.notify_all();
+      return 0;
+    }
+    return set_error(ASDPOCS_ERR_STATE, "job %lld is already copying out its results", job);
+  }
+  return set_error(ASDPOCS_ERR_STATE, "job %lld has finished", job);
+}
+
 int asdpocs_server_wait(asdpocs_server sv, long long job, float *m_res,
                         asdpocs_stats *st, double *rmse, asdpocs_job_times *t) {
   clear_error();
@@ -632,10 +698,13 @@ int asdpocs_server_wait(asdpocs_server sv, long long job, float *m_res,
   if (it == sv->jobs.end()) return set_error(ASDPOCS_ERR_ARG, "unknown job %lld", job);
   Job *J = it->second.get();
   sv->cv_done.wait(lk, [&] {
-    return J->state == ASDPOCS_JOB_DONE || J->state == ASDPOCS_JOB_FAILED;
+    return J->state == ASDPOCS_JOB_DONE || J->state == ASDPOCS_JOB_FAILED ||
+           J->state == ASDPOCS_JOB_CANCELLED;
   });
   int rc = 0;
-  if (J->state == ASDPOCS_JOB_FAILED) {
+  if (J->state == ASDPOCS_JOB_CANCELLED) {
+    rc = set_error(ASDPOCS_ERR_STATE, "job %lld was cancelled", job);
+  } else if (J->state == ASDPOCS_JOB_FAILED) {
     rc = set_error(ASDPOCS_ERR_CUDA, "job failed: %s",
                    sv->error.empty() ? "server stopped" : sv->error.c_str());
   } else {

@@ -70,6 +70,12 @@ class Server:
         check(load().asdpocs_server_poll(self._h, int(job), C.byref(st)))
         return st.value
 
+    def cancel(self, job: int):
+        """Cancel a queued or running job (its slot and memory are released in
+        stream order; the other jobs are unaffected).  The job must still be
+        collected with wait(), which then raises AsdpocsError."""
+        check(load().asdpocs_server_cancel(self._h, int(job)))
+
     def wait(self, job: int):
         """Block until the job is done; returns (m_res, out, times)."""
         info = self._jobs.pop(job, None)

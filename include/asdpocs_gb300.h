@@ -43,6 +43,15 @@ int asdpocs_last_status(void);
 /* Library version string. */
 const char *asdpocs_version(void);
 
+/* Bounds-checked build only (libasdpocs_gb300_checked.so, compiled with
+ * ASDPOCS_CHECKED; no counterpart in the reference, which checks nothing):
+ * the number of out-of-range volume, sinogram, residual and table indices
+ * the projector and TV kernels met since the last call (each such access
+ * was skipped), and the first one with its extent in first[0], first[1].
+ * Synchronises the device; clears the counts.  The normal build returns
+ * ASDPOCS_ERR_STATE. */
+int asdpocs_checked_errors(unsigned long long *count, long long first[2]);
+
 /* ------------------------------------------------------------------ */
 /* Launcher drop-ins: identical signatures to the reference            */
 /* ------------------------------------------------------------------ */
@@ -405,7 +414,8 @@ enum {
   ASDPOCS_JOB_QUEUED = 0,
   ASDPOCS_JOB_RUNNING = 1,
   ASDPOCS_JOB_DONE = 2,
-  ASDPOCS_JOB_FAILED = 3
+  ASDPOCS_JOB_FAILED = 3,
+  ASDPOCS_JOB_CANCELLED = 4
 };
 
 /* Times of a finished job (host steady clock, milliseconds). */
@@ -430,6 +440,14 @@ int asdpocs_server_submit(asdpocs_server server, const asdpocs_geometry *geom,
                           long long *job);
 /* Current state of a job (ASDPOCS_JOB_*). */
 int asdpocs_server_poll(asdpocs_server server, long long job, int *state);
+/* Cancel a job (no counterpart in the reference, which runs one
+ * reconstruction per call).  A queued job leaves its queue; a running job
+ * leaves its slot at the end of the iteration in flight, its device memory
+ * returned in stream order, without touching the jobs that share its
+ * launches.  Returns ASDPOCS_ERR_STATE for a job that has finished or is
+ * already copying out its results.  A cancelled job must still be released
+ * with asdpocs_server_wait, which then returns ASDPOCS_ERR_STATE. */
+int asdpocs_server_cancel(asdpocs_server server, long long job);
 /* Wait for a job and take its results (image nx*ny*nz floats, stats, the
  * per-iteration RMSE if a reference was given, times); any output may be
  * NULL.  The job is released: a second wait on it is an error. */

@@ -77,3 +77,15 @@ def test_ref_signatures_in_reference_source_if_present():
 
     for name in ("Ax_cone_mf_gpu_new", "Atx_cone_mf_gpu_new"):
         assert params(src, name) == params(hdr, name), name
+
+
+def test_normal_build_has_no_bounds_checks(lib):
+    """asdpocs_checked_errors exists in every build; only the bounds-checked
+    variant (libasdpocs_gb300_checked.so) counts, the normal one refuses."""
+    import ctypes as C
+
+    from asd_pocs_mex_cuda_demo_gb300._lib import AsdpocsError, check
+
+    cnt, first = C.c_ulonglong(), (C.c_longlong * 2)()
+    with pytest.raises(AsdpocsError, match="not a bounds-checked build"):
+        check(lib.asdpocs_checked_errors(C.byref(cnt), first))

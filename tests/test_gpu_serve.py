@@ -94,3 +94,36 @@ def test_server_budget_admission(gpu):
         with pytest.raises(pkg.AsdpocsError) as e:
             srv.submit(jobs[0][2], jobs[0][1])
         assert e.value.status == 3
+
+
+def test_server_cancel_queued_and_running_jobs(gpu):
+    """A queued job and a running job are cancelled from the host: the queued
+    one never runs, the running one leaves its slot at the end of the
+    iteration in flight, and every other job's result equals its run alone,
+    bit for bit; the device memory of all jobs returns to zero."""
+    jobs = [_job2d(40 + s, 48, 72, 12, 4, 5, shift=2.0) for s in range(4)]
+    long_job = _job2d(45, 48, 72, 12, 400, 20, shift=2.0)  # far from done when cancelled
+    ref = [_alone(*j) for j in jobs]
+    with pkg.Server(slots_per_lane=2) as srv:
+        x, P, para = long_job
+        run_id = srv.submit(para, P, I0=x)
+        deadline = time.time() + 30
+        while srv.poll(run_id) != 1 and time.time() < deadline:  # RUNNING
+            time.sleep(0.001)
+        assert srv.poll(run_id) == 1
+        ids = [srv.submit(para_k, P_k, I0=x_k) for x_k, P_k, para_k in jobs]
+        queued = srv.submit(para, P, I0=x)  # behind the four: still queued
+        assert srv.poll(queued) == 0
+        srv.cancel(queued)
+        assert srv.poll(queued) == 4  # CANCELLED
+        srv.cancel(run_id)
+        for k, j in enumerate(ids):
+            img, out, _ = srv.wait(j)
+            assert np.array_equal(img, ref[k][0]), k
+            np.testing.assert_array_equal(out["RMSE"], ref[k][1]["RMSE"])
+        for j in (queued, run_id):
+            with pytest.raises(pkg.AsdpocsError, match="cancelled"):
+                srv.wait(j)
+        with pytest.raises(pkg.AsdpocsError):
+            srv.cancel(ids[0])  # released
+        assert srv.memory()[0] == 0
