@@ -4,6 +4,9 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
+
+#include <utility>
 
 #include "../../include/asdpocs_gb300.h"
 
@@ -48,6 +51,62 @@ __device__ __forceinline__ bool asd_in(long long i, long long n) {
 #else
 #define ASD_IN(i, n) true
 #endif
+
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch.  The kernels of an ASD-POCS iteration of a
+// plan that runs on one stream are launched with programmatic stream
+// serialization (launch_iter inside a PdlScope), so a kernel's launch and
+// block scheduling overlap the tail of the kernel before it.  Each such
+// kernel calls pdl_enter() before its first global-memory access: it waits
+// there until the preceding kernel has completed and its writes are visible
+// (so every kernel still sees all earlier ones), then lets its own successor
+// be scheduled -- once all of its blocks are resident, so the successor's
+// waiting blocks never take the slots of its own.  In a kernel launched the
+// ordinary way both instructions do nothing.  Plans that run sub-batches on
+// concurrent streams (and the serving lanes) launch the ordinary way: there
+// the successor's early, waiting blocks hold SM slots the other stream's
+// kernels would use (measured 22 % slower at batch 64, against 4 % faster
+// for a single instance).  ASDPOCS_NO_PDL in the environment turns it off.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+inline bool pdl_on() {
+  static const bool on = getenv("ASDPOCS_NO_PDL") == nullptr;
+  return on;
+}
+
+// Launches of this host thread use programmatic serialization while a
+// PdlScope(true) is alive.
+inline bool &pdl_now() {
+  static thread_local bool now = false;
+  return now;
+}
+struct PdlScope {
+  bool prev;
+  explicit PdlScope(bool on) : prev(pdl_now()) { pdl_now() = on && pdl_on(); }
+  ~PdlScope() { pdl_now() = prev; }
+};
+
+// Launches kernel k (its kernel calls pdl_enter first) on st, with
+// programmatic stream serialization inside a PdlScope(true).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_iter(void (*k)(KArgs...), dim3 grid, dim3 block, cudaStream_t st,
+                        Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl_now() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // ---------------------------------------------------------------------------
 // Error reporting (thread-local last error, as returned by asdpocs_last_error)

@@ -854,7 +854,8 @@ namespace asd {
 
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk, bool finish, bool zcol, bool exact) {
+                              int tv_walk, bool finish, bool zcol, bool exact, bool pdl) {
+  const PdlScope scope(pdl);
   cudaError_t e = cudaSuccess;
   if (shared) e = launch_group_pack(d_inst, batch, d, 0, st);
   for (int v = 0; v < nv && e == cudaSuccess; v++) {
@@ -875,7 +876,8 @@ cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
 // One iteration of sub-batch s on its stream.
 static int plan_enqueue_sub(asdpocs_plan p, const SubBatch &s) {
   ASD_CUDA(enqueue_iteration(p->d_inst + s.first, s.count, s.d, s.nv, s.max_ng, p->shared,
-                             s.st, p->tv_walk, s.min_ng < 2, p->zcol, p->exact));
+                             s.st, p->tv_walk, s.min_ng < 2, p->zcol, p->exact,
+                             p->subs.size() == 1));
   return 0;
 }
 
@@ -1358,6 +1360,7 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   cudaEvent_t e0, e1;
   ASD_CUDA(cudaEventCreate(&e0));
   ASD_CUDA(cudaEventCreate(&e1));
+  const PdlScope scope(p->subs.size() == 1);  // launched as in the plan's iteration
   const int ng = p->max_ng > 0 ? p->max_ng : 1;
   // projector steps: views spread evenly over the scan (a view's cost
   // depends on its angle)

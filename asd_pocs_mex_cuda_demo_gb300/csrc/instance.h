@@ -78,11 +78,12 @@ cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st);
 // end-of-iteration kernel is needed (otherwise the last TV step ends every
 // instance's iteration and the launch is skipped).
 // `zcol`: cone-beam backward steps walk voxel columns (launch_sart_atx);
-// `exact`: forward steps use the exact projection (launch_sart_ax).
+// `exact`: forward steps use the exact projection (launch_sart_ax);
+// `pdl`: programmatic dependent launches (for work alone on its stream).
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
                               int tv_walk = 0, bool finish = true, bool zcol = true,
-                              bool exact = false);
+                              bool exact = false, bool pdl = false);
 
 // Backward-step chord tables (Inst::chtab) of instances sharing 2-D geometry
 // and view angles, from d_inst[0], whose view tables are built: a counting

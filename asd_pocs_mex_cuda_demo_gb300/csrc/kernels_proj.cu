@@ -368,6 +368,7 @@ template <bool k3D, bool kExact>
 __global__ void __launch_bounds__(kAxBlock)
     k_sart_ax(const Inst *__restrict__ insts, int view) {
   __shared__ float sp[kAxCols][kAxWarps][2][32];
+  pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (view >= I.nv) return;
   const bool done = ((volatile int *)&I.s->done)[0] != 0;
@@ -622,6 +623,7 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
 template <bool kPlanar>
 __global__ void __launch_bounds__(kAtxThreads, 4)
     k_sart_atx(const Inst *__restrict__ insts, int view) {
+  pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
   const Dims D = I.d;
@@ -783,6 +785,7 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
 __global__ void __launch_bounds__(kAtxThreads, 4)
     k_sart_atx_zcol(const Inst *__restrict__ insts, int view) {
   __shared__ ZColShared sh;
+  pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
   const Dims D = I.d;
@@ -1190,6 +1193,7 @@ __global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 5)
   __shared__ float s_beta[kShareGroup];
   __shared__ unsigned s_active;
   __shared__ int s_finite;
+  pdl_enter();
   const int g0 = blockIdx.z * kShareGroup;
   const int gn = min(kShareGroup, batch - g0);
   if (threadIdx.x == 0) {
@@ -1259,6 +1263,7 @@ template <bool k3D>
 __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
     k_sart_ax_shared(const Inst *__restrict__ insts, int batch, int view) {
   constexpr int kQuads = kShareGroup / 4;
+  pdl_enter();
   // this block: kAxShareQ of the group's quads (4 instances each), from q0
   constexpr int kQ = kAxShareQ<k3D>, kS = 4 * kQ;
   __shared__ unsigned s_active;
@@ -1433,6 +1438,7 @@ __global__ void __launch_bounds__(256)
     k_group_pack(const Inst *__restrict__ insts, int batch, int unpack) {
   __shared__ float *s_m[kShareGroup];
   __shared__ unsigned s_active;
+  pdl_enter();
   const int g0 = blockIdx.z * kShareGroup;
   const int gn = min(kShareGroup, batch - g0);
   if (threadIdx.x == 0) s_active = 0u;
@@ -1522,22 +1528,23 @@ cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &
 
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
                            int view, cudaStream_t st, bool exact) {
+  cudaError_t e;
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
   const dim3 grid(blocks, 1, batch);
   const bool p3 = d.nz > 1 || d.nb > 1;
   if (exact) {
     if (p3)
-      k_sart_ax<true, true><<<grid, kAxBlock, 0, st>>>(insts, view);
+      e = launch_iter(k_sart_ax<true, true>, grid, dim3(kAxBlock), st, insts, view);
     else
-      k_sart_ax<false, true><<<grid, kAxBlock, 0, st>>>(insts, view);
+      e = launch_iter(k_sart_ax<false, true>, grid, dim3(kAxBlock), st, insts, view);
   } else {
     if (p3)
-      k_sart_ax<true, false><<<grid, kAxBlock, 0, st>>>(insts, view);
+      e = launch_iter(k_sart_ax<true, false>, grid, dim3(kAxBlock), st, insts, view);
     else
-      k_sart_ax<false, false><<<grid, kAxBlock, 0, st>>>(insts, view);
+      e = launch_iter(k_sart_ax<false, false>, grid, dim3(kAxBlock), st, insts, view);
   }
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t launch_ax_siddon(const float *x, float *y, float *sr, const ViewGeo &g,
@@ -1551,47 +1558,56 @@ cudaError_t launch_ax_siddon(const float *x, float *y, float *sr, const ViewGeo 
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
                             int view, cudaStream_t st, bool zcol) {
+  cudaError_t e;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1 && zcol)
-    k_sart_atx_zcol<<<zcol_grid(d.nx, d.ny, d.nz, batch), kAtxThreads, 0, st>>>(insts, view);
+    e = launch_iter(k_sart_atx_zcol, zcol_grid(d.nx, d.ny, d.nz, batch), dim3(kAtxThreads),
+                    st, insts, view);
   else if (d.nz > 1 || d.nb > 1)
-    k_sart_atx<false><<<grid, kAtxThreads, 0, st>>>(insts, view);
+    e = launch_iter(k_sart_atx<false>, grid, dim3(kAtxThreads), st, insts, view);
   else
-    k_sart_atx<true><<<grid, kAtxThreads, 0, st>>>(insts, view);
-  return cudaGetLastError();
+    e = launch_iter(k_sart_atx<true>, grid, dim3(kAtxThreads), st, insts, view);
+  return e;
 }
 
 cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
                                    const Dims &d, int view, cudaStream_t st) {
+  cudaError_t e;
   dim3 grid = tile_grid(d.nx, d.ny, d.nz, 1);
   grid.z = (batch + kShareGroup - 1) / kShareGroup;
   if (d.nz > 1 || d.nb > 1)
-    k_sart_atx_shared<false><<<grid, kAtxThreads, 0, st>>>(insts, batch, view);
+    e = launch_iter(k_sart_atx_shared<false>, grid, dim3(kAtxThreads), st, insts, batch,
+                    view);
   else
-    k_sart_atx_shared<true><<<grid, kAtxThreads, 0, st>>>(insts, batch, view);
-  return cudaGetLastError();
+    e = launch_iter(k_sart_atx_shared<true>, grid, dim3(kAtxThreads), st, insts, batch,
+                    view);
+  return e;
 }
 
 cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
                                   int view, cudaStream_t st) {
+  cudaError_t e;
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
   const unsigned groups = (unsigned)((batch + kShareGroup - 1) / kShareGroup);
   if (d.nz > 1 || d.nb > 1)
-    k_sart_ax_shared<true><<<dim3(blocks, 1, groups * (kShareGroup / 4 / kAxShareQ<true>)),
-                             kAxBlock, 0, st>>>(insts, batch, view);
+    e = launch_iter(k_sart_ax_shared<true>,
+                    dim3(blocks, 1, groups * (kShareGroup / 4 / kAxShareQ<true>)),
+                    dim3(kAxBlock), st, insts, batch, view);
   else
-    k_sart_ax_shared<false><<<dim3(blocks, 1, groups * (kShareGroup / 4 / kAxShareQ<false>)),
-                              kAxBlock, 0, st>>>(insts, batch, view);
-  return cudaGetLastError();
+    e = launch_iter(k_sart_ax_shared<false>,
+                    dim3(blocks, 1, groups * (kShareGroup / 4 / kAxShareQ<false>)),
+                    dim3(kAxBlock), st, insts, batch, view);
+  return e;
 }
 
 cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,
                               int unpack, cudaStream_t st) {
+  cudaError_t e;
   const long long n = (long long)d.nx * d.ny * d.nz;
   const dim3 grid((unsigned)((n + 255) / 256), 1, (batch + kShareGroup - 1) / kShareGroup);
-  k_group_pack<<<grid, 256, 0, st>>>(insts, batch, unpack);
-  return cudaGetLastError();
+  e = launch_iter(k_group_pack, grid, dim3(256), st, insts, batch, unpack);
+  return e;
 }
 
 cudaError_t launch_atx_chords(const Inst *insts, const Dims &d, int nv, int K,

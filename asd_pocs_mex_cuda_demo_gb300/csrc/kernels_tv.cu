@@ -380,6 +380,7 @@ template <bool k3D>
 __global__ void __launch_bounds__(kThreads)
     k_after_sweep(const Inst *__restrict__ insts) {
   __shared__ Tile<1, k3D> t;
+  pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const Dims D = I.d;
@@ -652,6 +653,7 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
 __global__ void __launch_bounds__(kWalkWarps * 32, 8)
     k_tv_walk2d(const Inst *__restrict__ insts, int step, int bands) {
   __shared__ float2 ring[kWalkWarps][kWalkRing * 32], ring0[kWalkWarps][kWalkRing * 32];
+  pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
@@ -801,6 +803,7 @@ __device__ __forceinline__ void sweep_walk(const Inst &I, int y0, int y1, int xa
 __global__ void __launch_bounds__(kWalkWarps * 32)
     k_after_sweep_walk2d(const Inst *__restrict__ insts, int bands) {
   __shared__ float2 ring[kWalkWarps][4][kWalkRing * 32];
+  pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const Dims D = I.d;
@@ -1035,6 +1038,7 @@ __global__ void __launch_bounds__(kZThreads)
   __shared__ float sm[4][kZH][kZW], sr[2][kZH][kZW], sp[3][kZH][kZW], sq[2][kZH][kZW];
   __shared__ float shf[kZThreads / 32];
   __shared__ int s_last;
+  pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
@@ -1083,6 +1087,7 @@ __global__ void __launch_bounds__(kZThreads)
 // (ng == 0 or ng == 1): positivity (after a TV step), dg, alpha/beta, k.
 __global__ void __launch_bounds__(kThreads)
     k_finish_iter(const Inst *__restrict__ insts) {
+  pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
@@ -1150,7 +1155,7 @@ cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
                                cudaStream_t st) {
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1) {
-    k_after_sweep<true><<<grid, kThreads, 0, st>>>(insts);
+    return launch_iter(k_after_sweep<true>, grid, dim3(kThreads), st, insts);
   } else {
     // one band per walk up to a wave of walks (24 resident warps per SM at
     // 80 registers), then longer walks
@@ -1159,10 +1164,10 @@ cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
     const long long per = (units * batch + cap - 1) / cap;
     const int bands = (int)(per < 1 ? 1 : (per > walk_bands(d.ny) ? walk_bands(d.ny) : per));
     const long long walks = (long long)walk_strips(d.nx) * ((walk_bands(d.ny) + bands - 1) / bands);
-    k_after_sweep_walk2d<<<dim3((unsigned)((walks + kWalkWarps - 1) / kWalkWarps), 1, batch),
-                           kWalkWarps * 32, 0, st>>>(insts, bands);
+    return launch_iter(k_after_sweep_walk2d,
+                       dim3((unsigned)((walks + kWalkWarps - 1) / kWalkWarps), 1, batch),
+                       dim3(kWalkWarps * 32), st, insts, bands);
   }
-  return cudaGetLastError();
 }
 
 int tv_walk_max(const Dims &d) {
@@ -1182,7 +1187,8 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
     const long long per = walk > 0 ? walk : (units * batch + cap - 1) / cap;
     const int slabs = (int)(per < 1 ? 1 : (per > zwalk_slabs(d.nz) ? zwalk_slabs(d.nz) : per));
     const long long walks = tiles * ((zwalk_slabs(d.nz) + slabs - 1) / slabs);
-    k_tv_walk3d<<<dim3((unsigned)walks, 1, batch), kZThreads, 0, st>>>(insts, step, slabs);
+    return launch_iter(k_tv_walk3d, dim3((unsigned)walks, 1, batch), dim3(kZThreads), st,
+                       insts, step, slabs);
   } else {
     // bands per walk: the batch's walks within about one wave of 32
     // resident warps per SM; one band (16 rows) per walk for small batches,
@@ -1193,9 +1199,8 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
     const int bands = (int)(per < 1 ? 1 : (per > walk_bands(d.ny) ? walk_bands(d.ny) : per));
     const long long walks = (long long)walk_strips(d.nx) * ((walk_bands(d.ny) + bands - 1) / bands);
     const dim3 g2((unsigned)((walks + kWalkWarps - 1) / kWalkWarps), 1, batch);
-    k_tv_walk2d<<<g2, kWalkWarps * 32, 0, st>>>(insts, step, bands);
+    return launch_iter(k_tv_walk2d, g2, dim3(kWalkWarps * 32), st, insts, step, bands);
   }
-  return cudaGetLastError();
 }
 
 int tv_partials_for(const Dims &d) {
@@ -1206,8 +1211,8 @@ int tv_partials_for(const Dims &d) {
 cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
                                int ng, cudaStream_t st) {
   (void)ng;
-  k_finish_iter<<<tile_grid(d.nx, d.ny, d.nz, batch), kThreads, 0, st>>>(insts);
-  return cudaGetLastError();
+  return launch_iter(k_finish_iter, tile_grid(d.nx, d.ny, d.nz, batch), dim3(kThreads), st,
+                     insts);
 }
 
 #ifdef ASDPOCS_CHECKED
