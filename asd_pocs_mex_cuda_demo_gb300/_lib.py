@@ -55,6 +55,13 @@ class Geometry(C.Structure):
                 ("vxlsize", C.c_double), ("detsize", C.c_double)]
 
 
+class Shapes(C.Structure):
+    """asdpocs_shapes: a plan's launch shapes (none changes a result bit)."""
+
+    _fields_ = [("tv_walk", C.c_int), ("ax_cols", C.c_int), ("ax_quads", C.c_int),
+                ("zcol_segment", C.c_int), ("pdl", C.c_int), ("iteration_ms", C.c_double)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("slots_per_lane", C.c_int), ("hbm_budget_bytes", C.c_ulonglong),
                 ("inflight", C.c_int)]
@@ -132,6 +139,9 @@ SIGNATURES = [
     ("asdpocs_plan_set_tv_walk", C.c_int, [C.c_void_p, C.c_int]),
     ("asdpocs_plan_streams", C.c_int, [C.c_void_p]),
     ("asdpocs_plan_chord_slots", C.c_int, [C.c_void_p]),
+    ("asdpocs_plan_autotune_shapes", C.c_int, [C.c_void_p, C.c_int, C.POINTER(Shapes)]),
+    ("asdpocs_plan_get_shapes", C.c_int, [C.c_void_p, C.POINTER(Shapes)]),
+    ("asdpocs_plan_set_shapes", C.c_int, [C.c_void_p, C.POINTER(Shapes)]),
     ("asdpocs_phantom_device", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _D, C.c_int,
                                          C.c_double, C.c_void_p]),
     ("asdpocs_poisson_noise_device", C.c_int, [C.c_void_p, C.c_void_p, C.c_longlong,

@@ -13,7 +13,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import AX_MODE, SINO_STORAGE, AsdpocsError, Geometry, Options, Stats, check, load
+from ._lib import (AX_MODE, SINO_STORAGE, AsdpocsError, Geometry, Options, Shapes, Stats,
+                   check, load)
 
 _D = C.POINTER(C.c_double)
 _EPS = float(np.finfo(np.float64).eps)
@@ -262,6 +263,32 @@ class Plan:
         w, ms = C.c_int(), C.c_double()
         check(load().asdpocs_plan_autotune(self._h, int(reps), C.byref(w), C.byref(ms)))
         return w.value, ms.value
+
+    def autotune_shapes(self, reps: int = 10) -> dict:
+        """Times every launch shape that applies to the plan (TV walk, the
+        shared forward step's loads per round and quads per block, the
+        cone-beam backward step's column segment, programmatic launches) on
+        its own data and keeps the fastest; no shape changes a result bit.
+        Resets the plan.  Returns the chosen shapes and the iteration's
+        device milliseconds."""
+        sh = Shapes()
+        check(load().asdpocs_plan_autotune_shapes(self._h, int(reps), C.byref(sh)))
+        return {f: getattr(sh, f) for f, _ in Shapes._fields_}
+
+    @property
+    def shapes(self) -> dict:
+        sh = Shapes()
+        check(load().asdpocs_plan_get_shapes(self._h, C.byref(sh)))
+        return {f: getattr(sh, f) for f, _ in Shapes._fields_ if f != "iteration_ms"}
+
+    def set_shapes(self, **kw):
+        """Sets launch shapes by name (tv_walk, ax_cols, ax_quads,
+        zcol_segment, pdl); 0 = the default, pdl -1 = auto."""
+        sh = Shapes()
+        check(load().asdpocs_plan_get_shapes(self._h, C.byref(sh)))
+        for k, v in kw.items():
+            setattr(sh, k, int(v))
+        check(load().asdpocs_plan_set_shapes(self._h, C.byref(sh)))
 
     @property
     def streams(self) -> int:

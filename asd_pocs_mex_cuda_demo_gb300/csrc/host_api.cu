@@ -645,6 +645,10 @@ struct asdpocs_plan_s {
   bool zcol = true;     // cone beams: z-column backward step (else per voxel)
   bool exact = false;   // forward steps: exact Siddon projection (ax_mode)
   int tv_walk = 0;      // TV walk length (0: from the batch size)
+  int zseg = 0;         // z-column segment length (0: the default)
+  int ax_u = 0, ax_q = 0;  // shared forward step's shape (0: the defaults)
+  int pdl = -1;         // programmatic dependent launches: -1 = when the plan
+                        // runs on one stream, 0 = off, 1 = on
   Inst *d_inst = nullptr;
   void *arena = nullptr;
   size_t bytes = 0;
@@ -854,30 +858,42 @@ namespace asd {
 
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk, bool finish, bool zcol, bool exact, bool pdl) {
-  const PdlScope scope(pdl);
+                              const IterShape &sh, bool finish) {
+  const PdlScope scope(sh.pdl);
   cudaError_t e = cudaSuccess;
   if (shared) e = launch_group_pack(d_inst, batch, d, 0, st);
   for (int v = 0; v < nv && e == cudaSuccess; v++) {
-    e = shared ? launch_sart_ax_shared(d_inst, batch, d, v, st)
-               : launch_sart_ax(d_inst, batch, d, v, st, exact);
+    e = shared ? launch_sart_ax_shared(d_inst, batch, d, v, st, sh.ax_u, sh.ax_q)
+               : launch_sart_ax(d_inst, batch, d, v, st, sh.exact);
     if (e == cudaSuccess)
       e = shared ? launch_sart_atx_shared(d_inst, batch, d, v, st)
-                 : launch_sart_atx(d_inst, batch, d, v, st, zcol);
+                 : launch_sart_atx(d_inst, batch, d, v, st, sh.zcol, sh.zseg);
   }
   if (shared && e == cudaSuccess) e = launch_group_pack(d_inst, batch, d, 1, st);
   if (e == cudaSuccess) e = launch_after_sweep(d_inst, batch, d, st);
   for (int s = 0; s < ng && e == cudaSuccess; s++)
-    e = launch_tv_step(d_inst, batch, d, s, ng, st, tv_walk);
+    e = launch_tv_step(d_inst, batch, d, s, ng, st, sh.tv_walk);
   if (e == cudaSuccess && finish) e = launch_finish_iter(d_inst, batch, d, ng, st);
   return e;
+}
+
+// The launch shapes of the plan's iterations.
+static IterShape plan_shape(asdpocs_plan p) {
+  IterShape sh;
+  sh.tv_walk = p->tv_walk;
+  sh.zcol = p->zcol;
+  sh.zseg = p->zseg;
+  sh.ax_u = p->ax_u;
+  sh.ax_q = p->ax_q;
+  sh.pdl = p->pdl < 0 ? p->subs.size() == 1 : p->pdl == 1;
+  sh.exact = p->exact;
+  return sh;
 }
 
 // One iteration of sub-batch s on its stream.
 static int plan_enqueue_sub(asdpocs_plan p, const SubBatch &s) {
   ASD_CUDA(enqueue_iteration(p->d_inst + s.first, s.count, s.d, s.nv, s.max_ng, p->shared,
-                             s.st, p->tv_walk, s.min_ng < 2, p->zcol, p->exact,
-                             p->subs.size() == 1));
+                             s.st, plan_shape(p), s.min_ng < 2));
   return 0;
 }
 
@@ -1360,18 +1376,20 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   cudaEvent_t e0, e1;
   ASD_CUDA(cudaEventCreate(&e0));
   ASD_CUDA(cudaEventCreate(&e1));
-  const PdlScope scope(p->subs.size() == 1);  // launched as in the plan's iteration
+  const IterShape sh = plan_shape(p);
+  const PdlScope scope(sh.pdl);  // launched as in the plan's iteration
   const int ng = p->max_ng > 0 ? p->max_ng : 1;
   // projector steps: views spread evenly over the scan (a view's cost
   // depends on its angle)
   auto view_of_rep = [&](int i) { return (int)(((long long)i * p->nv / reps) % p->nv); };
   auto ax = [&](int v) {
-    return p->shared ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, v, p->st)
-                     : launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st, p->exact);
+    return p->shared ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, v, p->st, sh.ax_u,
+                                             sh.ax_q)
+                     : launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st, sh.exact);
   };
   auto atx = [&](int v) {
     return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, v, p->st)
-                     : launch_sart_atx(p->d_inst, p->batch, p->d, v, p->st, p->zcol);
+                     : launch_sart_atx(p->d_inst, p->batch, p->d, v, p->st, sh.zcol, sh.zseg);
   };
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {
@@ -1478,6 +1496,124 @@ int asdpocs_plan_autotune(asdpocs_plan p, int reps, int *walk, double *ms) {
   if (int rc = asdpocs_plan_set_tv_walk(p, best)) return rc;
   if (walk) *walk = best;
   if (ms) *ms = (double)best_ms / reps;
+  return 0;
+}
+
+int asdpocs_plan_get_shapes(asdpocs_plan p, asdpocs_shapes *out) {
+  clear_error();
+  if (!p || !out) return set_error(ASDPOCS_ERR_ARG, "null argument");
+  out->tv_walk = p->tv_walk;
+  out->ax_cols = p->ax_u;
+  out->ax_quads = p->ax_q;
+  out->zcol_segment = p->zseg;
+  out->pdl = p->pdl;
+  out->iteration_ms = 0.0;
+  return 0;
+}
+
+int asdpocs_plan_set_shapes(asdpocs_plan p, const asdpocs_shapes *s) {
+  clear_error();
+  if (!p || !s) return set_error(ASDPOCS_ERR_ARG, "null argument");
+  if (s->tv_walk < 0 || s->ax_cols < 0 || s->ax_cols > 2 || s->ax_quads < 0 ||
+      s->ax_quads > 2 || s->zcol_segment < 0 || s->zcol_segment > 256 || s->pdl < -1 ||
+      s->pdl > 1)
+    return set_error(ASDPOCS_ERR_ARG, "launch shape out of range");
+  plan_drop_graph(p);  // the captured launches change
+  p->tv_walk = s->tv_walk;
+  p->ax_u = s->ax_cols;
+  p->ax_q = s->ax_quads;
+  p->zseg = s->zcol_segment;
+  p->pdl = s->pdl;
+  return 0;
+}
+
+int asdpocs_plan_autotune_shapes(asdpocs_plan p, int reps, asdpocs_shapes *out) {
+  clear_error();
+  if (!p || reps <= 0) return set_error(ASDPOCS_ERR_ARG, "bad autotune arguments");
+  // the TV walk: its own tuner (steps of the plan's data, state unchanged)
+  if (int rc = asdpocs_plan_autotune(p, reps, nullptr, nullptr)) return rc;
+  double ms = 0.0;
+  auto pick = [&](int phase, int *knob, const std::vector<int> &cand) -> int {
+    int best = *knob;
+    double best_ms = 1e300;
+    for (int c : cand) {
+      *knob = c;
+      if (int rc = asdpocs_plan_time_phase(p, phase, reps, &ms)) return rc;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
+    }
+    *knob = best;
+    return 0;
+  };
+  if (p->shared) {  // the shared forward step's shape, timed on its kernel
+    int uq = p->ax_u * 4 + p->ax_q;
+    if (int rc = pick(0, &uq, {1 * 4 + 1, 2 * 4 + 1, 1 * 4 + 2, 2 * 4 + 2})) return rc;
+    p->ax_u = uq / 4;
+    p->ax_q = uq % 4;
+  } else if (p->d.nz > 1 && p->zcol) {  // the z-column segment length
+    if (int rc = pick(1, &p->zseg, {8, 16, 32, 64})) return rc;
+  }
+  // programmatic launches, on whole iterations (ordinary launches, no graph)
+  cudaEvent_t e0, e1;
+  ASD_CUDA(cudaEventCreate(&e0));
+  ASD_CUDA(cudaEventCreate(&e1));
+  // one iteration of every sub-batch, ordered after and before the plan's
+  // stream (as asdpocs_plan_run does)
+  auto one_iter = [&]() -> int {
+    const bool multi = p->subs.size() > 1;
+    if (multi) {
+      ASD_CUDA(cudaEventRecord(p->fork, p->st));
+      for (SubBatch &s : p->subs) ASD_CUDA(cudaStreamWaitEvent(s.st, p->fork, 0));
+    }
+    for (const SubBatch &s : p->subs)
+      if (int rc = plan_enqueue_sub(p, s)) return rc;
+    if (multi)
+      for (SubBatch &s : p->subs) {
+        ASD_CUDA(cudaEventRecord(s.done, s.st));
+        ASD_CUDA(cudaStreamWaitEvent(p->st, s.done, 0));
+      }
+    return 0;
+  };
+  auto iter_ms = [&](double *t) -> int {
+    if (int r = asdpocs_plan_reset(p)) return r;
+    if (int r = one_iter()) return r;  // warm-up
+    ASD_CUDA(cudaEventRecord(e0, p->st));
+    for (int r = 0; r < reps; r++)
+      if (int rc = one_iter()) return rc;
+    ASD_CUDA(cudaEventRecord(e1, p->st));
+    ASD_CUDA(cudaEventSynchronize(e1));
+    float f = 0.f;
+    ASD_CUDA(cudaEventElapsedTime(&f, e0, e1));
+    *t = (double)f / reps;
+    return 0;
+  };
+  int rc = 0;
+  double t_best = 0.0;
+  if (p->subs.size() == 1) {  // one stream: with and without
+    double t_on = 0.0, t_off = 0.0;
+    p->pdl = 1;
+    rc = iter_ms(&t_on);
+    if (!rc) {
+      p->pdl = 0;
+      rc = iter_ms(&t_off);
+    }
+    p->pdl = t_on <= t_off ? 1 : 0;
+    t_best = std::min(t_on, t_off);
+  } else {  // concurrent sub-batches: ordinary launches (see PdlScope)
+    p->pdl = 0;
+    rc = iter_ms(&t_best);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  plan_drop_graph(p);
+  if (int r2 = asdpocs_plan_reset(p)) return r2;
+  if (out) {
+    asdpocs_plan_get_shapes(p, out);
+    out->iteration_ms = t_best;
+  }
   return 0;
 }
 

@@ -77,13 +77,23 @@ cudaError_t reset_instance(const Inst &I, const Scalars &s, cudaStream_t st);
 // `finish`: some instance may run fewer than two TV steps, so the
 // end-of-iteration kernel is needed (otherwise the last TV step ends every
 // instance's iteration and the launch is skipped).
-// `zcol`: cone-beam backward steps walk voxel columns (launch_sart_atx);
-// `exact`: forward steps use the exact projection (launch_sart_ax);
-// `pdl`: programmatic dependent launches (for work alone on its stream).
+// How the kernels of an iteration are launched.  Every field but `exact`
+// is a launch shape that leaves every result bit unchanged (what
+// asdpocs_plan_autotune_shapes may pick); `exact` selects the exact forward
+// projection (a mode: different results).
+struct IterShape {
+  int tv_walk = 0;          // TV walk length (0: the batch-size rule)
+  bool zcol = true;         // cone beams: z-column backward step (else per voxel)
+  int zseg = 0;             //   its segment length in voxels (0: the default)
+  int ax_u = 0, ax_q = 0;   // shared forward step: columns of loads per round,
+                            //   quads of instances per block (0: the defaults)
+  bool pdl = false;         // programmatic dependent launches (work alone on
+                            //   its stream)
+  bool exact = false;       // forward steps: exact projection (launch_sart_ax)
+};
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              int tv_walk = 0, bool finish = true, bool zcol = true,
-                              bool exact = false, bool pdl = false);
+                              const IterShape &shape = IterShape(), bool finish = true);
 
 // Backward-step chord tables (Inst::chtab) of instances sharing 2-D geometry
 // and view angles, from d_inst[0], whose view tables are built: a counting

@@ -47,10 +47,11 @@ cudaError_t launch_store_sinogram(const float *src, void *dst, size_t n, int fmt
 // `exact`: the forward step uses the exact projection (launch_ax_siddon).
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
                            int view, cudaStream_t st, bool exact = false);
-// Cone beams (nz > 1) walk voxel columns (k_sart_atx_zcol) unless `zcol`
-// is false (the per-voxel form; bit-identical).
+// Cone beams (nz > 1) walk voxel columns (k_sart_atx_zcol) in segments of
+// `zseg` voxels (0: the default) unless `zcol` is false (the per-voxel form;
+// bit-identical).
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, cudaStream_t st, bool zcol = true);
+                            int view, cudaStream_t st, bool zcol = true, int zseg = 0);
 
 // ---- TV and scalars (kernels_tv.cu) ----
 // FP64 / FP32 TV minimisation on device buffers (reference semantics).
@@ -94,8 +95,11 @@ cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
 // Forward step for a batch whose instances share geometry and view angles:
 // the column march evaluated once per ray for groups of instances whose
 // images are interleaved (Inst::m_il) during the sweep.
+// `u` columns of loads per round and `q` quads of instances per block (1 or
+// 2 each; 0: the defaults, 2 x 1 for fan beams, 1 x 2 for cone beams) are
+// launch shapes that do not change results.
 cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
-                                  int view, cudaStream_t st);
+                                  int view, cudaStream_t st, int u = 0, int q = 0);
 // Copies the running instances' images into (unpack = 0) or out of
 // (unpack = 1) their group's interleaved images.
 cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,

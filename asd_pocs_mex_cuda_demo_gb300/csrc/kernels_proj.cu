@@ -669,22 +669,25 @@ struct ZColShared {
   unsigned bits[kZColA][kAtxThreads];
 };
 
-__host__ __device__ inline dim3 zcol_grid(int nx, int ny, int nz, int batch) {
+// Grid of segments of `seg` voxels (a launch shape: the sums of a voxel do not
+// depend on it).
+__host__ __device__ inline dim3 zcol_grid(int nx, int ny, int nz, int batch,
+                                          int seg = kZSeg) {
   return dim3((nx + kTileX - 1) / kTileX,
-              ((ny + kTileY - 1) / kTileY) * ((nz + kZSeg - 1) / kZSeg), batch);
+              ((ny + kTileY - 1) / kTileY) * ((nz + seg - 1) / seg), batch);
 }
 
 // This thread's column and segment [z0, z1) for an instance of sizes D;
 // false when the block lies outside the instance's own grid.
-__device__ __forceinline__ bool zcol_thread(const Dims &D, int &ix, int &iy, int &z0,
-                                            int &z1) {
-  const int ty = (D.ny + kTileY - 1) / kTileY, ns = (D.nz + kZSeg - 1) / kZSeg;
+__device__ __forceinline__ bool zcol_thread(const Dims &D, int seg, int &ix, int &iy,
+                                            int &z0, int &z1) {
+  const int ty = (D.ny + kTileY - 1) / kTileY, ns = (D.nz + seg - 1) / seg;
   if ((int)blockIdx.x * kTileX >= D.nx || (int)blockIdx.y >= ty * ns) return false;
-  const int seg = blockIdx.y / ty, yt = blockIdx.y - seg * ty;
+  const int sg = blockIdx.y / ty, yt = blockIdx.y - sg * ty;
   ix = blockIdx.x * kTileX + threadIdx.x % kTileX;
   iy = yt * kTileY + threadIdx.x / kTileX;
-  z0 = seg * kZSeg;
-  z1 = min(z0 + kZSeg, D.nz);
+  z0 = sg * seg;
+  z1 = min(z0 + seg, D.nz);
   return true;
 }
 
@@ -783,14 +786,14 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
 
 // SART backward step of cone-beam instances (see k_sart_atx) in z columns.
 __global__ void __launch_bounds__(kAtxThreads, 4)
-    k_sart_atx_zcol(const Inst *__restrict__ insts, int view) {
+    k_sart_atx_zcol(const Inst *__restrict__ insts, int view, int seg) {
   __shared__ ZColShared sh;
   pdl_enter();
   const Inst &I = insts[blockIdx.z];
   if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
   const Dims D = I.d;
   int ix, iy, z0, z1;
-  if (!zcol_thread(D, ix, iy, z0, z1)) return;
+  if (!zcol_thread(D, seg, ix, iy, z0, z1)) return;
   const ViewGeo G = view_of(I, view);
   const float4 *tabA = I.tabA + (long long)view * D.na;
   const bool narrow = !(I.vflags[view] & kViewAxisParallel) && I.s->cor_finite;
@@ -851,7 +854,7 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
                const int *__restrict__ flag, ViewGeo G, Dims D) {
   __shared__ ZColShared sh;
   int ix, iy, z0, z1;
-  if (!zcol_thread(D, ix, iy, z0, z1)) return;
+  if (!zcol_thread(D, kZSeg, ix, iy, z0, z1)) return;
   const bool narrow = flag[0] == 0;
   float acc = 0.f, accl = 0.f;
   atx_zcol_walk(
@@ -1259,13 +1262,17 @@ constexpr int kAxShareU = k3D ? 1 : 2;
 template <bool k3D>
 constexpr int kAxShareQ = k3D ? kShareGroup / 4 : 1;
 
-template <bool k3D>
+// kU columns per round and kQ quads per block are launch shapes that a plan's
+// autotuner may change (asdpocs_plan_autotune_shapes): neither changes the
+// order in which an instance's pieces are added, so every shape gives the
+// same bits.
+template <bool k3D, int kU, int kQ>
 __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
     k_sart_ax_shared(const Inst *__restrict__ insts, int batch, int view) {
   constexpr int kQuads = kShareGroup / 4;
   pdl_enter();
-  // this block: kAxShareQ of the group's quads (4 instances each), from q0
-  constexpr int kQ = kAxShareQ<k3D>, kS = 4 * kQ;
+  // this block: kQ of the group's quads (4 instances each), from q0
+  constexpr int kS = 4 * kQ;
   __shared__ unsigned s_active;
   __shared__ float sp[kAxCols][kAxWarps][kS + 1][32];
   __shared__ float s_part[2][kAxWarps][kS];
@@ -1312,11 +1319,10 @@ __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
     const float zd = G.z_det[ib];
     const RayMarch R = ray_setup(G, D, G.y_det[ia], zd);
     const bool planar = D.nz == 1 && zd == 0.0f;
-    // kAxShareU columns per round: their pieces first, then all their
+    // kU columns per round: their pieces first, then all their
     // (predicated) loads, then the accumulation in column and piece order
     auto march = [&](auto pieces) {
       constexpr int kP = decltype(pieces)::value;
-      constexpr int kU = kAxShareU<k3D>;
       for (int iu0 = lane + 32 * part; iu0 < R.nu; iu0 += 32 * kAxCols * kU) {
         unsigned id[kU][kP];
         float w[kU][kP];
@@ -1557,12 +1563,13 @@ cudaError_t launch_ax_siddon(const float *x, float *y, float *sr, const ViewGeo 
 }
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, cudaStream_t st, bool zcol) {
+                            int view, cudaStream_t st, bool zcol, int zseg) {
   cudaError_t e;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
+  zseg = zseg > 0 ? zseg : kZSeg;
   if (d.nz > 1 && zcol)
-    e = launch_iter(k_sart_atx_zcol, zcol_grid(d.nx, d.ny, d.nz, batch), dim3(kAtxThreads),
-                    st, insts, view);
+    e = launch_iter(k_sart_atx_zcol, zcol_grid(d.nx, d.ny, d.nz, batch, zseg),
+                    dim3(kAtxThreads), st, insts, view, zseg);
   else if (d.nz > 1 || d.nb > 1)
     e = launch_iter(k_sart_atx<false>, grid, dim3(kAtxThreads), st, insts, view);
   else
@@ -1584,21 +1591,35 @@ cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
   return e;
 }
 
+template <bool k3D, int kU, int kQ>
+static cudaError_t sart_ax_shared_as(const Inst *insts, int batch, unsigned blocks,
+                                     unsigned groups, int view, cudaStream_t st) {
+  return launch_iter(k_sart_ax_shared<k3D, kU, kQ>,
+                     dim3(blocks, 1, groups * (kShareGroup / 4 / kQ)), dim3(kAxBlock), st,
+                     insts, batch, view);
+}
+
+template <bool k3D>
+static cudaError_t sart_ax_shared_shape(const Inst *insts, int batch, unsigned blocks,
+                                        unsigned groups, int view, cudaStream_t st, int u,
+                                        int q) {
+  u = u ? u : kAxShareU<k3D>;
+  q = q ? q : kAxShareQ<k3D>;
+  if (u == 1 && q == 1) return sart_ax_shared_as<k3D, 1, 1>(insts, batch, blocks, groups, view, st);
+  if (u == 2 && q == 1) return sart_ax_shared_as<k3D, 2, 1>(insts, batch, blocks, groups, view, st);
+  if (u == 1 && q == 2) return sart_ax_shared_as<k3D, 1, 2>(insts, batch, blocks, groups, view, st);
+  if (u == 2 && q == 2) return sart_ax_shared_as<k3D, 2, 2>(insts, batch, blocks, groups, view, st);
+  return cudaErrorInvalidValue;
+}
+
 cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
-                                  int view, cudaStream_t st) {
-  cudaError_t e;
+                                  int view, cudaStream_t st, int u, int q) {
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
   const unsigned groups = (unsigned)((batch + kShareGroup - 1) / kShareGroup);
   if (d.nz > 1 || d.nb > 1)
-    e = launch_iter(k_sart_ax_shared<true>,
-                    dim3(blocks, 1, groups * (kShareGroup / 4 / kAxShareQ<true>)),
-                    dim3(kAxBlock), st, insts, batch, view);
-  else
-    e = launch_iter(k_sart_ax_shared<false>,
-                    dim3(blocks, 1, groups * (kShareGroup / 4 / kAxShareQ<false>)),
-                    dim3(kAxBlock), st, insts, batch, view);
-  return e;
+    return sart_ax_shared_shape<true>(insts, batch, blocks, groups, view, st, u, q);
+  return sart_ax_shared_shape<false>(insts, batch, blocks, groups, view, st, u, q);
 }
 
 cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,

@@ -431,10 +431,11 @@ def main():
         plan.set_sinogram(b, Ps[b])
         plan.set_reference(b, I0s[b])
     flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)  # > L2 (129 MB)
-    # the TV step's walk length, timed on this batch (results do not depend
-    # on it); untimed, like the graph capture
+    # the launch shapes (TV walk, forward-step shape, z-column segment,
+    # programmatic launches), timed on this batch (results do not depend on
+    # them); untimed, like the graph capture
     plan.reset()
-    tv_walk, tv_walk_ms = plan.autotune(reps=20)
+    shapes = plan.autotune_shapes(reps=20 if N * B <= (1 << 26) else 3)
 
     def step():
         plan.reset()
@@ -623,9 +624,9 @@ def main():
                                  "note": "created once per scan protocol, outside the timed "
                                          "region (view tables and, for 2-D plans, the "
                                          "backward step's chord tables)"},
-                        "tv_walk": {"autotuned": tv_walk, "ms_per_step": tv_walk_ms,
-                                    "note": "bands (2-D) or slabs (3-D) of 16 per walk; "
-                                            "0 = the batch-size rule"}},
+                        "shapes": dict(shapes, note="launch shapes picked by "
+                                       "asdpocs_plan_autotune_shapes on this batch; tv_walk "
+                                       "in bands (2-D) or slabs (3-D) of 16, 0 = defaults")},
             "latency_ms": {"p50": statistics.median(times), "p99": max(times),
                            "note": "every reconstruction of a batch completes at the end "
                                    "of its step"},

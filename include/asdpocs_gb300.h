@@ -305,6 +305,29 @@ float *asdpocs_plan_image_ptr(asdpocs_plan plan, int inst);
  * choice (0: the batch-size rule), *ms (may be NULL) its time per step.
  * Plans with fewer than two TV steps per iteration keep the rule. */
 int asdpocs_plan_autotune(asdpocs_plan plan, int reps, int *walk, double *ms);
+
+/* Launch shapes of a plan's kernels (no counterpart in the reference).  No
+ * shape changes any result bit; they only change how the work is laid out
+ * over the GPU.  0 selects the built-in default. */
+typedef struct {
+  int tv_walk;         /* TV step: bands (2-D) or slabs (3-D) per walk */
+  int ax_cols;         /* shared-geometry forward step: columns of loads per round, 1 or 2 */
+  int ax_quads;        /* ... and quads of 4 instances per block, 1 or 2 */
+  int zcol_segment;    /* cone-beam backward step: voxels per column segment, 8 .. 64 */
+  int pdl;             /* programmatic dependent launches: -1 auto (plans on one stream),
+                        * 0 off, 1 on */
+  double iteration_ms; /* autotune: one iteration with the chosen shapes (device time) */
+} asdpocs_shapes;
+
+/* Autotuner for every launch shape of the plan: each shape that applies to
+ * the plan's kind is timed over its candidates on the plan's own data (the
+ * TV walk and the forward and backward steps by their kernels, programmatic
+ * launches on whole iterations) and the fastest kept.  Ends with
+ * asdpocs_plan_reset (the reconstruction state goes back to its start). */
+int asdpocs_plan_autotune_shapes(asdpocs_plan plan, int reps, asdpocs_shapes *out);
+/* The plan's current shapes, or set them (0 = default; pdl -1 = auto). */
+int asdpocs_plan_get_shapes(asdpocs_plan plan, asdpocs_shapes *out);
+int asdpocs_plan_set_shapes(asdpocs_plan plan, const asdpocs_shapes *s);
 /* Pins the TV walk length (0: the batch-size rule; larger values are
  * clipped to a whole image). */
 int asdpocs_plan_set_tv_walk(asdpocs_plan plan, int walk);

@@ -587,3 +587,41 @@ def test_headline_fan_beam_geometry_vs_oracle(gpu, oracle_mod):
     assert out["IterationNum"] == oo["IterationNum"] == 4
     assert rel_l2(m.ravel(order="F"), mo) < RECON_TOL, rel_l2(m.ravel(order="F"), mo)
     np.testing.assert_allclose(out["RMSE"], oo["RMSE"], rtol=1e-4)
+
+
+def test_launch_shapes_do_not_change_results(gpu):
+    """Every launch shape the autotuner chooses from gives the same images,
+    bit for bit: the shared forward step's loads per round and quads per
+    block (fan and cone beams), the cone-beam backward step's column segment,
+    and programmatic dependent launches; so does the autotuner's pick."""
+    def recon(paras, phis, Ps, **shape):
+        with pkg.Plan(paras, phis) as pl:
+            for k, Pk in enumerate(Ps):
+                pl.set_sinogram(k, Pk)
+            if shape.pop("auto", False):
+                chosen = pl.autotune_shapes(reps=2)
+                assert chosen["iteration_ms"] > 0
+            elif shape:
+                pl.set_shapes(**shape)
+            pl.reset()
+            pl.run()
+            return [pl.image(k) for k in range(len(Ps))]
+
+    rng = np.random.default_rng(12)
+    fan = dict(SO=541.0, OD=408.0, vxlsize=1.2, nx=48, ny=40, nz=1, na=80, nb=1, detsize=1.0,
+               maxnumIter=2, numOfgradients=4, alpha=0.02)
+    cone = dict(SO=1000.0, OD=500.0, vxlsize=1.0, nx=24, ny=20, nz=30, na=48, nb=40,
+                detsize=1.5, maxnumIter=2, numOfgradients=3, alpha=0.02)
+    phi = phantoms.views(7)
+    for base, batch in ((fan, 11), (cone, 9), (cone, 1)):
+        paras = [base] * batch
+        Ps = [rng.random(base["na"] * base["nb"] * len(phi)).astype(np.float32)
+              for _ in range(batch)]
+        ref = recon(paras, [phi] * batch, Ps)
+        shapes = [dict(ax_cols=u, ax_quads=q) for u in (1, 2) for q in (1, 2)]
+        shapes += [dict(zcol_segment=z) for z in (8, 16, 64)]
+        shapes += [dict(pdl=0), dict(pdl=1), dict(auto=True)]
+        for sh in shapes:
+            out = recon(paras, [phi] * batch, Ps, **dict(sh))
+            for a, b in zip(ref, out):
+                assert np.array_equal(a, b), (batch, sh)
