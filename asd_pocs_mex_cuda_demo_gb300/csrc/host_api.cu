@@ -1532,35 +1532,12 @@ int asdpocs_plan_autotune_shapes(asdpocs_plan p, int reps, asdpocs_shapes *out) 
   if (!p || reps <= 0) return set_error(ASDPOCS_ERR_ARG, "bad autotune arguments");
   // the TV walk: its own tuner (steps of the plan's data, state unchanged)
   if (int rc = asdpocs_plan_autotune(p, reps, nullptr, nullptr)) return rc;
-  double ms = 0.0;
-  auto pick = [&](int phase, int *knob, const std::vector<int> &cand) -> int {
-    int best = *knob;
-    double best_ms = 1e300;
-    for (int c : cand) {
-      *knob = c;
-      if (int rc = asdpocs_plan_time_phase(p, phase, reps, &ms)) return rc;
-      if (ms < best_ms) {
-        best_ms = ms;
-        best = c;
-      }
-    }
-    *knob = best;
-    return 0;
-  };
-  if (p->shared) {  // the shared forward step's shape, timed on its kernel
-    int uq = p->ax_u * 4 + p->ax_q;
-    if (int rc = pick(0, &uq, {1 * 4 + 1, 2 * 4 + 1, 1 * 4 + 2, 2 * 4 + 2})) return rc;
-    p->ax_u = uq / 4;
-    p->ax_q = uq % 4;
-  } else if (p->d.nz > 1 && p->zcol) {  // the z-column segment length
-    if (int rc = pick(1, &p->zseg, {8, 16, 32, 64})) return rc;
-  }
-  // programmatic launches, on whole iterations (ordinary launches, no graph)
   cudaEvent_t e0, e1;
   ASD_CUDA(cudaEventCreate(&e0));
   ASD_CUDA(cudaEventCreate(&e1));
   // one iteration of every sub-batch, ordered after and before the plan's
-  // stream (as asdpocs_plan_run does)
+  // stream (as asdpocs_plan_run does), so concurrent sub-batches overlap as
+  // they do in a run
   auto one_iter = [&]() -> int {
     const bool multi = p->subs.size() > 1;
     if (multi) {
@@ -1576,6 +1553,7 @@ int asdpocs_plan_autotune_shapes(asdpocs_plan p, int reps, asdpocs_shapes *out) 
       }
     return 0;
   };
+  // device milliseconds of one whole iteration (ordinary launches, no graph)
   auto iter_ms = [&](double *t) -> int {
     if (int r = asdpocs_plan_reset(p)) return r;
     if (int r = one_iter()) return r;  // warm-up
@@ -1589,20 +1567,42 @@ int asdpocs_plan_autotune_shapes(asdpocs_plan p, int reps, asdpocs_shapes *out) 
     *t = (double)f / reps;
     return 0;
   };
-  int rc = 0;
-  double t_best = 0.0;
-  if (p->subs.size() == 1) {  // one stream: with and without
-    double t_on = 0.0, t_off = 0.0;
-    p->pdl = 1;
-    rc = iter_ms(&t_on);
-    if (!rc) {
-      p->pdl = 0;
-      rc = iter_ms(&t_off);
+  // the fastest candidate of one knob: by whole iterations (timer 0) or by
+  // the backward step's launches (timer 1)
+  auto pick = [&](int timer, int *knob, const std::vector<int> &cand) -> int {
+    int best = *knob;
+    double best_ms = 1e300, ms = 0.0;
+    for (int c : cand) {
+      *knob = c;
+      if (int rc = timer == 0 ? iter_ms(&ms) : asdpocs_plan_time_phase(p, 1, reps, &ms))
+        return rc;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+      }
     }
-    p->pdl = t_on <= t_off ? 1 : 0;
-    t_best = std::min(t_on, t_off);
-  } else {  // concurrent sub-batches: ordinary launches (see PdlScope)
-    p->pdl = 0;
+    *knob = best;
+    return 0;
+  };
+  int rc = 0;
+  // programmatic launches only where the plan runs on one stream (PdlScope)
+  const bool one_stream = p->subs.size() == 1;
+  p->pdl = 0;
+  if (p->shared) {
+    // the shared forward step's shape, on whole iterations: its kernels share
+    // the GPU with the other sub-batch's, which a kernel timed alone misses
+    int uq = p->ax_u * 4 + p->ax_q;
+    rc = pick(0, &uq, {2 * 4 + 1, 1 * 4 + 1, 1 * 4 + 2, 2 * 4 + 2});
+    p->ax_u = uq / 4;
+    p->ax_q = uq % 4;
+  } else if (p->d.nz > 1 && p->zcol) {
+    rc = pick(1, &p->zseg, {8, 16, 32, 64});  // the z-column segment length
+  }
+  double t_best = 0.0;
+  if (!rc && one_stream) {
+    rc = pick(0, &p->pdl, {0, 1});
+    if (!rc) rc = iter_ms(&t_best);
+  } else if (!rc) {
     rc = iter_ms(&t_best);
   }
   cudaEventDestroy(e0);

@@ -321,9 +321,11 @@ typedef struct {
 
 /* Autotuner for every launch shape of the plan: each shape that applies to
  * the plan's kind is timed over its candidates on the plan's own data (the
- * TV walk and the forward and backward steps by their kernels, programmatic
- * launches on whole iterations) and the fastest kept.  Ends with
- * asdpocs_plan_reset (the reconstruction state goes back to its start). */
+ * TV walk by its steps, the cone-beam column segment by the backward step,
+ * the shared forward step's shape and programmatic launches by whole
+ * iterations, where concurrent sub-batches overlap as in a run) and the
+ * fastest kept.  Ends with asdpocs_plan_reset (the reconstruction state goes
+ * back to its start). */
 int asdpocs_plan_autotune_shapes(asdpocs_plan plan, int reps, asdpocs_shapes *out);
 /* The plan's current shapes, or set them (0 = default; pdl -1 = auto). */
 int asdpocs_plan_get_shapes(asdpocs_plan plan, asdpocs_shapes *out);
