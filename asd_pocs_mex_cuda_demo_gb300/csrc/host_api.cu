@@ -1268,10 +1268,13 @@ int asdpocs_plan_reset(asdpocs_plan p) {
   return 0;
 }
 
-int asdpocs_plan_run(asdpocs_plan p, int use_graph) {
-  clear_error();
-  if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
-  if (p->max_iter <= 0) return 0;
+}  // extern "C"
+
+namespace asd {
+// Enqueues `iters` iterations of every sub-batch (through the captured
+// graphs when use_graph, capturing them first if needed), ordered after the
+// work queued on the plan's stream and before what follows it.
+static int plan_iterations(asdpocs_plan p, int iters, bool use_graph) {
   if (use_graph) {
     for (SubBatch &s : p->subs) {
       if (s.exec) continue;
@@ -1293,7 +1296,7 @@ int asdpocs_plan_run(asdpocs_plan p, int use_graph) {
     ASD_CUDA(cudaEventRecord(p->fork, p->st));
     for (SubBatch &s : p->subs) ASD_CUDA(cudaStreamWaitEvent(s.st, p->fork, 0));
   }
-  for (int k = 0; k < p->max_iter; k++)
+  for (int k = 0; k < iters; k++)
     for (SubBatch &s : p->subs) {
       if (use_graph)
         ASD_CUDA(cudaGraphLaunch(s.exec, s.st));
@@ -1307,6 +1310,16 @@ int asdpocs_plan_run(asdpocs_plan p, int use_graph) {
     }
   }
   return 0;
+}
+}  // namespace asd
+
+extern "C" {
+
+int asdpocs_plan_run(asdpocs_plan p, int use_graph) {
+  clear_error();
+  if (!p) return set_error(ASDPOCS_ERR_ARG, "null plan");
+  if (p->max_iter <= 0) return 0;
+  return plan_iterations(p, p->max_iter, use_graph != 0);
 }
 
 int asdpocs_plan_sync(asdpocs_plan p) {
@@ -1535,31 +1548,14 @@ int asdpocs_plan_autotune_shapes(asdpocs_plan p, int reps, asdpocs_shapes *out) 
   cudaEvent_t e0, e1;
   ASD_CUDA(cudaEventCreate(&e0));
   ASD_CUDA(cudaEventCreate(&e1));
-  // one iteration of every sub-batch, ordered after and before the plan's
-  // stream (as asdpocs_plan_run does), so concurrent sub-batches overlap as
-  // they do in a run
-  auto one_iter = [&]() -> int {
-    const bool multi = p->subs.size() > 1;
-    if (multi) {
-      ASD_CUDA(cudaEventRecord(p->fork, p->st));
-      for (SubBatch &s : p->subs) ASD_CUDA(cudaStreamWaitEvent(s.st, p->fork, 0));
-    }
-    for (const SubBatch &s : p->subs)
-      if (int rc = plan_enqueue_sub(p, s)) return rc;
-    if (multi)
-      for (SubBatch &s : p->subs) {
-        ASD_CUDA(cudaEventRecord(s.done, s.st));
-        ASD_CUDA(cudaStreamWaitEvent(p->st, s.done, 0));
-      }
-    return 0;
-  };
-  // device milliseconds of one whole iteration (ordinary launches, no graph)
+  // device milliseconds of one iteration run as asdpocs_plan_run runs it:
+  // the captured graphs, concurrent sub-batches overlapping
   auto iter_ms = [&](double *t) -> int {
+    plan_drop_graph(p);  // the shapes changed
     if (int r = asdpocs_plan_reset(p)) return r;
-    if (int r = one_iter()) return r;  // warm-up
+    if (int r = plan_iterations(p, 1, true)) return r;  // capture, warm-up
     ASD_CUDA(cudaEventRecord(e0, p->st));
-    for (int r = 0; r < reps; r++)
-      if (int rc = one_iter()) return rc;
+    if (int r = plan_iterations(p, reps, true)) return r;
     ASD_CUDA(cudaEventRecord(e1, p->st));
     ASD_CUDA(cudaEventSynchronize(e1));
     float f = 0.f;
@@ -1567,44 +1563,44 @@ int asdpocs_plan_autotune_shapes(asdpocs_plan p, int reps, asdpocs_shapes *out) 
     *t = (double)f / reps;
     return 0;
   };
-  // the fastest candidate of one knob: by whole iterations (timer 0) or by
-  // the backward step's launches (timer 1)
+  // the fastest candidate of one knob, by whole iterations (timer 0) or by
+  // the backward step's launches (timer 1); cand[0] is the default, which
+  // another candidate replaces only when faster by more than 2 %
   auto pick = [&](int timer, int *knob, const std::vector<int> &cand) -> int {
-    int best = *knob;
-    double best_ms = 1e300, ms = 0.0;
-    for (int c : cand) {
-      *knob = c;
+    int best = cand[0];
+    double best_ms = 0.0, ms = 0.0;
+    for (size_t k = 0; k < cand.size(); k++) {
+      *knob = cand[k];
       if (int rc = timer == 0 ? iter_ms(&ms) : asdpocs_plan_time_phase(p, 1, reps, &ms))
         return rc;
-      if (ms < best_ms) {
+      if (k == 0 || ms < 0.98 * best_ms) {
         best_ms = ms;
-        best = c;
+        best = cand[k];
       }
     }
     *knob = best;
     return 0;
   };
   int rc = 0;
-  // programmatic launches only where the plan runs on one stream (PdlScope)
-  const bool one_stream = p->subs.size() == 1;
   p->pdl = 0;
   if (p->shared) {
     // the shared forward step's shape, on whole iterations: its kernels share
     // the GPU with the other sub-batch's, which a kernel timed alone misses
-    int uq = p->ax_u * 4 + p->ax_q;
-    rc = pick(0, &uq, {2 * 4 + 1, 1 * 4 + 1, 1 * 4 + 2, 2 * 4 + 2});
+    const int dflt = p->d.nz > 1 || p->d.nb > 1 ? 1 * 4 + 2 : 2 * 4 + 1;
+    int uq = dflt;
+    std::vector<int> cand{dflt};
+    for (int c : {1 * 4 + 1, 2 * 4 + 1, 1 * 4 + 2, 2 * 4 + 2})
+      if (c != dflt) cand.push_back(c);
+    rc = pick(0, &uq, cand);
     p->ax_u = uq / 4;
     p->ax_q = uq % 4;
   } else if (p->d.nz > 1 && p->zcol) {
-    rc = pick(1, &p->zseg, {8, 16, 32, 64});  // the z-column segment length
+    rc = pick(1, &p->zseg, {32, 8, 16, 64});  // the z-column segment length
   }
   double t_best = 0.0;
-  if (!rc && one_stream) {
-    rc = pick(0, &p->pdl, {0, 1});
-    if (!rc) rc = iter_ms(&t_best);
-  } else if (!rc) {
-    rc = iter_ms(&t_best);
-  }
+  // programmatic launches only where the plan runs on one stream (PdlScope)
+  if (!rc && p->subs.size() == 1) rc = pick(0, &p->pdl, {0, 1});
+  if (!rc) rc = iter_ms(&t_best);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc) return rc;
