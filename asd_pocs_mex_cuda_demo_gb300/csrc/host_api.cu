@@ -1550,17 +1550,21 @@ int asdpocs_plan_autotune_shapes(asdpocs_plan p, int reps, asdpocs_shapes *out) 
   ASD_CUDA(cudaEventCreate(&e1));
   // device milliseconds of one iteration run as asdpocs_plan_run runs it:
   // the captured graphs, concurrent sub-batches overlapping
+  // (at most maxnumIter of them after a reset: later ones find every
+  // instance finished and would time empty launches)
+  const int n_it = std::max(1, std::min(reps, p->max_iter));
   auto iter_ms = [&](double *t) -> int {
     plan_drop_graph(p);  // the shapes changed
     if (int r = asdpocs_plan_reset(p)) return r;
     if (int r = plan_iterations(p, 1, true)) return r;  // capture, warm-up
+    if (int r = asdpocs_plan_reset(p)) return r;
     ASD_CUDA(cudaEventRecord(e0, p->st));
-    if (int r = plan_iterations(p, reps, true)) return r;
+    if (int r = plan_iterations(p, n_it, true)) return r;
     ASD_CUDA(cudaEventRecord(e1, p->st));
     ASD_CUDA(cudaEventSynchronize(e1));
     float f = 0.f;
     ASD_CUDA(cudaEventElapsedTime(&f, e0, e1));
-    *t = (double)f / reps;
+    *t = (double)f / n_it;
     return 0;
   };
   // the fastest candidate of one knob, by whole iterations (timer 0) or by
