@@ -113,23 +113,78 @@ __global__ void __launch_bounds__(kAxBlock)
   }
 }
 
-// Exact forward projection (siddon_columns): one warp per ray, lanes over
-// the columns of its dominant in-plane axis, the butterfly sum of k_ax.
+// Exact forward projection (siddon_setup, siddon_columns), a warp per 32
+// rays: lane j sets up ray j (its FP64 arithmetic once per ray, not once per
+// lane: the GPU's FP64 rate is a small fraction of its FP32 rate), then the
+// warp walks the 32 rays in turn, each ray's set-up broadcast from its lane
+// and its columns dealt to the lanes, summed by the butterfly; lane j keeps
+// ray j's totals.
+__device__ __forceinline__ SidRay sid_bcast(const SidRay &R, int src) {
+  SidRay o;
+#pragma unroll
+  for (int a = 0; a < 2; a++) {
+    o.pos0[a] = __shfl_sync(0xffffffffu, R.pos0[a], src);
+    o.r[a] = __shfl_sync(0xffffffffu, R.r[a], src);
+    o.n_ax[a] = __shfl_sync(0xffffffffu, R.n_ax[a], src);
+  }
+  o.ua = __shfl_sync(0xffffffffu, R.ua, src);
+  o.ub = __shfl_sync(0xffffffffu, R.ub, src);
+  o.Lu = __shfl_sync(0xffffffffu, R.Lu, src);
+  o.du = __shfl_sync(0xffffffffu, R.du, src);
+  o.nax = __shfl_sync(0xffffffffu, R.nax, src);
+  o.nu = __shfl_sync(0xffffffffu, R.nu, src);
+  o.su = __shfl_sync(0xffffffffu, R.su, src);
+  o.sv = __shfl_sync(0xffffffffu, R.sv, src);
+  o.sz = __shfl_sync(0xffffffffu, R.sz, src);
+  o.hit = __shfl_sync(0xffffffffu, (int)R.hit, src) != 0;
+  return o;
+}
+
+// Totals of rays r0 + lane (lane < nr - r0) for the whole warp.
+template <class Loader>
+__device__ __forceinline__ void siddon_warp_rays(const ViewGeo &G, const Dims &D,
+                                                 long long r0, long long nr, Loader ld,
+                                                 float &my_y, float &my_s) {
+  const int lane = threadIdx.x & 31;
+  SidRay mine;
+  mine.pos0[0] = mine.pos0[1] = mine.r[0] = mine.r[1] = mine.ua = mine.ub = 0.0;
+  mine.Lu = 0.f;
+  mine.du = mine.nax = mine.nu = mine.n_ax[0] = mine.n_ax[1] = 0;
+  mine.su = mine.sv = mine.sz = 0u;
+  mine.hit = false;
+  const long long r = r0 + lane;
+  if (r < nr) mine = siddon_setup(G, D, G.y_det[r % D.na], G.z_det[r / D.na]);
+  const int cnt = (int)min(32LL, nr - r0);
+  my_y = my_s = 0.f;
+  for (int j = 0; j < cnt; j++) {
+    const SidRay R = sid_bcast(mine, j);
+    float ys = 0.f, ss = 0.f;
+    siddon_columns(R, lane, 32, ld, ys, ss);
+    ys = warp_sum(ys);
+    ss = warp_sum(ss);
+    if (lane == j) {
+      my_y = ys;
+      my_s = ss;
+    }
+  }
+}
+
+constexpr int kSidRays = kAxWarps * 32;  // rays per block of the exact kernels
+
 __global__ void __launch_bounds__(kAxBlock)
     k_ax_siddon(const float *__restrict__ x, float *__restrict__ y,
                 float *__restrict__ sr, ViewGeo G, Dims D) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long r = (long long)blockIdx.x * kAxWarps + warp;
-  if (r >= (long long)D.na * D.nb) return;  // the whole warp
-  const SidRay R = siddon_setup(G, D, G.y_det[r % D.na], G.z_det[r / D.na]);
-  float ys = 0.f, ss = 0.f;
-  siddon_columns(R, lane, 32,
-                 [&](unsigned i) { return ASD_IN(i, nvox(D)) ? __ldg(x + i) : 0.f; }, ys, ss);
-  ys = warp_sum(ys);
-  ss = warp_sum(ss);
-  if (lane == 0) {
-    y[r] = ys * G.scale;
-    sr[r] = ss * G.scale;
+  const long long nr = (long long)D.na * D.nb;
+  const long long r0 = ((long long)blockIdx.x * kAxWarps + warp) * 32;
+  if (r0 >= nr) return;  // the whole warp
+  float yv, sv;
+  siddon_warp_rays(G, D, r0, nr,
+                   [&](unsigned i) { return ASD_IN(i, nvox(D)) ? __ldg(x + i) : 0.f; }, yv, sv);
+  const long long r = r0 + lane;
+  if (r < nr) {
+    y[r] = yv * G.scale;
+    sr[r] = sv * G.scale;
   }
 }
 
@@ -362,9 +417,8 @@ __global__ void __launch_bounds__(128)
 // Also records whether every residual is finite (Scalars::cor_finite), and
 // for 3D geometry writes the view's per-ray slopes ray_tab_c for the
 // backward step that follows (Inst::tabc_mode: a shared table's writer does
-// so even after its own iterations have ended).  kExact: the projection is
-// the exact one (siddon_columns) instead of the reference's column march.
-template <bool k3D, bool kExact>
+// so even after its own iterations have ended).
+template <bool k3D>
 __global__ void __launch_bounds__(kAxBlock)
     k_sart_ax(const Inst *__restrict__ insts, int view) {
   __shared__ float sp[kAxCols][kAxWarps][2][32];
@@ -390,15 +444,8 @@ __global__ void __launch_bounds__(kAxBlock)
   float v[2] = {0.f, 0.f};
   if (r < nr) {
     const float *m = I.m;
-    if constexpr (kExact) {
-      const SidRay R = siddon_setup(G, D, G.y_det[r % D.na], G.z_det[r / D.na]);
-      siddon_columns(R, lane + 32 * part, 32 * kAxCols,
-                     [&](unsigned i) { return ASD_IN(i, nvox(D)) ? m[i] : 0.f; }, v[0], v[1]);
-    } else {
-      ax_lane_partial(G, D, r, lane + 32 * part,
-                      [&](unsigned i) { return ASD_IN(i, nvox(D)) ? m[i] : 0.f; }, v[0],
-                      v[1]);
-    }
+    ax_lane_partial(G, D, r, lane + 32 * part,
+                    [&](unsigned i) { return ASD_IN(i, nvox(D)) ? m[i] : 0.f; }, v[0], v[1]);
   }
   ax_combine<2>(sp, v, part, rw, lane);
   float pt[2] = {0.f, 0.f};  // dd2, non-finite residuals
@@ -406,6 +453,54 @@ __global__ void __launch_bounds__(kAxBlock)
     const float yv = v[0] * G.scale, srv = v[1] * G.scale;
     const long long pi = (long long)view * nr + r;
     const float c0 = (ASD_IN(pi, nr * I.nv) ? sino_at(I, pi) : 0.f) - yv;
+    const float cr = c0 / (srv == 0.f ? 1.f : srv);
+    if (ASD_IN(r, nr)) I.cor[r * I.cor_stride] = cr;
+    pt[0] = c0 * c0;
+    pt[1] = isfinite(cr) ? 0.f : 1.f;
+  }
+  double tot[2];
+  if (grid_sum<kAxBlock, 2>(pt, I.partials, I.counter, ob.bid, ob.nblocks, tot)) {
+    if (threadIdx.x == 0) {
+      I.s->dd2_acc += tot[0];
+      I.s->cor_finite = tot[1] == 0.0;
+    }
+  }
+}
+
+// k_sart_ax with the exact projection (siddon_warp_rays): a warp per 32 rays,
+// lane j ray j's residual, normalisation and partial sums.
+template <bool k3D>
+__global__ void __launch_bounds__(kAxBlock)
+    k_sart_ax_exact(const Inst *__restrict__ insts, int view) {
+  pdl_enter();
+  const Inst &I = insts[blockIdx.z];
+  if (view >= I.nv) return;
+  const bool done = ((volatile int *)&I.s->done)[0] != 0;
+  const bool tabc = k3D && (I.tabc_mode == kTabcShared || (!done && I.tabc_mode == kTabcOwn));
+  if (done && !tabc) return;
+  const Dims D = I.d;
+  const long long nr = (long long)D.na * D.nb;
+  const OwnBlock ob = own_block(dim3((unsigned)((nr + kSidRays - 1) / kSidRays), 1));
+  if (ob.bid < 0) return;
+  const ViewGeo G = view_of(I, view);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long r0 = ((long long)blockIdx.x * kAxWarps + warp) * 32, r = r0 + lane;
+  if (tabc && r < nr && ASD_IN(r, nr)) {
+    const int ia = (int)(r % D.na), ib = (int)(r / D.na);
+    I.tabC[r] = ray_tab_c(I.tabA[(long long)view * D.na + ia], G.z_det[ib]);
+  }
+  if (done) return;  // the whole instance: no reduction
+  float yv = 0.f, sv = 0.f;
+  if (r0 < nr) {  // warp-uniform
+    const float *m = I.m;
+    siddon_warp_rays(G, D, r0, nr, [&](unsigned i) { return ASD_IN(i, nvox(D)) ? m[i] : 0.f; },
+                     yv, sv);
+  }
+  float pt[2] = {0.f, 0.f};  // dd2, non-finite residuals
+  if (r < nr) {
+    const float yy = yv * G.scale, srv = sv * G.scale;
+    const long long pi = (long long)view * nr + r;
+    const float c0 = (ASD_IN(pi, nr * I.nv) ? sino_at(I, pi) : 0.f) - yy;
     const float cr = c0 / (srv == 0.f ? 1.f : srv);
     if (ASD_IN(r, nr)) I.cor[r * I.cor_stride] = cr;
     pt[0] = c0 * c0;
@@ -1538,17 +1633,18 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
   const dim3 grid(blocks, 1, batch);
+  const dim3 grid_ex((unsigned)((nr + kSidRays - 1) / kSidRays), 1, batch);
   const bool p3 = d.nz > 1 || d.nb > 1;
   if (exact) {
     if (p3)
-      e = launch_iter(k_sart_ax<true, true>, grid, dim3(kAxBlock), st, insts, view);
+      e = launch_iter(k_sart_ax_exact<true>, grid_ex, dim3(kAxBlock), st, insts, view);
     else
-      e = launch_iter(k_sart_ax<false, true>, grid, dim3(kAxBlock), st, insts, view);
+      e = launch_iter(k_sart_ax_exact<false>, grid_ex, dim3(kAxBlock), st, insts, view);
   } else {
     if (p3)
-      e = launch_iter(k_sart_ax<true, false>, grid, dim3(kAxBlock), st, insts, view);
+      e = launch_iter(k_sart_ax<true>, grid, dim3(kAxBlock), st, insts, view);
     else
-      e = launch_iter(k_sart_ax<false, false>, grid, dim3(kAxBlock), st, insts, view);
+      e = launch_iter(k_sart_ax<false>, grid, dim3(kAxBlock), st, insts, view);
   }
   return e;
 }
@@ -1557,7 +1653,7 @@ cudaError_t launch_ax_siddon(const float *x, float *y, float *sr, const ViewGeo 
                              const Dims &d, cudaStream_t st) {
   const long long nr = (long long)d.na * d.nb;
   if (nr == 0) return cudaSuccess;
-  k_ax_siddon<<<(unsigned)((nr + kAxWarps - 1) / kAxWarps), kAxBlock, 0, st>>>(x, y, sr, g,
+  k_ax_siddon<<<(unsigned)((nr + kSidRays - 1) / kSidRays), kAxBlock, 0, st>>>(x, y, sr, g,
                                                                                 d);
   return cudaGetLastError();
 }

@@ -391,69 +391,115 @@ ASD_HD void ray_columns_planar_fast(const RayMarch &R, int first, int step,
 // ray with every voxel it crosses, not the reference's column march (whose
 // 3-D splits approximate them; its 2-D march is already exact).  The ray runs
 // from the source to the bin centre in voxel units; the volume spans
-// [-(n/2), n - n/2) along x and y and [-(nz/2), nz - nz/2) * dz along z.  The
-// parameters of the plane crossings are FP64 (as in an FP64 Siddon
-// reference), each segment's length is rounded to FP32 and the sums are
-// FP32.  The lanes of a warp share the ray's columns along its dominant
-// in-plane axis u; inside a column a merge walk over the planes of the other
-// axes yields the segments in order, each in the cell of its midpoint.
-// Fan beams (nz == nb == 1) are traced in the plane (two axes).
+// [-(n/2), n - n/2) along x and y and [-(nz/2), nz - nz/2) * dz along z.
+// The lanes of a warp share the ray's columns along its dominant in-plane
+// axis u.  Per ray (FP64, as an FP64 Siddon reference computes it): the
+// in-volume parameter range and, for the other axes, their position (in
+// cells) at the start of each column as a line in the column index.  Per
+// lane the positions at its columns' starts advance in double-single FP32
+// pairs (two-sum), so the loop has no FP64 arithmetic; inside a column
+// everything is FP32 in a local coordinate s in [0, 1] along u: the planes
+// of the other axes are crossed at (m - f) / k, the segments between
+// crossings lie in the cell of their midpoint, and a segment's length is
+// its s-extent times the ray's length per unit of u.  The two columns where
+// the ray enters and leaves the volume clip s in FP64.  Lengths and sums are
+// FP32.  Fan beams (nz == nb == 1) are traced in the plane (two axes).
 // ---------------------------------------------------------------------------
 struct SidRay {
-  double p0[3], d[3], inv[3], lo[3], h[3];
-  double amin, amax, L;  // in-volume parameter range; |d|
-  int n[3];
-  int naxes, du;         // 2 (fan beam) or 3; the dominant in-plane axis
+  // the dominant in-plane axis u and the other axes (in-plane, then z):
+  // positions in cells along the ray as lines in the u cell coordinate,
+  // pos_k(u) = pos0[k] + u * r[k]; the in-volume u range [ua, ub]
+  double pos0[2], r[2], ua, ub;
+  float Lu;   // ray length per cell of u
+  int du, nax, nu, n_ax[2];
+  unsigned su, sv, sz;  // memory strides of u, the other in-plane axis and z
   bool hit;
 };
 
 ASD_HD SidRay siddon_setup(const ViewGeo &G, const Dims &D, float ydet, float zdet) {
   SidRay s;
   const bool planar = D.nz == 1 && D.nb == 1;
-  s.naxes = planar ? 2 : 3;
-  s.p0[0] = (double)G.cos_phi * -(double)G.SO;
-  s.p0[1] = (double)G.sin_phi * -(double)G.SO;
-  s.p0[2] = 0.0;
+  s.nax = planar ? 1 : 2;
+  const double p0[3] = {(double)G.cos_phi * -(double)G.SO, (double)G.sin_phi * -(double)G.SO,
+                        0.0};
   const double p1[3] = {(double)G.cos_phi * G.OD - (double)G.sin_phi * ydet,
                         (double)G.sin_phi * G.OD + (double)G.cos_phi * ydet,
                         planar ? 0.0 : (double)zdet};
-  s.n[0] = D.nx;
-  s.n[1] = D.ny;
-  s.n[2] = D.nz;
-  s.h[0] = 1.0;
-  s.h[1] = 1.0;
-  s.h[2] = G.dz;
-  s.lo[0] = (double)(0 - D.nx / 2);
-  s.lo[1] = (double)(0 - D.ny / 2);
-  s.lo[2] = (double)(0 - D.nz / 2) * G.dz;
-  s.amin = 0.0;
-  s.amax = 1.0;
-  s.hit = true;
-  double L2 = 0.0;
-  for (int k = 0; k < 3; k++) {
-    const double dk = k < s.naxes ? p1[k] - s.p0[k] : 0.0;
-    s.d[k] = dk;
-    s.inv[k] = dk != 0.0 ? 1.0 / dk : 0.0;
-    if (k >= s.naxes) continue;
-    L2 += dk * dk;
-    const double b0 = s.lo[k], b1 = s.lo[k] + s.n[k] * s.h[k];
-    if (dk == 0.0) {
-      if (s.p0[k] < b0 || s.p0[k] > b1) s.hit = false;
-      continue;
+  const double d0 = p1[0] - p0[0], d1 = p1[1] - p0[1], d2 = planar ? 0.0 : p1[2] - p0[2];
+  const bool yu = fabs(d0) < fabs(d1);
+  s.du = yu ? 1 : 0;
+  const double du = yu ? d1 : d0, p0u = yu ? p0[1] : p0[0];
+  const double lou = (double)(0 - (yu ? D.ny : D.nx) / 2);
+  s.nu = yu ? D.ny : D.nx;
+  s.hit = du != 0.0;
+  const double rdu = s.hit ? 1.0 / du : 0.0;
+  // t (0 at the source, 1 at the bin) as a line in u: the ray segment
+  const double ut0 = p0u - lou, ut1 = p0u + du - lou;
+  double ua = fmax(0.0, fmin(ut0, ut1)), ub = fmin((double)s.nu, fmax(ut0, ut1));
+  const double dk[2] = {yu ? d0 : d1, d2};
+  const double p0k[2] = {yu ? p0[0] : p0[1], 0.0};
+  const double lok[2] = {(double)(0 - (yu ? D.nx : D.ny) / 2), (double)(0 - D.nz / 2) * G.dz};
+  const double hk[2] = {1.0, G.dz};
+  s.n_ax[0] = yu ? D.nx : D.ny;
+  s.n_ax[1] = D.nz;
+#pragma unroll
+  for (int a = 0; a < 2; a++) {
+    s.pos0[a] = 0.0;
+    s.r[a] = 0.0;
+    if (a >= s.nax || !s.hit) continue;
+    double r = dk[a] * rdu, q = (p0k[a] + (lou - p0u) * r - lok[a]);
+    if (hk[a] != 1.0) {
+      r /= hk[a];
+      q /= hk[a];
     }
-    double t0 = (b0 - s.p0[k]) / dk, t1 = (b1 - s.p0[k]) / dk;
-    if (t0 > t1) {
-      const double t = t0;
-      t0 = t1;
-      t1 = t;
+    s.pos0[a] = q;
+    s.r[a] = r;
+    // where the line leaves [0, n] of this axis
+    if (r != 0.0) {
+      const double ir = 1.0 / r;
+      const double e0 = (0.0 - q) * ir, e1 = ((double)s.n_ax[a] - q) * ir;
+      ua = fmax(ua, fmin(e0, e1));
+      ub = fmin(ub, fmax(e0, e1));
+    } else if (q < 0.0 || q > (double)s.n_ax[a]) {
+      s.hit = false;
     }
-    if (t0 > s.amin) s.amin = t0;
-    if (t1 < s.amax) s.amax = t1;
   }
-  s.L = sqrt(L2);
-  s.du = fabs(s.d[0]) >= fabs(s.d[1]) ? 0 : 1;
-  s.hit = s.hit && s.amax > s.amin && s.d[s.du] != 0.0;
+  s.ua = ua;
+  s.ub = ub;
+  s.hit = s.hit && ub > ua;
+  // the length per cell of u, in FP32 (a relative error of ~1e-7)
+  const float fd0 = (float)d0, fd1 = (float)d1, fd2 = (float)d2;
+  s.Lu = sqrtf(fd0 * fd0 + fd1 * fd1 + fd2 * fd2) / fabsf((float)du);
+  const unsigned nx = (unsigned)D.nx;
+  s.su = yu ? nx : 1u;
+  s.sv = yu ? 1u : nx;
+  s.sz = nx * (unsigned)D.ny;
   return s;
+}
+
+// A value as an unevaluated sum hi + lo of two floats (about 48 bits).
+struct DSFloat {
+  float hi, lo;
+};
+
+ASD_HD DSFloat ds_from(double x) {
+  DSFloat r;
+  r.hi = (float)x;
+  r.lo = (float)(x - (double)r.hi);
+  return r;
+}
+
+// a + b, both double-single (Knuth's two-sum on the high parts, then one
+// renormalisation); exact to about 2^-44 relative.
+ASD_HD DSFloat ds_add(DSFloat a, DSFloat b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb);
+  const float t = (a.lo + b.lo) + e;
+  DSFloat r;
+  r.hi = s + t;
+  r.lo = t - (r.hi - s);
+  return r;
 }
 
 // Adds the exact segments of columns first, first + step, ... of ray R's
@@ -461,63 +507,92 @@ ASD_HD SidRay siddon_setup(const ViewGeo &G, const Dims &D, float ydet, float zd
 template <class Loader>
 ASD_HD void siddon_columns(const SidRay &R, int first, int step, Loader ld, float &ys,
                            float &ss) {
-  if (!R.hit) return;
-  const int du = R.du;
-  const unsigned sx = 1u, sy = (unsigned)R.n[0], sz = (unsigned)R.n[0] * (unsigned)R.n[1];
-  for (int iu = first; iu < R.n[du]; iu += step) {
-    const double ta = (R.lo[du] + iu - R.p0[du]) * R.inv[du];
-    const double tb = (R.lo[du] + (iu + 1) - R.p0[du]) * R.inv[du];
-    double t = fmax(fmin(ta, tb), R.amin);
-    const double tend = fmin(fmax(ta, tb), R.amax);
-    if (!(tend > t)) continue;
-    // the other axes: cell at the column entry, sign of travel, parameter
-    // of the next plane crossed
-    int cell[3], sgn[3];
-    double tn[3];
-    for (int k = 0; k < 3; k++) {
-      cell[k] = 0;
-      sgn[k] = 0;
-      tn[k] = 1.0e300;
-      if (k == du || k >= R.naxes) continue;
-      const double pos = (R.p0[k] + t * R.d[k] - R.lo[k]) / R.h[k];
-      int c = (int)floor(pos);
-      if (R.d[k] == 0.0) {
-        cell[k] = c;
-        continue;
-      }
-      sgn[k] = R.d[k] > 0.0 ? 1 : -1;
-      if (sgn[k] < 0 && (double)c == pos) c -= 1;  // on a plane, moving down
-      // the next plane ahead; a plane whose crossing rounds to at or before t
-      // (the entry lies on it) is already behind: the cell is past it
-      double tk = (R.lo[k] + (sgn[k] > 0 ? c + 1 : c) * R.h[k] - R.p0[k]) * R.inv[k];
-      for (int g = 0; g < 2 && tk <= t; g++) {
-        c += sgn[k];
-        tk = (R.lo[k] + (sgn[k] > 0 ? c + 1 : c) * R.h[k] - R.p0[k]) * R.inv[k];
-      }
-      cell[k] = c;
-      tn[k] = tk;
+  if (!R.hit || first >= R.nu) return;
+  const int nax = R.nax;
+  const int full0 = (int)ceil(R.ua), full1 = (int)floor(R.ub);  // [full0, full1) whole
+  DSFloat pos[2], inc[2];
+  float kf[2], ikf[2];
+#pragma unroll
+  for (int a = 0; a < 2; a++) {
+    pos[a].hi = pos[a].lo = inc[a].hi = inc[a].lo = 0.f;
+    kf[a] = ikf[a] = 0.f;
+    if (a < nax) {
+      pos[a] = ds_from(R.pos0[a] + (double)first * R.r[a]);
+      inc[a] = ds_from((double)step * R.r[a]);
+      kf[a] = (float)R.r[a];
+      ikf[a] = kf[a] != 0.f ? 1.0f / kf[a] : 0.f;
     }
-    cell[du] = iu;
-    // merge walk over the crossings inside the column
-    for (int guard = 0; guard < 4 * (R.n[0] + R.n[1] + R.n[2]) + 8; guard++) {
-      const double tm = fmin(tend, fmin(tn[0], fmin(tn[1], tn[2])));
-      const float l = (float)((tm - t) * R.L);
-      bool in = l > 0.0f;
-      for (int k = 0; k < R.naxes; k++) in = in && cell[k] >= 0 && cell[k] < R.n[k];
-      if (in) {
-        const unsigned idx = (unsigned)cell[0] * sx + (unsigned)cell[1] * sy +
-                             (R.naxes == 3 ? (unsigned)cell[2] * sz : 0u);
-        ys += l * ld(idx);
-        ss += l;
+  }
+  const float Lu = R.Lu;
+  const unsigned su = R.su, sv = R.sv, sz = R.sz;
+  const int guard_max = 2 * (R.nu + R.n_ax[0] + R.n_ax[1]) + 8;
+  for (int iu = first; iu < R.nu; iu += step) {
+    // the column's in-volume s range
+    float s0 = 0.f, s1 = 1.f;
+    if (iu < full0 || iu + 1 > full1) {  // the ray enters or leaves here
+      s0 = (float)fmax(0.0, R.ua - iu);
+      s1 = (float)fmin(1.0, R.ub - iu);
+    }
+    // cells and fractions at s = 0, the next plane crossed after s0
+    int cell[2] = {0, 0}, m[2] = {0, 0}, sg[2] = {0, 0};
+    float f[2] = {0.f, 0.f}, sn[2] = {3.0e38f, 3.0e38f};
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+      if (a >= nax) continue;
+      const float c = floorf(pos[a].hi);
+      float fr = (pos[a].hi - c) + pos[a].lo;
+      int ci = (int)c;
+      if (fr >= 1.f) {
+        fr -= 1.f;
+        ci += 1;
+      } else if (fr < 0.f) {
+        fr += 1.f;
+        ci -= 1;
       }
-      if (tm >= tend) break;
-      for (int k = 0; k < 3; k++)
-        if (tn[k] == tm) {
-          cell[k] += sgn[k];
-          const int plane = sgn[k] > 0 ? cell[k] + 1 : cell[k];
-          tn[k] = (R.lo[k] + plane * R.h[k] - R.p0[k]) * R.inv[k];
+      cell[a] = ci;
+      f[a] = fr;
+      if (kf[a] != 0.f) {
+        sg[a] = kf[a] > 0.f ? 1 : -1;
+        const float pp = fr + s0 * kf[a];
+        int mm = sg[a] > 0 ? (int)floorf(pp) + 1 : (int)ceilf(pp) - 1;
+        float t = ((float)mm - fr) * ikf[a];
+        for (int g = 0; g < 2 && t <= s0; g++) {  // rounding: plane at or behind s0
+          mm += sg[a];
+          t = ((float)mm - fr) * ikf[a];
         }
-      t = tm;
+        m[a] = mm;
+        sn[a] = t;
+      }
+      pos[a] = ds_add(pos[a], inc[a]);
+    }
+    // merge walk over the crossings inside [s0, s1]
+    float s = s0;
+    for (int guard = 0; s < s1 && guard < guard_max; guard++) {
+      const float t = fminf(s1, fminf(sn[0], sn[1]));
+      if (t > s) {
+        const float mid = 0.5f * (s + t);
+        bool in = true;
+        unsigned idx = (unsigned)iu * su;
+#pragma unroll
+        for (int a = 0; a < 2; a++) {
+          if (a >= nax) continue;
+          const int c = cell[a] + (int)floorf(f[a] + mid * kf[a]);
+          in = in && c >= 0 && c < R.n_ax[a];
+          idx += (unsigned)c * (a == 0 ? sv : sz);
+        }
+        if (in) {
+          const float l = (t - s) * Lu;
+          ys += l * ld(idx);
+          ss += l;
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < 2; a++)
+        if (a < nax && sn[a] == t) {
+          m[a] += sg[a];
+          sn[a] = ((float)m[a] - f[a]) * ikf[a];
+        }
+      s = t;
     }
   }
 }
