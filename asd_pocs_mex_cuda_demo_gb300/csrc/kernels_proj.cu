@@ -119,20 +119,29 @@ __global__ void __launch_bounds__(kAxBlock)
 // warp walks the 32 rays in turn, each ray's set-up broadcast from its lane
 // and its columns dealt to the lanes, summed by the butterfly; lane j keeps
 // ray j's totals.
+__device__ __forceinline__ DSFloat ds_shfl(DSFloat v, int src) {
+  DSFloat o;
+  o.hi = __shfl_sync(0xffffffffu, v.hi, src);
+  o.lo = __shfl_sync(0xffffffffu, v.lo, src);
+  return o;
+}
+
 __device__ __forceinline__ SidRay sid_bcast(const SidRay &R, int src) {
   SidRay o;
 #pragma unroll
   for (int a = 0; a < 2; a++) {
-    o.pos0[a] = __shfl_sync(0xffffffffu, R.pos0[a], src);
-    o.r[a] = __shfl_sync(0xffffffffu, R.r[a], src);
+    o.pos0[a] = ds_shfl(R.pos0[a], src);
+    o.r[a] = ds_shfl(R.r[a], src);
     o.n_ax[a] = __shfl_sync(0xffffffffu, R.n_ax[a], src);
   }
-  o.ua = __shfl_sync(0xffffffffu, R.ua, src);
-  o.ub = __shfl_sync(0xffffffffu, R.ub, src);
+  o.ua = ds_shfl(R.ua, src);
+  o.ub = ds_shfl(R.ub, src);
   o.Lu = __shfl_sync(0xffffffffu, R.Lu, src);
   o.du = __shfl_sync(0xffffffffu, R.du, src);
   o.nax = __shfl_sync(0xffffffffu, R.nax, src);
   o.nu = __shfl_sync(0xffffffffu, R.nu, src);
+  o.full0 = __shfl_sync(0xffffffffu, R.full0, src);
+  o.full1 = __shfl_sync(0xffffffffu, R.full1, src);
   o.su = __shfl_sync(0xffffffffu, R.su, src);
   o.sv = __shfl_sync(0xffffffffu, R.sv, src);
   o.sz = __shfl_sync(0xffffffffu, R.sz, src);
@@ -147,9 +156,10 @@ __device__ __forceinline__ void siddon_warp_rays(const ViewGeo &G, const Dims &D
                                                  float &my_y, float &my_s) {
   const int lane = threadIdx.x & 31;
   SidRay mine;
-  mine.pos0[0] = mine.pos0[1] = mine.r[0] = mine.r[1] = mine.ua = mine.ub = 0.0;
+  const DSFloat z{0.f, 0.f};
+  mine.pos0[0] = mine.pos0[1] = mine.r[0] = mine.r[1] = mine.ua = mine.ub = z;
   mine.Lu = 0.f;
-  mine.du = mine.nax = mine.nu = mine.n_ax[0] = mine.n_ax[1] = 0;
+  mine.du = mine.nax = mine.nu = mine.n_ax[0] = mine.n_ax[1] = mine.full0 = mine.full1 = 0;
   mine.su = mine.sv = mine.sz = 0u;
   mine.hit = false;
   const long long r = r0 + lane;

@@ -405,13 +405,56 @@ ASD_HD void ray_columns_planar_fast(const RayMarch &R, int first, int step,
 // the ray enters and leaves the volume clip s in FP64.  Lengths and sums are
 // FP32.  Fan beams (nz == nb == 1) are traced in the plane (two axes).
 // ---------------------------------------------------------------------------
+// A value as an unevaluated sum hi + lo of two floats (about 48 bits).
+struct DSFloat {
+  float hi, lo;
+};
+
+ASD_HD DSFloat ds_from(double x) {
+  DSFloat r;
+  r.hi = (float)x;
+  r.lo = (float)(x - (double)r.hi);
+  return r;
+}
+
+// a * k for a small integer k (|k| < 2^16): the high product's rounding error
+// recovered exactly by a fused multiply-add.
+ASD_HD DSFloat ds_mul_int(DSFloat a, int k) {
+  const float kf = (float)k;
+  const float p = a.hi * kf;
+#ifdef __CUDA_ARCH__
+  const float e = __fmaf_rn(a.hi, kf, -p);
+#else
+  const float e = fmaf(a.hi, kf, -p);
+#endif
+  DSFloat r;
+  const float t = e + a.lo * kf;
+  r.hi = p + t;
+  r.lo = t - (r.hi - p);
+  return r;
+}
+
+// a + b, both double-single (Knuth's two-sum on the high parts, then one
+// renormalisation); exact to about 2^-44 relative.
+ASD_HD DSFloat ds_add(DSFloat a, DSFloat b) {
+  const float s = a.hi + b.hi;
+  const float bb = s - a.hi;
+  const float e = (a.hi - (s - bb)) + (b.hi - bb);
+  const float t = (a.lo + b.lo) + e;
+  DSFloat r;
+  r.hi = s + t;
+  r.lo = t - (r.hi - s);
+  return r;
+}
+
 struct SidRay {
   // the dominant in-plane axis u and the other axes (in-plane, then z):
   // positions in cells along the ray as lines in the u cell coordinate,
-  // pos_k(u) = pos0[k] + u * r[k]; the in-volume u range [ua, ub]
-  double pos0[2], r[2], ua, ub;
+  // pos_k(u) = pos0[k] + u * r[k] (double-single); the in-volume u range
+  // [ua, ub] and the columns [full0, full1) wholly inside it
+  DSFloat pos0[2], r[2], ua, ub;
   float Lu;   // ray length per cell of u
-  int du, nax, nu, n_ax[2];
+  int du, nax, nu, n_ax[2], full0, full1;
   unsigned su, sv, sz;  // memory strides of u, the other in-plane axis and z
   bool hit;
 };
@@ -442,18 +485,17 @@ ASD_HD SidRay siddon_setup(const ViewGeo &G, const Dims &D, float ydet, float zd
   const double hk[2] = {1.0, G.dz};
   s.n_ax[0] = yu ? D.nx : D.ny;
   s.n_ax[1] = D.nz;
+  double pos0d[2] = {0.0, 0.0}, rd[2] = {0.0, 0.0};
 #pragma unroll
   for (int a = 0; a < 2; a++) {
-    s.pos0[a] = 0.0;
-    s.r[a] = 0.0;
     if (a >= s.nax || !s.hit) continue;
     double r = dk[a] * rdu, q = (p0k[a] + (lou - p0u) * r - lok[a]);
     if (hk[a] != 1.0) {
       r /= hk[a];
       q /= hk[a];
     }
-    s.pos0[a] = q;
-    s.r[a] = r;
+    pos0d[a] = q;
+    rd[a] = r;
     // where the line leaves [0, n] of this axis
     if (r != 0.0) {
       const double ir = 1.0 / r;
@@ -464,9 +506,16 @@ ASD_HD SidRay siddon_setup(const ViewGeo &G, const Dims &D, float ydet, float zd
       s.hit = false;
     }
   }
-  s.ua = ua;
-  s.ub = ub;
+#pragma unroll
+  for (int a = 0; a < 2; a++) {
+    s.pos0[a] = ds_from(pos0d[a]);
+    s.r[a] = ds_from(rd[a]);
+  }
   s.hit = s.hit && ub > ua;
+  s.ua = ds_from(s.hit ? ua : 0.0);
+  s.ub = ds_from(s.hit ? ub : 0.0);
+  s.full0 = s.hit ? (int)ceil(ua) : 0;
+  s.full1 = s.hit ? (int)floor(ub) : 0;
   // the length per cell of u, in FP32 (a relative error of ~1e-7)
   const float fd0 = (float)d0, fd1 = (float)d1, fd2 = (float)d2;
   s.Lu = sqrtf(fd0 * fd0 + fd1 * fd1 + fd2 * fd2) / fabsf((float)du);
@@ -477,31 +526,6 @@ ASD_HD SidRay siddon_setup(const ViewGeo &G, const Dims &D, float ydet, float zd
   return s;
 }
 
-// A value as an unevaluated sum hi + lo of two floats (about 48 bits).
-struct DSFloat {
-  float hi, lo;
-};
-
-ASD_HD DSFloat ds_from(double x) {
-  DSFloat r;
-  r.hi = (float)x;
-  r.lo = (float)(x - (double)r.hi);
-  return r;
-}
-
-// a + b, both double-single (Knuth's two-sum on the high parts, then one
-// renormalisation); exact to about 2^-44 relative.
-ASD_HD DSFloat ds_add(DSFloat a, DSFloat b) {
-  const float s = a.hi + b.hi;
-  const float bb = s - a.hi;
-  const float e = (a.hi - (s - bb)) + (b.hi - bb);
-  const float t = (a.lo + b.lo) + e;
-  DSFloat r;
-  r.hi = s + t;
-  r.lo = t - (r.hi - s);
-  return r;
-}
-
 // Adds the exact segments of columns first, first + step, ... of ray R's
 // dominant axis to (ys, ss): ys += l * x[voxel], ss += l, l in FP32.
 template <class Loader>
@@ -509,7 +533,7 @@ ASD_HD void siddon_columns(const SidRay &R, int first, int step, Loader ld, floa
                            float &ss) {
   if (!R.hit || first >= R.nu) return;
   const int nax = R.nax;
-  const int full0 = (int)ceil(R.ua), full1 = (int)floor(R.ub);  // [full0, full1) whole
+  const int full0 = R.full0, full1 = R.full1;  // columns [full0, full1) wholly inside
   DSFloat pos[2], inc[2];
   float kf[2], ikf[2];
 #pragma unroll
@@ -517,9 +541,9 @@ ASD_HD void siddon_columns(const SidRay &R, int first, int step, Loader ld, floa
     pos[a].hi = pos[a].lo = inc[a].hi = inc[a].lo = 0.f;
     kf[a] = ikf[a] = 0.f;
     if (a < nax) {
-      pos[a] = ds_from(R.pos0[a] + (double)first * R.r[a]);
-      inc[a] = ds_from((double)step * R.r[a]);
-      kf[a] = (float)R.r[a];
+      pos[a] = ds_add(R.pos0[a], ds_mul_int(R.r[a], first));
+      inc[a] = ds_mul_int(R.r[a], step);
+      kf[a] = R.r[a].hi;
       ikf[a] = kf[a] != 0.f ? 1.0f / kf[a] : 0.f;
     }
   }
@@ -530,8 +554,8 @@ ASD_HD void siddon_columns(const SidRay &R, int first, int step, Loader ld, floa
     // the column's in-volume s range
     float s0 = 0.f, s1 = 1.f;
     if (iu < full0 || iu + 1 > full1) {  // the ray enters or leaves here
-      s0 = (float)fmax(0.0, R.ua - iu);
-      s1 = (float)fmin(1.0, R.ub - iu);
+      s0 = fmaxf(0.f, (R.ua.hi - (float)iu) + R.ua.lo);
+      s1 = fminf(1.f, (R.ub.hi - (float)iu) + R.ub.lo);
     }
     // cells and fractions at s = 0, the next plane crossed after s0
     int cell[2] = {0, 0}, m[2] = {0, 0}, sg[2] = {0, 0};
