@@ -767,10 +767,11 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 // Grid: (x tiles of 32, y tiles of 8 x segments, instances).
 // ---------------------------------------------------------------------------
 constexpr int kZSeg = 32;   // voxels of a column per thread
-constexpr int kZColA = 8;   // detector columns of a shadow kept per thread
+constexpr int kZColA = 6;   // detector columns of a shadow kept per thread
 
 struct ZColShared {
   float4 pts[kZColA][kAtxThreads];   // F1, F2 in-plane points
+  float4 nh[kZColA][kAtxThreads];    // F1, F2 z-half terms (n1, h1, n2, h2)
   unsigned bits[kZColA][kAtxThreads];
 };
 
@@ -845,6 +846,7 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
         if (!ASD_IN(col.lo + k, D.na)) continue;
         const ColFaces f = col_faces(__ldg(tabA + col.lo + k), col.rx, col.ry);
         sh.pts[k][t] = make_float4(f.p1x, f.p1y, f.p2x, f.p2y);
+        sh.nh[k][t] = make_float4(f.n1, f.h1, f.n2, f.h2);
         sh.bits[k][t] = f.bits;
       }
   }
@@ -869,8 +871,8 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
       const float4 Cs = rin ? __ldg(tabC + r) : make_float4(0.f, 0.f, 0.f, 0.f);
       float l;
       if (!wide) {
-        const float4 p = sh.pts[kk][t];
-        const ColFaces f{p.x, p.y, p.z, p.w, sh.bits[kk][t]};
+        const float4 p = sh.pts[kk][t], q = sh.nh[kk][t];
+        const ColFaces f{p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w, sh.bits[kk][t]};
         if (f.bits & kCfMany)
           l = (f.bits & kCfXF) ? chord3_axis<true>(__ldg(tabA + ia), Cs, col.rx, col.ry, rz, G.dz)
                                : chord3_axis<false>(__ldg(tabA + ia), Cs, col.rx, col.ry, rz, G.dz);

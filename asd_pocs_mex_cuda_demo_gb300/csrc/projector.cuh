@@ -11,6 +11,7 @@
 // the one the reference recomputes.
 #pragma once
 #include <math.h>
+#include <string.h>
 
 #include "common.cuh"
 
@@ -1231,8 +1232,22 @@ constexpr unsigned kCfXF = 128u;              // |a| > |b| (x faces first)
 
 struct ColFaces {
   float p1x, p1y, p2x, p2y;  // in-plane coordinates of F1 and F2
+  // z halves of F1 and F2: z = s * n + rz + s * h with s = c/a (x faces) or
+  // c/b (y faces), n = -rx or -ry (NaN when the face does not exist, so its
+  // z test fails by itself) and h = -1/2 (lower face) or +1/2 (upper face)
+  float n1, h1, n2, h2;
   unsigned bits;
 };
+
+ASD_HD float __int_as_float_hd(int i) {
+#ifdef __CUDA_ARCH__
+  return __int_as_float(i);
+#else
+  float f;
+  memcpy(&f, &i, 4);
+  return f;
+#endif
+}
 
 // In-plane part of the x/y face tests of ray A (ray_tab_a) for the voxel
 // column whose centre is the source minus (rx, ry).
@@ -1270,6 +1285,11 @@ ASD_HD ColFaces col_faces(const float4 A, float rx, float ry) {
   f.bits = (n >= 1 ? kCfV1 : 0u) | (n >= 2 ? kCfV2 : 0u) | ((k1 & 2u) ? kCfY1 : 0u) |
            ((k2 & 2u) ? kCfY2 : 0u) | ((k1 & 1u) ? kCfU1 : 0u) | ((k2 & 1u) ? kCfU2 : 0u) |
            (n > 2 ? kCfMany : 0u) | (xf ? kCfXF : 0u);
+  const float nan = __int_as_float_hd(0x7fc00000);
+  f.n1 = n >= 1 ? -((k1 & 2u) ? ry : rx) : nan;
+  f.n2 = n >= 2 ? -((k2 & 2u) ? ry : rx) : nan;
+  f.h1 = (k1 & 1u) ? 0.5f : -0.5f;
+  f.h2 = (k2 & 1u) ? 0.5f : -0.5f;
   return f;
 }
 
@@ -1278,16 +1298,15 @@ ASD_HD ColFaces col_faces(const float4 A, float rx, float ry) {
 ASD_HD float chord3_col(const ColFaces &f, const float4 Cs, float rx, float ry,
                         float rz, float hz) {
   const unsigned bits = f.bits;
-  // z parts of F1 and F2: t1 -/+ u1 with t1 = s * (-r) + rz, u1 = s * (1/2),
-  // s = c/a (x faces) or c/b (y faces)
-  const float c1 = (bits & kCfY1) ? Cs.y : Cs.x, r1 = (bits & kCfY1) ? ry : rx;
-  const float t1 = c1 * (-r1) + rz, u1 = c1 * 0.5f;
-  const float z1 = (bits & kCfU1) ? t1 + u1 : t1 - u1;
-  const float c2 = (bits & kCfY2) ? Cs.y : Cs.x, r2 = (bits & kCfY2) ? ry : rx;
-  const float t2 = c2 * (-r2) + rz, u2 = c2 * 0.5f;
-  const float z2 = (bits & kCfU2) ? t2 + u2 : t2 - u2;
-  const bool h1 = (bits & kCfV1) && fabsf(z1) <= hz;
-  const bool h2 = (bits & kCfV2) && fabsf(z2) <= hz;
+  // z parts of F1 and F2: t -/+ u with t = s * (-r) + rz, u = s * (1/2),
+  // s = c/a (x faces) or c/b (y faces); s * (-1/2) is -(s * (1/2)) exactly
+  // and t + (-u) is t - u, so these are the reference's values
+  const float c1 = (bits & kCfY1) ? Cs.y : Cs.x;
+  const float z1 = (c1 * f.n1 + rz) + c1 * f.h1;
+  const float c2 = (bits & kCfY2) ? Cs.y : Cs.x;
+  const float z2 = (c2 * f.n2 + rz) + c2 * f.h2;
+  const bool h1 = fabsf(z1) <= hz;  // false for a missing face (NaN)
+  const bool h2 = fabsf(z2) <= hz;
   // z faces
   const float zt0 = Cs.z * (-rz) + rx, zu0 = Cs.z * hz;
   const float zt1 = Cs.w * (-rz) + ry, zu1 = Cs.w * hz;
