@@ -1407,8 +1407,11 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   auto launch = [&](int i) -> cudaError_t {
     switch (phase) {
       case 0: return ax(view_of_rep(i));
-      case 2: return launch_tv_step(p->d_inst, p->batch, p->d, 1 + i % (ng > 1 ? ng - 1 : 1),
-                                    ng, p->st, p->tv_walk);
+      // the TV steps that do not end the iteration (the last one would
+      // advance the iteration count and, at maxIter, stop the instances, so
+      // that later launches had nothing to do)
+      case 2: return launch_tv_step(p->d_inst, p->batch, p->d,
+                                    ng > 2 ? 1 + i % (ng - 2) : 0, ng, p->st, p->tv_walk);
       default: return launch_after_sweep(p->d_inst, p->batch, p->d, p->st);
     }
   };

@@ -9,7 +9,8 @@
 // voxel), and the ||v|| that every step needs before it can update comes out
 // of the previous kernel.  2-D: warps walk down strips of columns with the
 // stencils in registers (k_tv_walk2d).  Cone beam: blocks walk down z over
-// (x, y) tiles with the slices staged in shared memory (k_tv_walk3d).  The
+// (x, y) tiles, a thread holding the stencils of eight rows of a column in
+// registers and the slices staged in shared memory (k_tv_walk3d).  The
 // end-of-sweep kernel provides ||v|| of the first step; the last step also
 // applies the positivity constraint and the alpha/beta step control.
 #include <type_traits>
@@ -122,25 +123,29 @@ __device__ __forceinline__ T tv_grad3(const U &u) {
 
 // FP32 form of the 3-D stencil with every rounding explicit.  At a voxel
 // with differences dx, dy, dz to its -x, -y, -z neighbours,
-//   r = 1/sqrt(eps + dx^2 + dy^2 + dz^2)
-// and the reference's four terms are
-//   v = (((6c - 2(xm + ym + zm)) r + (2c - 2zp) r(+z)) + (2c - 2yp) r(+y))
-//       + (2c - 2xp) r(+x):
-// the denominators of its second to fourth terms are those of the +z, +y
-// and +x neighbours' first terms, in the same order.
+//   r = 1/sqrt(eps + dx^2 + dy^2 + dz^2),
+// and the denominators of the reference's second to fourth terms are those
+// of the +z, +y and +x neighbours' first terms (r+z, r+y, r+x).  All four
+// terms carry a factor 2, so v = 2 u with
+//   u = (3c - ((xm + ym) + zm)) r + (c - yp) r+y + (c - xp) r+x + (c - zp) r+z
+// evaluated left to right, each later term by one fused multiply-add
+// (tv3_u).  Scaling by 2 is exact, so the TV step's m - coef v is
+// m - (2 coef) u and ||v||^2 = 4 sum u^2; the z walk (k_tv_walk3d), the end
+// of the sweep and the FP32 device entry point all use this one form.
 __device__ __forceinline__ float tv3_r(float dx, float dy, float dz) {
   return tv_rsqrt(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, tv_eps<float>()))));
 }
-__device__ __forceinline__ float tv3_combine(float c, float xm, float ym, float zm, float xp,
-                                             float yp, float zp, float r, float rx, float ry,
-                                             float rz) {
-  const float c2 = __fmul_rn(2.f, c);
-  const float g1 = __fmul_rn(
-      __fsub_rn(__fmul_rn(6.f, c), __fmul_rn(2.f, __fadd_rn(__fadd_rn(xm, ym), zm))), r);
-  const float g2 = __fmul_rn(__fsub_rn(c2, __fmul_rn(2.f, zp)), rz);
-  const float g3 = __fmul_rn(__fsub_rn(c2, __fmul_rn(2.f, yp)), ry);
-  const float g4 = __fmul_rn(__fsub_rn(c2, __fmul_rn(2.f, xp)), rx);
-  return __fadd_rn(__fadd_rn(__fadd_rn(g1, g2), g3), g4);
+// u's in-slice terms: (3c - ((xm + ym) + zm)) r + (c - yp) r+y + (c - xp) r+x
+__device__ __forceinline__ float tv3_inslice(float c, float xm, float ym, float zm, float xp,
+                                             float yp, float r, float rx, float ry) {
+  const float sum = __fadd_rn(__fadd_rn(xm, ym), zm);
+  float t = __fmul_rn(__fmaf_rn(3.f, c, -sum), r);
+  t = __fmaf_rn(__fsub_rn(c, yp), ry, t);
+  return __fmaf_rn(__fsub_rn(c, xp), rx, t);
+}
+// u from the in-slice terms s and the +z neighbour
+__device__ __forceinline__ float tv3_u(float s, float c, float zp, float rz) {
+  return __fmaf_rn(__fsub_rn(c, zp), rz, s);
 }
 template <class U>
 __device__ __forceinline__ float tv_grad3f(const U &u) {
@@ -151,7 +156,7 @@ __device__ __forceinline__ float tv_grad3f(const U &u) {
   const float rx = tv3_r(__fsub_rn(xp, c), __fsub_rn(xp, u(1, -1, 0)), __fsub_rn(xp, u(1, 0, -1)));
   const float ry = tv3_r(__fsub_rn(yp, u(-1, 1, 0)), __fsub_rn(yp, c), __fsub_rn(yp, u(0, 1, -1)));
   const float rz = tv3_r(__fsub_rn(zp, u(-1, 0, 1)), __fsub_rn(zp, u(0, -1, 1)), __fsub_rn(zp, c));
-  return tv3_combine(c, xm, ym, zm, xp, yp, zp, r, rx, ry, rz);
+  return __fmul_rn(2.f, tv3_u(tv3_inslice(c, xm, ym, zm, xp, yp, r, rx, ry), c, zp, rz));
 }
 
 template <class T, class U>
@@ -845,198 +850,311 @@ __global__ void __launch_bounds__(kWalkWarps * 32)
   }
 }
 
-// Cone-beam TV step (imgTVGradMin3D.cpp:83-170) as z walks (2.5-D
-// blocking).  A block of 16 warps owns a tile of 28 x 28 output voxels in
-// (x, y) and walks down z through a range of slices.  Each slice of m is
-// staged with a two-voxel halo (32 x 32: lane l holds column x0 - 2 + l,
-// warp w rows w and w + 16; zeros outside the image) into a ring of four
-// slices by cp.async, one slice ahead.  Per slice k the block forms, on
-// shrinking halo regions:
-//   A  r(k) = 1/sqrt(eps + dx^2 + dy^2 + dz^2) of m       ([1, 32)^2)
-//   B  v(m) of slice k - 1 from m and r (tv3_combine), and
-//      m' = m - coef v(m), zero outside the image          ([1, 31)^2)
-//   C  r'(k - 1) of m'                                      ([2, 31)^2)
-//   D  v(m') of slice k - 2 on the tile: ||v(m')||^2, and m' written out
-// so each voxel is read once and written once, with four passes of stencil
-// arithmetic over slightly larger regions instead of five full stencils.
-// ||v(m')||^2 (or the last step's positivity-change norm) is summed per
-// tile and slab of 16 slices, and the block that finishes last sums the
-// slab partials in order; walks of `slabs` consecutive slabs (host-chosen)
-// give the same bits for every choice.
-constexpr int kZTX = 28, kZTY = 28;                 // output tile
-constexpr int kZW = kZTX + 4, kZH = kZTY + 4;       // staged slice with halo 2
-constexpr int kZSlab = 16;                          // slices of a partial
-constexpr int kZThreads = 512;
-static_assert(kZW == 32 && kZH == 2 * (kZThreads / 32), "lane = column, two rows per warp");
+// Cone-beam TV step (imgTVGradMin3D.cpp:83-170) as z walks with the
+// stencils in registers.  A block of kZWarps warps owns an (x, y) tile of
+// 28 x kZTY output voxels and walks down z through a range of slices: lane
+// l holds image column x0 - 4 + l (outputs x0 - 2 .. x0 + 25, x0 a multiple
+// of 28, so that the staged columns start on a 16-byte boundary), warp w
+// the kZR rows y0 - 1 + kZR w .. (the tile and one row either side).  Each
+// slice of m is staged by cp.async (16-byte copies when rows are 16-byte
+// aligned), two slices ahead, into a ring of four slices of kZRows x 32
+// voxels (zeros outside the image), from which a thread reads its rows and
+// the row on either side.
+//
+// The stencil is the FP32 form above (tv3_r, tv3_inslice, tv3_u: v = 2 u,
+// m' = m - (2 coef) u, ||v||^2 = 4 sum u^2).  Each voxel's stencil is a
+// state of two registers carried down z (ZWalkField): its value at the last
+// slice in and u's in-slice terms there; the next slice gives r+z and
+// completes u.  x neighbours come by shuffles, y
+// neighbours from the thread's other rows, and r of the row below a thread's
+// last row is evaluated again by the thread itself, so the staged slice is
+// the only exchange between warps for m.  Per slice k:
+//   m(k) in: r(k); u(m) of slice k - 1 and m' = m - 2 coef u (zero outside
+//            the image); the in-slice terms of slice k;
+//   m'(k - 1): the same walk one slice behind on m' (the rows above and
+//            below each warp's rows through shared memory), giving u(m') of
+//            slice k - 2 on the tile: ||v(m')||^2.
+// A step reads each voxel once and writes it once.  ||v(m')||^2 (or the
+// last step's positivity-change norm) is summed per tile and slab of 16
+// slices, and the block that finishes last sums the slab partials in order;
+// walks of `slabs` consecutive slabs (host-chosen) give the same bits for
+// every choice.
+constexpr int kZTX = 28;                   // output columns of a tile
+constexpr int kZR = 8;                     // rows of a thread
+constexpr int kZWarps = 4;
+constexpr int kZThreads = kZWarps * 32;
+constexpr int kZTY = kZWarps * kZR - 2;    // output rows of a tile
+constexpr int kZRows = kZWarps * kZR + 2;  // staged rows
+constexpr int kZSlab = 16;                 // slices of a partial
+constexpr int kZMinBlocks = 3;             // resident blocks per SM
+constexpr int kZCopies = (kZRows * 8 + kZThreads - 1) / kZThreads;  // 16-byte copies of a thread
+static_assert(kZTX + 4 == 32 && kZThreads % 8 == 0, "lane = staged column");
 
-__host__ __device__ __forceinline__ int zwalk_tiles_x(int nx) { return (nx + kZTX - 1) / kZTX; }
+struct ZShared {
+  float m[4][kZRows][32];  // ring of staged slices of m
+  float p[2][kZRows][32];  // m' of two slices: the first and last row of each warp
+  float red[kZThreads / 32];
+};
+
+// tiles: output columns [28 t - 2, 28 t + 26), rows [kZTY t, kZTY (t + 1))
+__host__ __device__ __forceinline__ int zwalk_tiles_x(int nx) { return (nx + 2 + kZTX - 1) / kZTX; }
 __host__ __device__ __forceinline__ int zwalk_tiles_y(int ny) { return (ny + kZTY - 1) / kZTY; }
 __host__ __device__ __forceinline__ int zwalk_slabs(int nz) { return (nz + kZSlab - 1) / kZSlab; }
 
+// The stencil state of one field at a thread's rows: c the value at the last
+// slice in, s the in-slice part of u there; cb the value of the row below
+// the thread's last row.
+struct ZWalkField {
+  float c[kZR], s[kZR];
+  float cb;
+};
+// Slice k of a field comes in (n: the thread's rows; na, nb: the rows above
+// and below): u of slice k - 1 into u[] (when kU), and the state moves to
+// slice k.
+template <bool kU>
+__device__ __forceinline__ void zfield_push(ZWalkField &f, const float (&n)[kZR], float na,
+                                            float nb, float (&u)[kZR]) {
+  float r[kZR + 1], xm[kZR];
+#pragma unroll
+  for (int i = 0; i <= kZR; i++) {
+    const float v = i < kZR ? n[i] : nb;
+    const float up = i == 0 ? na : n[i - 1];
+    const float prev = i < kZR ? f.c[i] : f.cb;
+    const float l = __shfl_up_sync(0xffffffffu, v, 1);
+    r[i] = tv3_r(__fsub_rn(v, l), __fsub_rn(v, up), __fsub_rn(v, prev));
+    if (i < kZR) xm[i] = l;
+  }
+#pragma unroll
+  for (int i = 0; i < kZR; i++) {
+    if (kU) u[i] = tv3_u(f.s[i], f.c[i], n[i], r[i]);
+    const float up = i == 0 ? na : n[i - 1];
+    const float below = i + 1 < kZR ? n[i + 1] : nb;
+    const float xp = __shfl_down_sync(0xffffffffu, n[i], 1);
+    const float rx = __shfl_down_sync(0xffffffffu, r[i], 1);
+    f.s[i] = tv3_inslice(n[i], xm[i], up, f.c[i], xp, below, r[i], rx, r[i + 1]);
+    f.c[i] = n[i];
+  }
+  f.cb = nb;
+}
+
 // kMode as in tv_walk: 0 m' and ||v(m')||^2; 1 m' only; 2 the finishing step.
-template <int kMode>
+// kVec: rows of the image start on 16-byte boundaries (16-byte staging).
+template <int kMode, bool kVec>
 __device__ __forceinline__ void tv_zwalk(const Inst &I, int step, int x0, int y0, int z0,
                                          int z1, float coef, float &acc, int tile, int ntiles,
-                                         float (*sm)[kZH][kZW], float (*sr)[kZH][kZW],
-                                         float (*sp)[kZH][kZW], float (*sq)[kZH][kZW],
-                                         float *shf) {
+                                         ZShared &sh) {
   const Dims D = I.d;
   const float *src = tv_src(I, step);
   float *dst = tv_dst(I, step);
   float *const im = I.m, *const impre = I.m_pre;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const long long plane = (long long)D.nx * D.ny;
-  const int gx = x0 - 2 + lane;
+  const long long plane = (long long)D.nx * D.ny, nvox = plane * D.nz;
+  const int gx = x0 - 4 + lane;
   const bool colin = gx >= 0 && gx < D.nx;
-  int gy[2];
-  bool in2[2];  // this thread's staged voxels lie inside the image in (x, y)
+  const int sy = kZR * warp + 1;  // staged row of the thread's first row
+  const float coef2 = 2.f * coef;
+  // bit i: the thread's row i lies in the image (x, y) / is an output voxel
+  unsigned rin = 0u, rout = 0u;
 #pragma unroll
-  for (int h = 0; h < 2; h++) {
-    gy[h] = y0 - 2 + warp + 16 * h;
-    in2[h] = colin && gy[h] >= 0 && gy[h] < D.ny;
+  for (int i = 0; i < kZR; i++) {
+    const int gy = y0 - 2 + sy + i;
+    if (colin && gy >= 0 && gy < D.ny) {
+      rin |= 1u << i;
+      if (lane >= 2 && lane < 30 && sy + i >= 2 && sy + i < kZRows - 2) rout |= 1u << i;
+    }
   }
+  const long long row0 = (long long)(y0 - 2 + sy) * D.nx + gx;  // (x, y) of the first row
+  // staging.  kVec: thread t copies 4 columns (group t & 7) of rows
+  // t / 8 + j T / 8; otherwise warp w copies rows w + j kZWarps, a column per
+  // lane.  Bit j of smask: that copy lies in the image (x, y).
+  constexpr int kSR = kVec ? kZCopies : (kZRows + kZWarps - 1) / kZWarps;
+  constexpr int kRowStep = kVec ? kZThreads / 8 : kZWarps;
+  const int srow0 = kVec ? (int)threadIdx.x / 8 : warp;
+  const int scol = kVec ? x0 - 4 + 4 * (threadIdx.x & 7) : gx;
+  unsigned smask = 0u;
+#pragma unroll
+  for (int j = 0; j < kSR; j++) {
+    const int srow = srow0 + j * kRowStep, gy = y0 - 2 + srow;
+    if (srow < kZRows && scol >= 0 && scol < D.nx && gy >= 0 && gy < D.ny) smask |= 1u << j;
+  }
+  const long long soff = (long long)(y0 - 2 + srow0) * D.nx + scol;
+  const int sstep = kRowStep * D.nx;
+  const unsigned sbase = (unsigned)__cvta_generic_to_shared(
+      kVec ? &sh.m[0][srow0][4 * (threadIdx.x & 7)] : &sh.m[0][srow0][lane]);
   auto zin = [&](int z) { return z >= 0 && z < D.nz; };
   auto stage = [&](int z) {  // slice z into ring slot z & 3
+    const unsigned m = zin(z) ? smask : 0u;
+    const long long zo = z * plane + soff;
+    const unsigned sa = sbase + (unsigned)(z & 3) * (unsigned)sizeof(sh.m[0]);
 #pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const long long gi = z * plane + (long long)gy[h] * D.nx + gx;
-      const bool in = in2[h] && zin(z) && ASD_IN(gi, plane * D.nz);
+    for (int j = 0; j < kSR; j++) {
+      if (srow0 + j * kRowStep >= kZRows) break;
+      const long long gi = zo + (long long)j * sstep;
+      const bool in = ((m >> j) & 1u) && ASD_IN(gi, nvox) && (!kVec || ASD_IN(gi + 3, nvox));
       const float *g = in ? src + gi : src;
-      const unsigned sa = (unsigned)__cvta_generic_to_shared(&sm[z & 3][warp + 16 * h][lane]);
-      asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(g),
-                   "r"(in ? 4 : 0)
-                   : "memory");
+      const unsigned d = sa + (unsigned)(j * kRowStep * 32 * 4);
+      if (kVec)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(g),
+                     "r"(in ? 16 : 0)
+                     : "memory");
+      else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(g),
+                     "r"(in ? 4 : 0)
+                     : "memory");
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
-  };
-  // r of field f (previous slice fb) on [lo, hi)^2
-  auto pass_r = [&](const float(*f)[kZW], const float(*fb)[kZW], float(*r)[kZW], int lo,
-                    int hi) {
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int yy = warp + 16 * h;
-      if (yy < lo || yy >= hi || lane < lo || lane >= hi) continue;
-      const float c = f[yy][lane];
-      r[yy][lane] = tv3_r(__fsub_rn(c, f[yy][lane - 1]), __fsub_rn(c, f[yy - 1][lane]),
-                          __fsub_rn(c, fb[yy][lane]));
-    }
-  };
-  auto vat = [&](const float(*fm)[kZW], const float(*f)[kZW], const float(*fp)[kZW],
-                 const float(*r)[kZW], const float(*rp)[kZW], int yy) {
-    return tv3_combine(f[yy][lane], f[yy][lane - 1], f[yy - 1][lane], fm[yy][lane],
-                       f[yy][lane + 1], f[yy + 1][lane], fp[yy][lane], r[yy][lane],
-                       r[yy][lane + 1], r[yy + 1][lane], rp[yy][lane]);
   };
   auto flush = [&](int z) {  // the slab of output slice z is complete
     const float vv[1] = {acc};
     float bs[1];
-    block_sum_f<kZThreads, 1>(vv, bs, shf);
-    if (threadIdx.x == 0) I.partials[(long long)(z / kZSlab) * ntiles + tile] = (double)bs[0];
+    block_sum_f<kZThreads, 1>(vv, bs, sh.red);
+    // kMode 0 sums u^2 = v^2 / 4 (scaling by 4 is exact)
+    if (threadIdx.x == 0)
+      I.partials[(long long)(z / kZSlab) * ntiles + tile] =
+          (double)bs[0] * (kMode == 0 ? 4.0 : 1.0);
     acc = 0.f;
   };
-  auto ring3 = [](int z) { return (z % 3 + 3) % 3; };
-  // an output voxel of this thread: tile rows and columns [2, 30)
-  auto outvox = [&](int h) {
-    const int yy = warp + 16 * h;
-    return yy >= 2 && yy < kZH - 2 && lane >= 2 && lane < kZW - 2 && in2[h];
-  };
-  stage(z0 - 2);
-  stage(z0 - 1);
-  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-  __syncthreads();
-  stage(z0);
-  pass_r(sm[(z0 - 1) & 3], sm[(z0 - 2) & 3], sr[(z0 - 1) & 1], 1, kZW);
+  // z >= 0 here
+  auto slab_end = [&](int z) { return ((z + 1) & (kZSlab - 1)) == 0 || z + 1 == z1; };
+  // m slices kstart - 1 .. kend; u(m) of kstart .. kend - 1
+  const int kstart = kMode == 0 ? z0 - 1 : z0;
   const int kend = kMode == 0 ? z1 + 1 : z1;
-  for (int k = z0; k <= kend; k++) {
-    // the finishing step's pre-TV image at this thread's voxels of slice
-    // k - 1, loaded early so the load overlaps the wait and pass A
-    float f0[2] = {0.f, 0.f};
-    if (kMode == 2 && k - 1 >= z0 && k - 1 < z1) {
+  if (warp == 0) {  // rows of m' no warp writes (outside the block's rows)
+    sh.p[0][0][lane] = sh.p[1][0][lane] = 0.f;
+    sh.p[0][kZRows - 1][lane] = sh.p[1][kZRows - 1][lane] = 0.f;
+  }
+  stage(kstart - 1);
+  stage(kstart);
+  stage(kstart + 1);
+  asm volatile("cp.async.wait_group 2;\n" ::: "memory");  // slice kstart - 1 landed
+  __syncthreads();
+  ZWalkField fm, fp;
 #pragma unroll
-      for (int h = 0; h < 2; h++)
-        if (outvox(h)) {
-          const long long gi = (k - 1) * plane + (long long)gy[h] * D.nx + gx;
-          f0[h] = ASD_IN(gi, plane * D.nz) ? im[gi] : 0.f;
-        }
+  for (int i = 0; i < kZR; i++) {
+    fm.c[i] = sh.m[(kstart - 1) & 3][sy + i][lane];
+    fm.s[i] = 0.f;
+    fp.c[i] = fp.s[i] = 0.f;
+  }
+  fm.cb = sh.m[(kstart - 1) & 3][sy + kZR][lane];
+  fp.cb = 0.f;
+  float mp[kZR];  // m' of the thread's rows, from part A to the next step's part B
+  // Step k: one barrier (slice k of m staged; the edge rows of m'(k - 2)
+  // written by the other warps in the previous step), then
+  //   B: the walk on m' takes m'(k - 2) (kMode 0): u(m') of slice k - 3;
+  //   A: the walk on m takes slice k: u(m) and m' of slice k - 1.
+  // A steady step (kS) is one whose slices (k - 1 for A, k - 3 for B) are
+  // output slices of the walk, so that it needs no range tests; the steady
+  // steps run in pairs, which lets the state alternate between registers
+  // instead of being copied.
+  auto walk_step = [&](auto steady, int k) {
+    constexpr bool kS = decltype(steady)::value;
+    const int zb = k - 1;  // slice whose u(m) and m' part A gives
+    const long long ob = zb * plane + row0;  // its voxel at the thread's first row
+    const bool a_on = kS || k <= kend;
+    const bool a_out = kS || (k > kstart && zb >= z0 && zb < z1);
+    // the finishing step's pre-TV image at the output voxels of slice zb,
+    // loaded early so that the loads overlap the wait
+    float f0[kZR];
+#pragma unroll
+    for (int i = 0; i < kZR; i++) {
+      f0[i] = 0.f;
+      if (kMode == 2 && a_out && ((rout >> i) & 1u) && ASD_IN(ob + i * D.nx, nvox))
+        f0[i] = im[ob + i * D.nx];
     }
-    if (k + 1 <= kend)
-      stage(k + 1);
-    else
-      asm volatile("cp.async.commit_group;\n" ::: "memory");
-    asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // slice k landed
+    stage(k + 2);  // slices past the walk's end are staged too (in the image or zeros)
+    asm volatile("cp.async.wait_group 2;\n" ::: "memory");  // slice k landed
     __syncthreads();
-    // A: r(k)
-    pass_r(sm[k & 3], sm[(k - 1) & 3], sr[k & 1], 1, kZW);
-    __syncthreads();
-    // B: v(m) and m' of slice k - 1
-    const float(*m0)[kZW] = sm[(k - 2) & 3];
-    const float(*m1)[kZW] = sm[(k - 1) & 3];
-    const float(*m2)[kZW] = sm[k & 3];
-    const float(*r1)[kZW] = sr[(k - 1) & 1];
-    const float(*r2)[kZW] = sr[k & 1];
-    const int zb = k - 1;
-    if (kMode == 0) {
-      float(*mp)[kZW] = sp[ring3(zb)];
+    // B: m'(k - 2), written by part A of step k - 1 (kMode 0)
+    if (kMode == 0 && (kS || k - 1 > kstart)) {
+      const float(*ps)[32] = sh.p[k & 1];
+      const float pa = ps[sy - 1][lane], pb = ps[sy + kZR][lane];
+      const int zd = k - 3;  // slice whose u(m') this gives
+      float u[kZR];
+      if (kS || zd >= z0) {
+        zfield_push<true>(fp, mp, pa, pb, u);
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int yy = warp + 16 * h;
-        if (yy < 1 || yy >= kZH - 1 || lane < 1 || lane >= kZW - 1) continue;
-        const float v = vat(m0, m1, m2, r1, r2, yy);
-        mp[yy][lane] = (in2[h] && zin(zb)) ? __fmaf_rn(-coef, v, m1[yy][lane]) : 0.f;
+        for (int i = 0; i < kZR; i++)
+          if ((rout >> i) & 1u) acc += u[i] * u[i];
+        if (slab_end(zd)) flush(zd);
+      } else {
+        zfield_push<false>(fp, mp, pa, pb, u);
       }
-    } else if (zb >= z0 && zb < z1) {
-      // the single or finishing step: m' on the tile only
+    }
+    if (!a_on) return;
+    // A: slice k of m
+    const float(*ms)[32] = sh.m[k & 3];
+    float n[kZR], u[kZR];
 #pragma unroll
-      for (int h = 0; h < 2; h++) {
-        if (!outvox(h)) continue;
-        const int yy = warp + 16 * h;
-        const float mn = __fmaf_rn(-coef, vat(m0, m1, m2, r1, r2, yy), m1[yy][lane]);
-        const long long gi = zb * plane + (long long)gy[h] * D.nx + gx;
-        if (!ASD_IN(gi, plane * D.nz)) continue;
+    for (int i = 0; i < kZR; i++) n[i] = ms[sy + i][lane];
+    const float na = ms[sy - 1][lane], nb = ms[sy + kZR][lane];
+    if (!kS && k == kstart) {
+      zfield_push<false>(fm, n, na, nb, u);
+      return;  // the first slice: nothing else to do yet
+    }
+    float mprev[kZR];
+#pragma unroll
+    for (int i = 0; i < kZR; i++) mprev[i] = fm.c[i];
+    zfield_push<true>(fm, n, na, nb, u);
+    const unsigned rinz = (kS || zin(zb)) ? rin : 0u;
+#pragma unroll
+    for (int i = 0; i < kZR; i++) {
+      const float mn = __fmaf_rn(-coef2, u[i], mprev[i]);
+      const long long gi = ob + i * D.nx;
+      const bool o = a_out && ((rout >> i) & 1u) && ASD_IN(gi, nvox);
+      if (kMode == 0) {
+        mp[i] = ((rinz >> i) & 1u) ? mn : 0.f;
+        if (o) dst[gi] = mn;
+      } else if (o) {
         if (kMode == 1) {
           dst[gi] = mn;
         } else {
           const float mc = mn < 0.f ? 0.f : mn;  // imgTVGradMin3D.cpp:163-170
-          const float d = mc - f0[h];
+          const float d = mc - f0[i];
           acc += d * d;
           im[gi] = mc;
           impre[gi] = mc;
         }
       }
-      if (kMode == 2 && ((zb + 1) % kZSlab == 0 || zb + 1 == z1)) flush(zb);
     }
-    // the next step's staging overwrites slice k - 2's ring slot
-    __syncthreads();
-    if (kMode != 0) continue;
-    // C: r'(k - 1) (needs m' of k - 2, computed one step earlier)
-    const int zc = k - 1;
-    if (zc >= z0) pass_r(sp[ring3(zc)], sp[ring3(zc - 1)], sq[zc & 1], 2, kZW - 1);
-    __syncthreads();
-    // D: v(m') of slice k - 2 on the tile, m' written out
-    const int zd = k - 2;
-    if (zd >= z0) {
-      const float(*p0)[kZW] = sp[ring3(zd - 1)];
-      const float(*p1)[kZW] = sp[ring3(zd)];
-      const float(*p2)[kZW] = sp[ring3(zd + 1)];
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        if (!outvox(h)) continue;
-        const int yy = warp + 16 * h;
-        const long long gi = zd * plane + (long long)gy[h] * D.nx + gx;
-        if (ASD_IN(gi, plane * D.nz)) dst[gi] = p1[yy][lane];
-        const float w = vat(p0, p1, p2, sq[zd & 1], sq[(zd + 1) & 1], yy);
-        acc += w * w;
-      }
-      if ((zd + 1) % kZSlab == 0 || zd + 1 == z1) flush(zd);
+    if (kMode == 2 && a_out && slab_end(zb)) flush(zb);
+    if (kMode == 0) {  // the edge rows of m'(k - 1) for the neighbouring warps
+      float(*ps)[32] = sh.p[(k + 1) & 1];
+      ps[sy][lane] = mp[0];
+      ps[sy + kZR - 1][lane] = mp[kZR - 1];
     }
+  };
+  // steady steps: kMode 0 k = z0 + 3 .. z1 (A: k - 1, B: k - 3 inside
+  // [z0, z1)), kMode 1 and 2 k = z0 + 1 .. z1 (A: k - 1 inside [z0, z1))
+  const int ks0 = kMode == 0 ? z0 + 3 : z0 + 1, ks1 = z1;
+  const int klast = kMode == 0 ? kend + 1 : kend;  // kMode 0: a last step of part B only
+  int k = kstart;
+#pragma unroll 1
+  for (; k < ks0 && k <= klast; k++) walk_step(std::false_type(), k);
+#pragma unroll 1
+  for (; k + 1 <= ks1; k += 2) {
+    walk_step(std::true_type(), k);
+    walk_step(std::true_type(), k + 1);
   }
+#pragma unroll 1
+  for (; k <= klast; k++) walk_step(std::false_type(), k);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kZThreads)
+template <int kMode>
+__device__ __forceinline__ void tv_zwalk_any(const Inst &I, int step, int x0, int y0, int z0,
+                                             int z1, float coef, float &acc, int tile,
+                                             int ntiles, ZShared &sh) {
+  // 16-byte copies need 16-byte aligned rows
+  const bool vec = (I.d.nx & 3) == 0 && ((unsigned long long)tv_src(I, step) & 15) == 0;
+  if (vec)
+    tv_zwalk<kMode, true>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sh);
+  else
+    tv_zwalk<kMode, false>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sh);
+}
+
+__global__ void __launch_bounds__(kZThreads, kZMinBlocks)
     k_tv_walk3d(const Inst *__restrict__ insts, int step, int slabs) {
-  __shared__ float sm[4][kZH][kZW], sr[2][kZH][kZW], sp[3][kZH][kZW], sq[2][kZH][kZW];
-  __shared__ float shf[kZThreads / 32];
+  __shared__ __align__(16) ZShared sh;
   __shared__ int s_last;
   pdl_enter();
   const Inst &I = insts[blockIdx.z];
@@ -1057,11 +1175,11 @@ __global__ void __launch_bounds__(kZThreads)
   const float coef = I.s->tv_coef_f;
   float acc = 0.f;
   if (!last)
-    tv_zwalk<0>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sm, sr, sp, sq, shf);
+    tv_zwalk_any<0>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sh);
   else if (ng == 1)
-    tv_zwalk<1>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sm, sr, sp, sq, shf);
+    tv_zwalk_any<1>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sh);
   else
-    tv_zwalk<2>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sm, sr, sp, sq, shf);
+    tv_zwalk_any<2>(I, step, x0, y0, z0, z1, coef, acc, tile, ntiles, sh);
   if (last && ng == 1) return;
   if (threadIdx.x == 0) {
     __threadfence();
@@ -1179,11 +1297,11 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
   (void)ng;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1) {
-    // slabs per walk: the batch's walks within about one wave of 2 resident
-    // blocks per SM (16 warps and 44 KB of slices each)
+    // slabs per walk: the batch's walks within about one wave of resident
+    // blocks
     const long long tiles = (long long)zwalk_tiles_x(d.nx) * zwalk_tiles_y(d.ny);
     const long long units = tiles * zwalk_slabs(d.nz);
-    const long long cap = 152LL * 2;
+    const long long cap = 152LL * kZMinBlocks;
     const long long per = walk > 0 ? walk : (units * batch + cap - 1) / cap;
     const int slabs = (int)(per < 1 ? 1 : (per > zwalk_slabs(d.nz) ? zwalk_slabs(d.nz) : per));
     const long long walks = tiles * ((zwalk_slabs(d.nz) + slabs - 1) / slabs);

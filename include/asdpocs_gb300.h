@@ -361,7 +361,8 @@ int asdpocs_plan_chord_slots(asdpocs_plan plan);
  * batch.  phase: 0 = SART forward step (Ax + residual), 1 = SART backward
  * step (Atx + update; each timed launch follows its view's untimed
  * forward step, whose residuals and tables it reads), both at `reps` views
- * spread evenly over the scan, 2 = one TV step (norm pass + update pass),
+ * spread evenly over the scan, 2 = one TV step (the steps that do not end
+ * the iteration),
  * 3 = end-of-sweep scalars.  The launches modify the plan's state: call
  * asdpocs_plan_reset() before the next run. */
 int asdpocs_plan_time_phase(asdpocs_plan plan, int phase, int reps,
