@@ -1462,10 +1462,10 @@ __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
             if (!f[u][j]) continue;
 #pragma unroll
             for (int q = 0; q < kQ; q++) {
-              v[4 * q] += w[u][j] * x[u][j][q].x;
-              v[4 * q + 1] += w[u][j] * x[u][j][q].y;
-              v[4 * q + 2] += w[u][j] * x[u][j][q].z;
-              v[4 * q + 3] += w[u][j] * x[u][j][q].w;
+              v[4 * q] = weight_fma(w[u][j], x[u][j][q].x, v[4 * q]);
+              v[4 * q + 1] = weight_fma(w[u][j], x[u][j][q].y, v[4 * q + 1]);
+              v[4 * q + 2] = weight_fma(w[u][j], x[u][j][q].z, v[4 * q + 2]);
+              v[4 * q + 3] = weight_fma(w[u][j], x[u][j][q].w, v[4 * q + 3]);
             }
             v[kS] += w[u][j];
           }

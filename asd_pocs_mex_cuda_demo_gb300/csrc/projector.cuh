@@ -31,6 +31,26 @@ ASD_HD float fast_div(float a, float b) {
 #endif
 }
 
+// Forward-step weights and sums (never a branch decision): the hardware
+// square root (sqrt.approx, within 2^-22 relative) and fused multiply-adds
+// in device code; the IEEE square root and fmaf in the host build.
+ASD_HD float weight_sqrt(float x) {
+#ifdef __CUDA_ARCH__
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+#else
+  return sqrtf(x);
+#endif
+}
+ASD_HD float weight_fma(float a, float b, float c) {
+#ifdef __CUDA_ARCH__
+  return __fmaf_rn(a, b, c);
+#else
+  return fmaf(a, b, c);
+#endif
+}
+
 // ---------------------------------------------------------------------------
 // Ax: partial sums of one ray over the columns iu = first, first+step, ...
 // (Ax_cone_gpu.cu:339-776).
@@ -90,10 +110,12 @@ ASD_HD RayMarch ray_setup(const ViewGeo &G, const Dims &D,
 // kExact = true evaluates every weight with the reference's expressions
 // (bit-identical per column).  kExact = false (the kernels) keeps every
 // branch decision identical -- cell indices and split tests use the same
-// float expressions -- but forms the weights without IEEE divisions: the
-// column length as sqrt((d*d+1)*lfac) (lfac = (len2+dz2sq)/len2 per ray) and
-// the split fractions with the hardware reciprocal, each within 2 ulp of the
-// reference's value.
+// float expressions -- but forms the weights without IEEE divisions or
+// square roots: the column length as sqrt(fma(d, d, 1) * lfac) (lfac =
+// (len2+dz2sq)/len2 per ray) through the hardware square root and the split
+// fractions through the hardware reciprocal, each within 2 ulp of the
+// reference's value, and adds weight * voxel to the ray sum with one fused
+// multiply-add.
 template <bool kExact = true, class Loader>
 ASD_HD void ray_columns(const RayMarch &R, int first,
                                             int step, Loader ld, float &ys,
@@ -146,16 +168,16 @@ ASD_HD void ray_columns(const RayMarch &R, int first,
 
     const float d = v2 - v1;
     const float l = kExact ? sqrtf((d * d + 1) * (R.len2 + R.dz2sq) / R.len2)
-                           : sqrtf((d * d + 1) * R.lfac);
+                           : weight_sqrt(weight_fma(d, d, 1.f) * R.lfac);
     const unsigned base = (unsigned)iu * R.su;
     const unsigned ilo = base + (unsigned)cv1 * R.sv;
     const unsigned ihi = base + (unsigned)cv2 * R.sv;
     const unsigned zl = (unsigned)cz1 * R.sz, zh = (unsigned)cz2 * R.sz;
-#define ASD_PIECE(w, idx)   \
-  do {                      \
-    const float w_ = (w);   \
-    ys += w_ * ld(idx);     \
-    ss += w_;               \
+#define ASD_PIECE(w, idx)                                   \
+  do {                                                      \
+    const float w_ = (w);                                   \
+    ys = kExact ? ys + w_ * ld(idx) : weight_fma(w_, ld(idx), ys); \
+    ss += w_;                                               \
   } while (0)
     if (!vsplit && !zsplit) {
       ASD_PIECE(l, ilo + zl);
@@ -217,7 +239,7 @@ ASD_HD void column_pieces3(const RayMarch &R, int iu, unsigned (&id)[3],
                    cz1 >= 0 && cz1 < R.nz;
   const bool zhi = zs && (zmid || cz2 == 0) && cz2 >= 0 && cz2 < R.nz;
   const float d = v2 - v1;
-  const float l = sqrtf((d * d + 1) * R.lfac);
+  const float l = weight_sqrt(weight_fma(d, d, 1.f) * R.lfac);
   const float rv = fast_div(cv2 - v1, d);
   const float rz = fast_div(cz2 - w1, w2 - w1);
   const unsigned base = (unsigned)iu * R.su;
@@ -263,7 +285,7 @@ ASD_HD void ray_columns_fast(const RayMarch &R, int first, int step, Loader ld,
 #pragma unroll
       for (int j = 0; j < 3; j++)
         if (f[k][j]) {
-          ys += w[k][j] * x[k][j];
+          ys = weight_fma(w[k][j], x[k][j], ys);
           ss += w[k][j];
         }
   }
@@ -294,9 +316,10 @@ ASD_HD void ray_columns_planar(const RayMarch &R, int first,
     if (cv1 == cv2) {
       if (cv1 < 0 || cv1 > R.nv - 1) continue;
       const float l = kExact ? sqrtf((d * d + 1) * R.len2 / R.len2)
-                             : sqrtf(d * d + 1);
+                             : weight_sqrt(weight_fma(d, d, 1.f));
       const float w = l;
-      ys += w * ld(base + (unsigned)cv1 * R.sv);
+      const float x = ld(base + (unsigned)cv1 * R.sv);
+      ys = kExact ? ys + w * x : weight_fma(w, x, ys);
       ss += w;
     } else {
       bool vlo, vhi;
@@ -310,16 +333,18 @@ ASD_HD void ray_columns_planar(const RayMarch &R, int first,
       vhi = vhi && cv2 >= 0 && cv2 < R.nv;
       if (!(vlo || vhi)) continue;
       const float l = kExact ? sqrtf((d * d + 1) * R.len2 / R.len2)
-                             : sqrtf(d * d + 1);
+                             : weight_sqrt(weight_fma(d, d, 1.f));
       const float rv = kExact ? (cv2 - v1) / d : fast_div(cv2 - v1, d);
       if (vlo) {
         const float w = rv * l;
-        ys += w * ld(base + (unsigned)cv1 * R.sv);
+        const float x = ld(base + (unsigned)cv1 * R.sv);
+        ys = kExact ? ys + w * x : weight_fma(w, x, ys);
         ss += w;
       }
       if (vhi) {
         const float w = (1 - rv) * l;
-        ys += w * ld(base + (unsigned)cv2 * R.sv);
+        const float x = ld(base + (unsigned)cv2 * R.sv);
+        ys = kExact ? ys + w * x : weight_fma(w, x, ys);
         ss += w;
       }
     }
@@ -349,7 +374,7 @@ ASD_HD void column_pieces_planar(const RayMarch &R, int iu, unsigned (&id)[2],
   f[0] = in && cv1 >= 0 && cv1 < R.nv && (split ? (mid || cv2 == R.nv) : true);
   f[1] = in && split && cv2 >= 0 && cv2 < R.nv && (mid || cv2 == 0);
   const float d = v2 - v1;
-  const float l = sqrtf(d * d + 1);
+  const float l = weight_sqrt(weight_fma(d, d, 1.f));
   const float rv = fast_div(cv2 - v1, d);
   w[0] = split ? rv * l : l;
   w[1] = (1 - rv) * l;
@@ -381,7 +406,7 @@ ASD_HD void ray_columns_planar_fast(const RayMarch &R, int first, int step,
 #pragma unroll
       for (int j = 0; j < 2; j++)
         if (f[k][j]) {
-          ys += w[k][j] * x[k][j];
+          ys = weight_fma(w[k][j], x[k][j], ys);
           ss += w[k][j];
         }
   }
