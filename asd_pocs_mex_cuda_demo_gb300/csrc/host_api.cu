@@ -1,5 +1,6 @@
 // Host side of the asdpocs_gb300 C ABI: launcher drop-ins, mex-level entry
 // points, TV entry points and the device-resident ASD-POCS plans.
+#include <limits.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -9,6 +10,7 @@
 #include <algorithm>
 #include <mutex>
 #include <new>
+#include <numeric>
 #include <vector>
 
 #include "instance.h"
@@ -620,8 +622,25 @@ namespace asd {
 // Instances never read each other's state, so results do not change.
 struct SubBatch {
   int first = 0, count = 0;  // instances [first, first + count)
+  // plans of uneven instances: the sub-batch's instances (any of the plan's,
+  // in order) and their device list in the plan's arena (null: the range
+  // above)
+  std::vector<int> members;
+  std::vector<int> units;  // the groups (mixed plans) or instances dealt to it
+  const int *zall = nullptr;
+  // runs the shared-geometry kernels: over [first, first + count) in groups
+  // of kShareSlots, or (mixed plans) over the groups of groups_host (first
+  // position in d_inst, count) with their device list gall
+  bool shared = false;
+  std::vector<int2> groups_host;
+  const int2 *gall = nullptr;
+  std::vector<int2> gtab_host;  // mixed plans: the view sets' group lists
   Dims d{};                  // largest sizes of these instances
   int nv = 0, max_ng = 0, min_ng = 0;
+  // instances of different view counts: the runs of views and who has them
+  // (lists in the plan's arena), and the lists on the host
+  std::vector<ViewSet> sets;
+  std::vector<int> zmap_host;
   cudaStream_t st = nullptr;  // the plan's stream when there is one sub-batch
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -642,6 +661,15 @@ struct asdpocs_plan_s {
   std::vector<Inst> h_inst;
   std::vector<int> has_ref;
   bool shared = false;  // all instances share sizes, geometry and angles
+  // 2-D instances of several geometries that run as groups of instances
+  // sharing geometry (the shared-geometry kernels with group tables): the
+  // groups (instance indices) and each instance's position in d_inst, where
+  // every group is contiguous
+  bool mixed = false;
+  std::vector<std::vector<int>> groups;
+  std::vector<int> gclass;  // each group's geometry (groups of one geometry share it)
+  std::vector<int> slot;
+  std::vector<Inst> h_dev;  // mixed plans: the descriptors in d_inst order
   bool zcol = true;     // cone beams: z-column backward step (else per voxel)
   bool exact = false;   // forward steps: exact Siddon projection (ax_mode)
   int tv_walk = 0;      // TV walk length (0: from the batch size)
@@ -858,22 +886,41 @@ namespace asd {
 
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              const IterShape &sh, bool finish) {
+                              const IterShape &sh, bool finish,
+                              const std::vector<ViewSet> *sets, const int *zall,
+                              const int2 *gall, int ngroups) {
   const PdlScope scope(sh.pdl);
   cudaError_t e = cudaSuccess;
-  if (shared) e = launch_group_pack(d_inst, batch, d, 0, st);
+  if (shared) e = launch_group_pack(d_inst, batch, d, 0, st, gall, ngroups);
+  const bool by_set = sets && !sets->empty();
+  size_t si = 0;
   for (int v = 0; v < nv && e == cudaSuccess; v++) {
-    e = shared ? launch_sart_ax_shared(d_inst, batch, d, v, st, sh.ax_u, sh.ax_q)
-               : launch_sart_ax(d_inst, batch, d, v, st, sh.exact);
-    if (e == cudaSuccess)
-      e = shared ? launch_sart_atx_shared(d_inst, batch, d, v, st)
-                 : launch_sart_atx(d_inst, batch, d, v, st, sh.zcol, sh.zseg);
+    int vb = batch, vg = ngroups;
+    Dims vd = d;
+    const int *zmap = zall;
+    const int2 *gtab = gall;
+    if (by_set) {
+      while (si + 1 < sets->size() && v >= (*sets)[si].v1) si++;
+      const ViewSet &S = (*sets)[si];
+      vb = vg = S.count;
+      vd = S.d;
+      zmap = S.zmap;
+      gtab = S.gtab;
+      if (S.count == 0) continue;
+    }
+    if (shared) {
+      e = launch_sart_ax_shared(d_inst, batch, vd, v, st, sh.ax_u, sh.ax_q, gtab, vg);
+      if (e == cudaSuccess) e = launch_sart_atx_shared(d_inst, batch, vd, v, st, gtab, vg);
+      continue;
+    }
+    e = launch_sart_ax(d_inst, vb, vd, v, st, sh.exact, zmap);
+    if (e == cudaSuccess) e = launch_sart_atx(d_inst, vb, vd, v, st, sh.zcol, sh.zseg, zmap);
   }
-  if (shared && e == cudaSuccess) e = launch_group_pack(d_inst, batch, d, 1, st);
-  if (e == cudaSuccess) e = launch_after_sweep(d_inst, batch, d, st);
+  if (shared && e == cudaSuccess) e = launch_group_pack(d_inst, batch, d, 1, st, gall, ngroups);
+  if (e == cudaSuccess) e = launch_after_sweep(d_inst, batch, d, st, zall);
   for (int s = 0; s < ng && e == cudaSuccess; s++)
-    e = launch_tv_step(d_inst, batch, d, s, ng, st, sh.tv_walk);
-  if (e == cudaSuccess && finish) e = launch_finish_iter(d_inst, batch, d, ng, st);
+    e = launch_tv_step(d_inst, batch, d, s, ng, st, sh.tv_walk, zall);
+  if (e == cudaSuccess && finish) e = launch_finish_iter(d_inst, batch, d, ng, st, zall);
   return e;
 }
 
@@ -892,8 +939,11 @@ static IterShape plan_shape(asdpocs_plan p) {
 
 // One iteration of sub-batch s on its stream.
 static int plan_enqueue_sub(asdpocs_plan p, const SubBatch &s) {
-  ASD_CUDA(enqueue_iteration(p->d_inst + s.first, s.count, s.d, s.nv, s.max_ng, p->shared,
-                             s.st, plan_shape(p), s.min_ng < 2));
+  const bool listed = !s.members.empty();
+  ASD_CUDA(enqueue_iteration(listed ? p->d_inst : p->d_inst + s.first,
+                             listed ? (int)s.members.size() : s.count, s.d, s.nv, s.max_ng,
+                             s.shared, s.st, plan_shape(p), s.min_ng < 2, &s.sets, s.zall,
+                             s.gall, (int)s.groups_host.size()));
   return 0;
 }
 
@@ -902,7 +952,136 @@ static int plan_enqueue_sub(asdpocs_plan p, const SubBatch &s) {
 // sub-batch runs on the plan's stream.  Sizes, view and TV-step counts per
 // sub-batch.
 constexpr int kMaxSubBatches = 2, kSubGroups = 1;
+// Plans of instances that differ in view count or size run as up to
+// kUnevenSubBatches sub-batches on their own streams: the later views of the
+// instances with the most views are small launches bound by latency, which
+// overlap only across streams.  The units dealt are the plan's groups of
+// instances sharing geometry (mixed plans) or its instances.  Units of the
+// same sizes go to the same sub-batches (a launch's grid is sized for its
+// largest unit, so that mixed sizes leave blocks idle): each class of sizes
+// gets sub-batches in proportion to its work (views x voxels), and its units
+// are dealt by decreasing work to its sub-batch with the least work so far.
+// With more classes than sub-batches every unit is dealt that way over all
+// of them.
+constexpr int kUnevenSubBatches = 8;
+static bool plan_uneven(asdpocs_plan p) {
+  if (p->shared) return false;
+  const asdpocs_geometry &g0 = p->geom[0];
+  for (int i = 1; i < p->batch; i++) {
+    const asdpocs_geometry &g = p->geom[i];
+    if (g.nv != g0.nv || g.nx != g0.nx || g.ny != g0.ny || g.nz != g0.nz || g.na != g0.na ||
+        g.nb != g0.nb)
+      return true;
+  }
+  return false;
+}
+static bool same_sizes(const asdpocs_geometry &g, const asdpocs_geometry &h) {
+  return g.nx == h.nx && g.ny == h.ny && g.nz == h.nz && g.na == h.na && g.nb == h.nb;
+}
+// Units 0 .. n-1 (work[u], an instance of each in rep[u]) dealt to at most
+// nsub bins as described above.
+static std::vector<std::vector<int>> deal_units(asdpocs_plan p, const std::vector<double> &work,
+                                                const std::vector<int> &rep, int nsub) {
+  const int n = (int)work.size();
+  std::vector<std::vector<int>> cls;  // classes of equal sizes, in order of first appearance
+  for (int u = 0; u < n; u++) {
+    size_t c = 0;
+    while (c < cls.size() && !same_sizes(p->geom[rep[u]], p->geom[rep[cls[c][0]]])) c++;
+    if (c == cls.size()) cls.emplace_back();
+    cls[c].push_back(u);
+  }
+  if ((int)cls.size() > nsub) {  // more classes than sub-batches: one class
+    cls.assign(1, std::vector<int>(n));
+    std::iota(cls[0].begin(), cls[0].end(), 0);
+  }
+  // bins per class: one each, the rest one at a time to the class with the
+  // most work per bin (while it has units to spare)
+  std::vector<double> cw(cls.size(), 0.0);
+  std::vector<int> cn(cls.size(), 1);
+  for (size_t c = 0; c < cls.size(); c++)
+    for (int u : cls[c]) cw[c] += work[u];
+  for (int left = nsub - (int)cls.size(); left > 0; left--) {
+    int best = -1;
+    for (size_t c = 0; c < cls.size(); c++)
+      if (cn[c] < (int)cls[c].size() && (best < 0 || cw[c] / cn[c] > cw[best] / cn[best]))
+        best = (int)c;
+    if (best < 0) break;
+    cn[best]++;
+  }
+  std::vector<std::vector<int>> bins;
+  for (size_t c = 0; c < cls.size(); c++) {
+    std::vector<int> ord = cls[c];
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return work[a] > work[b]; });
+    const size_t b0 = bins.size();
+    bins.resize(b0 + cn[c]);
+    std::vector<double> load(cn[c], 0.0);
+    for (int u : ord) {
+      const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+      load[k] += work[u];
+      bins[b0 + k].push_back(u);
+    }
+  }
+  for (auto &b : bins) std::sort(b.begin(), b.end());
+  return bins;
+}
+static void sub_add(SubBatch &s, asdpocs_plan p, int i) {
+  const asdpocs_geometry &g = p->geom[i];
+  s.d.nx = std::max(s.d.nx, g.nx);
+  s.d.ny = std::max(s.d.ny, g.ny);
+  s.d.nz = std::max(s.d.nz, g.nz);
+  s.d.na = std::max(s.d.na, g.na);
+  s.d.nb = std::max(s.d.nb, g.nb);
+  s.nv = std::max(s.nv, g.nv);
+  const int ng = p->opt[i].numOfgradients;
+  s.max_ng = std::max(s.max_ng, ng);
+  s.min_ng = std::min(s.min_ng, ng);
+}
 static int plan_make_subs(asdpocs_plan p) {
+  if (p->mixed || plan_uneven(p)) {
+    // units: the groups (mixed plans) or the instances
+    const int n = p->mixed ? (int)p->groups.size() : p->batch;
+    std::vector<double> work(n);
+    std::vector<int> rep(n);
+    for (int u = 0; u < n; u++) {
+      rep[u] = p->mixed ? p->groups[u][0] : u;
+      const asdpocs_geometry &g = p->geom[rep[u]];
+      // a group's march is shared; its instances' loads and sums are not
+      const double per = p->mixed ? 1.0 + 0.25 * (double)p->groups[u].size() : 1.0;
+      work[u] = (double)g.nv * g.nx * g.ny * g.nz * per;
+    }
+    const std::vector<std::vector<int>> bins =
+        deal_units(p, work, rep, std::min(kUnevenSubBatches, n));
+    const int total = (int)bins.size();
+    p->subs.assign(total, SubBatch{});
+    for (int k = 0; k < total; k++) {
+      SubBatch &s = p->subs[k];
+      s.shared = p->mixed;
+      s.min_ng = INT_MAX;
+      for (int u : bins[k]) {
+        s.units.push_back(u);
+        if (p->mixed) {
+          const std::vector<int> &grp = p->groups[u];
+          s.groups_host.push_back(make_int2(p->slot[grp[0]], (int)grp.size()));
+          for (int i : grp) {
+            s.members.push_back(p->slot[i]);
+            sub_add(s, p, i);
+          }
+        } else {
+          s.members.push_back(u);
+          sub_add(s, p, u);
+        }
+      }
+      std::sort(s.members.begin(), s.members.end());
+      if (total == 1) {
+        s.st = p->st;
+      } else {
+        ASD_CUDA(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
+        ASD_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
+      }
+    }
+    if (total > 1) ASD_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
+    return 0;
+  }
   // whole groups per sub-batch, at least kSubGroups of them
   const int groups = (p->batch + kShareSlots - 1) / kShareSlots;
   const int want = std::max(1, std::min(kMaxSubBatches, groups / kSubGroups));
@@ -911,6 +1090,7 @@ static int plan_make_subs(asdpocs_plan p) {
   p->subs.assign(nsub, SubBatch{});
   for (int k = 0; k < nsub; k++) {
     SubBatch &s = p->subs[k];
+    s.shared = p->shared;
     s.first = k * per;
     s.count = std::min(p->batch, (k + 1) * per) - s.first;
     for (int i = s.first; i < s.first + s.count; i++) {
@@ -936,6 +1116,56 @@ static int plan_make_subs(asdpocs_plan p) {
   return 0;
 }
 
+// Instances of one sub-batch with different view counts (plans without
+// shared geometry): views [0, nv) cut at each distinct view count, and for
+// each run the instances that still have views there, at their largest
+// sizes -- so that the projector steps of the later views launch only those
+// instances' blocks.  Every instance keeps its own grid positions, so its
+// results are the same bits.
+static void plan_view_sets(asdpocs_plan p) {
+  if (p->shared) return;
+  for (SubBatch &s : p->subs) {
+    s.sets.clear();
+    s.zmap_host.clear();
+    s.gtab_host.clear();
+    // units: the sub-batch's groups (mixed plans) or instances
+    std::vector<int> who = s.units;
+    const bool listed = !who.empty();
+    if (!listed)
+      for (int i = s.first; i < s.first + s.count; i++) who.push_back(i);
+    auto rep_of = [&](int u) { return s.shared && listed ? p->groups[u][0] : u; };
+    std::vector<int> cuts;
+    for (int u : who) cuts.push_back(p->geom[rep_of(u)].nv);
+    std::sort(cuts.begin(), cuts.end());
+    cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+    if (cuts.size() < 2) continue;  // every instance has every view
+    int v0 = 0;
+    for (int t : cuts) {
+      ViewSet S;
+      S.v0 = v0;
+      S.v1 = t;
+      S.zoff = s.shared ? s.gtab_host.size() : s.zmap_host.size();
+      for (int u : who) {
+        const int r = rep_of(u);
+        const asdpocs_geometry &g = p->geom[r];
+        if (g.nv <= v0) continue;
+        if (s.shared)
+          s.gtab_host.push_back(make_int2(p->slot[r], (int)p->groups[u].size()));
+        else
+          s.zmap_host.push_back(listed ? u : u - s.first);
+        S.count++;
+        S.d.nx = std::max(S.d.nx, g.nx);
+        S.d.ny = std::max(S.d.ny, g.ny);
+        S.d.nz = std::max(S.d.nz, g.nz);
+        S.d.na = std::max(S.d.na, g.na);
+        S.d.nb = std::max(S.d.nb, g.nb);
+      }
+      s.sets.push_back(S);
+      v0 = t;
+    }
+  }
+}
+
 // First instance of the sub-batch holding instance i.
 static int plan_sub_first(asdpocs_plan p, int i) {
   int f = 0;
@@ -948,6 +1178,18 @@ static int plan_sub_first(asdpocs_plan p, int i) {
 
 extern "C" {
 
+
+// The instances' descriptors to d_inst (mixed plans: in group order).
+static cudaError_t plan_upload(asdpocs_plan p) {
+  const Inst *src = p->h_inst.data();
+  if (p->mixed) {
+    p->h_dev.resize(p->batch);
+    for (int i = 0; i < p->batch; i++) p->h_dev[p->slot[i]] = p->h_inst[i];
+    src = p->h_dev.data();
+  }
+  return cudaMemcpyAsync(p->d_inst, src, sizeof(Inst) * p->batch, cudaMemcpyHostToDevice,
+                         p->st);
+}
 
 // Device bytes the plan's chord tables may take: half the free memory, and
 // what is left of the plan's HBM budget.
@@ -977,8 +1219,49 @@ static cudaError_t plan_chord_tables(asdpocs_plan p) {
     I.chtab = tab;
     I.chK = K;
   }
-  e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(), sizeof(Inst) * p->batch,
-                      cudaMemcpyHostToDevice, p->st);
+  e = plan_upload(p);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
+  return e;
+}
+
+// Mixed plans: a table per geometry (the group's first instance, shared by
+// the groups of that geometry), in group order, while they fit.
+static cudaError_t plan_group_chord_tables(asdpocs_plan p) {
+  size_t room = 0;
+  cudaError_t e = plan_chord_room(p, room);
+  if (e != cudaSuccess) return e;
+  std::vector<int *> made(p->groups.size(), nullptr);
+  std::vector<int> madeK(p->groups.size(), 0);
+  bool any = false;
+  for (size_t k = 0; k < p->groups.size() && e == cudaSuccess; k++) {
+    const int r = p->groups[k][0];
+    int *tab = nullptr, K = 0;
+    // a group of a geometry that already has its table
+    for (size_t j = 0; j < k && !tab; j++)
+      if (made[j] && p->gclass[j] == p->gclass[k]) {
+        tab = made[j];
+        K = madeK[j];
+      }
+    if (!tab) {
+      const asdpocs_geometry &g = p->geom[r];
+      size_t bytes = 0;
+      e = build_chord_tables(p->d_inst + p->slot[r], Dims{g.nx, g.ny, g.nz, g.na, g.nb}, g.nv,
+                             room, p->st, &tab, &K, &bytes);
+      if (!tab) continue;
+      p->inst_tabs.push_back(tab);  // freed with the plan
+      p->bytes += bytes;
+      room -= bytes;
+    }
+    made[k] = tab;
+    madeK[k] = K;
+    p->chK = std::max(p->chK, K);
+    for (int i : p->groups[k]) {
+      p->h_inst[i].chtab = tab;
+      p->h_inst[i].chK = K;
+    }
+    any = true;
+  }
+  if (e == cudaSuccess && any) e = plan_upload(p);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
   return e;
 }
@@ -1007,8 +1290,7 @@ static cudaError_t plan_instance_chord_tables(asdpocs_plan p) {
     any = true;
   }
   if (e == cudaSuccess && any) {
-    e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(), sizeof(Inst) * p->batch,
-                        cudaMemcpyHostToDevice, p->st);
+    e = plan_upload(p);
     if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
   }
   return e;
@@ -1064,16 +1346,16 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   p->has_ref.assign(batch, 0);
   // instances with identical sizes, geometry and view angles share the
   // projector coefficients of every view
+  auto same_geometry = [&](int i, int j) {
+    const asdpocs_geometry &gi = geom[i], &gj = geom[j];
+    return gi.nx == gj.nx && gi.ny == gj.ny && gi.nz == gj.nz && gi.na == gj.na &&
+           gi.nb == gj.nb && gi.nv == gj.nv && gi.SO == gj.SO && gi.OD == gj.OD &&
+           gi.vxlsize == gj.vxlsize && gi.detsize == gj.detsize &&
+           memcmp(phi_vec_deg + phi_off[j], phi_vec_deg + phi_off[i],
+                  sizeof(double) * (size_t)gj.nv) == 0;
+  };
   p->shared = batch > 1;
-  for (int i = 1; i < batch && p->shared; i++) {
-    const asdpocs_geometry &gi = geom[i];
-    p->shared = gi.nx == g0.nx && gi.ny == g0.ny && gi.nz == g0.nz &&
-                gi.na == g0.na && gi.nb == g0.nb && gi.nv == g0.nv &&
-                gi.SO == g0.SO && gi.OD == g0.OD && gi.vxlsize == g0.vxlsize &&
-                gi.detsize == g0.detsize &&
-                memcmp(phi_vec_deg, phi_vec_deg + phi_off[i],
-                       sizeof(double) * (size_t)g0.nv) == 0;
-  }
+  for (int i = 1; i < batch && p->shared; i++) p->shared = same_geometry(i, 0);
   // forward mode: one per plan; the shared-geometry forward step runs the
   // reference's march only, so exact plans run every instance on its own
   for (int i = 0; i < batch; i++)
@@ -1085,6 +1367,50 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   p->exact = p->opt[0].ax_mode == ASDPOCS_AX_EXACT;
   if (p->exact) p->shared = false;
   if (getenv("ASDPOCS_NO_SHARED_GEOMETRY")) p->shared = false;
+  // 2-D instances of several geometries: groups of up to kShareSlots
+  // instances of one geometry (in instance order), laid out one after the
+  // other in d_inst, when some instances share their geometry
+  if (!p->shared && !p->exact && batch > 1 && !getenv("ASDPOCS_NO_SHARED_GEOMETRY")) {
+    bool planar = true;
+    for (int i = 0; i < batch; i++) planar = planar && geom[i].nz == 1 && geom[i].nb == 1;
+    if (planar) {
+      std::vector<int> cls(batch, -1), reps;
+      for (int i = 0; i < batch; i++) {
+        for (size_t c = 0; c < reps.size() && cls[i] < 0; c++)
+          if (same_geometry(i, reps[c])) cls[i] = (int)c;
+        if (cls[i] < 0) {
+          cls[i] = (int)reps.size();
+          reps.push_back(i);
+        }
+      }
+      for (size_t c = 0; c < reps.size(); c++) {
+        std::vector<int> cur;
+        for (int i = 0; i < batch; i++) {
+          if (cls[i] != (int)c) continue;
+          cur.push_back(i);
+          if ((int)cur.size() == kShareSlots) {
+            p->groups.push_back(cur);
+            p->gclass.push_back((int)c);
+            cur.clear();
+          }
+        }
+        if (!cur.empty()) {
+          p->groups.push_back(cur);
+          p->gclass.push_back((int)c);
+        }
+      }
+      p->mixed = p->groups.size() < (size_t)batch;  // else no instance shares
+      if (p->mixed) {
+        p->slot.assign(batch, 0);
+        int k = 0;
+        for (const auto &g : p->groups)
+          for (int i : g) p->slot[i] = k++;
+      } else {
+        p->groups.clear();
+        p->gclass.clear();
+      }
+    }
+  }
   // ASDPOCS_CONE_ATX=voxel: the per-voxel form of the cone-beam backward step
   // (same results; kept for comparison)
   {
@@ -1106,6 +1432,11 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     asdpocs_plan_destroy(p);
     return rc;
   }
+  plan_view_sets(p);
+  // mixed plans: the first instance of each instance's group
+  std::vector<int> group_first(batch, -1);
+  for (const auto &g : p->groups)
+    for (int i : g) group_first[i] = g[0];
   // ---- arena: each instance's block at its own sizes ----
   std::vector<InstLayout> lay(batch);
   std::vector<size_t> base(batch);
@@ -1114,7 +1445,7 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     const size_t M = (size_t)geom[i].na * geom[i].nb;
     // shared-geometry groups interleave their residuals in the buffer of
     // the group's first instance (kShareSlots values per ray)
-    const bool first = p->shared && i % kShareSlots == 0;
+    const bool first = p->shared ? i % kShareSlots == 0 : p->mixed && group_first[i] == i;
     const size_t N = (size_t)geom[i].nx * geom[i].ny * geom[i].nz;
     lay[i] = layout_instance(geom[i], p->opt[i].maxnumIter, first ? M * kShareSlots : M,
                              kLayoutState | kLayoutGeometry, first ? N * kShareSlots : 0,
@@ -1124,6 +1455,15 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   }
   const size_t inst_off = off;
   off += align256(sizeof(Inst) * batch);
+  const size_t zmap_off = off;  // the sub-batches' instance and group lists
+  size_t zints = 0, zpairs = 0;
+  for (const SubBatch &s : p->subs) {
+    zints += s.zmap_host.size() + s.members.size();
+    zpairs += s.groups_host.size() + s.gtab_host.size();
+  }
+  off += align256(zints * sizeof(int));
+  const size_t gtab_off = off;
+  off += align256(zpairs * sizeof(int2));
   p->bytes = off;
   if (hbm_budget_bytes && off > hbm_budget_bytes) {
     if (p->own_stream) cudaStreamDestroy(p->st);
@@ -1144,6 +1484,12 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   for (int i = 0; i < batch && e == cudaSuccess; i++) {
     Inst &I = p->h_inst[i];
     e = bind_instance(I, b + base[i], lay[i], geom[i], phi_vec_deg + phi_off[i], p->st);
+    if (p->mixed) {
+      const int g = group_first[i];
+      I.cor = (float *)(b + base[g] + lay[g].cor) + (p->slot[i] - p->slot[g]);
+      I.cor_stride = kShareSlots;
+      I.m_il = (float *)(b + base[g] + lay[g].m_il);
+    }
     if (p->shared) {
       const int g = i - i % kShareSlots;
       I.cor = (float *)(b + base[g] + lay[g].cor) + i % kShareSlots;
@@ -1157,13 +1503,47 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
     }
   }
   p->d_inst = (Inst *)(b + inst_off);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(p->d_inst, p->h_inst.data(),
-                                            sizeof(Inst) * batch,
-                                            cudaMemcpyHostToDevice, p->st);
+  if (e == cudaSuccess) e = plan_upload(p);
+  {
+    int *dz = (int *)(b + zmap_off);
+    for (SubBatch &s : p->subs) {
+      if (!s.members.empty()) {
+        s.zall = dz;
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(dz, s.members.data(), s.members.size() * sizeof(int),
+                              cudaMemcpyHostToDevice, p->st);
+        dz += s.members.size();
+      }
+      if (s.zmap_host.empty()) continue;
+      for (ViewSet &S : s.sets) S.zmap = dz + S.zoff;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dz, s.zmap_host.data(), s.zmap_host.size() * sizeof(int),
+                            cudaMemcpyHostToDevice, p->st);
+      dz += s.zmap_host.size();
+    }
+    int2 *dg = (int2 *)(b + gtab_off);
+    for (SubBatch &s : p->subs) {
+      if (!s.groups_host.empty()) {
+        s.gall = dg;
+        if (e == cudaSuccess)
+          e = cudaMemcpyAsync(dg, s.groups_host.data(), s.groups_host.size() * sizeof(int2),
+                              cudaMemcpyHostToDevice, p->st);
+        dg += s.groups_host.size();
+      }
+      if (s.gtab_host.empty()) continue;
+      for (ViewSet &S : s.sets) S.gtab = dg + S.zoff;
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dg, s.gtab_host.data(), s.gtab_host.size() * sizeof(int2),
+                            cudaMemcpyHostToDevice, p->st);
+      dg += s.gtab_host.size();
+    }
+  }
   if (e == cudaSuccess) e = launch_view_tables(p->d_inst, batch, p->d, p->nv, p->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(p->st);
   if (e == cudaSuccess && !getenv("ASDPOCS_NO_CHORD_TABLE"))
-    e = p->shared || batch == 1 ? plan_chord_tables(p) : plan_instance_chord_tables(p);
+    e = p->shared || batch == 1 ? plan_chord_tables(p)
+        : p->mixed              ? plan_group_chord_tables(p)
+                                : plan_instance_chord_tables(p);
   if (e != cudaSuccess) {
     asdpocs_plan_destroy(p);
     return cuda_status(e, "plan setup");
@@ -1395,12 +1775,29 @@ int asdpocs_plan_time_phase(asdpocs_plan p, int phase, int reps,
   // projector steps: views spread evenly over the scan (a view's cost
   // depends on its angle)
   auto view_of_rep = [&](int i) { return (int)(((long long)i * p->nv / reps) % p->nv); };
+  // mixed plans: each sub-batch's groups in turn
   auto ax = [&](int v) {
+    if (p->mixed) {
+      cudaError_t e = cudaSuccess;
+      for (const SubBatch &s : p->subs)
+        if (e == cudaSuccess)
+          e = launch_sart_ax_shared(p->d_inst, 0, s.d, v, p->st, sh.ax_u, sh.ax_q, s.gall,
+                                    (int)s.groups_host.size());
+      return e;
+    }
     return p->shared ? launch_sart_ax_shared(p->d_inst, p->batch, p->d, v, p->st, sh.ax_u,
                                              sh.ax_q)
                      : launch_sart_ax(p->d_inst, p->batch, p->d, v, p->st, sh.exact);
   };
   auto atx = [&](int v) {
+    if (p->mixed) {
+      cudaError_t e = cudaSuccess;
+      for (const SubBatch &s : p->subs)
+        if (e == cudaSuccess)
+          e = launch_sart_atx_shared(p->d_inst, 0, s.d, v, p->st, s.gall,
+                                     (int)s.groups_host.size());
+      return e;
+    }
     return p->shared ? launch_sart_atx_shared(p->d_inst, p->batch, p->d, v, p->st)
                      : launch_sart_atx(p->d_inst, p->batch, p->d, v, p->st, sh.zcol, sh.zseg);
   };

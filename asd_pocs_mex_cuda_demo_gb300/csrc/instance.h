@@ -1,6 +1,7 @@
 // Device state of one reconstruction instance (internal): shared by the
 // batched plans and the serving queue.
 #pragma once
+#include <vector>
 #include "kernels.h"
 
 namespace asd {
@@ -91,9 +92,31 @@ struct IterShape {
                             //   its stream)
   bool exact = false;       // forward steps: exact projection (launch_sart_ax)
 };
+// Instances of one launch with different view counts: for each run of
+// views [v0, v1), the instances that have those views (a device list of
+// `count` indices into the launch's instances) and their largest sizes, so
+// that the projector steps of those views cover only them.
+// Launches of the shared-geometry kernels with group tables list the
+// groups instead (gtab: `count` groups as (first instance, count)).
+struct ViewSet {
+  int v0 = 0, v1 = 0, count = 0;
+  Dims d{};
+  const int *zmap = nullptr;
+  const int2 *gtab = nullptr;
+  size_t zoff = 0;  // position of the list in its plan's index buffers
+};
+// `zall` (device, `batch` entries; null: 0 .. batch - 1): the instances of
+// d_inst the iteration runs.  `sets`: runs of views in order covering
+// [0, nv) (null or empty: every instance of zall in every view, at sizes d).
+// `gall` (shared only; device, `ngroups` entries; null: groups of
+// kShareSlots consecutive instances): the groups of instances sharing
+// geometry, as (first instance, count).
 cudaError_t enqueue_iteration(const Inst *d_inst, int batch, const Dims &d,
                               int nv, int ng, bool shared, cudaStream_t st,
-                              const IterShape &shape = IterShape(), bool finish = true);
+                              const IterShape &shape = IterShape(), bool finish = true,
+                              const std::vector<ViewSet> *sets = nullptr,
+                              const int *zall = nullptr, const int2 *gall = nullptr,
+                              int ngroups = 0);
 
 // Backward-step chord tables (Inst::chtab) of instances sharing 2-D geometry
 // and view angles, from d_inst[0], whose view tables are built: a counting

@@ -45,13 +45,18 @@ cudaError_t launch_store_sinogram(const float *src, void *dst, size_t n, int fmt
 // against P, dd2 accumulation, row normalisation -> cor.  sart_atx: Atx of
 // cor, column normalisation, update m += beta*bp/sumC, positivity.
 // `exact`: the forward step uses the exact projection (launch_ax_siddon).
+// `zmap` (device, `batch` entries; null: 0 .. batch - 1): the instances of
+// `insts` the launch covers, grid slice z running instance zmap[z]; `d` must
+// hold the largest sizes among them.
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
-                           int view, cudaStream_t st, bool exact = false);
+                           int view, cudaStream_t st, bool exact = false,
+                           const int *zmap = nullptr);
 // Cone beams (nz > 1) walk voxel columns (k_sart_atx_zcol) in segments of
 // `zseg` voxels (0: the default) unless `zcol` is false (the per-voxel form;
-// bit-identical).
+// bit-identical).  `zmap` as for launch_sart_ax.
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, cudaStream_t st, bool zcol = true, int zseg = 0);
+                            int view, cudaStream_t st, bool zcol = true, int zseg = 0,
+                            const int *zmap = nullptr);
 
 // ---- TV and scalars (kernels_tv.cu) ----
 // FP64 / FP32 TV minimisation on device buffers (reference semantics).
@@ -66,16 +71,19 @@ cudaError_t tv_minimize_f32(float *img, const float *img_old, float *work_a,
 
 // Per-iteration ASD-POCS steps for a batch (ASD_POCS_cuda.m:137-170).
 cudaError_t launch_iter_begin(const Inst *insts, int batch, cudaStream_t st);
+// `zmap` (device, `batch` entries; null: 0 .. batch - 1): the instances of
+// `insts` a launch covers, as for launch_sart_ax.
 cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
-                               cudaStream_t st);
+                               cudaStream_t st, const int *zmap = nullptr);
 // `walk`: bands (2-D) or slabs (3-D) per walk of the TV step; 0 picks it
 // from the batch size.  Results do not depend on it.
 cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
-                           int step, int ng, cudaStream_t st, int walk = 0);
+                           int step, int ng, cudaStream_t st, int walk = 0,
+                           const int *zmap = nullptr);
 // Largest useful `walk` for images of size d (the bands or slabs of one).
 int tv_walk_max(const Dims &d);
 cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
-                               int ng, cudaStream_t st);
+                               int ng, cudaStream_t st, const int *zmap = nullptr);
 
 int reduce_blocks_for(const Dims &d);
 // Strips x bands of the 2-D walks (the TV steps keep one partial for each,
@@ -89,8 +97,13 @@ cudaError_t launch_gather_done(const Inst *insts, int n, int *out,
 // Backward step for a batch whose instances share geometry and view angles:
 // chords computed once per voxel and applied to groups of instances (read
 // from the plan's chord tables, Inst::chtab, where it has them).
+// `gtab` (device, `ngroups` entries; null: groups of kShareSlots
+// consecutive instances): the launch's groups as (first instance, count),
+// each group's instances sharing geometry and view angles; groups of
+// different sizes may share a launch, `d` holding the largest sizes.
 cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
-                                   const Dims &d, int view, cudaStream_t st);
+                                   const Dims &d, int view, cudaStream_t st,
+                                   const int2 *gtab = nullptr, int ngroups = 0);
 
 // Forward step for a batch whose instances share geometry and view angles:
 // the column march evaluated once per ray for groups of instances whose
@@ -98,12 +111,16 @@ cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
 // `u` columns of loads per round and `q` quads of instances per block (1 or
 // 2 each; 0: the defaults, 2 x 1 for fan beams, 1 x 2 for cone beams) are
 // launch shapes that do not change results.
+// `gtab`, `ngroups` as for launch_sart_atx_shared.
 cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
-                                  int view, cudaStream_t st, int u = 0, int q = 0);
+                                  int view, cudaStream_t st, int u = 0, int q = 0,
+                                  const int2 *gtab = nullptr, int ngroups = 0);
 // Copies the running instances' images into (unpack = 0) or out of
-// (unpack = 1) their group's interleaved images.
+// (unpack = 1) their group's interleaved images (`gtab`, `ngroups` as for
+// launch_sart_atx_shared).
 cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,
-                              int unpack, cudaStream_t st);
+                              int unpack, cudaStream_t st, const int2 *gtab = nullptr,
+                              int ngroups = 0);
 
 // Backward-step chord tables (Inst::chtab) of the 2-D instance insts[0]
 // (and of the instances sharing its geometry), whose view tables must be

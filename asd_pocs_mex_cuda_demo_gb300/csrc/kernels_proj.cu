@@ -430,10 +430,10 @@ __global__ void __launch_bounds__(128)
 // so even after its own iterations have ended).
 template <bool k3D>
 __global__ void __launch_bounds__(kAxBlock)
-    k_sart_ax(const Inst *__restrict__ insts, int view) {
+    k_sart_ax(const Inst *__restrict__ insts, int view, const int *__restrict__ zmap) {
   __shared__ float sp[kAxCols][kAxWarps][2][32];
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (view >= I.nv) return;
   const bool done = ((volatile int *)&I.s->done)[0] != 0;
   const bool tabc = k3D && (I.tabc_mode == kTabcShared || (!done && I.tabc_mode == kTabcOwn));
@@ -481,9 +481,9 @@ __global__ void __launch_bounds__(kAxBlock)
 // lane j ray j's residual, normalisation and partial sums.
 template <bool k3D>
 __global__ void __launch_bounds__(kAxBlock)
-    k_sart_ax_exact(const Inst *__restrict__ insts, int view) {
+    k_sart_ax_exact(const Inst *__restrict__ insts, int view, const int *__restrict__ zmap) {
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (view >= I.nv) return;
   const bool done = ((volatile int *)&I.s->done)[0] != 0;
   const bool tabc = k3D && (I.tabc_mode == kTabcShared || (!done && I.tabc_mode == kTabcOwn));
@@ -727,9 +727,9 @@ __device__ __forceinline__ void sart_atx_tiles(const Inst &I, const ViewGeo &G,
 // axis-specialised chord.
 template <bool kPlanar>
 __global__ void __launch_bounds__(kAtxThreads, 4)
-    k_sart_atx(const Inst *__restrict__ insts, int view) {
+    k_sart_atx(const Inst *__restrict__ insts, int view, const int *__restrict__ zmap) {
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
   const Dims D = I.d;
   if (own_block(group_grid(D.nx, D.ny, D.nz, 1)).bid < 0) return;
@@ -893,10 +893,11 @@ __device__ __forceinline__ void atx_zcol_walk(const ViewGeo &G, const Dims &D,
 
 // SART backward step of cone-beam instances (see k_sart_atx) in z columns.
 __global__ void __launch_bounds__(kAtxThreads, 4)
-    k_sart_atx_zcol(const Inst *__restrict__ insts, int view, int seg) {
+    k_sart_atx_zcol(const Inst *__restrict__ insts, int view, int seg,
+                    const int *__restrict__ zmap) {
   __shared__ ZColShared sh;
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (view >= I.nv || ((volatile int *)&I.s->done)[0]) return;
   const Dims D = I.d;
   int ix, iy, z0, z1;
@@ -1299,13 +1300,14 @@ __device__ __forceinline__ void atx_shared_voxel_tab(
 // 128^3, 6 % slower for fan beams, whose extra spills cost more)
 template <bool kPlanar>
 __global__ void __launch_bounds__(kAtxThreads, kPlanar ? 4 : 5)
-    k_sart_atx_shared(const Inst *__restrict__ insts, int batch, int view) {
+    k_sart_atx_shared(const Inst *__restrict__ insts, int batch, int view,
+                      const int2 *__restrict__ gtab) {
   __shared__ float s_beta[kShareGroup];
   __shared__ unsigned s_active;
   __shared__ int s_finite;
   pdl_enter();
-  const int g0 = blockIdx.z * kShareGroup;
-  const int gn = min(kShareGroup, batch - g0);
+  const int g0 = gtab ? gtab[blockIdx.z].x : (int)blockIdx.z * kShareGroup;
+  const int gn = gtab ? gtab[blockIdx.z].y : min(kShareGroup, batch - g0);
   if (threadIdx.x == 0) {
     s_active = 0u;
     s_finite = 1;
@@ -1375,7 +1377,8 @@ constexpr int kAxShareQ = k3D ? kShareGroup / 4 : 1;
 // same bits.
 template <bool k3D, int kU, int kQ>
 __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
-    k_sart_ax_shared(const Inst *__restrict__ insts, int batch, int view) {
+    k_sart_ax_shared(const Inst *__restrict__ insts, int batch, int view,
+                     const int2 *__restrict__ gtab) {
   constexpr int kQuads = kShareGroup / 4;
   pdl_enter();
   // this block: kQ of the group's quads (4 instances each), from q0
@@ -1386,9 +1389,10 @@ __global__ void __launch_bounds__(kAxBlock, k3D ? 8 : 6)
   __shared__ int s_last[kS];
   __shared__ int s_nlast;
   const int q0 = (int)(blockIdx.z % (kQuads / kQ)) * kQ;
-  const int g0 = (int)(blockIdx.z / (kQuads / kQ)) * kShareGroup;  // the group
+  const int gz = (int)(blockIdx.z / (kQuads / kQ));                  // the group
+  const int g0 = gtab ? gtab[gz].x : gz * kShareGroup;
   const int gi = g0 + 4 * q0;                                        // first instance
-  const int gn = min(kS, batch - gi);
+  const int gn = min(kS, (gtab ? g0 + gtab[gz].y : batch) - gi);
   if (gn <= 0) return;
   const Inst &I0 = insts[g0];
   if (view >= I0.nv) return;
@@ -1548,12 +1552,13 @@ __global__ void __launch_bounds__(256)
 // own images (m) and the group's interleaved images (m_il): pack before the
 // SART sweep, unpack after it.  Grid (voxel blocks, 1, groups).
 __global__ void __launch_bounds__(256)
-    k_group_pack(const Inst *__restrict__ insts, int batch, int unpack) {
+    k_group_pack(const Inst *__restrict__ insts, int batch, int unpack,
+                 const int2 *__restrict__ gtab) {
   __shared__ float *s_m[kShareGroup];
   __shared__ unsigned s_active;
   pdl_enter();
-  const int g0 = blockIdx.z * kShareGroup;
-  const int gn = min(kShareGroup, batch - g0);
+  const int g0 = gtab ? gtab[blockIdx.z].x : (int)blockIdx.z * kShareGroup;
+  const int gn = gtab ? gtab[blockIdx.z].y : min(kShareGroup, batch - g0);
   if (threadIdx.x == 0) s_active = 0u;
   __syncthreads();
   if (threadIdx.x < gn) {
@@ -1640,7 +1645,7 @@ cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &
 }
 
 cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
-                           int view, cudaStream_t st, bool exact) {
+                           int view, cudaStream_t st, bool exact, const int *zmap) {
   cudaError_t e;
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
@@ -1649,14 +1654,14 @@ cudaError_t launch_sart_ax(const Inst *insts, int batch, const Dims &d,
   const bool p3 = d.nz > 1 || d.nb > 1;
   if (exact) {
     if (p3)
-      e = launch_iter(k_sart_ax_exact<true>, grid_ex, dim3(kAxBlock), st, insts, view);
+      e = launch_iter(k_sart_ax_exact<true>, grid_ex, dim3(kAxBlock), st, insts, view, zmap);
     else
-      e = launch_iter(k_sart_ax_exact<false>, grid_ex, dim3(kAxBlock), st, insts, view);
+      e = launch_iter(k_sart_ax_exact<false>, grid_ex, dim3(kAxBlock), st, insts, view, zmap);
   } else {
     if (p3)
-      e = launch_iter(k_sart_ax<true>, grid, dim3(kAxBlock), st, insts, view);
+      e = launch_iter(k_sart_ax<true>, grid, dim3(kAxBlock), st, insts, view, zmap);
     else
-      e = launch_iter(k_sart_ax<false>, grid, dim3(kAxBlock), st, insts, view);
+      e = launch_iter(k_sart_ax<false>, grid, dim3(kAxBlock), st, insts, view, zmap);
   }
   return e;
 }
@@ -1671,71 +1676,81 @@ cudaError_t launch_ax_siddon(const float *x, float *y, float *sr, const ViewGeo 
 }
 
 cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
-                            int view, cudaStream_t st, bool zcol, int zseg) {
+                            int view, cudaStream_t st, bool zcol, int zseg,
+                            const int *zmap) {
   cudaError_t e;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   zseg = zseg > 0 ? zseg : kZSeg;
   if (d.nz > 1 && zcol)
     e = launch_iter(k_sart_atx_zcol, zcol_grid(d.nx, d.ny, d.nz, batch, zseg),
-                    dim3(kAtxThreads), st, insts, view, zseg);
+                    dim3(kAtxThreads), st, insts, view, zseg, zmap);
   else if (d.nz > 1 || d.nb > 1)
-    e = launch_iter(k_sart_atx<false>, grid, dim3(kAtxThreads), st, insts, view);
+    e = launch_iter(k_sart_atx<false>, grid, dim3(kAtxThreads), st, insts, view, zmap);
   else
-    e = launch_iter(k_sart_atx<true>, grid, dim3(kAtxThreads), st, insts, view);
+    e = launch_iter(k_sart_atx<true>, grid, dim3(kAtxThreads), st, insts, view, zmap);
   return e;
 }
 
 cudaError_t launch_sart_atx_shared(const Inst *insts, int batch,
-                                   const Dims &d, int view, cudaStream_t st) {
+                                   const Dims &d, int view, cudaStream_t st,
+                                   const int2 *gtab, int ngroups) {
   cudaError_t e;
   dim3 grid = tile_grid(d.nx, d.ny, d.nz, 1);
-  grid.z = (batch + kShareGroup - 1) / kShareGroup;
+  grid.z = gtab ? ngroups : (batch + kShareGroup - 1) / kShareGroup;
   if (d.nz > 1 || d.nb > 1)
     e = launch_iter(k_sart_atx_shared<false>, grid, dim3(kAtxThreads), st, insts, batch,
-                    view);
+                    view, gtab);
   else
     e = launch_iter(k_sart_atx_shared<true>, grid, dim3(kAtxThreads), st, insts, batch,
-                    view);
+                    view, gtab);
   return e;
 }
 
 template <bool k3D, int kU, int kQ>
 static cudaError_t sart_ax_shared_as(const Inst *insts, int batch, unsigned blocks,
-                                     unsigned groups, int view, cudaStream_t st) {
+                                     unsigned groups, int view, cudaStream_t st,
+                                     const int2 *gtab) {
   return launch_iter(k_sart_ax_shared<k3D, kU, kQ>,
                      dim3(blocks, 1, groups * (kShareGroup / 4 / kQ)), dim3(kAxBlock), st,
-                     insts, batch, view);
+                     insts, batch, view, gtab);
 }
 
 template <bool k3D>
 static cudaError_t sart_ax_shared_shape(const Inst *insts, int batch, unsigned blocks,
                                         unsigned groups, int view, cudaStream_t st, int u,
-                                        int q) {
+                                        int q, const int2 *gtab) {
   u = u ? u : kAxShareU<k3D>;
   q = q ? q : kAxShareQ<k3D>;
-  if (u == 1 && q == 1) return sart_ax_shared_as<k3D, 1, 1>(insts, batch, blocks, groups, view, st);
-  if (u == 2 && q == 1) return sart_ax_shared_as<k3D, 2, 1>(insts, batch, blocks, groups, view, st);
-  if (u == 1 && q == 2) return sart_ax_shared_as<k3D, 1, 2>(insts, batch, blocks, groups, view, st);
-  if (u == 2 && q == 2) return sart_ax_shared_as<k3D, 2, 2>(insts, batch, blocks, groups, view, st);
+  if (u == 1 && q == 1)
+    return sart_ax_shared_as<k3D, 1, 1>(insts, batch, blocks, groups, view, st, gtab);
+  if (u == 2 && q == 1)
+    return sart_ax_shared_as<k3D, 2, 1>(insts, batch, blocks, groups, view, st, gtab);
+  if (u == 1 && q == 2)
+    return sart_ax_shared_as<k3D, 1, 2>(insts, batch, blocks, groups, view, st, gtab);
+  if (u == 2 && q == 2)
+    return sart_ax_shared_as<k3D, 2, 2>(insts, batch, blocks, groups, view, st, gtab);
   return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_sart_ax_shared(const Inst *insts, int batch, const Dims &d,
-                                  int view, cudaStream_t st, int u, int q) {
+                                  int view, cudaStream_t st, int u, int q,
+                                  const int2 *gtab, int ngroups) {
   const long long nr = (long long)d.na * d.nb;
   const unsigned blocks = (unsigned)((nr + kAxWarps - 1) / kAxWarps);
-  const unsigned groups = (unsigned)((batch + kShareGroup - 1) / kShareGroup);
+  const unsigned groups =
+      gtab ? (unsigned)ngroups : (unsigned)((batch + kShareGroup - 1) / kShareGroup);
   if (d.nz > 1 || d.nb > 1)
-    return sart_ax_shared_shape<true>(insts, batch, blocks, groups, view, st, u, q);
-  return sart_ax_shared_shape<false>(insts, batch, blocks, groups, view, st, u, q);
+    return sart_ax_shared_shape<true>(insts, batch, blocks, groups, view, st, u, q, gtab);
+  return sart_ax_shared_shape<false>(insts, batch, blocks, groups, view, st, u, q, gtab);
 }
 
 cudaError_t launch_group_pack(const Inst *insts, int batch, const Dims &d,
-                              int unpack, cudaStream_t st) {
+                              int unpack, cudaStream_t st, const int2 *gtab, int ngroups) {
   cudaError_t e;
   const long long n = (long long)d.nx * d.ny * d.nz;
-  const dim3 grid((unsigned)((n + 255) / 256), 1, (batch + kShareGroup - 1) / kShareGroup);
-  e = launch_iter(k_group_pack, grid, dim3(256), st, insts, batch, unpack);
+  const dim3 grid((unsigned)((n + 255) / 256), 1,
+                  gtab ? ngroups : (batch + kShareGroup - 1) / kShareGroup);
+  e = launch_iter(k_group_pack, grid, dim3(256), st, insts, batch, unpack, gtab);
   return e;
 }
 

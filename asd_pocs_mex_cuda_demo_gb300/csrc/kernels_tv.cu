@@ -383,10 +383,10 @@ __device__ __forceinline__ void sweep_scalars(const Inst &I, const double (&tot)
 // TV step, giving its step size alpha*d/||v||.
 template <bool k3D>
 __global__ void __launch_bounds__(kThreads)
-    k_after_sweep(const Inst *__restrict__ insts) {
+    k_after_sweep(const Inst *__restrict__ insts, const int *__restrict__ zmap) {
   __shared__ Tile<1, k3D> t;
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (inst_done(I)) return;
   const Dims D = I.d;
   const OwnBlock ob = own_block(group_grid(D.nx, D.ny, D.nz, 1));
@@ -656,10 +656,11 @@ __device__ __forceinline__ void tv_walk(const Inst &I, int step, int y0, int y1,
 }
 
 __global__ void __launch_bounds__(kWalkWarps * 32, 8)
-    k_tv_walk2d(const Inst *__restrict__ insts, int step, int bands) {
+    k_tv_walk2d(const Inst *__restrict__ insts, int step, int bands,
+                const int *__restrict__ zmap) {
   __shared__ float2 ring[kWalkWarps][kWalkRing * 32], ring0[kWalkWarps][kWalkRing * 32];
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
   if (step >= ng) return;
@@ -806,10 +807,11 @@ __device__ __forceinline__ void sweep_walk(const Inst &I, int y0, int y1, int xa
 }
 
 __global__ void __launch_bounds__(kWalkWarps * 32)
-    k_after_sweep_walk2d(const Inst *__restrict__ insts, int bands) {
+    k_after_sweep_walk2d(const Inst *__restrict__ insts, int bands,
+                         const int *__restrict__ zmap) {
   __shared__ float2 ring[kWalkWarps][4][kWalkRing * 32];
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (inst_done(I)) return;
   const Dims D = I.d;
   const int S = walk_strips(D.nx), NB = walk_bands(D.ny);
@@ -1153,11 +1155,12 @@ __device__ __forceinline__ void tv_zwalk_any(const Inst &I, int step, int x0, in
 }
 
 __global__ void __launch_bounds__(kZThreads, kZMinBlocks)
-    k_tv_walk3d(const Inst *__restrict__ insts, int step, int slabs) {
+    k_tv_walk3d(const Inst *__restrict__ insts, int step, int slabs,
+                const int *__restrict__ zmap) {
   __shared__ __align__(16) ZShared sh;
   __shared__ int s_last;
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
   if (step >= ng) return;
@@ -1204,9 +1207,9 @@ __global__ void __launch_bounds__(kZThreads, kZMinBlocks)
 // End of an iteration for instances whose last TV step did not finish it
 // (ng == 0 or ng == 1): positivity (after a TV step), dg, alpha/beta, k.
 __global__ void __launch_bounds__(kThreads)
-    k_finish_iter(const Inst *__restrict__ insts) {
+    k_finish_iter(const Inst *__restrict__ insts, const int *__restrict__ zmap) {
   pdl_enter();
-  const Inst &I = insts[blockIdx.z];
+  const Inst &I = insts[zmap ? zmap[blockIdx.z] : blockIdx.z];
   if (inst_done(I)) return;
   const int ng = I.s->ng;
   if (ng >= 2) return;  // finished by the last TV step
@@ -1270,10 +1273,10 @@ cudaError_t launch_iter_begin(const Inst *, int, cudaStream_t) {
 }
 
 cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
-                               cudaStream_t st) {
+                               cudaStream_t st, const int *zmap) {
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1) {
-    return launch_iter(k_after_sweep<true>, grid, dim3(kThreads), st, insts);
+    return launch_iter(k_after_sweep<true>, grid, dim3(kThreads), st, insts, zmap);
   } else {
     // one band per walk up to a wave of walks (24 resident warps per SM at
     // 80 registers), then longer walks
@@ -1284,7 +1287,7 @@ cudaError_t launch_after_sweep(const Inst *insts, int batch, const Dims &d,
     const long long walks = (long long)walk_strips(d.nx) * ((walk_bands(d.ny) + bands - 1) / bands);
     return launch_iter(k_after_sweep_walk2d,
                        dim3((unsigned)((walks + kWalkWarps - 1) / kWalkWarps), 1, batch),
-                       dim3(kWalkWarps * 32), st, insts, bands);
+                       dim3(kWalkWarps * 32), st, insts, bands, zmap);
   }
 }
 
@@ -1293,7 +1296,8 @@ int tv_walk_max(const Dims &d) {
 }
 
 cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
-                           int step, int ng, cudaStream_t st, int walk) {
+                           int step, int ng, cudaStream_t st, int walk,
+                           const int *zmap) {
   (void)ng;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
   if (d.nz > 1) {
@@ -1306,7 +1310,7 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
     const int slabs = (int)(per < 1 ? 1 : (per > zwalk_slabs(d.nz) ? zwalk_slabs(d.nz) : per));
     const long long walks = tiles * ((zwalk_slabs(d.nz) + slabs - 1) / slabs);
     return launch_iter(k_tv_walk3d, dim3((unsigned)walks, 1, batch), dim3(kZThreads), st,
-                       insts, step, slabs);
+                       insts, step, slabs, zmap);
   } else {
     // bands per walk: the batch's walks within about one wave of 32
     // resident warps per SM; one band (16 rows) per walk for small batches,
@@ -1317,7 +1321,7 @@ cudaError_t launch_tv_step(const Inst *insts, int batch, const Dims &d,
     const int bands = (int)(per < 1 ? 1 : (per > walk_bands(d.ny) ? walk_bands(d.ny) : per));
     const long long walks = (long long)walk_strips(d.nx) * ((walk_bands(d.ny) + bands - 1) / bands);
     const dim3 g2((unsigned)((walks + kWalkWarps - 1) / kWalkWarps), 1, batch);
-    return launch_iter(k_tv_walk2d, g2, dim3(kWalkWarps * 32), st, insts, step, bands);
+    return launch_iter(k_tv_walk2d, g2, dim3(kWalkWarps * 32), st, insts, step, bands, zmap);
   }
 }
 
@@ -1327,10 +1331,10 @@ int tv_partials_for(const Dims &d) {
 }
 
 cudaError_t launch_finish_iter(const Inst *insts, int batch, const Dims &d,
-                               int ng, cudaStream_t st) {
+                               int ng, cudaStream_t st, const int *zmap) {
   (void)ng;
   return launch_iter(k_finish_iter, tile_grid(d.nx, d.ny, d.nz, batch), dim3(kThreads), st,
-                     insts);
+                     insts, zmap);
 }
 
 #ifdef ASDPOCS_CHECKED

@@ -184,10 +184,13 @@ def test_shared_geometry_batch_equals_alone_bitwise(gpu, monkeypatch):
                 assert np.array_equal(pl.image(k), alone[k]), (force_per_instance, k)
 
 
-def _uneven(seed, n, na, nv, iters, ng, SO=541.0, OD=408.0, det=1.0):
+def _uneven(seed, n, na, nv, iters, ng, SO=541.0, OD=408.0, det=1.0, gseed=None):
+    """An instance: phantom and noise from `seed`, view angles offset by
+    `gseed` (default `seed`): instances of equal sizes and `gseed` share
+    their geometry."""
     vx = phantoms.fov_voxel_size(SO, OD, det, na, n)
     x = phantoms.random_ellipses(n, seed)
-    phi = phantoms.views(nv) + 0.5 * seed
+    phi = phantoms.views(nv) + 0.5 * (seed if gseed is None else gseed)
     para = dict(SO=SO, OD=OD, vxlsize=vx, nx=n, ny=n, nz=1, na=na, nb=1, detsize=det,
                 phi_vec=phi, maxnumIter=iters, numOfgradients=ng, alpha=0.002)
     P = np.stack([pkg.Ax_cone_gpu(x.astype(np.float32), dict(para, phi=-a / 180 * np.pi))[0]
@@ -229,6 +232,48 @@ def test_uneven_batch_equals_alone_bitwise(gpu, oracle_mod):
         _, P, para = insts[k]
         mo, _ = oracle_mod.asdpocs(P, para)
         assert rel_l2(alone[k][0], mo) < RECON_TOL, k
+
+
+@pytest.mark.parametrize("tables", [True, False], ids=["chord-tables", "direct"])
+def test_mixed_geometry_groups_equal_alone_bitwise(gpu, monkeypatch, tables):
+    """A 2-D plan whose instances fall into several geometries, some shared
+    by a few instances (one of them by nine: a full group of eight and one
+    more), listed out of order and with different iteration and TV-step
+    counts: the instances of a geometry run as groups through the
+    shared-geometry kernels, several geometries per launch, and each result
+    equals the instance's run alone bit for bit."""
+    if not tables:
+        monkeypatch.setenv("ASDPOCS_NO_CHORD_TABLE", "1")
+    A = dict(n=48, na=72, nv=12, gseed=1)
+    B = dict(n=64, na=96, nv=20, gseed=2)
+    C = dict(n=33, na=50, nv=7, gseed=3)
+    D = dict(n=80, na=120, nv=30, gseed=4)
+    spec = [(A, 3, 20), (B, 2, 5), (C, 4, 1), (B, 2, 5), (D, 2, 3), (A, 2, 20), (B, 3, 0),
+            (B, 2, 5), (C, 3, 2), (B, 2, 5), (B, 4, 5), (A, 4, 10), (B, 2, 5), (B, 2, 5),
+            (B, 3, 5)]
+    insts = [_uneven(40 + k, g["n"], g["na"], g["nv"], it, ng, gseed=g["gseed"])
+             for k, (g, it, ng) in enumerate(spec)]
+    alone = []
+    for x, P, para in insts:
+        with pkg.Plan(para, para["phi_vec"]) as pl:
+            pl.set_sinogram(0, P.ravel(order="F"))
+            pl.set_reference(0, x)
+            pl.reset()
+            pl.run()
+            alone.append((pl.image(0), pl.stats(0)))
+    paras = [i[2] for i in insts]
+    with pkg.Plan(paras, [p["phi_vec"] for p in paras]) as pl:
+        for k, (x, P, _) in enumerate(insts):
+            pl.set_sinogram(k, P.ravel(order="F"))
+            pl.set_reference(k, x)
+        for use_graph in (True, False):
+            pl.reset()
+            pl.run(use_graph=use_graph)
+            for k in range(len(insts)):
+                assert np.array_equal(pl.image(k), alone[k][0]), (use_graph, k)
+                s = pl.stats(k)
+                assert s["IterationNum"] == alone[k][1]["IterationNum"]
+                np.testing.assert_array_equal(s["RMSE"], alone[k][1]["RMSE"])
 
 
 def test_shared_geometry_cone_beam_instances_finishing_apart(gpu):
