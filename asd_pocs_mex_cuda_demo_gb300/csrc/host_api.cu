@@ -1999,7 +1999,7 @@ int asdpocs_plan_autotune_shapes(asdpocs_plan p, int reps, asdpocs_shapes *out) 
     p->ax_u = uq / 4;
     p->ax_q = uq % 4;
   } else if (p->d.nz > 1 && p->zcol) {
-    rc = pick(1, &p->zseg, {32, 8, 16, 64});  // the z-column segment length
+    rc = pick(1, &p->zseg, {0, 4, 8, 16, 32});  // the z-column segment length (0: by size)
   }
   double t_best = 0.0;
   // programmatic launches only where the plan runs on one stream (PdlScope)

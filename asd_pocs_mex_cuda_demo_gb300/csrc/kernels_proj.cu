@@ -766,7 +766,16 @@ __global__ void __launch_bounds__(kAtxThreads, 4)
 // evaluate their chords from the ray tables (chord3_bf).
 // Grid: (x tiles of 32, y tiles of 8 x segments, instances).
 // ---------------------------------------------------------------------------
-constexpr int kZSeg = 32;   // voxels of a column per thread
+constexpr int kZSeg = 32;   // longest default segment: voxels of a column per thread
+// Default segment for `voxels` voxels in a launch: the longest of 32, 16,
+// 8, 4 that still gives the launch 2^21 threads (a few per SM slot).
+// Measured on single volumes: 256^3 is fastest with 8 (0.566 ms against
+// 0.639 with 32), 64^3 - 128^3 with 4 (64^3: 0.026 ms against 0.107).
+__host__ __device__ inline int zcol_default_seg(long long voxels) {
+  int seg = kZSeg;
+  while (seg > 4 && voxels / seg < (1LL << 21)) seg /= 2;
+  return seg;
+}
 constexpr int kZColA = 6;   // detector columns of a shadow kept per thread
 
 struct ZColShared {
@@ -959,10 +968,10 @@ __global__ void __launch_bounds__(256)
 __global__ void __launch_bounds__(kAtxThreads, 4)
     k_atx_zcol(float *__restrict__ x, const float *__restrict__ yv, float *__restrict__ sc,
                const float4 *__restrict__ tabA, const float4 *__restrict__ tabC,
-               const int *__restrict__ flag, ViewGeo G, Dims D) {
+               const int *__restrict__ flag, ViewGeo G, Dims D, int seg) {
   __shared__ ZColShared sh;
   int ix, iy, z0, z1;
-  if (!zcol_thread(D, kZSeg, ix, iy, z0, z1)) return;
+  if (!zcol_thread(D, seg, ix, iy, z0, z1)) return;
   const bool narrow = flag[0] == 0;
   float acc = 0.f, accl = 0.f;
   atx_zcol_walk(
@@ -1639,8 +1648,10 @@ cudaError_t launch_atx_zcol(float *x, const float *y, float *sc, const ViewGeo &
   if (e != cudaSuccess) return e;
   const long long nr = (long long)d.na * d.nb;
   k_view_tab3<<<(unsigned)((nr + 255) / 256), 256, 0, st>>>(y, tabA, tabC, flag, g, d);
-  k_atx_zcol<<<zcol_grid(d.nx, d.ny, d.nz, 1), kAtxThreads, 0, st>>>(x, y, sc, tabA, tabC,
-                                                                     flag, g, d);
+  const int seg = zcol_default_seg((long long)d.nx * d.ny * d.nz);
+  k_atx_zcol<<<zcol_grid(d.nx, d.ny, d.nz, 1, seg), kAtxThreads, 0, st>>>(x, y, sc, tabA,
+                                                                          tabC, flag, g, d,
+                                                                          seg);
   return cudaGetLastError();
 }
 
@@ -1680,7 +1691,7 @@ cudaError_t launch_sart_atx(const Inst *insts, int batch, const Dims &d,
                             const int *zmap) {
   cudaError_t e;
   const dim3 grid = group_grid(d.nx, d.ny, d.nz, batch);
-  zseg = zseg > 0 ? zseg : kZSeg;
+  zseg = zseg > 0 ? zseg : zcol_default_seg((long long)d.nx * d.ny * d.nz * batch);
   if (d.nz > 1 && zcol)
     e = launch_iter(k_sart_atx_zcol, zcol_grid(d.nx, d.ny, d.nz, batch, zseg),
                     dim3(kAtxThreads), st, insts, view, zseg, zmap);
