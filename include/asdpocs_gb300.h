@@ -246,10 +246,12 @@ typedef struct asdpocs_plan_s *asdpocs_plan;
  * the instances are all 2-D (nz == nb == 1), all single-slice with nb > 1,
  * or all 3-D (nz > 1).  phi_vec_deg holds the instances' angle lists one
  * after the other (geom[0].nv values, then geom[1].nv, ...).  Each step of
- * the iteration is one launch for the whole batch; an instance gives the
- * same result, bit for bit, alone or in any batch.  All device memory is
- * allocated here; hbm_budget_bytes (0 = no limit) rejects plans that would
- * exceed it. */
+ * the iteration is one launch per sub-batch (up to eight, on their own
+ * streams); instances with equal sizes, geometry and angles run as groups
+ * that share the projector work, and a view's launches cover only the
+ * instances that have that view.  An instance gives the same result, bit
+ * for bit, alone or in any batch.  All device memory is allocated here;
+ * hbm_budget_bytes (0 = no limit) rejects plans that would exceed it. */
 int asdpocs_plan_create(asdpocs_plan *plan, int batch,
                         const asdpocs_geometry *geom,
                         const double *phi_vec_deg,
