@@ -276,6 +276,37 @@ def test_mixed_geometry_groups_equal_alone_bitwise(gpu, monkeypatch, tables):
                 np.testing.assert_array_equal(s["RMSE"], alone[k][1]["RMSE"])
 
 
+def test_mixed_geometry_many_classes_storage_and_autotune(gpu):
+    """More geometries than sub-batches (ten, most of them shared by two or
+    three instances), FP16 sinograms and a plan autotuned before it runs:
+    each result still equals its own one-instance FP16 plan bit for bit."""
+    spec = []
+    for c in range(10):
+        g = dict(n=24 + 4 * (c % 5), na=40 + 6 * (c % 4), nv=5 + 2 * c, gseed=100 + c)
+        spec += [(g, 2 + (c % 3), 5 * (c % 2))] * (1 + c % 3)
+    insts = [_uneven(200 + k, g["n"], g["na"], g["nv"], it, ng, gseed=g["gseed"])
+             for k, (g, it, ng) in enumerate(spec)]
+    paras = [dict(i[2], sino_storage="f16") for i in insts]
+    alone = []
+    for (x, P, _), para in zip(insts, paras):
+        with pkg.Plan(para, para["phi_vec"]) as pl:
+            pl.set_sinogram(0, P.ravel(order="F"))
+            pl.set_reference(0, x)
+            pl.reset()
+            pl.run()
+            alone.append(pl.image(0))
+    with pkg.Plan(paras, [p["phi_vec"] for p in paras]) as pl:
+        assert pl.streams > 1
+        for k, (x, P, _) in enumerate(insts):
+            pl.set_sinogram(k, P.ravel(order="F"))
+            pl.set_reference(k, x)
+        pl.autotune_shapes(reps=2)
+        pl.reset()
+        pl.run()
+        for k in range(len(insts)):
+            assert np.array_equal(pl.image(k), alone[k]), k
+
+
 def test_shared_geometry_cone_beam_instances_finishing_apart(gpu):
     """Cone-beam instances sharing geometry share one per-view ray-slope
     table; the instance that refreshes it keeps doing so after its own
