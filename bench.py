@@ -104,6 +104,9 @@ def parse():
                     help="device storage of the sinograms (default f32; uneven: f16)")
     ap.add_argument("--ax-mode", default="reference", choices=["reference", "exact"],
                     help="forward projection of the SART steps")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="uneven: wrap the timed steps in cudaProfilerStart/Stop (for "
+                         "ncu --profile-from-start off)")
     args = ap.parse_args()
     if args.workload == "serve":
         W = dict(SERVE, storage=args.storage or "f32", ax_mode="reference")
@@ -891,10 +894,14 @@ def uneven_main(args, W, rank, world, pg):
         plan.reset()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        if args.profile_range:
+            torch.cuda.profiler.start()
         e0.record(stream)
         plan.run(use_graph=True, sync=False)
         e1.record(stream)
         e1.synchronize()
+        if args.profile_range:
+            torch.cuda.profiler.stop()
         times.append(e0.elapsed_time(e1))
     clk = clocks.stop()
     ms = allmax(pg, statistics.mean(times))
