@@ -495,11 +495,18 @@ def main():
         pl.reset()
         kern = {
             "sart_ax": {"ms": t_ax, "per_iter_ms": t_ax * nv,
-                        "bytes": nb_inst * roofline.ax_bytes(nnz, M)},
+                        "bytes": nb_inst * roofline.ax_bytes(nnz, M),
+                        # rays projected and ray/voxel intersections per second
+                        "rays_per_s": nb_inst * M / (t_ax / 1e3),
+                        "pairs_per_s": nb_inst * nnz / (t_ax / 1e3)},
             "sart_atx": {"ms": t_atx, "per_iter_ms": t_atx * nv,
-                         "bytes": nb_inst * roofline.atx_bytes(nnz, N)},
+                         "bytes": nb_inst * roofline.atx_bytes(nnz, N),
+                         # voxels updated and voxel/ray pairs per second
+                         "voxel_updates_per_s": nb_inst * N / (t_atx / 1e3),
+                         "pairs_per_s": nb_inst * nnz / (t_atx / 1e3)},
             "tv_step": {"ms": t_tv, "per_iter_ms": t_tv * ng,
-                        "bytes": nb_inst * roofline.tv_step_bytes(N)},
+                        "bytes": nb_inst * roofline.tv_step_bytes(N),
+                        "voxel_updates_per_s": nb_inst * N / (t_tv / 1e3)},
         }
         for k in kern.values():
             k["GBps"] = k["bytes"] / (k["ms"] / 1e3) / 1e9
