@@ -123,6 +123,8 @@ SIGNATURES = [
                                       C.POINTER(Geometry), _D, C.POINTER(Options),
                                       C.c_ulonglong, C.c_void_p]),
     ("asdpocs_plan_destroy", C.c_int, [C.c_void_p]),
+    ("asdpocs_plan_layout", C.c_int, [C.c_int, C.POINTER(Geometry), _D, C.POINTER(Options),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("asdpocs_plan_bytes", C.c_ulonglong, [C.c_void_p]),
     ("asdpocs_plan_set_sinogram", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),
     ("asdpocs_plan_set_initial", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int]),

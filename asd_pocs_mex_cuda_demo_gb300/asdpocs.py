@@ -132,6 +132,36 @@ def SART_cuda_inline(P, para: dict):
     return m, out
 
 
+def _plan_args(paras, phi_vecs):
+    """The batch descriptor of asdpocs_plan_create: geometries, options and
+    the concatenated angle lists."""
+    if isinstance(paras, dict):
+        paras = [paras]
+    batch = len(paras)
+    phis = [np.asarray(p, np.float64).ravel() for p in
+            (phi_vecs if isinstance(phi_vecs, (list, tuple)) else [phi_vecs] * batch)]
+    if len(phis) != batch:
+        raise AsdpocsError(1, "one phi_vec per instance")
+    geoms = (Geometry * batch)(*[geometry_from_para(p, ph.size) for p, ph in zip(paras, phis)])
+    opts = (Options * batch)(*[options_from_para(p) for p in paras])
+    return geoms, opts, np.ascontiguousarray(np.concatenate(phis))
+
+
+def plan_layout(paras, phi_vecs):
+    """How a Plan of these instances would run, computed on the host without
+    a GPU (asdpocs_plan_layout): (group of each instance, -1 when it runs
+    through the per-instance kernels; sub-batch of each instance; number of
+    sub-batches)."""
+    geoms, opts, phi = _plan_args(paras, phi_vecs)
+    n = len(geoms)
+    group_of = (C.c_int * n)()
+    sub_of = (C.c_int * n)()
+    rc = load().asdpocs_plan_layout(n, geoms, phi.ctypes.data_as(_D), opts, group_of, sub_of)
+    if rc < 0:
+        check(-rc)
+    return list(group_of), list(sub_of), rc
+
+
 class Plan:
     """A batch of device-resident ASD-POCS reconstructions (per-instance
     sizes, geometry values, angles and options).  Instances of one plan are
@@ -144,17 +174,8 @@ class Plan:
     from a CUDA graph."""
 
     def __init__(self, paras, phi_vecs, hbm_budget_bytes: int = 0, stream: int = 0):
-        if isinstance(paras, dict):
-            paras = [paras]
-        self.batch = len(paras)
-        phis = [np.asarray(p, np.float64).ravel() for p in
-                (phi_vecs if isinstance(phi_vecs, (list, tuple)) else [phi_vecs] * self.batch)]
-        if len(phis) != self.batch:
-            raise AsdpocsError(1, "one phi_vec per instance")
-        geoms = (Geometry * self.batch)(*[geometry_from_para(p, ph.size)
-                                          for p, ph in zip(paras, phis)])
-        opts = (Options * self.batch)(*[options_from_para(p) for p in paras])
-        phi = np.ascontiguousarray(np.concatenate(phis))
+        geoms, opts, phi = _plan_args(paras, phi_vecs)
+        self.batch = len(geoms)
         self._geoms = geoms
         self._opts = opts
         h = C.c_void_p()

@@ -670,6 +670,7 @@ struct asdpocs_plan_s {
   std::vector<int> gclass;  // each group's geometry (groups of one geometry share it)
   std::vector<int> slot;
   std::vector<Inst> h_dev;  // mixed plans: the descriptors in d_inst order
+  std::vector<size_t> phi_off;  // each instance's first angle in phi_vec_deg
   bool zcol = true;     // cone beams: z-column backward step (else per voxel)
   bool exact = false;   // forward steps: exact Siddon projection (ax_mode)
   int tv_walk = 0;      // TV walk length (0: from the batch size)
@@ -1036,7 +1037,9 @@ static void sub_add(SubBatch &s, asdpocs_plan p, int i) {
   s.max_ng = std::max(s.max_ng, ng);
   s.min_ng = std::min(s.min_ng, ng);
 }
-static int plan_make_subs(asdpocs_plan p) {
+// The sub-batches' instances, sizes and counts (host only; plan_make_subs
+// adds their streams).
+static void plan_deal(asdpocs_plan p) {
   if (p->mixed || plan_uneven(p)) {
     // units: the groups (mixed plans) or the instances
     const int n = p->mixed ? (int)p->groups.size() : p->batch;
@@ -1072,15 +1075,8 @@ static int plan_make_subs(asdpocs_plan p) {
         }
       }
       std::sort(s.members.begin(), s.members.end());
-      if (total == 1) {
-        s.st = p->st;
-      } else {
-        ASD_CUDA(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
-        ASD_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
-      }
     }
-    if (total > 1) ASD_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
-    return 0;
+    return;
   }
   // whole groups per sub-batch, at least kSubGroups of them
   const int groups = (p->batch + kShareSlots - 1) / kShareSlots;
@@ -1105,14 +1101,21 @@ static int plan_make_subs(asdpocs_plan p) {
       s.max_ng = std::max(s.max_ng, ng);
       s.min_ng = i == s.first ? ng : std::min(s.min_ng, ng);
     }
-    if (nsub == 1) {
+  }
+}
+// Streams of the sub-batches: a single one runs on the plan's stream.
+static int plan_make_subs(asdpocs_plan p) {
+  plan_deal(p);
+  const bool multi = p->subs.size() > 1;
+  for (SubBatch &s : p->subs) {
+    if (!multi) {
       s.st = p->st;
     } else {
       ASD_CUDA(cudaStreamCreateWithFlags(&s.st, cudaStreamNonBlocking));
       ASD_CUDA(cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming));
     }
   }
-  if (nsub > 1) ASD_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
+  if (multi) ASD_CUDA(cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming));
   return 0;
 }
 
@@ -1172,6 +1175,134 @@ static int plan_sub_first(asdpocs_plan p, int i) {
   for (const SubBatch &s : p->subs)
     if (i >= s.first) f = s.first;
   return f;
+}
+
+}  // namespace asd
+
+namespace asd {
+// The host part of a plan: checks, per-instance options, and how the
+// instances run (shared geometry, groups of a mixed plan, exact mode).  No
+// GPU call; *out is a new plan, or null with the status set.
+static int plan_describe(asdpocs_plan *out, int batch, const asdpocs_geometry *geom,
+                         const double *phi_vec_deg, const asdpocs_options *opt) {
+  if (!out || !geom || !phi_vec_deg || batch <= 0)
+    return set_error(ASDPOCS_ERR_ARG, "bad plan arguments");
+  *out = nullptr;
+  const asdpocs_geometry &g0 = geom[0];
+  Dims dmax{0, 0, 0, 0, 0};
+  int nv_max = 0;
+  std::vector<size_t> phi_off(batch);
+  size_t phi_n = 0;
+  asdpocs_options dflt;
+  asdpocs_options_default(&dflt);
+  for (int i = 0; i < batch; i++) {
+    const asdpocs_geometry &gi = geom[i];
+    if (int e = check_instance(gi, opt ? opt[i] : dflt)) return e;
+    if (instance_kind(gi) != instance_kind(g0))
+      return set_error(ASDPOCS_ERR_ARG,
+                       "instances of one plan must be all 2-D (nz == nb == 1), "
+                       "all single-slice, or all 3-D");
+    dmax.nx = std::max(dmax.nx, gi.nx);
+    dmax.ny = std::max(dmax.ny, gi.ny);
+    dmax.nz = std::max(dmax.nz, gi.nz);
+    dmax.na = std::max(dmax.na, gi.na);
+    dmax.nb = std::max(dmax.nb, gi.nb);
+    nv_max = std::max(nv_max, gi.nv);
+    phi_off[i] = phi_n;
+    phi_n += (size_t)gi.nv;
+  }
+  asdpocs_plan p = new (std::nothrow) asdpocs_plan_s;
+  if (!p) return set_error(ASDPOCS_ERR_NOMEM, "host allocation");
+  p->batch = batch;
+  p->d = dmax;
+  p->nv = nv_max;
+  p->geom.assign(geom, geom + batch);
+  p->phi_off = phi_off;
+  p->opt.resize(batch);
+  for (int i = 0; i < batch; i++) {
+    p->opt[i] = opt ? opt[i] : dflt;
+    if (p->opt[i].maxnumIter > p->max_iter) p->max_iter = p->opt[i].maxnumIter;
+    if (p->opt[i].numOfgradients > p->max_ng)
+      p->max_ng = p->opt[i].numOfgradients;
+    if (i == 0 || p->opt[i].numOfgradients < p->min_ng)
+      p->min_ng = p->opt[i].numOfgradients;
+  }
+  p->has_ref.assign(batch, 0);
+  // instances with identical sizes, geometry and view angles share the
+  // projector coefficients of every view
+  auto same_geometry = [&](int i, int j) {
+    const asdpocs_geometry &gi = geom[i], &gj = geom[j];
+    return gi.nx == gj.nx && gi.ny == gj.ny && gi.nz == gj.nz && gi.na == gj.na &&
+           gi.nb == gj.nb && gi.nv == gj.nv && gi.SO == gj.SO && gi.OD == gj.OD &&
+           gi.vxlsize == gj.vxlsize && gi.detsize == gj.detsize &&
+           memcmp(phi_vec_deg + phi_off[j], phi_vec_deg + phi_off[i],
+                  sizeof(double) * (size_t)gj.nv) == 0;
+  };
+  p->shared = batch > 1;
+  for (int i = 1; i < batch && p->shared; i++) p->shared = same_geometry(i, 0);
+  // forward mode: one per plan; the shared-geometry forward step runs the
+  // reference's march only, so exact plans run every instance on its own
+  for (int i = 0; i < batch; i++)
+    if (p->opt[i].ax_mode != p->opt[0].ax_mode) {
+      delete p;
+      return set_error(ASDPOCS_ERR_ARG,
+                       "the instances of a plan must share one forward mode (ax_mode)");
+    }
+  p->exact = p->opt[0].ax_mode == ASDPOCS_AX_EXACT;
+  if (p->exact) p->shared = false;
+  if (getenv("ASDPOCS_NO_SHARED_GEOMETRY")) p->shared = false;
+  // 2-D instances of several geometries: groups of up to kShareSlots
+  // instances of one geometry (in instance order), laid out one after the
+  // other in d_inst, when some instances share their geometry
+  if (!p->shared && !p->exact && batch > 1 && !getenv("ASDPOCS_NO_SHARED_GEOMETRY")) {
+    bool planar = true;
+    for (int i = 0; i < batch; i++) planar = planar && geom[i].nz == 1 && geom[i].nb == 1;
+    if (planar) {
+      std::vector<int> cls(batch, -1), reps;
+      for (int i = 0; i < batch; i++) {
+        for (size_t c = 0; c < reps.size() && cls[i] < 0; c++)
+          if (same_geometry(i, reps[c])) cls[i] = (int)c;
+        if (cls[i] < 0) {
+          cls[i] = (int)reps.size();
+          reps.push_back(i);
+        }
+      }
+      for (size_t c = 0; c < reps.size(); c++) {
+        std::vector<int> cur;
+        for (int i = 0; i < batch; i++) {
+          if (cls[i] != (int)c) continue;
+          cur.push_back(i);
+          if ((int)cur.size() == kShareSlots) {
+            p->groups.push_back(cur);
+            p->gclass.push_back((int)c);
+            cur.clear();
+          }
+        }
+        if (!cur.empty()) {
+          p->groups.push_back(cur);
+          p->gclass.push_back((int)c);
+        }
+      }
+      p->mixed = p->groups.size() < (size_t)batch;  // else no instance shares
+      if (p->mixed) {
+        p->slot.assign(batch, 0);
+        int k = 0;
+        for (const auto &g : p->groups)
+          for (int i : g) p->slot[i] = k++;
+      } else {
+        p->groups.clear();
+        p->gclass.clear();
+      }
+    }
+  }
+  // ASDPOCS_CONE_ATX=voxel: the per-voxel form of the cone-beam backward step
+  // (same results; kept for comparison)
+  {
+    const char *f = getenv("ASDPOCS_CONE_ATX");
+    p->zcol = !(f && strcmp(f, "voxel") == 0);
+  }
+  *out = p;
+  return 0;
 }
 
 }  // namespace asd
@@ -1301,122 +1432,10 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
                         const double *phi_vec_deg, const asdpocs_options *opt,
                         unsigned long long hbm_budget_bytes, void *stream) {
   clear_error();
-  if (!out || !geom || !phi_vec_deg || batch <= 0)
-    return set_error(ASDPOCS_ERR_ARG, "bad plan arguments");
-  *out = nullptr;
-  const asdpocs_geometry &g0 = geom[0];
-  Dims dmax{0, 0, 0, 0, 0};
-  int nv_max = 0;
-  std::vector<size_t> phi_off(batch);
-  size_t phi_n = 0;
-  asdpocs_options dflt;
-  asdpocs_options_default(&dflt);
-  for (int i = 0; i < batch; i++) {
-    const asdpocs_geometry &gi = geom[i];
-    if (int e = check_instance(gi, opt ? opt[i] : dflt)) return e;
-    if (instance_kind(gi) != instance_kind(g0))
-      return set_error(ASDPOCS_ERR_ARG,
-                       "instances of one plan must be all 2-D (nz == nb == 1), "
-                       "all single-slice, or all 3-D");
-    dmax.nx = std::max(dmax.nx, gi.nx);
-    dmax.ny = std::max(dmax.ny, gi.ny);
-    dmax.nz = std::max(dmax.nz, gi.nz);
-    dmax.na = std::max(dmax.na, gi.na);
-    dmax.nb = std::max(dmax.nb, gi.nb);
-    nv_max = std::max(nv_max, gi.nv);
-    phi_off[i] = phi_n;
-    phi_n += (size_t)gi.nv;
-  }
-  asdpocs_plan p = new (std::nothrow) asdpocs_plan_s;
-  if (!p) return set_error(ASDPOCS_ERR_NOMEM, "host allocation");
-  p->batch = batch;
+  if (out) *out = nullptr;
+  asdpocs_plan p = nullptr;
+  if (int rc = plan_describe(&p, batch, geom, phi_vec_deg, opt)) return rc;
   p->budget = hbm_budget_bytes;
-  p->d = dmax;
-  p->nv = nv_max;
-  p->geom.assign(geom, geom + batch);
-  p->opt.resize(batch);
-  for (int i = 0; i < batch; i++) {
-    p->opt[i] = opt ? opt[i] : dflt;
-    if (p->opt[i].maxnumIter > p->max_iter) p->max_iter = p->opt[i].maxnumIter;
-    if (p->opt[i].numOfgradients > p->max_ng)
-      p->max_ng = p->opt[i].numOfgradients;
-    if (i == 0 || p->opt[i].numOfgradients < p->min_ng)
-      p->min_ng = p->opt[i].numOfgradients;
-  }
-  p->has_ref.assign(batch, 0);
-  // instances with identical sizes, geometry and view angles share the
-  // projector coefficients of every view
-  auto same_geometry = [&](int i, int j) {
-    const asdpocs_geometry &gi = geom[i], &gj = geom[j];
-    return gi.nx == gj.nx && gi.ny == gj.ny && gi.nz == gj.nz && gi.na == gj.na &&
-           gi.nb == gj.nb && gi.nv == gj.nv && gi.SO == gj.SO && gi.OD == gj.OD &&
-           gi.vxlsize == gj.vxlsize && gi.detsize == gj.detsize &&
-           memcmp(phi_vec_deg + phi_off[j], phi_vec_deg + phi_off[i],
-                  sizeof(double) * (size_t)gj.nv) == 0;
-  };
-  p->shared = batch > 1;
-  for (int i = 1; i < batch && p->shared; i++) p->shared = same_geometry(i, 0);
-  // forward mode: one per plan; the shared-geometry forward step runs the
-  // reference's march only, so exact plans run every instance on its own
-  for (int i = 0; i < batch; i++)
-    if (p->opt[i].ax_mode != p->opt[0].ax_mode) {
-      delete p;
-      return set_error(ASDPOCS_ERR_ARG,
-                       "the instances of a plan must share one forward mode (ax_mode)");
-    }
-  p->exact = p->opt[0].ax_mode == ASDPOCS_AX_EXACT;
-  if (p->exact) p->shared = false;
-  if (getenv("ASDPOCS_NO_SHARED_GEOMETRY")) p->shared = false;
-  // 2-D instances of several geometries: groups of up to kShareSlots
-  // instances of one geometry (in instance order), laid out one after the
-  // other in d_inst, when some instances share their geometry
-  if (!p->shared && !p->exact && batch > 1 && !getenv("ASDPOCS_NO_SHARED_GEOMETRY")) {
-    bool planar = true;
-    for (int i = 0; i < batch; i++) planar = planar && geom[i].nz == 1 && geom[i].nb == 1;
-    if (planar) {
-      std::vector<int> cls(batch, -1), reps;
-      for (int i = 0; i < batch; i++) {
-        for (size_t c = 0; c < reps.size() && cls[i] < 0; c++)
-          if (same_geometry(i, reps[c])) cls[i] = (int)c;
-        if (cls[i] < 0) {
-          cls[i] = (int)reps.size();
-          reps.push_back(i);
-        }
-      }
-      for (size_t c = 0; c < reps.size(); c++) {
-        std::vector<int> cur;
-        for (int i = 0; i < batch; i++) {
-          if (cls[i] != (int)c) continue;
-          cur.push_back(i);
-          if ((int)cur.size() == kShareSlots) {
-            p->groups.push_back(cur);
-            p->gclass.push_back((int)c);
-            cur.clear();
-          }
-        }
-        if (!cur.empty()) {
-          p->groups.push_back(cur);
-          p->gclass.push_back((int)c);
-        }
-      }
-      p->mixed = p->groups.size() < (size_t)batch;  // else no instance shares
-      if (p->mixed) {
-        p->slot.assign(batch, 0);
-        int k = 0;
-        for (const auto &g : p->groups)
-          for (int i : g) p->slot[i] = k++;
-      } else {
-        p->groups.clear();
-        p->gclass.clear();
-      }
-    }
-  }
-  // ASDPOCS_CONE_ATX=voxel: the per-voxel form of the cone-beam backward step
-  // (same results; kept for comparison)
-  {
-    const char *f = getenv("ASDPOCS_CONE_ATX");
-    p->zcol = !(f && strcmp(f, "voxel") == 0);
-  }
   cudaGetDevice(&p->device);
   if (stream) {
     p->st = (cudaStream_t)stream;
@@ -1483,7 +1502,7 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   p->h_inst.resize(batch);
   for (int i = 0; i < batch && e == cudaSuccess; i++) {
     Inst &I = p->h_inst[i];
-    e = bind_instance(I, b + base[i], lay[i], geom[i], phi_vec_deg + phi_off[i], p->st);
+    e = bind_instance(I, b + base[i], lay[i], geom[i], phi_vec_deg + p->phi_off[i], p->st);
     if (p->mixed) {
       const int g = group_first[i];
       I.cor = (float *)(b + base[g] + lay[g].cor) + (p->slot[i] - p->slot[g]);
@@ -1550,6 +1569,37 @@ int asdpocs_plan_create(asdpocs_plan *out, int batch,
   }
   *out = p;
   return asdpocs_plan_reset(p);
+}
+
+int asdpocs_plan_layout(int batch, const asdpocs_geometry *geom, const double *phi_vec_deg,
+                        const asdpocs_options *opt, int *group_of, int *sub_of) {
+  clear_error();
+  asdpocs_plan p = nullptr;
+  if (int rc = plan_describe(&p, batch, geom, phi_vec_deg, opt)) return -rc;
+  plan_deal(p);
+  std::vector<int> user(batch);  // instance at each position of d_inst
+  for (int i = 0; i < batch; i++) user[p->mixed ? p->slot[i] : i] = i;
+  for (int i = 0; i < batch; i++) {
+    if (group_of) group_of[i] = -1;
+    if (sub_of) sub_of[i] = -1;
+  }
+  if (group_of) {
+    if (p->shared)
+      for (int i = 0; i < batch; i++) group_of[i] = i / kShareSlots;
+    for (size_t k = 0; k < p->groups.size(); k++)
+      for (int i : p->groups[k]) group_of[i] = (int)k;
+  }
+  if (sub_of)
+    for (size_t k = 0; k < p->subs.size(); k++) {
+      const SubBatch &s = p->subs[k];
+      if (!s.members.empty())
+        for (int pos : s.members) sub_of[user[pos]] = (int)k;
+      else
+        for (int i = s.first; i < s.first + s.count; i++) sub_of[i] = (int)k;
+    }
+  const int n = (int)p->subs.size();
+  delete p;
+  return n;
 }
 
 int asdpocs_plan_destroy(asdpocs_plan p) {

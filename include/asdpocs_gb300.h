@@ -258,6 +258,17 @@ int asdpocs_plan_create(asdpocs_plan *plan, int batch,
                         const asdpocs_options *opt,
                         unsigned long long hbm_budget_bytes, void *stream);
 int asdpocs_plan_destroy(asdpocs_plan plan);
+/* How asdpocs_plan_create would run these instances, computed on the host
+ * without a GPU (same arguments, checks and messages): group_of[i] is the
+ * group of instances sharing geometry that instance i runs in (-1: it runs
+ * through the per-instance kernels), sub_of[i] its sub-batch (one stream
+ * each); either pointer may be NULL.  Returns the number of sub-batches, or
+ * minus the status (ASDPOCS_ERR_*) of the error asdpocs_plan_create would
+ * report.  Replaces nothing in the reference, which runs one
+ * reconstruction at a time (ASD_POCS_cuda.m:103-171). */
+int asdpocs_plan_layout(int batch, const asdpocs_geometry *geom,
+                        const double *phi_vec_deg, const asdpocs_options *opt,
+                        int *group_of, int *sub_of);
 /* Device bytes held by the plan. */
 unsigned long long asdpocs_plan_bytes(asdpocs_plan plan);
 
