@@ -307,6 +307,40 @@ def test_mixed_geometry_many_classes_storage_and_autotune(gpu):
             assert np.array_equal(pl.image(k), alone[k]), k
 
 
+def test_uneven_cone_beam_batch_equals_alone_bitwise(gpu):
+    """Cone-beam instances of different volume and detector sizes and view
+    counts in one plan (per-instance kernels, sub-batches by size, each
+    view's launches over the instances that have it): each result equals the
+    instance's run alone bit for bit."""
+    spec = [(24, 24, 16, 40, 30, 9, 2, 3), (32, 28, 20, 48, 40, 12, 3, 2),
+            (24, 24, 16, 40, 30, 9, 2, 3), (20, 20, 24, 36, 36, 7, 2, 0),
+            (32, 28, 20, 48, 40, 5, 1, 4)]
+    insts = []
+    for k, (nx, ny, nz, na, nb, nv, it, ng) in enumerate(spec):
+        phi = phantoms.views(nv) + 3.0 * k
+        para = dict(SO=1000.0, OD=500.0, vxlsize=1.0, nx=nx, ny=ny, nz=nz, na=na, nb=nb,
+                    detsize=1.6, phi_vec=phi, maxnumIter=it, numOfgradients=ng, alpha=0.05)
+        P = np.random.default_rng(300 + k).random(na * nb * nv).astype(np.float32)
+        insts.append((para, P))
+    alone = []
+    for para, P in insts:
+        with pkg.Plan(para, para["phi_vec"]) as pl:
+            pl.set_sinogram(0, P)
+            pl.reset()
+            pl.run()
+            alone.append(pl.image(0))
+    paras = [i[0] for i in insts]
+    with pkg.Plan(paras, [p["phi_vec"] for p in paras]) as pl:
+        assert pl.streams > 1
+        for k, (_, P) in enumerate(insts):
+            pl.set_sinogram(k, P)
+        pl.reset()
+        pl.run()
+        for k in range(len(insts)):
+            assert np.array_equal(pl.image(k), alone[k]), k
+            assert np.isfinite(alone[k]).all()
+
+
 def test_shared_geometry_cone_beam_instances_finishing_apart(gpu):
     """Cone-beam instances sharing geometry share one per-view ray-slope
     table; the instance that refreshes it keeps doing so after its own
@@ -427,9 +461,10 @@ def test_tv_walks_batch_equals_alone(gpu, nx, ny, batch, check):
 
 
 def test_tv_zwalks_batch_equals_alone(gpu):
-    """The cone-beam TV step walks 32 x 16 tiles down z in slabs of 16
-    slices, two slabs per walk in this batch (18 tiles x 3 slabs x 20) and
-    one alone; each instance's result is the same bits either way."""
+    """The cone-beam TV step walks 28 x 30 tiles down z in slabs of 16
+    slices (16 tiles x 3 slabs for each of the 20 instances here, walks of
+    several slabs in the batch and of one alone); each instance's result is
+    the same bits either way."""
     nx, ny, nz, na, nb, nv, batch = 96, 96, 40, 48, 48, 6, 20
     SO, OD, det = 1000.0, 500.0, 1.6
     phi = phantoms.views(nv)
