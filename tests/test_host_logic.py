@@ -105,9 +105,7 @@ def _fan(n, nv, gseed, na=None):
 
 
 def _layout(insts):
-    from asd_pocs_mex_cuda_demo_gb300.asdpocs import plan_layout
-
-    return plan_layout([p for p, _ in insts], [ph for _, ph in insts])
+    return pkg.plan_layout([p for p, _ in insts], [ph for _, ph in insts])
 
 
 def _check_layout(insts, group_of, sub_of, nsub):
